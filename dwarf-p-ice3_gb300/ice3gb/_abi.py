@@ -1,0 +1,116 @@
+"""ctypes binding of the C ABI declared in include/ice3gb.h.
+
+The shared library ``libice3gb.so`` is built in-tree by
+``dwarf-p-ice3_gb300/build.py`` (nvcc, sm_103a).  Loading fails loudly when it
+is missing: there is no CPU fallback for the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+from .constants import CONSTANT_NAMES, Ice3gbConstants, Ice3gbLuts  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.normpath(os.path.join(_HERE, ".."))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libice3gb.so")
+
+P = ctypes.c_void_p
+
+ICE3GB_OK = 0
+ERRORS = {
+    -1: "ICE3GB_ERR_NULL", -2: "ICE3GB_ERR_SHAPE", -3: "ICE3GB_ERR_ALIGN", -4: "ICE3GB_ERR_CUDA",
+    -5: "ICE3GB_ERR_UNSUPPORTED", -6: "ICE3GB_ERR_DEVICE", -7: "ICE3GB_ERR_HANDLE", -8: "ICE3GB_ERR_RANGE",
+}
+DEV_PASS_CAP = 1
+
+
+class IceAdjustFields(ctypes.Structure):
+    _fields_ = [(n, P) for n in (
+        "sigqsat", "pabs", "sigs", "th", "exn", "exn_ref", "rho_dry_ref",
+        "rv", "rc", "ri", "rr", "rs", "rg", "cf_mf", "rc_mf", "ri_mf",
+        "rvs", "rcs", "ris", "ths",
+        "t", "rv_out", "rc_out", "ri_out", "cldfr",
+        "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls")] + [("sigqsat_3d", ctypes.c_int64)]
+
+
+class SedimentationFields(ctypes.Structure):
+    _fields_ = [(n, P) for n in (
+        "rhodref", "dzz", "pabs", "tht", "sea", "town",
+        "rcs", "rrs", "ris", "rss", "rgs",
+        "inprc", "inprr", "inpri", "inprs", "inprg",
+        "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")] + [("fortran_semantics", ctypes.c_int64)]
+
+
+class RainIceFields(ctypes.Structure):
+    _fields_ = [(n, P) for n in (
+        "exn", "dzz", "rhodref", "exnref", "pabs", "cldfr", "sigs",
+        "tht", "rvt", "rct", "rrt", "rit", "rst", "rgt", "sea", "town",
+        "cit", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf",
+        "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs",
+        "evap3d", "rainfr", "inprc", "inprr", "inpri", "inprs", "inprg", "indep",
+        "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")]
+
+
+class RainIceOptions(ctypes.Structure):
+    _fields_ = [("lsedim_after", ctypes.c_int32), ("ldeposc", ctypes.c_int32),
+                ("lfeedbackt", ctypes.c_int32), ("max_passes", ctypes.c_int32),
+                ("sed_jax", ctypes.c_int32)]
+
+
+EXPORTED = (
+    "ice3gb_version", "ice3gb_constant_count", "ice3gb_constant_name", "ice3gb_create",
+    "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status", "ice3gb_ice_adjust",
+    "ice3gb_sedimentation", "ice3gb_rain_ice", "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host",
+)
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libice3gb.so (built by build.py) and declare the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} not found: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()' at the repository root)")
+    lib = ctypes.CDLL(path)
+    lib.ice3gb_version.restype = ctypes.c_int
+    lib.ice3gb_constant_count.restype = ctypes.c_int
+    lib.ice3gb_constant_name.restype = ctypes.c_char_p
+    lib.ice3gb_constant_name.argtypes = [ctypes.c_int]
+    lib.ice3gb_create.argtypes = [ctypes.POINTER(Ice3gbConstants), ctypes.POINTER(Ice3gbLuts),
+                                  ctypes.POINTER(ctypes.c_void_p)]
+    lib.ice3gb_destroy.argtypes = [P]
+    lib.ice3gb_last_error.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+    lib.ice3gb_status.argtypes = [P, P, ctypes.POINTER(ctypes.c_uint32)]
+    lib.ice3gb_ice_adjust.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.POINTER(IceAdjustFields), P]
+    lib.ice3gb_ice_adjust_host.argtypes = lib.ice3gb_ice_adjust.argtypes
+    lib.ice3gb_sedimentation.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.POINTER(SedimentationFields), P]
+    lib.ice3gb_rain_ice.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    ctypes.POINTER(RainIceOptions), ctypes.POINTER(RainIceFields), P]
+    lib.ice3gb_rain_ice_host.argtypes = lib.ice3gb_rain_ice.argtypes
+    for name in ("ice3gb_create", "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status",
+                 "ice3gb_ice_adjust", "ice3gb_sedimentation", "ice3gb_rain_ice",
+                 "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host"):
+        getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+class Ice3gbError(RuntimeError):
+    pass
+
+
+def check(rc: int, handle=None, what: str = "") -> None:
+    if rc == ICE3GB_OK:
+        return
+    lib = load()
+    buf = ctypes.create_string_buffer(512)
+    lib.ice3gb_last_error(handle, buf, len(buf))
+    raise Ice3gbError(f"{what}: {ERRORS.get(rc, rc)}: {buf.value.decode(errors='replace')}")

@@ -1,0 +1,181 @@
+"""Constants table: the reference's ``Phyex(program).to_externals()`` dict
+packed into the ``Ice3gbConstants`` / ``Ice3gbLuts`` structs of the C ABI.
+
+The table comes either from a live reference ``Phyex`` object or dict (so a
+caller of ``IceAdjustJAX(phyex)`` can pass the same object), or from the
+JSON snapshot of ``Phyex("AROME").to_externals()`` shipped in ``data/``.
+
+Two flavours exist because the reference's Python tables diverge from the
+PHYEX Fortran it was translated from:
+
+``table="jax"``   the Python values unchanged (parity with the reference JAX);
+``table="phyex"`` Fortran values for the three known divergences:
+  * TMINMIX/TMAXMIX swapped back (src/ice3/phyex_common/nebn.py:244-245 vs
+    PHYEX-IAL_CY50T1/micro/modd_nebn.F90:178-179);
+  * GAMINC_RIM1/2/4 with bound = BOUND_MIN * ZRATE**(j-1) and RIM4 built on
+    BG (rain_ice_parameters.py:1105-1156 vs mode_ini_rain_ice.F90:786-790).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import re
+from dataclasses import dataclass
+from typing import Any, Dict, List, Mapping, Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_HEADER = os.path.normpath(os.path.join(_HERE, "..", "..", "include", "ice3gb.h"))
+
+NGAMINC, NACCLBDAS, NACCLBDAR, NDRYLBDAG, NDRYLBDAS, NDRYLBDAR = 80, 40, 40, 40, 80, 40
+
+
+def constant_names(header: str = _HEADER) -> List[str]:
+    """Field order of ``Ice3gbConstants``, read from the X-macro list of the
+    public header (the library exports the same list through
+    ``ice3gb_constant_name``; a test checks both agree)."""
+    with open(header) as fh:
+        text = fh.read()
+    m = re.search(r"#define ICE3GB_CONSTANTS\(X\)(.*?)\n\s*\n", text, re.S)
+    if not m:
+        raise RuntimeError(f"ICE3GB_CONSTANTS list not found in {header}")
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    return re.findall(r"X\((\w+)\)", body)
+
+
+CONSTANT_NAMES: List[str] = constant_names()
+
+
+class Ice3gbConstants(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in CONSTANT_NAMES]
+
+
+class Ice3gbLuts(ctypes.Structure):
+    _fields_ = [
+        ("gaminc_rim1", ctypes.c_double * NGAMINC),
+        ("gaminc_rim2", ctypes.c_double * NGAMINC),
+        ("gaminc_rim4", ctypes.c_double * NGAMINC),
+        ("ker_raccss", ctypes.c_double * (NACCLBDAS * NACCLBDAR)),
+        ("ker_raccs", ctypes.c_double * (NACCLBDAS * NACCLBDAR)),
+        ("ker_saccrg", ctypes.c_double * (NACCLBDAR * NACCLBDAS)),
+        ("ker_rdryg", ctypes.c_double * (NDRYLBDAG * NDRYLBDAR)),
+        ("ker_sdryg", ctypes.c_double * (NDRYLBDAG * NDRYLBDAS)),
+    ]
+
+
+def load_snapshot(program: str = "AROME") -> Dict[str, Any]:
+    """Externals dict from the shipped JSON snapshot (arrays as numpy)."""
+    path = os.path.join(_HERE, "data", f"phyex_{program.lower()}.json")
+    with open(path) as fh:
+        raw = json.load(fh)["externals"]
+    out: Dict[str, Any] = {}
+    for k, v in raw.items():
+        if isinstance(v, dict) and "shape" in v:
+            out[k] = np.asarray(v["data"], dtype=np.float64).reshape(v["shape"])
+        else:
+            out[k] = v
+    return out
+
+
+def externals_from(phyex: Any = None, program: str = "AROME") -> Dict[str, Any]:
+    """Accept a reference ``Phyex`` object, an externals mapping, or None."""
+    if phyex is None:
+        return load_snapshot(program)
+    if hasattr(phyex, "to_externals"):
+        return dict(phyex.to_externals())
+    if isinstance(phyex, Mapping):
+        return dict(phyex)
+    raise TypeError("phyex must be a Phyex object, an externals mapping or None")
+
+
+def _gaminc_fortran(ext: Mapping[str, Any]):
+    """GAMINC_RIM tables as INI_RAIN_ICE builds them (mode_ini_rain_ice.F90:770-790):
+    P(a, bound_j) with bound_j = BOUND_MIN * ZRATE**(j-1), the regularised
+    lower incomplete gamma function."""
+    from scipy.special import gammainc
+
+    bmin, bmax, n = float(ext["GAMINC_BOUND_MIN"]), float(ext["GAMINC_BOUND_MAX"]), int(ext["NGAMINC"])
+    zrate = np.exp(np.log(bmax / bmin) / (n - 1))
+    bounds = bmin * zrate ** np.arange(n)
+    nus, ds, bs, bg, alphas = (float(ext[k]) for k in ("NUS", "DS", "BS", "BG", "ALPHAS"))
+    return (gammainc(nus + (2.0 + ds) / alphas, bounds),
+            gammainc(nus + bs / alphas, bounds),
+            gammainc(nus + bg / alphas, bounds))
+
+
+@dataclass
+class ConstantsTable:
+    """Packed constants for one (program, table flavour)."""
+
+    consts: Ice3gbConstants
+    luts: Ice3gbLuts
+    values: Dict[str, float]
+    table: str
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.values[n] for n in CONSTANT_NAMES], dtype=np.float64)
+
+
+_DEFAULTS = {"OCND2": 0.0}
+
+
+def build_table(phyex: Any = None, table: str = "jax", program: str = "AROME",
+                overrides: Optional[Mapping[str, float]] = None) -> ConstantsTable:
+    if table not in ("jax", "phyex"):
+        raise ValueError("table must be 'jax' or 'phyex'")
+    ext = externals_from(phyex, program)
+    values: Dict[str, float] = {}
+    for name in CONSTANT_NAMES:
+        if name in ext:
+            values[name] = float(ext[name])
+        elif name in _DEFAULTS:
+            values[name] = _DEFAULTS[name]
+        else:
+            raise KeyError(f"constant {name} missing from the externals table")
+    rim1 = np.asarray(ext["GAMINC_RIM1"], dtype=np.float64)
+    rim2 = np.asarray(ext["GAMINC_RIM2"], dtype=np.float64)
+    rim4 = np.asarray(ext["GAMINC_RIM4"], dtype=np.float64)
+    if table == "phyex":
+        values["TMINMIX"], values["TMAXMIX"] = 253.16, 273.16
+        rim1, rim2, rim4 = _gaminc_fortran(ext)
+    if overrides:
+        for k, v in overrides.items():
+            if k not in values:
+                raise KeyError(k)
+            values[k] = float(v)
+    consts = Ice3gbConstants(*[values[n] for n in CONSTANT_NAMES])
+    luts = Ice3gbLuts()
+
+    def fill(dst, arr, shape):
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64)[: shape[0], : shape[1]]
+                                 if len(shape) == 2 else np.asarray(arr, dtype=np.float64)[: shape[0]])
+        if a.shape != tuple(shape):
+            raise ValueError(f"lookup table has shape {a.shape}, expected {shape}")
+        ctypes.memmove(dst, a.ctypes.data, a.nbytes)
+
+    fill(luts.gaminc_rim1, rim1, (NGAMINC,))
+    fill(luts.gaminc_rim2, rim2, (NGAMINC,))
+    fill(luts.gaminc_rim4, rim4, (NGAMINC,))
+    fill(luts.ker_raccss, ext["ker_raccss"], (NACCLBDAS, NACCLBDAR))
+    fill(luts.ker_raccs, ext["ker_raccs"], (NACCLBDAS, NACCLBDAR))
+    fill(luts.ker_saccrg, ext["ker_saccrg"], (NACCLBDAR, NACCLBDAS))
+    fill(luts.ker_rdryg, ext["ker_rdryg"], (NDRYLBDAG, NDRYLBDAR))
+    fill(luts.ker_sdryg, ext["ker_sdryg"], (NDRYLBDAG, NDRYLBDAS))
+    return ConstantsTable(consts=consts, luts=luts, values=values, table=table)
+
+
+def luts_arrays(t: ConstantsTable) -> Dict[str, np.ndarray]:
+    """Numpy views of the lookup tables (for tests)."""
+    L = t.luts
+    return {
+        "gaminc_rim1": np.ctypeslib.as_array(L.gaminc_rim1).copy(),
+        "gaminc_rim2": np.ctypeslib.as_array(L.gaminc_rim2).copy(),
+        "gaminc_rim4": np.ctypeslib.as_array(L.gaminc_rim4).copy(),
+        "ker_raccss": np.ctypeslib.as_array(L.ker_raccss).reshape(NACCLBDAS, NACCLBDAR).copy(),
+        "ker_raccs": np.ctypeslib.as_array(L.ker_raccs).reshape(NACCLBDAS, NACCLBDAR).copy(),
+        "ker_saccrg": np.ctypeslib.as_array(L.ker_saccrg).reshape(NACCLBDAR, NACCLBDAS).copy(),
+        "ker_rdryg": np.ctypeslib.as_array(L.ker_rdryg).reshape(NDRYLBDAG, NDRYLBDAR).copy(),
+        "ker_sdryg": np.ctypeslib.as_array(L.ker_sdryg).reshape(NDRYLBDAG, NDRYLBDAS).copy(),
+    }

@@ -1,0 +1,231 @@
+/*
+ * ice3gb.h — C ABI of the GB300-native ICE3 one-moment microphysics hot path
+ * (saturation adjustment `ice_adjust`, the ICE4 `rain_ice` step and the
+ * statistical sedimentation sweep), FP64, one GPU.
+ *
+ * Reference interfaces this ABI replaces (maurinl26/dwarf-p-ice3):
+ *   - Fortran/C bridge `c_ice_adjust`    PHYEX-IAL_CY50T1/bridge/phyex_bridge.F90:27
+ *   - Fortran/C bridge `c_ini_rain_ice`  PHYEX-IAL_CY50T1/bridge/phyex_bridge.F90:215
+ *   - Fortran/C bridge `c_rain_ice`      PHYEX-IAL_CY50T1/bridge/phyex_bridge.F90:242
+ *   - Python components `IceAdjustJAX.__call__` src/ice3/jax/ice_adjust.py:139
+ *     and `RainIceJAX.__call__` src/ice3/jax/rain_ice.py:181
+ *   - `sedimentation_stat` src/ice3/jax/stencils/sedimentation.py:58
+ *
+ * Conventions (same memory order as the Fortran bridge's (nlon, nlev) arrays):
+ *   - every 3-D field is contiguous [nk][nij] (horizontal index fastest),
+ *     FP64, element (ij, k) at offset k*nij + ij; k = 0 is the lowest level
+ *     (ground-to-space ordering, PHYEX D%NKL = 1);
+ *   - 2-D (per column) fields are [nij];
+ *   - the device entry points take DEVICE pointers and run asynchronously on
+ *     `stream` (a cudaStream_t passed as void*; NULL = legacy default stream);
+ *     the `_host` entry points take HOST pointers, stage through device
+ *     buffers owned by the handle and return after the results are back;
+ *   - callers own all field memory; in-out fields are read then overwritten;
+ *   - every call returns ICE3GB_OK (0) or a negative ICE3GB_ERR_* code, no
+ *     exception or abort crosses the ABI; `ice3gb_last_error` gives the text.
+ *
+ * A handle holds one immutable constants table (the reference's
+ * `Phyex(...).to_externals()` flattened into Ice3gbConstants + Ice3gbLuts),
+ * so, unlike the Fortran module state set by `c_ini_rain_ice`, several tables
+ * can live side by side.  Concurrent calls on one handle must use distinct
+ * streams and are then safe, except the `_host` calls, which share the
+ * handle's staging buffers and must be serialised by the caller.
+ */
+#ifndef ICE3GB_H
+#define ICE3GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ICE3GB_VERSION 10000 /* 1.0.0 */
+
+/* ---- status codes ------------------------------------------------------ */
+#define ICE3GB_OK               0
+#define ICE3GB_ERR_NULL        -1  /* required pointer is NULL            */
+#define ICE3GB_ERR_SHAPE       -2  /* nij/nk out of range                  */
+#define ICE3GB_ERR_ALIGN       -3  /* field not 16-byte aligned            */
+#define ICE3GB_ERR_CUDA        -4  /* CUDA runtime error                   */
+#define ICE3GB_ERR_UNSUPPORTED -5  /* option value not implemented         */
+#define ICE3GB_ERR_DEVICE      -6  /* device-side status word set          */
+#define ICE3GB_ERR_HANDLE      -7  /* invalid handle                       */
+#define ICE3GB_ERR_RANGE       -8  /* size beyond a fixed limit            */
+
+/* Device status word bits (read by ice3gb_status). */
+#define ICE3GB_DEV_PASS_CAP     1u /* a point hit the sub-step pass cap     */
+
+/*
+ * Constants table: every field is a double (switches stored as 0.0/1.0,
+ * enumerations as their integer value).  Names are the keys of
+ * `Phyex(program).to_externals()` (src/ice3/phyex_common/phyex.py:307).
+ * `ice3gb_constant_name(i)` returns the i-th name, so hosts fill by name.
+ */
+#define ICE3GB_CONSTANTS(X)                                                   \
+  /* physical constants (modd_cst) */                                         \
+  X(TT) X(CPD) X(CPV) X(CL) X(CI) X(RD) X(RV) X(LVTT) X(LSTT) X(LMTT)         \
+  X(ESTT) X(ALPW) X(BETAW) X(GAMW) X(ALPI) X(BETAI) X(GAMI) X(EPSILO)         \
+  X(P00) X(RHOLW) X(MNH_TINY)                                                 \
+  /* subgrid condensation (modd_nebn) */                                      \
+  X(TMAXMIX) X(TMINMIX) X(LSUBG_COND) X(LSIGMAS) X(LSTATNW)                   \
+  X(FRAC_ICE_ADJUST) X(CONDENS) X(OCND2) X(NRR)                               \
+  /* ICE3/ICE4 switches (modd_param_icen) */                                  \
+  X(LWARM) X(LSEDIC) X(LDEPOSC) X(VDEPOSC) X(SEDIM) X(LFEEDBACKT)             \
+  X(LEVLIMIT) X(LNULLWETG) X(LWETGPOST) X(SNOW_RIMING) X(LCRFLIMIT)           \
+  X(NMAXITER_MICRO) X(MRSTEP) X(TSTEP_TS) X(SUBG_RC_RR_ACCR) X(SUBG_RR_EVAP)  \
+  X(SUBG_PR_PDF) X(SUBG_AUCV_RC) X(SUBG_AUCV_RI) X(SUBG_MF_PDF)               \
+  X(LSEDIM_AFTER) X(LSNOW_T)                                                  \
+  /* hydrometeor descriptors (modd_rain_ice_descrn) */                        \
+  X(CEXVT) X(V_RTMIN) X(C_RTMIN) X(R_RTMIN) X(I_RTMIN) X(S_RTMIN) X(G_RTMIN)  \
+  X(CC) X(DC) X(LBEXC) X(LBC_1) X(LBC_2) X(LBR) X(LBEXR) X(LBI) X(LBEXI)      \
+  X(DI) X(LBS) X(LBEXS) X(LBG) X(LBEXG) X(CXS) X(BS) X(CXG) X(DG)             \
+  X(LBDAS_MAX) X(LBDAS_MIN) X(TRANS_MP_GAMMAS) X(CONC_SEA) X(CONC_LAND)       \
+  X(CONC_URBAN) X(FVELOS) X(ALPHAS) X(NUS) X(GAC) X(GC) X(GAC2) X(GC2)        \
+  /* rate constants (modd_rain_ice_paramn) */                                 \
+  X(FSEDC_1) X(FSEDC_2) X(FSEDR) X(EXSEDR) X(FSEDI) X(EXCSEDI) X(FSEDS)       \
+  X(EXSEDS) X(FSEDG) X(EXSEDG) X(NU10) X(ALPHA1) X(BETA1) X(NU20) X(ALPHA2)   \
+  X(BETA2) X(MNU0) X(ALPHA3) X(BETA3) X(HON) X(SCFAC) X(O0EVAR) X(O1EVAR)     \
+  X(EX0EVAR) X(EX1EVAR) X(O0DEPI) X(O2DEPI) X(O0DEPS) X(O1DEPS) X(EX0DEPS)    \
+  X(EX1DEPS) X(O0DEPG) X(O1DEPG) X(EX0DEPG) X(EX1DEPG) X(TIMAUTI) X(TEXAUTI)  \
+  X(CRIAUTI) X(ACRIAUTI) X(BCRIAUTI) X(FIAGGS) X(COLEXIS) X(EXIAGGS)          \
+  X(TIMAUTC) X(CRIAUTC) X(FCACCR) X(EXCACCR) X(CRIMSS) X(EXCRIMSS) X(CRIMSG)  \
+  X(EXCRIMSG) X(SRIMCG) X(EXSRIMCG) X(SRIMCG2) X(EXSRIMCG2) X(SRIMCG3)        \
+  X(RIMINTP1) X(RIMINTP2) X(NGAMINC) X(FRACCSS) X(LBRACCS1) X(LBRACCS2)       \
+  X(LBRACCS3) X(FSACCRG) X(LBSACCR1) X(LBSACCR2) X(LBSACCR3) X(ACCINTP1S)     \
+  X(ACCINTP2S) X(ACCINTP1R) X(ACCINTP2R) X(NACCLBDAS) X(NACCLBDAR) X(FSCVMG)  \
+  X(RCFRI) X(EXRCFRI) X(ICFRR) X(EXICFRR) X(FCDRYG) X(COLIG) X(COLEXIG)       \
+  X(FIDRYG) X(COLSG) X(COLEXSG) X(FSDRYG) X(LBSDRYG1) X(LBSDRYG2)             \
+  X(LBSDRYG3) X(FRDRYG) X(LBRDRYG1) X(LBRDRYG2) X(LBRDRYG3) X(DRYINTP1R)      \
+  X(DRYINTP2R) X(DRYINTP1S) X(DRYINTP2S) X(DRYINTP1G) X(DRYINTP2G)            \
+  X(NDRYLBDAR) X(NDRYLBDAS) X(NDRYLBDAG)
+
+typedef struct Ice3gbConstants {
+#define ICE3GB_X_FIELD(name) double name;
+  ICE3GB_CONSTANTS(ICE3GB_X_FIELD)
+#undef ICE3GB_X_FIELD
+} Ice3gbConstants;
+
+/* Lookup tables of the ICE4 collection kernels, FP64.  Two-dimensional
+ * tables are row-major: ker_x[i*n2 + j] is the Fortran XKER_X(i+1, j+1)
+ * (micro/mode_ini_rain_ice.F90:768-890, data in src/ice3/phyex_common/xker_*.py). */
+#define ICE3GB_NGAMINC   80
+#define ICE3GB_NACCLBDAS 40
+#define ICE3GB_NACCLBDAR 40
+#define ICE3GB_NDRYLBDAG 40
+#define ICE3GB_NDRYLBDAS 80
+#define ICE3GB_NDRYLBDAR 40
+typedef struct Ice3gbLuts {
+  double gaminc_rim1[ICE3GB_NGAMINC];
+  double gaminc_rim2[ICE3GB_NGAMINC];
+  double gaminc_rim4[ICE3GB_NGAMINC];
+  double ker_raccss[ICE3GB_NACCLBDAS * ICE3GB_NACCLBDAR]; /* (lbdas, lbdar) */
+  double ker_raccs[ICE3GB_NACCLBDAS * ICE3GB_NACCLBDAR];  /* (lbdas, lbdar) */
+  double ker_saccrg[ICE3GB_NACCLBDAR * ICE3GB_NACCLBDAS]; /* (lbdar, lbdas) */
+  double ker_rdryg[ICE3GB_NDRYLBDAG * ICE3GB_NDRYLBDAR];  /* (lbdag, lbdar) */
+  double ker_sdryg[ICE3GB_NDRYLBDAG * ICE3GB_NDRYLBDAS];  /* (lbdag, lbdas) */
+} Ice3gbLuts;
+
+/* ---- ice_adjust -------------------------------------------------------- */
+/* Arguments of IceAdjustJAX.__call__ (src/ice3/jax/ice_adjust.py:139-160)
+ * and of c_ice_adjust (phyex_bridge.F90:27-35); outputs are the 16-tuple of
+ * src/ice3/jax/stencils/ice_adjust.py:381-398, written in place. */
+typedef struct Ice3gbIceAdjustFields {
+  const double *sigqsat;            /* [nij], or [nk][nij] if sigqsat_3d  */
+  const double *pabs, *sigs, *th, *exn, *exn_ref, *rho_dry_ref;
+  const double *rv, *rc, *ri, *rr, *rs, *rg;
+  const double *cf_mf, *rc_mf, *ri_mf;
+  double *rvs, *rcs, *ris, *ths;    /* in-out sources                    */
+  double *t, *rv_out, *rc_out, *ri_out, *cldfr;
+  double *hlc_hrc, *hlc_hcf, *hli_hri, *hli_hcf;
+  double *cph, *lv, *ls;
+  int64_t sigqsat_3d;               /* 0: per column, 1: full 3-D field   */
+} Ice3gbIceAdjustFields;
+
+/* ---- statistical sedimentation ---------------------------------------- */
+/* Arguments of sedimentation_stat (src/ice3/jax/stencils/sedimentation.py:58)
+ * ~ ICE4_SEDIMENTATION_STAT (micro/mode_ice4_sedimentation_stat.F90:9).
+ * The two reference implementations differ, `fortran_semantics` selects:
+ *   0: reference JAX — cloud mean-radius factor 1 (sedimentation.py:156) and
+ *      flux divergence divided by rho*dz*dt (sedimentation.py:337-341);
+ *   1: PHYEX Fortran — factor MAX(1, 0.5*Gamma(NUC+1/ALPHAC)/Gamma(NUC))
+ *      weighted by sea (mode_ice4_sedimentation_stat.F90:123-127, 253) and
+ *      divergence divided by rho*dz (:203-207). */
+typedef struct Ice3gbSedimentationFields {
+  const double *rhodref, *dzz, *pabs, *tht;
+  const double *sea, *town;         /* [nij], optional (NULL -> 0)        */
+  double *rcs, *rrs, *ris, *rss, *rgs;            /* in-out sources       */
+  double *inprc, *inprr, *inpri, *inprs, *inprg;  /* out [nij]            */
+  double *fpr_c, *fpr_r, *fpr_i, *fpr_s, *fpr_g;  /* out, optional        */
+  int64_t fortran_semantics;
+} Ice3gbSedimentationFields;
+
+/* ---- rain_ice ---------------------------------------------------------- */
+/* Arguments of c_rain_ice (phyex_bridge.F90:242-254) / RAIN_ICE
+ * (micro/rain_ice.F90) and of the RainIceJAX state dict
+ * (src/ice3/jax/rain_ice.py:181). */
+typedef struct Ice3gbRainIceFields {
+  const double *exn, *dzz, *rhodref, *exnref, *pabs, *cldfr, *sigs;
+  const double *tht, *rvt, *rct, *rrt, *rit, *rst, *rgt;
+  const double *sea, *town;         /* [nij], optional                    */
+  double *cit;                      /* in-out pristine ice concentration  */
+  double *hlc_hrc, *hlc_hcf, *hli_hri, *hli_hcf;  /* in-out               */
+  double *ths, *rvs, *rcs, *rrs, *ris, *rss, *rgs; /* in-out sources      */
+  double *evap3d, *rainfr;          /* out [nk][nij]                      */
+  double *inprc, *inprr, *inpri, *inprs, *inprg, *indep; /* out [nij]     */
+  double *fpr_c, *fpr_r, *fpr_i, *fpr_s, *fpr_g;  /* out, optional        */
+} Ice3gbRainIceFields;
+
+/* Per-call overrides of RainIceJAX.__call__ keywords
+ * (src/ice3/jax/rain_ice.py:181-190); a negative value keeps the table's. */
+typedef struct Ice3gbRainIceOptions {
+  int32_t lsedim_after;   /* LSEDIM_AFTER                                   */
+  int32_t ldeposc;        /* LDEPOSC (fog deposition)                       */
+  int32_t lfeedbackt;     /* LFEEDBACKT                                     */
+  int32_t max_passes;     /* cap on tendency passes per point (default 256) */
+  int32_t sed_jax;        /* 1: reference-JAX sedimentation semantics,
+                             0 (default): Fortran (see Ice3gbSedimentationFields) */
+} Ice3gbRainIceOptions;
+
+/* ---- library / handle -------------------------------------------------- */
+int         ice3gb_version(void);
+int         ice3gb_constant_count(void);
+const char *ice3gb_constant_name(int i);
+/* Replaces c_ini_rain_ice (phyex_bridge.F90:215): validates the table,
+ * uploads the lookup tables to the current device, returns a handle. */
+int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handle);
+int ice3gb_destroy(void *handle);
+/* Text of the last error on this handle (or of the last global error when
+ * handle is NULL); returns the message length. */
+int ice3gb_last_error(void *handle, char *buf, size_t n);
+/* Synchronises `stream`, reads and clears the device status word; returns
+ * ICE3GB_OK or ICE3GB_ERR_DEVICE (bits in *bits when non-NULL). */
+int ice3gb_status(void *handle, void *stream, uint32_t *bits);
+
+/* ---- device entry points (async on stream) ----------------------------- */
+/* Replaces c_ice_adjust (phyex_bridge.F90:27) / IceAdjustJAX.__call__. */
+int ice3gb_ice_adjust(void *handle, int nij, int nk, double dt,
+                      const Ice3gbIceAdjustFields *f, void *stream);
+/* Replaces sedimentation_stat (stencils/sedimentation.py:58). */
+int ice3gb_sedimentation(void *handle, int nij, int nk, double dt,
+                         const Ice3gbSedimentationFields *f, void *stream);
+/* Replaces c_rain_ice (phyex_bridge.F90:242) / RainIceJAX.__call__. */
+int ice3gb_rain_ice(void *handle, int nij, int nk, double dt,
+                    const Ice3gbRainIceOptions *opt,
+                    const Ice3gbRainIceFields *f, void *stream);
+
+/* ---- host-buffer entry points (synchronous) ---------------------------- */
+/* Same as above with HOST pointers, as c_ice_adjust / c_rain_ice take them:
+ * host->device copies, the kernels and device->host copies all run on
+ * `stream`; the call returns when the outputs are in host memory. */
+int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt,
+                           const Ice3gbIceAdjustFields *f, void *stream);
+int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt,
+                         const Ice3gbRainIceOptions *opt,
+                         const Ice3gbRainIceFields *f, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ICE3GB_H */

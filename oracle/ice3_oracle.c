@@ -1,0 +1,1373 @@
+/*
+ * ice3_oracle.c — CPU FP64 restatement of the ICE3 hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * smoke test and the CPU-baseline leg of the benchmark call it to produce the
+ * expected outputs and the host-core timing.  The product (the CUDA library
+ * under dwarf-p-ice3_gb300/) never links, loads or calls it.
+ *
+ * Every routine cites the reference lines it restates
+ * (maurinl26/dwarf-p-ice3; paths relative to that project):
+ *   - ice_adjust: src/ice3/jax/stencils/ice_adjust.py:26-398 (the reference
+ *     JAX, which is executed unmodified in FP64 to make the golden vectors);
+ *   - sedimentation: src/ice3/jax/stencils/sedimentation.py:58-352 and
+ *     PHYEX-IAL_CY50T1/micro/mode_ice4_sedimentation_stat.F90:9-455;
+ *   - rain_ice: PHYEX-IAL_CY50T1/micro/rain_ice.F90 (incl. the disabled
+ *     tail :758-790), mode_ice4_pack.F90, mode_ice4_stepping.F90,
+ *     mode_ice4_tendencies.F90 and the process modules it calls.
+ *
+ * Parallelised with OpenMP over grid points / columns.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/ice3gb.h"
+
+typedef Ice3gbConstants C;
+
+#define EXPORT __attribute__((visibility("default")))
+
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double clip01(double x) { return dmin(dmax(x, 0.0), 1.0); }
+static inline double sq(double x) { return x * x; }
+
+/* ===================================================================== */
+/* ice_adjust (src/ice3/jax/stencils/ice_adjust.py:26-398)               */
+/* ===================================================================== */
+
+/* Triangle-PDF subgrid autoconversion, stencils/ice_adjust.py:316-341. */
+static void triangle_pdf(double w_dt, double crit, double cf_mf, double *hcf_out, double *hr_out)
+{
+  const double wmax = dmax(1e-20, w_dt);
+  double hcf, hr;
+  if (w_dt > crit) {
+    hcf = 1.0 - 0.5 * sq(crit * cf_mf / wmax);
+    hr = w_dt - pow(crit * cf_mf, 3.0) / (3.0 * sq(wmax));
+  } else if (2.0 * w_dt <= crit) {
+    hcf = 0.0;
+    hr = 0.0;
+  } else {
+    hcf = sq(2.0 * w_dt - crit) / (2.0 * sq(wmax));
+    hr = (4.0 * pow(w_dt, 3.0) - 3.0 * w_dt * sq(crit) + pow(crit, 3.0)) / (3.0 * sq(wmax));
+  }
+  *hcf_out = hcf * cf_mf;
+  *hr_out = hr;
+}
+
+EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f)
+{
+  if (!c || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
+  const long n = (long)nij * nk;
+  const int nrr = (int)c->NRR;
+  const int subg = c->LSUBG_COND != 0.0;
+  const int fmode = (int)c->FRAC_ICE_ADJUST;
+  const int sigmas = c->LSIGMAS != 0.0 && c->LSTATNW == 0.0;
+  const int mfpdf = (int)c->SUBG_MF_PDF;
+  if (c->CONDENS != 0.0 || c->OCND2 != 0.0) return ICE3GB_ERR_UNSUPPORTED;
+#pragma omp parallel for schedule(static)
+  for (long p = 0; p < n; ++p) {
+    const long col = p % nij;
+    const double sigqsat = f->sigqsat_3d ? f->sigqsat[p] : f->sigqsat[col];
+    const double pabs = f->pabs[p], sigs = f->sigs[p];
+    const double rv = f->rv[p], rc = f->rc[p], ri = f->ri[p];
+    const double rr = f->rr[p], rs = f->rs[p], rg = f->rg[p];
+    double t = f->th[p] * f->exn[p];                                   /* :158 */
+    const double lv = c->LVTT + (c->CPV - c->CL) * (t - c->TT);        /* functions/ice_adjust.py:18 */
+    const double ls = c->LSTT + (c->CPV - c->CI) * (t - c->TT);        /* functions/ice_adjust.py:70 */
+    double cph;                                                        /* :163-172 */
+    if (nrr == 5) cph = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * (ri + rs);
+    else if (nrr == 4) cph = c->CPD + c->CPV * rv + c->CL * (rc + rr);
+    else if (nrr == 2) cph = c->CPD + c->CPV * rv + c->CL * rc + c->CI * ri;
+    else cph = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * (ri + rs + rg);
+    double cldfr = 0.0, rv_out = 0.0, rc_out = 0.0, ri_out = 0.0;
+    double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
+    if (subg) {
+      const double rt = rv + rc + ri;                                  /* :190 */
+      /* es_w/es_i: functions/tiwmx.py:18,60 */
+      const double pv = dmin(exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)), 0.99 * pabs);
+      const double piv = dmin(exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)), 0.99 * pabs);
+      double frac = (rc + ri > 1e-20) ? rc / (rc + ri) : 0.0;          /* :198-202 */
+      if (fmode == 3) frac = clip01(frac);
+      else if (fmode == 0) frac = clip01((c->TMAXMIX - t) / (c->TMAXMIX - c->TMINMIX));
+      double qsl = c->RD / c->RV * pv / (pabs - pv);                   /* :212 */
+      const double qsi = c->RD / c->RV * piv / (pabs - piv);
+      qsl = (1.0 - frac) * qsl + frac * qsi;
+      const double lvs = (1.0 - frac) * lv + frac * ls;
+      const double ah = lvs * qsl / (c->RV * sq(t)) * (1.0 + c->RV * qsl / c->RD);
+      const double a = 1.0 / (1.0 + lvs / cph * ah);
+      const double sbar = a * (rt - qsl + ah * lvs * (rc + ri) / cph);
+      double sigma;
+      if (sigmas)                                                      /* :226-233 */
+        sigma = (sigqsat != 0.0) ? sqrt(sq(2.0 * sigs) + sq(sigqsat * qsl * a)) : 2.0 * sigs;
+      else
+        sigma = 2.0 * sigs;
+      sigma = dmax(1e-10, sigma);
+      const double q1 = sbar / sigma;
+      double cond;                                                     /* :241-249 */
+      if (q1 > 0.0) cond = (q1 <= 2.0) ? dmin(exp(-1.0) + 0.66 * q1 + 0.086 * sq(q1), 2.0) : q1;
+      else cond = exp(1.2 * q1 - 1.0);
+      cond *= sigma;
+      cldfr = (cond >= 1e-12) ? clip01(0.5 + 0.36 * atan(1.55 * q1)) : 0.0;
+      if (cldfr == 0.0) cond = 0.0;
+      rc_out = (1.0 - frac) * cond;                                    /* :263-266 */
+      ri_out = frac * cond;
+      t = t + ((rc_out - rc) * lv + (ri_out - ri) * ls) / cph;
+      rv_out = rt - rc_out - ri_out;
+    }
+    double rvs = f->rvs[p], rcs = f->rcs[p], ris = f->ris[p], ths = f->ths[p];
+    const double exn_ref = f->exn_ref[p];
+    double w1 = (rc_out - rc) / dt, w2 = (ri_out - ri) / dt;           /* :269-281 */
+    w1 = (w1 < 0.0) ? dmax(w1, -rcs) : dmin(w1, rvs);
+    rvs = rvs - w1;
+    rcs = rcs + w1;
+    ths = ths + w1 * lv / (cph * exn_ref);
+    w2 = (w2 < 0.0) ? dmax(w2, -ris) : dmin(w2, rvs);
+    rvs = rvs - w2;
+    ris = ris + w2;
+    ths = ths + w2 * ls / (cph * exn_ref);
+    if (!subg) {
+      cldfr = ((rcs + ris) * dt > 1e-12) ? 1.0 : 0.0;                 /* :285 */
+    } else {
+      const double cf_mf = f->cf_mf[p];                                /* :288-305 */
+      double w1m = f->rc_mf[p] / dt, w2m = f->ri_mf[p] / dt;
+      const double tot = w1m + w2m;
+      const double scale = (tot > rvs) ? rvs / tot : 1.0;
+      w1m *= scale;
+      w2m *= scale;
+      cldfr = dmin(1.0, cldfr + cf_mf);
+      rcs = rcs + w1m;
+      ris = ris + w2m;
+      rvs = rvs - w1m - w2m;
+      ths = ths + (w1m * lv + w2m * ls) / (cph * exn_ref);
+      const double criaut = c->CRIAUTC / f->rho_dry_ref[p];            /* :308 */
+      if (mfpdf == 0) {
+        if (w1m * dt > cf_mf * criaut) { hlc_hrc = w1m * dt; hlc_hcf = dmin(1.0, cf_mf); }
+      } else if (mfpdf == 1) {
+        double hcf, hr;
+        triangle_pdf(w1m * dt, cf_mf * criaut, cf_mf, &hcf, &hr);
+        hlc_hcf = dmin(1.0, hcf);
+        hlc_hrc = hr;
+      }
+      const double criaut_i = dmin(c->CRIAUTI, pow(10.0, c->ACRIAUTI * (t - c->TT) + c->BCRIAUTI));
+      if (mfpdf == 0) {
+        if (w2m * dt > cf_mf * criaut_i) { hli_hri = w2m * dt; hli_hcf = dmin(1.0, cf_mf); }
+      } else if (mfpdf == 1) {
+        double hcf, hr;
+        triangle_pdf(w2m * dt, cf_mf * criaut_i, cf_mf, &hcf, &hr);
+        hli_hcf = dmin(1.0, hcf);
+        hli_hri = hr;
+      }
+    }
+    f->t[p] = t;
+    f->rv_out[p] = rv_out;
+    f->rc_out[p] = rc_out;
+    f->ri_out[p] = ri_out;
+    f->cldfr[p] = cldfr;
+    f->hlc_hrc[p] = hlc_hrc;
+    f->hlc_hcf[p] = hlc_hcf;
+    f->hli_hri[p] = hli_hri;
+    f->hli_hcf[p] = hli_hcf;
+    f->cph[p] = cph;
+    f->lv[p] = lv;
+    f->ls[p] = ls;
+    f->rvs[p] = rvs;
+    f->rcs[p] = rcs;
+    f->ris[p] = ris;
+    f->ths[p] = ths;
+  }
+  return ICE3GB_OK;
+}
+
+/* ===================================================================== */
+/* Statistical sedimentation                                             */
+/* ===================================================================== */
+
+/* Terminal velocity of rain/snow/graupel: sedimentation.py:35-43,
+ * mode_ice4_sedimentation_stat.F90:408,413. */
+static inline double sed_other(double fsed, double exsed, double r, double rho, double cexvt)
+{
+  return fsed * pow(r, exsed - 1.0) * pow(rho, exsed - cexvt - 1.0);
+}
+
+/* Pristine ice velocity: sedimentation.py:46-55, F90:307-319. */
+static inline double sed_ice(const C *c, double r, double rho)
+{
+  return c->FSEDI * pow(rho, -c->CEXVT) *
+         pow(dmax(0.05e6, -0.15319e6 - 0.021454e6 * log(rho * r)), c->EXCSEDI);
+}
+
+/* Cloud droplet velocity: sedimentation.py:206-214, F90:264-275. */
+static inline double sed_cloud(const C *c, double r, double rho, double wlbda, double lbc,
+                               double conc, double ray, double fsedc)
+{
+  const double wlbdc = pow(lbc * conc / (rho * r), c->LBEXC);
+  const double cc = c->CC * (1.0 + 1.26 * wlbda * wlbdc / ray);
+  return pow(rho, -c->CEXVT) * pow(wlbdc, -c->DC) * cc * fsedc;
+}
+
+/* One column, top (k = nk-1) to bottom (k = 0).  `rt` are the sedimenting
+ * contents (source * dt), `src` the sources updated in place.  Species order
+ * c, r, i, s, g.  fpr (optional) gets the downward flux F_k per level. */
+static void sed_column(const C *c, int nij, int nk, double dt, long col, int fortran,
+                       const double *rho, const double *dzz, const double *pabs,
+                       const double *tht, double sea, double town, int has_sea_town,
+                       double *src[5], double *fpr[5], double inpr[5])
+{
+  const double rtmin[5] = {c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN};
+  /* cloud parameters: sedimentation.py:153-156 / F90:122-127,252-260 */
+  double lbc, fsedc, conc, ray;
+  if (fortran) {
+    const double gac_gc = c->GAC / c->GC, gac2_gc2 = c->GAC2 / c->GC2;
+    if (has_sea_town) {
+      ray = dmax(1.0, 0.5 * ((1.0 - sea) * gac_gc + sea * gac2_gc2));
+      lbc = dmax(dmin(c->LBC_1, c->LBC_2), sea * c->LBC_2 + (1.0 - sea) * c->LBC_1);
+      fsedc = dmax(dmin(c->FSEDC_1, c->FSEDC_2), sea * c->FSEDC_2 + (1.0 - sea) * c->FSEDC_1);
+      conc = (1.0 - town) * (sea * c->CONC_SEA + (1.0 - sea) * c->CONC_LAND) + town * c->CONC_URBAN;
+    } else {
+      ray = dmax(1.0, 0.5 * gac_gc);
+      lbc = c->LBC_1;
+      fsedc = c->FSEDC_1;
+      conc = c->CONC_LAND;
+    }
+  } else {
+    ray = 1.0;
+    lbc = (1.0 - sea) * c->LBC_1 + sea * c->LBC_2;
+    fsedc = (1.0 - sea) * c->FSEDC_1 + sea * c->FSEDC_2;
+    conc = (1.0 - town) * ((1.0 - sea) * c->CONC_LAND + sea * c->CONC_SEA) + town * c->CONC_URBAN;
+  }
+  const double fsed[5] = {0.0, c->FSEDR, 0.0, c->FSEDS, c->FSEDG};
+  const double exsed[5] = {0.0, c->EXSEDR, 0.0, c->EXSEDS, c->EXSEDG};
+  const double imin = dmax(c->I_RTMIN, 1.0e-7);
+  double fabove[5] = {0, 0, 0, 0, 0};
+  for (int k = nk - 1; k >= 0; --k) {
+    const long p = (long)k * nij + col;
+    const double r_rho = rho[p], dz = dzz[p];
+    const double tsorhodz = dt / (r_rho * dz);
+    const double wlbda = 6.6e-8 * (101325.0 / pabs[p]) * (tht[p] / 293.15);
+    double fk[5];
+    for (int s = 0; s < 5; ++s) {
+      const double rt = src[s][p] * dt;                  /* sedimentation.py:134-138; F90 driver :167-173 */
+      const double qp = fabove[s] * tsorhodz;
+      double w1 = 0.0, w2 = 0.0;
+      if (s == 0) {
+        if (fortran && c->LSEDIC == 0.0) { fk[s] = 0.0; continue; }
+        if (rt > rtmin[0]) w1 = sed_cloud(c, rt, r_rho, wlbda, lbc, conc, ray, fsedc);
+        if (qp > rtmin[0]) w2 = sed_cloud(c, qp, r_rho, wlbda, lbc, conc, ray, fsedc);
+      } else if (s == 2) {
+        if (rt > imin) w1 = sed_ice(c, rt, r_rho);
+        if (qp > imin) w2 = sed_ice(c, qp, r_rho);
+      } else {
+        if (rt > rtmin[s]) w1 = sed_other(fsed[s], exsed[s], rt, r_rho, c->CEXVT);
+        if (qp > rtmin[s]) w2 = sed_other(fsed[s], exsed[s], qp, r_rho, c->CEXVT);
+      }
+      /* FWSED1/FWSED2: F90:442-453; sedimentation.py:216-223 */
+      double flux = dmin(r_rho * dz * rt * (1.0 / dt), w1 * r_rho * rt);
+      if (w2 != 0.0) flux += dmax(0.0, 1.0 - dz / (dt * w2)) * fabove[s];
+      fk[s] = flux;
+    }
+    for (int s = 0; s < 5; ++s) {
+      /* flux divergence: F90:203-207 (Fortran) vs sedimentation.py:337-341 (JAX) */
+      if (fortran)
+        src[s][p] = src[s][p] + tsorhodz * (fabove[s] - fk[s]) * (1.0 / dt);
+      else
+        src[s][p] = src[s][p] + (fabove[s] - fk[s]) / (r_rho * dz * dt);
+      if (fpr[s]) fpr[s][p] = fk[s];
+      fabove[s] = fk[s];
+    }
+  }
+  for (int s = 0; s < 5; ++s) inpr[s] = fabove[s] / c->RHOLW;   /* :344-348 / F90:213-223 */
+}
+
+EXPORT int ice3o_sedimentation(const C *c, int nij, int nk, double dt, const Ice3gbSedimentationFields *f)
+{
+  if (!c || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
+  const int fortran = f->fortran_semantics != 0;
+  const int has = f->sea != NULL && f->town != NULL;
+#pragma omp parallel for schedule(static)
+  for (long col = 0; col < nij; ++col) {
+    double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
+    double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
+    double inpr[5];
+    const double sea = f->sea ? f->sea[col] : 0.0, town = f->town ? f->town[col] : 0.0;
+    sed_column(c, nij, nk, dt, col, fortran, f->rhodref, f->dzz, f->pabs, f->tht, sea, town,
+               has, src, fpr, inpr);
+    f->inprc[col] = inpr[0];
+    f->inprr[col] = inpr[1];
+    f->inpri[col] = inpr[2];
+    f->inprs[col] = inpr[3];
+    f->inprg[col] = inpr[4];
+  }
+  return ICE3GB_OK;
+}
+
+/* ===================================================================== */
+/* ICE4 processes (one grid point)                                       */
+/* ===================================================================== */
+
+enum { ITH = 0, IRV = 1, IRC = 2, IRR = 3, IRI = 4, IRS = 5, IRG = 6, NV = 7 };
+
+/* Instantaneous/rate budget slots (Fortran IBU* indices, KRR=6 subset). */
+enum {
+  B_RVHENI_MR, B_RRHONG_MR, B_RIMLTC_MR, B_RSRIMCG_MR,
+  B_RCHONI, B_RVDEPS, B_RIAGGS, B_RIAUTS, B_RVDEPG,
+  B_RCAUTR, B_RCACCR, B_RREVAV,
+  B_RCRIMSS, B_RCRIMSG, B_RSRIMCG, B_RRACCSS, B_RRACCSG, B_RSACCRG, B_RSMLTG, B_RCMLTSR,
+  B_RICFRRG, B_RRCFRIG, B_RICFRR, B_RCWETG, B_RIWETG, B_RRWETG, B_RSWETG,
+  B_RCDRYG, B_RIDRYG, B_RRDRYG, B_RSDRYG, B_RGMLTR, B_RCBERI,
+  NBU
+};
+/* fast_rs persistent tendencies (mode_ice4_fast_rs.F90 IRCRIMS..IFREEZ2) */
+enum { RS_RCRIMS, RS_RCRIMSS, RS_RSRIMCG, RS_RRACCS, RS_RRACCSS, RS_RSACCRG, RS_FREEZ1, RS_FREEZ2, NRS };
+/* fast_rg persistent tendencies (mode_ice4_fast_rg.F90 IRCDRYG..IFREEZ2) */
+enum { RG_RCDRYG, RG_RIDRYG, RG_RIWETG, RG_RSDRYG, RG_RSWETG, RG_RRDRYG, RG_FREEZ1, RG_FREEZ2, NRG };
+
+typedef struct {
+  double bu[NBU];
+  double rs_tend[NRS];
+  double rg_tend[NRG];
+  double ssi, ka, dv, ai, cj;
+} PointRates;
+
+static inline double esatw(const C *c, double t) { return exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)); }
+static inline double esati(const C *c, double t) { return exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)); }
+
+/* ICE4_NUCLEATION, micro/ice4_nucleation.func.h:69-144 (LOCND2 = .FALSE.). */
+static void ice4_nucleation(const C *c, int ldcompute, double tht, double pabst, double rhodref,
+                            double exn, double lsfact, double t, double rvt, double *cit,
+                            double *rvheni_mr, double *ssi_out)
+{
+  const int gnegt = ldcompute && t < c->TT && rvt > c->V_RTMIN;
+  double zusw = 0.0, zzw = 0.0, zssi = 0.0;
+  *rvheni_mr = 0.0;
+  if (gnegt) {
+    zzw = log(t);
+    zusw = exp(c->ALPW - c->BETAW / t - c->GAMW * zzw);
+    zzw = exp(c->ALPI - c->BETAI / t - c->GAMI * zzw);
+    zzw = dmin(pabst / 2.0, zzw);
+    zssi = rvt * (pabst - zzw) / (c->EPSILO * zzw) - 1.0;
+    zusw = dmin(pabst / 2.0, zusw);
+    zusw = (zusw / zzw) * ((pabst - zzw) / (pabst - zusw)) - 1.0;
+    zssi = dmin(zssi, zusw);
+    zzw = 0.0;
+    if (t < c->TT - 5.0 && zssi > 0.0) {
+      zzw = c->NU20 * exp(c->ALPHA2 * zssi - c->BETA2);
+    } else if (t <= c->TT - 2.0 && t >= c->TT - 5.0 && zssi > 0.0) {
+      zzw = dmax(c->NU20 * exp(-c->BETA2), c->NU10 * exp(-c->BETA1 * (t - c->TT)) * pow(zssi / zusw, c->ALPHA1));
+    }
+    zzw = zzw - *cit;
+    zzw = dmin(zzw, 50.e3);
+    *rvheni_mr = dmax(zzw, 0.0) * c->MNU0 / rhodref;
+    *rvheni_mr = dmin(rvt, *rvheni_mr);
+    if (c->LFEEDBACKT != 0.0) {
+      const double w = dmin(*rvheni_mr, dmax(0.0, (c->TT / exn - tht) / lsfact)) / dmax(*rvheni_mr, 1.e-20);
+      *rvheni_mr *= w;
+      zzw *= w;
+    }
+    *cit = dmax(zzw + *cit, *cit);
+  }
+  if (ssi_out) *ssi_out = zssi;
+}
+
+/* ICE4_RRHONG, micro/mode_ice4_rrhong.F90. */
+static double ice4_rrhong(const C *c, int ldcompute, double exn, double lvfact, double lsfact,
+                          double t, double rrt, double tht)
+{
+  if (t < c->TT - 35.0 && rrt > c->R_RTMIN && ldcompute) {
+    double r = rrt;
+    if (c->LFEEDBACKT != 0.0) r = dmin(r, dmax(0.0, ((c->TT - 35.0) / exn - tht) / (lsfact - lvfact)));
+    return r;
+  }
+  return 0.0;
+}
+
+/* ICE4_RIMLTC, micro/mode_ice4_rimltc.F90. */
+static double ice4_rimltc(const C *c, int ldcompute, double exn, double lvfact, double lsfact,
+                          double t, double tht, double rit)
+{
+  if (rit > 0.0 && t > c->TT && ldcompute) {
+    double r = rit;
+    if (c->LFEEDBACKT != 0.0) r = dmin(r, dmax(0.0, (tht - c->TT / exn) / (lsfact - lvfact)));
+    return r;
+  }
+  return 0.0;
+}
+
+/* Derived fields, mode_ice4_tendencies.F90:303-320 (non-tabulated branch);
+ * same formulas as stencils/ice4_tendencies.py:191-245. */
+static void ice4_derived(const C *c, double t, double rhodref, double pres, double rv,
+                         double *ssi, double *ka, double *dv, double *ai, double *cj)
+{
+  const double zzw = exp(c->ALPI - c->BETAI / t - c->GAMI * log(t));
+  *ssi = rv * (pres - zzw) / (c->EPSILO * zzw) - 1.0;
+  *ka = 2.38e-2 + 7.1e-5 * (t - c->TT);
+  *dv = 2.11e-5 * pow(t / c->TT, 1.94) * (c->P00 / pres);
+  *ai = sq(c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / (*ka * c->RV * sq(t)) + (c->RV * t) / (*dv * zzw);
+  *cj = c->SCFAC * pow(rhodref, 0.3) / sqrt(1.718e-5 + 4.9e-8 * (t - c->TT));
+}
+
+/* ICE4_COMPUTE_PDF, micro/mode_ice4_compute_pdf.F90 (one point).
+ * hl[0..3] = HLC_HCF, HLC_LCF, HLC_HRC, HLC_LRC; hi[0..3] = HLI_HCF, HLI_LCF,
+ * HLI_HRI, HLI_LRI (in-out for the ADJU modes).  Returns the rain fraction. */
+static double ice4_compute_pdf(const C *c, int ldmicro, double rhodref, double rct, double rit,
+                               double cf, double t, double sigma_rc, double hl[4], double hi[4])
+{
+  const int aucv_rc = (int)c->SUBG_AUCV_RC, aucv_ri = (int)c->SUBG_AUCV_RI, prpdf = (int)c->SUBG_PR_PDF;
+  const double rcrautc = ldmicro ? c->CRIAUTC / rhodref : 0.0;
+  double hcf = 0, lcf = 0, hrc = 0, lrc = 0;
+  if (aucv_rc == 0) {               /* NONE */
+    if (rct > rcrautc && ldmicro) { hcf = 1.0; hrc = rct; }
+    else if (rct > c->C_RTMIN && ldmicro) { lcf = 1.0; lrc = rct; }
+  } else if (aucv_rc == 3) {        /* CLFR */
+    if (cf > 0.0 && rct > rcrautc * cf && ldmicro) { hcf = cf; hrc = rct; }
+    else if (cf > 0.0 && rct > c->C_RTMIN && ldmicro) { lcf = cf; lrc = rct; }
+  } else if (aucv_rc == 2) {        /* ADJU */
+    const double sum = ldmicro ? hl[3] + hl[2] : 0.0;
+    hcf = hl[0]; lcf = hl[1];
+    if (sum > 1.e-20 && ldmicro) { lrc = hl[3] * rct / sum; hrc = hl[2] * rct / sum; }
+  } else if (aucv_rc == 1 && prpdf == 0) {  /* PDF + SIGM */
+    if (rct > rcrautc + sigma_rc && ldmicro) {
+      hcf = 1.0; hrc = rct;
+    } else if (rct > rcrautc - sigma_rc && rct <= rcrautc + sigma_rc && ldmicro) {
+      hcf = (rct + sigma_rc - rcrautc) / (2.0 * sigma_rc);
+      lcf = dmax(0.0, cf - hcf);
+      hrc = (rct + sigma_rc - rcrautc) * (rct + sigma_rc + rcrautc) / (4.0 * sigma_rc);
+      lrc = dmax(0.0, rct - hrc);
+    } else if (rct > c->C_RTMIN && cf > 0.0 && ldmicro) {
+      lcf = cf; lrc = rct;
+    }
+  } else if (aucv_rc == 1) {        /* PDF + HLC*PDF */
+    const double coeff = (prpdf == 1 || prpdf == 2) ? 2.0 : (prpdf == 3 ? 3.0 : 4.0);
+    const double rcmax = (rct > 0.0 && cf > 0.0 && ldmicro) ? coeff * rct / cf : 0.0;
+    double lloc = 0.0, hloc = 0.0;
+    const int ok = rct > 0.0 && cf > 0.0 && rcmax > rcrautc && ldmicro;
+    if (prpdf == 1) {
+      if (ok) { lloc = 0.5 * rcrautc; hloc = (rcmax + rcrautc) / 2.0; }
+    } else if (prpdf == 3) {
+      if (ok) {
+        lloc = (rcrautc * (3.0 * rcmax - 2.0 * rcrautc)) / (3.0 * (2.0 * rcmax - rcrautc));
+        hloc = (rcmax + 2.0 * rcrautc) / 3.0;
+      }
+    } else if (prpdf == 4) {
+      if (ok) {
+        lloc = (3.0 * pow(rcrautc, 3) - 8.0 * sq(rcrautc) * rcmax + 6.0 * rcrautc * sq(rcmax)) /
+               (4.0 * sq(rcrautc) - 12.0 * rcrautc * rcmax + 12.0 * sq(rcmax));
+        hloc = (rcmax + 3.0 * rcrautc) / 4.0;
+      }
+    } else if (prpdf == 2) {
+      if (rct <= rcrautc * cf && ok) {
+        lloc = (pow(rcmax, 3) - 12.0 * rcmax * sq(rcrautc) + 8.0 * pow(rcrautc, 3)) /
+               (6.0 * sq(rcmax) - 24.0 * rcmax * rcrautc + 12.0 * sq(rcrautc));
+        hloc = (rcmax + 2.0 * rcrautc) / 3.0;
+      } else if (ok) {
+        lloc = (2.0 / 3.0) * rcrautc;
+        hloc = (3.0 * pow(rcmax, 3) - 8.0 * pow(rcrautc, 3)) / (6.0 * sq(rcmax) - 12.0 * sq(rcrautc));
+      }
+    }
+    if (ok) {
+      lcf = cf * (hloc - (rct / cf)) / (hloc - lloc);
+      hcf = dmax(0.0, cf - lcf);
+      lrc = lloc * lcf;
+      hrc = dmax(0.0, rct - lrc);
+    } else if (rct > 0.0 && cf > 0.0 && rcmax <= rcrautc && ldmicro) {
+      lcf = cf; lrc = rct;
+    }
+  }
+  hl[0] = hcf; hl[1] = lcf; hl[2] = hrc; hl[3] = lrc;
+  const double criauti = ldmicro ? dmin(c->CRIAUTI, pow(10.0, c->ACRIAUTI * (t - c->TT) + c->BCRIAUTI)) : 0.0;
+  double ihcf = 0, ilcf = 0, ihri = 0, ilri = 0;
+  if (aucv_ri == 0) {
+    if (rit > criauti && ldmicro) { ihcf = 1.0; ihri = rit; }
+    else if (rit > c->I_RTMIN && ldmicro) { ilcf = 1.0; ilri = rit; }
+  } else if (aucv_ri == 1) {
+    if (cf > 0.0 && rit > criauti * cf && ldmicro) { ihcf = cf; ihri = rit; }
+    else if (cf > 0.0 && rit > c->I_RTMIN && ldmicro) { ilcf = cf; ilri = rit; }
+  } else if (aucv_ri == 2) {
+    const double sum = ldmicro ? hi[3] + hi[2] : 0.0;
+    ihcf = hi[0]; ilcf = hi[1];
+    if (sum > 1.e-20 && ldmicro) { ilri = hi[3] * rit / sum; ihri = hi[2] * rit / sum; }
+  }
+  hi[0] = ihcf; hi[1] = ilcf; hi[2] = ihri; hi[3] = ilri;
+  return ldmicro ? dmax(hl[0], hi[0]) : 0.0;
+}
+
+/* INTERP_MICRO_1D / _2D (packed path), micro/interp_micro.func.h:5-269. */
+static inline double lut_index(double x, int knum, double p1, double p2, int *i)
+{
+  double z = dmax(1.00001, dmin((double)knum - 0.00001, p1 * log(x) + p2));
+  *i = (int)z;
+  return z - (double)(*i);
+}
+static inline double lut1d(const double *lt, int i, double f)
+{
+  return lt[i] * f - lt[i - 1] * (f - 1.0);  /* PLT(I+1)*F - PLT(I)*(F-1) */
+}
+/* PLT(i1, i2) with Fortran 1-based (i1, i2) = row-major lt[(i1-1)*n2 + (i2-1)] */
+static inline double lut2d(const double *lt, int n2, int i1, double f1, int i2, double f2)
+{
+#define L(a, b) lt[((a) - 1) * n2 + ((b) - 1)]
+  return (L(i1 + 1, i2 + 1) * f2 - L(i1 + 1, i2) * (f2 - 1.0)) * f1 -
+         (L(i1, i2 + 1) * f2 - L(i1, i2) * (f2 - 1.0)) * (f1 - 1.0);
+#undef L
+}
+
+/* Per-point context passed to the process routines. */
+typedef struct {
+  const C *c;
+  const Ice3gbLuts *lut;
+  int ldsoft, ldcompute;
+  double rhodref, pres, exn, lvfact, lsfact, cf, sigma_rc;
+  double t;          /* temperature after the instantaneous processes */
+  double v[NV];      /* state after the instantaneous processes       */
+  double lbdar, lbdar_rf, lbdas, lbdag;
+  double rainfr;     /* PRAINFR (packed, per point)                   */
+  double hl[4], hi[4];
+} Tctx;
+
+/* ICE4_SLOW, micro/mode_ice4_slow.F90 (LNEWCOEFF = LOCND2 = .FALSE.). */
+static void ice4_slow(const Tctx *x, PointRates *pr)
+{
+  const C *c = x->c;
+  const double t = x->t, rho = x->rhodref;
+  double *b = pr->bu;
+  if (t < c->TT - 35.0 && x->v[IRC] > c->C_RTMIN && x->ldcompute) {
+    if (!x->ldsoft) b[B_RCHONI] = dmin(1000., c->HON * rho * x->v[IRC] * exp(c->ALPHA3 * (t - c->TT) - c->BETA3));
+  } else b[B_RCHONI] = 0.0;
+  if (x->v[IRV] > c->V_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute) {
+    if (!x->ldsoft)
+      b[B_RVDEPS] = (pr->ssi / (rho * pr->ai)) *
+                    (c->O0DEPS * pow(x->lbdas, c->EX0DEPS) + c->O1DEPS * pr->cj * pow(x->lbdas, c->EX1DEPS));
+  } else b[B_RVDEPS] = 0.0;
+  if (x->v[IRI] > c->I_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute) {
+    if (!x->ldsoft)
+      b[B_RIAGGS] = c->FIAGGS * exp(c->COLEXIS * (t - c->TT)) * x->v[IRI] * pow(x->lbdas, c->EXIAGGS) *
+                    pow(rho, -c->CEXVT);
+  } else b[B_RIAGGS] = 0.0;
+  if (x->hi[2] > c->I_RTMIN && x->ldcompute) {
+    if (!x->ldsoft) {
+      const double criauti = dmin(c->CRIAUTI, pow(10.0, c->ACRIAUTI * (t - c->TT) + c->BCRIAUTI));
+      b[B_RIAUTS] = c->TIMAUTI * exp(c->TEXAUTI * (t - c->TT)) * dmax(x->hi[2] - criauti * x->hi[0], 0.0);
+    }
+  } else b[B_RIAUTS] = 0.0;
+  if (x->v[IRV] > c->V_RTMIN && x->v[IRG] > c->G_RTMIN && x->ldcompute) {
+    if (!x->ldsoft)
+      b[B_RVDEPG] = (pr->ssi / (rho * pr->ai)) *
+                    (c->O0DEPG * pow(x->lbdag, c->EX0DEPG) + c->O1DEPG * pr->cj * pow(x->lbdag, c->EX1DEPG));
+  } else b[B_RVDEPG] = 0.0;
+}
+
+/* ICE4_WARM, micro/mode_ice4_warm.F90 (LKOGAN = .FALSE.). */
+static void ice4_warm(const Tctx *x, PointRates *pr)
+{
+  const C *c = x->c;
+  const double t = x->t, rho = x->rhodref;
+  double *b = pr->bu;
+  if (c->LWARM == 0.0) { b[B_RCAUTR] = b[B_RCACCR] = b[B_RREVAV] = 0.0; return; }
+  if (x->hl[2] > c->C_RTMIN && x->hl[0] > 0.0 && x->ldcompute) {
+    if (!x->ldsoft) b[B_RCAUTR] = c->TIMAUTC * dmax(x->hl[2] - x->hl[0] * c->CRIAUTC / rho, 0.0);
+  } else b[B_RCAUTR] = 0.0;
+  if ((int)c->SUBG_RC_RR_ACCR == 0) {
+    if (x->v[IRC] > c->C_RTMIN && x->v[IRR] > c->R_RTMIN && x->ldcompute) {
+      if (!x->ldsoft)
+        b[B_RCACCR] = c->FCACCR * x->v[IRC] * 1.0 /* PACRF */ * pow(x->lbdar, c->EXCACCR) * pow(rho, -c->CEXVT);
+    } else b[B_RCACCR] = 0.0;
+  } else {
+    const int m = x->v[IRC] > c->C_RTMIN && x->v[IRR] > c->R_RTMIN && x->ldcompute;
+    const int m1 = m && x->hl[2] > c->C_RTMIN && x->hl[0] > 0.0;
+    const int m2 = m && x->hl[3] > c->C_RTMIN && x->hl[1] > 1.e-20;
+    if (m1 || m2) {
+      if (!x->ldsoft) {
+        double r = 0.0;
+        if (m1) r = c->FCACCR * x->hl[2] * pow(x->lbdar_rf, c->EXCACCR) * pow(rho, -c->CEXVT);
+        if (m2)
+          r += c->FCACCR * (x->hl[3] / x->hl[1]) * pow(x->lbdar_rf, c->EXCACCR) * pow(rho, -c->CEXVT) *
+               (dmin(x->cf, x->rainfr) - x->hl[0]);
+        b[B_RCACCR] = r;
+      }
+    } else b[B_RCACCR] = 0.0;
+  }
+  const int evap = (int)c->SUBG_RR_EVAP;
+  if (evap == 0) {
+    if (x->v[IRR] > c->R_RTMIN && x->v[IRC] <= c->C_RTMIN && x->ldcompute) {
+      if (!x->ldsoft) {
+        double r = esatw(c, t);
+        const double usw = 1. - x->v[IRV] * (x->pres - r) / (c->EPSILO * r);
+        r = sq(c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / (pr->ka * c->RV * sq(t)) + (c->RV * t) / (pr->dv * r);
+        b[B_RREVAV] = (dmax(0., usw) / (rho * r)) *
+                      (c->O0EVAR * pow(x->lbdar, c->EX0EVAR) + c->O1EVAR * pr->cj * pow(x->lbdar, c->EX1EVAR));
+      }
+    } else b[B_RREVAV] = 0.0;
+  } else {
+    const double zw4 = (evap == 1) ? 1.0 : x->rainfr;
+    const double zw3 = (evap == 1) ? x->lbdar : x->lbdar_rf;
+    if (x->v[IRR] > c->R_RTMIN && zw4 > x->cf && x->ldcompute) {
+      if (!x->ldsoft) {
+        const double tht = x->v[ITH];
+        const double thlt = tht - c->LVTT * tht / c->CPD / t * x->v[IRC];
+        const double zw2 = thlt * t / tht;
+        double r = esatw(c, zw2);
+        const double usw = 1.0 - x->v[IRV] * (x->pres - r) / (c->EPSILO * r);
+        r = sq(c->LVTT + (c->CPV - c->CL) * (zw2 - c->TT)) / (pr->ka * c->RV * sq(zw2)) + (c->RV * zw2) / (pr->dv * r);
+        r = dmax(0., usw) / (rho * r) * (c->O0EVAR * pow(zw3, c->EX0EVAR) + c->O1EVAR * pr->cj * pow(zw3, c->EX1EVAR));
+        b[B_RREVAV] = r * (zw4 - x->cf);
+      }
+    } else b[B_RREVAV] = 0.0;
+  }
+}
+
+/* Vapour/heat term shared by the freezing-rate and melting computations of
+ * fast_rs/fast_rg (mode_ice4_fast_rs.F90 IFREEZ1 / RSMLTG, fast_rg IFREEZ1 / RGMLTR). */
+static inline double heat_term(const C *c, double ka, double dv, double t, double rv, double pres, int ice)
+{
+  double e = rv * pres / (c->EPSILO + rv);
+  if (c->LEVLIMIT != 0.0) e = dmin(e, ice ? esati(c, t) : esatw(c, t));
+  return ka * (c->TT - t) + (dv * (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) * (c->ESTT - e) / (c->RV * t));
+}
+
+/* ICE4_FAST_RS, micro/mode_ice4_fast_rs.F90 (LNEWCOEFF = LOCND2 = .FALSE.). */
+static void ice4_fast_rs(const Tctx *x, PointRates *pr)
+{
+  const C *c = x->c;
+  const Ice3gbLuts *lut = x->lut;
+  const double t = x->t, rho = x->rhodref, lbdas = x->lbdas, lbdar = x->lbdar;
+  double *b = pr->bu, *rs = pr->rs_tend;
+  double freez;
+  if (x->v[IRS] > c->S_RTMIN && x->ldcompute) {                       /* :100-142 */
+    if (!x->ldsoft) {
+      double f1 = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 1);
+      f1 = f1 * (c->O0DEPS * pow(lbdas, c->EX0DEPS) + c->O1DEPS * pr->cj * pow(lbdas, c->EX1DEPS)) /
+           (rho * (c->LMTT - c->CL * (c->TT - t)));
+      rs[RS_FREEZ1] = f1;
+      rs[RS_FREEZ2] = (rho * (c->LMTT + (c->CI - c->CL) * (c->TT - t))) / (rho * (c->LMTT - c->CL * (c->TT - t)));
+    }
+    freez = dmax(0., dmax(0., rs[RS_FREEZ1] + rs[RS_FREEZ2] * b[B_RIAGGS]) - b[B_RIAGGS]);
+  } else {
+    rs[RS_FREEZ1] = rs[RS_FREEZ2] = 0.0;
+    freez = 0.0;
+  }
+  /* riming: :149-274 */
+  const int grim = x->v[IRC] > c->C_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute;
+  if (!grim) rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
+  if (!x->ldsoft && grim) {
+    int i;
+    const double fr = lut_index(lbdas, (int)c->NGAMINC, c->RIMINTP1, c->RIMINTP2, &i);
+    const double zw1 = lut1d(lut->gaminc_rim1, i, fr);
+    const double zw2 = lut1d(lut->gaminc_rim2, i, fr);
+    const double zw3 = lut1d(lut->gaminc_rim4, i, fr);
+    rs[RS_RCRIMSS] = c->CRIMSS * zw1 * x->v[IRC] * 1.0 /* PCOLF */ * pow(lbdas, c->EXCRIMSS) * pow(rho, -c->CEXVT);
+    rs[RS_RCRIMS] = c->CRIMSG * x->v[IRC] * 1.0 * pow(lbdas, c->EXCRIMSG) * pow(rho, -c->CEXVT);
+    if ((int)c->SNOW_RIMING == 0) { /* M90 */
+      const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
+      double r = c->SRIMCG * pow(lbdas, c->EXSRIMCG) * (1.0 - zw2);
+      r = zzw * r / dmax(1.e-20, c->SRIMCG3 * c->SRIMCG2 * pow(lbdas, c->EXSRIMCG2) * (1. - zw3) - c->SRIMCG3 * r);
+      rs[RS_RSRIMCG] = r;
+    } else rs[RS_RSRIMCG] = 0.0;
+  }
+  if (grim && t < c->TT) {
+    b[B_RCRIMSS] = dmin(freez, rs[RS_RCRIMSS]);
+    freez = dmax(0., freez - b[B_RCRIMSS]);
+    const double zzw0 = dmin(1., freez / dmax(1.e-20, rs[RS_RCRIMS] - b[B_RCRIMSS]));
+    b[B_RCRIMSG] = zzw0 * dmax(0., rs[RS_RCRIMS] - b[B_RCRIMSS]);
+    freez = dmax(0., freez - b[B_RCRIMSG]);
+    b[B_RSRIMCG] = zzw0 * rs[RS_RSRIMCG];
+    b[B_RSRIMCG] *= signbit(b[B_RCRIMSG]) ? 0.0 : 1.0;  /* MAX(0., -SIGN(1., -PRCRIMSG)) */
+    b[B_RCRIMSG] = dmax(0., b[B_RCRIMSG]);
+  } else {
+    b[B_RCRIMSS] = b[B_RCRIMSG] = b[B_RSRIMCG] = 0.0;
+  }
+  /* accretion of rain on snow: :281-388 */
+  const int gacc = x->v[IRR] > c->R_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute;
+  if (!gacc) rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
+  if (!x->ldsoft) {
+    rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
+    if (gacc) {
+      int i1, i2;
+      const double f1 = lut_index(lbdas, (int)c->NACCLBDAS, c->ACCINTP1S, c->ACCINTP2S, &i1);
+      const double f2 = lut_index(lbdar, (int)c->NACCLBDAR, c->ACCINTP1R, c->ACCINTP2R, &i2);
+      const double zw1 = lut2d(lut->ker_raccss, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
+      const double zw2 = lut2d(lut->ker_raccs, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
+      const double zw3 = lut2d(lut->ker_saccrg, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
+      const double zzw = c->FRACCSS * pow(lbdas, c->CXS) * pow(rho, -c->CEXVT - 1.) *
+                         (c->LBRACCS1 / sq(lbdas) + c->LBRACCS2 / (lbdas * lbdar) + c->LBRACCS3 / sq(lbdar)) /
+                         sq(sq(lbdar));
+      rs[RS_RRACCSS] = zw1 * zzw;
+      rs[RS_RRACCS] = zw2 * zzw;
+      rs[RS_RSACCRG] = c->FSACCRG * zw3 * pow(lbdas, c->CXS - c->BS) * pow(rho, -c->CEXVT - 1.) *
+                       (c->LBSACCR1 / sq(lbdar) + c->LBSACCR2 / (lbdar * lbdas) + c->LBSACCR3 / sq(lbdas)) / lbdar;
+    }
+  }
+  if (gacc && t < c->TT) {
+    b[B_RRACCSS] = dmin(freez, rs[RS_RRACCSS]);
+    freez = dmax(0., freez - b[B_RRACCSS]);
+    const double zzw = dmin(1., freez / dmax(1.e-20, rs[RS_RRACCS] - b[B_RRACCSS]));
+    b[B_RRACCSG] = zzw * dmax(0., rs[RS_RRACCS] - b[B_RRACCSS]);
+    freez = dmax(0., freez - b[B_RRACCSG]);
+    b[B_RSACCRG] = zzw * rs[RS_RSACCRG];
+    b[B_RSACCRG] *= signbit(b[B_RRACCSG]) ? 0.0 : 1.0;
+    b[B_RRACCSG] = dmax(0., b[B_RRACCSG]);
+  } else {
+    b[B_RRACCSS] = b[B_RRACCSG] = b[B_RSACCRG] = 0.0;
+  }
+  /* conversion-melting of snow: :396-441 */
+  if (x->v[IRS] > c->S_RTMIN && t > c->TT && x->ldcompute) {
+    if (!x->ldsoft) {
+      double r = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 0);
+      r = c->FSCVMG * dmax(0., (-r * (c->O0DEPS * pow(lbdas, c->EX0DEPS) + c->O1DEPS * pr->cj * pow(lbdas, c->EX1DEPS)) -
+                                 (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c->CL * (c->TT - t))) /
+                                (rho * c->LMTT));
+      b[B_RSMLTG] = r;
+      b[B_RCMLTSR] = rs[RS_RCRIMS];
+    }
+  } else {
+    b[B_RSMLTG] = b[B_RCMLTSR] = 0.0;
+  }
+}
+
+/* ICE4_FAST_RG, micro/mode_ice4_fast_rg.F90 (KRR = 6, LOCND2 = LNEWCOEFF = .FALSE.). */
+static void ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
+{
+  const C *c = x->c;
+  const Ice3gbLuts *lut = x->lut;
+  const double t = x->t, rho = x->rhodref, lbdar = x->lbdar, lbdas = x->lbdas, lbdag = x->lbdag;
+  double *b = pr->bu, *rg = pr->rg_tend;
+  /* rain contact freezing: :~100-176 */
+  if (x->v[IRI] > c->I_RTMIN && x->v[IRR] > c->R_RTMIN && x->ldcompute) {
+    if (!x->ldsoft) {
+      b[B_RICFRRG] = c->ICFRR * x->v[IRI] * pow(lbdar, c->EXICFRR) * pow(rho, -c->CEXVT);
+      b[B_RRCFRIG] = c->RCFRI * cit * pow(lbdar, c->EXRCFRI) * pow(rho, -c->CEXVT - 1.);
+      if (c->LCRFLIMIT != 0.0) {
+        const double zw = dmax(0., dmin(1., (b[B_RICFRRG] * c->CI + b[B_RRCFRIG] * c->CL) * (c->TT - t) /
+                                               dmax(1.e-20, c->LVTT * b[B_RRCFRIG])));
+        b[B_RRCFRIG] = zw * b[B_RRCFRIG];
+        b[B_RICFRR] = (1. - zw) * b[B_RICFRRG];
+        b[B_RICFRRG] = zw * b[B_RICFRRG];
+      } else b[B_RICFRR] = 0.0;
+    }
+  } else {
+    b[B_RICFRRG] = b[B_RRCFRIG] = b[B_RICFRR] = 0.0;
+  }
+  /* cloud/pristine collection: :182-~200 */
+  if (x->v[IRG] > c->G_RTMIN && x->v[IRC] > c->C_RTMIN && x->ldcompute) {
+    if (!x->ldsoft)
+      rg[RG_RCDRYG] = c->FCDRYG * x->v[IRC] * (pow(lbdag, c->CXG - c->DG - 2.) * pow(rho, -c->CEXVT));
+  } else rg[RG_RCDRYG] = 0.0;
+  if (x->v[IRG] > c->G_RTMIN && x->v[IRI] > c->I_RTMIN && x->ldcompute) {
+    if (!x->ldsoft) {
+      const double base = pow(lbdag, c->CXG - c->DG - 2.) * pow(rho, -c->CEXVT);
+      rg[RG_RIDRYG] = c->FIDRYG * exp(c->COLEXIG * (t - c->TT)) * x->v[IRI] * base;
+      rg[RG_RIWETG] = rg[RG_RIDRYG] / (c->COLIG * exp(c->COLEXIG * (t - c->TT)));
+    }
+  } else rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
+  /* snow collection (SDRYG LUT): :203-235 */
+  const int gdry_s = x->v[IRS] > c->S_RTMIN && x->v[IRG] > c->G_RTMIN && x->ldcompute;
+  if (!gdry_s) rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
+  if (!x->ldsoft && gdry_s) {
+    int i1, i2;
+    const double f1 = lut_index(lbdag, (int)c->NDRYLBDAG, c->DRYINTP1G, c->DRYINTP2G, &i1);
+    const double f2 = lut_index(lbdas, (int)c->NDRYLBDAS, c->DRYINTP1S, c->DRYINTP2S, &i2);
+    const double zw = lut2d(lut->ker_sdryg, ICE3GB_NDRYLBDAS, i1, f1, i2, f2);
+    rg[RG_RSWETG] = c->FSDRYG * zw / c->COLSG * pow(lbdas, c->CXS - c->BS) * pow(lbdag, c->CXG) *
+                    pow(rho, -c->CEXVT - 1.) *
+                    (c->LBSDRYG1 / sq(lbdag) + c->LBSDRYG2 / (lbdag * lbdas) + c->LBSDRYG3 / sq(lbdas));
+    rg[RG_RSDRYG] = rg[RG_RSWETG] * c->COLSG * exp(c->COLEXSG * (t - c->TT));
+  }
+  /* rain collection (RDRYG LUT): :241-271 */
+  const int gdry_r = x->v[IRR] > c->R_RTMIN && x->v[IRG] > c->G_RTMIN && x->ldcompute;
+  if (!gdry_r) rg[RG_RRDRYG] = 0.0;
+  if (!x->ldsoft && gdry_r) {
+    int i1, i2;
+    const double f1 = lut_index(lbdag, (int)c->NDRYLBDAG, c->DRYINTP1G, c->DRYINTP2G, &i1);
+    const double f2 = lut_index(lbdar, (int)c->NDRYLBDAR, c->DRYINTP1R, c->DRYINTP2R, &i2);
+    const double zw = lut2d(lut->ker_rdryg, ICE3GB_NDRYLBDAR, i1, f1, i2, f2);
+    rg[RG_RRDRYG] = c->FRDRYG * zw / sq(sq(lbdar)) * pow(lbdag, c->CXG) * pow(rho, -c->CEXVT - 1.) *
+                    (c->LBRDRYG1 / sq(lbdag) + c->LBRDRYG2 / (lbdag * lbdar) + c->LBRDRYG3 / sq(lbdar));
+  }
+  const double rdryg_init = rg[RG_RCDRYG] + rg[RG_RIDRYG] + rg[RG_RSDRYG] + rg[RG_RRDRYG];
+  /* wet/dry growth selection: :275-338 */
+  double rwetg_init = 0.0;
+  int ldwetg = 0, lldryg = 0;
+  if (x->v[IRG] > c->G_RTMIN && x->ldcompute) {
+    if (!x->ldsoft) {
+      double f1 = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 1);
+      f1 = f1 * (c->O0DEPG * pow(lbdag, c->EX0DEPG) + c->O1DEPG * pr->cj * pow(lbdag, c->EX1DEPG)) /
+           (rho * (c->LMTT - c->CL * (c->TT - t)));
+      rg[RG_FREEZ1] = f1;
+      rg[RG_FREEZ2] = (rho * (c->LMTT + (c->CI - c->CL) * (c->TT - t))) / (rho * (c->LMTT - c->CL * (c->TT - t)));
+    }
+    const double is = rg[RG_RIWETG] + rg[RG_RSWETG];
+    rwetg_init = dmax(is, dmax(0., rg[RG_FREEZ1] + rg[RG_FREEZ2] * is));
+    const double wet = dmax(0., rwetg_init - rg[RG_RIWETG] - rg[RG_RSWETG]);
+    const double dry = dmax(0., rdryg_init - rg[RG_RIDRYG] - rg[RG_RSDRYG]);
+    ldwetg = wet <= dry;
+    if (c->LNULLWETG != 0.0) ldwetg = ldwetg && rdryg_init > 0.;
+    else ldwetg = ldwetg && rwetg_init > 0.;
+    if (c->LWETGPOST == 0.0) ldwetg = ldwetg && t < c->TT;
+    lldryg = t < c->TT && rdryg_init > 1.e-20 && wet > dry;
+  } else {
+    rg[RG_FREEZ1] = rg[RG_FREEZ2] = 0.0;
+  }
+  if (ldwetg) {
+    b[B_RRWETG] = -(rg[RG_RIWETG] + rg[RG_RSWETG] + rg[RG_RCDRYG] - rwetg_init);
+    b[B_RCWETG] = rg[RG_RCDRYG];
+    b[B_RIWETG] = rg[RG_RIWETG];
+    b[B_RSWETG] = rg[RG_RSWETG];
+  } else {
+    b[B_RRWETG] = b[B_RCWETG] = b[B_RIWETG] = b[B_RSWETG] = 0.0;
+  }
+  if (lldryg) {
+    b[B_RCDRYG] = rg[RG_RCDRYG];
+    b[B_RRDRYG] = rg[RG_RRDRYG];
+    b[B_RIDRYG] = rg[RG_RIDRYG];
+    b[B_RSDRYG] = rg[RG_RSDRYG];
+  } else {
+    b[B_RCDRYG] = b[B_RRDRYG] = b[B_RIDRYG] = b[B_RSDRYG] = 0.0;
+  }
+  /* graupel melting: :390-410 */
+  if (x->v[IRG] > c->G_RTMIN && t > c->TT && x->ldcompute) {
+    if (!x->ldsoft) {
+      double r = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 0);
+      r = dmax(0., (-r * (c->O0DEPG * pow(lbdag, c->EX0DEPG) + c->O1DEPG * pr->cj * pow(lbdag, c->EX1DEPG)) -
+                    (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c->CL * (c->TT - t))) /
+                       (rho * c->LMTT));
+      b[B_RGMLTR] = r;
+    }
+  } else b[B_RGMLTR] = 0.0;
+}
+
+/* ICE4_FAST_RI, micro/mode_ice4_fast_ri.F90. */
+static void ice4_fast_ri(const Tctx *x, PointRates *pr, double cit)
+{
+  const C *c = x->c;
+  double *b = pr->bu;
+  if (pr->ssi > 0. && x->v[IRC] > c->C_RTMIN && x->v[IRI] > c->I_RTMIN && cit > 1.e-20 && x->ldcompute) {
+    if (!x->ldsoft) {
+      double l = dmin(1.e8, c->LBI * pow(x->rhodref * x->v[IRI] / cit, c->LBEXI));
+      b[B_RCBERI] = (pr->ssi / (x->rhodref * pr->ai)) * cit *
+                    (c->O0DEPI / l + c->O2DEPI * pr->cj * pr->cj / pow(l, c->DI + 2.0));
+    }
+  } else b[B_RCBERI] = 0.0;
+}
+
+/* Slope parameters, mode_ice4_tendencies.F90:389-433 (LSNOW_T optional). */
+static void ice4_slopes(Tctx *x)
+{
+  const C *c = x->c;
+  const double rho = x->rhodref;
+  x->lbdar = (x->v[IRR] > 0.) ? c->LBR * pow(rho * dmax(x->v[IRR], c->R_RTMIN), c->LBEXR) : 0.0;
+  const int llrfr = (int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2;
+  if (llrfr)
+    x->lbdar_rf = (x->v[IRR] > 0. && x->rainfr > 0.)
+                      ? c->LBR * pow(rho * dmax(x->v[IRR] / x->rainfr, c->R_RTMIN), c->LBEXR) : 0.0;
+  else
+    x->lbdar_rf = x->lbdar;
+  if (c->LSNOW_T != 0.0) {
+    if (x->v[IRS] > 0. && x->t > 263.15)
+      x->lbdas = dmax(dmin(c->LBDAS_MAX, pow(10.0, 14.554 - 0.0423 * x->t)), c->LBDAS_MIN) * c->TRANS_MP_GAMMAS;
+    else if (x->v[IRS] > 0. && x->t <= 263.15)
+      x->lbdas = dmax(dmin(c->LBDAS_MAX, pow(10.0, 6.226 - 0.0106 * x->t)), c->LBDAS_MIN) * c->TRANS_MP_GAMMAS;
+    else x->lbdas = 0.0;
+  } else {
+    x->lbdas = (x->v[IRS] > 0.) ? dmin(c->LBDAS_MAX, c->LBS * pow(rho * dmax(x->v[IRS], c->S_RTMIN), c->LBEXS)) : 0.0;
+  }
+  x->lbdag = (x->v[IRG] > 0.) ? c->LBG * pow(rho * dmax(x->v[IRG], c->G_RTMIN), c->LBEXG) : 0.0;
+}
+
+/* ICE4_TENDENCIES (mode_ice4_tendencies.F90:150-717) for one point.
+ * `vart` is the state at the start of the pass (PVART), `t` = th*exn.
+ * Outputs A (rates) and B (instantaneous increments). */
+static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int ldcompute,
+                            double exn, double rhodref, double lvfact, double lsfact, double pres,
+                            double cf, double sigma_rc, double *cit, double t, const double vart[NV],
+                            PointRates *pr, double *rainfr, double hl[4], double hi[4],
+                            double A[NV], double B[NV])
+{
+  Tctx x;
+  x.c = c; x.lut = lut; x.ldsoft = ldsoft; x.ldcompute = ldcompute;
+  x.rhodref = rhodref; x.pres = pres; x.exn = exn; x.lvfact = lvfact; x.lsfact = lsfact;
+  x.cf = cf; x.sigma_rc = sigma_rc; x.t = t; x.rainfr = *rainfr;
+  for (int v = 0; v < NV; ++v) { x.v[v] = vart[v]; A[v] = 0.0; B[v] = 0.0; }
+  for (int k = 0; k < 4; ++k) { x.hl[k] = hl[k]; x.hi[k] = hi[k]; }
+  double *b = pr->bu;
+  if (ldsoft) {
+    b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = b[B_RSRIMCG_MR] = 0.0;
+  } else {
+    /* :171-183 nucleation */
+    ice4_nucleation(c, ldcompute, x.v[ITH], pres, rhodref, exn, lsfact, x.t, x.v[IRV], cit, &b[B_RVHENI_MR], NULL);
+    x.v[ITH] += b[B_RVHENI_MR] * lsfact;
+    x.t = x.v[ITH] * exn;
+    x.v[IRV] -= b[B_RVHENI_MR];
+    x.v[IRI] += b[B_RVHENI_MR];
+    /* :188-201 rrhong */
+    b[B_RRHONG_MR] = ice4_rrhong(c, ldcompute, exn, lvfact, lsfact, x.t, x.v[IRR], x.v[ITH]);
+    x.v[ITH] += b[B_RRHONG_MR] * (lsfact - lvfact);
+    x.t = x.v[ITH] * exn;
+    x.v[IRR] -= b[B_RRHONG_MR];
+    x.v[IRG] += b[B_RRHONG_MR];
+    /* :206-219 rimltc */
+    b[B_RIMLTC_MR] = ice4_rimltc(c, ldcompute, exn, lvfact, lsfact, x.t, x.v[ITH], x.v[IRI]);
+    x.v[ITH] -= b[B_RIMLTC_MR] * (lsfact - lvfact);
+    x.t = x.v[ITH] * exn;
+    x.v[IRC] += b[B_RIMLTC_MR];
+    x.v[IRI] -= b[B_RIMLTC_MR];
+    b[B_RSRIMCG_MR] = 0.0;
+    /* :270-295 */
+    B[ITH] += b[B_RVHENI_MR] * lsfact;
+    B[ITH] += b[B_RRHONG_MR] * (lsfact - lvfact);
+    B[ITH] -= b[B_RIMLTC_MR] * (lsfact - lvfact);
+    B[IRV] -= b[B_RVHENI_MR];
+    B[IRC] += b[B_RIMLTC_MR];
+    B[IRR] -= b[B_RRHONG_MR];
+    B[IRI] += b[B_RVHENI_MR];
+    B[IRI] -= b[B_RIMLTC_MR];
+    B[IRS] -= b[B_RSRIMCG_MR];
+    B[IRG] += b[B_RRHONG_MR];
+    B[IRG] += b[B_RSRIMCG_MR];
+    /* :303-320 derived fields */
+    ice4_derived(c, x.t, rhodref, pres, x.v[IRV], &pr->ssi, &pr->ka, &pr->dv, &pr->ai, &pr->cj);
+  }
+  /* :352 compute_pdf */
+  x.rainfr = *rainfr;
+  double zrainfr = ice4_compute_pdf(c, ldcompute, rhodref, x.v[IRC], x.v[IRI], cf, x.t, sigma_rc, x.hl, x.hi);
+  const int llrfr = (int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2;
+  if (llrfr) {                                                        /* :357-380 */
+    x.rainfr = dmax(x.rainfr, zrainfr);
+    const int mask = x.v[IRR] > c->R_RTMIN || x.v[IRS] > c->S_RTMIN || x.v[IRG] > c->G_RTMIN;
+    if (mask && x.rainfr == 0.) x.rainfr = 1.;
+  } else {
+    x.rainfr = 1.;
+  }
+  ice4_slopes(&x);
+  ice4_slow(&x, pr);
+  ice4_warm(&x, pr);
+  ice4_fast_rs(&x, pr);
+  ice4_fast_rg(&x, pr, *cit);
+  ice4_fast_ri(&x, pr, *cit);
+  /* :606-717 aggregation (KRR = 6, LOCND2 = .FALSE.) */
+  const double lsv = lsfact - lvfact;
+  A[ITH] += b[B_RVDEPG] * lsfact;
+  A[ITH] += b[B_RCHONI] * lsv;
+  A[ITH] += b[B_RVDEPS] * lsfact;
+  A[ITH] -= b[B_RREVAV] * lvfact;
+  A[ITH] += b[B_RCRIMSS] * lsv;
+  A[ITH] += b[B_RCRIMSG] * lsv;
+  A[ITH] += b[B_RRACCSS] * lsv;
+  A[ITH] += b[B_RRACCSG] * lsv;
+  A[ITH] += (b[B_RRCFRIG] - b[B_RICFRR]) * lsv;
+  A[ITH] += (b[B_RCWETG] + b[B_RRWETG]) * lsv;
+  A[ITH] += (b[B_RCDRYG] + b[B_RRDRYG]) * lsv;
+  A[ITH] -= b[B_RGMLTR] * lsv;
+  A[ITH] += b[B_RCBERI] * lsv;
+  A[IRV] -= b[B_RVDEPG];
+  A[IRV] -= b[B_RVDEPS];
+  A[IRV] += b[B_RREVAV];
+  A[IRC] -= b[B_RCHONI];
+  A[IRC] -= b[B_RCAUTR];
+  A[IRC] -= b[B_RCACCR];
+  A[IRC] -= b[B_RCRIMSS];
+  A[IRC] -= b[B_RCRIMSG];
+  A[IRC] -= b[B_RCMLTSR];
+  A[IRC] -= b[B_RCWETG];
+  A[IRC] -= b[B_RCDRYG];
+  A[IRC] -= b[B_RCBERI];
+  A[IRR] += b[B_RCAUTR];
+  A[IRR] += b[B_RCACCR];
+  A[IRR] -= b[B_RREVAV];
+  A[IRR] -= b[B_RRACCSS];
+  A[IRR] -= b[B_RRACCSG];
+  A[IRR] += b[B_RCMLTSR];
+  A[IRR] = A[IRR] - b[B_RRCFRIG] + b[B_RICFRR];
+  A[IRR] -= b[B_RRWETG];
+  A[IRR] -= b[B_RRDRYG];
+  A[IRR] += b[B_RGMLTR];
+  A[IRI] += b[B_RCHONI];
+  A[IRI] -= b[B_RIAGGS];
+  A[IRI] -= b[B_RIAUTS];
+  A[IRI] = A[IRI] - b[B_RICFRRG] - b[B_RICFRR];
+  A[IRI] -= b[B_RIWETG];
+  A[IRI] -= b[B_RIDRYG];
+  A[IRI] += b[B_RCBERI];
+  A[IRS] += b[B_RVDEPS];
+  A[IRS] += b[B_RIAGGS];
+  A[IRS] += b[B_RIAUTS];
+  A[IRS] += b[B_RCRIMSS];
+  A[IRS] -= b[B_RSRIMCG];
+  A[IRS] += b[B_RRACCSS];
+  A[IRS] -= b[B_RSACCRG];
+  A[IRS] -= b[B_RSMLTG];
+  A[IRS] -= b[B_RSWETG];
+  A[IRS] -= b[B_RSDRYG];
+  A[IRG] += b[B_RVDEPG];                 /* * ZNODEPG_S = 1 */
+  A[IRG] += b[B_RCRIMSG] + b[B_RSRIMCG];
+  A[IRG] += b[B_RRACCSG] + b[B_RSACCRG];
+  A[IRG] += b[B_RSMLTG];
+  A[IRG] += b[B_RICFRRG] + b[B_RRCFRIG];
+  A[IRG] += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
+  A[IRG] += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
+  A[IRG] -= b[B_RGMLTR];
+  *rainfr = x.rainfr;
+  for (int k = 0; k < 4; ++k) { hl[k] = x.hl[k]; hi[k] = x.hi[k]; }
+}
+
+/* ICE4_STEPPING (mode_ice4_stepping.F90:139-518) restated for one packed
+ * point (every packed point is a micro point).  Points of one Fortran call
+ * march in lock-step through the same passes; a point only contributes in
+ * its own active passes, so its trajectory is the per-point loop below.  The
+ * only cross-point coupling kept is PRREVAV = ZBU_INST(:,IRREVAV) after the
+ * last pass of the whole call (:514-516), reproduced through `last_key`.
+ * Idle passes move a finished point by at most MNH_TINY seconds of its
+ * external tendency; that sub-1e-15 relative drift is not reproduced. */
+typedef struct {
+  double vart[NV];
+  double extpk[NV];
+  double cit, rainfr, rrevav;
+  int outer, inner, capped;
+} StepOut;
+
+static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
+                                double exn, double rhodref, double pres, double cf, double sigma_rc,
+                                double hlc_hcf, double hlc_hrc, double hli_hcf, double hli_hri,
+                                StepOut *s)
+{
+  const double rsmin[NV] = {0.0, c->V_RTMIN, c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN};
+  const double inv_dt = 1.0 / dt;
+  PointRates pr;
+  memset(&pr, 0, sizeof(pr));
+  double hl[4] = {hlc_hcf, 0.0, hlc_hrc, 0.0}, hi[4] = {hli_hcf, 0.0, hli_hri, 0.0};
+  /* :151-158 external tendencies */
+  for (int v = 0; v < NV; ++v) s->extpk[v] = s->extpk[v] - s->vart[v] * inv_dt;
+  if ((int)c->SUBG_AUCV_RC == 2 || (int)c->SUBG_AUCV_RI == 2) {     /* :170-189 */
+    hl[3] = s->vart[IRC] - hlc_hrc;
+    hi[3] = s->vart[IRI] - hli_hri;
+    hl[1] = (s->vart[IRC] > 0.) ? cf - hlc_hcf : 0.;
+    hi[1] = (s->vart[IRI] > 0.) ? cf - hli_hcf : 0.;
+  }
+  double ztime = 0.0;
+  int passes = 0;
+  s->outer = 0; s->inner = 0; s->capped = 0; s->rrevav = 0.0;
+  while (ztime < dt) {                                                /* :204 */
+    s->outer++;
+    int llcompute = 1, lsoft = 0, inner = 0;
+    while (llcompute) {                                               /* :227 */
+      if (passes >= max_passes) { s->capped = 1; goto done; }
+      passes++;
+      inner++;
+      const double zsum2 = s->vart[IRI] + s->vart[IRS] + s->vart[IRG];
+      const double zdev = (c->CPD + c->CPV * s->vart[IRV] + c->CL * (s->vart[IRC] + s->vart[IRR]) + c->CI * zsum2) * exn;
+      const double zzt = s->vart[ITH] * exn;
+      const double lsfact = (c->LSTT + (c->CPV - c->CI) * (zzt - c->TT)) / zdev;
+      const double lvfact = (c->LVTT + (c->CPV - c->CL) * (zzt - c->TT)) / zdev;
+      double A[NV], B[NV];
+      ice4_tendencies(c, lut, lsoft, 1, exn, rhodref, lvfact, lsfact, pres, cf, sigma_rc, &s->cit, zzt,
+                      s->vart, &pr, &s->rainfr, hl, hi, A, B);
+      for (int v = 0; v < NV; ++v) A[v] += s->extpk[v];             /* :265-272 */
+      double maxtime = dt - ztime;                                    /* :275-282 */
+      if (c->LFEEDBACKT != 0.0) {                                     /* :284-299 */
+        const double zx = c->TT / exn;
+        if ((s->vart[ITH] - zx) * (s->vart[ITH] + B[ITH] - zx) < 0.) maxtime = 0.;
+        if (fabs(A[ITH]) > 1.e-20) {
+          const double thr = (zx - B[ITH] - s->vart[ITH]) / A[ITH];
+          if (thr > 0.) maxtime = dmin(maxtime, thr);
+        }
+      }
+      for (int v = 1; v < NV; ++v) {                                  /* :302-311 */
+        if (A[v] < -1.e-20 && s->vart[v] > rsmin[v]) {
+          maxtime = dmin(maxtime, -(B[v] + s->vart[v]) / A[v]);
+          maxtime = dmax(maxtime, c->MNH_TINY);
+        }
+      }
+      if (ztime + maxtime >= dt) llcompute = 0;                       /* :314-319 */
+      for (int v = 0; v < NV; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
+      if (s->vart[IRI] <= 0.) s->cit = 0.;                            /* :398-401 */
+      ztime += maxtime;
+      s->rrevav = pr.bu[B_RREVAV];
+      lsoft = 1;
+    }
+    s->inner = inner;
+  }
+done:
+  for (int v = 0; v < NV; ++v) s->vart[v] = s->vart[v] - s->extpk[v] * dt;  /* :503-511 */
+}
+
+/* ===================================================================== */
+/* RAIN_ICE (micro/rain_ice.F90)                                          */
+/* ===================================================================== */
+
+static int rain_ice_supported(const C *c)
+{
+  if ((int)c->NRR != 6) return 0;
+  if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0) return 0;
+  if ((int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0) return 0;  /* PRFR/CLFR paths: see below */
+  return 1;
+}
+
+EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
+                          const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
+                          uint32_t *status_bits)
+{
+  if (!c || !lut || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
+  if (!rain_ice_supported(c)) return ICE3GB_ERR_UNSUPPORTED;
+  const long n = (long)nij * nk;
+  const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (c->LSEDIM_AFTER != 0.0);
+  const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (c->LDEPOSC != 0.0);
+  const int max_passes = (opt && opt->max_passes > 0) ? opt->max_passes : 256;
+  const int sed_fortran = !(opt && opt->sed_jax > 0);
+  C cc = *c;
+  if (opt && opt->lfeedbackt >= 0) cc.LFEEDBACKT = opt->lfeedbackt ? 1.0 : 0.0;
+  c = &cc;
+  const int has_st = f->sea != NULL && f->town != NULL;
+  double *lsf = (double *)malloc(sizeof(double) * n);
+  double *lvf = (double *)malloc(sizeof(double) * n);
+  double *rvheni = (double *)malloc(sizeof(double) * n);
+  int64_t *key = (int64_t *)malloc(sizeof(int64_t) * n);
+  if (!lsf || !lvf || !rvheni || !key) { free(lsf); free(lvf); free(rvheni); free(key); return ICE3GB_ERR_RANGE; }
+  int capped_any = 0;
+
+  /* 2. sedimentation before the microphysics (rain_ice.F90:442-462 -> ICE4_SEDIMENTATION) */
+  if (!lsedim_after) {
+#pragma omp parallel for schedule(static)
+    for (long col = 0; col < nij; ++col) {
+      double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
+      double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
+      double inpr[5];
+      sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht,
+                 f->sea ? f->sea[col] : 0.0, f->town ? f->town[col] : 0.0, has_st, src, fpr, inpr);
+      f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
+      f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+    }
+  }
+
+  /* 1., 3., 4., 5. pointwise part */
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : capped_any)
+  for (long p = 0; p < n; ++p) {
+    const double exn = f->exn[p], rho = f->rhodref[p], pres = f->pabs[p];
+    const double th = f->tht[p], rv = f->rvt[p], rc = f->rct[p], rr = f->rrt[p];
+    const double ri = f->rit[p], rs = f->rst[p], rg = f->rgt[p];
+    /* :334-345 lsfact/lvfact without exner */
+    const double zrice = ri + rs + rg;
+    const double zdev = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * zrice;
+    const double t = th * exn;
+    lsf[p] = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
+    lvf[p] = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
+    /* :370-381 LLMICRO */
+    const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN || rg > c->G_RTMIN;
+    if (c->LWARM != 0.0) f->evap3d[p] = 0.0;
+    f->rainfr[p] = 1.0;  /* :599-605 (no PRFR option) */
+    double cit = f->cit[p];
+    double zrvheni = 0.0;
+    if (!micro) {
+      /* :506-529 nucleation outside LLMICRO points */
+      cit = 0.0;
+      ice4_nucleation(c, 1, th, pres, rho, exn, lsf[p] / exn, t, rv, &cit, &zrvheni, NULL);
+    }
+    /* :535-539 */
+    zrvheni = dmin(f->rvs[p], zrvheni / dt);
+    rvheni[p] = zrvheni;
+    key[p] = -1;
+    if (micro) {
+      /* ICE4_PACK + ICE4_STEPPING (mode_ice4_pack.F90:230-330) */
+      StepOut s;
+      s.vart[ITH] = th; s.vart[IRV] = rv; s.vart[IRC] = rc; s.vart[IRR] = rr;
+      s.vart[IRI] = ri; s.vart[IRS] = rs; s.vart[IRG] = rg;
+      s.extpk[ITH] = f->ths[p]; s.extpk[IRV] = f->rvs[p]; s.extpk[IRC] = f->rcs[p]; s.extpk[IRR] = f->rrs[p];
+      s.extpk[IRI] = f->ris[p]; s.extpk[IRS] = f->rss[p]; s.extpk[IRG] = f->rgs[p];
+      s.cit = cit;
+      s.rainfr = 1.0;
+      const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
+      const double sigma_rc = sigm ? 2.0 * f->sigs[p] : 0.0;  /* pack :266 + stepping :160-166 */
+      ice4_stepping_point(c, lut, dt, max_passes, exn, rho, pres, f->cldfr[p], sigma_rc,
+                          f->hlc_hcf[p], f->hlc_hrc[p], f->hli_hcf[p], f->hli_hri[p], &s);
+      cit = s.cit;
+      if (c->LWARM != 0.0) f->evap3d[p] = s.rrevav;
+      f->rainfr[p] = s.rainfr;
+      capped_any |= s.capped;
+      key[p] = ((int64_t)s.outer << 32) | (int64_t)s.inner;
+      /* 8.1 total tendencies (rain_ice.F90:758-790, disabled in the vendored copy) */
+      const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
+      const double inv = 1.0 / dt;
+      const double wv = (s.vart[IRV] - rv) * inv, wc = (s.vart[IRC] - rc) * inv;
+      const double wr = (s.vart[IRR] - rr) * inv, wi = (s.vart[IRI] - ri) * inv;
+      const double ws = (s.vart[IRS] - rs) * inv, wg = (s.vart[IRG] - rg) * inv;
+      const double wth = (wc + wr) * lvx + (wi + ws + wg) * lsx;
+      f->ths[p] += wth + zrvheni * lsx;
+      f->rvs[p] += wv - zrvheni;
+      f->rcs[p] += wc;
+      f->rrs[p] += wr;
+      f->ris[p] += wi + zrvheni;
+      f->rss[p] += ws;
+      f->rgs[p] += wg;
+    } else {
+      const double lsx = lsf[p] / f->exnref[p];
+      f->ths[p] += zrvheni * lsx;
+      f->rvs[p] -= zrvheni;
+      f->ris[p] += zrvheni;
+    }
+    f->cit[p] = cit;
+  }
+  /* PRREVAV after the last pass of the call (mode_ice4_stepping.F90:514-516) */
+  if (c->LWARM != 0.0) {
+    int64_t kmax = -1;
+    for (long p = 0; p < n; ++p) if (key[p] > kmax) kmax = key[p];
+#pragma omp parallel for schedule(static)
+    for (long p = 0; p < n; ++p)
+      if (key[p] >= 0 && key[p] != kmax) f->evap3d[p] = 0.0;
+  }
+  /* 8.2 negativity correction on the sources (ICE4_CORRECT_NEGATIVITIES) */
+#pragma omp parallel for schedule(static)
+  for (long p = 0; p < n; ++p) {
+    const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
+    double rv = f->rvs[p], rc = f->rcs[p], rr = f->rrs[p], ri = f->ris[p], rs = f->rss[p], rg = f->rgs[p];
+    double th = f->ths[p], w;
+    w = rc - dmax(rc, 0.); rv += w; th -= w * lvx; rc -= w;
+    w = rr - dmax(rr, 0.); rv += w; th -= w * lvx; rr -= w;
+    w = ri - dmax(ri, 0.); rv += w; th -= w * lsx; ri -= w;
+    w = rs - dmax(rs, 0.); rv += w; th -= w * lsx; rs -= w;
+    w = rg - dmax(rg, 0.); rv += w; th -= w * lsx; rg -= w;
+    w = dmin(1., dmax(c->V_RTMIN - rv, 0.) / dmax(rc + ri, 1.e-20));
+    th -= w * (rc * lvx + ri * lsx);
+    rv += w * (rc + ri);
+    rc = (1. - w) * rc;
+    ri = (1. - w) * ri;
+    w = dmin(dmax(rr, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rr -= w; th -= w * lvx;
+    w = dmin(dmax(rs, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rs -= w; th -= w * lsx;
+    w = dmin(dmax(rg, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rg -= w; th -= w * lsx;
+    f->rvs[p] = rv; f->rcs[p] = rc; f->rrs[p] = rr; f->ris[p] = ri; f->rss[p] = rs; f->rgs[p] = rg;
+    f->ths[p] = th;
+  }
+  /* 9. sedimentation after (rain_ice.F90:816-841) */
+  if (lsedim_after) {
+#pragma omp parallel for schedule(static)
+    for (long col = 0; col < nij; ++col) {
+      double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
+      double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
+      double inpr[5];
+      sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht,
+                 f->sea ? f->sea[col] : 0.0, f->town ? f->town[col] : 0.0, has_st, src, fpr, inpr);
+      f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
+      f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+    }
+  }
+  /* 10. fog deposition (rain_ice.F90:876-895), level k = 0 */
+  for (long col = 0; col < nij; ++col) {
+    if (ldeposc) {
+      const double indep = c->VDEPOSC * f->rct[col] * f->rhodref[col] / c->RHOLW;
+      f->rcs[col] -= c->VDEPOSC * f->rct[col] / f->dzz[col];
+      f->inprc[col] += indep;
+      if (f->indep) f->indep[col] = indep;
+    } else if (f->indep) {
+      f->indep[col] = 0.0;
+    }
+  }
+  free(lsf); free(lvf); free(rvheni); free(key);
+  if (status_bits) *status_bits = capped_any ? ICE3GB_DEV_PASS_CAP : 0u;
+  return ICE3GB_OK;
+}
+
+/* ===================================================================== */
+/* Per-process entry points (hard pass) used by the golden-vector tests  */
+/* ===================================================================== */
+
+EXPORT void ice3o_nucleation(const C *c, long n, const double *tht, const double *pabst, const double *rhodref,
+                             const double *exn, const double *lsfact, const double *t, const double *rvt,
+                             const uint8_t *ldcompute, double *cit, double *rvheni_mr)
+{
+  for (long p = 0; p < n; ++p)
+    ice4_nucleation(c, ldcompute[p], tht[p], pabst[p], rhodref[p], exn[p], lsfact[p], t[p], rvt[p], &cit[p],
+                    &rvheni_mr[p], NULL);
+}
+
+EXPORT void ice3o_rrhong_rimltc(const C *c, long n, const double *t, const double *exn, const double *lvfact,
+                                const double *lsfact, const double *tht, const double *rrt, const double *rit,
+                                const uint8_t *ldcompute, double *rrhong, double *rimltc)
+{
+  for (long p = 0; p < n; ++p) {
+    rrhong[p] = ice4_rrhong(c, ldcompute[p], exn[p], lvfact[p], lsfact[p], t[p], rrt[p], tht[p]);
+    rimltc[p] = ice4_rimltc(c, ldcompute[p], exn[p], lvfact[p], lsfact[p], t[p], tht[p], rit[p]);
+  }
+}
+
+EXPORT void ice3o_derived_slopes(const C *c, long n, const double *t, const double *rhodref, const double *pres,
+                                 const double *rv, const double *rr, const double *rs, const double *rg,
+                                 double *out /* [9][n]: ssi ka dv ai cj lbdar lbdar_rf lbdas lbdag */)
+{
+  for (long p = 0; p < n; ++p) {
+    ice4_derived(c, t[p], rhodref[p], pres[p], rv[p], &out[p], &out[n + p], &out[2 * n + p], &out[3 * n + p],
+                 &out[4 * n + p]);
+    Tctx x;
+    memset(&x, 0, sizeof(x));
+    x.c = c; x.rhodref = rhodref[p]; x.t = t[p];
+    x.v[IRR] = rr[p]; x.v[IRS] = rs[p]; x.v[IRG] = rg[p];
+    ice4_slopes(&x);
+    out[5 * n + p] = x.lbdar; out[6 * n + p] = x.lbdar_rf; out[7 * n + p] = x.lbdas; out[8 * n + p] = x.lbdag;
+  }
+}
+
+EXPORT void ice3o_compute_pdf(const C *c, long n, const uint8_t *ldmicro, const double *rhodref, const double *rct,
+                              const double *rit, const double *cf, const double *t, const double *sigma_rc,
+                              double *out /* [9][n]: hlc_hcf hlc_lcf hlc_hrc hlc_lrc hli_hcf hli_lcf hli_hri hli_lri rf */)
+{
+  for (long p = 0; p < n; ++p) {
+    double hl[4] = {0, 0, 0, 0}, hi[4] = {0, 0, 0, 0};
+    const double rf = ice4_compute_pdf(c, ldmicro[p], rhodref[p], rct[p], rit[p], cf[p], t[p], sigma_rc[p], hl, hi);
+    for (int k = 0; k < 4; ++k) { out[k * n + p] = hl[k]; out[(4 + k) * n + p] = hi[k]; }
+    out[8 * n + p] = rf;
+  }
+}
+
+/* Hard-pass rates of the slow/warm/fast processes for given inputs.
+ * in: [17][n] = t rhodref pres rv rc rr ri rs rg cit ssi ka dv ai cj hlc_hcf hlc_hrc
+ *     (+ hli_hcf hli_hri at rows 17, 18)
+ * out: [NBU][n] budget rates, plus rs_tend [8][n] and rg_tend [8][n]. */
+EXPORT int ice3o_process_rates(const C *c, const Ice3gbLuts *lut, long n, const double *in, const uint8_t *ldcompute,
+                               double *out_bu, double *out_rs, double *out_rg)
+{
+  for (long p = 0; p < n; ++p) {
+    Tctx x;
+    PointRates pr;
+    memset(&x, 0, sizeof(x));
+    memset(&pr, 0, sizeof(pr));
+    x.c = c; x.lut = lut; x.ldsoft = 0; x.ldcompute = ldcompute[p];
+    x.t = in[p]; x.rhodref = in[n + p]; x.pres = in[2 * n + p];
+    x.v[IRV] = in[3 * n + p]; x.v[IRC] = in[4 * n + p]; x.v[IRR] = in[5 * n + p];
+    x.v[IRI] = in[6 * n + p]; x.v[IRS] = in[7 * n + p]; x.v[IRG] = in[8 * n + p];
+    const double cit = in[9 * n + p];
+    pr.ssi = in[10 * n + p]; pr.ka = in[11 * n + p]; pr.dv = in[12 * n + p]; pr.ai = in[13 * n + p];
+    pr.cj = in[14 * n + p];
+    x.hl[0] = in[15 * n + p]; x.hl[2] = in[16 * n + p];
+    x.hi[0] = in[17 * n + p]; x.hi[2] = in[18 * n + p];
+    x.cf = 1.0; x.rainfr = 1.0;
+    x.v[ITH] = x.t;  /* only used by the CLFR/PRFR evaporation, exn = 1 here */
+    ice4_slopes(&x);
+    ice4_slow(&x, &pr);
+    ice4_warm(&x, &pr);
+    ice4_fast_rs(&x, &pr);
+    ice4_fast_rg(&x, &pr, cit);
+    ice4_fast_ri(&x, &pr, cit);
+    for (int k = 0; k < NBU; ++k) out_bu[k * n + p] = pr.bu[k];
+    for (int k = 0; k < NRS; ++k) out_rs[k * n + p] = pr.rs_tend[k];
+    for (int k = 0; k < NRG; ++k) out_rg[k * n + p] = pr.rg_tend[k];
+  }
+  return NBU;
+}
+
+/* ICE4_RAINFR_VERT (micro/mode_ice4_rainfr_vert.F90; stencils/rain_ice.py:272-320). */
+EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
+                              const double *rg)
+{
+  for (long col = 0; col < nij; ++col) {
+    prfr[(long)(nk - 1) * nij + col] = 0.0;
+    for (int k = nk - 2; k >= 0; --k) {
+      const long p = (long)k * nij + col;
+      const int mask = rr[p] > c->R_RTMIN || rs[p] > c->S_RTMIN || rg[p] > c->G_RTMIN;
+      if (mask) {
+        prfr[p] = dmax(prfr[p], prfr[p + nij]);
+        if (prfr[p] == 0.) prfr[p] = 1.;
+      } else {
+        prfr[p] = 0.;
+      }
+    }
+  }
+}
+
+EXPORT int ice3o_budget_count(void) { return NBU; }

@@ -1,0 +1,231 @@
+"""ctypes wrapper of the CPU oracle (oracle/ice3_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by the CPU-baseline leg of bench.py, always as the checker.  The product
+never imports this module.
+
+Arrays are numpy float64, [nk, nij] C-contiguous (= the ABI's [nk][nij]).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from typing import Dict, Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REPO = os.path.dirname(_HERE)
+_PKG = os.path.join(_REPO, "dwarf-p-ice3_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+
+from ice3gb._abi import IceAdjustFields, RainIceFields, RainIceOptions, SedimentationFields  # noqa: E402
+from ice3gb.constants import ConstantsTable, Ice3gbConstants, Ice3gbLuts  # noqa: E402
+
+LIB_PATH = os.path.join(_HERE, "_build", "libice3_oracle.so")
+_lib = None
+
+IA_IN = ("sigqsat", "pabs", "sigs", "th", "exn", "exn_ref", "rho_dry_ref", "rv", "rc", "ri", "rr", "rs", "rg",
+         "cf_mf", "rc_mf", "ri_mf")
+IA_INOUT = ("rvs", "rcs", "ris", "ths")
+IA_OUT = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls")
+# order of the reference's 16-tuple (src/ice3/jax/stencils/ice_adjust.py:381-398)
+IA_RESULT = IA_OUT + IA_INOUT
+
+NBU_NAMES = ("rvheni_mr", "rrhong_mr", "rimltc_mr", "rsrimcg_mr", "rchoni", "rvdeps", "riaggs", "riauts",
+             "rvdepg", "rcautr", "rcaccr", "rrevav", "rcrimss", "rcrimsg", "rsrimcg", "rraccss", "rraccsg",
+             "rsaccrg", "rsmltg", "rcmltsr", "ricfrrg", "rrcfrig", "ricfrr", "rcwetg", "riwetg", "rrwetg",
+             "rswetg", "rcdryg", "ridryg", "rrdryg", "rsdryg", "rgmltr", "rcberi")
+RS_NAMES = ("rcrims", "rcrimss", "rsrimcg", "rraccs", "rraccss", "rsaccrg", "freez1", "freez2")
+RG_NAMES = ("rcdryg", "ridryg", "riwetg", "rsdryg", "rswetg", "rrdryg", "freez1", "freez2")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(_HERE, "ice3_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.ice3o_budget_count.restype = ctypes.c_int
+        assert _lib.ice3o_budget_count() == len(NBU_NAMES)
+    return _lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def ice_adjust(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float) -> Dict[str, np.ndarray]:
+    """Oracle ice_adjust; returns the 16 outputs keyed by name."""
+    lib = load()
+    ins = {k: _f64(st[k]) for k in IA_IN}
+    nk, nij = ins["pabs"].shape
+    io = {k: _f64(st[k]).copy() for k in IA_INOUT}
+    out = {k: np.empty((nk, nij)) for k in IA_OUT}
+    f = IceAdjustFields()
+    for k, v in {**ins, **io, **out}.items():
+        setattr(f, k, _ptr(v))
+    f.sigqsat_3d = 1 if ins["sigqsat"].ndim == 2 else 0
+    rc = lib.ice3o_ice_adjust(ctypes.byref(table.consts), nij, nk, ctypes.c_double(dt), ctypes.byref(f))
+    if rc != 0:
+        raise RuntimeError(f"oracle ice_adjust returned {rc}")
+    return {**out, **io}
+
+
+def sedimentation(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, fortran: bool,
+                  with_fpr: bool = False) -> Dict[str, np.ndarray]:
+    lib = load()
+    rho = _f64(st["rhodref"])
+    nk, nij = rho.shape
+    f = SedimentationFields()
+    keep = {}
+    for k in ("rhodref", "dzz", "pabs", "tht"):
+        keep[k] = _f64(st[k])
+        setattr(f, k, _ptr(keep[k]))
+    for k in ("sea", "town"):
+        if st.get(k) is not None:
+            keep[k] = _f64(st[k])
+            setattr(f, k, _ptr(keep[k]))
+    out = {}
+    for k in ("rcs", "rrs", "ris", "rss", "rgs"):
+        out[k] = _f64(st[k]).copy()
+        setattr(f, k, _ptr(out[k]))
+    for k in ("inprc", "inprr", "inpri", "inprs", "inprg"):
+        out[k] = np.empty(nij)
+        setattr(f, k, _ptr(out[k]))
+    if with_fpr:
+        for k in ("fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g"):
+            out[k] = np.empty((nk, nij))
+            setattr(f, k, _ptr(out[k]))
+    f.fortran_semantics = 1 if fortran else 0
+    rc = lib.ice3o_sedimentation(ctypes.byref(table.consts), nij, nk, ctypes.c_double(dt), ctypes.byref(f))
+    if rc != 0:
+        raise RuntimeError(f"oracle sedimentation returned {rc}")
+    return out
+
+
+RI_IN = ("exn", "dzz", "rhodref", "exnref", "pabs", "cldfr", "sigs", "tht", "rvt", "rct", "rrt", "rit", "rst",
+         "rgt")
+RI_INOUT = ("cit", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs")
+RI_OUT3 = ("evap3d", "rainfr")
+RI_OUT2 = ("inprc", "inprr", "inpri", "inprs", "inprg", "indep")
+
+
+def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim_after: int = -1,
+             ldeposc: int = -1, lfeedbackt: int = -1, max_passes: int = 0, sed_jax: int = 0,
+             with_fpr: bool = False):
+    """Oracle rain_ice on ABI-named fields; returns (outputs dict, status bits)."""
+    lib = load()
+    keep = {k: _f64(st[k]) for k in RI_IN}
+    nk, nij = keep["exn"].shape
+    f = RainIceFields()
+    for k, v in keep.items():
+        setattr(f, k, _ptr(v))
+    for k in ("sea", "town"):
+        if st.get(k) is not None:
+            keep[k] = _f64(st[k])
+            setattr(f, k, _ptr(keep[k]))
+    out = {k: _f64(st[k]).copy() for k in RI_INOUT}
+    out.update({k: np.empty((nk, nij)) for k in RI_OUT3})
+    out.update({k: np.empty(nij) for k in RI_OUT2})
+    if with_fpr:
+        out.update({k: np.empty((nk, nij)) for k in ("fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")})
+    for k, v in out.items():
+        setattr(f, k, _ptr(v))
+    opt = RainIceOptions(lsedim_after, ldeposc, lfeedbackt, max_passes, sed_jax)
+    bits = ctypes.c_uint32(0)
+    lib.ice3o_rain_ice.argtypes = [ctypes.POINTER(Ice3gbConstants), ctypes.POINTER(Ice3gbLuts), ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_double, ctypes.POINTER(RainIceOptions),
+                                   ctypes.POINTER(RainIceFields), ctypes.POINTER(ctypes.c_uint32)]
+    rc = lib.ice3o_rain_ice(ctypes.byref(table.consts), ctypes.byref(table.luts), nij, nk, dt, ctypes.byref(opt),
+                            ctypes.byref(f), ctypes.byref(bits))
+    if rc != 0:
+        raise RuntimeError(f"oracle rain_ice returned {rc}")
+    return out, bits.value
+
+
+# ---- per-process entry points (hard pass) --------------------------------
+
+def nucleation(table, tht, pabst, rhodref, exn, lsfact, t, rvt, cit, ldcompute):
+    lib = load()
+    a = [_f64(x).ravel() for x in (tht, pabst, rhodref, exn, lsfact, t, rvt)]
+    cit = _f64(cit).ravel().copy()
+    ld = np.ascontiguousarray(np.asarray(ldcompute, dtype=np.uint8).ravel())
+    out = np.empty_like(cit)
+    lib.ice3o_nucleation(ctypes.byref(table.consts), ctypes.c_long(cit.size), *[_ptr(x) for x in a],
+                         ld.ctypes.data_as(ctypes.c_void_p), _ptr(cit), _ptr(out))
+    return cit, out
+
+
+def rrhong_rimltc(table, t, exn, lvfact, lsfact, tht, rrt, rit, ldcompute):
+    lib = load()
+    a = [_f64(x).ravel() for x in (t, exn, lvfact, lsfact, tht, rrt, rit)]
+    ld = np.ascontiguousarray(np.asarray(ldcompute, dtype=np.uint8).ravel())
+    o1, o2 = np.empty(a[0].size), np.empty(a[0].size)
+    lib.ice3o_rrhong_rimltc(ctypes.byref(table.consts), ctypes.c_long(o1.size), *[_ptr(x) for x in a],
+                            ld.ctypes.data_as(ctypes.c_void_p), _ptr(o1), _ptr(o2))
+    return o1, o2
+
+
+def derived_slopes(table, t, rhodref, pres, rv, rr, rs, rg):
+    lib = load()
+    a = [_f64(x).ravel() for x in (t, rhodref, pres, rv, rr, rs, rg)]
+    n = a[0].size
+    out = np.empty((9, n))
+    lib.ice3o_derived_slopes(ctypes.byref(table.consts), ctypes.c_long(n), *[_ptr(x) for x in a], _ptr(out))
+    return dict(zip(("ssi", "ka", "dv", "ai", "cj", "lbdar", "lbdar_rf", "lbdas", "lbdag"), out))
+
+
+def compute_pdf(table, ldmicro, rhodref, rct, rit, cf, t, sigma_rc):
+    lib = load()
+    a = [_f64(x).ravel() for x in (rhodref, rct, rit, cf, t, sigma_rc)]
+    ld = np.ascontiguousarray(np.asarray(ldmicro, dtype=np.uint8).ravel())
+    n = a[0].size
+    out = np.empty((9, n))
+    lib.ice3o_compute_pdf(ctypes.byref(table.consts), ctypes.c_long(n), ld.ctypes.data_as(ctypes.c_void_p),
+                          *[_ptr(x) for x in a], _ptr(out))
+    return dict(zip(("hlc_hcf", "hlc_lcf", "hlc_hrc", "hlc_lrc", "hli_hcf", "hli_lcf", "hli_hri", "hli_lri", "rf"),
+                    out))
+
+
+def process_rates(table, inputs: Dict[str, np.ndarray], ldcompute):
+    """Hard-pass process rates; inputs keys: t rhodref pres rv rc rr ri rs rg cit ssi ka dv ai cj
+    hlc_hcf hlc_hrc hli_hcf hli_hri."""
+    lib = load()
+    keys = ("t", "rhodref", "pres", "rv", "rc", "rr", "ri", "rs", "rg", "cit", "ssi", "ka", "dv", "ai", "cj",
+            "hlc_hcf", "hlc_hrc", "hli_hcf", "hli_hri")
+    n = np.asarray(inputs["t"]).size
+    inp = np.ascontiguousarray(np.stack([_f64(inputs[k]).ravel() for k in keys]))
+    ld = np.ascontiguousarray(np.asarray(ldcompute, dtype=np.uint8).ravel())
+    bu, rs, rg = np.empty((len(NBU_NAMES), n)), np.empty((len(RS_NAMES), n)), np.empty((len(RG_NAMES), n))
+    lib.ice3o_process_rates(ctypes.byref(table.consts), ctypes.byref(table.luts), ctypes.c_long(n), _ptr(inp),
+                            ld.ctypes.data_as(ctypes.c_void_p), _ptr(bu), _ptr(rs), _ptr(rg))
+    res = dict(zip(NBU_NAMES, bu))
+    res.update({"rs_" + k: v for k, v in zip(RS_NAMES, rs)})
+    res.update({"rg_" + k: v for k, v in zip(RG_NAMES, rg)})
+    return res
+
+
+def rainfr_vert(table, prfr, rr, rs, rg):
+    lib = load()
+    prfr = _f64(prfr).copy()
+    nk, nij = prfr.shape
+    a = [_f64(x) for x in (rr, rs, rg)]
+    lib.ice3o_rainfr_vert(ctypes.byref(table.consts), nij, nk, _ptr(prfr), *[_ptr(x) for x in a])
+    return prfr

@@ -1,0 +1,231 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference code.
+
+Runs maurinl26/dwarf-p-ice3's own JAX implementation, unmodified, in float64
+through the numpy stand-in of refshim.py:
+
+* ``IceAdjustJAX.__call__``            (src/ice3/jax/ice_adjust.py:139)
+* ``sedimentation_stat``               (src/ice3/jax/stencils/sedimentation.py:58)
+* the ICE4 process stencils            (src/ice3/jax/stencils/ice4_*.py), hard pass
+* ``ice4_derived_fields`` / ``ice4_slope_parameters`` (stencils/ice4_tendencies.py:191,248)
+* ``ice4_rainfr_vert``                 (stencils/rain_ice.py:272)
+
+Inputs are seeded synthetic states (ice3gb.state.make_state) and seeded
+random point sets; both inputs and reference outputs are stored.
+
+Usage:  python tests/golden/make_golden.py [--reference-src DIR]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "dwarf-p-ice3_gb300"))
+sys.path.insert(0, HERE)
+
+DT = 50.0
+
+
+def _shim(a):
+    import refshim
+    return np.asarray(a, dtype=np.float64).view(refshim.ShimArray)
+
+
+def _np(st):
+    return {k: v.numpy().copy() for k, v in st.items()}
+
+
+def ice_adjust_cases(IceAdjustJAX, Phyex):
+    from ice3gb.state import make_state
+
+    ia = IceAdjustJAX(Phyex("AROME", TSTEP=DT), jit=False)
+    cases = {}
+    # config-0 distribution (AROME, CB02, sigqsat = 0.02), 32 columns x 90 levels
+    st = _np(make_state(32, 90, seed=0))
+    cases["ia_std"] = st
+    # mass-flux and source terms active, varying sigqsat (incl. zeros), NRR=6
+    st2 = _np(make_state(24, 90, seed=1, precip=True))
+    rng = np.random.default_rng(11)
+    shape = st2["pabs"].shape
+    st2["sigqsat"] = np.where(rng.random(shape) < 0.2, 0.0, rng.uniform(0.0, 0.05, shape))
+    st2["cf_mf"] = np.where(rng.random(shape) < 0.5, rng.uniform(0, 1, shape), 0.0)
+    st2["rc_mf"] = np.where(rng.random(shape) < 0.5, 10 ** rng.uniform(-8, -3, shape), 0.0)
+    st2["ri_mf"] = np.where(rng.random(shape) < 0.5, 10 ** rng.uniform(-8, -3, shape), 0.0)
+    st2["rvs"] = rng.uniform(-1e-6, 1e-5, shape)
+    st2["rcs"] = rng.uniform(-1e-7, 1e-6, shape)
+    st2["ris"] = rng.uniform(-1e-7, 1e-6, shape)
+    st2["ths"] = rng.uniform(-1e-3, 1e-3, shape)
+    cases["ia_mf"] = st2
+    out = {}
+    names = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv",
+             "ls", "rvs", "rcs", "ris", "ths")
+    for cname, st in cases.items():
+        nk, nij = st["pabs"].shape
+        sigq = st["sigqsat"] if st["sigqsat"].ndim == 2 else np.broadcast_to(st["sigqsat"], (nk, nij)).copy()
+        res = ia(sigqsat=sigq, pabs=st["pabs"], sigs=st["sigs"], th=st["th"], exn=st["exn"],
+                 exn_ref=st["exn_ref"], rho_dry_ref=st["rho_dry_ref"], rv=st["rv"], rc=st["rc"], ri=st["ri"],
+                 rr=st["rr"], rs=st["rs"], rg=st["rg"], cf_mf=st["cf_mf"], rc_mf=st["rc_mf"],
+                 ri_mf=st["ri_mf"], rvs=st["rvs"], rcs=st["rcs"], ris=st["ris"], ths=st["ths"], timestep=DT)
+        rec = {f"in_{k}": np.asarray(v) for k, v in st.items() if k in (
+            "sigqsat", "pabs", "sigs", "th", "exn", "exn_ref", "rho_dry_ref", "rv", "rc", "ri", "rr", "rs",
+            "rg", "cf_mf", "rc_mf", "ri_mf", "rvs", "rcs", "ris", "ths")}
+        rec.update({f"out_{n}": np.asarray(r, dtype=np.float64) for n, r in zip(names, res)})
+        out[cname] = rec
+    return out
+
+
+def sedimentation_case(sedimentation_stat, Phyex):
+    from ice3gb.state import make_state
+
+    ext = dict(Phyex("AROME", TSTEP=DT).to_externals())
+    ext.update(LBC_LAND=ext["LBC_1"], LBC_SEA=ext["LBC_2"], FSEDC_LAND=ext["FSEDC_1"], FSEDC_SEA=ext["FSEDC_2"])
+    st = _np(make_state(24, 90, seed=2, precip=True))
+    rng = np.random.default_rng(22)
+    nk, nij = st["pabs"].shape
+    # sources = mixing ratio / dt with a few negative sources
+    src = {}
+    for k, r in (("rcs", "rc"), ("rrs", "rr"), ("ris", "ri"), ("rss", "rs"), ("rgs", "rg")):
+        src[k] = st[r] / DT
+    src["ris"] = np.where(rng.random((nk, nij)) < 0.3, 10 ** rng.uniform(-8, -4, (nk, nij)) / DT, src["ris"])
+    src["rcs"][0, :3] = -1e-9
+    sea = rng.uniform(0, 1, nij)
+    town = rng.uniform(0, 0.5, nij)
+    T = lambda a: np.ascontiguousarray(a.T[None, :, :])
+    res = sedimentation_stat(T(st["rho_dry_ref"]), T(st["dzz"]), T(st["pabs"]), T(st["th"]), T(src["rcs"]),
+                             T(src["rrs"]), T(src["ris"]), T(src["rss"]), T(src["rgs"]), sea[None, :, None],
+                             town[None, :, None], ext)
+    names = ("rcs", "rrs", "ris", "rss", "rgs", "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g", "inprc", "inprr",
+             "inpri", "inprs", "inprg")
+    rec = {"in_rhodref": st["rho_dry_ref"], "in_dzz": st["dzz"], "in_pabs": st["pabs"], "in_tht": st["th"],
+           "in_sea": sea, "in_town": town}
+    rec.update({f"in_{k}": v for k, v in src.items()})
+    for n, r in zip(names, res):
+        r = np.asarray(r, dtype=np.float64)
+        rec[f"out_{n}"] = r[0].T.copy() if r.ndim == 3 else r[0].copy()
+    return {"sed_jax": rec}
+
+
+def process_cases(mods, Phyex):
+    """Hard-pass ICE4 processes on seeded random points."""
+    ext = dict(Phyex("AROME", TSTEP=DT).to_externals())
+    rng = np.random.default_rng(33)
+    n = 768
+
+    def mix(lo=-8, hi=-2, pzero=0.3):
+        v = 10 ** rng.uniform(lo, hi, n)
+        return np.where(rng.random(n) < pzero, 0.0, v)
+
+    t = rng.uniform(215.0, 300.0, n)
+    pres = rng.uniform(2e4, 1.02e5, n)
+    rhodref = pres / (287.06 * t)
+    exn = (pres / 1e5) ** (287.06 / 1004.71)
+    tht = t / exn
+    rv = 10 ** rng.uniform(-6, -1.8, n)
+    rc, rr, ri, rs, rg = mix(), mix(), mix(), mix(), mix()
+    cit = np.where(rng.random(n) < 0.4, 0.0, 10 ** rng.uniform(2, 6, n))
+    ld = rng.random(n) < 0.9
+    lsfact = rng.uniform(2400, 3200, n)
+    lvfact = lsfact - rng.uniform(300, 400, n)
+    cf = np.where(rng.random(n) < 0.3, 0.0, rng.uniform(0, 1, n))
+    sigma_rc = rng.uniform(1e-7, 2e-4, n)
+    hlc_hcf, hlc_hrc = rng.uniform(0, 1, n), mix(-7, -2, 0.3)
+    hli_hcf, hli_hri = rng.uniform(0, 1, n), mix(-7, -2, 0.3)
+    inp = dict(t=t, pres=pres, rhodref=rhodref, exn=exn, tht=tht, rv=rv, rc=rc, rr=rr, ri=ri, rs=rs, rg=rg,
+               cit=cit, ld=ld.astype(np.float64), lsfact=lsfact, lvfact=lvfact, cf=cf, sigma_rc=sigma_rc,
+               hlc_hcf=hlc_hcf, hlc_hrc=hlc_hrc, hli_hcf=hli_hcf, hli_hri=hli_hri)
+    out = {}
+    m = mods
+    cit_new, rvheni, _ = m["nucl"].ice4_nucleation(tht, pres, rhodref, exn, lsfact, t, rv, cit, ld, True, ext)
+    out.update(nucl_cit=cit_new, nucl_rvheni=rvheni)
+    out["rrhong"] = m["rrhong"].ice4_rrhong(t, exn, lvfact, lsfact, tht, rr, ld, True, ext)
+    out["rimltc"] = m["rimltc"].ice4_rimltc(t, exn, lvfact, lsfact, tht, ri, ld, True, ext)
+    ssi, ka, dv, ai, cj = m["tend"].ice4_derived_fields(t, rhodref, pres, rv, ext)
+    out.update(ssi=ssi, ka=ka, dv=dv, ai=ai, cj=cj)
+    lbdar, lbdar_rf, lbdas, lbdag = m["tend"].ice4_slope_parameters(rhodref, t, rr, rs, rg, ext)
+    out.update(lbdar=lbdar, lbdar_rf=lbdar_rf, lbdas=lbdas, lbdag=lbdag)
+    # compute_pdf: reference enum 0=NONE 1=CLFR 2=ADJU 3=PDF (stencils/ice4_compute_pdf.py:42-44)
+    for tag, rc_mode, ri_mode in (("pdf_sigm", 3, 0), ("none", 0, 0), ("clfr", 1, 1)):
+        res = m["pdf"].ice4_compute_pdf(rhodref, rc, ri, cf, t, sigma_rc, ld, rc_mode, ri_mode, 0, ext)
+        for nm, r in zip(("hlc_hcf", "hlc_lcf", "hlc_hrc", "hlc_lrc", "hli_hcf", "hli_lcf", "hli_hri", "hli_lri",
+                          "rf"), res):
+            out[f"pdf_{tag}_{nm}"] = r
+    slow = m["slow"].ice4_slow(rhodref, t, ssi, rv, rc, ri, rs, rg, lbdas, lbdag, ai, cj, hli_hcf, hli_hri, ld,
+                               False, ext)
+    for nm, r in zip(("rchoni", "rvdeps", "riaggs", "riauts", "rvdepg"), slow):
+        out[nm] = r
+    warm = m["warm"].ice4_warm(rhodref, t, pres, tht, lbdar, lbdar_rf, ka, dv, cj, hlc_hcf, hlc_hrc, cf,
+                               np.ones(n), rv, rc, rr, ld, False, 0, ext)
+    for nm, r in zip(("rcautr", "rcaccr", "rrevav"), warm):
+        out[nm] = r
+    out["rcberi"] = m["ri"].ice4_fast_ri(rhodref, ai, cj, cit, ssi, rc, ri, ld, False, ext)
+    fr, f1, f2 = m["rs"].compute_freezing_rate(rhodref, pres, dv, ka, cj, lbdas, t, rv, rs, slow[2], ld, False,
+                                               True, ext)
+    out.update(rs_freez=fr, rs_freez1=f1, rs_freez2=f2)
+    # melting of snow with no riming/accretion inputs (rc = rr = 0 points only)
+    z = np.zeros(n)
+    out["rsmltg"], out["rcmltsr"] = m["rs"].conversion_melting_snow(rhodref, pres, dv, ka, cj, lbdas, t, rv, rs,
+                                                                     z, z, ld & (rc == 0) & (rr == 0), False,
+                                                                     True, ext)
+    a, b, c = m["rg"].rain_contact_freezing(rhodref, lbdar, t, ri, rr, cit, ld, False, True, ext)
+    out.update(ricfrrg=a, rrcfrig=b, ricfrr=c)
+    rcdryg, ridryg, riwetg = m["rg"].cloud_pristine_collection_graupel(rhodref, lbdag, t, rc, ri, rg, ld, False,
+                                                                      ext)
+    out.update(rg_rcdryg=rcdryg, rg_ridryg=ridryg, rg_riwetg=riwetg)
+    out["rgmltr"] = m["rg"].graupel_melting(rhodref, pres, dv, ka, cj, lbdag, t, rv, rg, rcdryg, z,
+                                            ld & (rr == 0), False, True, ext)
+    rec = {f"in_{k}": np.asarray(v, dtype=np.float64) for k, v in inp.items()}
+    rec.update({f"out_{k}": np.asarray(v, dtype=np.float64) for k, v in out.items()})
+    # rain fraction column sweep on a small grid (ng=1, nproma=16, nz=30)
+    nk, nij = 30, 16
+    prfr = rng.uniform(0, 1, (nk, nij)) * (rng.random((nk, nij)) < 0.5)
+    prfr[-1, :] = 0.0
+    r3 = [np.where(rng.random((nk, nij)) < 0.5, 0.0, 10 ** rng.uniform(-18, -12, (nk, nij))) for _ in range(3)]
+    T = lambda a: _shim(np.ascontiguousarray(a.T[None]))
+    res = m["ri_top"].ice4_rainfr_vert(T(prfr), T(r3[0]), T(r3[1]), T(r3[2]), ext)
+    rec.update(rf_in_prfr=prfr, rf_in_rr=r3[0], rf_in_rs=r3[1], rf_in_rg=r3[2],
+               rf_out_prfr=np.asarray(res)[0].T.copy())
+    return {"processes": rec}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference-src", default="/root/reference/src")
+    args = ap.parse_args()
+    import refshim
+
+    refshim.install()
+    sys.path.insert(0, args.reference_src)
+    np.seterr(all="ignore")
+    from ice3.jax.ice_adjust import IceAdjustJAX
+    from ice3.jax.stencils.sedimentation import sedimentation_stat
+    from ice3.phyex_common.phyex import Phyex
+    import ice3.jax.stencils.ice4_nucleation as nucl
+    import ice3.jax.stencils.ice4_rrhong as rrhong
+    import ice3.jax.stencils.ice4_rimltc as rimltc
+    import ice3.jax.stencils.ice4_tendencies as tend
+    import ice3.jax.stencils.ice4_compute_pdf as pdf
+    import ice3.jax.stencils.ice4_slow as slow
+    import ice3.jax.stencils.ice4_warm as warm
+    import ice3.jax.stencils.ice4_fast_ri as fri
+    import ice3.jax.stencils.ice4_fast_rs as frs
+    import ice3.jax.stencils.ice4_fast_rg as frg
+    import ice3.jax.stencils.rain_ice as ri_top
+
+    mods = dict(nucl=nucl, rrhong=rrhong, rimltc=rimltc, tend=tend, pdf=pdf, slow=slow, warm=warm, ri=fri,
+                rs=frs, rg=frg, ri_top=ri_top)
+    blobs = {}
+    blobs.update(ice_adjust_cases(IceAdjustJAX, Phyex))
+    blobs.update(sedimentation_case(sedimentation_stat, Phyex))
+    blobs.update(process_cases(mods, Phyex))
+    for name, rec in blobs.items():
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v, dtype=np.float64) for k, v in rec.items()})
+        print(f"wrote {path} ({os.path.getsize(path) / 1e3:.0f} kB)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,725 @@
+// abi.cu — extern "C" entry points of libice3gb.so (declared in include/ice3gb.h).
+//
+// Handle = one immutable constants table + its lookup tables on one device,
+// plus a sticky device status word.  Every rain_ice call takes its scratch
+// (work counter, pass keys) from the stream-ordered allocator on the caller's
+// stream, so concurrent calls on distinct streams share nothing but the
+// atomically updated status word.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ice3gb_device.cuh"
+#include "ice3gb_kernels.h"
+
+namespace {
+
+constexpr uint32_t kMagic = 0x1CE3B300u;
+constexpr long kMaxPoints = 1L << 40;
+
+struct Handle {
+  uint32_t magic;
+  Ice3gbConstants c;
+  double *d_luts;
+  unsigned int *d_status;
+  int device, num_sms;
+  bool rain_ice_ok;
+  std::string rain_ice_why;
+  // staging buffers of the _host entry points (grow-only)
+  double *d_stage;
+  size_t stage_cap;
+  std::mutex mu;
+  char err[512];
+  // per-kernel timing (ice3gb_profile_*)
+  bool profiling;
+  std::mutex prof_mu;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
+};
+
+enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_COUNT };
+const char *kKernelNames[K_COUNT] = {"ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup",
+                                     "fog_deposition"};
+
+// Brackets one launch with events when the handle is profiling.
+struct ProfScope {
+  Handle *h;
+  int id;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(Handle *h_, int id_, cudaStream_t s_) : h(h_), id(id_), s(s_)
+  {
+    if (h->profiling && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+      cudaEventRecord(a, s);
+  }
+  ~ProfScope()
+  {
+    if (a && b) {
+      cudaEventRecord(b, s);
+      std::lock_guard<std::mutex> lock(h->prof_mu);
+      h->events.push_back({id, {a, b}});
+    }
+  }
+};
+
+thread_local char g_err[512] = "";
+
+int fail(Handle *h, int code, const char *fmt, ...) __attribute__((format(printf, 3, 4)));
+int fail(Handle *h, int code, const char *fmt, ...)
+{
+  char *dst = h ? h->err : g_err;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(dst, 512, fmt, ap);
+  va_end(ap);
+  if (h) snprintf(g_err, sizeof(g_err), "%s", h->err);
+  return code;
+}
+
+int cuda_fail(Handle *h, cudaError_t e, const char *where)
+{
+  return fail(h, ICE3GB_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+Handle *as_handle(void *p)
+{
+  Handle *h = static_cast<Handle *>(p);
+  if (!h || h->magic != kMagic) return nullptr;
+  return h;
+}
+
+int check_device(Handle *h)
+{
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetDevice");
+  if (dev != h->device)
+    return fail(h, ICE3GB_ERR_HANDLE, "handle created on device %d, current device is %d", h->device, dev);
+  return ICE3GB_OK;
+}
+
+int check_shape(Handle *h, int nij, int nk)
+{
+  if (nij <= 0 || nk <= 0) return fail(h, ICE3GB_ERR_SHAPE, "nij=%d nk=%d must be positive", nij, nk);
+  if ((long)nij * nk > kMaxPoints) return fail(h, ICE3GB_ERR_SHAPE, "nij*nk too large");
+  return ICE3GB_OK;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+#define REQUIRE(ptr)                                                              \
+  do {                                                                            \
+    if (!(ptr)) return fail(h, ICE3GB_ERR_NULL, "required field %s is NULL", #ptr); \
+  } while (0)
+
+int validate_ice_adjust(Handle *h, const Ice3gbIceAdjustFields *f)
+{
+  if (!f) return fail(h, ICE3GB_ERR_NULL, "fields pointer is NULL");
+  REQUIRE(f->sigqsat); REQUIRE(f->pabs); REQUIRE(f->sigs); REQUIRE(f->th); REQUIRE(f->exn);
+  REQUIRE(f->exn_ref); REQUIRE(f->rho_dry_ref); REQUIRE(f->rv); REQUIRE(f->rc); REQUIRE(f->ri);
+  REQUIRE(f->rr); REQUIRE(f->rs); REQUIRE(f->rg); REQUIRE(f->cf_mf); REQUIRE(f->rc_mf); REQUIRE(f->ri_mf);
+  REQUIRE(f->rvs); REQUIRE(f->rcs); REQUIRE(f->ris); REQUIRE(f->ths);
+  REQUIRE(f->t); REQUIRE(f->rv_out); REQUIRE(f->rc_out); REQUIRE(f->ri_out); REQUIRE(f->cldfr);
+  REQUIRE(f->hlc_hrc); REQUIRE(f->hlc_hcf); REQUIRE(f->hli_hri); REQUIRE(f->hli_hcf);
+  REQUIRE(f->cph); REQUIRE(f->lv); REQUIRE(f->ls);
+  if (h->c.CONDENS != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "CONDENS=%g (only CB02=0)", h->c.CONDENS);
+  if (h->c.OCND2 != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 is not supported");
+  return ICE3GB_OK;
+}
+
+bool ia_vec2_ok(const Ice3gbIceAdjustFields *f, long n)
+{
+  if (n % 2) return false;
+  const void *ptrs[] = {f->pabs, f->sigs, f->th, f->exn, f->exn_ref, f->rho_dry_ref, f->rv, f->rc, f->ri, f->rr,
+                        f->rs, f->rg, f->cf_mf, f->rc_mf, f->ri_mf, f->rvs, f->rcs, f->ris, f->ths, f->t,
+                        f->rv_out, f->rc_out, f->ri_out, f->cldfr, f->hlc_hrc, f->hlc_hcf, f->hli_hri, f->hli_hcf,
+                        f->cph, f->lv, f->ls};
+  for (const void *p : ptrs)
+    if (!aligned16(p)) return false;
+  if (f->sigqsat_3d && !aligned16(f->sigqsat)) return false;
+  return true;
+}
+
+int validate_sed(Handle *h, const Ice3gbSedimentationFields *f)
+{
+  if (!f) return fail(h, ICE3GB_ERR_NULL, "fields pointer is NULL");
+  REQUIRE(f->rhodref); REQUIRE(f->dzz); REQUIRE(f->pabs); REQUIRE(f->tht);
+  REQUIRE(f->rcs); REQUIRE(f->rrs); REQUIRE(f->ris); REQUIRE(f->rss); REQUIRE(f->rgs);
+  REQUIRE(f->inprc); REQUIRE(f->inprr); REQUIRE(f->inpri); REQUIRE(f->inprs); REQUIRE(f->inprg);
+  if ((f->sea == nullptr) != (f->town == nullptr))
+    return fail(h, ICE3GB_ERR_NULL, "sea and town must be both given or both NULL");
+  return ICE3GB_OK;
+}
+
+int validate_rain_ice(Handle *h, const Ice3gbRainIceFields *f)
+{
+  if (!f) return fail(h, ICE3GB_ERR_NULL, "fields pointer is NULL");
+  REQUIRE(f->exn); REQUIRE(f->dzz); REQUIRE(f->rhodref); REQUIRE(f->exnref); REQUIRE(f->pabs);
+  REQUIRE(f->cldfr); REQUIRE(f->sigs); REQUIRE(f->tht); REQUIRE(f->rvt); REQUIRE(f->rct); REQUIRE(f->rrt);
+  REQUIRE(f->rit); REQUIRE(f->rst); REQUIRE(f->rgt); REQUIRE(f->cit);
+  REQUIRE(f->ths); REQUIRE(f->rvs); REQUIRE(f->rcs); REQUIRE(f->rrs); REQUIRE(f->ris); REQUIRE(f->rss);
+  REQUIRE(f->rgs); REQUIRE(f->evap3d); REQUIRE(f->rainfr);
+  REQUIRE(f->inprc); REQUIRE(f->inprr); REQUIRE(f->inpri); REQUIRE(f->inprs); REQUIRE(f->inprg);
+  if ((int)h->c.SUBG_AUCV_RC == 2 || (int)h->c.SUBG_AUCV_RI == 2) {
+    REQUIRE(f->hlc_hrc); REQUIRE(f->hlc_hcf); REQUIRE(f->hli_hri); REQUIRE(f->hli_hcf);
+  }
+  if ((f->sea == nullptr) != (f->town == nullptr))
+    return fail(h, ICE3GB_ERR_NULL, "sea and town must be both given or both NULL");
+  if (!h->rain_ice_ok) return fail(h, ICE3GB_ERR_UNSUPPORTED, "%s", h->rain_ice_why.c_str());
+  return ICE3GB_OK;
+}
+
+SedArgs sed_args(const Ice3gbSedimentationFields &f, int nij, int nk, double dt, int fortran)
+{
+  SedArgs a;
+  a.rhodref = f.rhodref; a.dzz = f.dzz; a.pabs = f.pabs; a.tht = f.tht; a.sea = f.sea; a.town = f.town;
+  a.src[0] = f.rcs; a.src[1] = f.rrs; a.src[2] = f.ris; a.src[3] = f.rss; a.src[4] = f.rgs;
+  a.fpr[0] = f.fpr_c; a.fpr[1] = f.fpr_r; a.fpr[2] = f.fpr_i; a.fpr[3] = f.fpr_s; a.fpr[4] = f.fpr_g;
+  a.inpr[0] = f.inprc; a.inpr[1] = f.inprr; a.inpr[2] = f.inpri; a.inpr[3] = f.inprs; a.inpr[4] = f.inprg;
+  a.nij = nij; a.nk = nk; a.dt = dt; a.fortran = fortran;
+  return a;
+}
+
+int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                 const Ice3gbRainIceFields *f, cudaStream_t s)
+{
+  const long n = (long)nij * nk;
+  const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (h->c.LSEDIM_AFTER != 0.0);
+  const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (h->c.LDEPOSC != 0.0);
+  const int max_passes = (opt && opt->max_passes > 0) ? opt->max_passes : 256;
+  if (max_passes > 65535) return fail(h, ICE3GB_ERR_RANGE, "max_passes=%d above 65535", max_passes);
+  const int sed_fortran = !(opt && opt->sed_jax > 0);
+  Ice3gbConstants c = h->c;
+  if (opt && opt->lfeedbackt >= 0) c.LFEEDBACKT = opt->lfeedbackt ? 1.0 : 0.0;
+  Ice3gbSedimentationFields sf;
+  std::memset(&sf, 0, sizeof(sf));
+  sf.rhodref = f->rhodref; sf.dzz = f->dzz; sf.pabs = f->pabs; sf.tht = f->tht; sf.sea = f->sea; sf.town = f->town;
+  sf.rcs = f->rcs; sf.rrs = f->rrs; sf.ris = f->ris; sf.rss = f->rss; sf.rgs = f->rgs;
+  sf.inprc = f->inprc; sf.inprr = f->inprr; sf.inpri = f->inpri; sf.inprs = f->inprs; sf.inprg = f->inprg;
+  sf.fpr_c = f->fpr_c; sf.fpr_r = f->fpr_r; sf.fpr_i = f->fpr_i; sf.fpr_s = f->fpr_s; sf.fpr_g = f->fpr_g;
+  const SedArgs sa = sed_args(sf, nij, nk, dt, sed_fortran);
+  cudaError_t e;
+  if (!lsedim_after) {
+    ProfScope ps(h, K_SEDIM, s);
+    if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+  }
+  // per-call scratch: 3 words + n keys, stream-ordered
+  unsigned int *scr = nullptr;
+  const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n);
+  if ((e = cudaMallocAsync(&scr, bytes, s)) != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
+  if ((e = cudaMemsetAsync(scr, 0, 4 * sizeof(unsigned int), s)) != cudaSuccess) {
+    cudaFreeAsync(scr, s);
+    return cuda_fail(h, e, "cudaMemsetAsync");
+  }
+  RainIceArgs a;
+  a.f = *f;
+  a.luts = h->d_luts;
+  a.scr.status = h->d_status;
+  a.scr.chunk_counter = scr + 0;
+  a.scr.key_max = scr + 1;
+  a.scr.keys = scr + 4;
+  a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
+  {
+    ProfScope ps(h, K_RAIN_ICE, s);
+    e = launch_rain_ice_points(c, a, h->num_sms, s);
+  }
+  if (e == cudaSuccess) {
+    ProfScope ps(h, K_EVAP_FIXUP, s);
+    e = launch_rain_ice_evap_fixup(a, s);
+  }
+  cudaFreeAsync(scr, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "rain_ice launch");
+  if (lsedim_after) {
+    ProfScope ps(h, K_SEDIM, s);
+    if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+  }
+  if (ldeposc || f->indep) {
+    ProfScope ps(h, K_FOG, s);
+    FogArgs fa;
+    fa.rct = f->rct; fa.rhodref = f->rhodref; fa.dzz = f->dzz; fa.rcs = f->rcs; fa.inprc = f->inprc;
+    fa.indep = f->indep; fa.nij = nij; fa.enabled = ldeposc;
+    if ((e = launch_fog_deposition(c, fa, s)) != cudaSuccess) return cuda_fail(h, e, "fog launch");
+  }
+  return ICE3GB_OK;
+}
+
+int validate_step(Handle *h, const Ice3gbStepFields *f)
+{
+  if (!f) return fail(h, ICE3GB_ERR_NULL, "fields pointer is NULL");
+  REQUIRE(f->sigqsat); REQUIRE(f->pabs); REQUIRE(f->exn); REQUIRE(f->exnref); REQUIRE(f->rhodref);
+  REQUIRE(f->dzz); REQUIRE(f->sigs); REQUIRE(f->th); REQUIRE(f->rv); REQUIRE(f->rc); REQUIRE(f->ri);
+  REQUIRE(f->rr); REQUIRE(f->rs); REQUIRE(f->rg); REQUIRE(f->cf_mf); REQUIRE(f->rc_mf); REQUIRE(f->ri_mf);
+  REQUIRE(f->ths); REQUIRE(f->rvs); REQUIRE(f->rcs); REQUIRE(f->rrs); REQUIRE(f->ris); REQUIRE(f->rss);
+  REQUIRE(f->rgs); REQUIRE(f->cit); REQUIRE(f->t); REQUIRE(f->rv_out); REQUIRE(f->rc_out); REQUIRE(f->ri_out);
+  REQUIRE(f->cldfr); REQUIRE(f->hlc_hrc); REQUIRE(f->hlc_hcf); REQUIRE(f->hli_hri); REQUIRE(f->hli_hcf);
+  REQUIRE(f->evap3d); REQUIRE(f->rainfr); REQUIRE(f->inprc); REQUIRE(f->inprr); REQUIRE(f->inpri);
+  REQUIRE(f->inprs); REQUIRE(f->inprg);
+  if ((f->sea == nullptr) != (f->town == nullptr))
+    return fail(h, ICE3GB_ERR_NULL, "sea and town must be both given or both NULL");
+  if (h->c.CONDENS != 0.0 || h->c.OCND2 != 0.0)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "ice_adjust: only CONDENS=CB02 without OCND2");
+  if (!h->rain_ice_ok) return fail(h, ICE3GB_ERR_UNSUPPORTED, "%s", h->rain_ice_why.c_str());
+  return ICE3GB_OK;
+}
+
+int run_physics_step(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                     const Ice3gbStepFields *f, cudaStream_t s)
+{
+  const long n = (long)nij * nk;
+  double *scr = nullptr;
+  cudaError_t e = cudaMallocAsync(&scr, sizeof(double) * 5 * (size_t)n, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
+  double *cldfr1 = scr, *hlc_hrc1 = scr + n, *hlc_hcf1 = scr + 2 * n, *hli_hri1 = scr + 3 * n,
+         *hli_hcf1 = scr + 4 * n;
+  // 1. first adjustment: S0 -> S1, cloud fraction and subgrid partition to scratch
+  IaKernelFields k1;
+  std::memset(&k1, 0, sizeof(k1));
+  Ice3gbIceAdjustFields &a = k1.f;
+  a.sigqsat = f->sigqsat; a.pabs = f->pabs; a.sigs = f->sigs; a.th = f->th; a.exn = f->exn;
+  a.exn_ref = f->exnref; a.rho_dry_ref = f->rhodref; a.rv = f->rv; a.rc = f->rc; a.ri = f->ri; a.rr = f->rr;
+  a.rs = f->rs; a.rg = f->rg; a.cf_mf = f->cf_mf; a.rc_mf = f->rc_mf; a.ri_mf = f->ri_mf;
+  a.rvs = f->rvs; a.rcs = f->rcs; a.ris = f->ris; a.ths = f->ths;
+  a.cldfr = cldfr1; a.hlc_hrc = hlc_hrc1; a.hlc_hcf = hlc_hcf1; a.hli_hri = hli_hri1; a.hli_hcf = hli_hcf1;
+  a.sigqsat_3d = 0;
+  int rc = ICE3GB_OK;
+  {
+    ProfScope ps(h, K_ICE_ADJUST, s);
+    e = launch_ice_adjust(h->c, k1, nij, nk, dt, ia_vec2_ok(&a, n), h->num_sms, s);
+  }
+  if (e != cudaSuccess) rc = cuda_fail(h, e, "ice_adjust launch");
+  // 2. rain_ice on the time-t state with S1
+  if (rc == ICE3GB_OK) {
+    Ice3gbRainIceFields r;
+    std::memset(&r, 0, sizeof(r));
+    r.exn = f->exn; r.dzz = f->dzz; r.rhodref = f->rhodref; r.exnref = f->exnref; r.pabs = f->pabs;
+    r.cldfr = cldfr1; r.sigs = f->sigs; r.tht = f->th; r.rvt = f->rv; r.rct = f->rc; r.rrt = f->rr;
+    r.rit = f->ri; r.rst = f->rs; r.rgt = f->rg; r.sea = f->sea; r.town = f->town; r.cit = f->cit;
+    r.hlc_hrc = hlc_hrc1; r.hlc_hcf = hlc_hcf1; r.hli_hri = hli_hri1; r.hli_hcf = hli_hcf1;
+    r.ths = f->ths; r.rvs = f->rvs; r.rcs = f->rcs; r.rrs = f->rrs; r.ris = f->ris; r.rss = f->rss;
+    r.rgs = f->rgs; r.evap3d = f->evap3d; r.rainfr = f->rainfr; r.inprc = f->inprc; r.inprr = f->inprr;
+    r.inpri = f->inpri; r.inprs = f->inprs; r.inprg = f->inprg;
+    rc = run_rain_ice(h, nij, nk, dt, opt, &r, s);
+  }
+  // 3. final adjustment on the post-microphysics state dt*S2 with S2 -> S3
+  if (rc == ICE3GB_OK) {
+    IaKernelFields k2 = k1;
+    Ice3gbIceAdjustFields &b = k2.f;
+    b.t = f->t; b.rv_out = f->rv_out; b.rc_out = f->rc_out; b.ri_out = f->ri_out; b.cldfr = f->cldfr;
+    b.hlc_hrc = f->hlc_hrc; b.hlc_hcf = f->hlc_hcf; b.hli_hri = f->hli_hri; b.hli_hcf = f->hli_hcf;
+    k2.rrs = f->rrs; k2.rss = f->rss; k2.rgs = f->rgs;
+    k2.adv_dt = dt;
+    const bool v2 = ia_vec2_ok(&b, n) && aligned16(f->rrs) && aligned16(f->rss) && aligned16(f->rgs);
+    ProfScope ps(h, K_ICE_ADJUST, s);
+    e = launch_ice_adjust(h->c, k2, nij, nk, dt, v2, h->num_sms, s);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "ice_adjust launch");
+  }
+  cudaFreeAsync(scr, s);
+  return rc;
+}
+
+// ---- host staging -----------------------------------------------------------
+int ensure_stage(Handle *h, size_t bytes)
+{
+  if (h->stage_cap >= bytes) return ICE3GB_OK;
+  if (h->d_stage) cudaFree(h->d_stage);
+  h->d_stage = nullptr;
+  h->stage_cap = 0;
+  cudaError_t e = cudaMalloc(&h->d_stage, bytes);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(staging)");
+  h->stage_cap = bytes;
+  return ICE3GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ice3gb_version(void) { return ICE3GB_VERSION; }
+
+static const char *kNames[] = {
+#define ICE3GB_X_NAME(name) #name,
+    ICE3GB_CONSTANTS(ICE3GB_X_NAME)
+#undef ICE3GB_X_NAME
+};
+
+int ice3gb_constant_count(void) { return (int)(sizeof(kNames) / sizeof(kNames[0])); }
+
+const char *ice3gb_constant_name(int i)
+{
+  if (i < 0 || i >= ice3gb_constant_count()) return nullptr;
+  return kNames[i];
+}
+
+int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handle)
+{
+  if (!c || !luts || !handle) return fail(nullptr, ICE3GB_ERR_NULL, "ice3gb_create: NULL argument");
+  *handle = nullptr;
+  if ((int)c->NGAMINC != ICE3GB_NGAMINC || (int)c->NACCLBDAS != ICE3GB_NACCLBDAS ||
+      (int)c->NACCLBDAR != ICE3GB_NACCLBDAR || (int)c->NDRYLBDAG != ICE3GB_NDRYLBDAG ||
+      (int)c->NDRYLBDAS != ICE3GB_NDRYLBDAS || (int)c->NDRYLBDAR != ICE3GB_NDRYLBDAR)
+    return fail(nullptr, ICE3GB_ERR_RANGE, "lookup-table sizes differ from the compiled ones");
+  Handle *h = new Handle();
+  h->magic = kMagic;
+  h->c = *c;
+  h->d_luts = nullptr;
+  h->d_status = nullptr;
+  h->d_stage = nullptr;
+  h->stage_cap = 0;
+  h->err[0] = 0;
+  h->profiling = false;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_luts, sizeof(Ice3gbLuts));
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_luts, luts, sizeof(Ice3gbLuts), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_status, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    int rc = cuda_fail(nullptr, e, "ice3gb_create");
+    if (h->d_luts) cudaFree(h->d_luts);
+    if (h->d_status) cudaFree(h->d_status);
+    h->magic = 0;
+    delete h;
+    return rc;
+  }
+  h->rain_ice_ok = true;
+  char why[256] = "";
+  if ((int)c->NRR != 6) snprintf(why, sizeof(why), "rain_ice supports NRR=6 only (got %g)", c->NRR);
+  else if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)
+    snprintf(why, sizeof(why), "rain_ice: MRSTEP/TSTEP_TS time-splitting is not supported");
+  else if ((int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0)
+    snprintf(why, sizeof(why), "rain_ice: SUBG_RC_RR_ACCR/SUBG_RR_EVAP other than NONE are not supported");
+  if (why[0]) {
+    h->rain_ice_ok = false;
+    h->rain_ice_why = why;
+  }
+  *handle = h;
+  return ICE3GB_OK;
+}
+
+static void drop_events(Handle *h)
+{
+  std::lock_guard<std::mutex> lock(h->prof_mu);
+  for (auto &ev : h->events) {
+    cudaEventDestroy(ev.second.first);
+    cudaEventDestroy(ev.second.second);
+  }
+  h->events.clear();
+}
+
+int ice3gb_profile_enable(void *handle, int enable)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_profile_enable: invalid handle");
+  drop_events(h);
+  h->profiling = enable != 0;
+  return ICE3GB_OK;
+}
+
+int ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_profile_read: invalid handle");
+  if (kernel_id < 0 || kernel_id >= K_COUNT) return fail(h, ICE3GB_ERR_RANGE, "kernel id %d", kernel_id);
+  std::lock_guard<std::mutex> lock(h->prof_mu);
+  int cnt = 0;
+  double tot = 0.0;
+  for (auto &ev : h->events) {
+    if (ev.first != kernel_id) continue;
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(ev.second.second);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev.second.first, ev.second.second);
+    if (e != cudaSuccess) return cuda_fail(h, e, "ice3gb_profile_read");
+    ++cnt;
+    tot += ms;
+  }
+  if (launches) *launches = cnt;
+  if (total_ms) *total_ms = tot;
+  return ICE3GB_OK;
+}
+
+const char *ice3gb_kernel_name(int kernel_id)
+{
+  return (kernel_id >= 0 && kernel_id < K_COUNT) ? kKernelNames[kernel_id] : nullptr;
+}
+
+int ice3gb_destroy(void *handle)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_destroy: invalid handle");
+  drop_events(h);
+  cudaFree(h->d_luts);
+  cudaFree(h->d_status);
+  if (h->d_stage) cudaFree(h->d_stage);
+  h->magic = 0;
+  delete h;
+  return ICE3GB_OK;
+}
+
+int ice3gb_last_error(void *handle, char *buf, size_t n)
+{
+  Handle *h = as_handle(handle);
+  const char *src = h ? h->err : g_err;
+  if (buf && n) snprintf(buf, n, "%s", src);
+  return (int)strlen(src);
+}
+
+int ice3gb_status(void *handle, void *stream, uint32_t *bits)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_status: invalid handle");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned int v = 0;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemcpy(&v, h->d_status, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) return cuda_fail(h, e, "ice3gb_status");
+  if (bits) *bits = v;
+  if (v) return fail(h, ICE3GB_ERR_DEVICE, "device status 0x%x%s", v,
+                     (v & ICE3GB_DEV_PASS_CAP) ? " (sub-step pass cap reached)" : "");
+  return ICE3GB_OK;
+}
+
+int ice3gb_ice_adjust(void *handle, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_ice_adjust: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f)) || (rc = check_device(h))) return rc;
+  const long n = (long)nij * nk;
+  IaKernelFields kf;
+  kf.f = *f;
+  kf.rrs = kf.rss = kf.rgs = nullptr;
+  kf.adv_dt = 0.0;
+  cudaError_t e;
+  {
+    ProfScope ps(h, K_ICE_ADJUST, static_cast<cudaStream_t>(stream));
+    e = launch_ice_adjust(h->c, kf, nij, nk, dt, ia_vec2_ok(f, n), h->num_sms, static_cast<cudaStream_t>(stream));
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, "ice_adjust launch");
+  return ICE3GB_OK;
+}
+
+int ice3gb_sedimentation(void *handle, int nij, int nk, double dt, const Ice3gbSedimentationFields *f,
+                         void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_sedimentation: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_sed(h, f)) || (rc = check_device(h))) return rc;
+  cudaError_t e;
+  {
+    ProfScope ps(h, K_SEDIM, static_cast<cudaStream_t>(stream));
+    e = launch_sedimentation(h->c, sed_args(*f, nij, nk, dt, f->fortran_semantics != 0),
+                             static_cast<cudaStream_t>(stream));
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+  return ICE3GB_OK;
+}
+
+int ice3gb_physics_step(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                        const Ice3gbStepFields *f, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_physics_step: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_step(h, f)) || (rc = check_device(h))) return rc;
+  return run_physics_step(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream));
+}
+
+int ice3gb_physics_step_host(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                             const Ice3gbStepFields *f, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_physics_step_host: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_step(h, f)) || (rc = check_device(h))) return rc;
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)nij * nk, b3 = n * sizeof(double), b2 = (size_t)nij * sizeof(double);
+  const size_t b3p = (b3 + 255) & ~(size_t)255, b2p = (b2 + 255) & ~(size_t)255;
+  // 3-D: 16 inputs + 8 in-out + 11 outputs; 2-D: sigqsat, sea, town + 5 outputs
+  if ((rc = ensure_stage(h, 35 * b3p + 8 * b2p))) return rc;
+  char *base = reinterpret_cast<char *>(h->d_stage);
+  size_t off = 0;
+  cudaError_t e = cudaSuccess;
+  auto take = [&](size_t bp) { double *p = reinterpret_cast<double *>(base + off); off += bp; return p; };
+  auto up = [&](const double *src, size_t b, size_t bp) -> double * {
+    double *p = take(bp);
+    if (src && e == cudaSuccess) e = cudaMemcpyAsync(p, src, b, cudaMemcpyHostToDevice, s);
+    return src ? p : nullptr;
+  };
+  Ice3gbStepFields d;
+  std::memset(&d, 0, sizeof(d));
+  d.sigqsat = up(f->sigqsat, b2, b2p);
+  d.pabs = up(f->pabs, b3, b3p); d.exn = up(f->exn, b3, b3p); d.exnref = up(f->exnref, b3, b3p);
+  d.rhodref = up(f->rhodref, b3, b3p); d.dzz = up(f->dzz, b3, b3p); d.sigs = up(f->sigs, b3, b3p);
+  d.th = up(f->th, b3, b3p); d.rv = up(f->rv, b3, b3p); d.rc = up(f->rc, b3, b3p); d.ri = up(f->ri, b3, b3p);
+  d.rr = up(f->rr, b3, b3p); d.rs = up(f->rs, b3, b3p); d.rg = up(f->rg, b3, b3p);
+  d.cf_mf = up(f->cf_mf, b3, b3p); d.rc_mf = up(f->rc_mf, b3, b3p); d.ri_mf = up(f->ri_mf, b3, b3p);
+  d.sea = up(f->sea, b2, b2p); d.town = up(f->town, b2, b2p);
+  d.ths = up(f->ths, b3, b3p); d.rvs = up(f->rvs, b3, b3p); d.rcs = up(f->rcs, b3, b3p);
+  d.rrs = up(f->rrs, b3, b3p); d.ris = up(f->ris, b3, b3p); d.rss = up(f->rss, b3, b3p);
+  d.rgs = up(f->rgs, b3, b3p); d.cit = up(f->cit, b3, b3p);
+  d.t = take(b3p); d.rv_out = take(b3p); d.rc_out = take(b3p); d.ri_out = take(b3p); d.cldfr = take(b3p);
+  d.hlc_hrc = take(b3p); d.hlc_hcf = take(b3p); d.hli_hri = take(b3p); d.hli_hcf = take(b3p);
+  d.evap3d = take(b3p); d.rainfr = take(b3p);
+  d.inprc = take(b2p); d.inprr = take(b2p); d.inpri = take(b2p); d.inprs = take(b2p); d.inprg = take(b2p);
+  if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
+  if ((rc = run_physics_step(h, nij, nk, dt, opt, &d, s))) return rc;
+  struct Pair { double *dst; const double *src; size_t bytes; };
+  const Pair back[] = {
+      {f->ths, d.ths, b3}, {f->rvs, d.rvs, b3}, {f->rcs, d.rcs, b3}, {f->rrs, d.rrs, b3}, {f->ris, d.ris, b3},
+      {f->rss, d.rss, b3}, {f->rgs, d.rgs, b3}, {f->cit, d.cit, b3}, {f->t, d.t, b3}, {f->rv_out, d.rv_out, b3},
+      {f->rc_out, d.rc_out, b3}, {f->ri_out, d.ri_out, b3}, {f->cldfr, d.cldfr, b3},
+      {f->hlc_hrc, d.hlc_hrc, b3}, {f->hlc_hcf, d.hlc_hcf, b3}, {f->hli_hri, d.hli_hri, b3},
+      {f->hli_hcf, d.hli_hcf, b3}, {f->evap3d, d.evap3d, b3}, {f->rainfr, d.rainfr, b3},
+      {f->inprc, d.inprc, b2}, {f->inprr, d.inprr, b2}, {f->inpri, d.inpri, b2}, {f->inprs, d.inprs, b2},
+      {f->inprg, d.inprg, b2}};
+  for (const Pair &p : back)
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
+  return ICE3GB_OK;
+}
+
+int ice3gb_rain_ice(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                    const Ice3gbRainIceFields *f, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_rain_ice: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
+  return run_rain_ice(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream));
+}
+
+// ---- host-buffer entry points ---------------------------------------------
+
+int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f,
+                           void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_ice_adjust_host: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f)) || (rc = check_device(h))) return rc;
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)nij * nk, b3 = n * sizeof(double);
+  const size_t bq = (f->sigqsat_3d ? n : (size_t)nij) * sizeof(double);
+  const size_t bq_pad = (bq + 255) & ~(size_t)255, b3_pad = (b3 + 255) & ~(size_t)255;
+  // 15 inputs + 4 in-out + 12 outputs
+  if ((rc = ensure_stage(h, bq_pad + 31 * b3_pad))) return rc;
+  char *base = reinterpret_cast<char *>(h->d_stage);
+  Ice3gbIceAdjustFields d;
+  d.sigqsat = reinterpret_cast<double *>(base);
+  d.sigqsat_3d = f->sigqsat_3d;
+  double *slot = reinterpret_cast<double *>(base + bq_pad);
+  const size_t step = b3_pad / sizeof(double);
+  const double *const *in_src[] = {&f->pabs, &f->sigs, &f->th, &f->exn, &f->exn_ref, &f->rho_dry_ref, &f->rv,
+                                   &f->rc, &f->ri, &f->rr, &f->rs, &f->rg, &f->cf_mf, &f->rc_mf, &f->ri_mf};
+  const double **in_dst[] = {&d.pabs, &d.sigs, &d.th, &d.exn, &d.exn_ref, &d.rho_dry_ref, &d.rv,
+                             &d.rc, &d.ri, &d.rr, &d.rs, &d.rg, &d.cf_mf, &d.rc_mf, &d.ri_mf};
+  double *const *io_src[] = {&f->rvs, &f->rcs, &f->ris, &f->ths};
+  double **io_dst[] = {&d.rvs, &d.rcs, &d.ris, &d.ths};
+  double *const *out_src[] = {&f->t, &f->rv_out, &f->rc_out, &f->ri_out, &f->cldfr, &f->hlc_hrc, &f->hlc_hcf,
+                              &f->hli_hri, &f->hli_hcf, &f->cph, &f->lv, &f->ls};
+  double **out_dst[] = {&d.t, &d.rv_out, &d.rc_out, &d.ri_out, &d.cldfr, &d.hlc_hrc, &d.hlc_hcf,
+                        &d.hli_hri, &d.hli_hcf, &d.cph, &d.lv, &d.ls};
+  cudaError_t e = cudaMemcpyAsync((void *)d.sigqsat, f->sigqsat, bq, cudaMemcpyHostToDevice, s);
+  for (int i = 0; i < 15 && e == cudaSuccess; ++i, slot += step) {
+    *in_dst[i] = slot;
+    e = cudaMemcpyAsync(slot, *in_src[i], b3, cudaMemcpyHostToDevice, s);
+  }
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i, slot += step) {
+    *io_dst[i] = slot;
+    e = cudaMemcpyAsync(slot, *io_src[i], b3, cudaMemcpyHostToDevice, s);
+  }
+  for (int i = 0; i < 12; ++i, slot += step) *out_dst[i] = slot;
+  if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
+  IaKernelFields kf;
+  kf.f = d;
+  kf.rrs = kf.rss = kf.rgs = nullptr;
+  kf.adv_dt = 0.0;
+  {
+    ProfScope ps(h, K_ICE_ADJUST, s);
+    e = launch_ice_adjust(h->c, kf, nij, nk, dt, ia_vec2_ok(&d, (long)n), h->num_sms, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, "ice_adjust launch");
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaMemcpyAsync(*io_src[i], *io_dst[i], b3, cudaMemcpyDeviceToHost, s);
+  for (int i = 0; i < 12 && e == cudaSuccess; ++i)
+    e = cudaMemcpyAsync(*out_src[i], *out_dst[i], b3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
+  return ICE3GB_OK;
+}
+
+int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                         const Ice3gbRainIceFields *f, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_rain_ice_host: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)nij * nk, b3 = n * sizeof(double), b2 = (size_t)nij * sizeof(double);
+  const size_t b3p = (b3 + 255) & ~(size_t)255, b2p = (b2 + 255) & ~(size_t)255;
+  const bool adju = (int)h->c.SUBG_AUCV_RC == 2 || (int)h->c.SUBG_AUCV_RI == 2;
+  const bool st = f->sea != nullptr;
+  const bool fpr = f->fpr_c || f->fpr_r || f->fpr_i || f->fpr_s || f->fpr_g;
+  // 14 in + cit + (4 hl/hi) + 7 sources + 2 out 3-D (+5 fpr); 2-D: sea town + 6 out
+  const size_t n3 = 14 + 1 + (adju ? 4 : 0) + 7 + 2 + (fpr ? 5 : 0);
+  if ((rc = ensure_stage(h, n3 * b3p + 8 * b2p))) return rc;
+  char *base = reinterpret_cast<char *>(h->d_stage);
+  size_t off = 0;
+  auto take3 = [&]() { double *p = reinterpret_cast<double *>(base + off); off += b3p; return p; };
+  auto take2 = [&]() { double *p = reinterpret_cast<double *>(base + off); off += b2p; return p; };
+  Ice3gbRainIceFields d;
+  std::memset(&d, 0, sizeof(d));
+  cudaError_t e = cudaSuccess;
+  auto up3 = [&](const double *src) -> double * {
+    double *p = take3();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p, src, b3, cudaMemcpyHostToDevice, s);
+    return p;
+  };
+  d.exn = up3(f->exn); d.dzz = up3(f->dzz); d.rhodref = up3(f->rhodref); d.exnref = up3(f->exnref);
+  d.pabs = up3(f->pabs); d.cldfr = up3(f->cldfr); d.sigs = up3(f->sigs); d.tht = up3(f->tht);
+  d.rvt = up3(f->rvt); d.rct = up3(f->rct); d.rrt = up3(f->rrt); d.rit = up3(f->rit); d.rst = up3(f->rst);
+  d.rgt = up3(f->rgt); d.cit = up3(f->cit);
+  if (adju) {
+    d.hlc_hrc = up3(f->hlc_hrc); d.hlc_hcf = up3(f->hlc_hcf); d.hli_hri = up3(f->hli_hri);
+    d.hli_hcf = up3(f->hli_hcf);
+  }
+  d.ths = up3(f->ths); d.rvs = up3(f->rvs); d.rcs = up3(f->rcs); d.rrs = up3(f->rrs); d.ris = up3(f->ris);
+  d.rss = up3(f->rss); d.rgs = up3(f->rgs);
+  d.evap3d = take3(); d.rainfr = take3();
+  if (fpr) { d.fpr_c = take3(); d.fpr_r = take3(); d.fpr_i = take3(); d.fpr_s = take3(); d.fpr_g = take3(); }
+  if (st) {
+    double *ps = take2(), *pt = take2();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ps, f->sea, b2, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pt, f->town, b2, cudaMemcpyHostToDevice, s);
+    d.sea = ps; d.town = pt;
+  } else {
+    take2(); take2();
+  }
+  d.inprc = take2(); d.inprr = take2(); d.inpri = take2(); d.inprs = take2(); d.inprg = take2();
+  d.indep = f->indep ? take2() : nullptr;
+  if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
+  if ((rc = run_rain_ice(h, nij, nk, dt, opt, &d, s))) return rc;
+  struct Pair { double *dst; const double *src; size_t bytes; };
+  const Pair back[] = {
+      {f->cit, d.cit, b3}, {f->ths, d.ths, b3}, {f->rvs, d.rvs, b3}, {f->rcs, d.rcs, b3}, {f->rrs, d.rrs, b3},
+      {f->ris, d.ris, b3}, {f->rss, d.rss, b3}, {f->rgs, d.rgs, b3}, {f->evap3d, d.evap3d, b3},
+      {f->rainfr, d.rainfr, b3}, {f->inprc, d.inprc, b2}, {f->inprr, d.inprr, b2}, {f->inpri, d.inpri, b2},
+      {f->inprs, d.inprs, b2}, {f->inprg, d.inprg, b2}, {f->indep, d.indep, b2},
+      {f->fpr_c, d.fpr_c, b3}, {f->fpr_r, d.fpr_r, b3}, {f->fpr_i, d.fpr_i, b3}, {f->fpr_s, d.fpr_s, b3},
+      {f->fpr_g, d.fpr_g, b3}};
+  for (const Pair &p : back)
+    if (p.dst && p.src && e == cudaSuccess) e = cudaMemcpyAsync(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
+  return ICE3GB_OK;
+}
+
+}  // extern "C"

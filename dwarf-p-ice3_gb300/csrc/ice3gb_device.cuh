@@ -1,0 +1,71 @@
+// ice3gb_device.cuh — device-side helpers shared by the ICE3 kernels.
+//
+// Layout: every 3-D field is [nk][nij] FP64 (ij fastest), 2-D fields [nij].
+// The constants table (Ice3gbConstants, ~1.5 KB) is passed by value as a
+// __grid_constant__ kernel parameter, so every lane reads it from the
+// constant bank with no global-memory traffic.
+#pragma once
+
+#include <stdint.h>
+#if defined(__CUDACC__)
+#include <cuda_runtime.h>
+#else
+#include <cmath>
+using std::exp; using std::log; using std::fmin; using std::fmax; using std::sqrt; using std::fabs;
+using std::signbit;
+#endif
+
+#include "../../include/ice3gb.h"
+
+typedef Ice3gbConstants Cst;
+
+#if defined(__CUDACC__)
+#define ICE3_HD __host__ __device__ __forceinline__
+#else
+#define ICE3_HD inline
+#endif
+
+ICE3_HD double sq(double x) { return x * x; }
+// Separately rounded multiply and add (never fused into an FMA).
+ICE3_HD double mul_rn(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(a, b);
+#else
+  volatile double p = a * b;
+  return p;
+#endif
+}
+ICE3_HD double add_rn(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+  return __dadd_rn(a, b);
+#else
+  volatile double p = a + b;
+  return p;
+#endif
+}
+// NaN-propagating minimum/maximum/clip, as numpy's minimum/maximum/clip
+// (the reference JAX lets NaN through on degenerate inputs, e.g. a negative
+// vapour source with no mass flux, stencils/ice_adjust.py:293-296); CUDA's
+// fmin/fmax would return the other operand instead.
+ICE3_HD double nmin(double a, double b) { return (a < b || a != a) ? a : b; }
+ICE3_HD double nmax(double a, double b) { return (a > b || a != a) ? a : b; }
+ICE3_HD double nclip01(double x) { return nmin(nmax(x, 0.0), 1.0); }
+
+// x**a evaluated as exp(a*log(x)).  For the exponents of the scheme
+// (|a*log x| < 60) this stays within ~1e-14 relative of pow(), well inside
+// the 1e-10 parity bar, at about half the FP64 instruction count; callers
+// raising one base to several powers pass a shared log.
+ICE3_HD double powl_(double logx, double a) { return exp(a * logx); }
+ICE3_HD double fpow(double x, double a) { return exp(a * log(x)); }
+
+#if defined(__CUDACC__)
+// 128-bit streaming accessors (LDG.128 / STG.128).
+__device__ __forceinline__ double2 ld2(const double *p, long i) { return __ldg(reinterpret_cast<const double2 *>(p + i)); }
+__device__ __forceinline__ void st2(double *p, long i, double a, double b)
+{
+  __stcs(reinterpret_cast<double2 *>(p + i), make_double2(a, b));
+}
+__device__ __forceinline__ double ld1(const double *p, long i) { return __ldg(p + i); }
+#endif

@@ -1,0 +1,57 @@
+// ice3gb_kernels.h — host-side launchers of the ICE3 kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ice3gb.h"
+
+struct SedArgs {
+  const double *rhodref, *dzz, *pabs, *tht, *sea, *town;
+  double *src[5];   // rcs rrs ris rss rgs (in-out)
+  double *fpr[5];   // optional flux outputs
+  double *inpr[5];  // [nij] outputs
+  int nij, nk;
+  double dt;
+  int fortran;
+};
+
+struct FogArgs {
+  const double *rct, *rhodref, *dzz;
+  double *rcs, *inprc, *indep;
+  int nij, enabled;
+};
+
+// Scratch words of one rain_ice call (device memory, zeroed before launch).
+struct RainIceScratch {
+  unsigned int *status;            // ICE3GB_DEV_* bits
+  unsigned int *chunk_counter;     // dynamic work distribution
+  unsigned int *key_max;           // max over points of (outer << 16 | inner)
+  unsigned int *keys;              // [n] per-point pass key, 0 = not a micro point
+};
+
+struct RainIceArgs {
+  Ice3gbRainIceFields f;
+  const double *luts;  // Ice3gbLuts on the device
+  RainIceScratch scr;
+  int nij, nk;
+  double dt;
+  int max_passes;
+  int lfeedbackt;
+};
+
+// ice_adjust kernel arguments: the public fields plus the optional
+// "advance the state by adv_dt * sources first" extension of the chained step.
+struct IaKernelFields {
+  Ice3gbIceAdjustFields f;
+  const double *rrs, *rss, *rgs;
+  double adv_dt;
+};
+
+cudaError_t launch_ice_adjust(const Ice3gbConstants &c, const IaKernelFields &kf, int nij, int nk, double dt,
+                              bool vec2, int num_sms, cudaStream_t s);
+cudaError_t launch_sedimentation(const Ice3gbConstants &c, const SedArgs &a, cudaStream_t s);
+cudaError_t launch_fog_deposition(const Ice3gbConstants &c, const FogArgs &a, cudaStream_t s);
+cudaError_t launch_rain_ice_points(const Ice3gbConstants &c, const RainIceArgs &a, int num_sms, cudaStream_t s);
+cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s);
+size_t rain_ice_smem_bytes();

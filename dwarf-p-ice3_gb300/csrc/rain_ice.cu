@@ -1,0 +1,190 @@
+// rain_ice.cu — ICE4 one-moment microphysics step, one grid point per thread.
+//
+// Restates, per grid point, PHYEX RAIN_ICE (PHYEX-IAL_CY50T1/micro/
+// rain_ice.F90:334-652 and its disabled tail :758-790), ICE4_PACK
+// (mode_ice4_pack.F90), ICE4_STEPPING (mode_ice4_stepping.F90:139-518),
+// ICE4_TENDENCIES (mode_ice4_tendencies.F90:150-717) and the processes it
+// calls (nucleation, rrhong, rimltc, compute_pdf, slow, warm, fast_rs,
+// fast_rg, fast_ri), then the total tendencies and ICE4_CORRECT_NEGATIVITIES.
+//
+// GB300 mapping:
+//  * the ICE4 collection-kernel tables (GAMINC_RIM1/2/4, KER_RACCSS/RACCS/
+//    SACCRG, KER_RDRYG, KER_SDRYG; 78,720 B FP64) are staged once per block
+//    in shared memory; blocks are persistent (2 per SM) and pull 1-point-per-
+//    thread chunks from a global counter, which balances the data-dependent
+//    number of sub-steps across SMs;
+//  * every per-point quantity that is fixed over the sub-steps (log rho and
+//    the rho powers) is computed once; real powers are exp(a*log x) with the
+//    logarithms of the slope parameters shared by all processes;
+//  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
+//    after the last pass of the call, mode_ice4_stepping.F90:514-516) is
+//    kept with a per-point pass key and a warp-reduced atomicMax, resolved by
+//    a second small kernel.
+#include "ice3gb_device.cuh"
+#include "ice3gb_kernels.h"
+#include "rain_ice_point.cuh"
+
+namespace {
+using namespace ice3pt;
+
+__device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int key)
+{
+  const unsigned int m = __reduce_max_sync(0xffffffffu, key);
+  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(key_max, m);
+}
+
+__global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __grid_constant__ Cst c,
+                                                                         const __grid_constant__ RainIceArgs a)
+{
+  extern __shared__ double lut[];
+  for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
+  __shared__ unsigned int chunk;
+  __syncthreads();
+  const Ice3gbRainIceFields &f = a.f;
+  const long n = (long)a.nij * a.nk;
+  const double dt = a.dt, inv_dt = 1.0 / a.dt;
+  const bool lwarm = c.LWARM != 0.0;
+  const bool sigm = (int)c.SUBG_AUCV_RC == 1 && (int)c.SUBG_PR_PDF == 0;
+  const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
+  bool any_capped = false;
+  for (;;) {
+    if (threadIdx.x == 0) chunk = atomicAdd(a.scr.chunk_counter, 1u);
+    __syncthreads();
+    const long base = (long)chunk * blockDim.x;
+    __syncthreads();
+    if (base >= n) break;
+    const long p = base + threadIdx.x;
+    unsigned int key = 0u;
+    if (p < n) {
+      PointFix pf;
+      pf.exn = ld1(f.exn, p);
+      pf.rho = ld1(f.rhodref, p);
+      pf.pres = ld1(f.pabs, p);
+      const double th = ld1(f.tht, p), rv = ld1(f.rvt, p), rc = ld1(f.rct, p), rr = ld1(f.rrt, p);
+      const double ri = ld1(f.rit, p), rs = ld1(f.rst, p), rg = ld1(f.rgt, p);
+      const double exnref = ld1(f.exnref, p);
+      double ths = f.ths[p], rvs = f.rvs[p], rcs = f.rcs[p], rrs = f.rrs[p], ris = f.ris[p], rss = f.rss[p],
+             rgs = f.rgs[p];
+      double cit = f.cit[p];
+      // rain_ice.F90:334-345 (L/cph without exner) and :370-381 (LLMICRO)
+      const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
+      const double t = th * pf.exn;
+      const double izdev = 1.0 / zdev;
+      const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * izdev;
+      const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * izdev;
+      const bool micro = rc > c.C_RTMIN || rr > c.R_RTMIN || ri > c.I_RTMIN || rs > c.S_RTMIN || rg > c.G_RTMIN;
+      const double iexnref = 1.0 / exnref;
+      const double lsx = lsf * iexnref, lvx = lvf * iexnref;
+      double evap = 0.0, rainfr = 1.0;
+      double zrvheni = 0.0;
+      if (!micro) {
+        cit = 0.0;
+        nucleation(c, true, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
+      }
+      zrvheni = fmin(rvs, zrvheni * inv_dt);
+      if (micro) {
+        pf.lrho = log(pf.rho);
+        pf.rho_mcexvt = exp(-c.CEXVT * pf.lrho);
+        pf.rho_mcexvt1 = pf.rho_mcexvt / pf.rho;
+        pf.rcrautc = c.CRIAUTC / pf.rho;
+        pf.cf = ld1(f.cldfr, p);
+        pf.sigma_rc = sigm ? 2.0 * ld1(f.sigs, p) : 0.0;
+        double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
+        double ext[NV] = {ths - th * inv_dt, rvs - rv * inv_dt, rcs - rc * inv_dt, rrs - rr * inv_dt,
+                          ris - ri * inv_dt, rss - rs * inv_dt, rgs - rg * inv_dt};
+        double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
+        if (adju) {
+          hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
+          hl[3] = rc - hl[2];
+          hi[3] = ri - hi[2];
+          hl[1] = (rc > 0.) ? pf.cf - hl[0] : 0.;
+          hi[1] = (ri > 0.) ? pf.cf - hi[0] : 0.;
+        }
+        double rrevav;
+        bool capped;
+        key = stepping(c, lut, pf, dt, a.max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
+        any_capped |= capped;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
+        evap = lwarm ? rrevav : 0.0;
+        // total tendencies (rain_ice.F90:758-790)
+        const double wv = (vart[IRV] - rv) * inv_dt, wc = (vart[IRC] - rc) * inv_dt;
+        const double wr = (vart[IRR] - rr) * inv_dt, wi = (vart[IRI] - ri) * inv_dt;
+        const double ws = (vart[IRS] - rs) * inv_dt, wg = (vart[IRG] - rg) * inv_dt;
+        ths += (wc + wr) * lvx + (wi + ws + wg) * lsx + zrvheni * lsx;
+        rvs += wv - zrvheni;
+        rcs += wc;
+        rrs += wr;
+        ris += wi + zrvheni;
+        rss += ws;
+        rgs += wg;
+      } else {
+        ths += zrvheni * lsx;
+        rvs -= zrvheni;
+        ris += zrvheni;
+      }
+      // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the sources
+      double w;
+      w = rcs - fmax(rcs, 0.); rvs += w; ths -= w * lvx; rcs -= w;
+      w = rrs - fmax(rrs, 0.); rvs += w; ths -= w * lvx; rrs -= w;
+      w = ris - fmax(ris, 0.); rvs += w; ths -= w * lsx; ris -= w;
+      w = rss - fmax(rss, 0.); rvs += w; ths -= w * lsx; rss -= w;
+      w = rgs - fmax(rgs, 0.); rvs += w; ths -= w * lsx; rgs -= w;
+      w = fmin(1., fmax(c.V_RTMIN - rvs, 0.) / fmax(rcs + ris, 1.e-20));
+      ths -= w * (rcs * lvx + ris * lsx);
+      rvs += w * (rcs + ris);
+      rcs = (1. - w) * rcs;
+      ris = (1. - w) * ris;
+      w = fmin(fmax(rrs, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rrs -= w; ths -= w * lvx;
+      w = fmin(fmax(rss, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rss -= w; ths -= w * lsx;
+      w = fmin(fmax(rgs, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rgs -= w; ths -= w * lsx;
+      f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
+      f.rgs[p] = rgs;
+      f.cit[p] = cit;
+      f.evap3d[p] = evap;
+      f.rainfr[p] = rainfr;
+      a.scr.keys[p] = key;
+    }
+    warp_key_max(a.scr.key_max, key);
+  }
+  if (any_capped) atomicOr(a.scr.status, ICE3GB_DEV_PASS_CAP);
+}
+
+// PRREVAV after the last pass of the call: zero evap3d on micro points that
+// were not active in that pass (mode_ice4_stepping.F90:514-516).
+__global__ void rain_ice_evap_fixup_kernel(double *__restrict__ evap3d, const unsigned int *__restrict__ keys,
+                                           const unsigned int *__restrict__ key_max, long n)
+{
+  const unsigned int kmax = *key_max;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
+    const unsigned int k = keys[p];
+    if (k != 0u && k != kmax) evap3d[p] = 0.0;
+  }
+}
+
+}  // namespace
+
+size_t rain_ice_smem_bytes() { return sizeof(double) * LUT_N; }
+
+cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_sms, cudaStream_t s)
+{
+  cudaError_t e = cudaFuncSetAttribute(rain_ice_points_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)rain_ice_smem_bytes());
+  if (e != cudaSuccess) return e;
+  const long n = (long)a.nij * a.nk;
+  long chunks = (n + RI_THREADS - 1) / RI_THREADS;
+  long blocks = (long)num_sms * 2;
+  if (blocks > chunks) blocks = chunks;
+  if (blocks < 1) blocks = 1;
+  rain_ice_points_kernel<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s)
+{
+  const long n = (long)a.nij * a.nk;
+  long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  rain_ice_evap_fixup_kernel<<<(unsigned)blocks, 256, 0, s>>>(a.f.evap3d, a.scr.keys, a.scr.key_max, n);
+  return cudaGetLastError();
+}

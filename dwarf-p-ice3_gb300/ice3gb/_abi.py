@@ -53,6 +53,23 @@ class RainIceFields(ctypes.Structure):
         "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")]
 
 
+class StepFields(ctypes.Structure):
+    _fields_ = [(n, P) for n in (
+        "sigqsat", "pabs", "exn", "exnref", "rhodref", "dzz", "sigs",
+        "th", "rv", "rc", "ri", "rr", "rs", "rg", "cf_mf", "rc_mf", "ri_mf", "sea", "town",
+        "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "cit",
+        "t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf",
+        "evap3d", "rainfr", "inprc", "inprr", "inpri", "inprs", "inprg")]
+
+
+STEP_IN = ("sigqsat", "pabs", "exn", "exnref", "rhodref", "dzz", "sigs", "th", "rv", "rc", "ri", "rr", "rs", "rg",
+           "cf_mf", "rc_mf", "ri_mf")
+STEP_INOUT = ("ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "cit")
+STEP_OUT3 = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "evap3d",
+             "rainfr")
+STEP_OUT2 = ("inprc", "inprr", "inpri", "inprs", "inprg")
+
+
 class RainIceOptions(ctypes.Structure):
     _fields_ = [("lsedim_after", ctypes.c_int32), ("ldeposc", ctypes.c_int32),
                 ("lfeedbackt", ctypes.c_int32), ("max_passes", ctypes.c_int32),
@@ -63,7 +80,10 @@ EXPORTED = (
     "ice3gb_version", "ice3gb_constant_count", "ice3gb_constant_name", "ice3gb_create",
     "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status", "ice3gb_ice_adjust",
     "ice3gb_sedimentation", "ice3gb_rain_ice", "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host",
+    "ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_profile_enable", "ice3gb_profile_read",
+    "ice3gb_kernel_name",
 )
+KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition")
 
 _lib: Optional[ctypes.CDLL] = None
 
@@ -95,7 +115,16 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ice3gb_rain_ice.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                     ctypes.POINTER(RainIceOptions), ctypes.POINTER(RainIceFields), P]
     lib.ice3gb_rain_ice_host.argtypes = lib.ice3gb_rain_ice.argtypes
-    for name in ("ice3gb_create", "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status",
+    lib.ice3gb_physics_step.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.POINTER(RainIceOptions), ctypes.POINTER(StepFields), P]
+    lib.ice3gb_physics_step_host.argtypes = lib.ice3gb_physics_step.argtypes
+    lib.ice3gb_profile_enable.argtypes = [P, ctypes.c_int]
+    lib.ice3gb_profile_enable.restype = ctypes.c_int
+    lib.ice3gb_profile_read.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    lib.ice3gb_profile_read.restype = ctypes.c_int
+    lib.ice3gb_kernel_name.argtypes = [ctypes.c_int]
+    lib.ice3gb_kernel_name.restype = ctypes.c_char_p
+    for name in ("ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_create", "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status",
                  "ice3gb_ice_adjust", "ice3gb_sedimentation", "ice3gb_rain_ice",
                  "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host"):
         getattr(lib, name).restype = ctypes.c_int

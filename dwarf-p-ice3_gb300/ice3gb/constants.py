@@ -9,11 +9,17 @@ Two flavours exist because the reference's Python tables diverge from the
 PHYEX Fortran it was translated from:
 
 ``table="jax"``   the Python values unchanged (parity with the reference JAX);
-``table="phyex"`` Fortran values for the three known divergences:
+``table="phyex"`` Fortran values for the known divergences:
   * TMINMIX/TMAXMIX swapped back (src/ice3/phyex_common/nebn.py:244-245 vs
     PHYEX-IAL_CY50T1/micro/modd_nebn.F90:178-179);
   * GAMINC_RIM1/2/4 with bound = BOUND_MIN * ZRATE**(j-1) and RIM4 built on
-    BG (rain_ice_parameters.py:1105-1156 vs mode_ini_rain_ice.F90:786-790).
+    BG (rain_ice_parameters.py:1105-1156 vs mode_ini_rain_ice.F90:786-790);
+  * snow fall speed of the statistical sedimentation: the Python table
+    overwrites EXSEDS with DS-BS (= -1.63) and FSEDS with the LNEWCOEFF
+    prefactor (rain_ice_parameters.py:725-731), which makes snow fall at
+    ~1e16 m/s; PHYEX (LNEWCOEFF = .FALSE.) uses EXSEDS = (BS+DS-CXS)/(BS-CXS)
+    and FSEDS = the value the Python table keeps as SEDS
+    (mode_ini_rain_ice.F90:533-536, rain_ice_parameters.py:708-722).
 """
 from __future__ import annotations
 
@@ -140,6 +146,9 @@ def build_table(phyex: Any = None, table: str = "jax", program: str = "AROME",
     if table == "phyex":
         values["TMINMIX"], values["TMAXMIX"] = 253.16, 273.16
         rim1, rim2, rim4 = _gaminc_fortran(ext)
+        bs, ds, cxs = float(ext["BS"]), float(ext["DS"]), float(ext["CXS"])
+        values["EXSEDS"] = (bs + ds - cxs) / (bs - cxs)
+        values["FSEDS"] = float(ext["SEDS"])
     if overrides:
         for k, v in overrides.items():
             if k not in values:

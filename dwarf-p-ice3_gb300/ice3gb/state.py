@@ -14,7 +14,10 @@ The distributions follow the workload definitions of the benchmark:
   ice below (saturation formula and constants of the constants table);
 * rc, ri ~ LogNormal(ln 1e-5, 1), each zero with probability 0.5, ri = 0 where
   T >= 268 K; sigs ~ U[1e-6, 1e-4]; sigqsat = 0.02 per column;
-  cf_mf = rc_mf = ri_mf = 0 and zero initial sources;
+  cf_mf = rc_mf = ri_mf = 0;
+* sources S = x_t / dt (th/dt, r/dt): the PHYEX convention for a step with
+  no other tendency (the external tendency S - x_t/dt of
+  mode_ice4_stepping.F90:151-158 is then zero);
 * with ``precip=True`` also rr, rs, rg ~ LogNormal(ln 1e-5, 1.5) each zero
   with probability 0.6, cloud fraction ~ U[0, 1] where rc + ri > 0,
   ci_t = hlc_* = hli_* = 0, sea = town = 0.
@@ -41,7 +44,7 @@ def _lognormal(gen, shape, median, sigma, device):
 
 
 def make_state(nij: int, nk: int = 90, seed: int = 0, precip: bool = False,
-               device="cpu", phyex: Optional[Mapping] = None) -> Dict[str, torch.Tensor]:
+               device="cpu", phyex: Optional[Mapping] = None, dt: float = 50.0) -> Dict[str, torch.Tensor]:
     """Return a dict of [nk, nij] float64 tensors (2-D per-column fields are [nij])."""
     ext = externals_from(phyex)
     RD, CPD, P00, EPSILO = (float(ext[k]) for k in ("RD", "CPD", "P00", "EPSILO"))
@@ -88,7 +91,7 @@ def make_state(nij: int, nk: int = 90, seed: int = 0, precip: bool = False,
         "pabs": p, "sigs": sigs, "th": th, "exn": exn, "exn_ref": exn.clone(),
         "rho_dry_ref": rho, "rv": rv, "rc": rc, "ri": ri,
         "cf_mf": zeros.clone(), "rc_mf": zeros.clone(), "ri_mf": zeros.clone(),
-        "rvs": zeros.clone(), "rcs": zeros.clone(), "ris": zeros.clone(), "ths": zeros.clone(),
+        "rvs": rv / dt, "rcs": rc / dt, "ris": ri / dt, "ths": th / dt,
         "dzz": dz, "t": t,
     }
     if precip:
@@ -97,7 +100,9 @@ def make_state(nij: int, nk: int = 90, seed: int = 0, precip: bool = False,
             st[name] = torch.where(torch.rand((nk, nij), generator=gen, **f64) < 0.6, torch.zeros_like(r), r)
         cf = uni((nk, nij), 0.0, 1.0)
         st["cldfr"] = torch.where(rc + ri > 0, cf, torch.zeros_like(cf))
-        for name in ("rrs", "rss", "rgs", "ci_t", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf"):
+        for name in ("rr", "rs", "rg"):
+            st[name + "s"] = st[name] / dt
+        for name in ("ci_t", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf"):
             st[name] = zeros.clone()
         st["sea"] = torch.zeros((nij,), **f64)
         st["town"] = torch.zeros((nij,), **f64)

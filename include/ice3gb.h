@@ -188,6 +188,30 @@ typedef struct Ice3gbRainIceOptions {
                              0 (default): Fortran (see Ice3gbSedimentationFields) */
 } Ice3gbRainIceOptions;
 
+/* ---- chained physics step --------------------------------------------- */
+/* One AROME-style microphysics step on a time-t state, fused on the device:
+ *   S1 = ice_adjust(x_t, S0)
+ *   S2 = rain_ice(x_t, S1, cloud fraction and hl* of the first adjustment)
+ *   S3 = ice_adjust(dt*S2, S2)
+ * Sources are PHYEX total sources (x_{t+dt}/dt), so dt*S2 is the state after
+ * the microphysics; the order follows PHYEX's adjustment before and after the
+ * microphysics (micro/ice_adjust.F90, micro/rain_ice.F90).  In-out sources go
+ * S0 -> S3 (rrs/rss/rgs end as S2); the outputs are those of the final
+ * adjustment plus the rain_ice diagnostics.  No counterpart entry point exists
+ * in the reference; it chains the two reference interfaces above. */
+typedef struct Ice3gbStepFields {
+  const double *sigqsat;            /* [nij]                                */
+  const double *pabs, *exn, *exnref, *rhodref, *dzz, *sigs;
+  const double *th, *rv, *rc, *ri, *rr, *rs, *rg;
+  const double *cf_mf, *rc_mf, *ri_mf;
+  const double *sea, *town;         /* [nij], optional                    */
+  double *ths, *rvs, *rcs, *rrs, *ris, *rss, *rgs, *cit;  /* in-out        */
+  double *t, *rv_out, *rc_out, *ri_out, *cldfr;
+  double *hlc_hrc, *hlc_hcf, *hli_hri, *hli_hcf;
+  double *evap3d, *rainfr;          /* out [nk][nij]                      */
+  double *inprc, *inprr, *inpri, *inprs, *inprg;  /* out [nij]            */
+} Ice3gbStepFields;
+
 /* ---- library / handle -------------------------------------------------- */
 int         ice3gb_version(void);
 int         ice3gb_constant_count(void);
@@ -215,6 +239,22 @@ int ice3gb_rain_ice(void *handle, int nij, int nk, double dt,
                     const Ice3gbRainIceOptions *opt,
                     const Ice3gbRainIceFields *f, void *stream);
 
+/* Chained ice_adjust -> rain_ice -> ice_adjust step (see Ice3gbStepFields). */
+int ice3gb_physics_step(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                        const Ice3gbStepFields *f, void *stream);
+
+/* ---- per-kernel timing -------------------------------------------------- */
+/* While enabled, every kernel launch of the handle is bracketed by CUDA
+ * events recorded on the caller's stream.  ice3gb_profile_read synchronises
+ * those events and returns, per kernel id, the number of launches and their
+ * summed device time since the last enable.  Kernel ids: 0 ice_adjust,
+ * 1 sedimentation, 2 rain_ice (pointwise sub-stepping), 3 rain_ice evap3d
+ * fix-up, 4 fog deposition. */
+#define ICE3GB_NKERNELS 5
+int         ice3gb_profile_enable(void *handle, int enable);
+int         ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms);
+const char *ice3gb_kernel_name(int kernel_id);
+
 /* ---- host-buffer entry points (synchronous) ---------------------------- */
 /* Same as above with HOST pointers, as c_ice_adjust / c_rain_ice take them:
  * host->device copies, the kernels and device->host copies all run on
@@ -224,6 +264,8 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt,
 int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt,
                          const Ice3gbRainIceOptions *opt,
                          const Ice3gbRainIceFields *f, void *stream);
+int ice3gb_physics_step_host(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                             const Ice3gbStepFields *f, void *stream);
 
 #ifdef __cplusplus
 }

@@ -29,8 +29,10 @@ typedef Ice3gbConstants C;
 
 #define EXPORT __attribute__((visibility("default")))
 
-static inline double dmin(double a, double b) { return a < b ? a : b; }
-static inline double dmax(double a, double b) { return a > b ? a : b; }
+/* NaN-propagating minimum/maximum, as numpy.minimum/maximum (the reference
+ * JAX produces NaN on some degenerate inputs, stencils/ice_adjust.py:293-296). */
+static inline double dmin(double a, double b) { return (a < b || a != a) ? a : b; }
+static inline double dmax(double a, double b) { return (a > b || a != a) ? a : b; }
 static inline double clip01(double x) { return dmin(dmax(x, 0.0), 1.0); }
 static inline double sq(double x) { return x * x; }
 
@@ -1152,7 +1154,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     lvf[p] = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
     /* :370-381 LLMICRO */
     const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN || rg > c->G_RTMIN;
-    if (c->LWARM != 0.0) f->evap3d[p] = 0.0;
+    f->evap3d[p] = 0.0;
     f->rainfr[p] = 1.0;  /* :599-605 (no PRFR option) */
     double cit = f->cit[p];
     double zrvheni = 0.0;
@@ -1371,3 +1373,80 @@ EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const d
 }
 
 EXPORT int ice3o_budget_count(void) { return NBU; }
+
+/* ===================================================================== */
+/* Chained step: S1 = ice_adjust(x_t, S0); S2 = rain_ice(x_t, S1);        */
+/* S3 = ice_adjust(dt*S2, S2)  (same contract as ice3gb_physics_step)       */
+/* ===================================================================== */
+EXPORT int ice3o_physics_step(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
+                              const Ice3gbRainIceOptions *opt, const Ice3gbStepFields *f, uint32_t *bits)
+{
+  const long n = (long)nij * nk;
+  double *buf = (double *)malloc(sizeof(double) * 16 * (size_t)n);
+  if (!buf) return ICE3GB_ERR_RANGE;
+  double *d[16];
+  for (int i = 0; i < 16; ++i) d[i] = buf + (size_t)i * n;
+  /* 1. first adjustment; cldfr and hl* into scratch d[0..4], the rest discarded d[5..11] */
+  Ice3gbIceAdjustFields a;
+  memset(&a, 0, sizeof(a));
+  a.sigqsat = f->sigqsat; a.pabs = f->pabs; a.sigs = f->sigs; a.th = f->th; a.exn = f->exn;
+  a.exn_ref = f->exnref; a.rho_dry_ref = f->rhodref; a.rv = f->rv; a.rc = f->rc; a.ri = f->ri; a.rr = f->rr;
+  a.rs = f->rs; a.rg = f->rg; a.cf_mf = f->cf_mf; a.rc_mf = f->rc_mf; a.ri_mf = f->ri_mf;
+  a.rvs = f->rvs; a.rcs = f->rcs; a.ris = f->ris; a.ths = f->ths;
+  a.cldfr = d[0]; a.hlc_hrc = d[1]; a.hlc_hcf = d[2]; a.hli_hri = d[3]; a.hli_hcf = d[4];
+  a.t = d[5]; a.rv_out = d[6]; a.rc_out = d[7]; a.ri_out = d[8]; a.cph = d[9]; a.lv = d[10]; a.ls = d[11];
+  a.sigqsat_3d = 0;
+  int rc = ice3o_ice_adjust(c, nij, nk, dt, &a);
+  if (rc) { free(buf); return rc; }
+  /* 2. rain_ice */
+  Ice3gbRainIceFields r;
+  memset(&r, 0, sizeof(r));
+  r.exn = f->exn; r.dzz = f->dzz; r.rhodref = f->rhodref; r.exnref = f->exnref; r.pabs = f->pabs;
+  r.cldfr = d[0]; r.sigs = f->sigs; r.tht = f->th; r.rvt = f->rv; r.rct = f->rc; r.rrt = f->rr;
+  r.rit = f->ri; r.rst = f->rs; r.rgt = f->rg; r.sea = f->sea; r.town = f->town; r.cit = f->cit;
+  r.hlc_hrc = d[1]; r.hlc_hcf = d[2]; r.hli_hri = d[3]; r.hli_hcf = d[4];
+  r.ths = f->ths; r.rvs = f->rvs; r.rcs = f->rcs; r.rrs = f->rrs; r.ris = f->ris; r.rss = f->rss; r.rgs = f->rgs;
+  r.evap3d = f->evap3d; r.rainfr = f->rainfr; r.inprc = f->inprc; r.inprr = f->inprr; r.inpri = f->inpri;
+  r.inprs = f->inprs; r.inprg = f->inprg;
+  rc = ice3o_rain_ice(c, lut, nij, nk, dt, opt, &r, bits);
+  if (rc) { free(buf); return rc; }
+  /* 3. adjust again the post-microphysics state dt*S2 (d[5..11] reused) */
+  double *th2 = d[5], *rv2 = d[6], *rc2 = d[7], *ri2 = d[8], *rr2 = d[9], *rs2 = d[10], *rg2 = d[11];
+#pragma omp parallel for schedule(static)
+  for (long p = 0; p < n; ++p) {
+    th2[p] = dt * f->ths[p];
+    rv2[p] = dt * f->rvs[p];
+    rc2[p] = dt * f->rcs[p];
+    ri2[p] = dt * f->ris[p];
+    rr2[p] = dt * f->rrs[p];
+    rs2[p] = dt * f->rss[p];
+    rg2[p] = dt * f->rgs[p];
+  }
+  a.th = th2; a.rv = rv2; a.rc = rc2; a.ri = ri2; a.rr = rr2; a.rs = rs2; a.rg = rg2;
+  a.t = f->t; a.rv_out = f->rv_out; a.rc_out = f->rc_out; a.ri_out = f->ri_out; a.cldfr = f->cldfr;
+  a.hlc_hrc = f->hlc_hrc; a.hlc_hcf = f->hlc_hcf; a.hli_hri = f->hli_hri; a.hli_hcf = f->hli_hcf;
+  a.cph = d[12]; a.lv = d[13]; a.ls = d[14];
+  rc = ice3o_ice_adjust(c, nij, nk, dt, &a);
+  free(buf);
+  return rc;
+}
+
+/* Per-point ICE4_STEPPING on explicit inputs (test hook for point-level
+ * comparisons).  in: exn rho pres th rv rc rr ri rs rg cit ths rvs rcs rrs ris
+ * rss rgs cldfr sigs; out: the 7 state values after the step (external
+ * tendency removed), cit, rrevav, capped. */
+EXPORT int ice3o_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes, const double *in,
+                                double *out, int *outer, int *inner)
+{
+  StepOut s;
+  for (int v = 0; v < NV; ++v) { s.vart[v] = in[3 + v]; s.extpk[v] = in[11 + v]; }
+  s.cit = in[10];
+  s.rainfr = 1.0;
+  const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
+  ice4_stepping_point(c, lut, dt, max_passes, in[0], in[1], in[2], in[18], sigm ? 2.0 * in[19] : 0.0,
+                      0.0, 0.0, 0.0, 0.0, &s);
+  for (int v = 0; v < NV; ++v) out[v] = s.vart[v];
+  out[7] = s.cit; out[8] = s.rrevav; out[9] = s.capped;
+  *outer = s.outer; *inner = s.inner;
+  return 0;
+}

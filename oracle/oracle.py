@@ -22,7 +22,8 @@ _PKG = os.path.join(_REPO, "dwarf-p-ice3_gb300")
 if _PKG not in sys.path:
     sys.path.insert(0, _PKG)
 
-from ice3gb._abi import IceAdjustFields, RainIceFields, RainIceOptions, SedimentationFields  # noqa: E402
+from ice3gb._abi import (IceAdjustFields, RainIceFields, RainIceOptions, SedimentationFields, StepFields,  # noqa: E402
+                         STEP_IN, STEP_INOUT, STEP_OUT2, STEP_OUT3)
 from ice3gb.constants import ConstantsTable, Ice3gbConstants, Ice3gbLuts  # noqa: E402
 
 LIB_PATH = os.path.join(_HERE, "_build", "libice3_oracle.so")
@@ -229,3 +230,32 @@ def rainfr_vert(table, prfr, rr, rs, rg):
     a = [_f64(x) for x in (rr, rs, rg)]
     lib.ice3o_rainfr_vert(ctypes.byref(table.consts), nij, nk, _ptr(prfr), *[_ptr(x) for x in a])
     return prfr
+
+
+def physics_step(table, st: Dict[str, np.ndarray], dt: float, max_passes: int = 0, sed_jax: int = 0):
+    """Oracle chained step (ice3o_physics_step); `st` uses the StepFields names."""
+    lib = load()
+    keep = {k: _f64(st[k]) for k in STEP_IN}
+    nk, nij = keep["pabs"].shape
+    f = StepFields()
+    for k, v in keep.items():
+        setattr(f, k, _ptr(v))
+    for k in ("sea", "town"):
+        if st.get(k) is not None:
+            keep[k] = _f64(st[k])
+            setattr(f, k, _ptr(keep[k]))
+    out = {k: _f64(st[k]).copy() for k in STEP_INOUT}
+    out.update({k: np.empty((nk, nij)) for k in STEP_OUT3})
+    out.update({k: np.empty(nij) for k in STEP_OUT2})
+    for k, v in out.items():
+        setattr(f, k, _ptr(v))
+    opt = RainIceOptions(-1, -1, -1, max_passes, sed_jax)
+    bits = ctypes.c_uint32(0)
+    lib.ice3o_physics_step.argtypes = [ctypes.POINTER(Ice3gbConstants), ctypes.POINTER(Ice3gbLuts), ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_double, ctypes.POINTER(RainIceOptions),
+                                       ctypes.POINTER(StepFields), ctypes.POINTER(ctypes.c_uint32)]
+    rc = lib.ice3o_physics_step(ctypes.byref(table.consts), ctypes.byref(table.luts), nij, nk, dt, ctypes.byref(opt),
+                                ctypes.byref(f), ctypes.byref(bits))
+    if rc != 0:
+        raise RuntimeError(f"oracle physics_step returned {rc}")
+    return out, bits.value

@@ -42,3 +42,6 @@ def rel_err(a, b, floor_frac=1e-5):
     rms = float(np.sqrt(np.mean(b * b))) if b.size else 0.0
     floor = max(floor_frac * rms, 1e-300)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if b.size else 0.0
+
+
+from parity import assert_parity, sensitivity  # noqa: E402,F401

@@ -182,10 +182,11 @@ SedArgs sed_args(const Ice3gbSedimentationFields &f, int nij, int nk, double dt,
   return a;
 }
 
-int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                 const Ice3gbRainIceFields *f, cudaStream_t s)
+// Launch sequence of one rain_ice call.  `scr` holds 4 control words followed
+// by one pass key per grid point; the first 4 words are cleared here.
+int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                      const Ice3gbRainIceFields *f, unsigned int *scr, cudaStream_t s)
 {
-  const long n = (long)nij * nk;
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (h->c.LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (h->c.LDEPOSC != 0.0);
   const int max_passes = (opt && opt->max_passes > 0) ? opt->max_passes : 256;
@@ -205,14 +206,8 @@ int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptio
     ProfScope ps(h, K_SEDIM, s);
     if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
   }
-  // per-call scratch: 3 words + n keys, stream-ordered
-  unsigned int *scr = nullptr;
-  const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n);
-  if ((e = cudaMallocAsync(&scr, bytes, s)) != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
-  if ((e = cudaMemsetAsync(scr, 0, 4 * sizeof(unsigned int), s)) != cudaSuccess) {
-    cudaFreeAsync(scr, s);
+  if ((e = cudaMemsetAsync(scr, 0, 4 * sizeof(unsigned int), s)) != cudaSuccess)
     return cuda_fail(h, e, "cudaMemsetAsync");
-  }
   RainIceArgs a;
   a.f = *f;
   a.luts = h->d_luts;
@@ -229,7 +224,6 @@ int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptio
     ProfScope ps(h, K_EVAP_FIXUP, s);
     e = launch_rain_ice_evap_fixup(a, s);
   }
-  cudaFreeAsync(scr, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "rain_ice launch");
   if (lsedim_after) {
     ProfScope ps(h, K_SEDIM, s);
@@ -243,6 +237,20 @@ int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptio
     if ((e = launch_fog_deposition(c, fa, s)) != cudaSuccess) return cuda_fail(h, e, "fog launch");
   }
   return ICE3GB_OK;
+}
+
+// rain_ice with per-call scratch from the stream-ordered allocator.
+int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                 const Ice3gbRainIceFields *f, cudaStream_t s)
+{
+  const long n = (long)nij * nk;
+  unsigned int *scr = nullptr;
+  const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n);
+  cudaError_t e = cudaMallocAsync(&scr, bytes, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
+  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, scr, s);
+  cudaFreeAsync(scr, s);
+  return rc;
 }
 
 int validate_step(Handle *h, const Ice3gbStepFields *f)
@@ -333,6 +341,30 @@ int ensure_stage(Handle *h, size_t bytes)
 }
 
 }  // namespace
+
+// Validation + launch sequence with caller-provided scratch (used by the
+// entry point of rain_ice_noalloc.cu, which owns its static scratch).
+int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double dt,
+                                          const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
+                                          unsigned int *scratch, long scratch_points, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk))) return rc;
+  if ((long)nij * nk > scratch_points)
+    return fail(h, ICE3GB_ERR_RANGE, "nij*nk = %ld grid points exceeds the %ld-point static scratch",
+                (long)nij * nk, scratch_points);
+  if ((rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
+  if (!scratch) return fail(h, ICE3GB_ERR_CUDA, "static scratch address unavailable");
+  return run_rain_ice_core(h, nij, nk, dt, opt, f, scratch, static_cast<cudaStream_t>(stream));
+}
+
+// Records a CUDA error on the handle (or globally) for the other translation units.
+int ice3gb_internal_cuda_fail(void *handle, cudaError_t e, const char *where)
+{
+  return cuda_fail(as_handle(handle), e, where);
+}
 
 extern "C" {
 

@@ -81,8 +81,9 @@ EXPORTED = (
     "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status", "ice3gb_ice_adjust",
     "ice3gb_sedimentation", "ice3gb_rain_ice", "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host",
     "ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_profile_enable", "ice3gb_profile_read",
-    "ice3gb_kernel_name",
+    "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc",
 )
+NOALLOC_MAX_POINTS = 4194304
 KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition")
 
 _lib: Optional[ctypes.CDLL] = None
@@ -115,6 +116,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ice3gb_rain_ice.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                     ctypes.POINTER(RainIceOptions), ctypes.POINTER(RainIceFields), P]
     lib.ice3gb_rain_ice_host.argtypes = lib.ice3gb_rain_ice.argtypes
+    lib.ice3gb_rain_ice_noalloc.argtypes = lib.ice3gb_rain_ice.argtypes
+    lib.ice3gb_rain_ice_noalloc.restype = ctypes.c_int
     lib.ice3gb_physics_step.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                         ctypes.POINTER(RainIceOptions), ctypes.POINTER(StepFields), P]
     lib.ice3gb_physics_step_host.argtypes = lib.ice3gb_physics_step.argtypes

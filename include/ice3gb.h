@@ -243,6 +243,21 @@ int ice3gb_rain_ice(void *handle, int nij, int nk, double dt,
 int ice3gb_physics_step(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                         const Ice3gbStepFields *f, void *stream);
 
+/* ---- allocation-free rain_ice ------------------------------------------- */
+/* Same computation and arguments as ice3gb_rain_ice, for callers that must
+ * not allocate device memory during the call (a model that gives the GPU's
+ * memory to its own pool at start-up, or runs under a device-memory cap set
+ * outside the library).  Its scratch is a static device array
+ * inside the library, sized for ICE3GB_NOALLOC_MAX_POINTS grid points (16 MiB
+ * held on every GPU that loads the library, until exit); nij*nk above that is
+ * rejected with ICE3GB_ERR_RANGE.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  Calls that overlap on the GPU share the array and race:
+ * serialise them.  No counterpart exists in the reference. */
+#define ICE3GB_NOALLOC_MAX_POINTS 4194304
+int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                            const Ice3gbRainIceFields *f, void *stream);
+
 /* ---- per-kernel timing -------------------------------------------------- */
 /* While enabled, every kernel launch of the handle is bracketed by CUDA
  * events recorded on the caller's stream.  ice3gb_profile_read synchronises

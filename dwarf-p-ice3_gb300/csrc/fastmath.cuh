@@ -1,0 +1,239 @@
+// fastmath.cuh — FP64 exp, exp10 and log that spend as few FP64 instructions
+// as the result's 53 bits need.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate (a measured 1.0 TFLOP/s FMA),
+// and on it an FP64 compare, min/max or conversion costs as much as an FP64
+// FMA, while integer and FP32 instructions are almost free beside them.  The
+// microphysics kernels need a few dozen exp/log per grid point per sub-step,
+// so these functions do in FP64 only the steps that need 53 bits and move
+// the rest to the integer and FP32 pipes: range checks on the bit pattern,
+// the integer part of the argument reduction in FP32, int -> double by bit
+// construction, and the high-order polynomial terms (whose size is below
+// 2^-28 of the result, so FP32's 2^-24 suffices) in FP32.
+//
+//   fexp   P. T. P. Tang, "Table-driven implementation of the exponential
+//          function in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989:
+//          x = (256 m + j) ln2/256 + r, |r| <= ln2/512; e^x = 2^m 2^(j/256) e^r,
+//          2^(j/256) tabulated as a double + float pair, e^r - 1 by its Taylor
+//          series (r, r^2/2 in FP64; r^3/6 and beyond in FP32).  6 FP64 ops.
+//   fexp10 the same with log10(2)/256 and r scaled by ln 10.  7 FP64 ops.
+//   flog   P. T. P. Tang, "Table-driven implementation of the logarithm
+//          function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990,
+//          with the reduction made exact: x = 2^e z, z in [1, 2) split into
+//          128 intervals by its leading 7 fraction bits, intervals above
+//          sqrt(2) folded to [sqrt(1/2), 1) (e + 1); invc, a reciprocal of the
+//          interval's centre rounded to 8 significant bits, makes
+//          r = z*invc - 1 exact in one FMA (|r| < 2^-7); log x = e ln2 -
+//          log(invc) + log1p(r), log1p by its Taylor series (to r^4 in FP64,
+//          r^5 .. r^8 in FP32).  9 FP64 ops.
+//
+// Accuracy: within 2 ulp (tests compare the host build of this code with
+// 200-bit mpmath values, and the device build with the host build bit for
+// bit).  Every FP64 and FP32 operation is an explicit fma or a separately
+// rounded add/multiply, so host and device builds agree exactly.  Special
+// inputs (NaN, infinities, zero, negative, subnormal, overflow and underflow
+// ranges) leave the fast path through one integer test and get the IEEE
+// results of exp/log.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+#if !defined(__CUDACC__)
+#include <cmath>
+#endif
+
+#include "fastmath_tables.h"
+
+#if defined(__CUDACC__)
+#define FM_HD __host__ __device__ __forceinline__
+#else
+#define FM_HD inline
+#endif
+
+namespace fm {
+
+struct ExpEntry { double hi; float lo; int pad; };
+struct LogEntry { double invc, nlog_hi; float nlog_lo; int fold; double pad; };
+
+#if defined(__CUDA_ARCH__)
+__device__ const ExpEntry kExpTable[256] = FM_EXP_TABLE_INIT;
+__device__ const LogEntry kLogTable[128] = FM_LOG_TABLE_INIT;
+__device__ __forceinline__ void exp_entry(int j, double &hi, float &lo)
+{
+  const double2 v = __ldg(reinterpret_cast<const double2 *>(kExpTable) + j);
+  hi = v.x;
+  lo = __int_as_float((int)(uint32_t)__double_as_longlong(v.y));
+}
+__device__ __forceinline__ void log_entry(int i, double &invc, double &nlog_hi, float &nlog_lo, int &fold)
+{
+  const double2 *p = reinterpret_cast<const double2 *>(kLogTable) + 2 * i;
+  const double2 a = __ldg(p);
+  const float2 b = __ldg(reinterpret_cast<const float2 *>(p + 1));
+  invc = a.x; nlog_hi = a.y; nlog_lo = b.x; fold = __float_as_int(b.y);
+}
+__device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fmaf_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float addf_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float mulf_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ int64_t bits_(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double from_bits_(int64_t b) { return __longlong_as_double(b); }
+__device__ __forceinline__ int32_t fbits_(float x) { return __float_as_int(x); }
+__device__ __forceinline__ float ffrom_bits_(int32_t b) { return __int_as_float(b); }
+__device__ __forceinline__ int clz32_(uint32_t v) { return __clz((int)v); }
+#else
+static const ExpEntry kExpTable[256] = FM_EXP_TABLE_INIT;
+static const LogEntry kLogTable[128] = FM_LOG_TABLE_INIT;
+inline void exp_entry(int j, double &hi, float &lo) { hi = kExpTable[j].hi; lo = kExpTable[j].lo; }
+inline void log_entry(int i, double &invc, double &nlog_hi, float &nlog_lo, int &fold)
+{
+  invc = kLogTable[i].invc; nlog_hi = kLogTable[i].nlog_hi; nlog_lo = kLogTable[i].nlog_lo; fold = kLogTable[i].fold;
+}
+inline double fma_(double a, double b, double c) { return std::fma(a, b, c); }
+inline double add_(double a, double b) { volatile double s = a + b; return s; }
+inline double mul_(double a, double b) { volatile double s = a * b; return s; }
+inline float fmaf_(float a, float b, float c) { return std::fmaf(a, b, c); }
+inline float addf_(float a, float b) { volatile float s = a + b; return s; }
+inline float mulf_(float a, float b) { volatile float s = a * b; return s; }
+inline int64_t bits_(double x) { int64_t b; memcpy(&b, &x, 8); return b; }
+inline double from_bits_(int64_t b) { double x; memcpy(&x, &b, 8); return x; }
+inline int32_t fbits_(float x) { int32_t b; memcpy(&b, &x, 4); return b; }
+inline float ffrom_bits_(int32_t b) { float x; memcpy(&x, &b, 4); return x; }
+inline int clz32_(uint32_t v) { return v ? __builtin_clz(v) : 32; }
+#endif
+
+// double -> float by truncation of the significand, with integer operations
+// only; magnitudes below 2^-126 become zero.  For the small high-order terms
+// computed in FP32 the 2^-23 relative error is far below what they need.
+FM_HD float to_f32(double x)
+{
+  const int64_t b = bits_(x);
+  const int32_t e = (int32_t)((b >> 52) & 0x7ff) - 896;        // float biased exponent
+  const int32_t s = (int32_t)((uint64_t)b >> 32) & (int32_t)0x80000000;
+  if (e <= 0) return ffrom_bits_(s);
+  return ffrom_bits_(s | (e << 23) | (int32_t)((b >> 29) & 0x7fffff));
+}
+
+// float -> double, exact, with integer operations only (float zero and
+// subnormals give zero).
+FM_HD double to_f64(float x)
+{
+  const int32_t b = fbits_(x);
+  const int32_t e = (b >> 23) & 0xff;
+  const int64_t s = (int64_t)((uint64_t)((uint32_t)b & 0x80000000u) << 32);
+  if (e == 0) return from_bits_(s);
+  return from_bits_(s | ((int64_t)(e + 896) << 52) | ((int64_t)(b & 0x7fffff) << 29));
+}
+
+// int -> double, exact (|k| < 2^31), with integer operations only.
+FM_HD double i2d(int32_t k)
+{
+  if (k == 0) return 0.0;
+  const int64_t s = k < 0 ? (int64_t)(1ULL << 63) : 0;
+  const uint32_t a = k < 0 ? (uint32_t)(-(int64_t)k) : (uint32_t)k;
+  const int n = 31 - clz32_(a);                                  // index of the leading bit
+  const int64_t mant = ((int64_t)a << (52 - n)) & 0x000fffffffffffffLL;
+  return from_bits_(s | ((int64_t)(1023 + n) << 52) | mant);
+}
+
+// Nearest integer of a float with |t| < 2^22 (shifter trick, FP32 add).
+FM_HD int32_t rint_f32(float t)
+{
+  const float sh = 12582912.0f;                                  // 1.5 * 2^23
+  return fbits_(addf_(t, sh)) - fbits_(sh);
+}
+
+// 2^(k/256) * e^r * (1 - corr) for |r| <= ~ln2/512 and |corr| < 2^-40.
+FM_HD double exp_core(int32_t k, double r, float corr)
+{
+  const float rf = to_f32(r);
+  // (e^r - 1 - r - r^2/2) / r^3 = 1/6 + r/24 + r^2/120 (+ r^3/720 < 2^-31 of r^3/6)
+  float s = fmaf_(rf, 1.0f / 120.0f, 1.0f / 24.0f);
+  s = fmaf_(rf, s, 1.0f / 6.0f);
+  const double q = fma_(r, to_f64(s), 0.5);
+  const double p = fma_(mul_(r, r), q, r);                      // e^r - 1
+  double thi;
+  float tlo;
+  exp_entry(k & 255, thi, tlo);
+  // lo' = T_lo - T_hi*corr (both terms < 2^-38: FP32 carries them to 2^-62)
+  const float lo = fmaf_(-to_f32(thi), corr, tlo);
+  const double y = add_(thi, fma_(thi, p, to_f64(lo)));           // in [0.997, 2)
+  const int32_t m = k >> 8;
+  if (m >= -1021 && m <= 1022) return from_bits_(bits_(y) + (int64_t)m * ((int64_t)1 << 52));
+  // gradual underflow / overflow edges: scale in two steps
+  const double y1 = from_bits_(bits_(y) + (int64_t)(m / 2) * ((int64_t)1 << 52));
+  return mul_(y1, from_bits_((int64_t)(1023 + m - m / 2) << 52));
+}
+
+// e^x.
+FM_HD double fexp(double x)
+{
+  const int64_t ax = bits_(x) & 0x7fffffffffffffffLL;
+  if (ax > 0x40861f0000000000LL) {                               // |x| > 707.875, inf, NaN
+    if (ax > 0x7ff0000000000000LL) return x;                     // NaN
+    if (x > 709.782712893384) return from_bits_(0x7ff0000000000000LL);
+    if (x < -745.1332191019412) return 0.0;
+  }
+  const int32_t k = rint_f32(mulf_(to_f32(x), FM_INV_L256_F));   // |k| < 2^18; off by one at most
+  const double kd = i2d(k);
+  const double r = fma_(-kd, FM_L256_HI, x);                     // one rounding, < 2^-62
+  return exp_core(k, r, mulf_((float)k, FM_L256_LO_F));
+}
+
+// 10^x.
+FM_HD double fexp10(double x)
+{
+  const int64_t ax = bits_(x) & 0x7fffffffffffffffLL;
+  if (ax > 0x4073300000000000LL) {                               // |x| > 307, inf, NaN
+    if (ax > 0x7ff0000000000000LL) return x;
+    if (x > 308.2547155599167) return from_bits_(0x7ff0000000000000LL);
+    if (x < -323.60766413161369) return 0.0;
+  }
+  const int32_t k = rint_f32(mulf_(to_f32(x), FM_INV_LG256_F));
+  const double kd = i2d(k);
+  const double r10 = fma_(-kd, FM_LG256_HI, x);                  // |r10| <= ~log10(2)/512
+  return exp_core(k, mul_(r10, FM_LN10), mulf_(mulf_((float)k, FM_LG256_LO_F), FM_LN10_F));
+}
+
+// Natural logarithm.
+FM_HD double flog(double x)
+{
+  int64_t b = bits_(x);
+  int ebias = 0;
+  if (b < 0x0010000000000000LL || b >= 0x7ff0000000000000LL) {   // <= 0, subnormal, inf, NaN
+    if (x != x) return x;
+    if (x < 0.0) return from_bits_(0x7ff8000000000000LL);
+    if (x == 0.0) return from_bits_((int64_t)0xfff0000000000000ULL);
+    if (b >= 0x7ff0000000000000LL) return x;                      // +inf
+    x = mul_(x, 18014398509481984.0);                              // subnormal: * 2^54
+    b = bits_(x);
+    ebias = -54;
+  }
+  double invc, nlog_hi;
+  float nlog_lo;
+  int fold;
+  log_entry((int)((b >> 45) & 127), invc, nlog_hi, nlog_lo, fold);
+  const int32_t e = (int32_t)(b >> 52) - 1023 + ebias + fold;
+  const double z = from_bits_((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const double r = fma_(z, invc, -1.0);                          // exact
+  const double hi = fma_(i2d(e), FM_LN2_HI, nlog_hi);            // e*LN2_HI exact
+  const float lo = fmaf_((float)e, FM_LN2_LO_F, nlog_lo);        // < 2^-34: FP32 suffices
+  // (log1p(r) - r) / r^2 = -1/2 + r/3 - r^2/4 + r^3 s,  s = 1/5 - r/6 + r^2/7 - r^3/8
+  const float rf = to_f32(r);
+  float s = fmaf_(rf, -1.0f / 8.0f, 1.0f / 7.0f);
+  s = fmaf_(rf, s, -1.0f / 6.0f);
+  s = fmaf_(rf, s, 1.0f / 5.0f);
+  double q = fma_(r, to_f64(s), -0.25);
+  q = fma_(r, q, 1.0 / 3.0);
+  q = fma_(r, q, -0.5);
+  const double tail = fma_(mul_(r, r), q, to_f64(lo));
+  return add_(hi, add_(r, tail));
+}
+
+// x^a = e^(a log x) for x > 0 (relative error ~|a log x| ulp).
+FM_HD double fpow(double x, double a) { return fexp(mul_(a, flog(x))); }
+// x^a from a precomputed log x.
+FM_HD double fpowl(double logx, double a) { return fexp(mul_(a, logx)); }
+
+}  // namespace fm

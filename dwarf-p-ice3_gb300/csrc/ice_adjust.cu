@@ -54,10 +54,10 @@ ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaO
   double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
   if (c.LSUBG_COND != 0.0) {
     const double rt = x.rv + x.rc + x.ri;
-    // es_w and es_i share log(T) and 1/T (functions/tiwmx.py:18,60)
-    const double lt = log(t), it = 1.0 / t;
-    const double pv = nmin(exp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
-    const double piv = nmin(exp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
+    // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
+    const double lt = fm::flog(t), it = 1.0 / t;
+    const double pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
+    const double piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
     double frac = (x.rc + x.ri > 1e-20) ? x.rc / (x.rc + x.ri) : 0.0;
     const int fmode = (int)c.FRAC_ICE_ADJUST;
     if (fmode == 3) frac = nclip01(frac);
@@ -79,7 +79,7 @@ ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaO
     const double q1 = sbar / sigma;
     double cond;
     if (q1 > 0.0) cond = (q1 <= 2.0) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;
-    else cond = exp(1.2 * q1 - 1.0);
+    else cond = fm::fexp(1.2 * q1 - 1.0);
     cond *= sigma;
     cldfr = (cond >= 1e-12) ? nclip01(0.5 + 0.36 * atan(1.55 * q1)) : 0.0;
     if (cldfr == 0.0) cond = 0.0;
@@ -115,7 +115,7 @@ ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaO
     const int mfpdf = (int)c.SUBG_MF_PDF;
     if (mfpdf == 0 || mfpdf == 1) {
       const double criaut = c.CRIAUTC / x.rho;
-      const double criaut_i = nmin(c.CRIAUTI, exp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+      const double criaut_i = nmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
       if (mfpdf == 0) {
         if (w1m * dt > x.cf_mf * criaut) { hlc_hrc = w1m * dt; hlc_hcf = nmin(1.0, x.cf_mf); }
         if (w2m * dt > x.cf_mf * criaut_i) { hli_hri = w2m * dt; hli_hcf = nmin(1.0, x.cf_mf); }

@@ -14,7 +14,7 @@
 //    thread chunks from a global counter, which balances the data-dependent
 //    number of sub-steps across SMs;
 //  * every per-point quantity that is fixed over the sub-steps (log rho and
-//    the rho powers) is computed once; real powers are exp(a*log x) with the
+//    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;
 //  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
 //    after the last pass of the call, mode_ice4_stepping.F90:514-516) is
@@ -83,8 +83,8 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
       }
       zrvheni = fmin(rvs, zrvheni * inv_dt);
       if (micro) {
-        pf.lrho = log(pf.rho);
-        pf.rho_mcexvt = exp(-c.CEXVT * pf.lrho);
+        pf.lrho = fm::flog(pf.rho);
+        pf.rho_mcexvt = fm::fexp(-c.CEXVT * pf.lrho);
         pf.rho_mcexvt1 = pf.rho_mcexvt / pf.rho;
         pf.rcrautc = c.CRIAUTC / pf.rho;
         pf.cf = ld1(f.cldfr, p);

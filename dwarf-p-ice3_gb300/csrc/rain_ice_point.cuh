@@ -59,7 +59,7 @@ struct Pass {
 
 ICE3_HD double esat_from(double alp, double beta, double gam, double it, double lt)
 {
-  return exp(alp - beta * it - gam * lt);
+  return fm::fexp(alp - beta * it - gam * lt);
 }
 
 // ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.).
@@ -68,7 +68,7 @@ ICE3_HD void nucleation(const Cst &c, bool ld, double tht, double pabst, double 
 {
   rvheni = 0.0;
   if (!(ld && t < c.TT && rvt > c.V_RTMIN)) return;
-  const double lt = log(t), it = 1.0 / t;
+  const double lt = fm::flog(t), it = 1.0 / t;
   double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   double zzw = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
   zzw = fmin(pabst * 0.5, zzw);
@@ -78,9 +78,9 @@ ICE3_HD void nucleation(const Cst &c, bool ld, double tht, double pabst, double 
   zssi = fmin(zssi, zusw);
   zzw = 0.0;
   if (t < c.TT - 5.0 && zssi > 0.0) {
-    zzw = c.NU20 * exp(c.ALPHA2 * zssi - c.BETA2);
+    zzw = c.NU20 * fm::fexp(c.ALPHA2 * zssi - c.BETA2);
   } else if (t <= c.TT - 2.0 && t >= c.TT - 5.0 && zssi > 0.0) {
-    zzw = fmax(c.NU20 * exp(-c.BETA2), c.NU10 * exp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * log(zssi / zusw)));
+    zzw = fmax(c.NU20 * fm::fexp(-c.BETA2), c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(zssi / zusw)));
   }
   zzw = fmin(zzw - cit, 50.e3);
   rvheni = fmin(rvt, fmax(zzw, 0.0) * c.MNU0 / rhodref);
@@ -155,7 +155,7 @@ ICE3_HD double compute_pdf(const Cst &c, bool ld, double rcrautc_pt, double rct,
     }
   }
   hl[0] = hcf; hl[1] = lcf; hl[2] = hrc; hl[3] = lrc;
-  const double criauti = ld ? fmin(c.CRIAUTI, exp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI)) : 0.0;
+  const double criauti = ld ? fmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI)) : 0.0;
   double ihcf = 0, ilcf = 0, ihri = 0, ilri = 0;
   if (aucv_ri == 0) {
     if (rit > criauti && ld) { ihcf = 1.0; ihri = rit; }
@@ -172,7 +172,7 @@ ICE3_HD double compute_pdf(const Cst &c, bool ld, double rcrautc_pt, double rct,
   return ld ? fmax(hl[0], hi[0]) : 0.0;
 }
 
-// INTERP_MICRO (micro/interp_micro.func.h, packed path): index from log(x).
+// INTERP_MICRO (micro/interp_micro.func.h, packed path): index from fm::flog(x).
 ICE3_HD double lut_index(double logx, double knum, double p1, double p2, int &i)
 {
   const double z = fmax(1.00001, fmin(knum - 0.00001, p1 * logx + p2));
@@ -192,22 +192,22 @@ ICE3_HD double lut2d(const double *lt, int n2, int i1, double f1, int i2, double
 ICE3_HD void slopes(const Cst &c, const PointFix &pf, Pass &x)
 {
   if (x.v[IRR] > 0.) {
-    x.llbdar = log(c.LBR) + c.LBEXR * (pf.lrho + log(fmax(x.v[IRR], c.R_RTMIN)));
-    x.lbdar = exp(x.llbdar);
+    x.llbdar = fm::flog(c.LBR) + c.LBEXR * (pf.lrho + fm::flog(fmax(x.v[IRR], c.R_RTMIN)));
+    x.lbdar = fm::fexp(x.llbdar);
   } else { x.lbdar = 0.0; x.llbdar = -INFINITY; }
   if (c.LSNOW_T != 0.0) {
     if (x.v[IRS] > 0.) {
-      const double e = (x.t > 263.15) ? exp10(14.554 - 0.0423 * x.t) : exp10(6.226 - 0.0106 * x.t);
+      const double e = (x.t > 263.15) ? fm::fexp10(14.554 - 0.0423 * x.t) : fm::fexp10(6.226 - 0.0106 * x.t);
       x.lbdas = fmax(fmin(c.LBDAS_MAX, e), c.LBDAS_MIN) * c.TRANS_MP_GAMMAS;
-      x.llbdas = log(x.lbdas);
+      x.llbdas = fm::flog(x.lbdas);
     } else { x.lbdas = 0.0; x.llbdas = -INFINITY; }
   } else if (x.v[IRS] > 0.) {
-    x.llbdas = fmin(log(c.LBDAS_MAX), log(c.LBS) + c.LBEXS * (pf.lrho + log(fmax(x.v[IRS], c.S_RTMIN))));
-    x.lbdas = exp(x.llbdas);
+    x.llbdas = fmin(fm::flog(c.LBDAS_MAX), fm::flog(c.LBS) + c.LBEXS * (pf.lrho + fm::flog(fmax(x.v[IRS], c.S_RTMIN))));
+    x.lbdas = fm::fexp(x.llbdas);
   } else { x.lbdas = 0.0; x.llbdas = -INFINITY; }
   if (x.v[IRG] > 0.) {
-    x.llbdag = log(c.LBG) + c.LBEXG * (pf.lrho + log(fmax(x.v[IRG], c.G_RTMIN)));
-    x.lbdag = exp(x.llbdag);
+    x.llbdag = fm::flog(c.LBG) + c.LBEXG * (pf.lrho + fm::flog(fmax(x.v[IRG], c.G_RTMIN)));
+    x.lbdag = fm::fexp(x.llbdag);
   } else { x.lbdag = 0.0; x.llbdag = -INFINITY; }
 }
 
@@ -268,15 +268,15 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
     B[IRG] = b[B_RRHONG_MR];
     // derived fields (mode_ice4_tendencies.F90:303-320)
-    lt = log(x.t);
+    lt = fm::flog(x.t);
     it = 1.0 / x.t;
     esi = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
     esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
     R.ssi = x.v[IRV] * (pf.pres - esi) / (c.EPSILO * esi) - 1.0;
     R.ka = 2.38e-2 + 7.1e-5 * (x.t - c.TT);
-    R.dv = 2.11e-5 * exp(1.94 * (lt - log(c.TT))) * (c.P00 / pf.pres);
+    R.dv = 2.11e-5 * fm::fexp(1.94 * (lt - fm::flog(c.TT))) * (c.P00 / pf.pres);
     R.ai = sq(c.LSTT + (c.CPV - c.CI) * (x.t - c.TT)) / (R.ka * c.RV * x.t * x.t) + (c.RV * x.t) / (R.dv * esi);
-    R.cj = c.SCFAC * exp(0.3 * pf.lrho) / sqrt(1.718e-5 + 4.9e-8 * (x.t - c.TT));
+    R.cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) / sqrt(1.718e-5 + 4.9e-8 * (x.t - c.TT));
   }
   const double zrainfr = compute_pdf(c, true, pf.rcrautc, x.v[IRC], x.v[IRI], pf.cf, x.t, pf.sigma_rc, hl, hi);
   const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
@@ -292,27 +292,27 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
 
   // ---- ICE4_SLOW (mode_ice4_slow.F90) ----
   if (t < c.TT - 35.0 && v[IRC] > c.C_RTMIN) {
-    if (!soft) b[B_RCHONI] = fmin(1000., c.HON * rho * v[IRC] * exp(c.ALPHA3 * (t - c.TT) - c.BETA3));
+    if (!soft) b[B_RCHONI] = fmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3));
   } else b[B_RCHONI] = 0.0;
   if (v[IRV] > c.V_RTMIN && v[IRS] > c.S_RTMIN) {
     if (!soft)
       b[B_RVDEPS] = (R.ssi / (rho * R.ai)) *
-                    (c.O0DEPS * exp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * exp(c.EX1DEPS * x.llbdas));
+                    (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas));
   } else b[B_RVDEPS] = 0.0;
   if (v[IRI] > c.I_RTMIN && v[IRS] > c.S_RTMIN) {
     if (!soft)
-      b[B_RIAGGS] = c.FIAGGS * exp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * x.llbdas) * v[IRI] * pf.rho_mcexvt;
+      b[B_RIAGGS] = c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * x.llbdas) * v[IRI] * pf.rho_mcexvt;
   } else b[B_RIAGGS] = 0.0;
   if (hi[2] > c.I_RTMIN) {
     if (!soft) {
-      const double criauti = fmin(c.CRIAUTI, exp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
-      b[B_RIAUTS] = c.TIMAUTI * exp(c.TEXAUTI * (t - c.TT)) * fmax(hi[2] - criauti * hi[0], 0.0);
+      const double criauti = fmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+      b[B_RIAUTS] = c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * fmax(hi[2] - criauti * hi[0], 0.0);
     }
   } else b[B_RIAUTS] = 0.0;
   if (v[IRV] > c.V_RTMIN && v[IRG] > c.G_RTMIN) {
     if (!soft)
       b[B_RVDEPG] = (R.ssi / (rho * R.ai)) *
-                    (c.O0DEPG * exp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * exp(c.EX1DEPG * x.llbdag));
+                    (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag));
   } else b[B_RVDEPG] = 0.0;
 
   // ---- ICE4_WARM (mode_ice4_warm.F90), SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE ----
@@ -321,14 +321,14 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
       if (!soft) b[B_RCAUTR] = c.TIMAUTC * fmax(hl[2] - hl[0] * pf.rcrautc, 0.0);
     } else b[B_RCAUTR] = 0.0;
     if (v[IRC] > c.C_RTMIN && v[IRR] > c.R_RTMIN) {
-      if (!soft) b[B_RCACCR] = c.FCACCR * v[IRC] * exp(c.EXCACCR * x.llbdar) * pf.rho_mcexvt;
+      if (!soft) b[B_RCACCR] = c.FCACCR * v[IRC] * fm::fexp(c.EXCACCR * x.llbdar) * pf.rho_mcexvt;
     } else b[B_RCACCR] = 0.0;
     if (v[IRR] > c.R_RTMIN && v[IRC] <= c.C_RTMIN) {
       if (!soft) {
         const double usw = 1. - v[IRV] * (pf.pres - esw) / (c.EPSILO * esw);
         const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / (R.ka * c.RV * t * t) + (c.RV * t) / (R.dv * esw);
         b[B_RREVAV] = (fmax(0., usw) / (rho * av)) *
-                      (c.O0EVAR * exp(c.EX0EVAR * x.llbdar) + c.O1EVAR * R.cj * exp(c.EX1EVAR * x.llbdar));
+                      (c.O0EVAR * fm::fexp(c.EX0EVAR * x.llbdar) + c.O1EVAR * R.cj * fm::fexp(c.EX1EVAR * x.llbdar));
       }
     } else b[B_RREVAV] = 0.0;
   } else {
@@ -342,7 +342,7 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     if (!soft) {
       const double den = 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t)));
       rs[RS_FREEZ1] = heat_term(c, R, t, esi, v[IRV], pf.pres) *
-                      (c.O0DEPS * exp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * exp(c.EX1DEPS * x.llbdas)) * den;
+                      (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas)) * den;
       rs[RS_FREEZ2] = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
     }
     freez = fmax(0., fmax(0., rs[RS_FREEZ1] + rs[RS_FREEZ2] * b[B_RIAGGS]) - b[B_RIAGGS]);
@@ -358,12 +358,12 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     const double zw1 = lut1d(lut + O_RIM1, i, fr);
     const double zw2 = lut1d(lut + O_RIM2, i, fr);
     const double zw3 = lut1d(lut + O_RIM4, i, fr);
-    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * exp(c.EXCRIMSS * x.llbdas) * pf.rho_mcexvt;
-    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * exp(c.EXCRIMSG * x.llbdas) * pf.rho_mcexvt;
+    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * fm::fexp(c.EXCRIMSS * x.llbdas) * pf.rho_mcexvt;
+    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * fm::fexp(c.EXCRIMSG * x.llbdas) * pf.rho_mcexvt;
     if ((int)c.SNOW_RIMING == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
-      const double r = c.SRIMCG * exp(c.EXSRIMCG * x.llbdas) * (1.0 - zw2);
-      rs[RS_RSRIMCG] = zzw * r / fmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * exp(c.EXSRIMCG2 * x.llbdas) * (1. - zw3) -
+      const double r = c.SRIMCG * fm::fexp(c.EXSRIMCG * x.llbdas) * (1.0 - zw2);
+      rs[RS_RSRIMCG] = zzw * r / fmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * x.llbdas) * (1. - zw3) -
                                                  c.SRIMCG3 * r);
     } else rs[RS_RSRIMCG] = 0.0;
   }
@@ -390,11 +390,11 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
       const double zw2 = lut2d(lut + O_RACCS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
       const double zw3 = lut2d(lut + O_SACCRG, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
       const double ilr = 1.0 / x.lbdar, ils = 1.0 / x.lbdas;
-      const double zzw = c.FRACCSS * exp(c.CXS * x.llbdas) * pf.rho_mcexvt1 *
+      const double zzw = c.FRACCSS * fm::fexp(c.CXS * x.llbdas) * pf.rho_mcexvt1 *
                          (c.LBRACCS1 * ils * ils + c.LBRACCS2 * ils * ilr + c.LBRACCS3 * ilr * ilr) * sq(sq(ilr));
       rs[RS_RRACCSS] = zw1 * zzw;
       rs[RS_RRACCS] = zw2 * zzw;
-      rs[RS_RSACCRG] = c.FSACCRG * zw3 * exp((c.CXS - c.BS) * x.llbdas) * pf.rho_mcexvt1 *
+      rs[RS_RSACCRG] = c.FSACCRG * zw3 * fm::fexp((c.CXS - c.BS) * x.llbdas) * pf.rho_mcexvt1 *
                        (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr;
     }
   }
@@ -412,8 +412,8 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   if (v[IRS] > c.S_RTMIN && t > c.TT) {
     if (!soft) {
       const double h = heat_term(c, R, t, esw, v[IRV], pf.pres);
-      b[B_RSMLTG] = c.FSCVMG * fmax(0., (-h * (c.O0DEPS * exp(c.EX0DEPS * x.llbdas) +
-                                               c.O1DEPS * R.cj * exp(c.EX1DEPS * x.llbdas)) -
+      b[B_RSMLTG] = c.FSCVMG * fmax(0., (-h * (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) +
+                                               c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas)) -
                                          (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c.CL * (c.TT - t))) /
                                             (rho * c.LMTT));
       b[B_RCMLTSR] = rs[RS_RCRIMS];
@@ -426,8 +426,8 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   double *rg = R.rg;
   if (v[IRI] > c.I_RTMIN && v[IRR] > c.R_RTMIN) {
     if (!soft) {
-      b[B_RICFRRG] = c.ICFRR * v[IRI] * exp(c.EXICFRR * x.llbdar) * pf.rho_mcexvt;
-      b[B_RRCFRIG] = c.RCFRI * cit * exp(c.EXRCFRI * x.llbdar) * pf.rho_mcexvt1;
+      b[B_RICFRRG] = c.ICFRR * v[IRI] * fm::fexp(c.EXICFRR * x.llbdar) * pf.rho_mcexvt;
+      b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * x.llbdar) * pf.rho_mcexvt1;
       if (c.LCRFLIMIT != 0.0) {
         const double zw = fmax(0., fmin(1., (b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t) /
                                                 fmax(1.e-20, c.LVTT * b[B_RRCFRIG])));
@@ -439,13 +439,13 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   } else {
     b[B_RICFRRG] = b[B_RRCFRIG] = b[B_RICFRR] = 0.0;
   }
-  const double base_g = exp((c.CXG - c.DG - 2.) * x.llbdag) * pf.rho_mcexvt;
+  const double base_g = fm::fexp((c.CXG - c.DG - 2.) * x.llbdag) * pf.rho_mcexvt;
   if (v[IRG] > c.G_RTMIN && v[IRC] > c.C_RTMIN) {
     if (!soft) rg[RG_RCDRYG] = c.FCDRYG * v[IRC] * base_g;
   } else rg[RG_RCDRYG] = 0.0;
   if (v[IRG] > c.G_RTMIN && v[IRI] > c.I_RTMIN) {
     if (!soft) {
-      const double e = exp(c.COLEXIG * (t - c.TT));
+      const double e = fm::fexp(c.COLEXIG * (t - c.TT));
       rg[RG_RIDRYG] = c.FIDRYG * e * v[IRI] * base_g;
       rg[RG_RIWETG] = rg[RG_RIDRYG] / (c.COLIG * e);
     }
@@ -458,9 +458,9 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     const double f2 = lut_index(x.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
     const double zw = lut2d(lut + O_SDRYG, ICE3GB_NDRYLBDAS, i1, f1, i2, f2);
     const double ilg = 1.0 / x.lbdag, ils = 1.0 / x.lbdas;
-    rg[RG_RSWETG] = c.FSDRYG * zw / c.COLSG * exp((c.CXS - c.BS) * x.llbdas + c.CXG * x.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RSWETG] = c.FSDRYG * zw / c.COLSG * fm::fexp((c.CXS - c.BS) * x.llbdas + c.CXG * x.llbdag) * pf.rho_mcexvt1 *
                     (c.LBSDRYG1 * ilg * ilg + c.LBSDRYG2 * ilg * ils + c.LBSDRYG3 * ils * ils);
-    rg[RG_RSDRYG] = rg[RG_RSWETG] * c.COLSG * exp(c.COLEXSG * (t - c.TT));
+    rg[RG_RSDRYG] = rg[RG_RSWETG] * c.COLSG * fm::fexp(c.COLEXSG * (t - c.TT));
   }
   const bool gdry_r = v[IRR] > c.R_RTMIN && v[IRG] > c.G_RTMIN;
   if (!gdry_r) rg[RG_RRDRYG] = 0.0;
@@ -470,7 +470,7 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     const double f2 = lut_index(x.llbdar, c.NDRYLBDAR, c.DRYINTP1R, c.DRYINTP2R, i2);
     const double zw = lut2d(lut + O_RDRYG, ICE3GB_NDRYLBDAR, i1, f1, i2, f2);
     const double ilg = 1.0 / x.lbdag, ilr = 1.0 / x.lbdar;
-    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * exp(c.CXG * x.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * fm::fexp(c.CXG * x.llbdag) * pf.rho_mcexvt1 *
                     (c.LBRDRYG1 * ilg * ilg + c.LBRDRYG2 * ilg * ilr + c.LBRDRYG3 * ilr * ilr);
   }
   const double rdryg_init = rg[RG_RCDRYG] + rg[RG_RIDRYG] + rg[RG_RSDRYG] + rg[RG_RRDRYG];
@@ -480,7 +480,7 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
     if (!soft) {
       const double den = 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t)));
       rg[RG_FREEZ1] = heat_term(c, R, t, esi, v[IRV], pf.pres) *
-                      (c.O0DEPG * exp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * exp(c.EX1DEPG * x.llbdag)) * den;
+                      (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag)) * den;
       rg[RG_FREEZ2] = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
     }
     const double is = rg[RG_RIWETG] + rg[RG_RSWETG];
@@ -514,7 +514,7 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   if (v[IRG] > c.G_RTMIN && t > c.TT) {
     if (!soft) {
       const double h = heat_term(c, R, t, esw, v[IRV], pf.pres);
-      b[B_RGMLTR] = fmax(0., (-h * (c.O0DEPG * exp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * exp(c.EX1DEPG * x.llbdag)) -
+      b[B_RGMLTR] = fmax(0., (-h * (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag)) -
                               (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c.CL * (c.TT - t))) /
                                  (rho * c.LMTT));
     }
@@ -523,8 +523,8 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
   if (R.ssi > 0. && v[IRC] > c.C_RTMIN && v[IRI] > c.I_RTMIN && cit > 1.e-20) {
     if (!soft) {
-      const double l = fmin(1.e8, c.LBI * exp(c.LBEXI * log(rho * v[IRI] / cit)));
-      b[B_RCBERI] = (R.ssi / (rho * R.ai)) * cit * (c.O0DEPI / l + c.O2DEPI * R.cj * R.cj * exp(-(c.DI + 2.0) * log(l)));
+      const double l = fmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(rho * v[IRI] / cit)));
+      b[B_RCBERI] = (R.ssi / (rho * R.ai)) * cit * (c.O0DEPI / l + c.O2DEPI * R.cj * R.cj * fm::fexp(-(c.DI + 2.0) * fm::flog(l)));
     }
   } else b[B_RCBERI] = 0.0;
 

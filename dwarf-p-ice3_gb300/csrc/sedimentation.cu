@@ -40,32 +40,32 @@ ICE3_HD CloudPar cloud_params(const Cst &c, bool fortran, bool has_st, double se
     conc = (1.0 - town) * ((1.0 - sea) * c.CONC_LAND + sea * c.CONC_SEA) + town * c.CONC_URBAN;
   }
   CloudPar p;
-  p.log_lbc_conc = log(lbc * conc);
+  p.log_lbc_conc = fm::flog(lbc * conc);
   p.ray_inv = 1.0 / ray;
   p.fsedc = fsedc;
   return p;
 }
 
-// Fall speed for content r (> threshold checked by the caller); lrho = log(rho).
+// Fall speed for content r (> threshold checked by the caller); lrho = fm::flog(rho).
 ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlbda, const CloudPar &cp)
 {
-  const double lr = log(r);
+  const double lr = fm::flog(r);
   switch (s) {
     case 0: {  // cloud droplets: sedimentation.py:206-209, F90:264-267
       const double lwlbdc = c.LBEXC * (cp.log_lbc_conc - lrho - lr);
-      const double cc = c.CC * (1.0 + 1.26 * wlbda * exp(lwlbdc) * cp.ray_inv);
-      return exp(-c.CEXVT * lrho - c.DC * lwlbdc) * cc * cp.fsedc;
+      const double cc = c.CC * (1.0 + 1.26 * wlbda * fm::fexp(lwlbdc) * cp.ray_inv);
+      return fm::fexp(-c.CEXVT * lrho - c.DC * lwlbdc) * cc * cp.fsedc;
     }
     case 1:  // rain
-      return c.FSEDR * exp((c.EXSEDR - 1.0) * lr + (c.EXSEDR - c.CEXVT - 1.0) * lrho);
+      return c.FSEDR * fm::fexp((c.EXSEDR - 1.0) * lr + (c.EXSEDR - c.CEXVT - 1.0) * lrho);
     case 2: {  // pristine ice: sedimentation.py:46-55, F90:307-311
       const double dmax_ = fmax(0.05e6, -0.15319e6 - 0.021454e6 * (lrho + lr));
-      return c.FSEDI * exp(-c.CEXVT * lrho + c.EXCSEDI * log(dmax_));
+      return c.FSEDI * fm::fexp(-c.CEXVT * lrho + c.EXCSEDI * fm::flog(dmax_));
     }
     case 3:  // snow
-      return c.FSEDS * exp((c.EXSEDS - 1.0) * lr + (c.EXSEDS - c.CEXVT - 1.0) * lrho);
+      return c.FSEDS * fm::fexp((c.EXSEDS - 1.0) * lr + (c.EXSEDS - c.CEXVT - 1.0) * lrho);
     default:  // graupel
-      return c.FSEDG * exp((c.EXSEDG - 1.0) * lr + (c.EXSEDG - c.CEXVT - 1.0) * lrho);
+      return c.FSEDG * fm::fexp((c.EXSEDG - 1.0) * lr + (c.EXSEDG - c.CEXVT - 1.0) * lrho);
   }
 }
 
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) sedimentation_kernel(const __grid_constan
     const bool c1 = rt > rtmin, c2 = qp > rtmin;
     double w1 = 0.0, w2 = 0.0;
     if (c1 || c2) {
-      const double lrho = log(rho);
+      const double lrho = fm::flog(rho);
       if (c1) w1 = fall_speed(c, s, rt, lrho, wlbda, cp);
       if (c2) w2 = fall_speed(c, s, qp, lrho, wlbda, cp);
     }

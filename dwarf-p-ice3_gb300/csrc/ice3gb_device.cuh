@@ -54,6 +54,31 @@ ICE3_HD double nmin(double a, double b) { return (a < b || a != a) ? a : b; }
 ICE3_HD double nmax(double a, double b) { return (a > b || a != a) ? a : b; }
 ICE3_HD double nclip01(double x) { return nmin(nmax(x, 0.0), 1.0); }
 
+// Comparisons and clamps on the IEEE bit patterns.  On GB300 an FP64 compare
+// (and so fmin/fmax) issues on the FP64 pipe at the FP64 FMA rate, while the
+// same test on the 64-bit pattern runs on the integer pipe at ~30x the rate.
+// Ordering key: for finite and infinite doubles, the signed 64-bit integer
+// bits ^ (sign ? 0x7fff... : 0) is monotone in the value (-0 sorts just below
+// +0).  NaN operands are not supported: callers use these on values that are
+// finite by construction.
+ICE3_HD int64_t dkey(double x)
+{
+  const int64_t b = fm::bits_(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+ICE3_HD bool gtd(double a, double b) { return dkey(a) > dkey(b); }        // a > b
+ICE3_HD bool ltd(double a, double b) { return dkey(a) < dkey(b); }        // a < b
+// a > b for a threshold b >= +0 (a of any sign): the raw patterns suffice.
+ICE3_HD bool gtp(double a, double b) { return fm::bits_(a) > fm::bits_(b); }
+// a < b for a >= +0 (b of any sign >= +0).
+ICE3_HD bool ltp(double a, double b) { return fm::bits_(a) < fm::bits_(b); }
+ICE3_HD bool pos(double a) { return fm::bits_(a) > 0; }                   // a > 0
+ICE3_HD double pmax0(double a) { return pos(a) ? a : 0.0; }               // fmax(0, a)
+ICE3_HD double dmax(double a, double b) { return gtd(a, b) ? a : b; }
+ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
+// |a| > b for b >= +0.
+ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > fm::bits_(b); }
+
 // x**a evaluated as exp(a*log(x)) with the FP64-lean exp/log of
 // fastmath.cuh.  For the exponents of the scheme (|a*log x| < 60) this stays
 // within ~1e-14 relative of pow(), well inside the 1e-10 parity bar, at a

@@ -37,7 +37,9 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
                                                                          const __grid_constant__ RainIceArgs a)
 {
   extern __shared__ double lut[];
+  __shared__ Derived dsh;
   for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
+  if (threadIdx.x == 0) make_derived(c, dsh);
   __shared__ unsigned int chunk;
   __syncthreads();
   const Ice3gbRainIceFields &f = a.f;
@@ -72,16 +74,17 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
       const double izdev = 1.0 / zdev;
       const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * izdev;
       const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * izdev;
-      const bool micro = rc > c.C_RTMIN || rr > c.R_RTMIN || ri > c.I_RTMIN || rs > c.S_RTMIN || rg > c.G_RTMIN;
+      const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
+                         gtp(rg, c.G_RTMIN);
       const double iexnref = 1.0 / exnref;
       const double lsx = lsf * iexnref, lvx = lvf * iexnref;
       double evap = 0.0, rainfr = 1.0;
       double zrvheni = 0.0;
       if (!micro) {
         cit = 0.0;
-        nucleation(c, true, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
+        nucleation(c, dsh, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
       }
-      zrvheni = fmin(rvs, zrvheni * inv_dt);
+      zrvheni = dmin(rvs, zrvheni * inv_dt);
       if (micro) {
         pf.lrho = fm::flog(pf.rho);
         pf.rho_mcexvt = fm::fexp(-c.CEXVT * pf.lrho);
@@ -97,12 +100,12 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
           hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
           hl[3] = rc - hl[2];
           hi[3] = ri - hi[2];
-          hl[1] = (rc > 0.) ? pf.cf - hl[0] : 0.;
-          hi[1] = (ri > 0.) ? pf.cf - hi[0] : 0.;
+          hl[1] = pos(rc) ? pf.cf - hl[0] : 0.;
+          hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
         }
         double rrevav;
         bool capped;
-        key = stepping(c, lut, pf, dt, a.max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
+        key = stepping(c, dsh, lut, pf, dt, a.max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
         any_capped |= capped;
 #pragma unroll
         for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
@@ -125,19 +128,19 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
       }
       // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the sources
       double w;
-      w = rcs - fmax(rcs, 0.); rvs += w; ths -= w * lvx; rcs -= w;
-      w = rrs - fmax(rrs, 0.); rvs += w; ths -= w * lvx; rrs -= w;
-      w = ris - fmax(ris, 0.); rvs += w; ths -= w * lsx; ris -= w;
-      w = rss - fmax(rss, 0.); rvs += w; ths -= w * lsx; rss -= w;
-      w = rgs - fmax(rgs, 0.); rvs += w; ths -= w * lsx; rgs -= w;
-      w = fmin(1., fmax(c.V_RTMIN - rvs, 0.) / fmax(rcs + ris, 1.e-20));
+      w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
+      w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
+      w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
+      w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
+      w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
+      w = dmin(1., pmax0(c.V_RTMIN - rvs) / dmax(rcs + ris, 1.e-20));
       ths -= w * (rcs * lvx + ris * lsx);
       rvs += w * (rcs + ris);
       rcs = (1. - w) * rcs;
       ris = (1. - w) * ris;
-      w = fmin(fmax(rrs, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rrs -= w; ths -= w * lvx;
-      w = fmin(fmax(rss, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rss -= w; ths -= w * lsx;
-      w = fmin(fmax(rgs, 0.), fmax(c.V_RTMIN - rvs, 0.)); rvs += w; rgs -= w; ths -= w * lsx;
+      w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
+      w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
+      w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
       f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
       f.rgs[p] = rgs;
       f.cit[p] = cit;

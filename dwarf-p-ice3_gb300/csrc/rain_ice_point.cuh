@@ -1,15 +1,27 @@
 // rain_ice_point.cuh — per-grid-point ICE4 physics of the rain_ice kernel
 // (nucleation, compute_pdf, the slow/warm/fast processes, ICE4_TENDENCIES and
-// ICE4_STEPPING for one point).  Host-and-device code: the kernel in
-// rain_ice.cu runs it per lane; a host build of the same code serves to
-// separate algorithmic from math-library differences when comparing with a
-// CPU reference.
+// ICE4_STEPPING for one point).  Host-and-device code; the kernel in
+// rain_ice.cu runs it per lane.
+//
+// FP64 economy (GB300 issues FP64 at 1/64 of the FP32 rate; an FP64 compare
+// costs as much as an FMA, integer work is nearly free):
+//  * exp/log/exp10 are the table-driven versions of fastmath.cuh;
+//  * threshold tests and clamps run on the IEEE bit patterns (integer pipe),
+//    see gtp/pos/dmin/dmax in ice3gb_device.cuh;
+//  * what several processes share is computed once per hard pass: the
+//    ventilation factors of snow and graupel (deposition, freezing and
+//    melting all use O0DEP lbda^EX0DEP + O1DEP cj lbda^EX1DEP), the
+//    vapour/heat term of the freezing and melting rates, the reciprocal
+//    slopes, ssi/(rho ai), the collision-freezing denominator, and the ice
+//    autoconversion threshold that compute_pdf also needs;
+//  * soft passes (rates frozen at their hard-pass values) skip the slope
+//    parameters, which only the hard-pass rates use;
+//  * logs of table constants are computed once per block (Derived).
 #pragma once
 
 #include "ice3gb_device.cuh"
 
 namespace ice3pt {
-
 
 constexpr int RI_THREADS = 256;
 constexpr int LUT_N = sizeof(Ice3gbLuts) / sizeof(double);
@@ -30,13 +42,29 @@ enum {
 enum { RS_RCRIMS, RS_RCRIMSS, RS_RSRIMCG, RS_RRACCS, RS_RRACCSS, RS_RSACCRG, RS_FREEZ1, RS_FREEZ2, NRS };
 enum { RG_RCDRYG, RG_RIDRYG, RG_RIWETG, RG_RSDRYG, RG_RSWETG, RG_RRDRYG, RG_FREEZ1, RG_FREEZ2, NRG };
 
+// Constants derived from the table once per block (kept in shared memory).
+struct Derived {
+  double lLBR, lLBS, lLBG, lLBDAS_MAX, lTT;   // logs of table constants
+  double nu20_eb2;                            // NU20 * exp(-BETA2)
+};
+
+ICE3_HD void make_derived(const Cst &c, Derived &d)
+{
+  d.lLBR = fm::flog(c.LBR);
+  d.lLBS = fm::flog(c.LBS);
+  d.lLBG = fm::flog(c.LBG);
+  d.lLBDAS_MAX = fm::flog(c.LBDAS_MAX);
+  d.lTT = fm::flog(c.TT);
+  d.nu20_eb2 = c.NU20 * fm::fexp(-c.BETA2);
+}
+
 // Rates that persist between the hard pass and the following soft passes
-// (Fortran ZBU_INST, ZRS_TEND, ZRG_TEND, ZSSI) plus the derived fields.
+// (Fortran ZBU_INST, ZRS_TEND, ZRG_TEND, ZSSI).
 struct Rates {
   double bu[NBU];
   double rs[NRS];
   double rg[NRG];
-  double ssi, ka, dv, ai, cj;
+  double ssi;
 };
 
 // Per-point constants over the whole step.
@@ -47,85 +75,81 @@ struct PointFix {
   double rcrautc;       // CRIAUTC / rho
 };
 
-// Per-pass work state (ICE4_TENDENCIES locals).
-struct Pass {
-  double t;
-  double v[NV];
-  double lbdar, lbdas, lbdag;        // slope parameters
-  double llbdar, llbdas, llbdag;     // their logarithms
-  double rainfr;
-  double hl[4], hi[4];
-};
-
 ICE3_HD double esat_from(double alp, double beta, double gam, double it, double lt)
 {
   return fm::fexp(alp - beta * it - gam * lt);
 }
 
+// x < 0 (not -0), on the bit pattern.
+ICE3_HD bool negd(double x) { return fm::bits_(x) < 0 && fm::bits_(x) != INT64_MIN; }
+// x == 0 or -0, on the bit pattern.
+ICE3_HD bool zerod(double x) { return (fm::bits_(x) & 0x7fffffffffffffffLL) == 0; }
+
 // ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.).
-ICE3_HD void nucleation(const Cst &c, bool ld, double tht, double pabst, double rhodref, double exn,
+ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst, double rhodref, double exn,
                         double lsfact, double t, double rvt, double &cit, double &rvheni)
 {
   rvheni = 0.0;
-  if (!(ld && t < c.TT && rvt > c.V_RTMIN)) return;
+  if (!(ltp(t, c.TT) && gtp(rvt, c.V_RTMIN))) return;
   const double lt = fm::flog(t), it = 1.0 / t;
   double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   double zzw = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
-  zzw = fmin(pabst * 0.5, zzw);
+  zzw = dmin(pabst * 0.5, zzw);
   double zssi = rvt * (pabst - zzw) / (c.EPSILO * zzw) - 1.0;
-  zusw = fmin(pabst * 0.5, zusw);
+  zusw = dmin(pabst * 0.5, zusw);
   zusw = (zusw / zzw) * ((pabst - zzw) / (pabst - zusw)) - 1.0;
-  zssi = fmin(zssi, zusw);
+  zssi = dmin(zssi, zusw);
   zzw = 0.0;
-  if (t < c.TT - 5.0 && zssi > 0.0) {
+  if (ltp(t, c.TT - 5.0) && pos(zssi)) {
     zzw = c.NU20 * fm::fexp(c.ALPHA2 * zssi - c.BETA2);
-  } else if (t <= c.TT - 2.0 && t >= c.TT - 5.0 && zssi > 0.0) {
-    zzw = fmax(c.NU20 * fm::fexp(-c.BETA2), c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(zssi / zusw)));
+  } else if (!gtp(t, c.TT - 2.0) && !ltp(t, c.TT - 5.0) && pos(zssi)) {
+    zzw = dmax(d.nu20_eb2, c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(zssi / zusw)));
   }
-  zzw = fmin(zzw - cit, 50.e3);
-  rvheni = fmin(rvt, fmax(zzw, 0.0) * c.MNU0 / rhodref);
+  zzw = dmin(zzw - cit, 50.e3);
+  rvheni = dmin(rvt, pmax0(zzw) * c.MNU0 / rhodref);
   if (c.LFEEDBACKT != 0.0) {
-    const double w = fmin(rvheni, fmax(0.0, (c.TT / exn - tht) / lsfact)) / fmax(rvheni, 1.e-20);
+    const double w = dmin(rvheni, pmax0((c.TT / exn - tht) / lsfact)) / dmax(rvheni, 1.e-20);
     rvheni *= w;
     zzw *= w;
   }
-  cit = fmax(zzw + cit, cit);
+  cit = dmax(zzw + cit, cit);
 }
 
 // ICE4_COMPUTE_PDF (micro/mode_ice4_compute_pdf.F90), one point; returns RF.
-ICE3_HD double compute_pdf(const Cst &c, bool ld, double rcrautc_pt, double rct, double rit, double cf, double t,
-                           double sigma_rc, double hl[4], double hi[4])
+// `criauti` receives MIN(CRIAUTI, 10**(ACRIAUTI (T-TT) + BCRIAUTI)), which
+// the ice autoconversion of the same pass uses too.
+ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit, double cf, double t,
+                           double sigma_rc, double hl[4], double hi[4], double &criauti)
 {
   const int aucv_rc = (int)c.SUBG_AUCV_RC, aucv_ri = (int)c.SUBG_AUCV_RI, prpdf = (int)c.SUBG_PR_PDF;
-  const double rcrautc = ld ? rcrautc_pt : 0.0;
   double hcf = 0, lcf = 0, hrc = 0, lrc = 0;
   if (aucv_rc == 0) {
-    if (rct > rcrautc && ld) { hcf = 1.0; hrc = rct; }
-    else if (rct > c.C_RTMIN && ld) { lcf = 1.0; lrc = rct; }
+    if (gtd(rct, rcrautc)) { hcf = 1.0; hrc = rct; }
+    else if (gtp(rct, c.C_RTMIN)) { lcf = 1.0; lrc = rct; }
   } else if (aucv_rc == 3) {
-    if (cf > 0.0 && rct > rcrautc * cf && ld) { hcf = cf; hrc = rct; }
-    else if (cf > 0.0 && rct > c.C_RTMIN && ld) { lcf = cf; lrc = rct; }
+    if (pos(cf) && gtd(rct, rcrautc * cf)) { hcf = cf; hrc = rct; }
+    else if (pos(cf) && gtp(rct, c.C_RTMIN)) { lcf = cf; lrc = rct; }
   } else if (aucv_rc == 2) {
-    const double sum = ld ? hl[3] + hl[2] : 0.0;
+    const double sum = hl[3] + hl[2];
     hcf = hl[0]; lcf = hl[1];
-    if (sum > 1.e-20 && ld) { lrc = hl[3] * rct / sum; hrc = hl[2] * rct / sum; }
+    if (gtp(sum, 1.e-20)) { lrc = hl[3] * rct / sum; hrc = hl[2] * rct / sum; }
   } else if (aucv_rc == 1 && prpdf == 0) {
-    if (rct > rcrautc + sigma_rc && ld) {
+    if (gtd(rct, rcrautc + sigma_rc)) {
       hcf = 1.0; hrc = rct;
-    } else if (rct > rcrautc - sigma_rc && rct <= rcrautc + sigma_rc && ld) {
+    } else if (gtd(rct, rcrautc - sigma_rc)) {
       const double inv2s = 1.0 / (2.0 * sigma_rc);
       hcf = (rct + sigma_rc - rcrautc) * inv2s;
-      lcf = fmax(0.0, cf - hcf);
+      lcf = pmax0(cf - hcf);
       hrc = (rct + sigma_rc - rcrautc) * (rct + sigma_rc + rcrautc) * (0.5 * inv2s);
-      lrc = fmax(0.0, rct - hrc);
-    } else if (rct > c.C_RTMIN && cf > 0.0 && ld) {
+      lrc = pmax0(rct - hrc);
+    } else if (gtp(rct, c.C_RTMIN) && pos(cf)) {
       lcf = cf; lrc = rct;
     }
   } else if (aucv_rc == 1) {
     const double coeff = (prpdf == 1 || prpdf == 2) ? 2.0 : (prpdf == 3 ? 3.0 : 4.0);
-    const double rcmax = (rct > 0.0 && cf > 0.0 && ld) ? coeff * rct / cf : 0.0;
+    const double rcmax = (pos(rct) && pos(cf)) ? coeff * rct / cf : 0.0;
     double lloc = 0.0, hloc = 0.0;
-    const bool ok = rct > 0.0 && cf > 0.0 && rcmax > rcrautc && ld;
+    const bool ok = pos(rct) && pos(cf) && gtd(rcmax, rcrautc);
     const double a = rcrautc, m = rcmax;
     if (prpdf == 1) {
       if (ok) { lloc = 0.5 * a; hloc = (m + a) / 2.0; }
@@ -137,7 +161,7 @@ ICE3_HD double compute_pdf(const Cst &c, bool ld, double rcrautc_pt, double rct,
         hloc = (m + 3.0 * a) / 4.0;
       }
     } else if (prpdf == 2) {
-      if (rct <= a * cf && ok) {
+      if (!gtd(rct, a * cf) && ok) {
         lloc = (m * m * m - 12.0 * m * a * a + 8.0 * a * a * a) / (6.0 * m * m - 24.0 * m * a + 12.0 * a * a);
         hloc = (m + 2.0 * a) / 3.0;
       } else if (ok) {
@@ -147,35 +171,35 @@ ICE3_HD double compute_pdf(const Cst &c, bool ld, double rcrautc_pt, double rct,
     }
     if (ok) {
       lcf = cf * (hloc - (rct / cf)) / (hloc - lloc);
-      hcf = fmax(0.0, cf - lcf);
+      hcf = pmax0(cf - lcf);
       lrc = lloc * lcf;
-      hrc = fmax(0.0, rct - lrc);
-    } else if (rct > 0.0 && cf > 0.0 && rcmax <= rcrautc && ld) {
+      hrc = pmax0(rct - lrc);
+    } else if (pos(rct) && pos(cf) && !gtd(rcmax, rcrautc)) {
       lcf = cf; lrc = rct;
     }
   }
   hl[0] = hcf; hl[1] = lcf; hl[2] = hrc; hl[3] = lrc;
-  const double criauti = ld ? fmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI)) : 0.0;
+  criauti = dmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
   double ihcf = 0, ilcf = 0, ihri = 0, ilri = 0;
   if (aucv_ri == 0) {
-    if (rit > criauti && ld) { ihcf = 1.0; ihri = rit; }
-    else if (rit > c.I_RTMIN && ld) { ilcf = 1.0; ilri = rit; }
+    if (gtd(rit, criauti)) { ihcf = 1.0; ihri = rit; }
+    else if (gtp(rit, c.I_RTMIN)) { ilcf = 1.0; ilri = rit; }
   } else if (aucv_ri == 1) {
-    if (cf > 0.0 && rit > criauti * cf && ld) { ihcf = cf; ihri = rit; }
-    else if (cf > 0.0 && rit > c.I_RTMIN && ld) { ilcf = cf; ilri = rit; }
+    if (pos(cf) && gtd(rit, criauti * cf)) { ihcf = cf; ihri = rit; }
+    else if (pos(cf) && gtp(rit, c.I_RTMIN)) { ilcf = cf; ilri = rit; }
   } else if (aucv_ri == 2) {
-    const double sum = ld ? hi[3] + hi[2] : 0.0;
+    const double sum = hi[3] + hi[2];
     ihcf = hi[0]; ilcf = hi[1];
-    if (sum > 1.e-20 && ld) { ilri = hi[3] * rit / sum; ihri = hi[2] * rit / sum; }
+    if (gtp(sum, 1.e-20)) { ilri = hi[3] * rit / sum; ihri = hi[2] * rit / sum; }
   }
   hi[0] = ihcf; hi[1] = ilcf; hi[2] = ihri; hi[3] = ilri;
-  return ld ? fmax(hl[0], hi[0]) : 0.0;
+  return dmax(hl[0], hi[0]);
 }
 
-// INTERP_MICRO (micro/interp_micro.func.h, packed path): index from fm::flog(x).
+// INTERP_MICRO (micro/interp_micro.func.h, packed path): index from log(x).
 ICE3_HD double lut_index(double logx, double knum, double p1, double p2, int &i)
 {
-  const double z = fmax(1.00001, fmin(knum - 0.00001, p1 * logx + p2));
+  const double z = dmax(1.00001, dmin(knum - 0.00001, p1 * logx + p2));
   i = (int)z;
   return z - (double)i;
 }
@@ -188,312 +212,291 @@ ICE3_HD double lut2d(const double *lt, int n2, int i1, double f1, int i2, double
   return (r1[i2] * f2 - r1[i2 - 1] * (f2 - 1.0)) * f1 - (r0[i2] * f2 - r0[i2 - 1] * (f2 - 1.0)) * (f1 - 1.0);
 }
 
-// Slope parameters, mode_ice4_tendencies.F90:389-433.
-ICE3_HD void slopes(const Cst &c, const PointFix &pf, Pass &x)
+// Slope parameters (mode_ice4_tendencies.F90:389-433): lbda and log(lbda) per
+// precipitating species, zero / -inf where the species is absent.
+struct Slopes {
+  double lbdar, lbdas, lbdag;
+  double llbdar, llbdas, llbdag;
+};
+
+ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const double v[NV], Slopes &s)
 {
-  if (x.v[IRR] > 0.) {
-    x.llbdar = fm::flog(c.LBR) + c.LBEXR * (pf.lrho + fm::flog(fmax(x.v[IRR], c.R_RTMIN)));
-    x.lbdar = fm::fexp(x.llbdar);
-  } else { x.lbdar = 0.0; x.llbdar = -INFINITY; }
+  if (pos(v[IRR])) {
+    s.llbdar = d.lLBR + c.LBEXR * (lrho + fm::flog(dmax(v[IRR], c.R_RTMIN)));
+    s.lbdar = fm::fexp(s.llbdar);
+  } else { s.lbdar = 0.0; s.llbdar = -INFINITY; }
   if (c.LSNOW_T != 0.0) {
-    if (x.v[IRS] > 0.) {
-      const double e = (x.t > 263.15) ? fm::fexp10(14.554 - 0.0423 * x.t) : fm::fexp10(6.226 - 0.0106 * x.t);
-      x.lbdas = fmax(fmin(c.LBDAS_MAX, e), c.LBDAS_MIN) * c.TRANS_MP_GAMMAS;
-      x.llbdas = fm::flog(x.lbdas);
-    } else { x.lbdas = 0.0; x.llbdas = -INFINITY; }
-  } else if (x.v[IRS] > 0.) {
-    x.llbdas = fmin(fm::flog(c.LBDAS_MAX), fm::flog(c.LBS) + c.LBEXS * (pf.lrho + fm::flog(fmax(x.v[IRS], c.S_RTMIN))));
-    x.lbdas = fm::fexp(x.llbdas);
-  } else { x.lbdas = 0.0; x.llbdas = -INFINITY; }
-  if (x.v[IRG] > 0.) {
-    x.llbdag = fm::flog(c.LBG) + c.LBEXG * (pf.lrho + fm::flog(fmax(x.v[IRG], c.G_RTMIN)));
-    x.lbdag = fm::fexp(x.llbdag);
-  } else { x.lbdag = 0.0; x.llbdag = -INFINITY; }
+    if (pos(v[IRS])) {
+      const double e = gtp(t, 263.15) ? fm::fexp10(14.554 - 0.0423 * t) : fm::fexp10(6.226 - 0.0106 * t);
+      s.lbdas = dmax(dmin(c.LBDAS_MAX, e), c.LBDAS_MIN) * c.TRANS_MP_GAMMAS;
+      s.llbdas = fm::flog(s.lbdas);
+    } else { s.lbdas = 0.0; s.llbdas = -INFINITY; }
+  } else if (pos(v[IRS])) {
+    s.llbdas = dmin(d.lLBDAS_MAX, d.lLBS + c.LBEXS * (lrho + fm::flog(dmax(v[IRS], c.S_RTMIN))));
+    s.lbdas = fm::fexp(s.llbdas);
+  } else { s.lbdas = 0.0; s.llbdas = -INFINITY; }
+  if (pos(v[IRG])) {
+    s.llbdag = d.lLBG + c.LBEXG * (lrho + fm::flog(dmax(v[IRG], c.G_RTMIN)));
+    s.lbdag = fm::fexp(s.llbdag);
+  } else { s.lbdag = 0.0; s.llbdag = -INFINITY; }
 }
 
-// Heat/vapour term of the freezing and melting rates (fast_rs/fast_rg).
-ICE3_HD double heat_term(const Cst &c, const Rates &R, double t, double esat, double rv, double pres)
+// The hard-pass rates of ICE4_TENDENCIES after nucleation, RRHONG and RIMLTC
+// (mode_ice4_tendencies.F90:303-600): derived fields, slopes, ICE4_SLOW,
+// ICE4_WARM and the rate parts of ICE4_FAST_RS/RG/RI.  The parts that depend
+// on the current freezing budget (riming/accretion split, wet/dry growth
+// choice) are left to aggregate(), which every pass runs.
+ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
+                        double t, const double v[NV], double cit, const double hl[4], const double hi[4],
+                        double criauti, Rates &R)
 {
-  double e = rv * pres / (c.EPSILO + rv);
-  if (c.LEVLIMIT != 0.0) e = fmin(e, esat);
-  return R.ka * (c.TT - t) + (R.dv * (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * (c.ESTT - e) / (c.RV * t));
-}
-
-// ICE4_TENDENCIES for one point; see mode_ice4_tendencies.F90 for the order.
-ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft, const PointFix &pf,
-                        double lvfact, double lsfact, double &cit, double t0, const double vart[NV], Rates &R,
-                        double &rainfr, double hl[4], double hi[4], double A[NV], double B[NV])
-{
-  Pass x;
-  x.t = t0;
-#pragma unroll
-  for (int v = 0; v < NV; ++v) { x.v[v] = vart[v]; A[v] = 0.0; B[v] = 0.0; }
-  double *b = R.bu;
-  double lt = 0.0, it = 0.0, esw = 0.0, esi = 0.0;
-  if (soft) {
-    b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = 0.0;
-  } else {
-    nucleation(c, true, x.v[ITH], pf.pres, pf.rho, pf.exn, lsfact, x.t, x.v[IRV], cit, b[B_RVHENI_MR]);
-    x.v[ITH] += b[B_RVHENI_MR] * lsfact;
-    x.t = x.v[ITH] * pf.exn;
-    x.v[IRV] -= b[B_RVHENI_MR];
-    x.v[IRI] += b[B_RVHENI_MR];
-    // RRHONG (mode_ice4_rrhong.F90)
-    double r = 0.0;
-    if (x.t < c.TT - 35.0 && x.v[IRR] > c.R_RTMIN) {
-      r = x.v[IRR];
-      if (c.LFEEDBACKT != 0.0) r = fmin(r, fmax(0.0, ((c.TT - 35.0) / pf.exn - x.v[ITH]) / (lsfact - lvfact)));
-    }
-    b[B_RRHONG_MR] = r;
-    x.v[ITH] += r * (lsfact - lvfact);
-    x.t = x.v[ITH] * pf.exn;
-    x.v[IRR] -= r;
-    x.v[IRG] += r;
-    // RIMLTC (mode_ice4_rimltc.F90)
-    r = 0.0;
-    if (x.v[IRI] > 0. && x.t > c.TT) {
-      r = x.v[IRI];
-      if (c.LFEEDBACKT != 0.0) r = fmin(r, fmax(0.0, (x.v[ITH] - c.TT / pf.exn) / (lsfact - lvfact)));
-    }
-    b[B_RIMLTC_MR] = r;
-    x.v[ITH] -= r * (lsfact - lvfact);
-    x.t = x.v[ITH] * pf.exn;
-    x.v[IRC] += r;
-    x.v[IRI] -= r;
-    const double lsv = lsfact - lvfact;
-    B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
-    B[IRV] = -b[B_RVHENI_MR];
-    B[IRC] = b[B_RIMLTC_MR];
-    B[IRR] = -b[B_RRHONG_MR];
-    B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
-    B[IRG] = b[B_RRHONG_MR];
-    // derived fields (mode_ice4_tendencies.F90:303-320)
-    lt = fm::flog(x.t);
-    it = 1.0 / x.t;
-    esi = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
-    esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
-    R.ssi = x.v[IRV] * (pf.pres - esi) / (c.EPSILO * esi) - 1.0;
-    R.ka = 2.38e-2 + 7.1e-5 * (x.t - c.TT);
-    R.dv = 2.11e-5 * fm::fexp(1.94 * (lt - fm::flog(c.TT))) * (c.P00 / pf.pres);
-    R.ai = sq(c.LSTT + (c.CPV - c.CI) * (x.t - c.TT)) / (R.ka * c.RV * x.t * x.t) + (c.RV * x.t) / (R.dv * esi);
-    R.cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) / sqrt(1.718e-5 + 4.9e-8 * (x.t - c.TT));
+  double *b = R.bu, *rs = R.rs, *rg = R.rg;
+  const double rho = pf.rho;
+  // derived fields (mode_ice4_tendencies.F90:303-320)
+  const double lt = fm::flog(t), it = 1.0 / t;
+  const double esi = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+  const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
+  R.ssi = v[IRV] * (pf.pres - esi) / (c.EPSILO * esi) - 1.0;
+  const double ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
+  const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * (c.P00 / pf.pres);
+  const double ai = sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / (ka * c.RV * t * t) + (c.RV * t) / (dv * esi);
+  const double cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) / sqrt(1.718e-5 + 4.9e-8 * (t - c.TT));
+  const double ssi_rai = R.ssi / (rho * ai);
+  Slopes s;
+  slopes(c, d, pf.lrho, t, v, s);
+  const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
+  const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
+  const bool warm = gtp(t, c.TT);
+  // ventilation factors shared by deposition, freezing and melting
+  const double vent_s = has_s ? c.O0DEPS * fm::fexp(c.EX0DEPS * s.llbdas) + c.O1DEPS * cj * fm::fexp(c.EX1DEPS * s.llbdas)
+                              : 0.0;
+  const double vent_g = has_g ? c.O0DEPG * fm::fexp(c.EX0DEPG * s.llbdag) + c.O1DEPG * cj * fm::fexp(c.EX1DEPG * s.llbdag)
+                              : 0.0;
+  // vapour/heat term of the freezing and melting rates (mode_ice4_fast_rs.F90
+  // IFREEZ1/RSMLTG, mode_ice4_fast_rg.F90 IFREEZ1/RGMLTR), e limited by the
+  // saturation pressure over ice (freezing) or over water (melting)
+  double heat_i = 0.0, heat_w = 0.0;
+  if (has_s || has_g) {
+    const double ev = v[IRV] * pf.pres / (c.EPSILO + v[IRV]);
+    const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi) : ev;
+    const double ew = c.LEVLIMIT != 0.0 ? dmin(ev, esw) : ev;
+    const double kt = ka * (c.TT - t);
+    const double dl = dv * (c.LVTT + (c.CPV - c.CL) * (t - c.TT));
+    const double irt = 1.0 / (c.RV * t);
+    heat_i = kt + (dl * (c.ESTT - ei) * irt);
+    heat_w = kt + (dl * (c.ESTT - ew) * irt);
   }
-  const double zrainfr = compute_pdf(c, true, pf.rcrautc, x.v[IRC], x.v[IRI], pf.cf, x.t, pf.sigma_rc, hl, hi);
-  const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
-  if (llrfr) {
-    rainfr = fmax(rainfr, zrainfr);
-    if ((x.v[IRR] > c.R_RTMIN || x.v[IRS] > c.S_RTMIN || x.v[IRG] > c.G_RTMIN) && rainfr == 0.) rainfr = 1.;
-  } else {
-    rainfr = 1.;
-  }
-  slopes(c, pf, x);
-  const double t = x.t, rho = pf.rho;
-  const double *v = x.v;
 
   // ---- ICE4_SLOW (mode_ice4_slow.F90) ----
-  if (t < c.TT - 35.0 && v[IRC] > c.C_RTMIN) {
-    if (!soft) b[B_RCHONI] = fmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3));
-  } else b[B_RCHONI] = 0.0;
-  if (v[IRV] > c.V_RTMIN && v[IRS] > c.S_RTMIN) {
-    if (!soft)
-      b[B_RVDEPS] = (R.ssi / (rho * R.ai)) *
-                    (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas));
-  } else b[B_RVDEPS] = 0.0;
-  if (v[IRI] > c.I_RTMIN && v[IRS] > c.S_RTMIN) {
-    if (!soft)
-      b[B_RIAGGS] = c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * x.llbdas) * v[IRI] * pf.rho_mcexvt;
-  } else b[B_RIAGGS] = 0.0;
-  if (hi[2] > c.I_RTMIN) {
-    if (!soft) {
-      const double criauti = fmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
-      b[B_RIAUTS] = c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * fmax(hi[2] - criauti * hi[0], 0.0);
-    }
-  } else b[B_RIAUTS] = 0.0;
-  if (v[IRV] > c.V_RTMIN && v[IRG] > c.G_RTMIN) {
-    if (!soft)
-      b[B_RVDEPG] = (R.ssi / (rho * R.ai)) *
-                    (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag));
-  } else b[B_RVDEPG] = 0.0;
+  b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c)
+                    ? dmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3))
+                    : 0.0;
+  b[B_RVDEPS] = (has_v && has_s) ? ssi_rai * vent_s : 0.0;
+  b[B_RIAGGS] = (has_i && has_s)
+                    ? c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * s.llbdas) * v[IRI] * pf.rho_mcexvt
+                    : 0.0;
+  b[B_RIAUTS] = gtp(hi[2], c.I_RTMIN) ? c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * pmax0(hi[2] - criauti * hi[0])
+                                      : 0.0;
+  b[B_RVDEPG] = (has_v && has_g) ? ssi_rai * vent_g : 0.0;
 
   // ---- ICE4_WARM (mode_ice4_warm.F90), SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE ----
   if (c.LWARM != 0.0) {
-    if (hl[2] > c.C_RTMIN && hl[0] > 0.0) {
-      if (!soft) b[B_RCAUTR] = c.TIMAUTC * fmax(hl[2] - hl[0] * pf.rcrautc, 0.0);
-    } else b[B_RCAUTR] = 0.0;
-    if (v[IRC] > c.C_RTMIN && v[IRR] > c.R_RTMIN) {
-      if (!soft) b[B_RCACCR] = c.FCACCR * v[IRC] * fm::fexp(c.EXCACCR * x.llbdar) * pf.rho_mcexvt;
-    } else b[B_RCACCR] = 0.0;
-    if (v[IRR] > c.R_RTMIN && v[IRC] <= c.C_RTMIN) {
-      if (!soft) {
-        const double usw = 1. - v[IRV] * (pf.pres - esw) / (c.EPSILO * esw);
-        const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / (R.ka * c.RV * t * t) + (c.RV * t) / (R.dv * esw);
-        b[B_RREVAV] = (fmax(0., usw) / (rho * av)) *
-                      (c.O0EVAR * fm::fexp(c.EX0EVAR * x.llbdar) + c.O1EVAR * R.cj * fm::fexp(c.EX1EVAR * x.llbdar));
-      }
+    b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
+    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * fm::fexp(c.EXCACCR * s.llbdar) * pf.rho_mcexvt : 0.0;
+    if (has_r && !has_c) {
+      const double usw = 1. - v[IRV] * (pf.pres - esw) / (c.EPSILO * esw);
+      const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / (ka * c.RV * t * t) + (c.RV * t) / (dv * esw);
+      b[B_RREVAV] = (pmax0(usw) / (rho * av)) *
+                    (c.O0EVAR * fm::fexp(c.EX0EVAR * s.llbdar) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
     } else b[B_RREVAV] = 0.0;
   } else {
     b[B_RCAUTR] = b[B_RCACCR] = b[B_RREVAV] = 0.0;
   }
 
-  // ---- ICE4_FAST_RS (mode_ice4_fast_rs.F90) ----
-  double *rs = R.rs;
-  double freez;
-  if (v[IRS] > c.S_RTMIN) {
-    if (!soft) {
-      const double den = 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t)));
-      rs[RS_FREEZ1] = heat_term(c, R, t, esi, v[IRV], pf.pres) *
-                      (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) + c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas)) * den;
-      rs[RS_FREEZ2] = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
-    }
-    freez = fmax(0., fmax(0., rs[RS_FREEZ1] + rs[RS_FREEZ2] * b[B_RIAGGS]) - b[B_RIAGGS]);
-  } else {
-    rs[RS_FREEZ1] = rs[RS_FREEZ2] = 0.0;
-    freez = 0.0;
-  }
-  const bool grim = v[IRC] > c.C_RTMIN && v[IRS] > c.S_RTMIN;
-  if (!grim) rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
-  if (!soft && grim) {
+  // ---- ICE4_FAST_RS rates (mode_ice4_fast_rs.F90) ----
+  // collision-freezing denominator, shared with ICE4_FAST_RG
+  const double den = (has_s || has_g) ? 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
+  const double freez2 = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
+  rs[RS_FREEZ1] = has_s ? heat_i * vent_s * den : 0.0;
+  rs[RS_FREEZ2] = has_s ? freez2 : 0.0;
+  const double ilr = has_r ? 1.0 / s.lbdar : 0.0, ils = has_s ? 1.0 / s.lbdas : 0.0;
+  const double ilg = has_g ? 1.0 / s.lbdag : 0.0;
+  if (has_c && has_s) {
     int i;
-    const double fr = lut_index(x.llbdas, c.NGAMINC, c.RIMINTP1, c.RIMINTP2, i);
+    const double fr = lut_index(s.llbdas, c.NGAMINC, c.RIMINTP1, c.RIMINTP2, i);
     const double zw1 = lut1d(lut + O_RIM1, i, fr);
     const double zw2 = lut1d(lut + O_RIM2, i, fr);
     const double zw3 = lut1d(lut + O_RIM4, i, fr);
-    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * fm::fexp(c.EXCRIMSS * x.llbdas) * pf.rho_mcexvt;
-    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * fm::fexp(c.EXCRIMSG * x.llbdas) * pf.rho_mcexvt;
+    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * fm::fexp(c.EXCRIMSS * s.llbdas) * pf.rho_mcexvt;
+    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * fm::fexp(c.EXCRIMSG * s.llbdas) * pf.rho_mcexvt;
     if ((int)c.SNOW_RIMING == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
-      const double r = c.SRIMCG * fm::fexp(c.EXSRIMCG * x.llbdas) * (1.0 - zw2);
-      rs[RS_RSRIMCG] = zzw * r / fmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * x.llbdas) * (1. - zw3) -
-                                                 c.SRIMCG3 * r);
+      const double r = c.SRIMCG * fm::fexp(c.EXSRIMCG * s.llbdas) * (1.0 - zw2);
+      rs[RS_RSRIMCG] = zzw * r / dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * s.llbdas) * (1. - zw3) -
+                                                  c.SRIMCG3 * r);
     } else rs[RS_RSRIMCG] = 0.0;
-  }
-  if (grim && t < c.TT) {
-    b[B_RCRIMSS] = fmin(freez, rs[RS_RCRIMSS]);
-    freez = fmax(0., freez - b[B_RCRIMSS]);
-    const double zzw0 = fmin(1., freez / fmax(1.e-20, rs[RS_RCRIMS] - b[B_RCRIMSS]));
-    b[B_RCRIMSG] = zzw0 * fmax(0., rs[RS_RCRIMS] - b[B_RCRIMSS]);
-    freez = fmax(0., freez - b[B_RCRIMSG]);
-    b[B_RSRIMCG] = zzw0 * rs[RS_RSRIMCG] * (signbit(b[B_RCRIMSG]) ? 0.0 : 1.0);
-    b[B_RCRIMSG] = fmax(0., b[B_RCRIMSG]);
   } else {
-    b[B_RCRIMSS] = b[B_RCRIMSG] = b[B_RSRIMCG] = 0.0;
+    rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
   }
-  const bool gacc = v[IRR] > c.R_RTMIN && v[IRS] > c.S_RTMIN;
-  if (!gacc) rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
-  if (!soft) {
+  if (has_r && has_s) {
+    int i1, i2;
+    const double f1 = lut_index(s.llbdas, c.NACCLBDAS, c.ACCINTP1S, c.ACCINTP2S, i1);
+    const double f2 = lut_index(s.llbdar, c.NACCLBDAR, c.ACCINTP1R, c.ACCINTP2R, i2);
+    const double zw1 = lut2d(lut + O_RACCSS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
+    const double zw2 = lut2d(lut + O_RACCS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
+    const double zw3 = lut2d(lut + O_SACCRG, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
+    const double zzw = c.FRACCSS * fm::fexp(c.CXS * s.llbdas) * pf.rho_mcexvt1 *
+                       (c.LBRACCS1 * ils * ils + c.LBRACCS2 * ils * ilr + c.LBRACCS3 * ilr * ilr) * sq(sq(ilr));
+    rs[RS_RRACCSS] = zw1 * zzw;
+    rs[RS_RRACCS] = zw2 * zzw;
+    rs[RS_RSACCRG] = c.FSACCRG * zw3 * fm::fexp((c.CXS - c.BS) * s.llbdas) * pf.rho_mcexvt1 *
+                     (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr;
+  } else {
     rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
-    if (gacc) {
-      int i1, i2;
-      const double f1 = lut_index(x.llbdas, c.NACCLBDAS, c.ACCINTP1S, c.ACCINTP2S, i1);
-      const double f2 = lut_index(x.llbdar, c.NACCLBDAR, c.ACCINTP1R, c.ACCINTP2R, i2);
-      const double zw1 = lut2d(lut + O_RACCSS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
-      const double zw2 = lut2d(lut + O_RACCS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
-      const double zw3 = lut2d(lut + O_SACCRG, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
-      const double ilr = 1.0 / x.lbdar, ils = 1.0 / x.lbdas;
-      const double zzw = c.FRACCSS * fm::fexp(c.CXS * x.llbdas) * pf.rho_mcexvt1 *
-                         (c.LBRACCS1 * ils * ils + c.LBRACCS2 * ils * ilr + c.LBRACCS3 * ilr * ilr) * sq(sq(ilr));
-      rs[RS_RRACCSS] = zw1 * zzw;
-      rs[RS_RRACCS] = zw2 * zzw;
-      rs[RS_RSACCRG] = c.FSACCRG * zw3 * fm::fexp((c.CXS - c.BS) * x.llbdas) * pf.rho_mcexvt1 *
-                       (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr;
-    }
   }
-  if (gacc && t < c.TT) {
-    b[B_RRACCSS] = fmin(freez, rs[RS_RRACCSS]);
-    freez = fmax(0., freez - b[B_RRACCSS]);
-    const double zzw = fmin(1., freez / fmax(1.e-20, rs[RS_RRACCS] - b[B_RRACCSS]));
-    b[B_RRACCSG] = zzw * fmax(0., rs[RS_RRACCS] - b[B_RRACCSS]);
-    freez = fmax(0., freez - b[B_RRACCSG]);
-    b[B_RSACCRG] = zzw * rs[RS_RSACCRG] * (signbit(b[B_RRACCSG]) ? 0.0 : 1.0);
-    b[B_RRACCSG] = fmax(0., b[B_RRACCSG]);
-  } else {
-    b[B_RRACCSS] = b[B_RRACCSG] = b[B_RSACCRG] = 0.0;
-  }
-  if (v[IRS] > c.S_RTMIN && t > c.TT) {
-    if (!soft) {
-      const double h = heat_term(c, R, t, esw, v[IRV], pf.pres);
-      b[B_RSMLTG] = c.FSCVMG * fmax(0., (-h * (c.O0DEPS * fm::fexp(c.EX0DEPS * x.llbdas) +
-                                               c.O1DEPS * R.cj * fm::fexp(c.EX1DEPS * x.llbdas)) -
-                                         (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c.CL * (c.TT - t))) /
-                                            (rho * c.LMTT));
-      b[B_RCMLTSR] = rs[RS_RCRIMS];
-    }
+  if (has_s && warm) {
+    b[B_RSMLTG] = c.FSCVMG * pmax0((-heat_w * vent_s - (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c.CL * (c.TT - t))) /
+                                   (rho * c.LMTT));
+    b[B_RCMLTSR] = rs[RS_RCRIMS];
   } else {
     b[B_RSMLTG] = b[B_RCMLTSR] = 0.0;
   }
 
-  // ---- ICE4_FAST_RG (mode_ice4_fast_rg.F90, KRR = 6) ----
-  double *rg = R.rg;
-  if (v[IRI] > c.I_RTMIN && v[IRR] > c.R_RTMIN) {
-    if (!soft) {
-      b[B_RICFRRG] = c.ICFRR * v[IRI] * fm::fexp(c.EXICFRR * x.llbdar) * pf.rho_mcexvt;
-      b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * x.llbdar) * pf.rho_mcexvt1;
-      if (c.LCRFLIMIT != 0.0) {
-        const double zw = fmax(0., fmin(1., (b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t) /
-                                                fmax(1.e-20, c.LVTT * b[B_RRCFRIG])));
-        b[B_RRCFRIG] = zw * b[B_RRCFRIG];
-        b[B_RICFRR] = (1. - zw) * b[B_RICFRRG];
-        b[B_RICFRRG] = zw * b[B_RICFRRG];
-      } else b[B_RICFRR] = 0.0;
-    }
+  // ---- ICE4_FAST_RG rates (mode_ice4_fast_rg.F90, KRR = 6) ----
+  if (has_i && has_r) {
+    b[B_RICFRRG] = c.ICFRR * v[IRI] * fm::fexp(c.EXICFRR * s.llbdar) * pf.rho_mcexvt;
+    b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * s.llbdar) * pf.rho_mcexvt1;
+    if (c.LCRFLIMIT != 0.0) {
+      const double zw = pmax0(dmin(1., (b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t) /
+                                           dmax(1.e-20, c.LVTT * b[B_RRCFRIG])));
+      b[B_RRCFRIG] = zw * b[B_RRCFRIG];
+      b[B_RICFRR] = (1. - zw) * b[B_RICFRRG];
+      b[B_RICFRRG] = zw * b[B_RICFRRG];
+    } else b[B_RICFRR] = 0.0;
   } else {
     b[B_RICFRRG] = b[B_RRCFRIG] = b[B_RICFRR] = 0.0;
   }
-  const double base_g = fm::fexp((c.CXG - c.DG - 2.) * x.llbdag) * pf.rho_mcexvt;
-  if (v[IRG] > c.G_RTMIN && v[IRC] > c.C_RTMIN) {
-    if (!soft) rg[RG_RCDRYG] = c.FCDRYG * v[IRC] * base_g;
-  } else rg[RG_RCDRYG] = 0.0;
-  if (v[IRG] > c.G_RTMIN && v[IRI] > c.I_RTMIN) {
-    if (!soft) {
-      const double e = fm::fexp(c.COLEXIG * (t - c.TT));
-      rg[RG_RIDRYG] = c.FIDRYG * e * v[IRI] * base_g;
-      rg[RG_RIWETG] = rg[RG_RIDRYG] / (c.COLIG * e);
-    }
+  const double base_g = (has_g && (has_c || has_i)) ? fm::fexp((c.CXG - c.DG - 2.) * s.llbdag) * pf.rho_mcexvt : 0.0;
+  rg[RG_RCDRYG] = (has_g && has_c) ? c.FCDRYG * v[IRC] * base_g : 0.0;
+  if (has_g && has_i) {
+    const double e = fm::fexp(c.COLEXIG * (t - c.TT));
+    rg[RG_RIDRYG] = c.FIDRYG * e * v[IRI] * base_g;
+    rg[RG_RIWETG] = rg[RG_RIDRYG] / (c.COLIG * e);
   } else rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
-  const bool gdry_s = v[IRS] > c.S_RTMIN && v[IRG] > c.G_RTMIN;
-  if (!gdry_s) rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
-  if (!soft && gdry_s) {
+  if (has_s && has_g) {
     int i1, i2;
-    const double f1 = lut_index(x.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
-    const double f2 = lut_index(x.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
+    const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
+    const double f2 = lut_index(s.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
     const double zw = lut2d(lut + O_SDRYG, ICE3GB_NDRYLBDAS, i1, f1, i2, f2);
-    const double ilg = 1.0 / x.lbdag, ils = 1.0 / x.lbdas;
-    rg[RG_RSWETG] = c.FSDRYG * zw / c.COLSG * fm::fexp((c.CXS - c.BS) * x.llbdas + c.CXG * x.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RSWETG] = c.FSDRYG * zw / c.COLSG * fm::fexp((c.CXS - c.BS) * s.llbdas + c.CXG * s.llbdag) * pf.rho_mcexvt1 *
                     (c.LBSDRYG1 * ilg * ilg + c.LBSDRYG2 * ilg * ils + c.LBSDRYG3 * ils * ils);
     rg[RG_RSDRYG] = rg[RG_RSWETG] * c.COLSG * fm::fexp(c.COLEXSG * (t - c.TT));
-  }
-  const bool gdry_r = v[IRR] > c.R_RTMIN && v[IRG] > c.G_RTMIN;
-  if (!gdry_r) rg[RG_RRDRYG] = 0.0;
-  if (!soft && gdry_r) {
+  } else rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
+  if (has_r && has_g) {
     int i1, i2;
-    const double f1 = lut_index(x.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
-    const double f2 = lut_index(x.llbdar, c.NDRYLBDAR, c.DRYINTP1R, c.DRYINTP2R, i2);
+    const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
+    const double f2 = lut_index(s.llbdar, c.NDRYLBDAR, c.DRYINTP1R, c.DRYINTP2R, i2);
     const double zw = lut2d(lut + O_RDRYG, ICE3GB_NDRYLBDAR, i1, f1, i2, f2);
-    const double ilg = 1.0 / x.lbdag, ilr = 1.0 / x.lbdar;
-    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * fm::fexp(c.CXG * x.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * fm::fexp(c.CXG * s.llbdag) * pf.rho_mcexvt1 *
                     (c.LBRDRYG1 * ilg * ilg + c.LBRDRYG2 * ilg * ilr + c.LBRDRYG3 * ilr * ilr);
+  } else rg[RG_RRDRYG] = 0.0;
+  rg[RG_FREEZ1] = has_g ? heat_i * vent_g * den : 0.0;
+  rg[RG_FREEZ2] = has_g ? freez2 : 0.0;
+  if (has_g && warm) {
+    b[B_RGMLTR] = pmax0((-heat_w * vent_g - (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c.CL * (c.TT - t))) /
+                        (rho * c.LMTT));
+  } else b[B_RGMLTR] = 0.0;
+
+  // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
+  if (pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20)) {
+    const double l = dmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(rho * v[IRI] / cit)));
+    b[B_RCBERI] = ssi_rai * cit * (c.O0DEPI / l + c.O2DEPI * cj * cj * fm::fexp(-(c.DI + 2.0) * fm::flog(l)));
+  } else b[B_RCBERI] = 0.0;
+}
+
+// Rates of a soft pass: the hard-pass values where their condition still
+// holds on the current state, zero elsewhere (the ELSE branches of the
+// process routines under LDSOFT).
+ICE3_HD void soft_rates(const Cst &c, double t, const double v[NV], double cit, const double hl[4],
+                        const double hi[4], Rates &R)
+{
+  double *b = R.bu, *rs = R.rs, *rg = R.rg;
+  const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
+  const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
+  const bool warm = gtp(t, c.TT);
+  if (!(ltp(t, c.TT - 35.0) && has_c)) b[B_RCHONI] = 0.0;
+  if (!(has_v && has_s)) b[B_RVDEPS] = 0.0;
+  if (!(has_i && has_s)) b[B_RIAGGS] = 0.0;
+  if (!gtp(hi[2], c.I_RTMIN)) b[B_RIAUTS] = 0.0;
+  if (!(has_v && has_g)) b[B_RVDEPG] = 0.0;
+  if (c.LWARM != 0.0) {
+    if (!(gtp(hl[2], c.C_RTMIN) && pos(hl[0]))) b[B_RCAUTR] = 0.0;
+    if (!(has_c && has_r)) b[B_RCACCR] = 0.0;
+    if (!(has_r && !has_c)) b[B_RREVAV] = 0.0;
+  } else {
+    b[B_RCAUTR] = b[B_RCACCR] = b[B_RREVAV] = 0.0;
+  }
+  if (!has_s) rs[RS_FREEZ1] = rs[RS_FREEZ2] = 0.0;
+  if (!(has_c && has_s)) rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
+  if (!(has_r && has_s)) rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
+  if (!(has_s && warm)) b[B_RSMLTG] = b[B_RCMLTSR] = 0.0;
+  if (!(has_i && has_r)) b[B_RICFRRG] = b[B_RRCFRIG] = b[B_RICFRR] = 0.0;
+  if (!(has_g && has_c)) rg[RG_RCDRYG] = 0.0;
+  if (!(has_g && has_i)) rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
+  if (!(has_s && has_g)) rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
+  if (!(has_r && has_g)) rg[RG_RRDRYG] = 0.0;
+  if (!has_g) rg[RG_FREEZ1] = rg[RG_FREEZ2] = 0.0;
+  if (!(has_g && warm)) b[B_RGMLTR] = 0.0;
+  if (!(pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20))) b[B_RCBERI] = 0.0;
+}
+
+// Freezing-budget split of riming/accretion and the wet/dry growth choice
+// (mode_ice4_fast_rs.F90:144-176, :188-219; mode_ice4_fast_rg.F90:180-260),
+// evaluated on every pass, then the aggregation into the tendency A (per
+// second), mode_ice4_tendencies.F90:606-717 (KRR = 6).
+ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact, double lsfact, Rates &R,
+                       double A[NV])
+{
+  double *b = R.bu;
+  const double *rs = R.rs, *rg = R.rg;
+  const bool has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN);
+  const bool has_g = gtp(v[IRG], c.G_RTMIN), cold = ltp(t, c.TT);
+  double freez = has_s ? pmax0(pmax0(rs[RS_FREEZ1] + rs[RS_FREEZ2] * b[B_RIAGGS]) - b[B_RIAGGS]) : 0.0;
+  if (has_c && has_s && cold) {
+    b[B_RCRIMSS] = dmin(freez, rs[RS_RCRIMSS]);
+    freez = pmax0(freez - b[B_RCRIMSS]);
+    const double zzw0 = dmin(1., freez / dmax(1.e-20, rs[RS_RCRIMS] - b[B_RCRIMSS]));
+    b[B_RCRIMSG] = zzw0 * pmax0(rs[RS_RCRIMS] - b[B_RCRIMSS]);
+    freez = pmax0(freez - b[B_RCRIMSG]);
+    b[B_RSRIMCG] = zzw0 * rs[RS_RSRIMCG] * (signbit(b[B_RCRIMSG]) ? 0.0 : 1.0);
+    b[B_RCRIMSG] = pmax0(b[B_RCRIMSG]);
+  } else {
+    b[B_RCRIMSS] = b[B_RCRIMSG] = b[B_RSRIMCG] = 0.0;
+  }
+  if (has_r && has_s && cold) {
+    b[B_RRACCSS] = dmin(freez, rs[RS_RRACCSS]);
+    freez = pmax0(freez - b[B_RRACCSS]);
+    const double zzw = dmin(1., freez / dmax(1.e-20, rs[RS_RRACCS] - b[B_RRACCSS]));
+    b[B_RRACCSG] = zzw * pmax0(rs[RS_RRACCS] - b[B_RRACCSS]);
+    freez = pmax0(freez - b[B_RRACCSG]);
+    b[B_RSACCRG] = zzw * rs[RS_RSACCRG] * (signbit(b[B_RRACCSG]) ? 0.0 : 1.0);
+    b[B_RRACCSG] = pmax0(b[B_RRACCSG]);
+  } else {
+    b[B_RRACCSS] = b[B_RRACCSG] = b[B_RSACCRG] = 0.0;
   }
   const double rdryg_init = rg[RG_RCDRYG] + rg[RG_RIDRYG] + rg[RG_RSDRYG] + rg[RG_RRDRYG];
-  double rwetg_init = 0.0;
   bool ldwetg = false, lldryg = false;
-  if (v[IRG] > c.G_RTMIN) {
-    if (!soft) {
-      const double den = 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t)));
-      rg[RG_FREEZ1] = heat_term(c, R, t, esi, v[IRV], pf.pres) *
-                      (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag)) * den;
-      rg[RG_FREEZ2] = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
-    }
+  double rwetg_init = 0.0;
+  if (has_g) {
     const double is = rg[RG_RIWETG] + rg[RG_RSWETG];
-    rwetg_init = fmax(is, fmax(0., rg[RG_FREEZ1] + rg[RG_FREEZ2] * is));
-    const double wet = fmax(0., rwetg_init - rg[RG_RIWETG] - rg[RG_RSWETG]);
-    const double dry = fmax(0., rdryg_init - rg[RG_RIDRYG] - rg[RG_RSDRYG]);
-    ldwetg = wet <= dry;
-    if (c.LNULLWETG != 0.0) ldwetg = ldwetg && rdryg_init > 0.;
-    else ldwetg = ldwetg && rwetg_init > 0.;
-    if (c.LWETGPOST == 0.0) ldwetg = ldwetg && t < c.TT;
-    lldryg = t < c.TT && rdryg_init > 1.e-20 && wet > dry;
-  } else {
-    rg[RG_FREEZ1] = rg[RG_FREEZ2] = 0.0;
+    rwetg_init = dmax(is, pmax0(rg[RG_FREEZ1] + rg[RG_FREEZ2] * is));
+    const double wet = pmax0(rwetg_init - rg[RG_RIWETG] - rg[RG_RSWETG]);
+    const double dry = pmax0(rdryg_init - rg[RG_RIDRYG] - rg[RG_RSDRYG]);
+    ldwetg = !gtd(wet, dry);
+    if (c.LNULLWETG != 0.0) ldwetg = ldwetg && pos(rdryg_init);
+    else ldwetg = ldwetg && pos(rwetg_init);
+    if (c.LWETGPOST == 0.0) ldwetg = ldwetg && cold;
+    lldryg = cold && gtp(rdryg_init, 1.e-20) && gtd(wet, dry);
   }
   if (ldwetg) {
     b[B_RRWETG] = -(rg[RG_RIWETG] + rg[RG_RSWETG] + rg[RG_RCDRYG] - rwetg_init);
@@ -511,24 +514,6 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
   } else {
     b[B_RCDRYG] = b[B_RRDRYG] = b[B_RIDRYG] = b[B_RSDRYG] = 0.0;
   }
-  if (v[IRG] > c.G_RTMIN && t > c.TT) {
-    if (!soft) {
-      const double h = heat_term(c, R, t, esw, v[IRV], pf.pres);
-      b[B_RGMLTR] = fmax(0., (-h * (c.O0DEPG * fm::fexp(c.EX0DEPG * x.llbdag) + c.O1DEPG * R.cj * fm::fexp(c.EX1DEPG * x.llbdag)) -
-                              (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c.CL * (c.TT - t))) /
-                                 (rho * c.LMTT));
-    }
-  } else b[B_RGMLTR] = 0.0;
-
-  // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
-  if (R.ssi > 0. && v[IRC] > c.C_RTMIN && v[IRI] > c.I_RTMIN && cit > 1.e-20) {
-    if (!soft) {
-      const double l = fmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(rho * v[IRI] / cit)));
-      b[B_RCBERI] = (R.ssi / (rho * R.ai)) * cit * (c.O0DEPI / l + c.O2DEPI * R.cj * R.cj * fm::fexp(-(c.DI + 2.0) * fm::flog(l)));
-    }
-  } else b[B_RCBERI] = 0.0;
-
-  // ---- aggregation (mode_ice4_tendencies.F90:606-717, KRR = 6) ----
   const double lsv = lsfact - lvfact;
   A[ITH] = b[B_RVDEPG] * lsfact + b[B_RCHONI] * lsv + b[B_RVDEPS] * lsfact - b[B_RREVAV] * lvfact +
            b[B_RCRIMSS] * lsv + b[B_RCRIMSG] * lsv + b[B_RRACCSS] * lsv + b[B_RRACCSG] * lsv +
@@ -548,10 +533,75 @@ ICE3_HD void tendencies(const Cst &c, const double *__restrict__ lut, bool soft,
            b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
 }
 
+// ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
+// nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
+// and all rates are computed; a soft pass keeps the hard-pass rates.
+ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict__ lut, bool soft,
+                        const PointFix &pf, double lvfact, double lsfact, double &cit, double t0,
+                        const double vart[NV], Rates &R, double &rainfr, double hl[4], double hi[4], double A[NV],
+                        double B[NV])
+{
+  double v[NV];
+  double t = t0;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) { v[k] = vart[k]; B[k] = 0.0; }
+  double *b = R.bu;
+  if (!soft) {
+    nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
+    v[ITH] += b[B_RVHENI_MR] * lsfact;
+    t = v[ITH] * pf.exn;
+    v[IRV] -= b[B_RVHENI_MR];
+    v[IRI] += b[B_RVHENI_MR];
+    // RRHONG (mode_ice4_rrhong.F90)
+    double r = 0.0;
+    if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
+      r = v[IRR];
+      if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
+    }
+    b[B_RRHONG_MR] = r;
+    v[ITH] += r * (lsfact - lvfact);
+    t = v[ITH] * pf.exn;
+    v[IRR] -= r;
+    v[IRG] += r;
+    // RIMLTC (mode_ice4_rimltc.F90)
+    r = 0.0;
+    if (pos(v[IRI]) && gtp(t, c.TT)) {
+      r = v[IRI];
+      if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0((v[ITH] - c.TT / pf.exn) / (lsfact - lvfact)));
+    }
+    b[B_RIMLTC_MR] = r;
+    v[ITH] -= r * (lsfact - lvfact);
+    t = v[ITH] * pf.exn;
+    v[IRC] += r;
+    v[IRI] -= r;
+    const double lsv = lsfact - lvfact;
+    B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
+    B[IRV] = -b[B_RVHENI_MR];
+    B[IRC] = b[B_RIMLTC_MR];
+    B[IRR] = -b[B_RRHONG_MR];
+    B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
+    B[IRG] = b[B_RRHONG_MR];
+  } else {
+    b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = 0.0;
+  }
+  double criauti;
+  const double zrainfr = compute_pdf(c, pf.rcrautc, v[IRC], v[IRI], pf.cf, t, pf.sigma_rc, hl, hi, criauti);
+  const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
+  if (llrfr) {
+    rainfr = dmax(rainfr, zrainfr);
+    if ((gtp(v[IRR], c.R_RTMIN) || gtp(v[IRS], c.S_RTMIN) || gtp(v[IRG], c.G_RTMIN)) && zerod(rainfr)) rainfr = 1.;
+  } else {
+    rainfr = 1.;
+  }
+  if (!soft) hard_rates(c, d, lut, pf, t, v, cit, hl, hi, criauti, R);
+  else soft_rates(c, t, v, cit, hl, hi, R);
+  aggregate(c, t, v, lvfact, lsfact, R, A);
+}
+
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
-ICE3_HD unsigned int stepping(const Cst &c, const double *__restrict__ lut, const PointFix &pf, double dt,
-                              int max_passes, double vart[NV], const double ext[NV], double &cit,
+ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
+                              double dt, int max_passes, double vart[NV], const double ext[NV], double &cit,
                               double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped)
 {
   const double rsmin[NV] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN};
@@ -562,12 +612,13 @@ ICE3_HD unsigned int stepping(const Cst &c, const double *__restrict__ lut, cons
   for (int k = 0; k < NRS; ++k) R.rs[k] = 0.0;
 #pragma unroll
   for (int k = 0; k < NRG; ++k) R.rg[k] = 0.0;
-  R.ssi = R.ka = R.dv = R.ai = R.cj = 0.0;
+  R.ssi = 0.0;
   double ztime = 0.0;
   int passes = 0, outer = 0, inner = 0;
   rrevav = 0.0;
   capped = false;
-  while (ztime < dt) {
+  const double zx = c.TT / pf.exn;
+  while (ltd(ztime, dt)) {
     ++outer;
     inner = 0;
     bool llcompute = true, soft = false;
@@ -582,26 +633,25 @@ ICE3_HD unsigned int stepping(const Cst &c, const double *__restrict__ lut, cons
       const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) * izdev;
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) * izdev;
       double A[NV], B[NV];
-      tendencies(c, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
+      tendencies(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
 #pragma unroll
       for (int v = 0; v < NV; ++v) A[v] += ext[v];
       double maxtime = dt - ztime;
       if (c.LFEEDBACKT != 0.0) {
-        const double zx = c.TT / pf.exn;
-        if ((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx) < 0.) maxtime = 0.;
-        if (fabs(A[ITH]) > 1.e-20) {
+        if (negd((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx))) maxtime = 0.;
+        if (abs_gtp(A[ITH], 1.e-20)) {
           const double thr = (zx - B[ITH] - vart[ITH]) / A[ITH];
-          if (thr > 0.) maxtime = fmin(maxtime, thr);
+          if (pos(thr)) maxtime = dmin(maxtime, thr);
         }
       }
 #pragma unroll
       for (int v = 1; v < NV; ++v) {
-        if (A[v] < -1.e-20 && vart[v] > rsmin[v]) {
-          maxtime = fmin(maxtime, -(B[v] + vart[v]) / A[v]);
-          maxtime = fmax(maxtime, c.MNH_TINY);
+        if (ltd(A[v], -1.e-20) && gtp(vart[v], rsmin[v])) {
+          maxtime = dmin(maxtime, -(B[v] + vart[v]) / A[v]);
+          maxtime = dmax(maxtime, c.MNH_TINY);
         }
       }
-      if (ztime + maxtime >= dt) llcompute = false;
+      if (!ltd(ztime + maxtime, dt)) llcompute = false;
       // State update with separately rounded product and sums (no FMA
       // contraction): after a species is depleted, v + A*t + B leaves a
       // rounding residual, and whether it exceeds XRTMIN decides whether the
@@ -611,7 +661,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const double *__restrict__ lut, cons
       // reference) rather than a fused multiply-add.
 #pragma unroll
       for (int v = 0; v < NV; ++v) vart[v] = add_rn(add_rn(vart[v], mul_rn(A[v], maxtime)), B[v]);
-      if (vart[IRI] <= 0.) cit = 0.;
+      if (!pos(vart[IRI])) cit = 0.;
       ztime += maxtime;
       rrevav = R.bu[B_RREVAV];
       soft = true;
@@ -619,6 +669,5 @@ ICE3_HD unsigned int stepping(const Cst &c, const double *__restrict__ lut, cons
   }
   return ((unsigned)outer << 16) | (unsigned)inner;
 }
-
 
 }  // namespace ice3pt

@@ -39,9 +39,9 @@ struct Handle {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
 
-enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_COUNT };
+enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_COUNT };
 const char *kKernelNames[K_COUNT] = {"ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup",
-                                     "fog_deposition"};
+                                     "fog_deposition", "rain_ice_order"};
 
 // Brackets one launch with events when the handle is profiling.
 struct ProfScope {
@@ -184,8 +184,10 @@ SedArgs sed_args(const Ice3gbSedimentationFields &f, int nij, int nk, double dt,
 
 // Launch sequence of one rain_ice call.  `scr` holds 4 control words followed
 // by one pass key per grid point; the first 4 words are cleared here.
+// `order` (n words, or NULL for index order) receives the regime-sorted
+// processing order of the points.
 int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                      const Ice3gbRainIceFields *f, unsigned int *scr, cudaStream_t s)
+                      const Ice3gbRainIceFields *f, unsigned int *scr, unsigned int *order, cudaStream_t s)
 {
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (h->c.LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (h->c.LDEPOSC != 0.0);
@@ -215,7 +217,12 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   a.scr.chunk_counter = scr + 0;
   a.scr.key_max = scr + 1;
   a.scr.keys = scr + 4;
+  a.order = order;
   a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
+  if (order) {
+    ProfScope ps(h, K_ORDER, s);
+    if ((e = launch_rain_ice_order(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice order launch");
+  }
   {
     ProfScope ps(h, K_RAIN_ICE, s);
     e = launch_rain_ice_points(c, a, h->num_sms, s);
@@ -239,16 +246,18 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   return ICE3GB_OK;
 }
 
-// rain_ice with per-call scratch from the stream-ordered allocator.
+// rain_ice with per-call scratch from the stream-ordered allocator: control
+// words, pass keys and (below 2^32 points) the processing order.
 int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                  const Ice3gbRainIceFields *f, cudaStream_t s)
 {
   const long n = (long)nij * nk;
+  const bool ordered = n < 4294967296L;
   unsigned int *scr = nullptr;
-  const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n);
+  const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n * (ordered ? 2 : 1));
   cudaError_t e = cudaMallocAsync(&scr, bytes, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
-  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, scr, s);
+  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, scr, ordered ? scr + 4 + n : nullptr, s);
   cudaFreeAsync(scr, s);
   return rc;
 }
@@ -357,7 +366,7 @@ int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double 
                 (long)nij * nk, scratch_points);
   if ((rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
   if (!scratch) return fail(h, ICE3GB_ERR_CUDA, "static scratch address unavailable");
-  return run_rain_ice_core(h, nij, nk, dt, opt, f, scratch, static_cast<cudaStream_t>(stream));
+  return run_rain_ice_core(h, nij, nk, dt, opt, f, scratch, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 // Records a CUDA error on the handle (or globally) for the other translation units.

@@ -34,6 +34,7 @@ struct RainIceArgs {
   Ice3gbRainIceFields f;
   const double *luts;  // Ice3gbLuts on the device
   RainIceScratch scr;
+  unsigned int *order; // [n] processing order of the grid points, or NULL (index order)
   int nij, nk;
   double dt;
   int max_passes;
@@ -54,4 +55,5 @@ cudaError_t launch_sedimentation(const Ice3gbConstants &c, const SedArgs &a, cud
 cudaError_t launch_fog_deposition(const Ice3gbConstants &c, const FogArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_points(const Ice3gbConstants &c, const RainIceArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s);
+cudaError_t launch_rain_ice_order(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 size_t rain_ice_smem_bytes();

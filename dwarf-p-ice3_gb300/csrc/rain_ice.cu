@@ -16,6 +16,12 @@
 //  * every per-point quantity that is fixed over the sub-steps (log rho and
 //    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;
+//  * points are processed in regime order: a first kernel sorts each tile of
+//    32,768 points by which hydrometeors are present and whether T < TT (the
+//    masks that decide which process branches and how many sub-steps a point
+//    takes), so a warp's lanes take the same branches instead of the union
+//    of all regimes; the tile keeps the gathered accesses within a window of
+//    256 KB per field.  Results do not depend on the order;
 //  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
 //    after the last pass of the call, mode_ice4_stepping.F90:514-516) is
 //    kept with a per-point pass key and a warp-reduced atomicMax, resolved by
@@ -55,9 +61,10 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
     const long base = (long)chunk * blockDim.x;
     __syncthreads();
     if (base >= n) break;
-    const long p = base + threadIdx.x;
+    const long slot = base + threadIdx.x;
     unsigned int key = 0u;
-    if (p < n) {
+    if (slot < n) {
+      const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       PointFix pf;
       pf.exn = ld1(f.exn, p);
       pf.rho = ld1(f.rhodref, p);
@@ -153,6 +160,66 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
   if (any_capped) atomicOr(a.scr.status, ICE3GB_DEV_PASS_CAP);
 }
 
+// Processing order: per tile of ORDER_TILE points, a counting sort by regime
+// (bit 0..4: cloud, rain, ice, snow, graupel above XRTMIN; bit 5: T < TT).
+// Warp-aggregated shared-memory atomics give each point its slot in the tile;
+// the order inside a regime follows the atomics and does not matter.
+constexpr int ORDER_TILE = 32768, ORDER_THREADS = 1024, ORDER_BINS = 64;
+
+__global__ void __launch_bounds__(ORDER_THREADS) rain_ice_order_kernel(const __grid_constant__ Cst c,
+                                                                       const __grid_constant__ RainIceArgs a)
+{
+  __shared__ unsigned char key[ORDER_TILE];
+  __shared__ unsigned int cnt[ORDER_BINS];
+  const Ice3gbRainIceFields &f = a.f;
+  const long n = (long)a.nij * a.nk;
+  const long base = (long)blockIdx.x * ORDER_TILE;
+  const int m = (int)((n - base) < ORDER_TILE ? (n - base) : ORDER_TILE);
+  const unsigned lane = threadIdx.x & 31u;
+  if (threadIdx.x < ORDER_BINS) cnt[threadIdx.x] = 0u;
+  __syncthreads();
+  for (int i0 = 0; i0 < m; i0 += ORDER_THREADS) {       // uniform trip count: full warps in the collectives
+    const int i = i0 + (int)threadIdx.x;
+    unsigned k = 0xffu;
+    if (i < m) {
+      const long p = base + i;
+      k = (gtp(ld1(f.rct, p), c.C_RTMIN) ? 1u : 0u) | (gtp(ld1(f.rrt, p), c.R_RTMIN) ? 2u : 0u) |
+          (gtp(ld1(f.rit, p), c.I_RTMIN) ? 4u : 0u) | (gtp(ld1(f.rst, p), c.S_RTMIN) ? 8u : 0u) |
+          (gtp(ld1(f.rgt, p), c.G_RTMIN) ? 16u : 0u) | (ltp(ld1(f.tht, p) * ld1(f.exn, p), c.TT) ? 32u : 0u);
+      key[i] = (unsigned char)k;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (k != 0xffu && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&cnt[k], (unsigned)__popc(peers));
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {                               // exclusive scan of the 64 counts, two per lane
+    const unsigned c0 = cnt[2 * lane], c1 = cnt[2 * lane + 1];
+    unsigned s = c0 + c1;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= (unsigned)d) s += t;
+    }
+    const unsigned excl = s - (c0 + c1);
+    cnt[2 * lane] = excl;
+    cnt[2 * lane + 1] = excl + c0;
+  }
+  __syncthreads();
+  for (int i0 = 0; i0 < m; i0 += ORDER_THREADS) {
+    const int i = i0 + (int)threadIdx.x;
+    const unsigned k = i < m ? (unsigned)key[i] : 0xffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    const unsigned leader = (unsigned)(__ffs(peers) - 1);
+    unsigned first = 0u;
+    if (k != 0xffu && lane == leader) first = atomicAdd(&cnt[k], (unsigned)__popc(peers));
+    first = __shfl_sync(0xffffffffu, first, (int)leader);
+    if (k != 0xffu) {
+      const unsigned rank = (unsigned)__popc(peers & ((1u << lane) - 1u));
+      a.order[base + first + rank] = (unsigned int)(base + i);
+    }
+  }
+}
+
 // PRREVAV after the last pass of the call: zero evap3d on micro points that
 // were not active in that pass (mode_ice4_stepping.F90:514-516).
 __global__ void rain_ice_evap_fixup_kernel(double *__restrict__ evap3d, const unsigned int *__restrict__ keys,
@@ -180,6 +247,14 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
   if (blocks > chunks) blocks = chunks;
   if (blocks < 1) blocks = 1;
   rain_ice_points_kernel<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rain_ice_order(const Cst &c, const RainIceArgs &a, cudaStream_t s)
+{
+  const long n = (long)a.nij * a.nk;
+  const long tiles = (n + ORDER_TILE - 1) / ORDER_TILE;
+  rain_ice_order_kernel<<<(unsigned)tiles, ORDER_THREADS, 0, s>>>(c, a);
   return cudaGetLastError();
 }
 

@@ -84,7 +84,7 @@ EXPORTED = (
     "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc",
 )
 NOALLOC_MAX_POINTS = 4194304
-KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition")
+KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order")
 
 _lib: Optional[ctypes.CDLL] = None
 

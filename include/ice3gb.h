@@ -264,8 +264,8 @@ int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3
  * those events and returns, per kernel id, the number of launches and their
  * summed device time since the last enable.  Kernel ids: 0 ice_adjust,
  * 1 sedimentation, 2 rain_ice (pointwise sub-stepping), 3 rain_ice evap3d
- * fix-up, 4 fog deposition. */
-#define ICE3GB_NKERNELS 5
+ * fix-up, 4 fog deposition, 5 rain_ice point ordering (regime sort). */
+#define ICE3GB_NKERNELS 6
 int         ice3gb_profile_enable(void *handle, int enable);
 int         ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms);
 const char *ice3gb_kernel_name(int kernel_id);

@@ -26,6 +26,18 @@
 //          r = z*invc - 1 exact in one FMA (|r| < 2^-7); log x = e ln2 -
 //          log(invc) + log1p(r), log1p by its Taylor series (to r^4 in FP64,
 //          r^5 .. r^8 in FP32).  9 FP64 ops.
+//   frcp   1/d: a correctly rounded FP32 reciprocal of d (truncated to FP32)
+//          as the seed r0 (|eps| = |1 - d r0| < 2^-22), then one Newton-
+//          Raphson step with the quadratic term of 1/(1-eps) = 1 + eps +
+//          eps^2 + ..., r1 = r0 (1 + eps + eps^2), leaving eps^3 < 2^-66.
+//          3 FP64 ops (an IEEE FP64 divide costs ~9 on GB300).  fdiv(a, b) =
+//          a * frcp(b), within 2 ulp.  Outside 2^-125 < |d| < 2^125 (and for
+//          zero, inf, NaN) it falls back to the IEEE division.
+//   fatan  reduction to [0, 1] by atan(x) = pi/2 - atan(1/x), then
+//          atan(y) = atan(c) + atan(r), c = j/64 the nearest table point,
+//          r = (y - c)/(1 + y c) (|r| <= 1/128), atan(r) by its Taylor series
+//          (r^3 in FP64, r^5 .. r^9 in FP32); atan(c) and pi/2 - atan(c)
+//          tabulated.  ~15 FP64 ops.
 //
 // Accuracy: within 2 ulp (tests compare the host build of this code with
 // 200-bit mpmath values, and the device build with the host build bit for
@@ -53,11 +65,21 @@
 namespace fm {
 
 struct ExpEntry { double hi; float lo; int pad; };
+struct AtanEntry { double hi; float lo; int pad; };
 struct LogEntry { double invc, nlog_hi; float nlog_lo; int fold; double pad; };
 
 #if defined(__CUDA_ARCH__)
 __device__ const ExpEntry kExpTable[256] = FM_EXP_TABLE_INIT;
 __device__ const LogEntry kLogTable[128] = FM_LOG_TABLE_INIT;
+__device__ const AtanEntry kAtanTable[65] = FM_ATAN_TABLE_INIT;
+__device__ const AtanEntry kAtanCTable[65] = FM_ATANC_TABLE_INIT;
+__device__ __forceinline__ void atan_entry(bool comp, int j, double &hi, float &lo)
+{
+  const double2 v = __ldg(reinterpret_cast<const double2 *>(comp ? kAtanCTable : kAtanTable) + j);
+  hi = v.x;
+  lo = __int_as_float((int)(uint32_t)__double_as_longlong(v.y));
+}
+__device__ __forceinline__ float rcpf_(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ void exp_entry(int j, double &hi, float &lo)
 {
   const double2 v = __ldg(reinterpret_cast<const double2 *>(kExpTable) + j);
@@ -85,6 +107,14 @@ __device__ __forceinline__ int clz32_(uint32_t v) { return __clz((int)v); }
 #else
 static const ExpEntry kExpTable[256] = FM_EXP_TABLE_INIT;
 static const LogEntry kLogTable[128] = FM_LOG_TABLE_INIT;
+static const AtanEntry kAtanTable[65] = FM_ATAN_TABLE_INIT;
+static const AtanEntry kAtanCTable[65] = FM_ATANC_TABLE_INIT;
+inline void atan_entry(bool comp, int j, double &hi, float &lo)
+{
+  const AtanEntry &e = comp ? kAtanCTable[j] : kAtanTable[j];
+  hi = e.hi; lo = e.lo;
+}
+inline float rcpf_(float x) { volatile float r = 1.0f / x; return r; }
 inline void exp_entry(int j, double &hi, float &lo) { hi = kExpTable[j].hi; lo = kExpTable[j].lo; }
 inline void log_entry(int i, double &invc, double &nlog_hi, float &nlog_lo, int &fold)
 {
@@ -229,6 +259,46 @@ FM_HD double flog(double x)
   q = fma_(r, q, -0.5);
   const double tail = fma_(mul_(r, r), q, to_f64(lo));
   return add_(hi, add_(r, tail));
+}
+
+// 1/d (see the header): FP32 seed + one Newton-Raphson step with its
+// quadratic term.
+FM_HD double frcp(double d)
+{
+  const int64_t e = (bits_(d) >> 52) & 0x7ff;
+  if (e < 1023 - 125 || e > 1023 + 125) return 1.0 / d;          // zero, tiny, huge, inf, NaN
+  const double r0 = to_f64(rcpf_(to_f32(d)));
+  const double eps = fma_(-d, r0, 1.0);
+  return fma_(r0, fma_(eps, eps, eps), r0);
+}
+FM_HD double fdiv(double a, double b) { return mul_(a, frcp(b)); }
+
+// Arc tangent (see the header).
+FM_HD double fatan(double x)
+{
+  const int64_t b = bits_(x), ab = b & 0x7fffffffffffffffLL;
+  if (ab < 0x3e10000000000000LL) return x;                        // |x| < 2^-30: atan x = x (1 - x^2/3), +-0
+  if (ab > 0x43b0000000000000LL) {                                // |x| > 2^60, inf, NaN
+    if (ab > 0x7ff0000000000000LL) return x;
+    return b < 0 ? -FM_PIO2 : FM_PIO2;
+  }
+  const bool comp = ab > 0x3ff0000000000000LL;                    // |x| > 1: pi/2 - atan(1/|x|)
+  const double ax = from_bits_(ab);
+  const double y = comp ? frcp(ax) : ax;
+  const int32_t j = rint_f32(mulf_(to_f32(y), 64.0f));            // 0..64
+  const double c = j == 0 ? 0.0 : from_bits_(bits_(i2d(j)) - ((int64_t)6 << 52));   // j/64, exact
+  const double r = mul_(add_(y, -c), frcp(fma_(y, c, 1.0)));      // y - c exact (Sterbenz)
+  const double r2 = mul_(r, r);
+  const float r2f = to_f32(r2);
+  // (atan r - r) / r^3 = -1/3 + r^2 (1/5 - r^2/7 + r^4/9)
+  const float s = fmaf_(r2f, fmaf_(r2f, 1.0f / 9.0f, -1.0f / 7.0f), 1.0f / 5.0f);
+  const double q = fma_(r2, to_f64(s), -1.0 / 3.0);
+  const double at = fma_(mul_(r2, r), q, r);
+  double hi;
+  float lo;
+  atan_entry(comp, j, hi, lo);
+  const double res = comp ? add_(hi, add_(to_f64(lo), -at)) : add_(hi, add_(to_f64(lo), at));
+  return b < 0 ? -res : res;
 }
 
 // x^a = e^(a log x) for x > 0 (relative error ~|a log x| ulp).

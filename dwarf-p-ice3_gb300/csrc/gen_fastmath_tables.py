@@ -7,6 +7,9 @@ and rounded to nearest.
 exp (Tang, ACM TOMS 15(2), 1989): 2^(j/256), j = 0..255, as a double hi and
 a float lo (the rounding error of hi, < 2^-53, needs only ~20 bits).
 
+atan (table-driven reduction in the manner of Tang's methods): atan(j/64) and
+pi/2 - atan(j/64), j = 0..64, as a double hi and a float lo.
+
 log (Tang, ACM TOMS 16(4), 1990, with an exact reduction): the mantissa
 z in [1, 2) is split into 128 intervals by its 7 leading fraction bits.
 Intervals at or above sqrt(2) are folded (z/2, exponent + 1) so that results
@@ -74,6 +77,19 @@ def main() -> None:
         lo = flt(v - mp.mpf(hi))
         invc_tab = invc / 2 if fold else invc
         lines.append(f"  {{{invc_tab.hex()}, {hi.hex()}, {fhex(lo)}, {1 if fold else 0}, 0.0}}, \\")
+    lines += ["}", "",
+              "// atan(j/64): {hi (double), lo (float)}, j = 0..64",
+              "#define FM_ATAN_TABLE_INIT { \\"]
+    for j in range(65):
+        a = mp.atan(mp.mpf(j) / 64)
+        ah = dbl(a)
+        lines.append(f"  {{{ah.hex()}, {fhex(flt(a - mp.mpf(ah)))}, 0}}, \\")
+    lines += ["}", "", "// pi/2 - atan(j/64): {hi (double), lo (float)}, j = 0..64",
+              "#define FM_ATANC_TABLE_INIT { \\"]
+    for j in range(65):
+        b = mp.pi / 2 - mp.atan(mp.mpf(j) / 64)
+        bh = dbl(b)
+        lines.append(f"  {{{bh.hex()}, {fhex(flt(b - mp.mpf(bh)))}, 0}}, \\")
     lines += ["}", ""]
     ln2_hi = round_bits(mp.log(2), 42)             # e*ln2_hi exact for |e| < 2^11
     l256 = mp.log(2) / 256
@@ -85,6 +101,7 @@ def main() -> None:
         "FM_INV_LG256_F": fhex(flt(256 / mp.log10(2))),
         "FM_LG256_HI": dbl(lg256).hex(), "FM_LG256_LO_F": fhex(flt(lg256 - mp.mpf(dbl(lg256)))),
         "FM_LN10": dbl(mp.log(10)).hex(), "FM_LN10_F": fhex(flt(mp.log(10))),
+        "FM_PIO2": dbl(mp.pi / 2).hex(),
     }
     for k, v in consts.items():
         lines.append(f"#define {k} {v}")

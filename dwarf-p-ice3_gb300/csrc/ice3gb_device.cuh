@@ -46,26 +46,31 @@ ICE3_HD double add_rn(double a, double b)
   return p;
 #endif
 }
-// NaN-propagating minimum/maximum/clip, as numpy's minimum/maximum/clip
-// (the reference JAX lets NaN through on degenerate inputs, e.g. a negative
-// vapour source with no mass flux, stencils/ice_adjust.py:293-296); CUDA's
-// fmin/fmax would return the other operand instead.
-ICE3_HD double nmin(double a, double b) { return (a < b || a != a) ? a : b; }
-ICE3_HD double nmax(double a, double b) { return (a > b || a != a) ? a : b; }
-ICE3_HD double nclip01(double x) { return nmin(nmax(x, 0.0), 1.0); }
-
 // Comparisons and clamps on the IEEE bit patterns.  On GB300 an FP64 compare
 // (and so fmin/fmax) issues on the FP64 pipe at the FP64 FMA rate, while the
 // same test on the 64-bit pattern runs on the integer pipe at ~30x the rate.
-// Ordering key: for finite and infinite doubles, the signed 64-bit integer
-// bits ^ (sign ? 0x7fff... : 0) is monotone in the value (-0 sorts just below
-// +0).  NaN operands are not supported: callers use these on values that are
-// finite by construction.
+// Ordering key: for non-NaN doubles the signed 64-bit integer
+// (sign ? -|bits| : bits) orders like the values, with -0 and +0 equal as
+// IEEE compares them.  The plain versions below do not handle NaN operands
+// (their callers see finite values by construction); nmin/nmax do.
 ICE3_HD int64_t dkey(double x)
 {
   const int64_t b = fm::bits_(x);
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+  return b < 0 ? -(b & 0x7fffffffffffffffLL) : b;
 }
+ICE3_HD bool isnan_(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+
+// NaN-propagating minimum/maximum/clip, as numpy's minimum/maximum/clip
+// (the reference JAX lets NaN through on degenerate inputs, e.g. a negative
+// vapour source with no mass flux, stencils/ice_adjust.py:293-296); CUDA's
+// fmin/fmax would return the other operand instead.  Same results as
+// (a < b || a != a) ? a : b, evaluated on the integer pipe.
+ICE3_HD double nmin(double a, double b) { return (isnan_(a) || (!isnan_(b) && dkey(a) < dkey(b))) ? a : b; }
+ICE3_HD double nmax(double a, double b) { return (isnan_(a) || (!isnan_(b) && dkey(a) > dkey(b))) ? a : b; }
+ICE3_HD double nclip01(double x) { return nmin(nmax(x, 0.0), 1.0); }
+// IEEE a > b / a >= b (false when either is NaN), on the integer pipe.
+ICE3_HD bool fgt(double a, double b) { return !isnan_(a) && !isnan_(b) && dkey(a) > dkey(b); }
+ICE3_HD bool fge(double a, double b) { return !isnan_(a) && !isnan_(b) && dkey(a) >= dkey(b); }
 ICE3_HD bool gtd(double a, double b) { return dkey(a) > dkey(b); }        // a > b
 ICE3_HD bool ltd(double a, double b) { return dkey(a) < dkey(b); }        // a < b
 // a > b for a threshold b >= +0 (a of any sign): the raw patterns suffice.
@@ -76,6 +81,8 @@ ICE3_HD bool pos(double a) { return fm::bits_(a) > 0; }                   // a >
 ICE3_HD double pmax0(double a) { return pos(a) ? a : 0.0; }               // fmax(0, a)
 ICE3_HD double dmax(double a, double b) { return gtd(a, b) ? a : b; }
 ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
+// a == +-0.
+ICE3_HD bool zerod_(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) == 0; }
 // |a| > b for b >= +0.
 ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > fm::bits_(b); }
 

@@ -23,22 +23,28 @@ struct IaOut {
 ICE3_HD void triangle_pdf(double w_dt, double crit, double cf_mf, double &hcf, double &hr)
 {
   const double wmax = nmax(1e-20, w_dt);
-  const double inv_w2 = 1.0 / sq(wmax);
-  if (w_dt > crit) {
+  const double inv_w2 = fm::frcp(sq(wmax));
+  if (fgt(w_dt, crit)) {
     const double cc = crit * cf_mf;
     hcf = 1.0 - 0.5 * sq(cc) * inv_w2;
-    hr = w_dt - cc * cc * cc * (inv_w2 / 3.0);
-  } else if (2.0 * w_dt <= crit) {
+    hr = w_dt - cc * cc * cc * (inv_w2 * (1.0 / 3.0));
+  } else if (fge(crit, 2.0 * w_dt)) {
     hcf = 0.0;
     hr = 0.0;
   } else {
     hcf = 0.5 * sq(2.0 * w_dt - crit) * inv_w2;
-    hr = (4.0 * w_dt * w_dt * w_dt - 3.0 * w_dt * sq(crit) + crit * crit * crit) * (inv_w2 / 3.0);
+    hr = (4.0 * w_dt * w_dt * w_dt - 3.0 * w_dt * sq(crit) + crit * crit * crit) * (inv_w2 * (1.0 / 3.0));
   }
   hcf *= cf_mf;
 }
 
-ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaOut &o)
+// Constants derived once per thread (divisions of table constants).
+struct IaDerived {
+  double rdrv, rvrd, irv;   // RD/RV, RV/RD, 1/RV
+};
+ICE3_HD IaDerived ia_derived(const Cst &c) { return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV}; }
+
+ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt, const IaIn &x, IaOut &o)
 {
   const int nrr = (int)c.NRR;
   double t = x.th * x.exn;
@@ -49,62 +55,62 @@ ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaO
   else if (nrr == 4) cph = c.CPD + c.CPV * x.rv + c.CL * (x.rc + x.rr);
   else if (nrr == 2) cph = c.CPD + c.CPV * x.rv + c.CL * x.rc + c.CI * x.ri;
   else cph = c.CPD + c.CPV * x.rv + c.CL * (x.rc + x.rr) + c.CI * (x.ri + x.rs + x.rg);
-  const double inv_cph = 1.0 / cph;
+  const double inv_cph = fm::frcp(cph);
   double cldfr = 0.0, rv_out = 0.0, rc_out = 0.0, ri_out = 0.0;
   double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
   if (c.LSUBG_COND != 0.0) {
     const double rt = x.rv + x.rc + x.ri;
     // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
-    const double lt = fm::flog(t), it = 1.0 / t;
+    const double lt = fm::flog(t), it = fm::frcp(t);
     const double pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
     const double piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
-    double frac = (x.rc + x.ri > 1e-20) ? x.rc / (x.rc + x.ri) : 0.0;
+    double frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
     const int fmode = (int)c.FRAC_ICE_ADJUST;
     if (fmode == 3) frac = nclip01(frac);
-    else if (fmode == 0) frac = nclip01((c.TMAXMIX - t) / (c.TMAXMIX - c.TMINMIX));
-    const double rdrv = c.RD / c.RV;
-    double qsl = rdrv * pv / (x.pabs - pv);
-    const double qsi = rdrv * piv / (x.pabs - piv);
+    else if (fmode == 0) frac = nclip01(fm::fdiv(c.TMAXMIX - t, c.TMAXMIX - c.TMINMIX));
+    double qsl = fm::fdiv(d.rdrv * pv, x.pabs - pv);
+    const double qsi = fm::fdiv(d.rdrv * piv, x.pabs - piv);
     qsl = (1.0 - frac) * qsl + frac * qsi;
     const double lvs = (1.0 - frac) * lv + frac * ls;
-    const double ah = lvs * qsl / (c.RV * t * t) * (1.0 + c.RV * qsl / c.RD);
-    const double a = 1.0 / (1.0 + lvs * inv_cph * ah);
+    const double ah = lvs * qsl * (it * it * d.irv) * (1.0 + qsl * d.rvrd);
+    const double a = fm::frcp(1.0 + lvs * inv_cph * ah);
     const double sbar = a * (rt - qsl + ah * lvs * (x.rc + x.ri) * inv_cph);
     double sigma;
     if (c.LSIGMAS != 0.0 && c.LSTATNW == 0.0)
-      sigma = (x.sigqsat != 0.0) ? sqrt(sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a)) : 2.0 * x.sigs;
+      sigma = !(fge(x.sigqsat, 0.0) && fge(0.0, x.sigqsat)) ? sqrt(sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a))
+                                                             : 2.0 * x.sigs;
     else
       sigma = 2.0 * x.sigs;
     sigma = nmax(1e-10, sigma);
-    const double q1 = sbar / sigma;
+    const double q1 = fm::fdiv(sbar, sigma);
     double cond;
-    if (q1 > 0.0) cond = (q1 <= 2.0) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;
+    if (fgt(q1, 0.0)) cond = fge(2.0, q1) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;
     else cond = fm::fexp(1.2 * q1 - 1.0);
     cond *= sigma;
-    cldfr = (cond >= 1e-12) ? nclip01(0.5 + 0.36 * atan(1.55 * q1)) : 0.0;
-    if (cldfr == 0.0) cond = 0.0;
+    cldfr = fge(cond, 1e-12) ? nclip01(0.5 + 0.36 * fm::fatan(1.55 * q1)) : 0.0;
+    if (fge(cldfr, 0.0) && fge(0.0, cldfr)) cond = 0.0;
     rc_out = (1.0 - frac) * cond;
     ri_out = frac * cond;
     t = t + ((rc_out - x.rc) * lv + (ri_out - x.ri) * ls) * inv_cph;
     rv_out = rt - rc_out - ri_out;
   }
   double rvs = x.rvs, rcs = x.rcs, ris = x.ris, ths = x.ths;
-  const double inv_cphex = inv_cph / x.exn_ref;
+  const double inv_cphex = fm::fdiv(inv_cph, x.exn_ref);
   double w1 = (rc_out - x.rc) * inv_dt, w2 = (ri_out - x.ri) * inv_dt;
-  w1 = (w1 < 0.0) ? nmax(w1, -rcs) : nmin(w1, rvs);
+  w1 = fgt(0.0, w1) ? nmax(w1, -rcs) : nmin(w1, rvs);
   rvs = rvs - w1;
   rcs = rcs + w1;
   ths = ths + w1 * lv * inv_cphex;
-  w2 = (w2 < 0.0) ? nmax(w2, -ris) : nmin(w2, rvs);
+  w2 = fgt(0.0, w2) ? nmax(w2, -ris) : nmin(w2, rvs);
   rvs = rvs - w2;
   ris = ris + w2;
   ths = ths + w2 * ls * inv_cphex;
   if (c.LSUBG_COND == 0.0) {
-    cldfr = ((rcs + ris) * dt > 1e-12) ? 1.0 : 0.0;
+    cldfr = fgt((rcs + ris) * dt, 1e-12) ? 1.0 : 0.0;
   } else {
     double w1m = x.rc_mf * inv_dt, w2m = x.ri_mf * inv_dt;
     const double tot = w1m + w2m;
-    const double scale = (tot > rvs) ? rvs / tot : 1.0;
+    const double scale = fgt(tot, rvs) ? fm::fdiv(rvs, tot) : 1.0;
     w1m *= scale;
     w2m *= scale;
     cldfr = nmin(1.0, cldfr + x.cf_mf);
@@ -114,11 +120,11 @@ ICE3_HD void ia_point(const Cst &c, double dt, double inv_dt, const IaIn &x, IaO
     ths = ths + (w1m * lv + w2m * ls) * inv_cphex;
     const int mfpdf = (int)c.SUBG_MF_PDF;
     if (mfpdf == 0 || mfpdf == 1) {
-      const double criaut = c.CRIAUTC / x.rho;
+      const double criaut = fm::fdiv(c.CRIAUTC, x.rho);
       const double criaut_i = nmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
       if (mfpdf == 0) {
-        if (w1m * dt > x.cf_mf * criaut) { hlc_hrc = w1m * dt; hlc_hcf = nmin(1.0, x.cf_mf); }
-        if (w2m * dt > x.cf_mf * criaut_i) { hli_hri = w2m * dt; hli_hcf = nmin(1.0, x.cf_mf); }
+        if (fgt(w1m * dt, x.cf_mf * criaut)) { hlc_hrc = w1m * dt; hlc_hcf = nmin(1.0, x.cf_mf); }
+        if (fgt(w2m * dt, x.cf_mf * criaut_i)) { hli_hri = w2m * dt; hli_hcf = nmin(1.0, x.cf_mf); }
       } else {
         double hcf, hr;
         triangle_pdf(w1m * dt, x.cf_mf * criaut, x.cf_mf, hcf, hr);
@@ -149,6 +155,7 @@ __global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constan
 {
   const Ice3gbIceAdjustFields &f = kf.f;
   const double inv_dt = 1.0 / dt;
+  const IaDerived d = ia_derived(c);
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < npairs; q += (long)gridDim.x * blockDim.x) {
     const long p = 2 * q;
     IaIn x0, x1;
@@ -184,8 +191,8 @@ __global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constan
       x1.sigqsat = ld1(f.sigqsat, (p + 1) % nij);
     }
     IaOut o0, o1;
-    ia_point(c, dt, inv_dt, x0, o0);
-    ia_point(c, dt, inv_dt, x1, o1);
+    ia_point(c, d, dt, inv_dt, x0, o0);
+    ia_point(c, d, dt, inv_dt, x1, o1);
 #define ST2(field) if (f.field) st2(f.field, p, o0.field, o1.field);
     ST2(t) ST2(rv_out) ST2(rc_out) ST2(ri_out) ST2(cldfr) ST2(hlc_hrc) ST2(hlc_hcf) ST2(hli_hri) ST2(hli_hcf)
     ST2(cph) ST2(lv) ST2(ls) ST2(rvs) ST2(rcs) ST2(ris) ST2(ths)
@@ -201,6 +208,7 @@ __global__ void __launch_bounds__(256) ice_adjust_v1_kernel(const __grid_constan
 {
   const Ice3gbIceAdjustFields &f = kf.f;
   const double inv_dt = 1.0 / dt;
+  const IaDerived d = ia_derived(c);
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
     IaIn x;
     x.sigqsat = f.sigqsat_3d ? ld1(f.sigqsat, p) : ld1(f.sigqsat, p % nij);
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__(256) ice_adjust_v1_kernel(const __grid_constan
       x.rr = ld1(f.rr, p); x.rs = ld1(f.rs, p); x.rg = ld1(f.rg, p);
     }
     IaOut o;
-    ia_point(c, dt, inv_dt, x, o);
+    ia_point(c, d, dt, inv_dt, x, o);
 #define ST1(field) if (f.field) f.field[p] = o.field;
     ST1(t) ST1(rv_out) ST1(rc_out) ST1(ri_out) ST1(cldfr) ST1(hlc_hrc) ST1(hlc_hcf) ST1(hli_hri) ST1(hli_hcf)
     ST1(cph) ST1(lv) ST1(ls) ST1(rvs) ST1(rcs) ST1(ris) ST1(ths)

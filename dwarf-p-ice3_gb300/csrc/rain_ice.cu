@@ -50,10 +50,7 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
   __syncthreads();
   const Ice3gbRainIceFields &f = a.f;
   const long n = (long)a.nij * a.nk;
-  const double dt = a.dt, inv_dt = 1.0 / a.dt;
-  const bool lwarm = c.LWARM != 0.0;
-  const bool sigm = (int)c.SUBG_AUCV_RC == 1 && (int)c.SUBG_PR_PDF == 0;
-  const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
+  const double dt = a.dt;
   bool any_capped = false;
   for (;;) {
     if (threadIdx.x == 0) chunk = atomicAdd(a.scr.chunk_counter, 1u);
@@ -65,94 +62,9 @@ __global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __
     unsigned int key = 0u;
     if (slot < n) {
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
-      PointFix pf;
-      pf.exn = ld1(f.exn, p);
-      pf.rho = ld1(f.rhodref, p);
-      pf.pres = ld1(f.pabs, p);
-      const double th = ld1(f.tht, p), rv = ld1(f.rvt, p), rc = ld1(f.rct, p), rr = ld1(f.rrt, p);
-      const double ri = ld1(f.rit, p), rs = ld1(f.rst, p), rg = ld1(f.rgt, p);
-      const double exnref = ld1(f.exnref, p);
-      double ths = f.ths[p], rvs = f.rvs[p], rcs = f.rcs[p], rrs = f.rrs[p], ris = f.ris[p], rss = f.rss[p],
-             rgs = f.rgs[p];
-      double cit = f.cit[p];
-      // rain_ice.F90:334-345 (L/cph without exner) and :370-381 (LLMICRO)
-      const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
-      const double t = th * pf.exn;
-      const double izdev = 1.0 / zdev;
-      const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * izdev;
-      const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * izdev;
-      const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
-                         gtp(rg, c.G_RTMIN);
-      const double iexnref = 1.0 / exnref;
-      const double lsx = lsf * iexnref, lvx = lvf * iexnref;
-      double evap = 0.0, rainfr = 1.0;
-      double zrvheni = 0.0;
-      if (!micro) {
-        cit = 0.0;
-        nucleation(c, dsh, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
-      }
-      zrvheni = dmin(rvs, zrvheni * inv_dt);
-      if (micro) {
-        pf.lrho = fm::flog(pf.rho);
-        pf.rho_mcexvt = fm::fexp(-c.CEXVT * pf.lrho);
-        pf.rho_mcexvt1 = pf.rho_mcexvt / pf.rho;
-        pf.rcrautc = c.CRIAUTC / pf.rho;
-        pf.cf = ld1(f.cldfr, p);
-        pf.sigma_rc = sigm ? 2.0 * ld1(f.sigs, p) : 0.0;
-        double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
-        double ext[NV] = {ths - th * inv_dt, rvs - rv * inv_dt, rcs - rc * inv_dt, rrs - rr * inv_dt,
-                          ris - ri * inv_dt, rss - rs * inv_dt, rgs - rg * inv_dt};
-        double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
-        if (adju) {
-          hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
-          hl[3] = rc - hl[2];
-          hi[3] = ri - hi[2];
-          hl[1] = pos(rc) ? pf.cf - hl[0] : 0.;
-          hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
-        }
-        double rrevav;
-        bool capped;
-        key = stepping(c, dsh, lut, pf, dt, a.max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
-        any_capped |= capped;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
-        evap = lwarm ? rrevav : 0.0;
-        // total tendencies (rain_ice.F90:758-790)
-        const double wv = (vart[IRV] - rv) * inv_dt, wc = (vart[IRC] - rc) * inv_dt;
-        const double wr = (vart[IRR] - rr) * inv_dt, wi = (vart[IRI] - ri) * inv_dt;
-        const double ws = (vart[IRS] - rs) * inv_dt, wg = (vart[IRG] - rg) * inv_dt;
-        ths += (wc + wr) * lvx + (wi + ws + wg) * lsx + zrvheni * lsx;
-        rvs += wv - zrvheni;
-        rcs += wc;
-        rrs += wr;
-        ris += wi + zrvheni;
-        rss += ws;
-        rgs += wg;
-      } else {
-        ths += zrvheni * lsx;
-        rvs -= zrvheni;
-        ris += zrvheni;
-      }
-      // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the sources
-      double w;
-      w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
-      w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
-      w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
-      w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
-      w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
-      w = dmin(1., pmax0(c.V_RTMIN - rvs) / dmax(rcs + ris, 1.e-20));
-      ths -= w * (rcs * lvx + ris * lsx);
-      rvs += w * (rcs + ris);
-      rcs = (1. - w) * rcs;
-      ris = (1. - w) * ris;
-      w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
-      w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
-      w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
-      f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
-      f.rgs[p] = rgs;
-      f.cit[p] = cit;
-      f.evap3d[p] = evap;
-      f.rainfr[p] = rainfr;
+      bool capped;
+      key = rain_ice_point(c, dsh, lut, f, p, dt, a.max_passes, capped);
+      any_capped |= capped;
       a.scr.keys[p] = key;
     }
     warp_key_max(a.scr.key_max, key);

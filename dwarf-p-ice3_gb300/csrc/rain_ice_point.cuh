@@ -46,6 +46,7 @@ enum { RG_RCDRYG, RG_RIDRYG, RG_RIWETG, RG_RSDRYG, RG_RSWETG, RG_RRDRYG, RG_FREE
 struct Derived {
   double lLBR, lLBS, lLBG, lLBDAS_MAX, lTT;   // logs of table constants
   double nu20_eb2;                            // NU20 * exp(-BETA2)
+  double irv;                                 // 1/RV
 };
 
 ICE3_HD void make_derived(const Cst &c, Derived &d)
@@ -56,6 +57,7 @@ ICE3_HD void make_derived(const Cst &c, Derived &d)
   d.lLBDAS_MAX = fm::flog(c.LBDAS_MAX);
   d.lTT = fm::flog(c.TT);
   d.nu20_eb2 = c.NU20 * fm::fexp(-c.BETA2);
+  d.irv = 1.0 / c.RV;
 }
 
 // Rates that persist between the hard pass and the following soft passes
@@ -91,23 +93,25 @@ ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst
 {
   rvheni = 0.0;
   if (!(ltp(t, c.TT) && gtp(rvt, c.V_RTMIN))) return;
-  const double lt = fm::flog(t), it = 1.0 / t;
+  const double lt = fm::flog(t), it = fm::frcp(t);
   double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   double zzw = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
   zzw = dmin(pabst * 0.5, zzw);
-  double zssi = rvt * (pabst - zzw) / (c.EPSILO * zzw) - 1.0;
+  double zssi = fm::fdiv(rvt * (pabst - zzw), c.EPSILO * zzw) - 1.0;
   zusw = dmin(pabst * 0.5, zusw);
-  zusw = (zusw / zzw) * ((pabst - zzw) / (pabst - zusw)) - 1.0;
+  zusw = fm::fdiv(zusw * (pabst - zzw), zzw * (pabst - zusw)) - 1.0;
   zssi = dmin(zssi, zusw);
   zzw = 0.0;
   if (ltp(t, c.TT - 5.0) && pos(zssi)) {
     zzw = c.NU20 * fm::fexp(c.ALPHA2 * zssi - c.BETA2);
   } else if (!gtp(t, c.TT - 2.0) && !ltp(t, c.TT - 5.0) && pos(zssi)) {
-    zzw = dmax(d.nu20_eb2, c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(zssi / zusw)));
+    zzw = dmax(d.nu20_eb2, c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(fm::fdiv(zssi, zusw))));
   }
   zzw = dmin(zzw - cit, 50.e3);
-  rvheni = dmin(rvt, pmax0(zzw) * c.MNU0 / rhodref);
+  rvheni = dmin(rvt, fm::fdiv(pmax0(zzw) * c.MNU0, rhodref));
   if (c.LFEEDBACKT != 0.0) {
+    // IEEE divisions: the limiter puts th exactly on TT/exn, and the next
+    // T < TT test must see the same rounding as the Fortran
     const double w = dmin(rvheni, pmax0((c.TT / exn - tht) / lsfact)) / dmax(rvheni, 1.e-20);
     rvheni *= w;
     zzw *= w;
@@ -137,7 +141,7 @@ ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit,
     if (gtd(rct, rcrautc + sigma_rc)) {
       hcf = 1.0; hrc = rct;
     } else if (gtd(rct, rcrautc - sigma_rc)) {
-      const double inv2s = 1.0 / (2.0 * sigma_rc);
+      const double inv2s = fm::frcp(2.0 * sigma_rc);
       hcf = (rct + sigma_rc - rcrautc) * inv2s;
       lcf = pmax0(cf - hcf);
       hrc = (rct + sigma_rc - rcrautc) * (rct + sigma_rc + rcrautc) * (0.5 * inv2s);
@@ -253,15 +257,16 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
   // derived fields (mode_ice4_tendencies.F90:303-320)
-  const double lt = fm::flog(t), it = 1.0 / t;
+  const double lt = fm::flog(t), it = fm::frcp(t);
   const double esi = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
   const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
-  R.ssi = v[IRV] * (pf.pres - esi) / (c.EPSILO * esi) - 1.0;
+  R.ssi = fm::fdiv(v[IRV] * (pf.pres - esi), c.EPSILO * esi) - 1.0;
   const double ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
-  const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * (c.P00 / pf.pres);
-  const double ai = sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / (ka * c.RV * t * t) + (c.RV * t) / (dv * esi);
-  const double cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) / sqrt(1.718e-5 + 4.9e-8 * (t - c.TT));
-  const double ssi_rai = R.ssi / (rho * ai);
+  const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
+  const double ika = fm::frcp(ka), idv = fm::frcp(dv);
+  const double ai = sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esi);
+  const double cj = fm::fdiv(c.SCFAC * fm::fexp(0.3 * pf.lrho), sqrt(1.718e-5 + 4.9e-8 * (t - c.TT)));
+  const double ssi_rai = fm::fdiv(R.ssi, rho * ai);
   Slopes s;
   slopes(c, d, pf.lrho, t, v, s);
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
@@ -277,12 +282,12 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // saturation pressure over ice (freezing) or over water (melting)
   double heat_i = 0.0, heat_w = 0.0;
   if (has_s || has_g) {
-    const double ev = v[IRV] * pf.pres / (c.EPSILO + v[IRV]);
+    const double ev = fm::fdiv(v[IRV] * pf.pres, c.EPSILO + v[IRV]);
     const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi) : ev;
     const double ew = c.LEVLIMIT != 0.0 ? dmin(ev, esw) : ev;
     const double kt = ka * (c.TT - t);
     const double dl = dv * (c.LVTT + (c.CPV - c.CL) * (t - c.TT));
-    const double irt = 1.0 / (c.RV * t);
+    const double irt = it * d.irv;
     heat_i = kt + (dl * (c.ESTT - ei) * irt);
     heat_w = kt + (dl * (c.ESTT - ew) * irt);
   }
@@ -304,9 +309,9 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
     b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * fm::fexp(c.EXCACCR * s.llbdar) * pf.rho_mcexvt : 0.0;
     if (has_r && !has_c) {
-      const double usw = 1. - v[IRV] * (pf.pres - esw) / (c.EPSILO * esw);
-      const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / (ka * c.RV * t * t) + (c.RV * t) / (dv * esw);
-      b[B_RREVAV] = (pmax0(usw) / (rho * av)) *
+      const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
+      const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esw);
+      b[B_RREVAV] = fm::fdiv(pmax0(usw), rho * av) *
                     (c.O0EVAR * fm::fexp(c.EX0EVAR * s.llbdar) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
     } else b[B_RREVAV] = 0.0;
   } else {
@@ -315,12 +320,12 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 
   // ---- ICE4_FAST_RS rates (mode_ice4_fast_rs.F90) ----
   // collision-freezing denominator, shared with ICE4_FAST_RG
-  const double den = (has_s || has_g) ? 1.0 / (rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
+  const double den = (has_s || has_g) ? fm::frcp(rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
   const double freez2 = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
   rs[RS_FREEZ1] = has_s ? heat_i * vent_s * den : 0.0;
   rs[RS_FREEZ2] = has_s ? freez2 : 0.0;
-  const double ilr = has_r ? 1.0 / s.lbdar : 0.0, ils = has_s ? 1.0 / s.lbdas : 0.0;
-  const double ilg = has_g ? 1.0 / s.lbdag : 0.0;
+  const double ilr = has_r ? fm::frcp(s.lbdar) : 0.0, ils = has_s ? fm::frcp(s.lbdas) : 0.0;
+  const double ilg = has_g ? fm::frcp(s.lbdag) : 0.0;
   if (has_c && has_s) {
     int i;
     const double fr = lut_index(s.llbdas, c.NGAMINC, c.RIMINTP1, c.RIMINTP2, i);
@@ -332,8 +337,8 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     if ((int)c.SNOW_RIMING == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
       const double r = c.SRIMCG * fm::fexp(c.EXSRIMCG * s.llbdas) * (1.0 - zw2);
-      rs[RS_RSRIMCG] = zzw * r / dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * s.llbdas) * (1. - zw3) -
-                                                  c.SRIMCG3 * r);
+      rs[RS_RSRIMCG] = fm::fdiv(zzw * r, dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * s.llbdas) * (1. - zw3) -
+                                                          c.SRIMCG3 * r));
     } else rs[RS_RSRIMCG] = 0.0;
   } else {
     rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
@@ -355,8 +360,8 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
   }
   if (has_s && warm) {
-    b[B_RSMLTG] = c.FSCVMG * pmax0((-heat_w * vent_s - (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c.CL * (c.TT - t))) /
-                                   (rho * c.LMTT));
+    b[B_RSMLTG] = c.FSCVMG * pmax0(fm::fdiv(-heat_w * vent_s - (rs[RS_RCRIMS] + rs[RS_RRACCS]) * (rho * c.CL * (c.TT - t)),
+                                            rho * c.LMTT));
     b[B_RCMLTSR] = rs[RS_RCRIMS];
   } else {
     b[B_RSMLTG] = b[B_RCMLTSR] = 0.0;
@@ -367,8 +372,8 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     b[B_RICFRRG] = c.ICFRR * v[IRI] * fm::fexp(c.EXICFRR * s.llbdar) * pf.rho_mcexvt;
     b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * s.llbdar) * pf.rho_mcexvt1;
     if (c.LCRFLIMIT != 0.0) {
-      const double zw = pmax0(dmin(1., (b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t) /
-                                           dmax(1.e-20, c.LVTT * b[B_RRCFRIG])));
+      const double zw = pmax0(dmin(1., fm::fdiv((b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t),
+                                                  dmax(1.e-20, c.LVTT * b[B_RRCFRIG]))));
       b[B_RRCFRIG] = zw * b[B_RRCFRIG];
       b[B_RICFRR] = (1. - zw) * b[B_RICFRRG];
       b[B_RICFRRG] = zw * b[B_RICFRRG];
@@ -381,14 +386,14 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   if (has_g && has_i) {
     const double e = fm::fexp(c.COLEXIG * (t - c.TT));
     rg[RG_RIDRYG] = c.FIDRYG * e * v[IRI] * base_g;
-    rg[RG_RIWETG] = rg[RG_RIDRYG] / (c.COLIG * e);
+    rg[RG_RIWETG] = fm::fdiv(rg[RG_RIDRYG], c.COLIG * e);
   } else rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
   if (has_s && has_g) {
     int i1, i2;
     const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
     const double f2 = lut_index(s.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
     const double zw = lut2d(lut + O_SDRYG, ICE3GB_NDRYLBDAS, i1, f1, i2, f2);
-    rg[RG_RSWETG] = c.FSDRYG * zw / c.COLSG * fm::fexp((c.CXS - c.BS) * s.llbdas + c.CXG * s.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RSWETG] = fm::fdiv(c.FSDRYG * zw, c.COLSG) * fm::fexp((c.CXS - c.BS) * s.llbdas + c.CXG * s.llbdag) * pf.rho_mcexvt1 *
                     (c.LBSDRYG1 * ilg * ilg + c.LBSDRYG2 * ilg * ils + c.LBSDRYG3 * ils * ils);
     rg[RG_RSDRYG] = rg[RG_RSWETG] * c.COLSG * fm::fexp(c.COLEXSG * (t - c.TT));
   } else rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
@@ -403,14 +408,14 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   rg[RG_FREEZ1] = has_g ? heat_i * vent_g * den : 0.0;
   rg[RG_FREEZ2] = has_g ? freez2 : 0.0;
   if (has_g && warm) {
-    b[B_RGMLTR] = pmax0((-heat_w * vent_g - (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c.CL * (c.TT - t))) /
-                        (rho * c.LMTT));
+    b[B_RGMLTR] = pmax0(fm::fdiv(-heat_w * vent_g - (rg[RG_RCDRYG] + rg[RG_RRDRYG]) * (rho * c.CL * (c.TT - t)),
+                                 rho * c.LMTT));
   } else b[B_RGMLTR] = 0.0;
 
   // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
   if (pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20)) {
-    const double l = dmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(rho * v[IRI] / cit)));
-    b[B_RCBERI] = ssi_rai * cit * (c.O0DEPI / l + c.O2DEPI * cj * cj * fm::fexp(-(c.DI + 2.0) * fm::flog(l)));
+    const double l = dmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(fm::fdiv(rho * v[IRI], cit))));
+    b[B_RCBERI] = ssi_rai * cit * (fm::fdiv(c.O0DEPI, l) + c.O2DEPI * cj * cj * fm::fexp(-(c.DI + 2.0) * fm::flog(l)));
   } else b[B_RCBERI] = 0.0;
 }
 
@@ -465,7 +470,7 @@ ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact
   if (has_c && has_s && cold) {
     b[B_RCRIMSS] = dmin(freez, rs[RS_RCRIMSS]);
     freez = pmax0(freez - b[B_RCRIMSS]);
-    const double zzw0 = dmin(1., freez / dmax(1.e-20, rs[RS_RCRIMS] - b[B_RCRIMSS]));
+    const double zzw0 = dmin(1., fm::fdiv(freez, dmax(1.e-20, rs[RS_RCRIMS] - b[B_RCRIMSS])));
     b[B_RCRIMSG] = zzw0 * pmax0(rs[RS_RCRIMS] - b[B_RCRIMSS]);
     freez = pmax0(freez - b[B_RCRIMSG]);
     b[B_RSRIMCG] = zzw0 * rs[RS_RSRIMCG] * (signbit(b[B_RCRIMSG]) ? 0.0 : 1.0);
@@ -476,7 +481,7 @@ ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact
   if (has_r && has_s && cold) {
     b[B_RRACCSS] = dmin(freez, rs[RS_RRACCSS]);
     freez = pmax0(freez - b[B_RRACCSS]);
-    const double zzw = dmin(1., freez / dmax(1.e-20, rs[RS_RRACCS] - b[B_RRACCSS]));
+    const double zzw = dmin(1., fm::fdiv(freez, dmax(1.e-20, rs[RS_RRACCS] - b[B_RRACCSS])));
     b[B_RRACCSG] = zzw * pmax0(rs[RS_RRACCS] - b[B_RRACCSS]);
     freez = pmax0(freez - b[B_RRACCSG]);
     b[B_RSACCRG] = zzw * rs[RS_RSACCRG] * (signbit(b[B_RRACCSG]) ? 0.0 : 1.0);
@@ -617,6 +622,9 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
   int passes = 0, outer = 0, inner = 0;
   rrevav = 0.0;
   capped = false;
+  // TT/exn, lsfact and lvfact with IEEE divisions, as the Fortran: the
+  // LFEEDBACKT sub-step ends with th on TT/exn, and which side of TT the next
+  // pass sees is decided by their rounding
   const double zx = c.TT / pf.exn;
   while (ltd(ztime, dt)) {
     ++outer;
@@ -629,9 +637,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       const double zsum2 = vart[IRI] + vart[IRS] + vart[IRG];
       const double zdev = (c.CPD + c.CPV * vart[IRV] + c.CL * (vart[IRC] + vart[IRR]) + c.CI * zsum2) * pf.exn;
       const double zzt = vart[ITH] * pf.exn;
-      const double izdev = 1.0 / zdev;
-      const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) * izdev;
-      const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) * izdev;
+      const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
+      const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
       double A[NV], B[NV];
       tendencies(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
 #pragma unroll
@@ -668,6 +675,119 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
     }
   }
   return ((unsigned)outer << 16) | (unsigned)inner;
+}
+
+// Load of a read-only field (the read-only data path on the device).
+ICE3_HD double ldp(const double *p, long i)
+{
+#if defined(__CUDA_ARCH__)
+  return __ldg(p + i);
+#else
+  return p[i];
+#endif
+}
+
+// One grid point of RAIN_ICE (rain_ice.F90:334-652 and the disabled tail
+// :758-790): L/cph and LLMICRO, nucleation outside micro points, the ICE4
+// sub-stepping, total tendencies and ICE4_CORRECT_NEGATIVITIES on the
+// sources, written back in place.  Returns the pass key (0 for points
+// outside LLMICRO or capped); `capped` reports a point that hit max_passes.
+ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
+                                    const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped)
+{
+  const double inv_dt = 1.0 / dt;
+  const bool lwarm = c.LWARM != 0.0;
+  const bool sigm = (int)c.SUBG_AUCV_RC == 1 && (int)c.SUBG_PR_PDF == 0;
+  const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
+  unsigned int key = 0u;
+  capped = false;
+  PointFix pf;
+  pf.exn = ldp(f.exn, p);
+  pf.rho = ldp(f.rhodref, p);
+  pf.pres = ldp(f.pabs, p);
+  const double th = ldp(f.tht, p), rv = ldp(f.rvt, p), rc = ldp(f.rct, p), rr = ldp(f.rrt, p);
+  const double ri = ldp(f.rit, p), rs = ldp(f.rst, p), rg = ldp(f.rgt, p);
+  const double exnref = ldp(f.exnref, p);
+  double ths = f.ths[p], rvs = f.rvs[p], rcs = f.rcs[p], rrs = f.rrs[p], ris = f.ris[p], rss = f.rss[p],
+         rgs = f.rgs[p];
+  double cit = f.cit[p];
+  // rain_ice.F90:334-345 (L/cph without exner) and :370-381 (LLMICRO)
+  const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
+  const double t = th * pf.exn;
+  const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
+  const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
+  const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
+                     gtp(rg, c.G_RTMIN);
+  const double iexnref = fm::frcp(exnref);
+  const double lsx = lsf * iexnref, lvx = lvf * iexnref;
+  double evap = 0.0, rainfr = 1.0;
+  double zrvheni = 0.0;
+  if (!micro) {
+    cit = 0.0;
+    nucleation(c, d, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
+  }
+  zrvheni = dmin(rvs, zrvheni * inv_dt);
+  if (micro) {
+    pf.lrho = fm::flog(pf.rho);
+    pf.rho_mcexvt = fm::fexp(-c.CEXVT * pf.lrho);
+    const double irho = fm::frcp(pf.rho);
+    pf.rho_mcexvt1 = pf.rho_mcexvt * irho;
+    pf.rcrautc = c.CRIAUTC * irho;
+    pf.cf = ldp(f.cldfr, p);
+    pf.sigma_rc = sigm ? 2.0 * ldp(f.sigs, p) : 0.0;
+    double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
+    double ext[NV] = {ths - th * inv_dt, rvs - rv * inv_dt, rcs - rc * inv_dt, rrs - rr * inv_dt,
+                      ris - ri * inv_dt, rss - rs * inv_dt, rgs - rg * inv_dt};
+    double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
+    if (adju) {
+      hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
+      hl[3] = rc - hl[2];
+      hi[3] = ri - hi[2];
+      hl[1] = pos(rc) ? pf.cf - hl[0] : 0.;
+      hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
+    }
+    double rrevav;
+    key = stepping(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
+    evap = lwarm ? rrevav : 0.0;
+    // total tendencies (rain_ice.F90:758-790)
+    const double wv = (vart[IRV] - rv) * inv_dt, wc = (vart[IRC] - rc) * inv_dt;
+    const double wr = (vart[IRR] - rr) * inv_dt, wi = (vart[IRI] - ri) * inv_dt;
+    const double ws = (vart[IRS] - rs) * inv_dt, wg = (vart[IRG] - rg) * inv_dt;
+    ths += (wc + wr) * lvx + (wi + ws + wg) * lsx + zrvheni * lsx;
+    rvs += wv - zrvheni;
+    rcs += wc;
+    rrs += wr;
+    ris += wi + zrvheni;
+    rss += ws;
+    rgs += wg;
+  } else {
+    ths += zrvheni * lsx;
+    rvs -= zrvheni;
+    ris += zrvheni;
+  }
+  // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the sources
+  double w;
+  w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
+  w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
+  w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
+  w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
+  w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
+  w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
+  ths -= w * (rcs * lvx + ris * lsx);
+  rvs += w * (rcs + ris);
+  rcs = (1. - w) * rcs;
+  ris = (1. - w) * ris;
+  w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
+  w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
+  w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
+  f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
+  f.rgs[p] = rgs;
+  f.cit[p] = cit;
+  f.evap3d[p] = evap;
+  f.rainfr[p] = rainfr;
+  return key;
 }
 
 }  // namespace ice3pt

@@ -4,10 +4,13 @@
 // mode_ice4_sedimentation_stat.F90:143-229) and the reference JAX
 // sedimentation_stat (src/ice3/jax/stencils/sedimentation.py:58-352), the two
 // differing in the cloud mean-radius factor and the flux-divergence scaling
-// (selected by `fortran`).  The five species are independent in the sweep, so
-// a thread owns one (column, species) pair and walks k from the top level to
-// the surface keeping the incoming flux F_{k+1} in a register; consecutive
-// threads own consecutive columns, so every level access is coalesced.
+// (selected by `fortran`).  A thread owns one column and walks k from the top
+// level to the surface with the five species side by side, keeping each
+// species' incoming flux F_{k+1} in a register; consecutive threads own
+// consecutive columns, so every level access is coalesced.  What the species
+// share at a level (rho, dz, rho dz, dt/(rho dz) and log rho, computed only
+// when a species sediments there) is computed once; threshold tests and
+// clamps run on the integer pipe (GB300's FP64 pipe is the bound).
 #include "ice3gb_device.cuh"
 #include "ice3gb_kernels.h"
 
@@ -46,7 +49,7 @@ ICE3_HD CloudPar cloud_params(const Cst &c, bool fortran, bool has_st, double se
   return p;
 }
 
-// Fall speed for content r (> threshold checked by the caller); lrho = fm::flog(rho).
+// Fall speed for content r (> threshold checked by the caller); lrho = log(rho).
 ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlbda, const CloudPar &cp)
 {
   const double lr = fm::flog(r);
@@ -59,7 +62,7 @@ ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlb
     case 1:  // rain
       return c.FSEDR * fm::fexp((c.EXSEDR - 1.0) * lr + (c.EXSEDR - c.CEXVT - 1.0) * lrho);
     case 2: {  // pristine ice: sedimentation.py:46-55, F90:307-311
-      const double dmax_ = fmax(0.05e6, -0.15319e6 - 0.021454e6 * (lrho + lr));
+      const double dmax_ = dmax(0.05e6, -0.15319e6 - 0.021454e6 * (lrho + lr));
       return c.FSEDI * fm::fexp(-c.CEXVT * lrho + c.EXCSEDI * fm::flog(dmax_));
     }
     case 3:  // snow
@@ -69,53 +72,62 @@ ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlb
   }
 }
 
-__global__ void __launch_bounds__(256) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
+__global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
 {
-  const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (q >= 5L * a.nij) return;
-  const int s = (int)(q / a.nij);
-  const long col = q - (long)s * a.nij;
-  if (s == 0 && a.fortran && c.LSEDIC == 0.0) {
+  const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (col >= a.nij) return;
+  // PHYEX skips the cloud species when LSEDIC is off
+  const bool skip_c = a.fortran && c.LSEDIC == 0.0;
+  if (skip_c) {
     if (a.fpr[0])
       for (int k = 0; k < a.nk; ++k) a.fpr[0][(long)k * a.nij + col] = 0.0;
     a.inpr[0][col] = 0.0;
-    return;
   }
-  double *src = a.src[s];
-  double *fpr = a.fpr[s];
-  const double rtmin = (s == 0) ? c.C_RTMIN : (s == 1) ? c.R_RTMIN
-                     : (s == 2) ? fmax(c.I_RTMIN, 1.0e-7) : (s == 3) ? c.S_RTMIN : c.G_RTMIN;
+  const double rtmin[5] = {c.C_RTMIN, c.R_RTMIN, dmax(c.I_RTMIN, 1.0e-7), c.S_RTMIN, c.G_RTMIN};
   CloudPar cp;
-  if (s == 0) {
+  {
     const bool has_st = a.sea != nullptr && a.town != nullptr;
     const double sea = a.sea ? a.sea[col] : 0.0, town = a.town ? a.town[col] : 0.0;
     cp = cloud_params(c, a.fortran, has_st, sea, town);
   }
   const double dt = a.dt, inv_dt = 1.0 / a.dt;
-  double fabove = 0.0;
+  double fabove[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int k = a.nk - 1; k >= 0; --k) {
     const long p = (long)k * a.nij + col;
     const double rho = ld1(a.rhodref, p), dz = ld1(a.dzz, p);
-    const double rt = src[p] * dt;
-    const double tsorhodz = dt / (rho * dz);
-    const double qp = fabove * tsorhodz;
-    double wlbda = 0.0;
-    if (s == 0) wlbda = 6.6e-8 * (101325.0 / ld1(a.pabs, p)) * (ld1(a.tht, p) / 293.15);
-    const bool c1 = rt > rtmin, c2 = qp > rtmin;
-    double w1 = 0.0, w2 = 0.0;
-    if (c1 || c2) {
-      const double lrho = fm::flog(rho);
-      if (c1) w1 = fall_speed(c, s, rt, lrho, wlbda, cp);
-      if (c2) w2 = fall_speed(c, s, qp, lrho, wlbda, cp);
+    const double rhodz = rho * dz;
+    const double tsorhodz = fm::fdiv(dt, rhodz);
+    double src[5], rt[5], qp[5];
+    bool c1[5], c2[5];
+    bool any = false;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      if (s == 0 && skip_c) { c1[s] = c2[s] = false; src[s] = rt[s] = qp[s] = 0.0; continue; }
+      src[s] = a.src[s][p];
+      rt[s] = src[s] * dt;
+      qp[s] = fabove[s] * tsorhodz;
+      c1[s] = gtp(rt[s], rtmin[s]);
+      c2[s] = gtp(qp[s], rtmin[s]);
+      any = any || c1[s] || c2[s];
     }
-    double flux = fmin(rho * dz * rt * inv_dt, w1 * rho * rt);
-    if (w2 != 0.0) flux += fmax(0.0, 1.0 - dz / (dt * w2)) * fabove;
-    if (a.fortran) src[p] = src[p] + tsorhodz * (fabove - flux) * inv_dt;
-    else src[p] = src[p] + (fabove - flux) / (rho * dz * dt);
-    if (fpr) fpr[p] = flux;
-    fabove = flux;
+    const double lrho = any ? fm::flog(rho) : 0.0;
+    const double wlbda = (c1[0] || c2[0]) ? 6.6e-8 * fm::fdiv(101325.0, ld1(a.pabs, p)) * (ld1(a.tht, p) * (1.0 / 293.15)) : 0.0;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      if (s == 0 && skip_c) continue;
+      const double w1 = c1[s] ? fall_speed(c, s, rt[s], lrho, wlbda, cp) : 0.0;
+      const double w2 = c2[s] ? fall_speed(c, s, qp[s], lrho, wlbda, cp) : 0.0;
+      double flux = dmin(rhodz * rt[s] * inv_dt, w1 * rho * rt[s]);
+      if (!zerod_(w2)) flux += pmax0(1.0 - fm::fdiv(dz, dt * w2)) * fabove[s];
+      if (a.fortran) a.src[s][p] = src[s] + tsorhodz * (fabove[s] - flux) * inv_dt;
+      else a.src[s][p] = src[s] + fm::fdiv(fabove[s] - flux, rhodz * dt);
+      if (a.fpr[s]) a.fpr[s][p] = flux;
+      fabove[s] = flux;
+    }
   }
-  a.inpr[s][col] = fabove / c.RHOLW;
+#pragma unroll
+  for (int s = 0; s < 5; ++s)
+    if (!(s == 0 && skip_c)) a.inpr[s][col] = fabove[s] / c.RHOLW;
 }
 
 // Fog deposition on the lowest level (rain_ice.F90:876-895).
@@ -138,7 +150,7 @@ __global__ void fog_deposition_kernel(const __grid_constant__ Cst c, FogArgs a)
 
 cudaError_t launch_sedimentation(const Cst &c, const SedArgs &a, cudaStream_t s)
 {
-  const long n = 5L * a.nij;
+  const long n = a.nij;
   const int threads = 128;
   sedimentation_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(c, a);
   return cudaGetLastError();

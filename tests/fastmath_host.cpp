@@ -1,9 +1,10 @@
-// Host build of the kernels' table-driven exp/exp10/log (same source as the
+// Host build of the kernels' table-driven exp/exp10/log/rcp/atan (same source as the
 // device build), exported for tests/test_fastmath.py.
 #include "../dwarf-p-ice3_gb300/csrc/fastmath.cuh"
 
 extern "C" void fm_eval(int fn, const double *x, double *y, long n)
 {
   for (long i = 0; i < n; ++i)
-    y[i] = fn == 0 ? fm::fexp(x[i]) : fn == 1 ? fm::fexp10(x[i]) : fm::flog(x[i]);
+    y[i] = fn == 0 ? fm::fexp(x[i]) : fn == 1 ? fm::fexp10(x[i]) : fn == 2 ? fm::flog(x[i])
+         : fn == 3 ? fm::frcp(x[i]) : fm::fatan(x[i]);
 }

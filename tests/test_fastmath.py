@@ -86,3 +86,23 @@ def test_exp_log_round_trip(fm):
     x = 10.0 ** rng.uniform(-30, 30, 100000)
     y = fm(0, fm(2, x))
     assert np.max(np.abs(y / x - 1.0)) < 2e-14      # |log x| <= 70: ~70 ulp amplification at most
+
+
+def test_frcp_within_2ulp(fm):
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([10.0 ** rng.uniform(-37, 37, 4000), -(10.0 ** rng.uniform(-30, 30, 2000)),
+                         rng.uniform(1.0, 2.0, 2000), [1.0, 2.0, 3.0, 0.1, 1e-20, 1e20]])
+    assert ulp_err(fm(3, xs), lambda v: 1 / v, xs) <= 1.0
+    edge = fm(3, np.array([0.0, -0.0, np.inf, 1e-300, 1e300, np.nan]))
+    assert edge[0] == np.inf and edge[1] == -np.inf and edge[2] == 0.0 and np.isnan(edge[5])
+    assert edge[3] == 1.0 / 1e-300 and edge[4] == 1.0 / 1e300
+
+
+def test_fatan_within_2ulp(fm):
+    rng = np.random.default_rng(6)
+    xs = np.concatenate([rng.uniform(-1, 1, 3000), rng.uniform(-20, 20, 3000), 10.0 ** rng.uniform(-12, 17, 2000),
+                         -(10.0 ** rng.uniform(-12, 17, 1000)), [0.0, 1.0, -1.0, 1e-40, 0.5, 2.0, 1.55 * 2.0]])
+    assert ulp_err(fm(4, xs), mp.atan, xs) <= 2.0
+    edge = fm(4, np.array([np.inf, -np.inf, np.nan, -0.0, 1e300]))
+    assert edge[0] == np.pi / 2 and edge[1] == -np.pi / 2 and np.isnan(edge[2]) and edge[3] == 0.0
+    assert edge[4] == np.pi / 2

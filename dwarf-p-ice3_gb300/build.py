@@ -4,6 +4,8 @@
 
 Each .cu is compiled in parallel (one -gencode, -lineinfo), then linked into
 dwarf-p-ice3_gb300/lib/libice3gb.so with the CUDA runtime linked statically.
+Extra nvcc flags (e.g. -D switches of the kernels) can be given in the
+ICE3GB_NVCC_FLAGS environment variable; use --force after changing them.
 """
 from __future__ import annotations
 
@@ -52,7 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        extra = os.environ.get("ICE3GB_NVCC_FLAGS", "").split()
+        cmd = [cc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

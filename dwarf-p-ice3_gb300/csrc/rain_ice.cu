@@ -30,6 +30,12 @@
 #include "ice3gb_kernels.h"
 #include "rain_ice_point.cuh"
 
+// Resident blocks of rain_ice_points_kernel per SM (2 x 256 threads: 128
+// registers per thread, two copies of the 78.7 KB lookup tables per SM).
+#ifndef RI_BLOCKS_PER_SM
+#define RI_BLOCKS_PER_SM 2
+#endif
+
 namespace {
 using namespace ice3pt;
 
@@ -39,7 +45,7 @@ __device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int
   if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(key_max, m);
 }
 
-__global__ void __launch_bounds__(RI_THREADS, 2) rain_ice_points_kernel(const __grid_constant__ Cst c,
+__global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_kernel(const __grid_constant__ Cst c,
                                                                          const __grid_constant__ RainIceArgs a)
 {
   extern __shared__ double lut[];
@@ -155,7 +161,7 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
   if (e != cudaSuccess) return e;
   const long n = (long)a.nij * a.nk;
   long chunks = (n + RI_THREADS - 1) / RI_THREADS;
-  long blocks = (long)num_sms * 2;
+  long blocks = (long)num_sms * RI_BLOCKS_PER_SM;
   if (blocks > chunks) blocks = chunks;
   if (blocks < 1) blocks = 1;
   rain_ice_points_kernel<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);

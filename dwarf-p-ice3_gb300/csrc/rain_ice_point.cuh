@@ -47,6 +47,10 @@ struct Derived {
   double lLBR, lLBS, lLBG, lLBDAS_MAX, lTT;   // logs of table constants
   double nu20_eb2;                            // NU20 * exp(-BETA2)
   double irv;                                 // 1/RV
+  // exponent identities of the table, tested once so that a power already
+  // computed is reused (AROME: EX0DEPS = 0, EXCRIMSG = EXCRIMSS,
+  // EXSRIMCG2 = 2 EXSRIMCG, CXS = 1, EXICFRR = EXCACCR, EX0EVAR = -2)
+  int ex0deps_zero, ex0depg_zero, crims_same, srimcg2_twice, cxs_one, icfrr_caccr, ex0evar_m2;
 };
 
 ICE3_HD void make_derived(const Cst &c, Derived &d)
@@ -58,6 +62,13 @@ ICE3_HD void make_derived(const Cst &c, Derived &d)
   d.lTT = fm::flog(c.TT);
   d.nu20_eb2 = c.NU20 * fm::fexp(-c.BETA2);
   d.irv = 1.0 / c.RV;
+  d.ex0deps_zero = c.EX0DEPS == 0.0;
+  d.ex0depg_zero = c.EX0DEPG == 0.0;
+  d.crims_same = c.EXCRIMSG == c.EXCRIMSS;
+  d.srimcg2_twice = c.EXSRIMCG2 == 2.0 * c.EXSRIMCG;
+  d.cxs_one = c.CXS == 1.0;
+  d.icfrr_caccr = c.EXICFRR == c.EXCACCR;
+  d.ex0evar_m2 = c.EX0EVAR == -2.0;
 }
 
 // Rates that persist between the hard pass and the following soft passes
@@ -273,10 +284,19 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
   const bool warm = gtp(t, c.TT);
   // ventilation factors shared by deposition, freezing and melting
-  const double vent_s = has_s ? c.O0DEPS * fm::fexp(c.EX0DEPS * s.llbdas) + c.O1DEPS * cj * fm::fexp(c.EX1DEPS * s.llbdas)
+  const double vent_s = has_s ? c.O0DEPS * (d.ex0deps_zero ? 1.0 : fm::fexp(c.EX0DEPS * s.llbdas)) +
+                                    c.O1DEPS * cj * fm::fexp(c.EX1DEPS * s.llbdas)
                               : 0.0;
-  const double vent_g = has_g ? c.O0DEPG * fm::fexp(c.EX0DEPG * s.llbdag) + c.O1DEPG * cj * fm::fexp(c.EX1DEPG * s.llbdag)
+  const double vent_g = has_g ? c.O0DEPG * (d.ex0depg_zero ? 1.0 : fm::fexp(c.EX0DEPG * s.llbdag)) +
+                                    c.O1DEPG * cj * fm::fexp(c.EX1DEPG * s.llbdag)
                               : 0.0;
+  const double ilr = has_r ? fm::frcp(s.lbdar) : 0.0, ils = has_s ? fm::frcp(s.lbdas) : 0.0;
+  const double ilg = has_g ? fm::frcp(s.lbdag) : 0.0;
+  // lbdar^EXCACCR, shared by RCACCR and (EXICFRR = EXCACCR) RICFRRG
+  const double e_caccr = (has_r && (has_c || (has_i && d.icfrr_caccr))) ? fm::fexp(c.EXCACCR * s.llbdar) : 0.0;
+  // lbdas^(CXS-BS) (RSACCRG, RSWETG) and lbdag^CXG (RSWETG, RRDRYG)
+  const double e_cxsbs = (has_s && (has_r || has_g)) ? fm::fexp((c.CXS - c.BS) * s.llbdas) : 0.0;
+  const double e_cxg = (has_g && (has_s || has_r)) ? fm::fexp(c.CXG * s.llbdag) : 0.0;
   // vapour/heat term of the freezing and melting rates (mode_ice4_fast_rs.F90
   // IFREEZ1/RSMLTG, mode_ice4_fast_rg.F90 IFREEZ1/RGMLTR), e limited by the
   // saturation pressure over ice (freezing) or over water (melting)
@@ -307,12 +327,13 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // ---- ICE4_WARM (mode_ice4_warm.F90), SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE ----
   if (c.LWARM != 0.0) {
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
-    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * fm::fexp(c.EXCACCR * s.llbdar) * pf.rho_mcexvt : 0.0;
+    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt : 0.0;
     if (has_r && !has_c) {
       const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
       const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esw);
       b[B_RREVAV] = fm::fdiv(pmax0(usw), rho * av) *
-                    (c.O0EVAR * fm::fexp(c.EX0EVAR * s.llbdar) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
+                    (c.O0EVAR * (d.ex0evar_m2 ? ilr * ilr : fm::fexp(c.EX0EVAR * s.llbdar)) +
+                     c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
     } else b[B_RREVAV] = 0.0;
   } else {
     b[B_RCAUTR] = b[B_RCACCR] = b[B_RREVAV] = 0.0;
@@ -324,21 +345,21 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   const double freez2 = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
   rs[RS_FREEZ1] = has_s ? heat_i * vent_s * den : 0.0;
   rs[RS_FREEZ2] = has_s ? freez2 : 0.0;
-  const double ilr = has_r ? fm::frcp(s.lbdar) : 0.0, ils = has_s ? fm::frcp(s.lbdas) : 0.0;
-  const double ilg = has_g ? fm::frcp(s.lbdag) : 0.0;
   if (has_c && has_s) {
     int i;
     const double fr = lut_index(s.llbdas, c.NGAMINC, c.RIMINTP1, c.RIMINTP2, i);
     const double zw1 = lut1d(lut + O_RIM1, i, fr);
     const double zw2 = lut1d(lut + O_RIM2, i, fr);
     const double zw3 = lut1d(lut + O_RIM4, i, fr);
-    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * fm::fexp(c.EXCRIMSS * s.llbdas) * pf.rho_mcexvt;
-    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * fm::fexp(c.EXCRIMSG * s.llbdas) * pf.rho_mcexvt;
+    const double e_crimss = fm::fexp(c.EXCRIMSS * s.llbdas);
+    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * e_crimss * pf.rho_mcexvt;
+    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * (d.crims_same ? e_crimss : fm::fexp(c.EXCRIMSG * s.llbdas)) * pf.rho_mcexvt;
     if ((int)c.SNOW_RIMING == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
-      const double r = c.SRIMCG * fm::fexp(c.EXSRIMCG * s.llbdas) * (1.0 - zw2);
-      rs[RS_RSRIMCG] = fm::fdiv(zzw * r, dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * fm::fexp(c.EXSRIMCG2 * s.llbdas) * (1. - zw3) -
-                                                          c.SRIMCG3 * r));
+      const double e_srimcg = fm::fexp(c.EXSRIMCG * s.llbdas);
+      const double e_srimcg2 = d.srimcg2_twice ? e_srimcg * e_srimcg : fm::fexp(c.EXSRIMCG2 * s.llbdas);
+      const double r = c.SRIMCG * e_srimcg * (1.0 - zw2);
+      rs[RS_RSRIMCG] = fm::fdiv(zzw * r, dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * e_srimcg2 * (1. - zw3) - c.SRIMCG3 * r));
     } else rs[RS_RSRIMCG] = 0.0;
   } else {
     rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
@@ -350,11 +371,11 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double zw1 = lut2d(lut + O_RACCSS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
     const double zw2 = lut2d(lut + O_RACCS, ICE3GB_NACCLBDAR, i1, f1, i2, f2);
     const double zw3 = lut2d(lut + O_SACCRG, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
-    const double zzw = c.FRACCSS * fm::fexp(c.CXS * s.llbdas) * pf.rho_mcexvt1 *
+    const double zzw = c.FRACCSS * (d.cxs_one ? s.lbdas : fm::fexp(c.CXS * s.llbdas)) * pf.rho_mcexvt1 *
                        (c.LBRACCS1 * ils * ils + c.LBRACCS2 * ils * ilr + c.LBRACCS3 * ilr * ilr) * sq(sq(ilr));
     rs[RS_RRACCSS] = zw1 * zzw;
     rs[RS_RRACCS] = zw2 * zzw;
-    rs[RS_RSACCRG] = c.FSACCRG * zw3 * fm::fexp((c.CXS - c.BS) * s.llbdas) * pf.rho_mcexvt1 *
+    rs[RS_RSACCRG] = c.FSACCRG * zw3 * e_cxsbs * pf.rho_mcexvt1 *
                      (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr;
   } else {
     rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
@@ -369,7 +390,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 
   // ---- ICE4_FAST_RG rates (mode_ice4_fast_rg.F90, KRR = 6) ----
   if (has_i && has_r) {
-    b[B_RICFRRG] = c.ICFRR * v[IRI] * fm::fexp(c.EXICFRR * s.llbdar) * pf.rho_mcexvt;
+    b[B_RICFRRG] = c.ICFRR * v[IRI] * (d.icfrr_caccr ? e_caccr : fm::fexp(c.EXICFRR * s.llbdar)) * pf.rho_mcexvt;
     b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * s.llbdar) * pf.rho_mcexvt1;
     if (c.LCRFLIMIT != 0.0) {
       const double zw = pmax0(dmin(1., fm::fdiv((b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t),
@@ -393,7 +414,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
     const double f2 = lut_index(s.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
     const double zw = lut2d(lut + O_SDRYG, ICE3GB_NDRYLBDAS, i1, f1, i2, f2);
-    rg[RG_RSWETG] = fm::fdiv(c.FSDRYG * zw, c.COLSG) * fm::fexp((c.CXS - c.BS) * s.llbdas + c.CXG * s.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RSWETG] = fm::fdiv(c.FSDRYG * zw, c.COLSG) * (e_cxsbs * e_cxg) * pf.rho_mcexvt1 *
                     (c.LBSDRYG1 * ilg * ilg + c.LBSDRYG2 * ilg * ils + c.LBSDRYG3 * ils * ils);
     rg[RG_RSDRYG] = rg[RG_RSWETG] * c.COLSG * fm::fexp(c.COLEXSG * (t - c.TT));
   } else rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
@@ -402,7 +423,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
     const double f2 = lut_index(s.llbdar, c.NDRYLBDAR, c.DRYINTP1R, c.DRYINTP2R, i2);
     const double zw = lut2d(lut + O_RDRYG, ICE3GB_NDRYLBDAR, i1, f1, i2, f2);
-    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * fm::fexp(c.CXG * s.llbdag) * pf.rho_mcexvt1 *
+    rg[RG_RRDRYG] = c.FRDRYG * zw * sq(sq(ilr)) * e_cxg * pf.rho_mcexvt1 *
                     (c.LBRDRYG1 * ilg * ilg + c.LBRDRYG2 * ilg * ilr + c.LBRDRYG3 * ilr * ilr);
   } else rg[RG_RRDRYG] = 0.0;
   rg[RG_FREEZ1] = has_g ? heat_i * vent_g * den : 0.0;

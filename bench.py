@@ -289,17 +289,22 @@ def run_ours(args):
     dom_name, dom_st = dom
     bytes_launch = ALGO_BYTES[dom_name] * n
     achieved = bytes_launch / (dom_st["avg_ms"] / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "traffic_per_point.json")
+    traffic, fp64_pct = None, None
+    tpath = os.path.join(REPO, "profiles", "traffic_per_point.txt")
     if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(dom_name)
-            traffic = None if traffic is None else float(traffic) * n
-        except Exception:
-            traffic = None
+        # "<kernel> <DRAM bytes per point>" and "fp64_pipe_pct <kernel> <pct>" lines
+        # summarised from an ncu capture of the same kernels
+        for line in open(tpath):
+            f = line.split()
+            if len(f) == 2 and f[0] == dom_name:
+                traffic = float(f[1]) * n
+            elif len(f) == 3 and f[0] == "fp64_pipe_pct" and f[1] == dom_name:
+                fp64_pct = float(f[2])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": dom_name, "peak_source": f"hbm_gbs of {peak_kind}",
                 "algorithmic_bytes_per_launch": bytes_launch,
+                # the bound that binds: GB300 FP64 issue rate (ncu pipe utilisation of this kernel)
+                "fp64_pipe_pct_ncu": fp64_pct,
                 "kernels": kstats}
 
     # e2e through the host-buffer entry point

@@ -20,6 +20,23 @@ namespace {
 constexpr uint32_t kMagic = 0x1CE3B300u;
 constexpr long kMaxPoints = 1L << 40;
 
+// Resources of the slab pipeline of ice3gb_physics_step_host (created on
+// first use, grow-only): copy-in, compute and copy-out streams, NB rotating
+// sets of slab buffers, and the full-size evap3d / pass-key arrays whose
+// fix-up needs the maximum pass key over all slabs.
+struct HostPipe {
+  static constexpr int NB = 3;
+  bool ready = false;
+  cudaStream_t s_in = nullptr, s_cmp = nullptr, s_out = nullptr;
+  cudaEvent_t in_done[NB] = {}, cmp_done[NB] = {}, out_done[NB] = {};
+  cudaEvent_t start = nullptr, fix_done = nullptr;
+  char *buf[NB] = {};
+  size_t buf_cap = 0;              // bytes per slab set
+  double *evap_all = nullptr;      // [n] evap3d, slab after slab
+  unsigned int *keys_all = nullptr;  // 4 control words + [n] pass keys
+  size_t all_cap = 0;              // points
+};
+
 struct Handle {
   uint32_t magic;
   Ice3gbConstants c;
@@ -31,6 +48,7 @@ struct Handle {
   // staging buffers of the _host entry points (grow-only)
   double *d_stage;
   size_t stage_cap;
+  HostPipe pipe;
   std::mutex mu;
   char err[512];
   // per-kernel timing (ice3gb_profile_*)
@@ -182,12 +200,19 @@ SedArgs sed_args(const Ice3gbSedimentationFields &f, int nij, int nk, double dt,
   return a;
 }
 
-// Launch sequence of one rain_ice call.  `scr` holds 4 control words followed
-// by one pass key per grid point; the first 4 words are cleared here.
-// `order` (n words, or NULL for index order) receives the regime-sorted
-// processing order of the points.
+// Scratch of one rain_ice launch sequence (device words).
+struct RiScratch {
+  unsigned int *chunk;     // work counter, cleared here
+  unsigned int *key_max;   // max pass key; cleared here unless shared across calls
+  unsigned int *keys;      // [n] pass key per point
+  unsigned int *order;     // [n] processing order, or NULL (index order)
+  bool clear_key_max;      // false: the caller cleared it once for several calls
+  bool evap_fixup;         // false: the caller runs the fix-up after the last call
+};
+
+// Launch sequence of one rain_ice call.
 int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                      const Ice3gbRainIceFields *f, unsigned int *scr, unsigned int *order, cudaStream_t s)
+                      const Ice3gbRainIceFields *f, const RiScratch &rs, cudaStream_t s)
 {
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (h->c.LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (h->c.LDEPOSC != 0.0);
@@ -208,18 +233,19 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
     ProfScope ps(h, K_SEDIM, s);
     if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
   }
-  if ((e = cudaMemsetAsync(scr, 0, 4 * sizeof(unsigned int), s)) != cudaSuccess)
+  if ((e = cudaMemsetAsync(rs.chunk, 0, sizeof(unsigned int), s)) != cudaSuccess ||
+      (rs.clear_key_max && (e = cudaMemsetAsync(rs.key_max, 0, sizeof(unsigned int), s)) != cudaSuccess))
     return cuda_fail(h, e, "cudaMemsetAsync");
   RainIceArgs a;
   a.f = *f;
   a.luts = h->d_luts;
   a.scr.status = h->d_status;
-  a.scr.chunk_counter = scr + 0;
-  a.scr.key_max = scr + 1;
-  a.scr.keys = scr + 4;
-  a.order = order;
+  a.scr.chunk_counter = rs.chunk;
+  a.scr.key_max = rs.key_max;
+  a.scr.keys = rs.keys;
+  a.order = rs.order;
   a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
-  if (order) {
+  if (rs.order) {
     ProfScope ps(h, K_ORDER, s);
     if ((e = launch_rain_ice_order(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice order launch");
   }
@@ -227,7 +253,7 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
     ProfScope ps(h, K_RAIN_ICE, s);
     e = launch_rain_ice_points(c, a, h->num_sms, s);
   }
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && rs.evap_fixup) {
     ProfScope ps(h, K_EVAP_FIXUP, s);
     e = launch_rain_ice_evap_fixup(a, s);
   }
@@ -257,7 +283,8 @@ int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptio
   const size_t bytes = sizeof(unsigned int) * (4 + (size_t)n * (ordered ? 2 : 1));
   cudaError_t e = cudaMallocAsync(&scr, bytes, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
-  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, scr, ordered ? scr + 4 + n : nullptr, s);
+  const RiScratch rs = {scr, scr + 1, scr + 4, ordered ? scr + 4 + n : nullptr, true, true};
+  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, rs, s);
   cudaFreeAsync(scr, s);
   return rc;
 }
@@ -282,7 +309,7 @@ int validate_step(Handle *h, const Ice3gbStepFields *f)
 }
 
 int run_physics_step(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                     const Ice3gbStepFields *f, cudaStream_t s)
+                     const Ice3gbStepFields *f, cudaStream_t s, const RiScratch *ri_scr = nullptr)
 {
   const long n = (long)nij * nk;
   double *scr = nullptr;
@@ -317,7 +344,7 @@ int run_physics_step(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceO
     r.ths = f->ths; r.rvs = f->rvs; r.rcs = f->rcs; r.rrs = f->rrs; r.ris = f->ris; r.rss = f->rss;
     r.rgs = f->rgs; r.evap3d = f->evap3d; r.rainfr = f->rainfr; r.inprc = f->inprc; r.inprr = f->inprr;
     r.inpri = f->inpri; r.inprs = f->inprs; r.inprg = f->inprg;
-    rc = run_rain_ice(h, nij, nk, dt, opt, &r, s);
+    rc = ri_scr ? run_rain_ice_core(h, nij, nk, dt, opt, &r, *ri_scr, s) : run_rain_ice(h, nij, nk, dt, opt, &r, s);
   }
   // 3. final adjustment on the post-microphysics state dt*S2 with S2 -> S3
   if (rc == ICE3GB_OK) {
@@ -349,6 +376,204 @@ int ensure_stage(Handle *h, size_t bytes)
   return ICE3GB_OK;
 }
 
+
+// ---- slab pipeline of the chained step on host buffers -----------------------
+// Columns are independent, so ice3gb_physics_step_host runs the step on
+// column slabs: pitched copies of slab i+1 in (host [nk][nij] -> compact
+// device [nk][w]) and of slab i-1 out overlap the kernels of slab i, on three
+// streams ordered by events.  evap3d keeps PRREVAV only at points active in
+// the last pass of the whole call, so the slabs share one maximum-pass-key
+// word and write evap3d and the pass keys to full-size arrays; one fix-up
+// after the last slab and a final copy-out of evap3d give the same result as
+// ice3gb_physics_step on the whole grid.
+int pipe_init(Handle *h)
+{
+  HostPipe &P = h->pipe;
+  if (P.ready) return ICE3GB_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.s_cmp, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking);
+  for (int b = 0; b < HostPipe::NB && e == cudaSuccess; ++b) {
+    e = cudaEventCreateWithFlags(&P.in_done[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.cmp_done[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.out_done[b], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.fix_done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(h, e, "slab pipeline streams/events");
+  P.ready = true;
+  return ICE3GB_OK;
+}
+
+void pipe_free(Handle *h)
+{
+  HostPipe &P = h->pipe;
+  if (!P.ready) return;
+  cudaStreamSynchronize(P.s_in);
+  cudaStreamSynchronize(P.s_cmp);
+  cudaStreamSynchronize(P.s_out);
+  for (int b = 0; b < HostPipe::NB; ++b) {
+    cudaEventDestroy(P.in_done[b]);
+    cudaEventDestroy(P.cmp_done[b]);
+    cudaEventDestroy(P.out_done[b]);
+    if (P.buf[b]) cudaFree(P.buf[b]);
+  }
+  cudaEventDestroy(P.start);
+  cudaEventDestroy(P.fix_done);
+  cudaStreamDestroy(P.s_in);
+  cudaStreamDestroy(P.s_cmp);
+  cudaStreamDestroy(P.s_out);
+  if (P.evap_all) cudaFree(P.evap_all);
+  if (P.keys_all) cudaFree(P.keys_all);
+  P = HostPipe();
+}
+
+int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                               const Ice3gbStepFields *f, cudaStream_t s)
+{
+  int rc;
+  if ((rc = pipe_init(h))) return rc;
+  HostPipe &P = h->pipe;
+  // slab width: about 8 slabs, at least 4096 columns, a multiple of 64
+  long w_max = ((long)nij / 8 + 63) / 64 * 64;
+  if (w_max < 4096) w_max = 4096;
+  if (w_max > nij) w_max = nij;
+  const long n_all = (long)nij * nk;
+  const size_t b3 = (size_t)w_max * nk * sizeof(double), b2 = (size_t)w_max * sizeof(double);
+  const size_t b3p = (b3 + 255) & ~(size_t)255, b2p = (b2 + 255) & ~(size_t)255;
+  const size_t bo = ((size_t)w_max * nk * sizeof(unsigned int) + 255) & ~(size_t)255;
+  // per set: 16 inputs + 8 in-out + 10 outputs (evap3d goes to evap_all) 3-D; sigqsat, sea, town + 5 2-D;
+  // the processing order of rain_ice
+  const size_t set_bytes = 34 * b3p + 8 * b2p + bo;
+  cudaError_t e = cudaSuccess;
+  if (P.buf_cap < set_bytes) {
+    for (int b = 0; b < HostPipe::NB; ++b) {
+      if (P.buf[b]) cudaFree(P.buf[b]);
+      P.buf[b] = nullptr;
+    }
+    P.buf_cap = 0;
+    for (int b = 0; b < HostPipe::NB && e == cudaSuccess; ++b) e = cudaMalloc(&P.buf[b], set_bytes);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(slab buffers)");
+    P.buf_cap = set_bytes;
+  }
+  if (P.all_cap < (size_t)n_all) {
+    if (P.evap_all) cudaFree(P.evap_all);
+    if (P.keys_all) cudaFree(P.keys_all);
+    P.evap_all = nullptr;
+    P.keys_all = nullptr;
+    P.all_cap = 0;
+    e = cudaMalloc(&P.evap_all, sizeof(double) * (size_t)n_all);
+    if (e == cudaSuccess) e = cudaMalloc(&P.keys_all, sizeof(unsigned int) * (4 + (size_t)n_all));
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(evap3d/keys)");
+    P.all_cap = (size_t)n_all;
+  }
+  // order after the caller's earlier work on its stream; clear the shared key_max
+  if ((e = cudaEventRecord(P.start, s)) != cudaSuccess || (e = cudaStreamWaitEvent(P.s_in, P.start, 0)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(P.s_cmp, P.start, 0)) != cudaSuccess ||
+      (e = cudaMemsetAsync(P.keys_all, 0, 4 * sizeof(unsigned int), P.s_cmp)) != cudaSuccess)
+    return cuda_fail(h, e, "slab pipeline start");
+  const size_t hp = (size_t)nij * sizeof(double);   // host row pitch of 3-D fields
+  const long nslab = ((long)nij + w_max - 1) / w_max;
+  long pt_off = 0;                                   // offset of the slab in evap_all / keys
+  for (long i = 0; i < nslab && rc == ICE3GB_OK; ++i) {
+    const int b = (int)(i % HostPipe::NB);
+    const long col0 = i * w_max;
+    const long w = ((long)nij - col0) < w_max ? ((long)nij - col0) : w_max;
+    const size_t wb = (size_t)w * sizeof(double);
+    char *base = P.buf[b];
+    size_t off = 0;
+    auto take = [&](size_t bp) { double *p = reinterpret_cast<double *>(base + off); off += bp; return p; };
+    // ---- copy in
+    if (i >= HostPipe::NB && (e = cudaStreamWaitEvent(P.s_in, P.out_done[b], 0)) != cudaSuccess) break;
+    auto up3 = [&](const double *src) -> double * {
+      double *p = take(b3p);
+      if (src && e == cudaSuccess)
+        e = cudaMemcpy2DAsync(p, wb, src + col0, hp, wb, (size_t)nk, cudaMemcpyHostToDevice, P.s_in);
+      return src ? p : nullptr;
+    };
+    auto up2 = [&](const double *src) -> double * {
+      double *p = take(b2p);
+      if (src && e == cudaSuccess) e = cudaMemcpyAsync(p, src + col0, wb, cudaMemcpyHostToDevice, P.s_in);
+      return src ? p : nullptr;
+    };
+    Ice3gbStepFields d;
+    std::memset(&d, 0, sizeof(d));
+    d.sigqsat = up2(f->sigqsat);
+    d.pabs = up3(f->pabs); d.exn = up3(f->exn); d.exnref = up3(f->exnref); d.rhodref = up3(f->rhodref);
+    d.dzz = up3(f->dzz); d.sigs = up3(f->sigs); d.th = up3(f->th); d.rv = up3(f->rv); d.rc = up3(f->rc);
+    d.ri = up3(f->ri); d.rr = up3(f->rr); d.rs = up3(f->rs); d.rg = up3(f->rg);
+    d.cf_mf = up3(f->cf_mf); d.rc_mf = up3(f->rc_mf); d.ri_mf = up3(f->ri_mf);
+    d.sea = up2(f->sea); d.town = up2(f->town);
+    d.ths = up3(f->ths); d.rvs = up3(f->rvs); d.rcs = up3(f->rcs); d.rrs = up3(f->rrs); d.ris = up3(f->ris);
+    d.rss = up3(f->rss); d.rgs = up3(f->rgs); d.cit = up3(f->cit);
+    d.t = take(b3p); d.rv_out = take(b3p); d.rc_out = take(b3p); d.ri_out = take(b3p); d.cldfr = take(b3p);
+    d.hlc_hrc = take(b3p); d.hlc_hcf = take(b3p); d.hli_hri = take(b3p); d.hli_hcf = take(b3p);
+    d.rainfr = take(b3p);
+    d.inprc = take(b2p); d.inprr = take(b2p); d.inpri = take(b2p); d.inprs = take(b2p); d.inprg = take(b2p);
+    unsigned int *order = reinterpret_cast<unsigned int *>(base + off);
+    d.evap3d = P.evap_all + pt_off;
+    if (e == cudaSuccess) e = cudaEventRecord(P.in_done[b], P.s_in);
+    if (e != cudaSuccess) break;
+    // ---- compute (the fix-up of evap3d waits for the last slab)
+    if ((e = cudaStreamWaitEvent(P.s_cmp, P.in_done[b], 0)) != cudaSuccess) break;
+    const RiScratch rs = {P.keys_all + 0, P.keys_all + 1, P.keys_all + 4 + pt_off, order, false, false};
+    if ((rc = run_physics_step(h, (int)w, nk, dt, opt, &d, P.s_cmp, &rs))) break;
+    if ((e = cudaEventRecord(P.cmp_done[b], P.s_cmp)) != cudaSuccess) break;
+    // ---- copy out (everything but evap3d)
+    if ((e = cudaStreamWaitEvent(P.s_out, P.cmp_done[b], 0)) != cudaSuccess) break;
+    struct Out { double *dst; const double *src; bool three_d; };
+    const Out outs[] = {
+        {f->ths, d.ths, true}, {f->rvs, d.rvs, true}, {f->rcs, d.rcs, true}, {f->rrs, d.rrs, true},
+        {f->ris, d.ris, true}, {f->rss, d.rss, true}, {f->rgs, d.rgs, true}, {f->cit, d.cit, true},
+        {f->t, d.t, true}, {f->rv_out, d.rv_out, true}, {f->rc_out, d.rc_out, true}, {f->ri_out, d.ri_out, true},
+        {f->cldfr, d.cldfr, true}, {f->hlc_hrc, d.hlc_hrc, true}, {f->hlc_hcf, d.hlc_hcf, true},
+        {f->hli_hri, d.hli_hri, true}, {f->hli_hcf, d.hli_hcf, true}, {f->rainfr, d.rainfr, true},
+        {f->inprc, d.inprc, false}, {f->inprr, d.inprr, false}, {f->inpri, d.inpri, false},
+        {f->inprs, d.inprs, false}, {f->inprg, d.inprg, false}};
+    for (const Out &o : outs) {
+      if (e != cudaSuccess) break;
+      e = o.three_d ? cudaMemcpy2DAsync(o.dst + col0, hp, o.src, wb, wb, (size_t)nk, cudaMemcpyDeviceToHost, P.s_out)
+                    : cudaMemcpyAsync(o.dst + col0, o.src, wb, cudaMemcpyDeviceToHost, P.s_out);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(P.out_done[b], P.s_out);
+    if (e != cudaSuccess) break;
+    pt_off += w * nk;
+  }
+  if (rc == ICE3GB_OK && e == cudaSuccess) {
+    // evap3d: zero it where the point was not active in the last pass of the call
+    RainIceArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.f.evap3d = P.evap_all;
+    a.scr.keys = P.keys_all + 4;
+    a.scr.key_max = P.keys_all + 1;
+    a.nij = nij;
+    a.nk = nk;
+    {
+      ProfScope ps(h, K_EVAP_FIXUP, P.s_cmp);
+      e = launch_rain_ice_evap_fixup(a, P.s_cmp);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(P.fix_done, P.s_cmp);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_out, P.fix_done, 0);
+    long off_pts = 0;
+    for (long i = 0; i < nslab && e == cudaSuccess; ++i) {
+      const long col0 = i * w_max;
+      const long w = ((long)nij - col0) < w_max ? ((long)nij - col0) : w_max;
+      const size_t wb = (size_t)w * sizeof(double);
+      e = cudaMemcpy2DAsync(f->evap3d + col0, hp, P.evap_all + off_pts, wb, wb, (size_t)nk, cudaMemcpyDeviceToHost,
+                            P.s_out);
+      off_pts += w * nk;
+    }
+  }
+  // drain all three streams before returning (the call is synchronous)
+  const cudaError_t e1 = cudaStreamSynchronize(P.s_in);
+  const cudaError_t e2 = cudaStreamSynchronize(P.s_cmp);
+  const cudaError_t e3 = cudaStreamSynchronize(P.s_out);
+  if (rc != ICE3GB_OK) return rc;
+  if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
+  if (e != cudaSuccess) return cuda_fail(h, e, "slab pipeline");
+  return ICE3GB_OK;
+}
+
 }  // namespace
 
 // Validation + launch sequence with caller-provided scratch (used by the
@@ -366,7 +591,8 @@ int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double 
                 (long)nij * nk, scratch_points);
   if ((rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
   if (!scratch) return fail(h, ICE3GB_ERR_CUDA, "static scratch address unavailable");
-  return run_rain_ice_core(h, nij, nk, dt, opt, f, scratch, nullptr, static_cast<cudaStream_t>(stream));
+  const RiScratch rs = {scratch, scratch + 1, scratch + 4, nullptr, true, true};
+  return run_rain_ice_core(h, nij, nk, dt, opt, f, rs, static_cast<cudaStream_t>(stream));
 }
 
 // Records a CUDA error on the handle (or globally) for the other translation units.
@@ -490,6 +716,7 @@ int ice3gb_destroy(void *handle)
   Handle *h = as_handle(handle);
   if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_destroy: invalid handle");
   drop_events(h);
+  pipe_free(h);
   cudaFree(h->d_luts);
   cudaFree(h->d_status);
   if (h->d_stage) cudaFree(h->d_stage);
@@ -577,52 +804,7 @@ int ice3gb_physics_step_host(void *handle, int nij, int nk, double dt, const Ice
   int rc;
   if ((rc = check_shape(h, nij, nk)) || (rc = validate_step(h, f)) || (rc = check_device(h))) return rc;
   std::lock_guard<std::mutex> lock(h->mu);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t n = (size_t)nij * nk, b3 = n * sizeof(double), b2 = (size_t)nij * sizeof(double);
-  const size_t b3p = (b3 + 255) & ~(size_t)255, b2p = (b2 + 255) & ~(size_t)255;
-  // 3-D: 16 inputs + 8 in-out + 11 outputs; 2-D: sigqsat, sea, town + 5 outputs
-  if ((rc = ensure_stage(h, 35 * b3p + 8 * b2p))) return rc;
-  char *base = reinterpret_cast<char *>(h->d_stage);
-  size_t off = 0;
-  cudaError_t e = cudaSuccess;
-  auto take = [&](size_t bp) { double *p = reinterpret_cast<double *>(base + off); off += bp; return p; };
-  auto up = [&](const double *src, size_t b, size_t bp) -> double * {
-    double *p = take(bp);
-    if (src && e == cudaSuccess) e = cudaMemcpyAsync(p, src, b, cudaMemcpyHostToDevice, s);
-    return src ? p : nullptr;
-  };
-  Ice3gbStepFields d;
-  std::memset(&d, 0, sizeof(d));
-  d.sigqsat = up(f->sigqsat, b2, b2p);
-  d.pabs = up(f->pabs, b3, b3p); d.exn = up(f->exn, b3, b3p); d.exnref = up(f->exnref, b3, b3p);
-  d.rhodref = up(f->rhodref, b3, b3p); d.dzz = up(f->dzz, b3, b3p); d.sigs = up(f->sigs, b3, b3p);
-  d.th = up(f->th, b3, b3p); d.rv = up(f->rv, b3, b3p); d.rc = up(f->rc, b3, b3p); d.ri = up(f->ri, b3, b3p);
-  d.rr = up(f->rr, b3, b3p); d.rs = up(f->rs, b3, b3p); d.rg = up(f->rg, b3, b3p);
-  d.cf_mf = up(f->cf_mf, b3, b3p); d.rc_mf = up(f->rc_mf, b3, b3p); d.ri_mf = up(f->ri_mf, b3, b3p);
-  d.sea = up(f->sea, b2, b2p); d.town = up(f->town, b2, b2p);
-  d.ths = up(f->ths, b3, b3p); d.rvs = up(f->rvs, b3, b3p); d.rcs = up(f->rcs, b3, b3p);
-  d.rrs = up(f->rrs, b3, b3p); d.ris = up(f->ris, b3, b3p); d.rss = up(f->rss, b3, b3p);
-  d.rgs = up(f->rgs, b3, b3p); d.cit = up(f->cit, b3, b3p);
-  d.t = take(b3p); d.rv_out = take(b3p); d.rc_out = take(b3p); d.ri_out = take(b3p); d.cldfr = take(b3p);
-  d.hlc_hrc = take(b3p); d.hlc_hcf = take(b3p); d.hli_hri = take(b3p); d.hli_hcf = take(b3p);
-  d.evap3d = take(b3p); d.rainfr = take(b3p);
-  d.inprc = take(b2p); d.inprr = take(b2p); d.inpri = take(b2p); d.inprs = take(b2p); d.inprg = take(b2p);
-  if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
-  if ((rc = run_physics_step(h, nij, nk, dt, opt, &d, s))) return rc;
-  struct Pair { double *dst; const double *src; size_t bytes; };
-  const Pair back[] = {
-      {f->ths, d.ths, b3}, {f->rvs, d.rvs, b3}, {f->rcs, d.rcs, b3}, {f->rrs, d.rrs, b3}, {f->ris, d.ris, b3},
-      {f->rss, d.rss, b3}, {f->rgs, d.rgs, b3}, {f->cit, d.cit, b3}, {f->t, d.t, b3}, {f->rv_out, d.rv_out, b3},
-      {f->rc_out, d.rc_out, b3}, {f->ri_out, d.ri_out, b3}, {f->cldfr, d.cldfr, b3},
-      {f->hlc_hrc, d.hlc_hrc, b3}, {f->hlc_hcf, d.hlc_hcf, b3}, {f->hli_hri, d.hli_hri, b3},
-      {f->hli_hcf, d.hli_hcf, b3}, {f->evap3d, d.evap3d, b3}, {f->rainfr, d.rainfr, b3},
-      {f->inprc, d.inprc, b2}, {f->inprr, d.inprr, b2}, {f->inpri, d.inpri, b2}, {f->inprs, d.inprs, b2},
-      {f->inprg, d.inprg, b2}};
-  for (const Pair &p : back)
-    if (e == cudaSuccess) e = cudaMemcpyAsync(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
-  return ICE3GB_OK;
+  return run_physics_step_pipelined(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream));
 }
 
 int ice3gb_rain_ice(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,

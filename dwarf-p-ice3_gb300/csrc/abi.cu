@@ -57,9 +57,9 @@ struct Handle {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
 
-enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_COUNT };
+enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_IA_VJP, K_SED_VJP, K_COUNT };
 const char *kKernelNames[K_COUNT] = {"ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup",
-                                     "fog_deposition", "rain_ice_order"};
+                                     "fog_deposition", "rain_ice_order", "ice_adjust_vjp", "sedimentation_vjp"};
 
 // Brackets one launch with events when the handle is profiling.
 struct ProfScope {
@@ -783,6 +783,91 @@ int ice3gb_sedimentation(void *handle, int nij, int nk, double dt, const Ice3gbS
                              static_cast<cudaStream_t>(stream));
   }
   if (e != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+  return ICE3GB_OK;
+}
+
+int ice3gb_ice_adjust_vjp(void *handle, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f,
+                          const Ice3gbIceAdjustCotangents *g, const Ice3gbIceAdjustGradients *gx, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_ice_adjust_vjp: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk))) return rc;
+  if (!f || !g || !gx) return fail(h, ICE3GB_ERR_NULL, "fields, cotangents or gradients pointer is NULL");
+  REQUIRE(f->sigqsat); REQUIRE(f->pabs); REQUIRE(f->sigs); REQUIRE(f->th); REQUIRE(f->exn);
+  REQUIRE(f->exn_ref); REQUIRE(f->rho_dry_ref); REQUIRE(f->rv); REQUIRE(f->rc); REQUIRE(f->ri);
+  REQUIRE(f->rr); REQUIRE(f->rs); REQUIRE(f->rg); REQUIRE(f->cf_mf); REQUIRE(f->rc_mf); REQUIRE(f->ri_mf);
+  REQUIRE(f->rvs); REQUIRE(f->rcs); REQUIRE(f->ris); REQUIRE(f->ths);
+  if (h->c.CONDENS != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "CONDENS=%g (only CB02=0)", h->c.CONDENS);
+  if (h->c.OCND2 != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 is not supported");
+  if ((rc = check_device(h))) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long n = (long)nij * nk;
+  IaVjpArgs a;
+  a.f = *f;
+  a.g = *g;
+  a.gx = *gx;
+  a.nij = nij;
+  a.nk = nk;
+  a.dt = dt;
+  a.sigqsat_out = nullptr;
+  double *scr = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (gx->sigqsat) {
+    if (f->sigqsat_3d) {
+      a.sigqsat_out = gx->sigqsat;
+    } else {
+      if ((e = cudaMallocAsync(&scr, sizeof(double) * (size_t)n, s)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaMallocAsync");
+      a.sigqsat_out = scr;
+    }
+  }
+  {
+    ProfScope ps(h, K_IA_VJP, s);
+    e = launch_ice_adjust_vjp(h->c, a, h->num_sms, s);
+  }
+  if (e == cudaSuccess && scr) e = launch_column_sum(scr, gx->sigqsat, nij, nk, s);
+  if (scr) cudaFreeAsync(scr, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "ice_adjust_vjp launch");
+  return ICE3GB_OK;
+}
+
+int ice3gb_sedimentation_vjp(void *handle, int nij, int nk, double dt, const Ice3gbSedimentationFields *f,
+                             const Ice3gbSedimentationCotangents *g, const Ice3gbSedimentationGradients *gx,
+                             void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_sedimentation_vjp: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk))) return rc;
+  if (!f || !g || !gx) return fail(h, ICE3GB_ERR_NULL, "fields, cotangents or gradients pointer is NULL");
+  REQUIRE(f->rhodref); REQUIRE(f->dzz); REQUIRE(f->pabs); REQUIRE(f->tht);
+  REQUIRE(f->rcs); REQUIRE(f->rrs); REQUIRE(f->ris); REQUIRE(f->rss); REQUIRE(f->rgs);
+  if ((f->sea == nullptr) != (f->town == nullptr))
+    return fail(h, ICE3GB_ERR_NULL, "sea and town must be both given or both NULL");
+  if ((rc = check_device(h))) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long n = (long)nij * nk;
+  SedVjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.rhodref = f->rhodref; a.dzz = f->dzz; a.pabs = f->pabs; a.tht = f->tht; a.sea = f->sea; a.town = f->town;
+  a.src[0] = f->rcs; a.src[1] = f->rrs; a.src[2] = f->ris; a.src[3] = f->rss; a.src[4] = f->rgs;
+  a.nij = nij; a.nk = nk; a.dt = dt; a.fortran = f->fortran_semantics ? 1 : 0;
+  a.g.src[0] = g->rcs; a.g.src[1] = g->rrs; a.g.src[2] = g->ris; a.g.src[3] = g->rss; a.g.src[4] = g->rgs;
+  a.g.inpr[0] = g->inprc; a.g.inpr[1] = g->inprr; a.g.inpr[2] = g->inpri; a.g.inpr[3] = g->inprs;
+  a.g.inpr[4] = g->inprg;
+  a.g.fpr[0] = g->fpr_c; a.g.fpr[1] = g->fpr_r; a.g.fpr[2] = g->fpr_i; a.g.fpr[3] = g->fpr_s; a.g.fpr[4] = g->fpr_g;
+  a.gx.src[0] = gx->rcs; a.gx.src[1] = gx->rrs; a.gx.src[2] = gx->ris; a.gx.src[3] = gx->rss;
+  a.gx.src[4] = gx->rgs;
+  a.gx.rhodref = gx->rhodref; a.gx.dzz = gx->dzz; a.gx.pabs = gx->pabs; a.gx.tht = gx->tht;
+  cudaError_t e = cudaMallocAsync(&a.flux, sizeof(double) * 5 * (size_t)n, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
+  {
+    ProfScope ps(h, K_SED_VJP, s);
+    e = launch_sedimentation_vjp(h->c, a, s);
+  }
+  cudaFreeAsync(a.flux, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "sedimentation_vjp launch");
   return ICE3GB_OK;
 }
 

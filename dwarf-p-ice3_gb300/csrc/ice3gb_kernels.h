@@ -49,6 +49,39 @@ struct IaKernelFields {
   double adv_dt;
 };
 
+// ice_adjust adjoint arguments; sigqsat_out receives the per-point sigqsat
+// gradient ([nk][nij]: the 3-D gradient itself, or the terms of the column sum).
+struct IaVjpArgs {
+  Ice3gbIceAdjustFields f;
+  Ice3gbIceAdjustCotangents g;
+  Ice3gbIceAdjustGradients gx;
+  double *sigqsat_out;
+  int nij, nk;
+  double dt;
+};
+
+// sedimentation adjoint arguments (the cotangent / gradient pointer sets
+// mirror Ice3gbSedimentationCotangents / Ice3gbSedimentationGradients);
+// flux is a [5][nk][nij] scratch for the recomputed forward fluxes.
+struct SedVjpArgs {
+  const double *rhodref, *dzz, *pabs, *tht, *sea, *town;
+  const double *src[5];
+  double *flux;
+  int nij, nk;
+  double dt;
+  int fortran;
+  struct {
+    const double *src[5], *inpr[5], *fpr[5];
+  } g;
+  struct {
+    double *src[5];
+    double *rhodref, *dzz, *pabs, *tht;
+  } gx;
+};
+cudaError_t launch_sedimentation_vjp(const Ice3gbConstants &c, const SedVjpArgs &a, cudaStream_t s);
+
+cudaError_t launch_ice_adjust_vjp(const Ice3gbConstants &c, const IaVjpArgs &a, int num_sms, cudaStream_t s);
+cudaError_t launch_column_sum(const double *in, double *out, int nij, int nk, cudaStream_t s);
 cudaError_t launch_ice_adjust(const Ice3gbConstants &c, const IaKernelFields &kf, int nij, int nk, double dt,
                               bool vec2, int num_sms, cudaStream_t s);
 cudaError_t launch_sedimentation(const Ice3gbConstants &c, const SedArgs &a, cudaStream_t s);

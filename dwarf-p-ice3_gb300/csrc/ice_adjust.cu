@@ -7,140 +7,10 @@
 // 280 algorithmic bytes per point.
 #include "ice3gb_device.cuh"
 #include "ice3gb_kernels.h"
+#include "ice_adjust_point.cuh"
 
 namespace {
-
-struct IaIn {
-  double sigqsat, pabs, sigs, th, exn, exn_ref, rho, rv, rc, ri, rr, rs, rg, cf_mf, rc_mf, ri_mf;
-  double rvs, rcs, ris, ths;
-};
-struct IaOut {
-  double t, rv_out, rc_out, ri_out, cldfr, hlc_hrc, hlc_hcf, hli_hri, hli_hcf, cph, lv, ls;
-  double rvs, rcs, ris, ths;
-};
-
-// Triangle-PDF subgrid autoconversion (stencils/ice_adjust.py:316-341).
-ICE3_HD void triangle_pdf(double w_dt, double crit, double cf_mf, double &hcf, double &hr)
-{
-  const double wmax = nmax(1e-20, w_dt);
-  const double inv_w2 = fm::frcp(sq(wmax));
-  if (fgt(w_dt, crit)) {
-    const double cc = crit * cf_mf;
-    hcf = 1.0 - 0.5 * sq(cc) * inv_w2;
-    hr = w_dt - cc * cc * cc * (inv_w2 * (1.0 / 3.0));
-  } else if (fge(crit, 2.0 * w_dt)) {
-    hcf = 0.0;
-    hr = 0.0;
-  } else {
-    hcf = 0.5 * sq(2.0 * w_dt - crit) * inv_w2;
-    hr = (4.0 * w_dt * w_dt * w_dt - 3.0 * w_dt * sq(crit) + crit * crit * crit) * (inv_w2 * (1.0 / 3.0));
-  }
-  hcf *= cf_mf;
-}
-
-// Constants derived once per thread (divisions of table constants).
-struct IaDerived {
-  double rdrv, rvrd, irv;   // RD/RV, RV/RD, 1/RV
-};
-ICE3_HD IaDerived ia_derived(const Cst &c) { return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV}; }
-
-ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt, const IaIn &x, IaOut &o)
-{
-  const int nrr = (int)c.NRR;
-  double t = x.th * x.exn;
-  const double lv = c.LVTT + (c.CPV - c.CL) * (t - c.TT);
-  const double ls = c.LSTT + (c.CPV - c.CI) * (t - c.TT);
-  double cph;
-  if (nrr == 5) cph = c.CPD + c.CPV * x.rv + c.CL * (x.rc + x.rr) + c.CI * (x.ri + x.rs);
-  else if (nrr == 4) cph = c.CPD + c.CPV * x.rv + c.CL * (x.rc + x.rr);
-  else if (nrr == 2) cph = c.CPD + c.CPV * x.rv + c.CL * x.rc + c.CI * x.ri;
-  else cph = c.CPD + c.CPV * x.rv + c.CL * (x.rc + x.rr) + c.CI * (x.ri + x.rs + x.rg);
-  const double inv_cph = fm::frcp(cph);
-  double cldfr = 0.0, rv_out = 0.0, rc_out = 0.0, ri_out = 0.0;
-  double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
-  if (c.LSUBG_COND != 0.0) {
-    const double rt = x.rv + x.rc + x.ri;
-    // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
-    const double lt = fm::flog(t), it = fm::frcp(t);
-    const double pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
-    const double piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
-    double frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
-    const int fmode = (int)c.FRAC_ICE_ADJUST;
-    if (fmode == 3) frac = nclip01(frac);
-    else if (fmode == 0) frac = nclip01(fm::fdiv(c.TMAXMIX - t, c.TMAXMIX - c.TMINMIX));
-    double qsl = fm::fdiv(d.rdrv * pv, x.pabs - pv);
-    const double qsi = fm::fdiv(d.rdrv * piv, x.pabs - piv);
-    qsl = (1.0 - frac) * qsl + frac * qsi;
-    const double lvs = (1.0 - frac) * lv + frac * ls;
-    const double ah = lvs * qsl * (it * it * d.irv) * (1.0 + qsl * d.rvrd);
-    const double a = fm::frcp(1.0 + lvs * inv_cph * ah);
-    const double sbar = a * (rt - qsl + ah * lvs * (x.rc + x.ri) * inv_cph);
-    double sigma;
-    if (c.LSIGMAS != 0.0 && c.LSTATNW == 0.0)
-      sigma = !(fge(x.sigqsat, 0.0) && fge(0.0, x.sigqsat)) ? sqrt(sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a))
-                                                             : 2.0 * x.sigs;
-    else
-      sigma = 2.0 * x.sigs;
-    sigma = nmax(1e-10, sigma);
-    const double q1 = fm::fdiv(sbar, sigma);
-    double cond;
-    if (fgt(q1, 0.0)) cond = fge(2.0, q1) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;
-    else cond = fm::fexp(1.2 * q1 - 1.0);
-    cond *= sigma;
-    cldfr = fge(cond, 1e-12) ? nclip01(0.5 + 0.36 * fm::fatan(1.55 * q1)) : 0.0;
-    if (fge(cldfr, 0.0) && fge(0.0, cldfr)) cond = 0.0;
-    rc_out = (1.0 - frac) * cond;
-    ri_out = frac * cond;
-    t = t + ((rc_out - x.rc) * lv + (ri_out - x.ri) * ls) * inv_cph;
-    rv_out = rt - rc_out - ri_out;
-  }
-  double rvs = x.rvs, rcs = x.rcs, ris = x.ris, ths = x.ths;
-  const double inv_cphex = fm::fdiv(inv_cph, x.exn_ref);
-  double w1 = (rc_out - x.rc) * inv_dt, w2 = (ri_out - x.ri) * inv_dt;
-  w1 = fgt(0.0, w1) ? nmax(w1, -rcs) : nmin(w1, rvs);
-  rvs = rvs - w1;
-  rcs = rcs + w1;
-  ths = ths + w1 * lv * inv_cphex;
-  w2 = fgt(0.0, w2) ? nmax(w2, -ris) : nmin(w2, rvs);
-  rvs = rvs - w2;
-  ris = ris + w2;
-  ths = ths + w2 * ls * inv_cphex;
-  if (c.LSUBG_COND == 0.0) {
-    cldfr = fgt((rcs + ris) * dt, 1e-12) ? 1.0 : 0.0;
-  } else {
-    double w1m = x.rc_mf * inv_dt, w2m = x.ri_mf * inv_dt;
-    const double tot = w1m + w2m;
-    const double scale = fgt(tot, rvs) ? fm::fdiv(rvs, tot) : 1.0;
-    w1m *= scale;
-    w2m *= scale;
-    cldfr = nmin(1.0, cldfr + x.cf_mf);
-    rcs = rcs + w1m;
-    ris = ris + w2m;
-    rvs = rvs - w1m - w2m;
-    ths = ths + (w1m * lv + w2m * ls) * inv_cphex;
-    const int mfpdf = (int)c.SUBG_MF_PDF;
-    if (mfpdf == 0 || mfpdf == 1) {
-      const double criaut = fm::fdiv(c.CRIAUTC, x.rho);
-      const double criaut_i = nmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
-      if (mfpdf == 0) {
-        if (fgt(w1m * dt, x.cf_mf * criaut)) { hlc_hrc = w1m * dt; hlc_hcf = nmin(1.0, x.cf_mf); }
-        if (fgt(w2m * dt, x.cf_mf * criaut_i)) { hli_hri = w2m * dt; hli_hcf = nmin(1.0, x.cf_mf); }
-      } else {
-        double hcf, hr;
-        triangle_pdf(w1m * dt, x.cf_mf * criaut, x.cf_mf, hcf, hr);
-        hlc_hcf = nmin(1.0, hcf);
-        hlc_hrc = hr;
-        triangle_pdf(w2m * dt, x.cf_mf * criaut_i, x.cf_mf, hcf, hr);
-        hli_hcf = nmin(1.0, hcf);
-        hli_hri = hr;
-      }
-    }
-  }
-  o.t = t; o.rv_out = rv_out; o.rc_out = rc_out; o.ri_out = ri_out; o.cldfr = cldfr;
-  o.hlc_hrc = hlc_hrc; o.hlc_hcf = hlc_hcf; o.hli_hri = hli_hri; o.hli_hcf = hli_hcf;
-  o.cph = cph; o.lv = lv; o.ls = ls;
-  o.rvs = rvs; o.rcs = rcs; o.ris = ris; o.ths = ths;
-}
+using namespace ice3ia;
 
 // Two points per thread, double2 loads/stores; requires an even point count
 // and 16-byte aligned fields (checked by the host).  ADV: the state adjusted

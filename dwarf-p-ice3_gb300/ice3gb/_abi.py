@@ -62,6 +62,29 @@ class StepFields(ctypes.Structure):
         "evap3d", "rainfr", "inprc", "inprr", "inpri", "inprs", "inprg")]
 
 
+IA_IN = ("sigqsat", "pabs", "sigs", "th", "exn", "exn_ref", "rho_dry_ref", "rv", "rc", "ri", "rr", "rs", "rg",
+         "cf_mf", "rc_mf", "ri_mf", "rvs", "rcs", "ris", "ths")
+IA_OUT = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls",
+          "rvs", "rcs", "ris", "ths")
+
+
+class SedimentationCotangents(ctypes.Structure):
+    _fields_ = [(n, P) for n in ("rcs", "rrs", "ris", "rss", "rgs", "inprc", "inprr", "inpri", "inprs", "inprg",
+                                 "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")]
+
+
+class SedimentationGradients(ctypes.Structure):
+    _fields_ = [(n, P) for n in ("rcs", "rrs", "ris", "rss", "rgs", "rhodref", "dzz", "pabs", "tht")]
+
+
+class IceAdjustCotangents(ctypes.Structure):
+    _fields_ = [(n, P) for n in IA_OUT]
+
+
+class IceAdjustGradients(ctypes.Structure):
+    _fields_ = [(n, P) for n in IA_IN]
+
+
 STEP_IN = ("sigqsat", "pabs", "exn", "exnref", "rhodref", "dzz", "sigs", "th", "rv", "rc", "ri", "rr", "rs", "rg",
            "cf_mf", "rc_mf", "ri_mf")
 STEP_INOUT = ("ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "cit")
@@ -81,10 +104,12 @@ EXPORTED = (
     "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status", "ice3gb_ice_adjust",
     "ice3gb_sedimentation", "ice3gb_rain_ice", "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host",
     "ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_profile_enable", "ice3gb_profile_read",
-    "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc",
+    "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc", "ice3gb_ice_adjust_vjp",
+    "ice3gb_sedimentation_vjp",
 )
 NOALLOC_MAX_POINTS = 4194304
-KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order")
+KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order",
+                "ice_adjust_vjp", "sedimentation_vjp")
 
 _lib: Optional[ctypes.CDLL] = None
 
@@ -121,6 +146,15 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ice3gb_physics_step.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                         ctypes.POINTER(RainIceOptions), ctypes.POINTER(StepFields), P]
     lib.ice3gb_physics_step_host.argtypes = lib.ice3gb_physics_step.argtypes
+    lib.ice3gb_ice_adjust_vjp.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                          ctypes.POINTER(IceAdjustFields), ctypes.POINTER(IceAdjustCotangents),
+                                          ctypes.POINTER(IceAdjustGradients), P]
+    lib.ice3gb_ice_adjust_vjp.restype = ctypes.c_int
+    lib.ice3gb_sedimentation_vjp.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                             ctypes.POINTER(SedimentationFields),
+                                             ctypes.POINTER(SedimentationCotangents),
+                                             ctypes.POINTER(SedimentationGradients), P]
+    lib.ice3gb_sedimentation_vjp.restype = ctypes.c_int
     lib.ice3gb_profile_enable.argtypes = [P, ctypes.c_int]
     lib.ice3gb_profile_enable.restype = ctypes.c_int
     lib.ice3gb_profile_read.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]

@@ -243,6 +243,61 @@ int ice3gb_rain_ice(void *handle, int nij, int nk, double dt,
 int ice3gb_physics_step(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                         const Ice3gbStepFields *f, void *stream);
 
+/* ---- adjoint of ice_adjust ---------------------------------------------- */
+/* Cotangents of the 16 outputs of ice3gb_ice_adjust (NULL = zero), same
+ * names and shapes as in Ice3gbIceAdjustFields. */
+typedef struct Ice3gbIceAdjustCotangents {
+  const double *t, *rv_out, *rc_out, *ri_out, *cldfr;
+  const double *hlc_hrc, *hlc_hcf, *hli_hri, *hli_hcf;
+  const double *cph, *lv, *ls;
+  const double *rvs, *rcs, *ris, *ths;
+} Ice3gbIceAdjustCotangents;
+
+/* Gradients of the 20 inputs (NULL = not wanted; written, not accumulated).
+ * sigqsat is [nij] when the forward's sigqsat is per column (its gradient is
+ * then summed over the levels), [nk][nij] otherwise. */
+typedef struct Ice3gbIceAdjustGradients {
+  double *sigqsat, *pabs, *sigs, *th, *exn, *exn_ref, *rho_dry_ref;
+  double *rv, *rc, *ri, *rr, *rs, *rg;
+  double *cf_mf, *rc_mf, *ri_mf;
+  double *rvs, *rcs, *ris, *ths;
+} Ice3gbIceAdjustGradients;
+
+/* Vector-Jacobian product of ice3gb_ice_adjust at the inputs of `f` (its
+ * output pointers are not used): gradients of <cotangents, outputs> with
+ * respect to every input.  Hand-written reverse mode that recomputes the
+ * forward intermediates per point; at kinks (min/max, clips) the derivative
+ * of the branch the forward takes.  No counterpart in the reference (which
+ * relies on jax.vjp of IceAdjustJAX, src/ice3/jax/ice_adjust.py:139). */
+int ice3gb_ice_adjust_vjp(void *handle, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f,
+                          const Ice3gbIceAdjustCotangents *g, const Ice3gbIceAdjustGradients *gx, void *stream);
+
+/* ---- adjoint of the sedimentation sweep ---------------------------------- */
+/* Cotangents of the outputs of ice3gb_sedimentation (NULL = zero): the
+ * updated sources [nk][nij], the surface precipitation [nij] and the
+ * fluxes fpr_* [nk][nij]. */
+typedef struct Ice3gbSedimentationCotangents {
+  const double *rcs, *rrs, *ris, *rss, *rgs;
+  const double *inprc, *inprr, *inpri, *inprs, *inprg;
+  const double *fpr_c, *fpr_r, *fpr_i, *fpr_s, *fpr_g;
+} Ice3gbSedimentationCotangents;
+
+/* Gradients of the inputs (NULL = not wanted): the sources before the sweep
+ * and rhodref, dzz, pabs, tht [nk][nij]. */
+typedef struct Ice3gbSedimentationGradients {
+  double *rcs, *rrs, *ris, *rss, *rgs;
+  double *rhodref, *dzz, *pabs, *tht;
+} Ice3gbSedimentationGradients;
+
+/* Vector-Jacobian product of ice3gb_sedimentation at the inputs of `f` (its
+ * rcs..rgs are read as the sources before the sweep and not modified; its
+ * output pointers are not used).  Hand-written reverse sweep (bottom-up)
+ * that recomputes the column fluxes first.  No counterpart in the reference
+ * (sedimentation_stat, src/ice3/jax/stencils/sedimentation.py:58). */
+int ice3gb_sedimentation_vjp(void *handle, int nij, int nk, double dt, const Ice3gbSedimentationFields *f,
+                             const Ice3gbSedimentationCotangents *g, const Ice3gbSedimentationGradients *gx,
+                             void *stream);
+
 /* ---- allocation-free rain_ice ------------------------------------------- */
 /* Same computation and arguments as ice3gb_rain_ice, for callers that must
  * not allocate device memory during the call (a model that gives the GPU's
@@ -264,8 +319,9 @@ int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3
  * those events and returns, per kernel id, the number of launches and their
  * summed device time since the last enable.  Kernel ids: 0 ice_adjust,
  * 1 sedimentation, 2 rain_ice (pointwise sub-stepping), 3 rain_ice evap3d
- * fix-up, 4 fog deposition, 5 rain_ice point ordering (regime sort). */
-#define ICE3GB_NKERNELS 6
+ * fix-up, 4 fog deposition, 5 rain_ice point ordering (regime sort),
+ * 6 ice_adjust adjoint, 7 sedimentation adjoint. */
+#define ICE3GB_NKERNELS 8
 int         ice3gb_profile_enable(void *handle, int enable);
 int         ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms);
 const char *ice3gb_kernel_name(int kernel_id);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cuda_bf16.h>
 
 #include "../../include/ice3gb.h"
 
@@ -82,6 +83,35 @@ cudaError_t launch_sedimentation_vjp(const Ice3gbConstants &c, const SedVjpArgs 
 
 cudaError_t launch_ice_adjust_vjp(const Ice3gbConstants &c, const IaVjpArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_column_sum(const double *in, double *out, int nij, int nk, cudaStream_t s);
+// BF16 tensor-core GEMM (mlp.cu): C[m][n] = sum_k A(m, k) B(n, k) with
+// A(m, k) = A[m * sam + k * sak], B(n, k) = B[n * sbn + k * sbk]; N <= 256.
+enum { EPI_STORE = 0, EPI_BIAS_GELU = 1, EPI_BIAS = 2, EPI_DGELU = 3 };
+struct TcGemmArgs {
+  const __nv_bfloat16 *A;
+  long sam, sak;
+  const __nv_bfloat16 *B;
+  long sbn, sbk;
+  int M, N, K, k_split;
+  int epi;
+  float *C;                 // EPI_STORE (split partials), EPI_BIAS, EPI_DGELU (f32 dZ, optional)
+  long ldc;
+  const float *bias;        // EPI_BIAS_GELU, EPI_BIAS
+  const float *Zin;         // EPI_DGELU
+  float *Zout;              // EPI_BIAS_GELU (optional)
+  long ldz;
+  __nv_bfloat16 *H;         // EPI_BIAS_GELU, EPI_DGELU
+  long ldh;
+  int *err;
+};
+cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t s);
+cudaError_t launch_sum_splits(const float *part, float *out, long n, int splits, cudaStream_t s);
+cudaError_t launch_col_sum(const float *x, float *out, int rows, int cols, long ld, cudaStream_t s);
+cudaError_t launch_surrogate_loss(const float *y, const float *tgt, int rows, int nrates, __nv_bfloat16 *dy, float *dyf,
+                                  float *loss, cudaStream_t s);
+cudaError_t launch_adam(float *w, const float *g, float *m1, float *m2, __nv_bfloat16 *w16, long n, float lr, float b1,
+                        float b2, float eps, int step, cudaStream_t s);
+cudaError_t launch_to_bf16(const float *x, __nv_bfloat16 *y, long n, cudaStream_t s);
+
 cudaError_t launch_ice_adjust(const Ice3gbConstants &c, const IaKernelFields &kf, int nij, int nk, double dt,
                               bool vec2, int num_sms, cudaStream_t s);
 cudaError_t launch_sedimentation(const Ice3gbConstants &c, const SedArgs &a, cudaStream_t s);

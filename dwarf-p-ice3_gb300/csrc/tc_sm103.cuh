@@ -1,0 +1,94 @@
+// tc_sm103.cuh — inline-PTX wrappers for the 5th-generation tensor cores
+// (tcgen05) of sm_103a: TMEM allocation, shared-memory matrix descriptors,
+// the BF16 MMA with FP32 accumulation in TMEM, its completion through an
+// mbarrier, and TMEM loads for the epilogue.
+//
+// Operands live in shared memory in the K-major layout without swizzle:
+// 8-row x 16-byte core matrices (8 x 8 BF16) stored as 128 contiguous bytes;
+// in the descriptor the leading byte offset is the distance between
+// core matrices adjacent along K and the stride byte offset the distance
+// between core matrices adjacent along M (or N).  One MMA consumes K = 16.
+#pragma once
+
+#include <stdint.h>
+#include <cuda_bf16.h>
+
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor (no swizzle, base offset 0).
+__device__ __forceinline__ uint64_t desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+  uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;                      // fixed field 0b001 (bits 46-48)
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Offset (elements) of (row, k) in a [rows x kc] K-major tile, kc % 8 == 0.
+__device__ __forceinline__ int core_off(int row, int k, int kc) { return ((row >> 3) * (kc >> 3) + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols)
+{
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(dst_smem)), "r"(ncols));
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(ncols));
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes made visible to the tensor core
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count));
+}
+
+// D (TMEM) (+)= A * B^T for one K = 16 step.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc, bool acc)
+{
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+               :: "r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(acc ? 1u : 0u));
+}
+// Arrive on the mbarrier when all MMAs issued so far by this thread complete.
+__device__ __forceinline__ void commit(uint64_t *bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(bar)));
+}
+// Bounded wait for the completion of phase `parity`; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long max_iter)
+{
+  uint32_t done = 0;
+  for (long it = 0; it < max_iter && !done; ++it)
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(smem_u32(bar)), "r"(parity));
+  return done != 0;
+}
+
+// 16 consecutive FP32 columns of one TMEM lane per thread: warp w (of the
+// 4 warps of the CTA) reads lanes 32w .. 32w + 31.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
+{
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+}  // namespace tc

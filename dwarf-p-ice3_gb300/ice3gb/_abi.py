@@ -93,6 +93,11 @@ STEP_OUT3 = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "
 STEP_OUT2 = ("inprc", "inprr", "inpri", "inprs", "inprg")
 
 
+class MlpShape(ctypes.Structure):
+    _fields_ = [("n_in", ctypes.c_int32), ("n_hidden", ctypes.c_int32),
+                ("n_hidden_layers", ctypes.c_int32), ("n_out", ctypes.c_int32)]
+
+
 class RainIceOptions(ctypes.Structure):
     _fields_ = [("lsedim_after", ctypes.c_int32), ("ldeposc", ctypes.c_int32),
                 ("lfeedbackt", ctypes.c_int32), ("max_passes", ctypes.c_int32),
@@ -105,7 +110,9 @@ EXPORTED = (
     "ice3gb_sedimentation", "ice3gb_rain_ice", "ice3gb_ice_adjust_host", "ice3gb_rain_ice_host",
     "ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_profile_enable", "ice3gb_profile_read",
     "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc", "ice3gb_ice_adjust_vjp",
-    "ice3gb_sedimentation_vjp",
+    "ice3gb_sedimentation_vjp", "ice3gb_mlp_create", "ice3gb_mlp_destroy", "ice3gb_mlp_param_count",
+    "ice3gb_mlp_get_params", "ice3gb_mlp_set_params", "ice3gb_mlp_forward", "ice3gb_mlp_loss_grad",
+    "ice3gb_mlp_train_step", "ice3gb_mlp_error", "ice3gb_tc_gemm_bf16",
 )
 NOALLOC_MAX_POINTS = 4194304
 KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order",
@@ -159,6 +166,24 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ice3gb_profile_enable.restype = ctypes.c_int
     lib.ice3gb_profile_read.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     lib.ice3gb_profile_read.restype = ctypes.c_int
+    F = ctypes.POINTER(ctypes.c_float)
+    I64 = ctypes.c_int64
+    lib.ice3gb_mlp_create.argtypes = [ctypes.POINTER(MlpShape), ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]
+    lib.ice3gb_mlp_destroy.argtypes = [P]
+    lib.ice3gb_mlp_param_count.argtypes = [P]
+    lib.ice3gb_mlp_param_count.restype = I64
+    lib.ice3gb_mlp_get_params.argtypes = [P, F]
+    lib.ice3gb_mlp_set_params.argtypes = [P, F]
+    lib.ice3gb_mlp_forward.argtypes = [P, ctypes.c_int, P, P, P]
+    lib.ice3gb_mlp_loss_grad.argtypes = [P, ctypes.c_int, P, P, P, P, P]
+    lib.ice3gb_mlp_train_step.argtypes = [P, ctypes.c_int, P, P, ctypes.c_float, P, P]
+    lib.ice3gb_mlp_error.argtypes = [P]
+    lib.ice3gb_tc_gemm_bf16.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, I64, I64, P, I64, I64, P, I64,
+                                        P, P]
+    for name in ("ice3gb_mlp_create", "ice3gb_mlp_destroy", "ice3gb_mlp_get_params", "ice3gb_mlp_set_params",
+                 "ice3gb_mlp_forward", "ice3gb_mlp_loss_grad", "ice3gb_mlp_train_step", "ice3gb_mlp_error",
+                 "ice3gb_tc_gemm_bf16"):
+        getattr(lib, name).restype = ctypes.c_int
     lib.ice3gb_kernel_name.argtypes = [ctypes.c_int]
     lib.ice3gb_kernel_name.restype = ctypes.c_char_p
     for name in ("ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_create", "ice3gb_destroy", "ice3gb_last_error", "ice3gb_status",

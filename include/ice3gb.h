@@ -298,6 +298,39 @@ int ice3gb_sedimentation_vjp(void *handle, int nij, int nk, double dt, const Ice
                              const Ice3gbSedimentationCotangents *g, const Ice3gbSedimentationGradients *gx,
                              void *stream);
 
+/* ---- BF16 tensor-core MLP (the slow-process surrogate) ------------------ */
+/* A per-point MLP n_in -> n_hidden (GELU) x n_hidden_layers -> n_out with
+ * BF16 weights and activations on the tcgen05 tensor cores (FP32
+ * accumulation), FP32 master weights and Adam; hand-written backward pass.
+ * Limits: n_in <= 256, 16 <= n_hidden <= 256, n_hidden_layers <= 8, n_out
+ * even and <= 16.  Parameters: a flat FP32 vector, per layer W [out][in]
+ * then b [out].  Arrays are device FP32: x [n][n_in], y [n][n_out], targets
+ * [n][16] (per rate r: 2r = 1 if the rate is nonzero, 2r + 1 = transformed
+ * value).  No counterpart exists in the reference. */
+typedef struct Ice3gbMlpShape {
+  int32_t n_in, n_hidden, n_hidden_layers, n_out;
+} Ice3gbMlpShape;
+int     ice3gb_mlp_create(const Ice3gbMlpShape *shape, uint64_t seed, void **mlp);
+int     ice3gb_mlp_destroy(void *mlp);
+int64_t ice3gb_mlp_param_count(void *mlp);
+int     ice3gb_mlp_get_params(void *mlp, float *host);
+int     ice3gb_mlp_set_params(void *mlp, const float *host);
+int     ice3gb_mlp_forward(void *mlp, int n, const float *x, float *y, void *stream);
+/* Loss (binary cross-entropy of the activity logits + squared error of the
+ * values where active, mean over the n rows) and its gradient (device
+ * [param_count] or NULL) for one batch. */
+int     ice3gb_mlp_loss_grad(void *mlp, int n, const float *x, const float *targets, float *grad, float *loss,
+                             void *stream);
+/* One Adam step (lr, beta 0.9 / 0.999) on one batch; loss: device float or NULL. */
+int     ice3gb_mlp_train_step(void *mlp, int n, const float *x, const float *targets, float lr, float *loss,
+                              void *stream);
+/* ICE3GB_ERR_DEVICE if a tensor-core kernel of this MLP timed out on its barrier. */
+int     ice3gb_mlp_error(void *mlp);
+/* The GEMM building block: C[m][n] (FP32, row stride ldc) = sum_k A(m,k) B(n,k)
+ * with BF16 A(m,k) = A[m*sam + k*sak], B(n,k) = B[n*sbn + k*sbk], N <= 256. */
+int     ice3gb_tc_gemm_bf16(int M, int N, int K, const void *A, int64_t sam, int64_t sak, const void *B, int64_t sbn,
+                            int64_t sbk, float *C, int64_t ldc, int *err, void *stream);
+
 /* ---- allocation-free rain_ice ------------------------------------------- */
 /* Same computation and arguments as ice3gb_rain_ice, for callers that must
  * not allocate device memory during the call (a model that gives the GPU's

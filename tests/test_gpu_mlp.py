@@ -1,0 +1,93 @@
+"""The BF16 tensor-core (tcgen05) GEMM and the surrogate MLP built on it:
+the GEMM against an FP64 product of the same BF16 operands (row- and
+column-major operands, ragged M/N/K, split-free and many-CTA grids), the
+MLP forward and its hand-written gradients against the NumPy restatement
+(oracle/mlp_ref.py), and a few Adam steps lowering the loss."""
+import mlp_ref
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf(shape, gen, scale=1.0, transposed=False):
+    t = (torch.randn(shape[::-1] if transposed else shape, generator=gen, device="cuda") * scale).to(torch.bfloat16)
+    return t.t() if transposed else t
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 16, 16), (300, 256, 64), (1000, 10, 256), (777, 200, 40), (129, 48, 1000),
+                                   (70000, 256, 256), (5, 16, 10)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+def test_tc_gemm_matches_fp64(M, N, K, ta, tb):
+    from ice3gb.mlp import tc_gemm_bf16
+    gen = torch.Generator(device="cuda").manual_seed(M * 7 + N * 3 + K)
+    a = _bf((M, K), gen, transposed=ta)
+    b = _bf((N, K), gen, transposed=tb)
+    c = tc_gemm_bf16(a, b)
+    ref = a.double() @ b.double().t()
+    bound = a.double().abs() @ b.double().abs().t()
+    err = (c.double() - ref).abs()
+    assert bool((err <= 1e-6 * bound + 1e-30).all()), float((err / (bound + 1e-30)).max())
+
+
+def _mlp_case(seed, n, n_in=16, n_hidden=256, layers=3, n_out=10):
+    from ice3gb.mlp import Mlp
+    net = Mlp(n_in, n_hidden, layers, n_out, seed=seed)
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, n_in)).astype(np.float32)
+    t = np.zeros((n, 16), dtype=np.float32)
+    act = (rng.uniform(size=(n, n_out // 2)) < 0.6).astype(np.float32)
+    t[:, 0:n_out:2] = act
+    t[:, 1:n_out:2] = rng.standard_normal((n, n_out // 2)).astype(np.float32)
+    return net, x, t
+
+
+def test_mlp_forward_matches_oracle():
+    net, x, _ = _mlp_case(1, 3000)
+    y = net(torch.as_tensor(x).cuda()).cpu().numpy().astype(np.float64)
+    net.check()
+    yr, _ = mlp_ref.forward(net.get_params(), net.layout(), x)
+    # BF16 roundings of the hidden activations may fall differently where the
+    # FP32 sums differ in their last bits: compare in RMS, per output
+    rms = np.sqrt(np.mean((y - yr) ** 2, axis=0))
+    scale = np.sqrt(np.mean(yr ** 2, axis=0))
+    assert np.all(rms <= 5e-3 * scale), (rms / scale)
+
+
+@pytest.mark.parametrize("n", [1000, 4096, 20000])
+def test_mlp_gradients_match_oracle(n):
+    """Hand-written backward pass (tcgen05 GEMMs with transposed staging,
+    split-K over the batch) against the FP64 restatement, per layer."""
+    net, x, t = _mlp_case(2 + n, n)
+    loss, g = net.loss_grad(torch.as_tensor(x).cuda(), torch.as_tensor(t).cuda())
+    net.check()
+    g = g.cpu().numpy().astype(np.float64)
+    lr, gr = mlp_ref.loss_grad(net.get_params(), net.layout(), x, t)
+    assert abs(loss - lr) <= 1e-4 * abs(lr), (loss, lr)
+    for (wo, bo, o, i) in net.layout():
+        for lo, hi in ((wo, wo + o * i), (bo, bo + o)):
+            a, r = g[lo:hi], gr[lo:hi]
+            rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+            assert rel <= 2e-2, (lo, hi, rel)
+
+
+def test_mlp_training_lowers_loss():
+    """A smooth synthetic regression learnt by Adam on the device."""
+    from ice3gb.mlp import Mlp
+    net = Mlp(16, 256, 3, 10, seed=5)
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    n = 8192
+    losses = []
+    lbuf = torch.zeros(1, dtype=torch.float32, device="cuda")
+    for it in range(300):
+        x = torch.randn((n, 16), generator=gen, device="cuda")
+        t = torch.zeros((n, 16), device="cuda")
+        for r in range(5):
+            t[:, 2 * r] = (x[:, r] + 0.5 * x[:, r + 5] > 0).float()
+            t[:, 2 * r + 1] = torch.sin(x[:, r]) * x[:, 10 + r]
+        net.train_step(x, t, 1e-3, lbuf)
+        if it % 50 == 0 or it == 299:
+            losses.append(float(lbuf.item()))
+    net.check()
+    assert losses[-1] < 0.35 * losses[0], losses

@@ -57,9 +57,13 @@ struct Handle {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
 };
 
-enum { K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_IA_VJP, K_SED_VJP, K_COUNT };
+enum {
+  K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_IA_VJP, K_SED_VJP, K_SUR_SAMPLE, K_SUR_MLP,
+  K_SUR_RAIN_ICE, K_COUNT
+};
 const char *kKernelNames[K_COUNT] = {"ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup",
-                                     "fog_deposition", "rain_ice_order", "ice_adjust_vjp", "sedimentation_vjp"};
+                                     "fog_deposition", "rain_ice_order", "ice_adjust_vjp", "sedimentation_vjp",
+                                     "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate"};
 
 // Brackets one launch with events when the handle is profiling.
 struct ProfScope {
@@ -210,9 +214,86 @@ struct RiScratch {
   bool evap_fixup;         // false: the caller runs the fix-up after the last call
 };
 
-// Launch sequence of one rain_ice call.
+// The learned slow rates of a surrogate-assisted rain_ice call.
+struct SurCall {
+  void *mlp;
+  const Ice3gbSurrogateNorm *norm;
+  uint64_t *stats;   // host [ICE3GB_SUR_NSTATS] or NULL
+};
+
+int check_surrogate(Handle *h, const SurCall &sur, long n)
+{
+  int n_in = 0, n_out = 0;
+  if (!mlp_dims(sur.mlp, &n_in, &n_out)) return fail(h, ICE3GB_ERR_HANDLE, "surrogate: not an MLP handle");
+  if (n_in != ICE3GB_SUR_NFEAT || n_out != ICE3GB_SUR_NOUT)
+    return fail(h, ICE3GB_ERR_SHAPE, "surrogate: the MLP maps %d -> %d, expected %d -> %d", n_in, n_out,
+                ICE3GB_SUR_NFEAT, ICE3GB_SUR_NOUT);
+  if (!sur.norm) return fail(h, ICE3GB_ERR_NULL, "surrogate: normalisation is NULL");
+  if (n > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "surrogate: at most 2^31 - 1 points per call");
+  return ICE3GB_OK;
+}
+
+// Features -> network -> rain_ice with the learned slow rates.  Synchronises
+// the stream once to size the network's batch and once at the end (device
+// error flag of the tensor-core kernels, counters).
+int run_surrogate_points(Handle *h, const Ice3gbConstants &c, const RainIceArgs &a, const SurCall &sur,
+                         cudaStream_t s)
+{
+  const long n = (long)a.nij * a.nk;
+  const size_t fb = ((sizeof(float) * 16 * (size_t)n + 255) / 256) * 256;
+  const size_t yb = ((sizeof(float) * ICE3GB_SUR_NOUT * (size_t)n + 255) / 256) * 256;
+  const size_t rb = ((sizeof(int) * (size_t)n + 255) / 256) * 256;
+  char *scr = nullptr;
+  cudaError_t e = cudaMallocAsync(&scr, fb + yb + rb + 256, s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
+  float *feat = reinterpret_cast<float *>(scr), *y = reinterpret_cast<float *>(scr + fb);
+  int *row_of_point = reinterpret_cast<int *>(scr + fb + yb);
+  unsigned long long *ctr = reinterpret_cast<unsigned long long *>(scr + fb + yb + rb);
+  int rc = ICE3GB_OK;
+  e = cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (1 + ICE3GB_SUR_NSTATS), s);
+  if (e == cudaSuccess) {
+    SurSampleArgs sa;
+    std::memset(&sa, 0, sizeof(sa));
+    sa.f = a.f; sa.luts = a.luts; sa.nij = a.nij; sa.nk = a.nk; sa.dt = a.dt;
+    sa.norm_on = 1; sa.norm = *sur.norm;
+    sa.feat = feat; sa.row_of_point = row_of_point; sa.count = ctr; sa.stats = ctr + 1; sa.cap = n;
+    ProfScope ps(h, K_SUR_SAMPLE, s);
+    e = launch_surrogate_sample(c, sa, h->num_sms, s);
+  }
+  unsigned long long rows = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&rows, ctr, sizeof(rows), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) rc = cuda_fail(h, e, "surrogate sampling");
+  if (rc == ICE3GB_OK && rows > 0) {
+    ProfScope ps(h, K_SUR_MLP, s);
+    e = mlp_infer(sur.mlp, (long)(rows < (unsigned long long)n ? rows : n), feat, y, s);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "surrogate network");
+  }
+  if (rc == ICE3GB_OK) {
+    SurRainIceArgs ra;
+    ra.ri = a; ra.y = y; ra.ldy = ICE3GB_SUR_NOUT; ra.row_of_point = row_of_point; ra.stats = ctr + 1;
+    ProfScope ps(h, K_SUR_RAIN_ICE, s);
+    e = launch_rain_ice_surrogate(c, ra, h->num_sms, s);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "rain_ice surrogate launch");
+  }
+  unsigned long long st[ICE3GB_SUR_NSTATS] = {};
+  if (rc == ICE3GB_OK) {
+    e = cudaMemcpyAsync(st, ctr + 1, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "surrogate counters");
+  }
+  if (rc == ICE3GB_OK && mlp_device_error(sur.mlp))
+    rc = fail(h, ICE3GB_ERR_DEVICE, "surrogate network: a tensor-core barrier timed out");
+  if (rc == ICE3GB_OK && sur.stats)
+    for (int i = 0; i < ICE3GB_SUR_NSTATS; ++i) sur.stats[i] = st[i];
+  cudaFreeAsync(scr, s);
+  return rc;
+}
+
+// Launch sequence of one rain_ice call (sur: with the learned slow rates).
 int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                      const Ice3gbRainIceFields *f, const RiScratch &rs, cudaStream_t s)
+                      const Ice3gbRainIceFields *f, const RiScratch &rs, cudaStream_t s,
+                      const SurCall *sur = nullptr)
 {
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (h->c.LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (h->c.LDEPOSC != 0.0);
@@ -249,7 +330,11 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
     ProfScope ps(h, K_ORDER, s);
     if ((e = launch_rain_ice_order(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice order launch");
   }
-  {
+  if (sur) {
+    const int rc = run_surrogate_points(h, c, a, *sur, s);
+    if (rc != ICE3GB_OK) return rc;
+    e = cudaSuccess;
+  } else {
     ProfScope ps(h, K_RAIN_ICE, s);
     e = launch_rain_ice_points(c, a, h->num_sms, s);
   }
@@ -275,7 +360,7 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
 // rain_ice with per-call scratch from the stream-ordered allocator: control
 // words, pass keys and (below 2^32 points) the processing order.
 int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                 const Ice3gbRainIceFields *f, cudaStream_t s)
+                 const Ice3gbRainIceFields *f, cudaStream_t s, const SurCall *sur = nullptr)
 {
   const long n = (long)nij * nk;
   const bool ordered = n < 4294967296L;
@@ -284,7 +369,7 @@ int run_rain_ice(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptio
   cudaError_t e = cudaMallocAsync(&scr, bytes, s);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocAsync");
   const RiScratch rs = {scr, scr + 1, scr + 4, ordered ? scr + 4 + n : nullptr, true, true};
-  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, rs, s);
+  const int rc = run_rain_ice_core(h, nij, nk, dt, opt, f, rs, s, sur);
   cudaFreeAsync(scr, s);
   return rc;
 }
@@ -309,7 +394,8 @@ int validate_step(Handle *h, const Ice3gbStepFields *f)
 }
 
 int run_physics_step(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
-                     const Ice3gbStepFields *f, cudaStream_t s, const RiScratch *ri_scr = nullptr)
+                     const Ice3gbStepFields *f, cudaStream_t s, const RiScratch *ri_scr = nullptr,
+                     const SurCall *sur = nullptr)
 {
   const long n = (long)nij * nk;
   double *scr = nullptr;
@@ -344,7 +430,8 @@ int run_physics_step(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceO
     r.ths = f->ths; r.rvs = f->rvs; r.rcs = f->rcs; r.rrs = f->rrs; r.ris = f->ris; r.rss = f->rss;
     r.rgs = f->rgs; r.evap3d = f->evap3d; r.rainfr = f->rainfr; r.inprc = f->inprc; r.inprr = f->inprr;
     r.inpri = f->inpri; r.inprs = f->inprs; r.inprg = f->inprg;
-    rc = ri_scr ? run_rain_ice_core(h, nij, nk, dt, opt, &r, *ri_scr, s) : run_rain_ice(h, nij, nk, dt, opt, &r, s);
+    rc = ri_scr ? run_rain_ice_core(h, nij, nk, dt, opt, &r, *ri_scr, s, sur)
+                : run_rain_ice(h, nij, nk, dt, opt, &r, s, sur);
   }
   // 3. final adjustment on the post-microphysics state dt*S2 with S2 -> S3
   if (rc == ICE3GB_OK) {
@@ -900,6 +987,65 @@ int ice3gb_rain_ice(void *handle, int nij, int nk, double dt, const Ice3gbRainIc
   int rc;
   if ((rc = check_shape(h, nij, nk)) || (rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
   return run_rain_ice(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream));
+}
+
+// ---- learned surrogate of the ICE4_SLOW rates ------------------------------
+
+int ice3gb_surrogate_sample(void *handle, int nij, int nk, double dt, const Ice3gbRainIceFields *f,
+                            const Ice3gbSurrogateNorm *norm, int64_t cap, float *features, float *targets,
+                            int64_t *point_of_row, int32_t *row_of_point, uint64_t *counters, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_surrogate_sample: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
+  if (!features || !counters) return fail(h, ICE3GB_ERR_NULL, "ice3gb_surrogate_sample: features or counters NULL");
+  if (cap < 0 || cap > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "ice3gb_surrogate_sample: cap %lld", (long long)cap);
+  if (!aligned16(features) || (targets && !aligned16(targets)))
+    return fail(h, ICE3GB_ERR_ALIGN, "ice3gb_surrogate_sample: features/targets not 16-byte aligned");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(uint64_t) * (1 + ICE3GB_SUR_NSTATS), s);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
+  SurSampleArgs sa;
+  std::memset(&sa, 0, sizeof(sa));
+  sa.f = *f; sa.luts = h->d_luts; sa.nij = nij; sa.nk = nk; sa.dt = dt;
+  sa.norm_on = norm != nullptr;
+  if (norm) sa.norm = *norm;
+  sa.feat = features; sa.targets = targets;
+  sa.point_of_row = reinterpret_cast<long long *>(point_of_row);
+  sa.row_of_point = row_of_point;
+  sa.count = reinterpret_cast<unsigned long long *>(counters);
+  sa.stats = reinterpret_cast<unsigned long long *>(counters) + 1;
+  sa.cap = (long)cap;
+  ProfScope ps(h, K_SUR_SAMPLE, s);
+  if ((e = launch_surrogate_sample(h->c, sa, h->num_sms, s)) != cudaSuccess) return cuda_fail(h, e, "surrogate sample");
+  return ICE3GB_OK;
+}
+
+int ice3gb_rain_ice_surrogate(void *handle, void *mlp, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                              const Ice3gbRainIceFields *f, const Ice3gbSurrogateNorm *norm, uint64_t *stats,
+                              void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_rain_ice_surrogate: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
+  const SurCall sur = {mlp, norm, stats};
+  if ((rc = check_surrogate(h, sur, (long)nij * nk))) return rc;
+  return run_rain_ice(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream), &sur);
+}
+
+int ice3gb_physics_step_surrogate(void *handle, void *mlp, int nij, int nk, double dt,
+                                  const Ice3gbRainIceOptions *opt, const Ice3gbStepFields *f,
+                                  const Ice3gbSurrogateNorm *norm, uint64_t *stats, void *stream)
+{
+  Handle *h = as_handle(handle);
+  if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_physics_step_surrogate: invalid handle");
+  int rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_step(h, f)) || (rc = check_device(h))) return rc;
+  const SurCall sur = {mlp, norm, stats};
+  if ((rc = check_surrogate(h, sur, (long)nij * nk))) return rc;
+  return run_physics_step(h, nij, nk, dt, opt, f, static_cast<cudaStream_t>(stream), nullptr, &sur);
 }
 
 // ---- host-buffer entry points ---------------------------------------------

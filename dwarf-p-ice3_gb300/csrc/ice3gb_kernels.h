@@ -42,6 +42,32 @@ struct RainIceArgs {
   int lfeedbackt;
 };
 
+// Surrogate feature sampling (surrogate_rain_ice.cu).
+struct SurSampleArgs {
+  Ice3gbRainIceFields f;
+  const double *luts;
+  int nij, nk;
+  double dt;
+  int norm_on;                      // standardise + envelope check
+  Ice3gbSurrogateNorm norm;
+  float *feat;                      // [cap][16]
+  float *targets;                   // [cap][16] or NULL
+  long long *point_of_row;          // [cap] or NULL
+  int *row_of_point;                // [n] or NULL
+  unsigned long long *count;        // rows handed out (may exceed cap)
+  unsigned long long *stats;        // ICE3GB_SUR_* counters
+  long cap;
+};
+
+// rain_ice with the learned slow rates.
+struct SurRainIceArgs {
+  RainIceArgs ri;
+  const float *y;                   // network outputs, row stride ldy
+  int ldy;
+  const int *row_of_point;          // [n], -1: plain path
+  unsigned long long *stats;
+};
+
 // ice_adjust kernel arguments: the public fields plus the optional
 // "advance the state by adv_dt * sources first" extension of the chained step.
 struct IaKernelFields {
@@ -104,6 +130,20 @@ struct TcGemmArgs {
   int *err;
 };
 cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t s);
+// Fused inference of the 16 -> 256 x 3 (GELU) -> n_out <= 16 MLP (mlp.cu).
+struct MlpFusedArgs {
+  const float *x;           // [n][16]
+  float *y;                 // [n][n_out]
+  long n;
+  int n_out;
+  const __nv_bfloat16 *w1, *w2, *w3, *w4;   // packed by launch_mlp_pack
+  const float *b1, *b2, *b3, *b4;
+  int *err;
+};
+constexpr long MLP_PACKED_ELEMS = 4096 + 65536 + 65536 + 4096;
+cudaError_t launch_mlp_pack(const float *p, long w1, long w2, long w3, long w4, int n_out, __nv_bfloat16 *out,
+                            cudaStream_t s);
+cudaError_t launch_mlp_fused(const MlpFusedArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_sum_splits(const float *part, float *out, long n, int splits, cudaStream_t s);
 cudaError_t launch_col_sum(const float *x, float *out, int rows, int cols, long ld, cudaStream_t s);
 cudaError_t launch_surrogate_loss(const float *y, const float *tgt, int rows, int nrates, __nv_bfloat16 *dy, float *dyf,
@@ -120,3 +160,13 @@ cudaError_t launch_rain_ice_points(const Ice3gbConstants &c, const RainIceArgs &
 cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_order(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 size_t rain_ice_smem_bytes();
+
+cudaError_t launch_surrogate_sample(const Ice3gbConstants &c, const SurSampleArgs &a, int num_sms, cudaStream_t s);
+cudaError_t launch_rain_ice_surrogate(const Ice3gbConstants &c, const SurRainIceArgs &a, int num_sms, cudaStream_t s);
+// Forward pass of an MLP handle (ice3gb_mlp_create) over n rows in chunks,
+// without keeping activations; cudaErrorInvalidValue for a bad handle.
+cudaError_t mlp_infer(void *mlp, long n, const float *x, float *y, cudaStream_t s);
+// n_in / n_out of an MLP handle; false for a bad handle.
+bool mlp_dims(void *mlp, int *n_in, int *n_out);
+// 1 if a tensor-core kernel of the MLP timed out (device flag, synchronous read).
+int mlp_device_error(void *mlp);

@@ -26,12 +26,30 @@
 namespace {
 
 constexpr int KC = 64;                 // K chunk per stage
-constexpr long WAIT_ITERS = 1L << 26;  // bounded mbarrier wait (~seconds)
+constexpr long WAIT_ITERS = 1L << 22;  // bounded mbarrier wait (about a second at most)
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))
+// (Hendrycks & Gimpel 2016), with the hardware tanh.approx.f32: one MUFU
+// operation and five FP32 operations per activation, the same function in
+// training and inference.
+__device__ __forceinline__ float tanh_hw(float x)
+{
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu(float z)
+{
+  const float u = z * fmaf(0.035677408136300125f, z * z, 0.7978845608028654f);
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_hw(u), h);
+}
 __device__ __forceinline__ float dgelu(float z)
 {
-  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+  const float z2 = z * z;
+  const float th = tanh_hw(z * fmaf(0.035677408136300125f, z2, 0.7978845608028654f));
+  const float du = fmaf(0.10703222440890037f, z2, 0.7978845608028654f);
+  return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * du;
 }
 
 __global__ void __launch_bounds__(128) tc_gemm_kernel(const TcGemmArgs a)
@@ -168,6 +186,247 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const TcGemmArgs a)
   if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// Fused inference of the surrogate's MLP shape (16 -> 256 -> 256 -> 256 ->
+// n_out <= 16, GELU): one persistent CTA per SM walks 128-row tiles.  Per
+// tile the 128 x 256 FP32 accumulator lives in TMEM (256 columns), the BF16
+// activations in shared memory (64 KB, K-major core matrices), W1 and the
+// output layer stay resident in shared memory, and W2 / W3 stream from L2 as
+// eight 32 KB K-chunks (pre-packed in the core-matrix layout) through a
+// three-stage ring filled by bulk asynchronous copies.  Thread 0 issues the
+// copies and the tcgen05.mma; all four warps run the epilogues (tcgen05.ld,
+// bias, GELU, BF16 pack into the activation tile).
+constexpr int FZ_NST = 3;                               // weight ring stages
+constexpr uint32_t FZ_CHUNK_BYTES = 256 * 64 * 2;       // one K-chunk of W2 / W3
+constexpr int FZ_OFF_H = 0, FZ_OFF_STAGE = 65536, FZ_OFF_W1 = FZ_OFF_STAGE + FZ_NST * 32768;
+constexpr int FZ_OFF_W4 = FZ_OFF_W1 + 8192, FZ_OFF_X = FZ_OFF_W4 + 8192, FZ_OFF_B = FZ_OFF_X + 4096;
+constexpr int FZ_SMEM = FZ_OFF_B + (3 * 256 + 16) * 4;
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
+{
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// Bias + GELU of the 128 x 256 accumulator into the activation tile.
+__device__ __forceinline__ void fz_epilogue_gelu(uint32_t tmem, int warp, int row, const float *bias,
+                                                 __nv_bfloat16 *sH)
+{
+#pragma unroll 1
+  for (int c0 = 0; c0 < 256; c0 += 16) {
+    float v[16];
+    tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) w[j] = pack_bf16x2(gelu(v[2 * j] + bias[c0 + 2 * j]), gelu(v[2 * j + 1] + bias[c0 + 2 * j + 1]));
+    *reinterpret_cast<uint4 *>(sH + tc::core_off(row, c0, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(sH + tc::core_off(row, c0 + 8, 256)) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
+__global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
+{
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __nv_bfloat16 *sH = reinterpret_cast<__nv_bfloat16 *>(smem + FZ_OFF_H);
+  __nv_bfloat16 *sW1 = reinterpret_cast<__nv_bfloat16 *>(smem + FZ_OFF_W1);
+  __nv_bfloat16 *sW4 = reinterpret_cast<__nv_bfloat16 *>(smem + FZ_OFF_W4);
+  __nv_bfloat16 *sX = reinterpret_cast<__nv_bfloat16 *>(smem + FZ_OFF_X);
+  float *sB = reinterpret_cast<float *>(smem + FZ_OFF_B);
+  __shared__ __align__(8) uint64_t bar_mma, bar_full[FZ_NST], bar_free[FZ_NST];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long ntiles = (a.n + 127) / 128;
+  const long my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const long total_chunks = 8 * my_tiles;
+  // resident operands: W1 (256 x 16), output layer (16 x 256), biases
+  for (int i = tid; i < 4096 / 8; i += 128) {
+    reinterpret_cast<uint4 *>(sW1)[i] = __ldg(reinterpret_cast<const uint4 *>(a.w1) + i);
+    reinterpret_cast<uint4 *>(sW4)[i] = __ldg(reinterpret_cast<const uint4 *>(a.w4) + i);
+  }
+  for (int i = tid; i < 256; i += 128) {
+    sB[i] = a.b1[i];
+    sB[256 + i] = a.b2[i];
+    sB[512 + i] = a.b3[i];
+  }
+  if (tid < 16) sB[768 + tid] = tid < a.n_out ? a.b4[tid] : 0.0f;
+  if (tid == 0) {
+    tc::mbar_init(&bar_mma, 1);
+    for (int s = 0; s < FZ_NST; ++s) {
+      tc::mbar_init(&bar_full[s], 1);
+      tc::mbar_init(&bar_free[s], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 256);
+  tc::fence_async_smem();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_base;
+  const uint32_t id256 = tc::idesc_bf16_f32(128, 256), id16 = tc::idesc_bf16_f32(128, 16);
+  const uint32_t aH = tc::smem_u32(sH), aX = tc::smem_u32(sX), aW1 = tc::smem_u32(sW1), aW4 = tc::smem_u32(sW4);
+  long issued = 0, consumed = 0;       // weight chunks (thread 0's bookkeeping)
+  uint32_t mma_phase = 0;
+  bool ok = true;
+  // chunk g of the stream: W2 chunks 0..3, then W3 chunks 0..3, per tile
+  auto issue = [&](long g) -> bool {
+    const int s = (int)(g % FZ_NST);
+    if (g >= FZ_NST && !tc::mbar_wait(&bar_free[s], (uint32_t)((g / FZ_NST - 1) & 1), WAIT_ITERS)) return false;
+    const int j = (int)(g % 8);
+    const __nv_bfloat16 *src = (j < 4 ? a.w2 : a.w3) + (long)(j & 3) * (256 * 64);
+    tc::mbar_expect_tx(&bar_full[s], FZ_CHUNK_BYTES);
+    tc::bulk_g2s(smem + FZ_OFF_STAGE + s * 32768, src, FZ_CHUNK_BYTES, &bar_full[s]);
+    ++issued;
+    return true;
+  };
+  if (tid == 0)
+    for (long g = 0; g < FZ_NST - 1 && g < total_chunks && ok; ++g) ok = issue(g);
+  long tile = blockIdx.x;
+  for (long it = 0; it < my_tiles; ++it, tile += gridDim.x) {
+    const long r0 = tile * 128;
+    // ---- input rows -> BF16 tile
+    {
+      const long row = r0 + tid;
+      float x[16];
+      if (row < a.n) {
+        const float4 *xp = reinterpret_cast<const float4 *>(a.x + row * 16);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 v = __ldg(xp + q);
+          x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) x[q] = 0.0f;
+      }
+      *reinterpret_cast<uint4 *>(sX + tc::core_off(tid, 0, 16)) =
+          make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), pack_bf16x2(x[4], x[5]), pack_bf16x2(x[6], x[7]));
+      *reinterpret_cast<uint4 *>(sX + tc::core_off(tid, 8, 16)) =
+          make_uint4(pack_bf16x2(x[8], x[9]), pack_bf16x2(x[10], x[11]), pack_bf16x2(x[12], x[13]),
+                     pack_bf16x2(x[14], x[15]));
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    // ---- layer 1: K = 16, one MMA
+    if (tid == 0) {
+      tc::mma_bf16(tmem, tc::desc(aX, 128u, 256u), tc::desc(aW1, 128u, 256u), id256, false);
+      tc::commit(&bar_mma);
+    }
+    ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
+    mma_phase ^= 1u;
+    tc::fence_after();
+    if (!ok) break;
+    fz_epilogue_gelu(tmem, warp, tid, sB, sH);
+    // ---- layers 2 and 3: K = 256 in four chunks each
+    for (int layer = 0; layer < 2 && ok; ++layer) {
+      tc::fence_async_smem();
+      tc::fence_before();
+      __syncthreads();
+      tc::fence_after();
+      if (tid == 0) {
+        for (int c = 0; c < 4 && ok; ++c) {
+          const long g = consumed;
+          const int s = (int)(g % FZ_NST);
+          ok = tc::mbar_wait(&bar_full[s], (uint32_t)((g / FZ_NST) & 1), WAIT_ITERS);
+          if (!ok) break;
+          tc::fence_after();
+          const uint32_t aS = tc::smem_u32(smem + FZ_OFF_STAGE + s * 32768);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            tc::mma_bf16(tmem, tc::desc(aH + (uint32_t)(c * 8 + 2 * j) * 128u, 128u, 4096u),
+                         tc::desc(aS + (uint32_t)(2 * j) * 128u, 128u, 1024u), id256, c > 0 || j > 0);
+          tc::commit(&bar_free[s]);
+          ++consumed;
+          const long gn = g + FZ_NST - 1;
+          if (gn < total_chunks && gn >= issued) ok = issue(gn);
+        }
+        tc::commit(&bar_mma);
+      }
+      ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
+      mma_phase ^= 1u;
+      tc::fence_after();
+      if (!ok) break;
+      fz_epilogue_gelu(tmem, warp, tid, sB + 256 * (layer + 1), sH);
+    }
+    if (!ok) break;
+    // ---- output layer: N = 16, K = 256
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        tc::mma_bf16(tmem, tc::desc(aH + (uint32_t)(2 * j) * 128u, 128u, 4096u),
+                     tc::desc(aW4 + (uint32_t)(2 * j) * 128u, 128u, 4096u), id16, j > 0);
+      tc::commit(&bar_mma);
+    }
+    ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
+    mma_phase ^= 1u;
+    tc::fence_after();
+    if (!ok) break;
+    {
+      float v[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
+      const long row = r0 + tid;
+      if (row < a.n) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (j < a.n_out) a.y[row * a.n_out + j] = v[j] + sB[768 + j];
+      }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(a.err, 1);
+    // let the tensor core and the copies in flight finish before the
+    // shared memory and TMEM are released (the last committed MMA phase is
+    // mma_phase ^ 1)
+    if (tid == 0) {
+      tc::mbar_wait(&bar_mma, mma_phase ^ 1u, WAIT_ITERS);
+      for (long g = consumed; g < issued; ++g)
+        tc::mbar_wait(&bar_full[g % FZ_NST], (uint32_t)((g / FZ_NST) & 1), WAIT_ITERS);
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
+// FP32 master weights -> the fused kernel's BF16 layouts: W1 [256][16] and
+// the output layer [16][256] (rows >= n_out zero) as K-major core-matrix
+// tiles, W2 / W3 [256][256] as four K-chunks of 256 x 64 each.
+__global__ void mlp_pack_kernel(const float *__restrict__ p, long w1, long w2, long w3, long w4, int n_out,
+                                __nv_bfloat16 *__restrict__ out)
+{
+  const long total = 4096 + 65536 + 65536 + 4096;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    float v;
+    long dst;
+    if (i < 4096) {                                   // W1: n = i / 16, k = i % 16
+      const int n = (int)(i / 16), k = (int)(i % 16);
+      v = p[w1 + i];
+      dst = tc::core_off(n, k, 16);
+    } else if (i < 4096 + 131072) {                   // W2 / W3: n, k in 256 x 256
+      const long j = i - 4096;
+      const int l = (int)(j / 65536);
+      const int n = (int)((j % 65536) / 256), k = (int)(j % 256);
+      v = p[(l == 0 ? w2 : w3) + (long)n * 256 + k];
+      dst = 4096 + (long)l * 65536 + (long)(k / 64) * (256 * 64) + tc::core_off(n, k % 64, 64);
+    } else {                                          // output layer: n < 16, k < 256
+      const long j = i - 4096 - 131072;
+      const int n = (int)(j / 256), k = (int)(j % 256);
+      v = n < n_out ? p[w4 + (long)n * 256 + k] : 0.0f;
+      dst = 4096 + 131072 + tc::core_off(n, k, 256);
+    }
+    out[dst] = __float2bfloat16(v);
+  }
+}
+
 // Sum of the split-K partials in a fixed order: out[i] = sum_s part[s * n + i].
 __global__ void sum_splits_kernel(const float *__restrict__ part, float *__restrict__ out, long n, int splits)
 {
@@ -265,6 +524,25 @@ cudaError_t launch_tc_gemm(const TcGemmArgs &a, cudaStream_t s)
   if (e != cudaSuccess) return e;
   dim3 grid((unsigned)((a.M + 127) / 128), (unsigned)a.k_split);
   tc_gemm_kernel<<<grid, 128, tc_gemm_smem_bytes(), s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_pack(const float *p, long w1, long w2, long w3, long w4, int n_out, __nv_bfloat16 *out,
+                            cudaStream_t s)
+{
+  mlp_pack_kernel<<<136, 1024, 0, s>>>(p, w1, w2, w3, w4, n_out, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_fused(const MlpFusedArgs &a, int num_sms, cudaStream_t s)
+{
+  cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FZ_SMEM);
+  if (e != cudaSuccess) return e;
+  const long tiles = (a.n + 127) / 128;
+  long blocks = num_sms;
+  if (blocks > tiles) blocks = tiles;
+  if (blocks < 1) return cudaSuccess;
+  mlp_fused_kernel<<<(unsigned)blocks, 128, FZ_SMEM, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -559,13 +559,31 @@ ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact
            b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
 }
 
+// The five ICE4_SLOW rates of a hard pass taken from the learned surrogate
+// (sur: RCHONI, RVDEPS, RIAGGS, RIAUTS, RVDEPG): each process keeps its exact
+// activity condition of mode_ice4_slow.F90 and the physical sign and cap of
+// its rate; only the magnitude comes from the network.
+ICE3_HD void slow_rates_from(const Cst &c, double t, const double v[NV], const double hi[4], const double *sur,
+                             Rates &R)
+{
+  double *b = R.bu;
+  const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_i = gtp(v[IRI], c.I_RTMIN);
+  const bool has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
+  b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c) ? dmin(1000., pmax0(sur[0])) : 0.0;
+  b[B_RVDEPS] = (has_v && has_s) ? sur[1] : 0.0;
+  b[B_RIAGGS] = (has_i && has_s) ? pmax0(sur[2]) : 0.0;
+  b[B_RIAUTS] = gtp(hi[2], c.I_RTMIN) ? pmax0(sur[3]) : 0.0;
+  b[B_RVDEPG] = (has_v && has_g) ? sur[4] : 0.0;
+}
+
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
 // nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
 // and all rates are computed; a soft pass keeps the hard-pass rates.
+template <bool SUR = false>
 ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict__ lut, bool soft,
                         const PointFix &pf, double lvfact, double lsfact, double &cit, double t0,
                         const double vart[NV], Rates &R, double &rainfr, double hl[4], double hi[4], double A[NV],
-                        double B[NV])
+                        double B[NV], const double *sur = nullptr)
 {
   double v[NV];
   double t = t0;
@@ -621,14 +639,17 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   }
   if (!soft) hard_rates(c, d, lut, pf, t, v, cit, hl, hi, criauti, R);
   else soft_rates(c, t, v, cit, hl, hi, R);
+  if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
   aggregate(c, t, v, lvfact, lsfact, R, A);
 }
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
+template <bool SUR = false>
 ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                               double dt, int max_passes, double vart[NV], const double ext[NV], double &cit,
-                              double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped)
+                              double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped,
+                              const double *sur = nullptr)
 {
   const double rsmin[NV] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN};
   Rates R;
@@ -661,7 +682,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
       double A[NV], B[NV];
-      tendencies(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
+      tendencies<SUR>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur);
+      if (SUR) sur = nullptr;          // learned slow rates: first hard pass only
 #pragma unroll
       for (int v = 0; v < NV; ++v) A[v] += ext[v];
       double maxtime = dt - ztime;
@@ -713,8 +735,10 @@ ICE3_HD double ldp(const double *p, long i)
 // sub-stepping, total tendencies and ICE4_CORRECT_NEGATIVITIES on the
 // sources, written back in place.  Returns the pass key (0 for points
 // outside LLMICRO or capped); `capped` reports a point that hit max_passes.
+template <bool SUR = false>
 ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
-                                    const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped)
+                                    const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped,
+                                    const double *sur = nullptr)
 {
   const double inv_dt = 1.0 / dt;
   const bool lwarm = c.LWARM != 0.0;
@@ -768,7 +792,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
       hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
     }
     double rrevav;
-    key = stepping(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped);
+    key = stepping<SUR>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur);
 #pragma unroll
     for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;

@@ -39,9 +39,17 @@ struct Mlp {
   std::vector<float *> Z;             // [n_layers] [cap][n_hid]
   float *y = nullptr, *dyf = nullptr, *dzf = nullptr, *part = nullptr;
   long part_cap = 0;
+  // inference buffers for INFER_CHUNK rows (no activations kept)
+  __nv_bfloat16 *xi = nullptr, *hi[2] = {nullptr, nullptr};
+  // packed BF16 weights of the fused inference kernel, valid for version pk_version
+  __nv_bfloat16 *wpk = nullptr;
+  long version = 0, pk_version = -1;
+  int num_sms = 0;
   int step = 0;
   std::mutex mu;
 };
+
+constexpr long INFER_CHUNK = 1L << 21;
 
 Mlp *as_mlp(void *p)
 {
@@ -82,6 +90,24 @@ cudaError_t ensure_acts(Mlp *m, long n)
   return e;
 }
 
+cudaError_t ensure_infer(Mlp *m)
+{
+  if (m->xi) return cudaSuccess;
+  cudaError_t e = cudaMalloc(&m->xi, sizeof(__nv_bfloat16) * INFER_CHUNK * m->n_in);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMalloc(&m->hi[i], sizeof(__nv_bfloat16) * INFER_CHUNK * m->n_hid);
+  if (e != cudaSuccess) {
+    cudaFree(m->xi); cudaFree(m->hi[0]); cudaFree(m->hi[1]);
+    m->xi = m->hi[0] = m->hi[1] = nullptr;
+  }
+  return e;
+}
+
+void free_infer(Mlp *m)
+{
+  cudaFree(m->xi); cudaFree(m->hi[0]); cudaFree(m->hi[1]);
+  m->xi = m->hi[0] = m->hi[1] = nullptr;
+}
+
 TcGemmArgs gemm(const __nv_bfloat16 *A, long sam, long sak, const __nv_bfloat16 *B, long sbn, long sbk, int M, int N,
                 int K, int epi, int *err)
 {
@@ -115,6 +141,63 @@ cudaError_t mlp_forward_dev(Mlp *m, int n, float *y_out, long ldy, cudaStream_t 
     e = launch_tc_gemm(a, s);
   }
   return e;
+}
+
+bool fused_shape(const Mlp *m) { return m->n_in == 16 && m->n_hid == 256 && m->n_layers == 3 && m->n_out <= 16; }
+
+// Forward through the fused kernel (surrogate shape): packs the weights when
+// they changed since the last pack.
+cudaError_t mlp_infer_fused(Mlp *m, long n, const float *x, float *y, cudaStream_t s)
+{
+  cudaError_t e = cudaSuccess;
+  if (!m->wpk) e = cudaMalloc(&m->wpk, sizeof(__nv_bfloat16) * MLP_PACKED_ELEMS);
+  if (e == cudaSuccess && m->pk_version != m->version) {
+    e = launch_mlp_pack(m->p, m->woff[0], m->woff[1], m->woff[2], m->woff[3], m->n_out, m->wpk, s);
+    if (e == cudaSuccess) m->pk_version = m->version;
+  }
+  if (e != cudaSuccess) return e;
+  MlpFusedArgs a;
+  a.x = x; a.y = y; a.n = n; a.n_out = m->n_out;
+  a.w1 = m->wpk; a.w2 = m->wpk + 4096; a.w3 = m->wpk + 4096 + 65536; a.w4 = m->wpk + 4096 + 131072;
+  a.b1 = m->p + m->boff[0]; a.b2 = m->p + m->boff[1]; a.b3 = m->p + m->boff[2]; a.b4 = m->p + m->boff[3];
+  a.err = m->err;
+  return launch_mlp_fused(a, m->num_sms, s);
+}
+
+// Forward of n rows of x (f32 [n][n_in]) into y (f32 [n][n_out]) with one
+// GEMM launch per layer, chunk by chunk through ping-pong BF16 activation
+// buffers (any shape; the training path's forward).
+cudaError_t mlp_infer_layered(Mlp *m, long n, const float *x, float *y, cudaStream_t s)
+{
+  cudaError_t e = ensure_infer(m);
+  for (long r0 = 0; r0 < n && e == cudaSuccess; r0 += INFER_CHUNK) {
+    const int rows = (int)(n - r0 < INFER_CHUNK ? n - r0 : INFER_CHUNK);
+    e = launch_to_bf16(x + r0 * m->n_in, m->xi, (long)rows * m->n_in, s);
+    const __nv_bfloat16 *in = m->xi;
+    long ldin = m->n_in;
+    for (int l = 0; l < m->n_layers && e == cudaSuccess; ++l) {
+      TcGemmArgs a = gemm(in, ldin, 1, m->w16[l], m->din[l], 1, rows, m->dout[l], m->din[l], EPI_BIAS_GELU, m->err);
+      a.bias = m->p + m->boff[l];
+      a.H = m->hi[l & 1]; a.ldh = m->n_hid;
+      e = launch_tc_gemm(a, s);
+      in = m->hi[l & 1];
+      ldin = m->n_hid;
+    }
+    if (e == cudaSuccess) {
+      const int L = m->nl - 1;
+      TcGemmArgs a = gemm(in, ldin, 1, m->w16[L], m->din[L], 1, rows, m->dout[L], m->din[L], EPI_BIAS, m->err);
+      a.bias = m->p + m->boff[L];
+      a.C = y + r0 * m->n_out; a.ldc = m->n_out;
+      e = launch_tc_gemm(a, s);
+    }
+  }
+  return e;
+}
+
+cudaError_t mlp_infer_dev(Mlp *m, long n, const float *x, float *y, cudaStream_t s)
+{
+  if ((((uintptr_t)x) & 15) == 0 && fused_shape(m)) return mlp_infer_fused(m, n, x, y, s);
+  return mlp_infer_layered(m, n, x, y, s);
 }
 
 int split_for(int n) { int sp = n / 512; return sp < 1 ? 1 : (sp > 32 ? 32 : sp); }
@@ -183,6 +266,31 @@ cudaError_t mlp_loss_grad(Mlp *m, int n, const float *x, const float *tgt, cudaS
 
 }  // namespace
 
+cudaError_t mlp_infer(void *mlp, long n, const float *x, float *y, cudaStream_t s)
+{
+  Mlp *m = as_mlp(mlp);
+  if (!m || n < 0) return cudaErrorInvalidValue;
+  std::lock_guard<std::mutex> lock(m->mu);
+  return mlp_infer_dev(m, n, x, y, s);
+}
+
+bool mlp_dims(void *mlp, int *n_in, int *n_out)
+{
+  Mlp *m = as_mlp(mlp);
+  if (!m) return false;
+  *n_in = m->n_in;
+  *n_out = m->n_out;
+  return true;
+}
+
+int mlp_device_error(void *mlp)
+{
+  Mlp *m = as_mlp(mlp);
+  int err = 0;
+  if (!m || cudaMemcpy(&err, m->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+  return err != 0;
+}
+
 extern "C" {
 
 int ice3gb_mlp_create(const Ice3gbMlpShape *shape, uint64_t seed, void **out)
@@ -208,6 +316,10 @@ int ice3gb_mlp_create(const Ice3gbMlpShape *shape, uint64_t seed, void **out)
     off += dout;
   }
   m->nparam = off;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || m->num_sms < 1)
+    m->num_sms = 1;
   // He-normal hidden weights, scaled-down output weights, zero biases
   std::vector<float> host(off, 0.0f);
   std::mt19937_64 rng(seed);
@@ -248,6 +360,8 @@ int ice3gb_mlp_destroy(void *mlp)
   Mlp *m = as_mlp(mlp);
   if (!m) return ICE3GB_ERR_HANDLE;
   free_acts(m);
+  free_infer(m);
+  cudaFree(m->wpk);
   cudaFree(m->p); cudaFree(m->g); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->err); cudaFree(m->loss);
   cudaFree(m->part);
   for (auto *w : m->w16) cudaFree(w);
@@ -282,6 +396,7 @@ int ice3gb_mlp_set_params(void *mlp, const float *host)
   if (e == cudaSuccess) e = cudaMemset(m->m1, 0, sizeof(float) * m->nparam);
   if (e == cudaSuccess) e = cudaMemset(m->m2, 0, sizeof(float) * m->nparam);
   m->step = 0;
+  m->version += 1;
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e == cudaSuccess ? ICE3GB_OK : ICE3GB_ERR_CUDA;
 }
@@ -293,11 +408,18 @@ int ice3gb_mlp_forward(void *mlp, int n, const float *x, float *y, void *stream)
   if (!x || !y) return ICE3GB_ERR_NULL;
   if (n < 1) return ICE3GB_ERR_SHAPE;
   std::lock_guard<std::mutex> lock(m->mu);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = ensure_acts(m, n);
-  if (e == cudaSuccess) e = launch_to_bf16(x, m->xb, (long)n * m->n_in, s);
-  if (e == cudaSuccess) e = mlp_forward_dev(m, n, y, m->n_out, s);
-  return e == cudaSuccess ? ICE3GB_OK : ICE3GB_ERR_CUDA;
+  return mlp_infer_dev(m, n, x, y, static_cast<cudaStream_t>(stream)) == cudaSuccess ? ICE3GB_OK : ICE3GB_ERR_CUDA;
+}
+
+int ice3gb_mlp_forward_layered(void *mlp, int n, const float *x, float *y, void *stream)
+{
+  Mlp *m = as_mlp(mlp);
+  if (!m) return ICE3GB_ERR_HANDLE;
+  if (!x || !y) return ICE3GB_ERR_NULL;
+  if (n < 1) return ICE3GB_ERR_SHAPE;
+  std::lock_guard<std::mutex> lock(m->mu);
+  return mlp_infer_layered(m, n, x, y, static_cast<cudaStream_t>(stream)) == cudaSuccess ? ICE3GB_OK
+                                                                                           : ICE3GB_ERR_CUDA;
 }
 
 int ice3gb_mlp_loss_grad(void *mlp, int n, const float *x, const float *tgt, float *grad, float *loss, void *stream)
@@ -324,6 +446,7 @@ int ice3gb_mlp_train_step(void *mlp, int n, const float *x, const float *tgt, fl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = mlp_loss_grad(m, n, x, tgt, s);
   m->step += 1;
+  m->version += 1;
   for (int l = 0; l < m->nl && e == cudaSuccess; ++l) {
     const long nw = (long)m->din[l] * m->dout[l];
     e = launch_adam(m->p + m->woff[l], m->g + m->woff[l], m->m1 + m->woff[l], m->m2 + m->woff[l], m->w16[l], nw, lr,

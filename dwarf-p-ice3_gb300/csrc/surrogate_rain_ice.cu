@@ -1,0 +1,191 @@
+// surrogate_rain_ice.cu — the learned surrogate of the ICE4_SLOW rates in
+// the rain_ice step.
+//
+// surrogate_sample_kernel: per grid point, the 16 features of a micro point
+//   at its first hard pass (and, for training, the plain kernel's slow rates
+//   as targets); with a normalisation it standardises the features and
+//   checks them against the training envelope.  Accepted points get a row of
+//   a compacted [rows][16] matrix (warp-aggregated atomics; a point's row
+//   number does not change its result), the others row -1.
+// rain_ice_surrogate_kernel: the rain_ice point loop of rain_ice.cu where a
+//   point with a row takes its first hard pass's slow rates from the
+//   network's output row, then passes a fix-up check (finite sources,
+//   non-negative hydrometeor sources, vapour not driven below its input or
+//   zero, total water conserved to 1e-12 of the water sources); a point that
+//   fails it is recomputed by the plain path in the same launch, as are
+//   points without a row.
+#include "ice3gb_device.cuh"
+#include "ice3gb_kernels.h"
+#include "surrogate_point.cuh"
+
+#ifndef RI_BLOCKS_PER_SM
+#define RI_BLOCKS_PER_SM 2
+#endif
+
+namespace {
+using namespace ice3pt;
+using namespace ice3sur;
+
+constexpr int SAMPLE_THREADS = 256;
+
+__device__ __forceinline__ void warp_add(unsigned long long *ctr, bool pred)
+{
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(ctr, (unsigned long long)__popc(m));
+}
+
+__global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const __grid_constant__ Cst c,
+                                                                          const __grid_constant__ SurSampleArgs a)
+{
+  extern __shared__ double lut[];
+  __shared__ Derived dsh;
+  for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
+  if (threadIdx.x == 0) make_derived(c, dsh);
+  __syncthreads();
+  const long n = (long)a.nij * a.nk;
+  const unsigned lane = threadIdx.x & 31u;
+  // uniform trip count: whole warps reach the ballots
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long p0 = (long)blockIdx.x * blockDim.x; p0 < n; p0 += stride) {
+    const long p = p0 + threadIdx.x;
+    double x[NFEAT], r[NRATE];
+    bool micro = false, ok = false;
+    if (p < n) micro = sample_point(c, dsh, lut, a.f, p, a.dt, x, r);
+    float xf[NFEAT];
+    if (micro) {
+      ok = true;
+#pragma unroll
+      for (int j = 0; j < NFEAT; ++j) {
+        float v = (float)x[j];
+        if (a.norm_on) {
+          v = (v - a.norm.mean[j]) * a.norm.inv_std[j];
+          ok = ok && v >= a.norm.lo[j] && v <= a.norm.hi[j];   // false for NaN
+        }
+        xf[j] = v;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(a.count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const long row = ok ? (long)(base + __popc(m & ((1u << lane) - 1u))) : -1;
+    const bool kept = ok && row < a.cap;
+    if (kept) {
+      float4 *fr = reinterpret_cast<float4 *>(a.feat + row * ROW);
+#pragma unroll
+      for (int j = 0; j < NFEAT; j += 4) fr[j / 4] = make_float4(xf[j], xf[j + 1], xf[j + 2], xf[j + 3]);
+      if (a.targets) {
+        float t[ROW];
+        encode_targets(r, t);
+        float4 *tr = reinterpret_cast<float4 *>(a.targets + row * ROW);
+#pragma unroll
+        for (int j = 0; j < ROW; j += 4) tr[j / 4] = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
+      }
+      if (a.point_of_row) a.point_of_row[row] = (long long)p;
+    }
+    if (p < n && a.row_of_point) a.row_of_point[p] = kept ? (int)row : -1;
+    warp_add(a.stats + 0, micro);
+    warp_add(a.stats + 1, micro && !ok);
+    warp_add(a.stats + 2, ok && !kept);
+  }
+}
+
+__device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int key)
+{
+  const unsigned int m = __reduce_max_sync(0xffffffffu, key);
+  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(key_max, m);
+}
+
+__device__ __forceinline__ bool finite_(double x) { return (fm::bits_(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL; }
+
+__global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM)
+    rain_ice_surrogate_kernel(const __grid_constant__ Cst c, const __grid_constant__ SurRainIceArgs sa)
+{
+  extern __shared__ double lut[];
+  __shared__ Derived dsh;
+  const RainIceArgs &a = sa.ri;
+  for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
+  if (threadIdx.x == 0) make_derived(c, dsh);
+  __shared__ unsigned int chunk;
+  __syncthreads();
+  const Ice3gbRainIceFields &f = a.f;
+  const long n = (long)a.nij * a.nk;
+  const double dt = a.dt;
+  bool any_capped = false;
+  for (;;) {
+    if (threadIdx.x == 0) chunk = atomicAdd(a.scr.chunk_counter, 1u);
+    __syncthreads();
+    const long base = (long)chunk * blockDim.x;
+    __syncthreads();
+    if (base >= n) break;
+    const long slot = base + threadIdx.x;
+    unsigned int key = 0u;
+    bool used = false, fell_back = false;
+    if (slot < n) {
+      const long p = a.order ? (long)__ldg(a.order + slot) : slot;
+      const int row = __ldg(sa.row_of_point + p);
+      double sur[NRATE];
+      const double *use = nullptr;
+      if (row >= 0) {
+        decode_rates(sa.y + (long)row * sa.ldy, sur);
+        use = sur;
+      }
+      const double in[8] = {f.ths[p], f.rvs[p], f.rcs[p], f.rrs[p], f.ris[p], f.rss[p], f.rgs[p], f.cit[p]};
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        bool capped;
+        key = rain_ice_point<true>(c, dsh, lut, f, p, dt, a.max_passes, capped, use);
+        if (!use) { any_capped |= capped; break; }
+        // fix-up check of the surrogate-assisted point
+        const double o_th = f.ths[p], o_v = f.rvs[p], o_c = f.rcs[p], o_r = f.rrs[p], o_i = f.ris[p];
+        const double o_s = f.rss[p], o_g = f.rgs[p];
+        const double w_in = in[1] + in[2] + in[3] + in[4] + in[5] + in[6];
+        const double w_out = o_v + o_c + o_r + o_i + o_s + o_g;
+        const double w_abs = fabs(in[1]) + fabs(in[2]) + fabs(in[3]) + fabs(in[4]) + fabs(in[5]) + fabs(in[6]);
+        const bool ok = finite_(o_th) && finite_(w_out) && !negd(o_c) && !negd(o_r) && !negd(o_i) && !negd(o_s) &&
+                        !negd(o_g) && (!negd(o_v) || o_v >= in[1]) && fabs(w_out - w_in) <= 1e-12 * w_abs;
+        if (ok) { used = true; any_capped |= capped; break; }
+        // restore the in-out fields and take the plain path
+        f.ths[p] = in[0]; f.rvs[p] = in[1]; f.rcs[p] = in[2]; f.rrs[p] = in[3]; f.ris[p] = in[4];
+        f.rss[p] = in[5]; f.rgs[p] = in[6]; f.cit[p] = in[7];
+        use = nullptr;
+        fell_back = true;
+      }
+      a.scr.keys[p] = key;
+    }
+    warp_key_max(a.scr.key_max, key);
+    warp_add(sa.stats + 3, used);
+    warp_add(sa.stats + 4, fell_back);
+  }
+  if (any_capped) atomicOr(a.scr.status, ICE3GB_DEV_PASS_CAP);
+}
+
+size_t lut_smem_bytes() { return sizeof(double) * LUT_N; }
+
+}  // namespace
+
+cudaError_t launch_surrogate_sample(const Cst &c, const SurSampleArgs &a, int num_sms, cudaStream_t s)
+{
+  cudaError_t e = cudaFuncSetAttribute(surrogate_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)lut_smem_bytes());
+  if (e != cudaSuccess) return e;
+  const long n = (long)a.nij * a.nk;
+  long blocks = (n + SAMPLE_THREADS - 1) / SAMPLE_THREADS;
+  if (blocks > (long)num_sms * 2) blocks = (long)num_sms * 2;
+  if (blocks < 1) blocks = 1;
+  surrogate_sample_kernel<<<(unsigned)blocks, SAMPLE_THREADS, lut_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rain_ice_surrogate(const Cst &c, const SurRainIceArgs &a, int num_sms, cudaStream_t s)
+{
+  cudaError_t e = cudaFuncSetAttribute(rain_ice_surrogate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)lut_smem_bytes());
+  if (e != cudaSuccess) return e;
+  const long n = (long)a.ri.nij * a.ri.nk;
+  long chunks = (n + RI_THREADS - 1) / RI_THREADS;
+  long blocks = (long)num_sms * RI_BLOCKS_PER_SM;
+  if (blocks > chunks) blocks = chunks;
+  if (blocks < 1) blocks = 1;
+  rain_ice_surrogate_kernel<<<(unsigned)blocks, RI_THREADS, lut_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}

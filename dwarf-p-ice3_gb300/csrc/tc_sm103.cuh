@@ -77,6 +77,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long m
   return done != 0;
 }
 
+// mbarrier arrival that also expects `bytes` of asynchronous copies.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk (non-tensor) asynchronous copy global -> shared of `bytes` (multiple
+// of 16, both addresses 16-byte aligned), completing on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
 // 16 consecutive FP32 columns of one TMEM lane per thread: warp w (of the
 // 4 warps of the CTA) reads lanes 32w .. 32w + 31.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])

@@ -98,6 +98,16 @@ class MlpShape(ctypes.Structure):
                 ("n_hidden_layers", ctypes.c_int32), ("n_out", ctypes.c_int32)]
 
 
+class SurrogateNorm(ctypes.Structure):
+    _fields_ = [("mean", ctypes.c_float * 16), ("inv_std", ctypes.c_float * 16), ("lo", ctypes.c_float * 16),
+                ("hi", ctypes.c_float * 16)]
+
+
+# counters of the surrogate calls (ICE3GB_SUR_*)
+SUR_STATS = ("micro", "outside_envelope", "over_capacity", "used", "fixup_fallback")
+SUR_NSTATS = 8
+
+
 class RainIceOptions(ctypes.Structure):
     _fields_ = [("lsedim_after", ctypes.c_int32), ("ldeposc", ctypes.c_int32),
                 ("lfeedbackt", ctypes.c_int32), ("max_passes", ctypes.c_int32),
@@ -111,12 +121,14 @@ EXPORTED = (
     "ice3gb_physics_step", "ice3gb_physics_step_host", "ice3gb_profile_enable", "ice3gb_profile_read",
     "ice3gb_kernel_name", "ice3gb_rain_ice_noalloc", "ice3gb_ice_adjust_vjp",
     "ice3gb_sedimentation_vjp", "ice3gb_mlp_create", "ice3gb_mlp_destroy", "ice3gb_mlp_param_count",
-    "ice3gb_mlp_get_params", "ice3gb_mlp_set_params", "ice3gb_mlp_forward", "ice3gb_mlp_loss_grad",
-    "ice3gb_mlp_train_step", "ice3gb_mlp_error", "ice3gb_tc_gemm_bf16",
+    "ice3gb_mlp_get_params", "ice3gb_mlp_set_params", "ice3gb_mlp_forward", "ice3gb_mlp_forward_layered",
+    "ice3gb_mlp_loss_grad",
+    "ice3gb_mlp_train_step", "ice3gb_mlp_error", "ice3gb_tc_gemm_bf16", "ice3gb_surrogate_sample",
+    "ice3gb_rain_ice_surrogate", "ice3gb_physics_step_surrogate",
 )
 NOALLOC_MAX_POINTS = 4194304
 KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order",
-                "ice_adjust_vjp", "sedimentation_vjp")
+                "ice_adjust_vjp", "sedimentation_vjp", "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate")
 
 _lib: Optional[ctypes.CDLL] = None
 
@@ -175,14 +187,27 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ice3gb_mlp_get_params.argtypes = [P, F]
     lib.ice3gb_mlp_set_params.argtypes = [P, F]
     lib.ice3gb_mlp_forward.argtypes = [P, ctypes.c_int, P, P, P]
+    lib.ice3gb_mlp_forward_layered.argtypes = [P, ctypes.c_int, P, P, P]
     lib.ice3gb_mlp_loss_grad.argtypes = [P, ctypes.c_int, P, P, P, P, P]
     lib.ice3gb_mlp_train_step.argtypes = [P, ctypes.c_int, P, P, ctypes.c_float, P, P]
     lib.ice3gb_mlp_error.argtypes = [P]
     lib.ice3gb_tc_gemm_bf16.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, I64, I64, P, I64, I64, P, I64,
                                         P, P]
     for name in ("ice3gb_mlp_create", "ice3gb_mlp_destroy", "ice3gb_mlp_get_params", "ice3gb_mlp_set_params",
-                 "ice3gb_mlp_forward", "ice3gb_mlp_loss_grad", "ice3gb_mlp_train_step", "ice3gb_mlp_error",
+                 "ice3gb_mlp_forward", "ice3gb_mlp_forward_layered", "ice3gb_mlp_loss_grad", "ice3gb_mlp_train_step", "ice3gb_mlp_error",
                  "ice3gb_tc_gemm_bf16"):
+        getattr(lib, name).restype = ctypes.c_int
+    NP = ctypes.POINTER(SurrogateNorm)
+    U64P = ctypes.POINTER(ctypes.c_uint64)
+    lib.ice3gb_surrogate_sample.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                            ctypes.POINTER(RainIceFields), NP, I64, P, P, P, P, P, P]
+    lib.ice3gb_rain_ice_surrogate.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                              ctypes.POINTER(RainIceOptions), ctypes.POINTER(RainIceFields), NP,
+                                              U64P, P]
+    lib.ice3gb_physics_step_surrogate.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.POINTER(RainIceOptions), ctypes.POINTER(StepFields), NP,
+                                                  U64P, P]
+    for name in ("ice3gb_surrogate_sample", "ice3gb_rain_ice_surrogate", "ice3gb_physics_step_surrogate"):
         getattr(lib, name).restype = ctypes.c_int
     lib.ice3gb_kernel_name.argtypes = [ctypes.c_int]
     lib.ice3gb_kernel_name.restype = ctypes.c_char_p

@@ -204,11 +204,10 @@ class RainIce:
             return t.reshape(z, g, p).permute(1, 2, 0).contiguous()
         return t
 
-    def __call__(self, state: Mapping[str, Any], dt: float, lsedim_after: bool = False, ldeposc: bool = False,
-                 ldsoft: bool = False, lfeedbackt: bool = True, max_iterations: Optional[int] = None,
-                 with_fluxes: bool = False):
-        # ldsoft is accepted for signature compatibility: the soft/hard passes are
-        # decided inside the ICE4 sub-stepping as in PHYEX.
+    def prepare(self, state: Mapping[str, Any], with_fluxes: bool = False) -> Dict[str, Any]:
+        """The ABI field set of one call: {"f": RainIceFields, "fields": in/in-out
+        tensors (in-out ones cloned), "diag": outputs, "nij", "nk", "shape",
+        "host"}; the tensors must stay alive while the call runs."""
         ref = state["th_t"]
         host = isinstance(ref, np.ndarray)
         if host:
@@ -260,15 +259,39 @@ class RainIce:
         for k, v in diag.items():
             setattr(f, k, _ptr(v))
         f.sea, f.town = _ptr(sea), _ptr(town)
+        return {"f": f, "fields": fields, "diag": diag, "sea": sea, "town": town, "nij": nij, "nk": nk,
+                "shape": shape, "host": host}
+
+    def __call__(self, state: Mapping[str, Any], dt: float, lsedim_after: bool = False, ldeposc: bool = False,
+                 ldsoft: bool = False, lfeedbackt: bool = True, max_iterations: Optional[int] = None,
+                 with_fluxes: bool = False, surrogate: Any = None):
+        """``surrogate``: an ``ice3gb.surrogate.SlowSurrogate`` to take the
+        ICE4_SLOW rates from the learned network (CUDA tensors only); its
+        counters of the call go to ``self.surrogate_stats``."""
+        # ldsoft is accepted for signature compatibility: the soft/hard passes are
+        # decided inside the ICE4 sub-stepping as in PHYEX.
+        c = self.prepare(state, with_fluxes)
+        f, fields, diag, nij, nk, shape, host = (c["f"], c["fields"], c["diag"], c["nij"], c["nk"], c["shape"],
+                                                 c["host"])
         opt = _abi.RainIceOptions(int(bool(lsedim_after)), int(bool(ldeposc)), int(bool(lfeedbackt)),
                                   int(max_iterations or 0), self.sed_jax)
         h = self.handle
-        if host:
-            _abi.check(h.lib.ice3gb_rain_ice_host(h.h, nij, nk, float(dt), ctypes.byref(opt), ctypes.byref(f),
-                                                  ctypes.c_void_p(_stream_ptr())), h.h, "ice3gb_rain_ice_host")
+        sptr = ctypes.c_void_p(_stream_ptr())
+        if surrogate is not None:
+            if host:
+                raise ValueError("the surrogate-assisted rain_ice takes CUDA tensors")
+            stats = (ctypes.c_uint64 * _abi.SUR_NSTATS)()
+            norm = surrogate.norm_struct()
+            _abi.check(h.lib.ice3gb_rain_ice_surrogate(h.h, surrogate.mlp.h, nij, nk, float(dt), ctypes.byref(opt),
+                                                       ctypes.byref(f), ctypes.byref(norm), stats, sptr),
+                       h.h, "ice3gb_rain_ice_surrogate")
+            self.surrogate_stats = dict(zip(_abi.SUR_STATS, (int(v) for v in stats)))
+        elif host:
+            _abi.check(h.lib.ice3gb_rain_ice_host(h.h, nij, nk, float(dt), ctypes.byref(opt), ctypes.byref(f), sptr),
+                       h.h, "ice3gb_rain_ice_host")
         else:
-            _abi.check(h.lib.ice3gb_rain_ice(h.h, nij, nk, float(dt), ctypes.byref(opt), ctypes.byref(f),
-                                             ctypes.c_void_p(_stream_ptr())), h.h, "ice3gb_rain_ice")
+            _abi.check(h.lib.ice3gb_rain_ice(h.h, nij, nk, float(dt), ctypes.byref(opt), ctypes.byref(f), sptr),
+                       h.h, "ice3gb_rain_ice")
         out_state = dict(state)
         for key, abi in RI_STATE_INOUT.items():
             v = self._from_kij(fields[abi], shape)

@@ -97,6 +97,14 @@ class Mlp:
 
     __call__ = forward
 
+    def forward_layered(self, x: torch.Tensor) -> torch.Tensor:
+        """The same forward with one GEMM launch per layer (the training path)."""
+        x = self._check_x(x)
+        y = torch.empty((x.shape[0], self.shape[3]), dtype=torch.float32, device=x.device)
+        _abi.check(self.lib.ice3gb_mlp_forward_layered(self.h, int(x.shape[0]), _ptr(x), _ptr(y), _stream()), None,
+                   "ice3gb_mlp_forward_layered")
+        return y
+
     def loss_grad(self, x: torch.Tensor, targets: torch.Tensor) -> Tuple[float, torch.Tensor]:
         x = self._check_x(x)
         t = self._check_t(targets, x.shape[0])

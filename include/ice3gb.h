@@ -315,7 +315,13 @@ int     ice3gb_mlp_destroy(void *mlp);
 int64_t ice3gb_mlp_param_count(void *mlp);
 int     ice3gb_mlp_get_params(void *mlp, float *host);
 int     ice3gb_mlp_set_params(void *mlp, const float *host);
+/* Inference.  The surrogate's shape (16 -> 256 x 3 -> <= 16) with 16-byte
+ * aligned x runs one fused persistent kernel (weights streamed from L2,
+ * activations kept on chip); other shapes, and ice3gb_mlp_forward_layered
+ * always, run one tensor-core GEMM launch per layer (the training forward).
+ * Both give the same values bit for bit. */
 int     ice3gb_mlp_forward(void *mlp, int n, const float *x, float *y, void *stream);
+int     ice3gb_mlp_forward_layered(void *mlp, int n, const float *x, float *y, void *stream);
 /* Loss (binary cross-entropy of the activity logits + squared error of the
  * values where active, mean over the n rows) and its gradient (device
  * [param_count] or NULL) for one batch. */
@@ -330,6 +336,57 @@ int     ice3gb_mlp_error(void *mlp);
  * with BF16 A(m,k) = A[m*sam + k*sak], B(n,k) = B[n*sbn + k*sbk], N <= 256. */
 int     ice3gb_tc_gemm_bf16(int M, int N, int K, const void *A, int64_t sam, int64_t sak, const void *B, int64_t sbn,
                             int64_t sbk, float *C, int64_t ldc, int *err, void *stream);
+
+/* ---- learned surrogate of the ICE4_SLOW rates ----------------------------- */
+/* The MLP (16 features -> 10 outputs: per slow rate RCHONI, RVDEPS, RIAGGS,
+ * RIAUTS, RVDEPG a logit "nonzero" and asinh(rate / 1e-12) / 10) stands in
+ * for the five ICE4_SLOW rates (PHYEX mode_ice4_slow.F90, reached from the
+ * reference's rain_ice through src/ice3/jax/rain_ice.py:181) at the first
+ * hard pass of each micro point.  Features: T, ln p, ln rho, ln rv, ln rc,
+ * ln rr, ln ri, ln rs, ln rg, cloud fraction, Exner, dt, ln lbda of rain /
+ * snow / graupel, ssi, taken where the plain kernel evaluates the rates.
+ * Standardised as (x - mean) * inv_std; points whose standardised features
+ * leave [lo, hi] run the plain path.  No counterpart exists in the
+ * reference. */
+#define ICE3GB_SUR_NFEAT 16
+#define ICE3GB_SUR_NOUT 10
+typedef struct Ice3gbSurrogateNorm {
+  float mean[16], inv_std[16], lo[16], hi[16];
+} Ice3gbSurrogateNorm;
+/* counters of a surrogate call (uint64 each) */
+enum {
+  ICE3GB_SUR_MICRO = 0,           /* micro points of rain_ice */
+  ICE3GB_SUR_OUTSIDE = 1,         /* micro points outside the envelope (plain path) */
+  ICE3GB_SUR_OVER_CAP = 2,        /* accepted points beyond the row capacity (plain path) */
+  ICE3GB_SUR_USED = 3,            /* points that kept the learned slow rates */
+  ICE3GB_SUR_FIXUP_FALLBACK = 4,  /* points recomputed by the plain path after the fix-up check */
+  ICE3GB_SUR_NSTATS = 8
+};
+/* Features (and, if targets != NULL, the plain kernel's slow rates encoded
+ * as training targets: per rate k, column 2k = 1 if nonzero, 2k+1 = coded
+ * value, 10 + k = the rate) of the micro points of one rain_ice call,
+ * compacted to rows in an unspecified order: point_of_row / row_of_point
+ * (either may be NULL) map rows to grid points (-1: no row).  norm = NULL:
+ * raw features, no envelope.  counters: device uint64[1 + ICE3GB_SUR_NSTATS]
+ * = rows handed out, then the counters; zeroed by the call.  features and
+ * targets: 16-byte aligned device float [cap][16]; cap <= 2^31 - 1.  The
+ * fields are only read. */
+int ice3gb_surrogate_sample(void *handle, int nij, int nk, double dt, const Ice3gbRainIceFields *f,
+                            const Ice3gbSurrogateNorm *norm, int64_t cap, float *features, float *targets,
+                            int64_t *point_of_row, int32_t *row_of_point, uint64_t *counters, void *stream);
+/* ice3gb_rain_ice with the network's slow rates (mlp: ice3gb_mlp_create
+ * handle with n_in 16, n_out 10) where a point is inside the envelope and
+ * passes the fix-up check, the plain path elsewhere, in the same launch.
+ * stats: host uint64[ICE3GB_SUR_NSTATS] or NULL (NULL avoids the final
+ * synchronisation; the call synchronises once on the stream to size the
+ * network's batch). */
+int ice3gb_rain_ice_surrogate(void *handle, void *mlp, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
+                              const Ice3gbRainIceFields *f, const Ice3gbSurrogateNorm *norm, uint64_t *stats,
+                              void *stream);
+/* ice3gb_physics_step with the surrogate-assisted rain_ice. */
+int ice3gb_physics_step_surrogate(void *handle, void *mlp, int nij, int nk, double dt,
+                                  const Ice3gbRainIceOptions *opt, const Ice3gbStepFields *f,
+                                  const Ice3gbSurrogateNorm *norm, uint64_t *stats, void *stream);
 
 /* ---- allocation-free rain_ice ------------------------------------------- */
 /* Same computation and arguments as ice3gb_rain_ice, for callers that must
@@ -353,8 +410,10 @@ int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3
  * summed device time since the last enable.  Kernel ids: 0 ice_adjust,
  * 1 sedimentation, 2 rain_ice (pointwise sub-stepping), 3 rain_ice evap3d
  * fix-up, 4 fog deposition, 5 rain_ice point ordering (regime sort),
- * 6 ice_adjust adjoint, 7 sedimentation adjoint. */
-#define ICE3GB_NKERNELS 8
+ * 6 ice_adjust adjoint, 7 sedimentation adjoint, 8 surrogate feature
+ * sampling, 9 surrogate network (all its tensor-core launches of one call),
+ * 10 rain_ice with the learned slow rates. */
+#define ICE3GB_NKERNELS 11
 int         ice3gb_profile_enable(void *handle, int enable);
 int         ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms);
 const char *ice3gb_kernel_name(int kernel_id);

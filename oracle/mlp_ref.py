@@ -12,14 +12,13 @@ no counterpart in the reference; this file states what the kernels compute:
 
 with W in BF16 (the FP32 masters rounded to nearest even), the output
 cotangent dY and the hidden cotangents dZ rounded to BF16 before they enter
-a GEMM, and GELU the exact erf form.
+a GEMM, and GELU in its tanh form.
 """
 from __future__ import annotations
 
 from typing import Dict, List, Tuple
 
 import numpy as np
-from scipy.special import erf
 
 
 def bf16(x: np.ndarray) -> np.ndarray:
@@ -33,12 +32,19 @@ def bf16(x: np.ndarray) -> np.ndarray:
     return out
 
 
+_K0 = np.sqrt(2.0 / np.pi)
+_K1 = 0.044715 * _K0
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU, tanh form (Hendrycks & Gimpel 2016); the kernels evaluate the
+    tanh with the hardware approximation (relative error below 2^-10)."""
+    return 0.5 * z * (1.0 + np.tanh(z * (_K0 + _K1 * z * z)))
 
 
 def dgelu(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    th = np.tanh(z * (_K0 + _K1 * z * z))
+    return 0.5 * (1.0 + th) + 0.5 * z * (1.0 - th * th) * (_K0 + 3.0 * _K1 * z * z)
 
 
 def unpack(params: np.ndarray, layout: List[Tuple[int, int, int, int]]):

@@ -15,3 +15,23 @@ extern "C" int rain_ice_points_host(const Ice3gbConstants *c, const Ice3gbLuts *
   }
   return capped_any;
 }
+
+// Host build of the surrogate's feature / target sampling (surrogate_point.cuh):
+// per grid point the 16 features and the five plain slow rates of a micro
+// point at its first hard pass; micro[p] = 0 elsewhere.
+#include "../dwarf-p-ice3_gb300/csrc/surrogate_point.cuh"
+
+extern "C" long sur_sample_host(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk, double dt,
+                                const Ice3gbRainIceFields *f, double *feat, double *rate, unsigned char *micro)
+{
+  ice3pt::Derived d;
+  ice3pt::make_derived(*c, d);
+  long cnt = 0;
+  for (long p = 0; p < (long)nij * nk; ++p) {
+    const bool m = ice3sur::sample_point(*c, d, reinterpret_cast<const double *>(luts), *f, p, dt, feat + 16 * p,
+                                         rate + 5 * p);
+    micro[p] = m ? 1 : 0;
+    cnt += m;
+  }
+  return cnt;
+}

@@ -23,7 +23,7 @@ def lib():
 
 def declared_functions():
     text = open(os.path.join(REPO, "include", "ice3gb.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(ice3gb_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int64_t|int|const char \*)\s*(ice3gb_\w+)\(", text, re.M)))
 
 
 def test_exports_every_declared_symbol(lib):

@@ -55,6 +55,25 @@ def test_mlp_forward_matches_oracle():
     assert np.all(rms <= 5e-3 * scale), (rms / scale)
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 5000, 152 * 128 + 77, 1 << 20])
+def test_fused_inference_equals_layered(n):
+    """The fused persistent inference kernel (weights streamed through the
+    bulk-copy ring, activations on chip) against one GEMM launch per layer:
+    same MMA order and epilogue arithmetic, so equal bit for bit."""
+    net, _, _ = _mlp_case(11, 1)
+    gen = torch.Generator(device="cuda").manual_seed(n)
+    x = torch.randn((n, 16), generator=gen, device="cuda")
+    a = net(x)
+    b = net.forward_layered(x)
+    net.check()
+    assert torch.equal(a, b), float((a - b).abs().max())
+    # after a parameter change the packed weights follow
+    p = net.get_params()
+    p *= 0.5
+    net.set_params(p)
+    assert torch.equal(net(x), net.forward_layered(x))
+
+
 @pytest.mark.parametrize("n", [1000, 4096, 20000])
 def test_mlp_gradients_match_oracle(n):
     """Hand-written backward pass (tcgen05 GEMMs with transposed staging,

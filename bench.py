@@ -295,11 +295,11 @@ def run_ours(args):
         # "<kernel> <DRAM bytes per point>" and "fp64_pipe_pct <kernel> <pct>" lines
         # summarised from an ncu capture of the same kernels
         for line in open(tpath):
-            f = line.split()
-            if len(f) == 2 and f[0] == dom_name:
-                traffic = float(f[1]) * n
-            elif len(f) == 3 and f[0] == "fp64_pipe_pct" and f[1] == dom_name:
-                fp64_pct = float(f[2])
+            w = line.split()
+            if len(w) == 2 and w[0] == dom_name:
+                traffic = float(w[1]) * n
+            elif len(w) == 3 and w[0] == "fp64_pipe_pct" and w[1] == dom_name:
+                fp64_pct = float(w[2])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": dom_name, "peak_source": f"hbm_gbs of {peak_kind}",
                 "algorithmic_bytes_per_launch": bytes_launch,
@@ -307,7 +307,12 @@ def run_ours(args):
                 "fp64_pipe_pct_ncu": fp64_pct,
                 "kernels": kstats}
 
-    # e2e through the host-buffer entry point
+    # surrogate-assisted step (the metric's second arm), then e2e through the
+    # host-buffer entry point
+    surrogate = None
+    if not args.no_surrogate:
+        surrogate = run_surrogate(args, lib, handle, st, f, work, pristine, outs, opt, nij, n, dev, stream, world,
+                                  dist, value)
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist)
@@ -322,7 +327,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (no flush)",
                    "timed_step": "restore 8 in-out fields (device copies) + ice3gb_physics_step"},
         "gpu_launches": launches_total, "device_status_bits": bits,
-        "roofline": roofline, "clocks": clocks.summary(), "e2e": e2e,
+        "roofline": roofline, "clocks": clocks.summary(), "e2e": e2e, "surrogate": surrogate,
     }
     if not args.no_cpu and rank == 0:
         cols = args.cpu_cols
@@ -340,6 +345,112 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+# forward FLOPs per point of the surrogate network 16 -> 256 x 3 -> 10
+MLP_FLOP_PER_ROW = 2 * (16 * 256 + 2 * 256 * 256 + 256 * 10)
+SUR_FIELDS = ("ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "t", "rv_out", "rc_out", "ri_out", "cldfr")
+
+
+def run_surrogate(args, lib, handle, st, f, work, pristine, outs, opt, nij, n, dev, stream, world, dist,
+                  plain_value):
+    """The chained step with the learned ICE4_SLOW rates
+    (ice3gb_physics_step_surrogate) on the same state: device time per step,
+    counters, the error per field against the plain FP64 step, per-tendency
+    RMSE of the network against the plain kernel's rates on a column sample,
+    and the tensor-core roofline of the network kernel."""
+    import torch
+
+    from ice3gb import _abi
+    from ice3gb.surrogate import DEFAULT_PATH, SlowSurrogate, physics_step_surrogate
+
+    if not os.path.exists(DEFAULT_PATH):
+        return {"unavailable": "no trained surrogate in the package"}
+    sur = SlowSurrogate.load(DEFAULT_PATH)
+
+    def restore():
+        for k in STEP_INOUT:
+            work[k].copy_(pristine[k], non_blocking=True)
+
+    def fields():
+        return {**work, **outs}
+
+    # one plain step and one surrogate step on identical inputs
+    restore()
+    _abi.check(lib.ice3gb_physics_step(handle.h, nij, NK, DT, ctypes.byref(opt), ctypes.byref(f),
+                                       ctypes.c_void_p(stream.cuda_stream)), handle.h, "ice3gb_physics_step")
+    plain = {k: fields()[k].clone() for k in SUR_FIELDS}
+    restore()
+    stats = physics_step_surrogate(handle, sur, f, nij, NK, DT, opt)
+    err = {}
+    for k in SUR_FIELDS:
+        ref = plain[k]
+        d = (fields()[k] - ref).double()
+        base = pristine[k] if k in pristine else None
+        scale = torch.sqrt(((ref - base) ** 2).mean()) if base is not None else torch.sqrt((ref ** 2).mean())
+        err[k] = {"rmse": float(torch.sqrt((d * d).mean())), "nrmse": float(torch.sqrt((d * d).mean()) / scale),
+                  "max_abs": float(d.abs().max())}
+    del plain
+    # timing (each call synchronises the stream twice: batch sizing, counters)
+    for _ in range(2):
+        restore()
+        physics_step_surrogate(handle, sur, f, nij, NK, DT, opt)
+    ksteps = max(2, min(args.steps, 4))
+    lib.ice3gb_profile_enable(handle.h, 1)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(ksteps):
+        restore()
+        physics_step_surrogate(handle, sur, f, nij, NK, DT, opt)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / ksteps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    kst = {}
+    for kid, name in enumerate(_abi.KERNEL_NAMES):
+        cnt, tot = ctypes.c_int(0), ctypes.c_double(0.0)
+        _abi.check(lib.ice3gb_profile_read(handle.h, kid, ctypes.byref(cnt), ctypes.byref(tot)), handle.h, "profile")
+        if cnt.value:
+            kst[name] = {"launches": cnt.value, "total_ms": tot.value, "avg_ms": tot.value / cnt.value}
+    lib.ice3gb_profile_enable(handle.h, 0)
+    rows = stats["used"] + stats["fixup_fallback"]
+    mlp = kst.get("surrogate_mlp")
+    bf16_peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            bf16_peak, peak_kind = float(json.load(fh)["bf16_tflops"]), "measured"
+    except Exception:
+        bf16_peak, peak_kind = 1900.0, "fallback"
+    mlp_roof = None
+    if mlp:
+        ach = rows * MLP_FLOP_PER_ROW / (mlp["avg_ms"] / 1e3) / 1e12
+        mlp_roof = {"bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s", "frac": ach / bf16_peak,
+                    "peak_source": f"bf16_tflops of {peak_kind}", "rows_per_launch": rows,
+                    "flop_per_row": MLP_FLOP_PER_ROW}
+    # per-tendency error of the network on a column sample (plain kernel's rates as truth)
+    tend = None
+    try:
+        from ice3gb.state import make_state
+        from ice3gb.surrogate import training_set
+        raw, tgt = training_set(1 << 20, nij=16384, seed=700000 + args.seed)
+        tend = sur.rate_errors(raw, tgt)
+    except Exception as e:  # noqa: BLE001
+        tend = {"error": repr(e)}
+    value = world * n / (ms / 1e3)
+    return {"metric": METRIC + ", surrogate-assisted (learned ICE4_SLOW rates)", "value": value,
+            "unit": "grid-points/s", "ms_per_step": ms, "steps": ksteps, "vs_plain": value / plain_value,
+            "counters": stats, "field_error_vs_plain_fp64": err, "tendency_error_vs_plain": tend,
+            "kernels": kst, "mlp_roofline": mlp_roof,
+            "network": "16 -> 256 x 3 (GELU) -> 10, BF16 weights/activations, FP32 accumulation (tcgen05), "
+                       "trained on 2^24 plain-kernel points",
+            "timed_step": "restore 8 in-out fields + ice3gb_physics_step_surrogate (features, network, "
+                          "rain_ice with learned slow rates and in-launch fallback, ice_adjust x2, sedimentation)"}
 
 
 def run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist):
@@ -404,6 +515,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)   # timing rule: at least 3 warm-up steps
     if args.impl == "reference":

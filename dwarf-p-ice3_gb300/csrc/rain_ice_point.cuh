@@ -261,9 +261,10 @@ ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const
 // ICE4_WARM and the rate parts of ICE4_FAST_RS/RG/RI.  The parts that depend
 // on the current freezing budget (riming/accretion split, wet/dry growth
 // choice) are left to aggregate(), which every pass runs.
+template <bool SUR = false>
 ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                         double t, const double v[NV], double cit, const double hl[4], const double hi[4],
-                        double criauti, Rates &R)
+                        double criauti, Rates &R, bool learned_slow = false)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
@@ -312,17 +313,21 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     heat_w = kt + (dl * (c.ESTT - ew) * irt);
   }
 
-  // ---- ICE4_SLOW (mode_ice4_slow.F90) ----
-  b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c)
-                    ? dmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3))
-                    : 0.0;
-  b[B_RVDEPS] = (has_v && has_s) ? ssi_rai * vent_s : 0.0;
-  b[B_RIAGGS] = (has_i && has_s)
-                    ? c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * s.llbdas) * v[IRI] * pf.rho_mcexvt
-                    : 0.0;
-  b[B_RIAUTS] = gtp(hi[2], c.I_RTMIN) ? c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * pmax0(hi[2] - criauti * hi[0])
-                                      : 0.0;
-  b[B_RVDEPG] = (has_v && has_g) ? ssi_rai * vent_g : 0.0;
+  // ---- ICE4_SLOW (mode_ice4_slow.F90); taken from the surrogate instead
+  // where it supplies them (slow_rates_from) ----
+  if (!(SUR && learned_slow)) {
+    b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c)
+                      ? dmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3))
+                      : 0.0;
+    b[B_RVDEPS] = (has_v && has_s) ? ssi_rai * vent_s : 0.0;
+    b[B_RIAGGS] = (has_i && has_s)
+                      ? c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * s.llbdas) * v[IRI] * pf.rho_mcexvt
+                      : 0.0;
+    b[B_RIAUTS] = gtp(hi[2], c.I_RTMIN)
+                      ? c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * pmax0(hi[2] - criauti * hi[0])
+                      : 0.0;
+    b[B_RVDEPG] = (has_v && has_g) ? ssi_rai * vent_g : 0.0;
+  }
 
   // ---- ICE4_WARM (mode_ice4_warm.F90), SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE ----
   if (c.LWARM != 0.0) {
@@ -576,6 +581,48 @@ ICE3_HD void slow_rates_from(const Cst &c, double t, const double v[NV], const d
   b[B_RVDEPG] = (has_v && has_g) ? sur[4] : 0.0;
 }
 
+// The state adjustments of a hard pass (mode_ice4_tendencies.F90:166-300):
+// nucleation (HENI), RRHONG and RIMLTC with their T-feedback limits; v and
+// t are updated in place, the increments go to b and B.
+ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, double lvfact, double lsfact,
+                         double &cit, double &t, double v[NV], double *b, double B[NV])
+{
+  nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
+  v[ITH] += b[B_RVHENI_MR] * lsfact;
+  t = v[ITH] * pf.exn;
+  v[IRV] -= b[B_RVHENI_MR];
+  v[IRI] += b[B_RVHENI_MR];
+  // RRHONG (mode_ice4_rrhong.F90)
+  double r = 0.0;
+  if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
+    r = v[IRR];
+    if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
+  }
+  b[B_RRHONG_MR] = r;
+  v[ITH] += r * (lsfact - lvfact);
+  t = v[ITH] * pf.exn;
+  v[IRR] -= r;
+  v[IRG] += r;
+  // RIMLTC (mode_ice4_rimltc.F90)
+  r = 0.0;
+  if (pos(v[IRI]) && gtp(t, c.TT)) {
+    r = v[IRI];
+    if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0((v[ITH] - c.TT / pf.exn) / (lsfact - lvfact)));
+  }
+  b[B_RIMLTC_MR] = r;
+  v[ITH] -= r * (lsfact - lvfact);
+  t = v[ITH] * pf.exn;
+  v[IRC] += r;
+  v[IRI] -= r;
+  const double lsv = lsfact - lvfact;
+  B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
+  B[IRV] = -b[B_RVHENI_MR];
+  B[IRC] = b[B_RIMLTC_MR];
+  B[IRR] = -b[B_RRHONG_MR];
+  B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
+  B[IRG] = b[B_RRHONG_MR];
+}
+
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
 // nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
 // and all rates are computed; a soft pass keeps the hard-pass rates.
@@ -591,40 +638,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   for (int k = 0; k < NV; ++k) { v[k] = vart[k]; B[k] = 0.0; }
   double *b = R.bu;
   if (!soft) {
-    nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
-    v[ITH] += b[B_RVHENI_MR] * lsfact;
-    t = v[ITH] * pf.exn;
-    v[IRV] -= b[B_RVHENI_MR];
-    v[IRI] += b[B_RVHENI_MR];
-    // RRHONG (mode_ice4_rrhong.F90)
-    double r = 0.0;
-    if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
-      r = v[IRR];
-      if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
-    }
-    b[B_RRHONG_MR] = r;
-    v[ITH] += r * (lsfact - lvfact);
-    t = v[ITH] * pf.exn;
-    v[IRR] -= r;
-    v[IRG] += r;
-    // RIMLTC (mode_ice4_rimltc.F90)
-    r = 0.0;
-    if (pos(v[IRI]) && gtp(t, c.TT)) {
-      r = v[IRI];
-      if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0((v[ITH] - c.TT / pf.exn) / (lsfact - lvfact)));
-    }
-    b[B_RIMLTC_MR] = r;
-    v[ITH] -= r * (lsfact - lvfact);
-    t = v[ITH] * pf.exn;
-    v[IRC] += r;
-    v[IRI] -= r;
-    const double lsv = lsfact - lvfact;
-    B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
-    B[IRV] = -b[B_RVHENI_MR];
-    B[IRC] = b[B_RIMLTC_MR];
-    B[IRR] = -b[B_RRHONG_MR];
-    B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
-    B[IRG] = b[B_RRHONG_MR];
+    hard_adjust(c, d, pf, lvfact, lsfact, cit, t, v, b, B);
   } else {
     b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = 0.0;
   }
@@ -637,7 +651,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   } else {
     rainfr = 1.;
   }
-  if (!soft) hard_rates(c, d, lut, pf, t, v, cit, hl, hi, criauti, R);
+  if (!soft) hard_rates<SUR>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr);
   else soft_rates(c, t, v, cit, hl, hi, R);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
   aggregate(c, t, v, lvfact, lsfact, R, A);

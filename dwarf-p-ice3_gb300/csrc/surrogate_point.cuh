@@ -4,13 +4,14 @@
 // point at its first hard pass, the target encoding, and the decoding of
 // the network's outputs.  Host-and-device code.
 //
-// Features (FP64, stored FP32; the network standardises them with the
-// training-set mean and spread):
+// Features (FP32; the network standardises them with the training-set mean
+// and spread):
 //   0 T   1 ln p   2 ln rho   3 ln max(rv, 1e-12)   4-8 ln max(r, 1e-14) for
 //   rc rr ri rs rg   9 cloud fraction   10 Exner   11 dt   12-14 ln lbda of
 //   rain, snow, graupel (0 where the species is absent)   15 ssi
-// all taken after the hard pass's nucleation / RRHONG / RIMLTC adjustments,
-// where the slow rates are evaluated.
+// from the state at the start of the step; the targets are the rates the
+// plain kernel evaluates at the first hard pass, after its nucleation /
+// RRHONG / RIMLTC adjustments (the network learns that map too).
 // Targets per rate k (columns of a 16-wide row): 2k = 1 if the rate is
 // nonzero, 2k+1 = asinh(rate / SUR_SCALE) / SUR_AMP; columns 10-14 carry
 // the rates themselves (FP32) for error statistics.
@@ -42,63 +43,88 @@ ICE3_HD void point_fix(const Cst &c, const Ice3gbRainIceFields &f, long p, Point
   pf.sigma_rc = sigm ? 2.0 * ldp(f.sigs, p) : 0.0;
 }
 
-// Features and plain slow rates of grid point p at its first hard pass;
-// false (nothing written) if p is not a micro point of rain_ice.
+// The 16 features of grid point p from its state at the start of the step,
+// in FP32 (they are stored and consumed in FP32): logarithms of the mixing
+// ratios, the slope parameters of rain / snow / graupel as
+// mode_ice4_tendencies.F90:389-433 forms them, and the supersaturation over
+// ice as :303-306 does.
+ICE3_HD void feature_row(const Cst &c, const Derived &d, const Ice3gbRainIceFields &f, long p, double dt,
+                         float feat[NFEAT])
+{
+  const float exn = (float)ldp(f.exn, p), pres = (float)ldp(f.pabs, p), rho = (float)ldp(f.rhodref, p);
+  const float t = (float)(ldp(f.tht, p) * ldp(f.exn, p));
+  const float rv = (float)ldp(f.rvt, p), rc = (float)ldp(f.rct, p), rr = (float)ldp(f.rrt, p);
+  const float ri = (float)ldp(f.rit, p), rs = (float)ldp(f.rst, p), rg = (float)ldp(f.rgt, p);
+  const float lrho = logf(rho);
+  feat[0] = t;
+  feat[1] = logf(pres);
+  feat[2] = lrho;
+  feat[3] = logf(fmaxf(rv, 1e-12f));
+  feat[4] = logf(fmaxf(rc, 1e-14f));
+  feat[5] = logf(fmaxf(rr, 1e-14f));
+  feat[6] = logf(fmaxf(ri, 1e-14f));
+  feat[7] = logf(fmaxf(rs, 1e-14f));
+  feat[8] = logf(fmaxf(rg, 1e-14f));
+  feat[9] = (float)ldp(f.cldfr, p);
+  feat[10] = exn;
+  feat[11] = (float)dt;
+  feat[12] = rr > 0.0f ? (float)d.lLBR + (float)c.LBEXR * (lrho + logf(fmaxf(rr, (float)c.R_RTMIN))) : 0.0f;
+  float ls = 0.0f;
+  if (rs > 0.0f) {
+    if (c.LSNOW_T != 0.0) {
+      const float e = t > 263.15f ? 14.554f - 0.0423f * t : 6.226f - 0.0106f * t;
+      const float lb = fmaxf(fminf((float)c.LBDAS_MAX, expf(2.302585093f * e)), (float)c.LBDAS_MIN);
+      ls = logf(lb * (float)c.TRANS_MP_GAMMAS);
+    } else {
+      ls = fminf((float)d.lLBDAS_MAX, (float)d.lLBS + (float)c.LBEXS * (lrho + logf(fmaxf(rs, (float)c.S_RTMIN))));
+    }
+  }
+  feat[13] = ls;
+  feat[14] = rg > 0.0f ? (float)d.lLBG + (float)c.LBEXG * (lrho + logf(fmaxf(rg, (float)c.G_RTMIN))) : 0.0f;
+  const float esi = expf((float)c.ALPI - (float)c.BETAI / t - (float)c.GAMI * logf(t));
+  feat[15] = rv * (pres - esi) / ((float)c.EPSILO * esi) - 1.0f;
+}
+
+// Features (and, with RATES, the plain FP64 slow rates of the first hard
+// pass) of grid point p; false (nothing written) if p is not a micro point
+// of rain_ice.
+template <bool RATES>
 ICE3_HD bool sample_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
-                          const Ice3gbRainIceFields &f, long p, double dt, double feat[NFEAT], double rate[NRATE])
+                          const Ice3gbRainIceFields &f, long p, double dt, float feat[NFEAT], double rate[NRATE])
 {
   const double th = ldp(f.tht, p), rv = ldp(f.rvt, p), rc = ldp(f.rct, p), rr = ldp(f.rrt, p);
   const double ri = ldp(f.rit, p), rs = ldp(f.rst, p), rg = ldp(f.rgt, p);
   const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
                      gtp(rg, c.G_RTMIN);
   if (!micro) return false;
-  PointFix pf;
-  point_fix(c, f, p, pf);
-  const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
-  double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
-  double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
-  if (adju) {
-    hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
-    hl[3] = rc - hl[2];
-    hi[3] = ri - hi[2];
-    hl[1] = pos(rc) ? pf.cf - hl[0] : 0.;
-    hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
+  feature_row(c, d, f, p, dt, feat);
+  if (RATES) {
+    PointFix pf;
+    point_fix(c, f, p, pf);
+    // first pass of ICE4_STEPPING (mode_ice4_stepping.F90:212-240)
+    const double zdev = (c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg)) * pf.exn;
+    const double zzt = th * pf.exn;
+    const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
+    const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
+    const double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
+    const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
+    double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
+    if (adju) {
+      hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
+      hl[3] = rc - hl[2];
+      hi[3] = ri - hi[2];
+      hl[1] = pos(rc) ? pf.cf - hl[0] : 0.;
+      hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
+    }
+    Rates R;
+    for (int k = 0; k < NBU; ++k) R.bu[k] = 0.0;
+    for (int k = 0; k < NRS; ++k) R.rs[k] = 0.0;
+    for (int k = 0; k < NRG; ++k) R.rg[k] = 0.0;
+    R.ssi = 0.0;
+    double cit = f.cit[p], rainfr = 1.0, A[NV], B[NV];
+    tendencies(c, d, lut, false, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
+    for (int k = 0; k < NRATE; ++k) rate[k] = R.bu[B_RCHONI + k];
   }
-  // first pass of ICE4_STEPPING (mode_ice4_stepping.F90:212-240)
-  const double zdev = (c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg)) * pf.exn;
-  const double zzt = th * pf.exn;
-  const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
-  const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
-  Rates R;
-  for (int k = 0; k < NBU; ++k) R.bu[k] = 0.0;
-  for (int k = 0; k < NRS; ++k) R.rs[k] = 0.0;
-  for (int k = 0; k < NRG; ++k) R.rg[k] = 0.0;
-  R.ssi = 0.0;
-  double cit = f.cit[p], rainfr = 1.0, A[NV], B[NV];
-  tendencies(c, d, lut, false, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B);
-  for (int k = 0; k < NRATE; ++k) rate[k] = R.bu[B_RCHONI + k];
-  // the state the rates saw: the hard pass's adjustments are B
-  double v[NV];
-  for (int k = 0; k < NV; ++k) v[k] = vart[k] + B[k];
-  const double t = v[ITH] * pf.exn;
-  Slopes s;
-  slopes(c, d, pf.lrho, t, v, s);
-  feat[0] = t;
-  feat[1] = fm::flog(pf.pres);
-  feat[2] = pf.lrho;
-  feat[3] = fm::flog(dmax(v[IRV], 1e-12));
-  feat[4] = fm::flog(dmax(v[IRC], 1e-14));
-  feat[5] = fm::flog(dmax(v[IRR], 1e-14));
-  feat[6] = fm::flog(dmax(v[IRI], 1e-14));
-  feat[7] = fm::flog(dmax(v[IRS], 1e-14));
-  feat[8] = fm::flog(dmax(v[IRG], 1e-14));
-  feat[9] = pf.cf;
-  feat[10] = pf.exn;
-  feat[11] = dt;
-  feat[12] = pos(v[IRR]) ? s.llbdar : 0.0;
-  feat[13] = pos(v[IRS]) ? s.llbdas : 0.0;
-  feat[14] = pos(v[IRG]) ? s.llbdag : 0.0;
-  feat[15] = R.ssi;
   return true;
 }
 

@@ -34,12 +34,16 @@ __device__ __forceinline__ void warp_add(unsigned long long *ctr, bool pred)
   if ((threadIdx.x & 31) == 0 && m) atomicAdd(ctr, (unsigned long long)__popc(m));
 }
 
+// RATES: also the plain slow rates (training targets), which need the
+// lookup tables in shared memory; without, only the features.
+template <bool RATES>
 __global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const __grid_constant__ Cst c,
                                                                           const __grid_constant__ SurSampleArgs a)
 {
   extern __shared__ double lut[];
   __shared__ Derived dsh;
-  for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
+  if (RATES)
+    for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
   if (threadIdx.x == 0) make_derived(c, dsh);
   __syncthreads();
   const long n = (long)a.nij * a.nk;
@@ -48,15 +52,16 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const 
   const long stride = (long)gridDim.x * blockDim.x;
   for (long p0 = (long)blockIdx.x * blockDim.x; p0 < n; p0 += stride) {
     const long p = p0 + threadIdx.x;
-    double x[NFEAT], r[NRATE];
+    float x[NFEAT];
+    double r[NRATE];
     bool micro = false, ok = false;
-    if (p < n) micro = sample_point(c, dsh, lut, a.f, p, a.dt, x, r);
+    if (p < n) micro = sample_point<RATES>(c, dsh, lut, a.f, p, a.dt, x, r);
     float xf[NFEAT];
     if (micro) {
       ok = true;
 #pragma unroll
       for (int j = 0; j < NFEAT; ++j) {
-        float v = (float)x[j];
+        float v = x[j];
         if (a.norm_on) {
           v = (v - a.norm.mean[j]) * a.norm.inv_std[j];
           ok = ok && v >= a.norm.lo[j] && v <= a.norm.hi[j];   // false for NaN
@@ -74,7 +79,7 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const 
       float4 *fr = reinterpret_cast<float4 *>(a.feat + row * ROW);
 #pragma unroll
       for (int j = 0; j < NFEAT; j += 4) fr[j / 4] = make_float4(xf[j], xf[j + 1], xf[j + 2], xf[j + 3]);
-      if (a.targets) {
+      if (RATES) {
         float t[ROW];
         encode_targets(r, t);
         float4 *tr = reinterpret_cast<float4 *>(a.targets + row * ROW);
@@ -165,14 +170,18 @@ size_t lut_smem_bytes() { return sizeof(double) * LUT_N; }
 
 cudaError_t launch_surrogate_sample(const Cst &c, const SurSampleArgs &a, int num_sms, cudaStream_t s)
 {
-  cudaError_t e = cudaFuncSetAttribute(surrogate_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const bool rates = a.targets != nullptr;
+  const size_t smem = rates ? lut_smem_bytes() : 0;
+  cudaError_t e = cudaFuncSetAttribute(surrogate_sample_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)lut_smem_bytes());
   if (e != cudaSuccess) return e;
   const long n = (long)a.nij * a.nk;
   long blocks = (n + SAMPLE_THREADS - 1) / SAMPLE_THREADS;
-  if (blocks > (long)num_sms * 2) blocks = (long)num_sms * 2;
+  const long cap = (long)num_sms * (rates ? 2 : 8);      // resident blocks per SM
+  if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  surrogate_sample_kernel<<<(unsigned)blocks, SAMPLE_THREADS, lut_smem_bytes(), s>>>(c, a);
+  if (rates) surrogate_sample_kernel<true><<<(unsigned)blocks, SAMPLE_THREADS, smem, s>>>(c, a);
+  else surrogate_sample_kernel<false><<<(unsigned)blocks, SAMPLE_THREADS, smem, s>>>(c, a);
   return cudaGetLastError();
 }
 

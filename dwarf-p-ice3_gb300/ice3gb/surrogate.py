@@ -9,8 +9,9 @@ micro point by a per-point MLP (16 features -> 3 x 256 GELU -> 10 outputs,
 BF16 weights, FP32 accumulation on the tcgen05 tensor cores; ice3gb.mlp).
 
 * Features and targets come from the plain kernel itself
-  (``ice3gb_surrogate_sample``): the state a micro point has at its first
-  hard pass and the five rates the plain FP64 code computes there.
+  (``ice3gb_surrogate_sample``): 16 FP32 features of a micro point's state
+  at the start of the step and the five rates the plain FP64 code computes
+  at its first hard pass.
 * Training runs on the GPU through the library's own forward and backward
   kernels (``Mlp.train_step``, Adam).
 * Inference (``RainIce(..., surrogate=...)``, ``physics_step_surrogate``)

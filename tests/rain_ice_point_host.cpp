@@ -22,13 +22,13 @@ extern "C" int rain_ice_points_host(const Ice3gbConstants *c, const Ice3gbLuts *
 #include "../dwarf-p-ice3_gb300/csrc/surrogate_point.cuh"
 
 extern "C" long sur_sample_host(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk, double dt,
-                                const Ice3gbRainIceFields *f, double *feat, double *rate, unsigned char *micro)
+                                const Ice3gbRainIceFields *f, float *feat, double *rate, unsigned char *micro)
 {
   ice3pt::Derived d;
   ice3pt::make_derived(*c, d);
   long cnt = 0;
   for (long p = 0; p < (long)nij * nk; ++p) {
-    const bool m = ice3sur::sample_point(*c, d, reinterpret_cast<const double *>(luts), *f, p, dt, feat + 16 * p,
+    const bool m = ice3sur::sample_point<true>(*c, d, reinterpret_cast<const double *>(luts), *f, p, dt, feat + 16 * p,
                                          rate + 5 * p);
     micro[p] = m ? 1 : 0;
     cnt += m;

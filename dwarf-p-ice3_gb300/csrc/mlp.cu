@@ -197,6 +197,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const TcGemmArgs a)
 // copies and the tcgen05.mma; all four warps run the epilogues (tcgen05.ld,
 // bias, GELU, BF16 pack into the activation tile).
 constexpr int FZ_NST = 3;                               // weight ring stages
+constexpr int FZ_THREADS = 512;                         // 16 warps: 4 row groups x 4 column quarters
 constexpr uint32_t FZ_CHUNK_BYTES = 256 * 64 * 2;       // one K-chunk of W2 / W3
 constexpr int FZ_OFF_H = 0, FZ_OFF_STAGE = 65536, FZ_OFF_W1 = FZ_OFF_STAGE + FZ_NST * 32768;
 constexpr int FZ_OFF_W4 = FZ_OFF_W1 + 8192, FZ_OFF_X = FZ_OFF_W4 + 8192, FZ_OFF_B = FZ_OFF_X + 4096;
@@ -208,23 +209,33 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// Bias + GELU of the 128 x 256 accumulator into the activation tile.
-__device__ __forceinline__ void fz_epilogue_gelu(uint32_t tmem, int warp, int row, const float *bias,
-                                                 __nv_bfloat16 *sH)
+// Bias + GELU of the 128 x 256 accumulator into the activation tile.  Warp
+// w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the 64 columns
+// 64 (w / 4) .. + 63, two 32-column loads in flight per wait.
+__device__ __forceinline__ void fz_epilogue_gelu(uint32_t tmem, int warp, const float *bias, __nv_bfloat16 *sH)
 {
-#pragma unroll 1
-  for (int c0 = 0; c0 < 256; c0 += 16) {
-    float v[16];
-    tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-    uint32_t w[8];
+  const int q = warp & 3, c0 = (warp >> 2) * 64;
+  const int row = 32 * q + (threadIdx.x & 31);
+  uint32_t r[2][32];
+  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, r[0]);
+  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 32), r[1]);
+  tc::tmem_wait_ld();
 #pragma unroll
-    for (int j = 0; j < 8; ++j) w[j] = pack_bf16x2(gelu(v[2 * j] + bias[c0 + 2 * j]), gelu(v[2 * j + 1] + bias[c0 + 2 * j + 1]));
-    *reinterpret_cast<uint4 *>(sH + tc::core_off(row, c0, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4 *>(sH + tc::core_off(row, c0 + 8, 256)) = make_uint4(w[4], w[5], w[6], w[7]);
+  for (int h = 0; h < 2; ++h) {
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int cb = c0 + 32 * h + 8 * g;
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        w[j] = pack_bf16x2(gelu(__uint_as_float(r[h][8 * g + 2 * j]) + bias[cb + 2 * j]),
+                           gelu(__uint_as_float(r[h][8 * g + 2 * j + 1]) + bias[cb + 2 * j + 1]));
+      *reinterpret_cast<uint4 *>(sH + tc::core_off(row, cb, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
   }
 }
 
-__global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
+__global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFusedArgs a)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
   __nv_bfloat16 *sH = reinterpret_cast<__nv_bfloat16 *>(smem + FZ_OFF_H);
@@ -239,11 +250,11 @@ __global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
   const long my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const long total_chunks = 8 * my_tiles;
   // resident operands: W1 (256 x 16), output layer (16 x 256), biases
-  for (int i = tid; i < 4096 / 8; i += 128) {
+  for (int i = tid; i < 4096 / 8; i += FZ_THREADS) {
     reinterpret_cast<uint4 *>(sW1)[i] = __ldg(reinterpret_cast<const uint4 *>(a.w1) + i);
     reinterpret_cast<uint4 *>(sW4)[i] = __ldg(reinterpret_cast<const uint4 *>(a.w4) + i);
   }
-  for (int i = tid; i < 256; i += 128) {
+  for (int i = tid; i < 256; i += FZ_THREADS) {
     sB[i] = a.b1[i];
     sB[256 + i] = a.b2[i];
     sB[512 + i] = a.b3[i];
@@ -284,8 +295,8 @@ __global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
   long tile = blockIdx.x;
   for (long it = 0; it < my_tiles; ++it, tile += gridDim.x) {
     const long r0 = tile * 128;
-    // ---- input rows -> BF16 tile
-    {
+    // ---- input rows -> BF16 tile (threads 0..127, one row each)
+    if (tid < 128) {
       const long row = r0 + tid;
       float x[16];
       if (row < a.n) {
@@ -318,7 +329,7 @@ __global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
     mma_phase ^= 1u;
     tc::fence_after();
     if (!ok) break;
-    fz_epilogue_gelu(tmem, warp, tid, sB, sH);
+    fz_epilogue_gelu(tmem, warp, sB, sH);
     // ---- layers 2 and 3: K = 256 in four chunks each
     for (int layer = 0; layer < 2 && ok; ++layer) {
       tc::fence_async_smem();
@@ -348,7 +359,7 @@ __global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
       mma_phase ^= 1u;
       tc::fence_after();
       if (!ok) break;
-      fz_epilogue_gelu(tmem, warp, tid, sB + 256 * (layer + 1), sH);
+      fz_epilogue_gelu(tmem, warp, sB + 256 * (layer + 1), sH);
     }
     if (!ok) break;
     // ---- output layer: N = 16, K = 256
@@ -367,7 +378,7 @@ __global__ void __launch_bounds__(128, 1) mlp_fused_kernel(const MlpFusedArgs a)
     mma_phase ^= 1u;
     tc::fence_after();
     if (!ok) break;
-    {
+    if (warp < 4) {                  // output columns 0..15: the first column quarter's warps
       float v[16];
       tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
       const long row = r0 + tid;
@@ -542,7 +553,7 @@ cudaError_t launch_mlp_fused(const MlpFusedArgs &a, int num_sms, cudaStream_t s)
   long blocks = num_sms;
   if (blocks > tiles) blocks = tiles;
   if (blocks < 1) return cudaSuccess;
-  mlp_fused_kernel<<<(unsigned)blocks, 128, FZ_SMEM, s>>>(a);
+  mlp_fused_kernel<<<(unsigned)blocks, FZ_THREADS, FZ_SMEM, s>>>(a);
   return cudaGetLastError();
 }
 

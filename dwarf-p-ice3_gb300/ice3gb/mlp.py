@@ -146,3 +146,39 @@ def tc_gemm_bf16(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     if int(err.item()) != 0:
         raise _abi.Ice3gbError("tc_gemm_bf16: tensor-core barrier timed out")
     return c
+
+
+def main(argv=None) -> int:
+    """Time the surrogate-shaped network's inference on random rows:
+    python -m ice3gb.mlp --rows 8388608 --reps 5 [--layered]"""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rows", type=int, default=1 << 23)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--layered", action="store_true", help="one GEMM launch per layer instead of the fused kernel")
+    a = ap.parse_args(argv)
+    net = Mlp(16, 256, 3, 10, seed=0)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((a.rows, 16), generator=gen, device="cuda")
+    fwd = net.forward_layered if a.layered else net.forward
+    fwd(x)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(a.reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fwd(x)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    net.check()
+    ms = min(times)
+    flop = a.rows * 2 * (16 * 256 + 2 * 256 * 256 + 256 * 10)
+    print(json.dumps({"rows": a.rows, "path": "layered" if a.layered else "fused", "ms_best": ms,
+                      "rows_per_s": a.rows / ms * 1e3, "tflops": flop / ms / 1e9}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

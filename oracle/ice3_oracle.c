@@ -1096,11 +1096,15 @@ done:
 /* RAIN_ICE (micro/rain_ice.F90)                                          */
 /* ===================================================================== */
 
+EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
+                              const double *rg);
+
 static int rain_ice_supported(const C *c)
 {
   if ((int)c->NRR != 6) return 0;
   if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0) return 0;
-  if ((int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0) return 0;  /* PRFR/CLFR paths: see below */
+  if ((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) return 0;  /* NONE, PRFR */
+  if ((int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2) return 0;          /* NONE, CLFR, PRFR */
   return 1;
 }
 
@@ -1140,6 +1144,34 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     }
   }
 
+  /* 4.2 precipitation fraction (rain_ice.F90:555-605): with a PRFR option,
+   * ICE4_COMPUTE_PDF on the time-t state of the LLMICRO points (its
+   * partition overwrites PHLC_HCF/HRC, PHLI_HCF/HRI), then ICE4_RAINFR_VERT
+   * down each column; the sub-stepping starts from that fraction. */
+  const int llrfr = (int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2;
+  if (llrfr) {
+    const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
+    const int adju = (int)c->SUBG_AUCV_RC == 2 || (int)c->SUBG_AUCV_RI == 2;
+#pragma omp parallel for schedule(static)
+    for (long p = 0; p < n; ++p) {
+      const double rc = f->rct[p], ri = f->rit[p], cf = f->cldfr[p];
+      const int micro = rc > c->C_RTMIN || f->rrt[p] > c->R_RTMIN || ri > c->I_RTMIN || f->rst[p] > c->S_RTMIN ||
+                        f->rgt[p] > c->G_RTMIN;
+      double hl[4] = {f->hlc_hcf[p], 0.0, f->hlc_hrc[p], 0.0}, hi[4] = {f->hli_hcf[p], 0.0, f->hli_hri[p], 0.0};
+      if (adju) {                                                     /* :564-581 */
+        hl[3] = rc - hl[2];
+        hi[3] = ri - hi[2];
+        hl[1] = rc > 0. ? cf - hl[0] : 0.;
+        hi[1] = ri > 0. ? cf - hi[0] : 0.;
+      }
+      const double sigma_rc = sigm ? f->sigs[p] * f->sigs[p] : 0.0;  /* :556-563 */
+      const double rf = ice4_compute_pdf(c, micro, f->rhodref[p], rc, ri, cf, f->tht[p] * f->exn[p], sigma_rc, hl, hi);
+      f->hlc_hcf[p] = hl[0]; f->hlc_hrc[p] = hl[2]; f->hli_hcf[p] = hi[0]; f->hli_hri[p] = hi[2];
+      f->rainfr[p] = rf;
+    }
+    ice3o_rainfr_vert(c, nij, nk, f->rainfr, f->rrt, f->rst, f->rgt);
+  }
+
   /* 1., 3., 4., 5. pointwise part */
 #pragma omp parallel for schedule(dynamic, 1024) reduction(| : capped_any)
   for (long p = 0; p < n; ++p) {
@@ -1155,7 +1187,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     /* :370-381 LLMICRO */
     const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN || rg > c->G_RTMIN;
     f->evap3d[p] = 0.0;
-    f->rainfr[p] = 1.0;  /* :599-605 (no PRFR option) */
+    if (!llrfr) f->rainfr[p] = 1.0;  /* :603-605 */
     double cit = f->cit[p];
     double zrvheni = 0.0;
     if (!micro) {
@@ -1175,7 +1207,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       s.extpk[ITH] = f->ths[p]; s.extpk[IRV] = f->rvs[p]; s.extpk[IRC] = f->rcs[p]; s.extpk[IRR] = f->rrs[p];
       s.extpk[IRI] = f->ris[p]; s.extpk[IRS] = f->rss[p]; s.extpk[IRG] = f->rgs[p];
       s.cit = cit;
-      s.rainfr = 1.0;
+      s.rainfr = llrfr ? f->rainfr[p] : 1.0;
       const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
       const double sigma_rc = sigm ? 2.0 * f->sigs[p] : 0.0;  /* pack :266 + stepping :160-166 */
       ice4_stepping_point(c, lut, dt, max_passes, exn, rho, pres, f->cldfr[p], sigma_rc,
@@ -1318,8 +1350,9 @@ EXPORT void ice3o_compute_pdf(const C *c, long n, const uint8_t *ldmicro, const 
 }
 
 /* Hard-pass rates of the slow/warm/fast processes for given inputs.
- * in: [17][n] = t rhodref pres rv rc rr ri rs rg cit ssi ka dv ai cj hlc_hcf hlc_hrc
- *     (+ hli_hcf hli_hri at rows 17, 18)
+ * in: [22][n] = t rhodref pres rv rc rr ri rs rg cit ssi ka dv ai cj hlc_hcf hlc_hrc
+ *     hli_hcf hli_hri cf rainfr tht (cf, rainfr, tht: the cloud fraction,
+ *     precipitation fraction and theta the CLFR/PRFR warm processes use)
  * out: [NBU][n] budget rates, plus rs_tend [8][n] and rg_tend [8][n]. */
 EXPORT int ice3o_process_rates(const C *c, const Ice3gbLuts *lut, long n, const double *in, const uint8_t *ldcompute,
                                double *out_bu, double *out_rs, double *out_rg)
@@ -1338,8 +1371,8 @@ EXPORT int ice3o_process_rates(const C *c, const Ice3gbLuts *lut, long n, const 
     pr.cj = in[14 * n + p];
     x.hl[0] = in[15 * n + p]; x.hl[2] = in[16 * n + p];
     x.hi[0] = in[17 * n + p]; x.hi[2] = in[18 * n + p];
-    x.cf = 1.0; x.rainfr = 1.0;
-    x.v[ITH] = x.t;  /* only used by the CLFR/PRFR evaporation, exn = 1 here */
+    x.cf = in[19 * n + p]; x.rainfr = in[20 * n + p];
+    x.v[ITH] = in[21 * n + p];  /* only used by the CLFR/PRFR evaporation */
     ice4_slopes(&x);
     ice4_slow(&x, &pr);
     ice4_warm(&x, &pr);

@@ -207,11 +207,16 @@ def compute_pdf(table, ldmicro, rhodref, rct, rit, cf, t, sigma_rc):
 
 def process_rates(table, inputs: Dict[str, np.ndarray], ldcompute):
     """Hard-pass process rates; inputs keys: t rhodref pres rv rc rr ri rs rg cit ssi ka dv ai cj
-    hlc_hcf hlc_hrc hli_hcf hli_hri."""
+    hlc_hcf hlc_hrc hli_hcf hli_hri, optional cf and rainfr (default 1) and
+    tht (default t), which the CLFR/PRFR warm processes use."""
     lib = load()
     keys = ("t", "rhodref", "pres", "rv", "rc", "rr", "ri", "rs", "rg", "cit", "ssi", "ka", "dv", "ai", "cj",
-            "hlc_hcf", "hlc_hrc", "hli_hcf", "hli_hri")
+            "hlc_hcf", "hlc_hrc", "hli_hcf", "hli_hri", "cf", "rainfr", "tht")
     n = np.asarray(inputs["t"]).size
+    inputs = dict(inputs)
+    inputs.setdefault("cf", np.ones(n))
+    inputs.setdefault("rainfr", np.ones(n))
+    inputs.setdefault("tht", inputs["t"])
     inp = np.ascontiguousarray(np.stack([_f64(inputs[k]).ravel() for k in keys]))
     ld = np.ascontiguousarray(np.asarray(ldcompute, dtype=np.uint8).ravel())
     bu, rs, rg = np.empty((len(NBU_NAMES), n)), np.empty((len(RS_NAMES), n)), np.empty((len(RG_NAMES), n))

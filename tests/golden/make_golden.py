@@ -8,6 +8,7 @@ through the numpy stand-in of refshim.py:
 * the ICE4 process stencils            (src/ice3/jax/stencils/ice4_*.py), hard pass
 * ``ice4_derived_fields`` / ``ice4_slope_parameters`` (stencils/ice4_tendencies.py:191,248)
 * ``ice4_rainfr_vert``                 (stencils/rain_ice.py:272)
+* ``ice4_warm`` with the CLFR / PRFR evaporation options (stencils/ice4_warm.py:15)
 
 Inputs are seeded synthetic states (ice3gb.state.make_state) and seeded
 random point sets; both inputs and reference outputs are stored.
@@ -191,9 +192,51 @@ def process_cases(mods, Phyex):
     return {"processes": rec}
 
 
+def warm_subg_case(mods, Phyex):
+    """ICE4_WARM with the subgrid evaporation options CLFR (1) and PRFR (2)
+    (src/ice3/jax/stencils/ice4_warm.py:15), hard pass, on seeded random
+    points; lbdar_rf is formed from the precipitation fraction as
+    mode_ice4_tendencies.F90 forms it (LBR (rho max(rr / rf, R_RTMIN))^LBEXR)."""
+    ext = dict(Phyex("AROME", TSTEP=DT).to_externals())
+    rng = np.random.default_rng(44)
+    n = 1024
+
+    def mix(lo=-8, hi=-2, pzero=0.3):
+        v = 10 ** rng.uniform(lo, hi, n)
+        return np.where(rng.random(n) < pzero, 0.0, v)
+
+    t = rng.uniform(250.0, 305.0, n)
+    pres = rng.uniform(3e4, 1.02e5, n)
+    rhodref = pres / (287.06 * t)
+    exn = (pres / 1e5) ** (287.06 / 1004.71)
+    tht = t / exn
+    rv = 10 ** rng.uniform(-5, -1.8, n)
+    rc, rr = mix(), mix(pzero=0.2)
+    ld = rng.random(n) < 0.9
+    cf = np.where(rng.random(n) < 0.3, 0.0, rng.uniform(0, 1, n))
+    rf = np.where(rng.random(n) < 0.2, 0.0, rng.uniform(0, 1, n))
+    hlc_hcf, hlc_hrc = rng.uniform(0, 1, n), mix(-7, -2, 0.3)
+    ssi, ka, dv, ai, cj = mods["tend"].ice4_derived_fields(t, rhodref, pres, rv, ext)
+    lbdar, _, _, _ = mods["tend"].ice4_slope_parameters(rhodref, t, rr, np.zeros(n), np.zeros(n), ext)
+    lbdar = np.asarray(lbdar, dtype=np.float64)
+    lbdar_rf = np.where((rr > 0) & (rf > 0),
+                        ext["LBR"] * (rhodref * np.maximum(rr / np.where(rf > 0, rf, 1.0), ext["R_RTMIN"]))
+                        ** ext["LBEXR"], 0.0)
+    rec = dict(in_t=t, in_pres=pres, in_rhodref=rhodref, in_tht=tht, in_rv=rv, in_rc=rc, in_rr=rr,
+               in_ld=ld.astype(np.float64), in_cf=cf, in_rf=rf, in_hlc_hcf=hlc_hcf, in_hlc_hrc=hlc_hrc,
+               in_ssi=ssi, in_ka=ka, in_dv=dv, in_ai=ai, in_cj=cj, in_lbdar=lbdar, in_lbdar_rf=lbdar_rf)
+    for mode in (1, 2):
+        res = mods["warm"].ice4_warm(rhodref, t, pres, tht, lbdar, lbdar_rf, ka, dv, cj, hlc_hcf, hlc_hrc, cf, rf,
+                                     rv, rc, rr, ld, False, mode, ext)
+        for nm, r in zip(("rcautr", "rcaccr", "rrevav"), res):
+            rec[f"out{mode}_{nm}"] = r
+    return {"warm_subg": rec}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-src", default="/root/reference/src")
+    ap.add_argument("--only", nargs="*", default=None, help="write only these golden files (names without .npz)")
     args = ap.parse_args()
     import refshim
 
@@ -221,7 +264,10 @@ def main():
     blobs.update(ice_adjust_cases(IceAdjustJAX, Phyex))
     blobs.update(sedimentation_case(sedimentation_stat, Phyex))
     blobs.update(process_cases(mods, Phyex))
+    blobs.update(warm_subg_case(mods, Phyex))
     for name, rec in blobs.items():
+        if args.only is not None and name not in args.only:
+            continue
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v, dtype=np.float64) for k, v in rec.items()})
         print(f"wrote {path} ({os.path.getsize(path) / 1e3:.0f} kB)")

@@ -117,3 +117,21 @@ def test_rainfr_vert(jax_table):
     g = load_golden("processes")
     out = oracle.rainfr_vert(jax_table, g["rf_in_prfr"], g["rf_in_rr"], g["rf_in_rs"], g["rf_in_rg"])
     assert rel_err(out, g["rf_out_prfr"]) <= TOL
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_warm_subgrid_evaporation(mode):
+    """CLFR (1) and PRFR (2) rain evaporation (and autoconversion /
+    accretion on the same points) against the reference JAX ice4_warm."""
+    g = load_golden("warm_subg")
+    i = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    table = build_table(table="jax", overrides={"SUBG_RR_EVAP": mode})
+    n = i["t"].size
+    z = np.zeros(n)
+    inp = dict(t=i["t"], rhodref=i["rhodref"], pres=i["pres"], rv=i["rv"], rc=i["rc"], rr=i["rr"], ri=z, rs=z,
+               rg=z, cit=z, ssi=i["ssi"], ka=i["ka"], dv=i["dv"], ai=i["ai"], cj=i["cj"], hlc_hcf=i["hlc_hcf"],
+               hlc_hrc=i["hlc_hrc"], hli_hcf=z, hli_hri=z, cf=i["cf"], rainfr=i["rf"], tht=i["tht"])
+    r = oracle.process_rates(table, inp, i["ld"] > 0.5)
+    for k in ("rcautr", "rcaccr", "rrevav"):
+        assert rel_err(r[k], g[f"out{mode}_{k}"]) <= TOL, (mode, k)
+    assert np.count_nonzero(g[f"out{mode}_rrevav"]) > 50

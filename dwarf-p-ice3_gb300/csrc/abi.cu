@@ -59,11 +59,12 @@ struct Handle {
 
 enum {
   K_ICE_ADJUST = 0, K_SEDIM, K_RAIN_ICE, K_EVAP_FIXUP, K_FOG, K_ORDER, K_IA_VJP, K_SED_VJP, K_SUR_SAMPLE, K_SUR_MLP,
-  K_SUR_RAIN_ICE, K_COUNT
+  K_SUR_RAIN_ICE, K_PRFR, K_COUNT
 };
 const char *kKernelNames[K_COUNT] = {"ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup",
                                      "fog_deposition", "rain_ice_order", "ice_adjust_vjp", "sedimentation_vjp",
-                                     "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate"};
+                                     "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate",
+                                     "rain_ice_precip_fraction"};
 
 // Brackets one launch with events when the handle is profiling.
 struct ProfScope {
@@ -229,6 +230,8 @@ int check_surrogate(Handle *h, const SurCall &sur, long n)
     return fail(h, ICE3GB_ERR_SHAPE, "surrogate: the MLP maps %d -> %d, expected %d -> %d", n_in, n_out,
                 ICE3GB_SUR_NFEAT, ICE3GB_SUR_NOUT);
   if (!sur.norm) return fail(h, ICE3GB_ERR_NULL, "surrogate: normalisation is NULL");
+  if ((int)h->c.SUBG_RC_RR_ACCR != 0 || (int)h->c.SUBG_RR_EVAP != 0)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained with SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE only");
   if (n > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "surrogate: at most 2^31 - 1 points per call");
   return ICE3GB_OK;
 }
@@ -326,6 +329,10 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   a.scr.keys = rs.keys;
   a.order = rs.order;
   a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
+  if ((int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2) {
+    ProfScope ps(h, K_PRFR, s);
+    if ((e = launch_rain_ice_prfr(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice precipitation fraction");
+  }
   if (rs.order) {
     ProfScope ps(h, K_ORDER, s);
     if ((e = launch_rain_ice_order(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice order launch");
@@ -742,8 +749,9 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   if ((int)c->NRR != 6) snprintf(why, sizeof(why), "rain_ice supports NRR=6 only (got %g)", c->NRR);
   else if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)
     snprintf(why, sizeof(why), "rain_ice: MRSTEP/TSTEP_TS time-splitting is not supported");
-  else if ((int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0)
-    snprintf(why, sizeof(why), "rain_ice: SUBG_RC_RR_ACCR/SUBG_RR_EVAP other than NONE are not supported");
+  else if (((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) ||
+           (int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2)
+    snprintf(why, sizeof(why), "rain_ice: SUBG_RC_RR_ACCR must be NONE or PRFR, SUBG_RR_EVAP NONE, CLFR or PRFR");
   if (why[0]) {
     h->rain_ice_ok = false;
     h->rain_ice_why = why;

@@ -161,6 +161,8 @@ cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_order(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 size_t rain_ice_smem_bytes();
 
+// Precipitation fraction of a rain_ice call with a PRFR option (before the point kernel).
+cudaError_t launch_rain_ice_prfr(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_surrogate_sample(const Ice3gbConstants &c, const SurSampleArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_rain_ice_surrogate(const Ice3gbConstants &c, const SurRainIceArgs &a, int num_sms, cudaStream_t s);
 // Forward pass of an MLP handle (ice3gb_mlp_create) over n rows in chunks,

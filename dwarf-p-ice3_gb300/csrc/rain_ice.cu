@@ -22,6 +22,8 @@
 //    takes), so a warp's lanes take the same branches instead of the union
 //    of all regimes; the tile keeps the gathered accesses within a window of
 //    256 KB per field.  Results do not depend on the order;
+//  * with a PRFR option a column kernel first forms the precipitation
+//    fraction the sub-stepping starts from (prfr_column);
 //  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
 //    after the last pass of the call, mode_ice4_stepping.F90:514-516) is
 //    kept with a per-point pass key and a warp-reduced atomicMax, resolved by
@@ -45,6 +47,9 @@ __device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int
   if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(key_max, m);
 }
 
+// SUBG: the subgrid warm-process options (SUBG_RC_RR_ACCR / SUBG_RR_EVAP
+// other than NONE); the NONE instantiation carries none of their code.
+template <bool SUBG>
 __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_kernel(const __grid_constant__ Cst c,
                                                                          const __grid_constant__ RainIceArgs a)
 {
@@ -69,13 +74,21 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
     if (slot < n) {
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       bool capped;
-      key = rain_ice_point(c, dsh, lut, f, p, dt, a.max_passes, capped);
+      key = rain_ice_point<false, SUBG>(c, dsh, lut, f, p, dt, a.max_passes, capped);
       any_capped |= capped;
       a.scr.keys[p] = key;
     }
     warp_key_max(a.scr.key_max, key);
   }
   if (any_capped) atomicOr(a.scr.status, ICE3GB_DEV_PASS_CAP);
+}
+
+// The precipitation fraction of a call with a PRFR option, one thread per
+// column (prfr_column); runs before the point kernel, which starts from it.
+__global__ void rain_ice_prfr_kernel(const __grid_constant__ Cst c, const __grid_constant__ RainIceArgs a)
+{
+  const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (col < a.nij) prfr_column(c, a.f, a.nij, a.nk, col);
 }
 
 // Processing order: per tile of ORDER_TILE points, a counting sort by regime
@@ -156,15 +169,23 @@ size_t rain_ice_smem_bytes() { return sizeof(double) * LUT_N; }
 
 cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_sms, cudaStream_t s)
 {
-  cudaError_t e = cudaFuncSetAttribute(rain_ice_points_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)rain_ice_smem_bytes());
+  const bool subg = (int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0;
+  cudaError_t e = cudaFuncSetAttribute(subg ? rain_ice_points_kernel<true> : rain_ice_points_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rain_ice_smem_bytes());
   if (e != cudaSuccess) return e;
   const long n = (long)a.nij * a.nk;
   long chunks = (n + RI_THREADS - 1) / RI_THREADS;
   long blocks = (long)num_sms * RI_BLOCKS_PER_SM;
   if (blocks > chunks) blocks = chunks;
   if (blocks < 1) blocks = 1;
-  rain_ice_points_kernel<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  if (subg) rain_ice_points_kernel<true><<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  else rain_ice_points_kernel<false><<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rain_ice_prfr(const Cst &c, const RainIceArgs &a, cudaStream_t s)
+{
+  rain_ice_prfr_kernel<<<(unsigned)((a.nij + 127) / 128), 128, 0, s>>>(c, a);
   return cudaGetLastError();
 }
 

@@ -256,15 +256,78 @@ ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const
   } else { s.lbdag = 0.0; s.llbdag = -INFINITY; }
 }
 
+// log of the rain slope parameter within the precipitation fraction
+// (mode_ice4_tendencies.F90:395-405, LLRFR): -inf where rr or rainfr is 0.
+ICE3_HD double llbdar_rf(const Cst &c, const Derived &d, double lrho, double rr, double rainfr)
+{
+  if (!(pos(rr) && pos(rainfr))) return -INFINITY;
+  return d.lLBR + c.LBEXR * (lrho + fm::flog(dmax(rr / rainfr, c.R_RTMIN)));
+}
+
+// The subgrid forms of RCACCR (SUBG_RC_RR_ACCR = PRFR: accretion in the high
+// and low cloud parts within the precipitation fraction) and RREVAV
+// (SUBG_RR_EVAP = CLFR / PRFR: evaporation in the clear part of the grid or
+// of the precipitation fraction, at the liquid-water temperature), hard
+// pass (mode_ice4_warm.F90).
+ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, double t, const double v[NV],
+                          const double hl[4], double ka, double dv, double cj, const Slopes &s, double rainfr,
+                          double e_caccr, Rates &R)
+{
+  double *b = R.bu;
+  const bool has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
+  const int accr = (int)c.SUBG_RC_RR_ACCR, evap = (int)c.SUBG_RR_EVAP;
+  const bool llrfr = accr == 1 || evap == 2;
+  const double llrf = llrfr ? llbdar_rf(c, d, pf.lrho, v[IRR], rainfr) : s.llbdar;
+  if (accr == 0) {
+    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt : 0.0;
+  } else {
+    const bool m = has_c && has_r;
+    const bool m1 = m && gtp(hl[2], c.C_RTMIN) && pos(hl[0]);
+    const bool m2 = m && gtp(hl[3], c.C_RTMIN) && gtp(hl[1], 1.e-20);
+    double r = 0.0;
+    if (m1 || m2) {
+      const double k = c.FCACCR * fm::fexp(c.EXCACCR * llrf) * pf.rho_mcexvt;
+      if (m1) r = k * hl[2];
+      if (m2) r += k * fm::fdiv(hl[3], hl[1]) * (dmin(pf.cf, rainfr) - hl[0]);
+    }
+    b[B_RCACCR] = r;
+  }
+  if (evap == 0) {
+    if (has_r && !has_c) {
+      const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, fm::frcp(t), fm::flog(t));
+      const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
+      const double av = fm::fdiv(sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)), ka * c.RV * t * t) +
+                        fm::fdiv(c.RV * t, dv * esw);
+      b[B_RREVAV] = fm::fdiv(pmax0(usw), pf.rho * av) *
+                    (c.O0EVAR * fm::fexp(c.EX0EVAR * s.llbdar) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
+    } else b[B_RREVAV] = 0.0;
+  } else {
+    const double zw4 = evap == 1 ? 1.0 : rainfr;
+    const double lz3 = evap == 1 ? s.llbdar : llrf;
+    if (has_r && gtd(zw4, pf.cf)) {
+      const double tht = v[ITH];
+      const double thlt = tht - fm::fdiv(c.LVTT * tht, c.CPD * t) * v[IRC];
+      const double zw2 = fm::fdiv(thlt * t, tht);
+      const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, fm::frcp(zw2), fm::flog(zw2));
+      const double usw = 1.0 - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
+      const double av = fm::fdiv(sq(c.LVTT + (c.CPV - c.CL) * (zw2 - c.TT)), ka * c.RV * zw2 * zw2) +
+                        fm::fdiv(c.RV * zw2, dv * esw);
+      b[B_RREVAV] = fm::fdiv(pmax0(usw), pf.rho * av) *
+                    (c.O0EVAR * fm::fexp(c.EX0EVAR * lz3) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * lz3)) *
+                    (zw4 - pf.cf);
+    } else b[B_RREVAV] = 0.0;
+  }
+}
+
 // The hard-pass rates of ICE4_TENDENCIES after nucleation, RRHONG and RIMLTC
 // (mode_ice4_tendencies.F90:303-600): derived fields, slopes, ICE4_SLOW,
 // ICE4_WARM and the rate parts of ICE4_FAST_RS/RG/RI.  The parts that depend
 // on the current freezing budget (riming/accretion split, wet/dry growth
 // choice) are left to aggregate(), which every pass runs.
-template <bool SUR = false>
+template <bool SUR = false, bool SUBG = false>
 ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                         double t, const double v[NV], double cit, const double hl[4], const double hi[4],
-                        double criauti, Rates &R, bool learned_slow = false)
+                        double criauti, Rates &R, bool learned_slow = false, double rainfr = 1.0)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
@@ -329,8 +392,12 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     b[B_RVDEPG] = (has_v && has_g) ? ssi_rai * vent_g : 0.0;
   }
 
-  // ---- ICE4_WARM (mode_ice4_warm.F90), SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE ----
-  if (c.LWARM != 0.0) {
+  // ---- ICE4_WARM (mode_ice4_warm.F90) ----
+  if (SUBG && c.LWARM != 0.0 && ((int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0)) {
+    b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
+    warm_subgrid(c, d, pf, t, v, hl, ka, dv, cj, s, rainfr, e_caccr, R);
+  } else if (c.LWARM != 0.0) {
+    // SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
     b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt : 0.0;
     if (has_r && !has_c) {
@@ -448,8 +515,9 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 // Rates of a soft pass: the hard-pass values where their condition still
 // holds on the current state, zero elsewhere (the ELSE branches of the
 // process routines under LDSOFT).
+template <bool SUBG = false>
 ICE3_HD void soft_rates(const Cst &c, double t, const double v[NV], double cit, const double hl[4],
-                        const double hi[4], Rates &R)
+                        const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
@@ -460,7 +528,22 @@ ICE3_HD void soft_rates(const Cst &c, double t, const double v[NV], double cit, 
   if (!(has_i && has_s)) b[B_RIAGGS] = 0.0;
   if (!gtp(hi[2], c.I_RTMIN)) b[B_RIAUTS] = 0.0;
   if (!(has_v && has_g)) b[B_RVDEPG] = 0.0;
-  if (c.LWARM != 0.0) {
+  if (SUBG && c.LWARM != 0.0 && ((int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0)) {
+    if (!(gtp(hl[2], c.C_RTMIN) && pos(hl[0]))) b[B_RCAUTR] = 0.0;
+    if ((int)c.SUBG_RC_RR_ACCR == 0) {
+      if (!(has_c && has_r)) b[B_RCACCR] = 0.0;
+    } else {
+      const bool m = has_c && has_r;
+      if (!((m && gtp(hl[2], c.C_RTMIN) && pos(hl[0])) || (m && gtp(hl[3], c.C_RTMIN) && gtp(hl[1], 1.e-20))))
+        b[B_RCACCR] = 0.0;
+    }
+    const int evap = (int)c.SUBG_RR_EVAP;
+    if (evap == 0) {
+      if (!(has_r && !has_c)) b[B_RREVAV] = 0.0;
+    } else if (!(has_r && gtd(evap == 1 ? 1.0 : rainfr, cf))) {
+      b[B_RREVAV] = 0.0;
+    }
+  } else if (c.LWARM != 0.0) {
     if (!(gtp(hl[2], c.C_RTMIN) && pos(hl[0]))) b[B_RCAUTR] = 0.0;
     if (!(has_c && has_r)) b[B_RCACCR] = 0.0;
     if (!(has_r && !has_c)) b[B_RREVAV] = 0.0;
@@ -626,7 +709,7 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
 // nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
 // and all rates are computed; a soft pass keeps the hard-pass rates.
-template <bool SUR = false>
+template <bool SUR = false, bool SUBG = false>
 ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict__ lut, bool soft,
                         const PointFix &pf, double lvfact, double lsfact, double &cit, double t0,
                         const double vart[NV], Rates &R, double &rainfr, double hl[4], double hi[4], double A[NV],
@@ -651,15 +734,15 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   } else {
     rainfr = 1.;
   }
-  if (!soft) hard_rates<SUR>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr);
-  else soft_rates(c, t, v, cit, hl, hi, R);
+  if (!soft) hard_rates<SUR, SUBG>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr);
+  else soft_rates<SUBG>(c, t, v, cit, hl, hi, R, pf.cf, rainfr);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
   aggregate(c, t, v, lvfact, lsfact, R, A);
 }
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
-template <bool SUR = false>
+template <bool SUR = false, bool SUBG = false>
 ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                               double dt, int max_passes, double vart[NV], const double ext[NV], double &cit,
                               double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped,
@@ -696,7 +779,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
       double A[NV], B[NV];
-      tendencies<SUR>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur);
+      tendencies<SUR, SUBG>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur);
       if (SUR) sur = nullptr;          // learned slow rates: first hard pass only
 #pragma unroll
       for (int v = 0; v < NV; ++v) A[v] += ext[v];
@@ -749,7 +832,7 @@ ICE3_HD double ldp(const double *p, long i)
 // sub-stepping, total tendencies and ICE4_CORRECT_NEGATIVITIES on the
 // sources, written back in place.  Returns the pass key (0 for points
 // outside LLMICRO or capped); `capped` reports a point that hit max_passes.
-template <bool SUR = false>
+template <bool SUR = false, bool SUBG = false>
 ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
                                     const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped,
                                     const double *sur = nullptr)
@@ -779,7 +862,10 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
                      gtp(rg, c.G_RTMIN);
   const double iexnref = fm::frcp(exnref);
   const double lsx = lsf * iexnref, lvx = lvf * iexnref;
-  double evap = 0.0, rainfr = 1.0;
+  // with a PRFR option the sub-stepping starts from the precipitation
+  // fraction of prfr_column (rain_ice.F90:555-602, ICE4_PACK :326)
+  const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
+  double evap = 0.0, rainfr = (SUBG && llrfr) ? f.rainfr[p] : 1.0;
   double zrvheni = 0.0;
   if (!micro) {
     cit = 0.0;
@@ -806,7 +892,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
       hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
     }
     double rrevav;
-    key = stepping<SUR>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur);
+    key = stepping<SUR, SUBG>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur);
 #pragma unroll
     for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;
@@ -847,6 +933,56 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   f.evap3d[p] = evap;
   f.rainfr[p] = rainfr;
   return key;
+}
+
+// The precipitation fraction a rain_ice call with a PRFR option starts from
+// (rain_ice.F90:555-605), for one column: ICE4_COMPUTE_PDF on the time-t
+// state of each micro point (its partition overwrites hlc_hcf / hlc_hrc /
+// hli_hcf / hli_hri, as the Fortran's INOUT arguments; outside micro points
+// the masked form: zeros, ADJU keeps the fractions), then ICE4_RAINFR_VERT
+// from the top level down (mode_ice4_rainfr_vert.F90: 0 at the top, the
+// maximum with the level above where rain, snow or graupel is present, 1 if
+// that is 0, else 0).  Writes f.rainfr of the column.
+ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, int nk, long col)
+{
+  const int aucv_rc = (int)c.SUBG_AUCV_RC, aucv_ri = (int)c.SUBG_AUCV_RI;
+  const bool sigm = aucv_rc == 1 && (int)c.SUBG_PR_PDF == 0;
+  const bool adju = aucv_rc == 2 || aucv_ri == 2;
+  double above = 0.0;
+  for (int k = nk - 1; k >= 0; --k) {
+    const long p = (long)k * nij + col;
+    const double rc = ldp(f.rct, p), rr = ldp(f.rrt, p), ri = ldp(f.rit, p), rs = ldp(f.rst, p);
+    const double rg = ldp(f.rgt, p), cf = ldp(f.cldfr, p);
+    const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
+                       gtp(rg, c.G_RTMIN);
+    double hl[4] = {f.hlc_hcf[p], 0.0, f.hlc_hrc[p], 0.0}, hi[4] = {f.hli_hcf[p], 0.0, f.hli_hri[p], 0.0};
+    if (adju) {                                                    // rain_ice.F90:564-581
+      hl[3] = rc - hl[2];
+      hi[3] = ri - hi[2];
+      hl[1] = pos(rc) ? cf - hl[0] : 0.;
+      hi[1] = pos(ri) ? cf - hi[0] : 0.;
+    }
+    double rf = 0.0;
+    if (micro) {
+      const double sig = sigm ? ldp(f.sigs, p) : 0.0;
+      const double rho = ldp(f.rhodref, p);
+      double criauti;
+      rf = compute_pdf(c, c.CRIAUTC / rho, rc, ri, cf, ldp(f.tht, p) * ldp(f.exn, p), sig * sig, hl, hi, criauti);
+    } else {
+      if (aucv_rc != 2) hl[0] = 0.0;
+      hl[2] = 0.0;
+      if (aucv_ri != 2) hi[0] = 0.0;
+      hi[2] = 0.0;
+    }
+    f.hlc_hcf[p] = hl[0]; f.hlc_hrc[p] = hl[2]; f.hli_hcf[p] = hi[0]; f.hli_hri[p] = hi[2];
+    double pr = 0.0;
+    if (k < nk - 1 && (gtp(rr, c.R_RTMIN) || gtp(rs, c.S_RTMIN) || gtp(rg, c.G_RTMIN))) {
+      pr = dmax(rf, above);
+      if (zerod(pr)) pr = 1.0;
+    }
+    f.rainfr[p] = pr;
+    above = pr;
+  }
 }
 
 }  // namespace ice3pt

@@ -128,7 +128,8 @@ EXPORTED = (
 )
 NOALLOC_MAX_POINTS = 4194304
 KERNEL_NAMES = ("ice_adjust", "sedimentation", "rain_ice", "rain_ice_evap_fixup", "fog_deposition", "rain_ice_order",
-                "ice_adjust_vjp", "sedimentation_vjp", "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate")
+                "ice_adjust_vjp", "sedimentation_vjp", "surrogate_sample", "surrogate_mlp", "rain_ice_surrogate",
+                "rain_ice_precip_fraction")
 
 _lib: Optional[ctypes.CDLL] = None
 

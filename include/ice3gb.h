@@ -164,7 +164,13 @@ typedef struct Ice3gbSedimentationFields {
 /* ---- rain_ice ---------------------------------------------------------- */
 /* Arguments of c_rain_ice (phyex_bridge.F90:242-254) / RAIN_ICE
  * (micro/rain_ice.F90) and of the RainIceJAX state dict
- * (src/ice3/jax/rain_ice.py:181). */
+ * (src/ice3/jax/rain_ice.py:181).  The handle's SUBG_RC_RR_ACCR (NONE,
+ * PRFR) and SUBG_RR_EVAP (NONE, CLFR, PRFR) select the warm-process forms;
+ * with a PRFR option the call first forms the precipitation fraction from
+ * the time-t state (rain_ice.F90:555-605), which rewrites hlc_hcf, hlc_hrc,
+ * hli_hcf and hli_hri with ICE4_COMPUTE_PDF's partition, as the Fortran's
+ * INOUT arguments; rainfr returns the precipitation fraction (1 everywhere
+ * without a PRFR option). */
 typedef struct Ice3gbRainIceFields {
   const double *exn, *dzz, *rhodref, *exnref, *pabs, *cldfr, *sigs;
   const double *tht, *rvt, *rct, *rrt, *rit, *rst, *rgt;
@@ -412,8 +418,9 @@ int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3
  * fix-up, 4 fog deposition, 5 rain_ice point ordering (regime sort),
  * 6 ice_adjust adjoint, 7 sedimentation adjoint, 8 surrogate feature
  * sampling, 9 surrogate network (all its tensor-core launches of one call),
- * 10 rain_ice with the learned slow rates. */
-#define ICE3GB_NKERNELS 11
+ * 10 rain_ice with the learned slow rates, 11 rain_ice precipitation
+ * fraction (PRFR options). */
+#define ICE3GB_NKERNELS 12
 int         ice3gb_profile_enable(void *handle, int enable);
 int         ice3gb_profile_read(void *handle, int kernel_id, int *launches, double *total_ms);
 const char *ice3gb_kernel_name(int kernel_id);

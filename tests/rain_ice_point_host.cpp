@@ -16,6 +16,27 @@ extern "C" int rain_ice_points_host(const Ice3gbConstants *c, const Ice3gbLuts *
   return capped_any;
 }
 
+// The same with the subgrid warm-process options (SUBG_RC_RR_ACCR /
+// SUBG_RR_EVAP): the precipitation fraction of each column first when a
+// PRFR option is set (prfr_column), then the points.
+extern "C" int rain_ice_points_host_subg(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk,
+                                         double dt, int max_passes, const Ice3gbRainIceFields *f,
+                                         unsigned int *keys)
+{
+  ice3pt::Derived d;
+  ice3pt::make_derived(*c, d);
+  if ((int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2)
+    for (long col = 0; col < nij; ++col) ice3pt::prfr_column(*c, *f, nij, nk, col);
+  int capped_any = 0;
+  for (long p = 0; p < (long)nij * nk; ++p) {
+    bool capped;
+    keys[p] = ice3pt::rain_ice_point<false, true>(*c, d, reinterpret_cast<const double *>(luts), *f, p, dt,
+                                                  max_passes, capped);
+    capped_any |= capped;
+  }
+  return capped_any;
+}
+
 // Host build of the surrogate's feature / target sampling (surrogate_point.cuh):
 // per grid point the 16 features and the five plain slow rates of a micro
 // point at its first hard pass; micro[p] = 0 elsewhere.

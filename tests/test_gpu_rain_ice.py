@@ -278,3 +278,23 @@ def test_physics_step_host_slab_pipeline_matches_device(nij):
     for k in dev:
         np.testing.assert_array_equal(host[k], dev[k], err_msg=k)
     assert h.status() == 0
+
+
+@pytest.mark.parametrize("accr,evap,aucv_rc,aucv_ri", [(1, 2, 3, 1), (0, 1, 1, 0), (1, 0, 3, 0), (0, 2, 3, 1)])
+def test_rain_ice_subgrid_warm_options_match_oracle(accr, evap, aucv_rc, aucv_ri):
+    """SUBG_RC_RR_ACCR / SUBG_RR_EVAP other than NONE on the device: the
+    precipitation-fraction column kernel, then the point kernel's subgrid
+    instantiation, against the oracle's RAIN_ICE (sources, ci_t, evap3d,
+    the precipitation fraction and the partitions the PRFR set-up rewrites)."""
+    from ice3gb import RainIce
+    from ice3gb.constants import build_table
+    ri = RainIce()
+    ri.table = build_table(table="phyex", overrides={"SUBG_RC_RR_ACCR": accr, "SUBG_RR_EVAP": evap,
+                                                     "SUBG_AUCV_RC": aucv_rc, "SUBG_AUCV_RI": aucv_ri})
+    st = _np_state(32 * 32, seed=21)
+    ref, spread = _oracle_ri(ri.table, st)
+    out = _run_gpu(ri, st)
+    _compare(out, ref, spread)
+    for k in ("hlc_hcf", "hlc_hrc", "hli_hcf", "hli_hri"):
+        assert_parity(out[k], ref[k], spread[k], k)
+    assert ri.device_status() == 0

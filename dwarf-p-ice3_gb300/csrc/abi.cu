@@ -162,6 +162,7 @@ bool ia_vec2_ok(const Ice3gbIceAdjustFields *f, long n)
   for (const void *p : ptrs)
     if (!aligned16(p)) return false;
   if (f->sigqsat_3d && !aligned16(f->sigqsat)) return false;
+  if (f->srcs && !aligned16(f->srcs)) return false;
   return true;
 }
 
@@ -1070,10 +1071,12 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
   const size_t n = (size_t)nij * nk, b3 = n * sizeof(double);
   const size_t bq = (f->sigqsat_3d ? n : (size_t)nij) * sizeof(double);
   const size_t bq_pad = (bq + 255) & ~(size_t)255, b3_pad = (b3 + 255) & ~(size_t)255;
-  // 15 inputs + 4 in-out + 12 outputs
-  if ((rc = ensure_stage(h, bq_pad + 31 * b3_pad))) return rc;
+  // 15 inputs + 4 in-out + 12 outputs (+ srcs)
+  const int nsrc = f->srcs ? 1 : 0;
+  if ((rc = ensure_stage(h, bq_pad + (31 + nsrc) * b3_pad))) return rc;
   char *base = reinterpret_cast<char *>(h->d_stage);
   Ice3gbIceAdjustFields d;
+  std::memset(&d, 0, sizeof(d));
   d.sigqsat = reinterpret_cast<double *>(base);
   d.sigqsat_3d = f->sigqsat_3d;
   double *slot = reinterpret_cast<double *>(base + bq_pad);
@@ -1098,6 +1101,7 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
     e = cudaMemcpyAsync(slot, *io_src[i], b3, cudaMemcpyHostToDevice, s);
   }
   for (int i = 0; i < 12; ++i, slot += step) *out_dst[i] = slot;
+  if (nsrc) d.srcs = slot;
   if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
   IaKernelFields kf;
   kf.f = d;
@@ -1111,6 +1115,7 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaMemcpyAsync(*io_src[i], *io_dst[i], b3, cudaMemcpyDeviceToHost, s);
   for (int i = 0; i < 12 && e == cudaSuccess; ++i)
     e = cudaMemcpyAsync(*out_src[i], *out_dst[i], b3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && nsrc) e = cudaMemcpyAsync(f->srcs, d.srcs, b3, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
   return ICE3GB_OK;

@@ -18,7 +18,7 @@ using namespace ice3ia;
 // microphysics in the chained physics step) instead of th/rv/.../rg, which
 // are then not read; rrs/rss/rgs are read instead.  Output pointers may be
 // NULL in the internal chained use (store skipped).
-template <bool ADV>
+template <bool ADV, bool SRC>
 __global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constant__ Cst c,
                                                             const __grid_constant__ IaKernelFields kf,
                                                             long npairs, int nij, double dt)
@@ -61,8 +61,10 @@ __global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constan
       x1.sigqsat = ld1(f.sigqsat, (p + 1) % nij);
     }
     IaOut o0, o1;
-    ia_point(c, d, dt, inv_dt, x0, o0);
-    ia_point(c, d, dt, inv_dt, x1, o1);
+    double s0 = 0.0, s1 = 0.0;
+    ia_point(c, d, dt, inv_dt, x0, o0, SRC ? &s0 : nullptr);
+    ia_point(c, d, dt, inv_dt, x1, o1, SRC ? &s1 : nullptr);
+    if (SRC) st2(f.srcs, p, s0, s1);
 #define ST2(field) if (f.field) st2(f.field, p, o0.field, o1.field);
     ST2(t) ST2(rv_out) ST2(rc_out) ST2(ri_out) ST2(cldfr) ST2(hlc_hrc) ST2(hlc_hcf) ST2(hli_hri) ST2(hli_hcf)
     ST2(cph) ST2(lv) ST2(ls) ST2(rvs) ST2(rcs) ST2(ris) ST2(ths)
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constan
 }
 
 // Scalar path: odd point counts or unaligned fields.
-template <bool ADV>
+template <bool ADV, bool SRC>
 __global__ void __launch_bounds__(256) ice_adjust_v1_kernel(const __grid_constant__ Cst c,
                                                             const __grid_constant__ IaKernelFields kf,
                                                             long n, int nij, double dt)
@@ -95,7 +97,9 @@ __global__ void __launch_bounds__(256) ice_adjust_v1_kernel(const __grid_constan
       x.rr = ld1(f.rr, p); x.rs = ld1(f.rs, p); x.rg = ld1(f.rg, p);
     }
     IaOut o;
-    ia_point(c, d, dt, inv_dt, x, o);
+    double s0 = 0.0;
+    ia_point(c, d, dt, inv_dt, x, o, SRC ? &s0 : nullptr);
+    if (SRC) f.srcs[p] = s0;
 #define ST1(field) if (f.field) f.field[p] = o.field;
     ST1(t) ST1(rv_out) ST1(rc_out) ST1(ri_out) ST1(cldfr) ST1(hlc_hrc) ST1(hlc_hcf) ST1(hli_hri) ST1(hli_hcf)
     ST1(cph) ST1(lv) ST1(ls) ST1(rvs) ST1(rcs) ST1(ris) ST1(ths)
@@ -112,17 +116,28 @@ cudaError_t launch_ice_adjust(const Cst &c, const IaKernelFields &kf, int nij, i
   const int threads = 256;
   const long cap = (long)num_sms * 64;
   const bool adv = kf.adv_dt != 0.0;
+  const bool src = kf.f.srcs != nullptr;
   if (vec2) {
     const long npairs = n / 2;
     long blocks = (npairs + threads - 1) / threads;
     if (blocks > cap) blocks = cap;
-    if (adv) ice_adjust_v2_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
-    else ice_adjust_v2_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
+    if (src) {
+      if (adv) ice_adjust_v2_kernel<true, true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
+      else ice_adjust_v2_kernel<false, true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
+    } else {
+      if (adv) ice_adjust_v2_kernel<true, false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
+      else ice_adjust_v2_kernel<false, false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, npairs, nij, dt);
+    }
   } else {
     long blocks = (n + threads - 1) / threads;
     if (blocks > cap) blocks = cap;
-    if (adv) ice_adjust_v1_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
-    else ice_adjust_v1_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
+    if (src) {
+      if (adv) ice_adjust_v1_kernel<true, true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
+      else ice_adjust_v1_kernel<false, true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
+    } else {
+      if (adv) ice_adjust_v1_kernel<true, false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
+      else ice_adjust_v1_kernel<false, false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, dt);
+    }
   }
   return cudaGetLastError();
 }

@@ -42,13 +42,46 @@ ICE3_HD void triangle_pdf(double w_dt, double crit, double cf_mf, double &hcf, d
   hcf *= cf_mf;
 }
 
+// SRC_1D of condensation.F90:208-214 (index -22..11; the same values as
+// src/ice3/phyex_common/lookup_table.py:4-40): s'r_c'/sigma_s^2 of the
+// Gaussian subgrid scheme tabulated against 2 q1.
+#define ICE3_SRC_1D_VALUES                                                                                      \
+  0., 0., 2.0094444e-04, 0.316670e-03, 4.9965648e-04, 0.785956e-03, 1.2341294e-03, 0.193327e-02,            \
+      3.0190963e-03, 0.470144e-02, 7.2950651e-03, 0.112759e-01, 1.7350994e-02, 0.265640e-01, 4.0427860e-02,  \
+      0.610997e-01, 9.1578111e-02, 0.135888, 0.1991484, 0.230756, 0.2850565, 0.375050, 0.5000000, 0.691489,   \
+      0.8413813, 0.933222, 0.9772662, 0.993797, 0.9986521, 0.999768, 0.9999684, 0.999997, 1.0000000, 1.000000
+#if defined(__CUDACC__)
+static __constant__ double kSrc1dDev[34] = {ICE3_SRC_1D_VALUES};
+#endif
+static const double kSrc1dHost[34] = {ICE3_SRC_1D_VALUES};
+
+// PSIGRC of condensation.F90:566-571 from q1, times the CB lambda3 factor
+// min(3, max(1, 1 - q1)) of :638-647 when LAMBDA3 = CB (0).
+ICE3_HD double sigrc_cb(const Cst &c, double q1)
+{
+  const double x = 2.0 * nmin(100.0, nmax(-100.0, q1));
+  const int i = (int)floor(x);
+  const int inq1 = i < -22 ? -22 : (i > 10 ? 10 : i);
+  const double inc = 2.0 * q1 - inq1;
+#if defined(__CUDA_ARCH__)
+  const double s0 = kSrc1dDev[inq1 + 22], s1 = kSrc1dDev[inq1 + 23];
+#else
+  const double s0 = kSrc1dHost[inq1 + 22], s1 = kSrc1dHost[inq1 + 23];
+#endif
+  double r = nmin(1.0, (1.0 - inc) * s0 + inc * s1);
+  if ((int)c.LAMBDA3 == 0) r *= nmin(3.0, nmax(1.0, 1.0 - q1));
+  return r;
+}
+
 // Constants derived once per thread (divisions of table constants).
 struct IaDerived {
   double rdrv, rvrd, irv;   // RD/RV, RV/RD, 1/RV
 };
 ICE3_HD IaDerived ia_derived(const Cst &c) { return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV}; }
 
-ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt, const IaIn &x, IaOut &o)
+// srcs (optional): PSRCS of the point (ice_adjust.F90:360, :468).
+ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt, const IaIn &x, IaOut &o,
+                      double *srcs = nullptr)
 {
   const int nrr = (int)c.NRR;
   double t = x.th * x.exn;
@@ -87,6 +120,7 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
       sigma = 2.0 * x.sigs;
     sigma = nmax(1e-10, sigma);
     const double q1 = fm::fdiv(sbar, sigma);
+    if (srcs) *srcs = sigrc_cb(c, q1);
     double cond;
     if (fgt(q1, 0.0)) cond = fge(2.0, q1) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;
     else cond = fm::fexp(1.2 * q1 - 1.0);
@@ -111,6 +145,7 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
   ths = ths + w2 * ls * inv_cphex;
   if (c.LSUBG_COND == 0.0) {
     cldfr = fgt((rcs + ris) * dt, 1e-12) ? 1.0 : 0.0;
+    if (srcs) *srcs = cldfr;
   } else {
     double w1m = x.rc_mf * inv_dt, w2m = x.ri_mf * inv_dt;
     const double tot = w1m + w2m;

@@ -32,7 +32,8 @@ class IceAdjustFields(ctypes.Structure):
         "rv", "rc", "ri", "rr", "rs", "rg", "cf_mf", "rc_mf", "ri_mf",
         "rvs", "rcs", "ris", "ths",
         "t", "rv_out", "rc_out", "ri_out", "cldfr",
-        "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls")] + [("sigqsat_3d", ctypes.c_int64)]
+        "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls")] + [("sigqsat_3d", ctypes.c_int64),
+                                                                         ("srcs", P)]
 
 
 class SedimentationFields(ctypes.Structure):

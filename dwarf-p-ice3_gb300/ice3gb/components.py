@@ -98,12 +98,15 @@ class IceAdjust:
         return self._handle
 
     def __call__(self, sigqsat, pabs, sigs, th, exn, exn_ref, rho_dry_ref, rv, rc, ri, rr, rs, rg, cf_mf, rc_mf,
-                 ri_mf, rvs, rcs, ris, ths, timestep: float) -> Tuple:
+                 ri_mf, rvs, rcs, ris, ths, timestep: float, return_srcs: bool = False) -> Tuple:
+        """The 16-tuple of IceAdjustJAX; with ``return_srcs`` a 17th element,
+        PSRCS (s'r_c'/sigma_s^2, the second-order flux term the Fortran
+        ICE_ADJUST returns, ice_adjust.F90:468)."""
         args = dict(sigqsat=sigqsat, pabs=pabs, sigs=sigs, th=th, exn=exn, exn_ref=exn_ref,
                     rho_dry_ref=rho_dry_ref, rv=rv, rc=rc, ri=ri, rr=rr, rs=rs, rg=rg, cf_mf=cf_mf, rc_mf=rc_mf,
                     ri_mf=ri_mf, rvs=rvs, rcs=rcs, ris=ris, ths=ths)
         if isinstance(pabs, np.ndarray):
-            return self._call_host(args, float(timestep))
+            return self._call_host(args, float(timestep), return_srcs)
         ref = pabs
         shape = tuple(ref.shape)
         dev = {k: _as_device_f64(v, ref) for k, v in args.items()}
@@ -119,10 +122,13 @@ class IceAdjust:
         for k, v in {**io, **outs}.items():
             setattr(f, k, _ptr(v))
         f.sigqsat_3d = sig3d
+        srcs = torch.empty(shape, dtype=torch.float64, device=ref.device) if return_srcs else None
+        f.srcs = _ptr(srcs)
         h = self.handle
         _abi.check(h.lib.ice3gb_ice_adjust(h.h, nij, nk, float(timestep), ctypes.byref(f),
                                            ctypes.c_void_p(_stream_ptr())), h.h, "ice3gb_ice_adjust")
-        return tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
+        res = tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
+        return res + (srcs,) if return_srcs else res
 
     @staticmethod
     def _geometry(shape, sig_shape):
@@ -133,7 +139,7 @@ class IceAdjust:
             return int(np.prod(shape[1:])), int(shape[0]), 0   # [nk, ...] with per-column sigqsat
         raise ValueError(f"sigqsat shape {sig_shape} matches neither the fields {shape} nor one level")
 
-    def _call_host(self, args: Dict[str, np.ndarray], dt: float) -> Tuple:
+    def _call_host(self, args: Dict[str, np.ndarray], dt: float, return_srcs: bool = False) -> Tuple:
         shape = args["pabs"].shape
         host = {k: np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for k, v in args.items()}
         nij, nk, sig3d = self._geometry(shape, host["sigqsat"].shape)
@@ -145,10 +151,14 @@ class IceAdjust:
         for k, v in {**io, **outs}.items():
             setattr(f, k, v.ctypes.data_as(ctypes.c_void_p))
         f.sigqsat_3d = sig3d
+        srcs = np.empty(shape) if return_srcs else None
+        if return_srcs:
+            f.srcs = srcs.ctypes.data_as(ctypes.c_void_p)
         h = self.handle
         _abi.check(h.lib.ice3gb_ice_adjust_host(h.h, nij, nk, dt, ctypes.byref(f), ctypes.c_void_p(_stream_ptr())),
                    h.h, "ice3gb_ice_adjust_host")
-        return tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
+        res = tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
+        return res + (srcs,) if return_srcs else res
 
 
 # RainIceJAX state keys -> ABI fields (src/ice3/jax/rain_ice.py:209-260,

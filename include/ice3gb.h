@@ -70,7 +70,7 @@ extern "C" {
   X(P00) X(RHOLW) X(MNH_TINY)                                                 \
   /* subgrid condensation (modd_nebn) */                                      \
   X(TMAXMIX) X(TMINMIX) X(LSUBG_COND) X(LSIGMAS) X(LSTATNW)                   \
-  X(FRAC_ICE_ADJUST) X(CONDENS) X(OCND2) X(NRR)                               \
+  X(FRAC_ICE_ADJUST) X(CONDENS) X(OCND2) X(NRR) X(LAMBDA3)                    \
   /* ICE3/ICE4 switches (modd_param_icen) */                                  \
   X(LWARM) X(LSEDIC) X(LDEPOSC) X(VDEPOSC) X(SEDIM) X(LFEEDBACKT)             \
   X(LEVLIMIT) X(LNULLWETG) X(LWETGPOST) X(SNOW_RIMING) X(LCRFLIMIT)           \
@@ -141,6 +141,10 @@ typedef struct Ice3gbIceAdjustFields {
   double *hlc_hrc, *hlc_hcf, *hli_hri, *hli_hcf;
   double *cph, *lv, *ls;
   int64_t sigqsat_3d;               /* 0: per column, 1: full 3-D field   */
+  double *srcs;                     /* optional out (NULL: not computed):
+                                       PSRCS = s'r_c'/sigma_s^2 of
+                                       ice_adjust.F90:360,468 and
+                                       condensation.F90:566-571, :638-647  */
 } Ice3gbIceAdjustFields;
 
 /* ---- statistical sedimentation ---------------------------------------- */

@@ -59,6 +59,27 @@ static void triangle_pdf(double w_dt, double crit, double cf_mf, double *hcf_out
   *hr_out = hr;
 }
 
+/* SRC_1D of condensation.F90:208-214 (index -22..11). */
+static const double SRC_1D[34] = {
+    0., 0., 2.0094444e-04, 0.316670e-03, 4.9965648e-04, 0.785956e-03, 1.2341294e-03, 0.193327e-02,
+    3.0190963e-03, 0.470144e-02, 7.2950651e-03, 0.112759e-01, 1.7350994e-02, 0.265640e-01, 4.0427860e-02,
+    0.610997e-01, 9.1578111e-02, 0.135888, 0.1991484, 0.230756, 0.2850565, 0.375050, 0.5000000, 0.691489,
+    0.8413813, 0.933222, 0.9772662, 0.993797, 0.9986521, 0.999768, 0.9999684, 0.999997, 1.0000000, 1.000000};
+
+EXPORT double ice3o_src_1d(int i) { return (i >= -22 && i <= 11) ? SRC_1D[i + 22] : 0.0 / 0.0; }
+
+/* PSIGRC from q1 (condensation.F90:566-571) with the CB lambda3 factor
+ * (:638-647, NEBN%CLAMBDA3 = 'CB' <-> LAMBDA3 = 0). */
+static double sigrc(const C *c, double q1)
+{
+  int inq1 = (int)floor(dmin(100.0, dmax(-100.0, 2.0 * q1)));
+  inq1 = inq1 < -22 ? -22 : (inq1 > 10 ? 10 : inq1);
+  const double inc = 2.0 * q1 - inq1;
+  double r = dmin(1.0, (1.0 - inc) * SRC_1D[inq1 + 22] + inc * SRC_1D[inq1 + 23]);
+  if ((int)c->LAMBDA3 == 0) r *= dmin(3.0, dmax(1.0, 1.0 - q1));
+  return r;
+}
+
 EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f)
 {
   if (!c || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
@@ -108,6 +129,7 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
         sigma = 2.0 * sigs;
       sigma = dmax(1e-10, sigma);
       const double q1 = sbar / sigma;
+      if (f->srcs) f->srcs[p] = sigrc(c, q1);                          /* ice_adjust.F90:468 */
       double cond;                                                     /* :241-249 */
       if (q1 > 0.0) cond = (q1 <= 2.0) ? dmin(exp(-1.0) + 0.66 * q1 + 0.086 * sq(q1), 2.0) : q1;
       else cond = exp(1.2 * q1 - 1.0);
@@ -132,6 +154,7 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
     ths = ths + w2 * ls / (cph * exn_ref);
     if (!subg) {
       cldfr = ((rcs + ris) * dt > 1e-12) ? 1.0 : 0.0;                 /* :285 */
+      if (f->srcs) f->srcs[p] = cldfr;                                 /* ice_adjust.F90:360 */
     } else {
       const double cf_mf = f->cf_mf[p];                                /* :288-305 */
       double w1m = f->rc_mf[p] / dt, w2m = f->ri_mf[p] / dt;

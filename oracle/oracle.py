@@ -72,13 +72,17 @@ def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
 
 
-def ice_adjust(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float) -> Dict[str, np.ndarray]:
-    """Oracle ice_adjust; returns the 16 outputs keyed by name."""
+def ice_adjust(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, srcs: bool = False
+               ) -> Dict[str, np.ndarray]:
+    """Oracle ice_adjust; returns the 16 outputs keyed by name (and "srcs",
+    PSRCS, when asked)."""
     lib = load()
     ins = {k: _f64(st[k]) for k in IA_IN}
     nk, nij = ins["pabs"].shape
     io = {k: _f64(st[k]).copy() for k in IA_INOUT}
     out = {k: np.empty((nk, nij)) for k in IA_OUT}
+    if srcs:
+        out["srcs"] = np.empty((nk, nij))
     f = IceAdjustFields()
     for k, v in {**ins, **io, **out}.items():
         setattr(f, k, _ptr(v))
@@ -87,6 +91,14 @@ def ice_adjust(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float) -> D
     if rc != 0:
         raise RuntimeError(f"oracle ice_adjust returned {rc}")
     return {**out, **io}
+
+
+def src_1d() -> np.ndarray:
+    """The oracle's SRC_1D table (condensation.F90 index -22..11)."""
+    lib = load()
+    lib.ice3o_src_1d.restype = ctypes.c_double
+    lib.ice3o_src_1d.argtypes = [ctypes.c_int]
+    return np.array([lib.ice3o_src_1d(i) for i in range(-22, 12)])
 
 
 def sedimentation(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, fortran: bool,

@@ -9,6 +9,7 @@ through the numpy stand-in of refshim.py:
 * ``ice4_derived_fields`` / ``ice4_slope_parameters`` (stencils/ice4_tendencies.py:191,248)
 * ``ice4_rainfr_vert``                 (stencils/rain_ice.py:272)
 * ``ice4_warm`` with the CLFR / PRFR evaporation options (stencils/ice4_warm.py:15)
+* the SRC_1D table                     (phyex_common/lookup_table.py:4)
 
 Inputs are seeded synthetic states (ice3gb.state.make_state) and seeded
 random point sets; both inputs and reference outputs are stored.
@@ -233,6 +234,12 @@ def warm_subg_case(mods, Phyex):
     return {"warm_subg": rec}
 
 
+def src_1d_case():
+    """The SRC_1D table of the reference (src/ice3/phyex_common/lookup_table.py:4)."""
+    from ice3.phyex_common.lookup_table import SRC_1D
+    return {"src_1d": {"SRC_1D": np.asarray(SRC_1D, dtype=np.float64)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-src", default="/root/reference/src")
@@ -265,6 +272,7 @@ def main():
     blobs.update(sedimentation_case(sedimentation_stat, Phyex))
     blobs.update(process_cases(mods, Phyex))
     blobs.update(warm_subg_case(mods, Phyex))
+    blobs.update(src_1d_case())
     for name, rec in blobs.items():
         if args.only is not None and name not in args.only:
             continue

@@ -40,3 +40,16 @@ extern "C" void ia_vjp_host(const Ice3gbConstants *c, double dt, long n, const d
     for (int k = 0; k < 20; ++k) gin[k][p] = bv[k];
   }
 }
+
+// PSRCS (s'r_c'/sigma_s^2) of each point, as the forward kernel's SRC
+// instantiation writes it.
+extern "C" void ia_srcs_host(const Ice3gbConstants *c, double dt, long n, const double *const *in, double *srcs)
+{
+  const IaDerived d = ia_derived(*c);
+  for (long p = 0; p < n; ++p) {
+    IaIn x;
+    gather_in(in, p, x);
+    IaOut o;
+    ia_point(*c, d, dt, 1.0 / dt, x, o, srcs + p);
+  }
+}

@@ -214,6 +214,7 @@ struct RiScratch {
   unsigned int *order;     // [n] processing order, or NULL (index order)
   bool clear_key_max;      // false: the caller cleared it once for several calls
   bool evap_fixup;         // false: the caller runs the fix-up after the last call
+  bool may_alloc = true;   // false: no stream-ordered allocation (SPLI sedimentation refused)
 };
 
 // The learned slow rates of a surrogate-assisted rain_ice call.
@@ -314,9 +315,33 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   sf.fpr_c = f->fpr_c; sf.fpr_r = f->fpr_r; sf.fpr_i = f->fpr_i; sf.fpr_s = f->fpr_s; sf.fpr_g = f->fpr_g;
   const SedArgs sa = sed_args(sf, nij, nk, dt, sed_fortran);
   cudaError_t e;
-  if (!lsedim_after) {
+  // SEDIM: 1 = STAT (statistical), 0 = SPLI (time-split, needs 2 n doubles of scratch)
+  const bool spli = (int)c.SEDIM == 0;
+  if (spli && !rs.may_alloc)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "SEDIM=SPLI needs scratch memory: not available in this entry point");
+  auto sediment = [&]() -> int {
     ProfScope ps(h, K_SEDIM, s);
-    if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+    if (!spli) {
+      cudaError_t e2 = launch_sedimentation(c, sa, s);
+      return e2 == cudaSuccess ? ICE3GB_OK : cuda_fail(h, e2, "sedimentation launch");
+    }
+    SplitArgs sp;
+    sp.sed = sa;
+    sp.rt[0] = f->rct; sp.rt[1] = f->rrt; sp.rt[2] = f->rit; sp.rt[3] = f->rst; sp.rt[4] = f->rgt;
+    sp.rvt = f->rvt; sp.exn = f->exn; sp.rvs = f->rvs; sp.ths = f->ths;
+    sp.status = h->d_status;
+    sp.max_iter = 10000;
+    double *scr = nullptr;
+    cudaError_t e2 = cudaMallocAsync(&scr, sizeof(double) * 2 * (size_t)nij * nk, s);
+    if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaMallocAsync");
+    sp.scratch = scr;
+    e2 = launch_sedimentation_split(c, sp, s);
+    cudaFreeAsync(scr, s);
+    return e2 == cudaSuccess ? ICE3GB_OK : cuda_fail(h, e2, "sedimentation (SPLI) launch");
+  };
+  if (!lsedim_after) {
+    const int rc = sediment();
+    if (rc != ICE3GB_OK) return rc;
   }
   if ((e = cudaMemsetAsync(rs.chunk, 0, sizeof(unsigned int), s)) != cudaSuccess ||
       (rs.clear_key_max && (e = cudaMemsetAsync(rs.key_max, 0, sizeof(unsigned int), s)) != cudaSuccess))
@@ -352,8 +377,8 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   }
   if (e != cudaSuccess) return cuda_fail(h, e, "rain_ice launch");
   if (lsedim_after) {
-    ProfScope ps(h, K_SEDIM, s);
-    if ((e = launch_sedimentation(c, sa, s)) != cudaSuccess) return cuda_fail(h, e, "sedimentation launch");
+    const int rc = sediment();
+    if (rc != ICE3GB_OK) return rc;
   }
   if (ldeposc || f->indep) {
     ProfScope ps(h, K_FOG, s);
@@ -686,7 +711,7 @@ int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double 
                 (long)nij * nk, scratch_points);
   if ((rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
   if (!scratch) return fail(h, ICE3GB_ERR_CUDA, "static scratch address unavailable");
-  const RiScratch rs = {scratch, scratch + 1, scratch + 4, nullptr, true, true};
+  const RiScratch rs = {scratch, scratch + 1, scratch + 4, nullptr, true, true, false};
   return run_rain_ice_core(h, nij, nk, dt, opt, f, rs, static_cast<cudaStream_t>(stream));
 }
 
@@ -750,6 +775,8 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   if ((int)c->NRR != 6) snprintf(why, sizeof(why), "rain_ice supports NRR=6 only (got %g)", c->NRR);
   else if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)
     snprintf(why, sizeof(why), "rain_ice: MRSTEP/TSTEP_TS time-splitting is not supported");
+  else if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1)
+    snprintf(why, sizeof(why), "rain_ice: SEDIM must be SPLI (0) or STAT (1), got %g", c->SEDIM);
   else if (((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) ||
            (int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2)
     snprintf(why, sizeof(why), "rain_ice: SUBG_RC_RR_ACCR must be NONE or PRFR, SUBG_RR_EVAP NONE, CLFR or PRFR");

@@ -17,6 +17,16 @@ struct SedArgs {
   int fortran;
 };
 
+// Time-split sedimentation (SEDIM = SPLI) of a rain_ice call.
+struct SplitArgs {
+  SedArgs sed;                     // geometry, sources, outputs, sea/town
+  const double *rt[5], *rvt, *exn; // mixing ratios at t, exner
+  double *rvs, *ths;               // in-out (negativity correction)
+  double *scratch;                 // 2 * nij * nk doubles
+  unsigned int *status;            // ICE3GB_DEV_SED_CAP
+  int max_iter;
+};
+
 struct FogArgs {
   const double *rct, *rhodref, *dzz;
   double *rcs, *inprc, *indep;
@@ -161,6 +171,7 @@ cudaError_t launch_rain_ice_evap_fixup(const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_order(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 size_t rain_ice_smem_bytes();
 
+cudaError_t launch_sedimentation_split(const Ice3gbConstants &c, const SplitArgs &a, cudaStream_t s);
 // Precipitation fraction of a rain_ice call with a PRFR option (before the point kernel).
 cudaError_t launch_rain_ice_prfr(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_surrogate_sample(const Ice3gbConstants &c, const SurSampleArgs &a, int num_sms, cudaStream_t s);

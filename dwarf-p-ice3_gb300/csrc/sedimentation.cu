@@ -46,6 +46,32 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constan
 }
 
 // Fog deposition on the lowest level (rain_ice.F90:876-895).
+// SEDIM = SPLI: one column per thread (sed_split_column).
+__global__ void __launch_bounds__(128) sedimentation_split_kernel(const __grid_constant__ Cst c,
+                                                                  const __grid_constant__ SplitArgs a)
+{
+  const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (col >= a.sed.nij) return;
+  const bool has_st = a.sed.sea != nullptr && a.sed.town != nullptr;
+  const double sea = has_st ? a.sed.sea[col] : 0.0, town = has_st ? a.sed.town[col] : 0.0;
+  const CloudPar cp = cloud_params(c, true, has_st, sea, town);
+  const long n = (long)a.sed.nij * a.sed.nk;
+  SplitColumnIO io;
+  io.rhodref = a.sed.rhodref; io.dzz = a.sed.dzz; io.pabs = a.sed.pabs; io.tht = a.sed.tht; io.exn = a.exn;
+  io.rvt = a.rvt; io.rvs = a.rvs; io.ths = a.ths;
+  for (int s = 0; s < 5; ++s) {
+    io.rt[s] = a.rt[s];
+    io.src[s] = a.sed.src[s];
+    io.fpr[s] = a.sed.fpr[s];
+    io.inpr[s] = a.sed.inpr[s];
+  }
+  io.rtmp = a.scratch;
+  io.ext = a.scratch + n;
+  io.nij = a.sed.nij;
+  io.nk = a.sed.nk;
+  if (!sed_split_column(c, cp, a.sed.dt, io, col, a.max_iter)) atomicOr(a.status, ICE3GB_DEV_SED_CAP);
+}
+
 __global__ void fog_deposition_kernel(const __grid_constant__ Cst c, FogArgs a)
 {
   const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -68,6 +94,14 @@ cudaError_t launch_sedimentation(const Cst &c, const SedArgs &a, cudaStream_t s)
   const long n = a.nij;
   const int threads = 128;
   sedimentation_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sedimentation_split(const Cst &c, const SplitArgs &a, cudaStream_t s)
+{
+  const long n = a.sed.nij;
+  const int threads = 128;
+  sedimentation_split_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(c, a);
   return cudaGetLastError();
 }
 

@@ -323,4 +323,139 @@ ICE3_HD void sed_column_vjp(const Cst &c, bool fortran, bool skip_c, const Cloud
   }
 }
 
+// ---- time-split sedimentation (SEDIM = SPLI) ------------------------------
+// mode_ice4_sedimentation_split.F90 (INTERNAL_SEDIM_SPLI, without the
+// electric charges and the Beard velocity correction) and the negativity
+// correction that ICE4_SEDIMENTATION applies after it
+// (mode_ice4_sedimentation.F90:196-229).  Per species, in CFL-limited
+// sub-steps until the time step is used up: the flux of each level from the
+// temporary mixing ratio (initialised with the value at t), the column's
+// sub-step = min(remaining time, SPLIT_MAXCFL rho r dz / flux), then the
+// temporary mixing ratio moves by the flux divergence plus its external
+// tendency (source - r_t / dt) over the sub-step and the source by the flux
+// divergence.
+struct SplitColumnIO {
+  const double *rhodref, *dzz, *pabs, *tht, *exn;
+  const double *rt[5];       // mixing ratios at t: rc rr ri rs rg
+  const double *rvt;
+  double *src[5];            // in-out sources rcs rrs ris rss rgs
+  double *rvs, *ths;         // in-out (negativity correction)
+  double *fpr[5];            // accumulated fluxes, or NULL
+  double *inpr[5];           // [nij]
+  double *rtmp, *ext;        // [nk][nij] scratch: temporary mixing ratio, external tendency
+  long nij;
+  int nk;
+};
+
+// Flux rho r v(r) of species s at content r (0 below the species' threshold;
+// ice: max(XRTMIN, 1e-7)), INTERNAL_SEDIM_SPLI :500-700.
+ICE3_HD double split_flux(const Cst &c, int s, double r, double rho, double lrho, double p, double th,
+                          const CloudPar &cp)
+{
+  if (!gtp(r, sed_rtmin(c, s))) return 0.0;
+  double wlbda = 0.0;
+  if (s == 0) {
+    // ZZT = theta (p / P00)^(RD/CPD): the temperature (:520)
+    const double t = th * fm::fexp((c.RD / c.CPD) * fm::flog(fm::fdiv(p, c.P00)));
+    wlbda = 6.6e-8 * fm::fdiv(101325.0, p) * (t * (1.0 / 293.15));
+  }
+  return fall_speed(c, s, r, lrho, wlbda, cp) * rho * r;
+}
+
+// ICE4_CORRECT_NEGATIVITIES on the sources (mode_ice4_correct_negativities.F90)
+// with the latent-heat factors lv / ls.
+ICE3_HD void correct_negativities(const Cst &c, double lv, double ls, double &ths, double &rvs, double &rcs,
+                                  double &rrs, double &ris, double &rss, double &rgs)
+{
+  double w;
+  w = rcs - pmax0(rcs); rvs += w; ths -= w * lv; rcs -= w;
+  w = rrs - pmax0(rrs); rvs += w; ths -= w * lv; rrs -= w;
+  w = ris - pmax0(ris); rvs += w; ths -= w * ls; ris -= w;
+  w = rss - pmax0(rss); rvs += w; ths -= w * ls; rss -= w;
+  w = rgs - pmax0(rgs); rvs += w; ths -= w * ls; rgs -= w;
+  w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
+  ths -= w * (rcs * lv + ris * ls);
+  rvs += w * (rcs + ris);
+  rcs = (1. - w) * rcs;
+  ris = (1. - w) * ris;
+  w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lv;
+  w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * ls;
+  w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * ls;
+}
+
+// One column; returns false if a species needed more than max_iter sub-steps
+// (the sub-stepping then stops for that species).
+ICE3_HD bool sed_split_column(const Cst &c, const CloudPar &cp, double dt, const SplitColumnIO &io, long col,
+                              int max_iter)
+{
+  const double inv_dt = 1.0 / dt;
+  bool ok = true;
+  for (int s = 0; s < 5; ++s) {
+    if (s == 0 && c.LSEDIC == 0.0) {          // GSEDIC = .FALSE.: cloud not sedimented
+      if (io.inpr[0]) io.inpr[0][col] = 0.0;
+      if (io.fpr[0])
+        for (int k = 0; k < io.nk; ++k) io.fpr[0][(long)k * io.nij + col] = 0.0;
+      continue;
+    }
+    const double rtmin = s == 0 ? c.C_RTMIN : s == 1 ? c.R_RTMIN : s == 2 ? c.I_RTMIN : s == 3 ? c.S_RTMIN : c.G_RTMIN;
+    for (int k = 0; k < io.nk; ++k) {
+      const long p = (long)k * io.nij + col;
+      const double r = sed_load(io.rt[s], p);
+      io.rtmp[p] = r;
+      io.ext[p] = io.src[s][p] - r * inv_dt;    // ZPR.S (:180-190)
+      if (io.fpr[s]) io.fpr[s][p] = 0.0;
+    }
+    double remaint = dt, inpr = 0.0;
+    int it = 0;
+    while (gtp(remaint, 0.0)) {
+      if (++it > max_iter) { ok = false; break; }
+      // the column's sub-step (:780-805)
+      double mt = remaint;
+      for (int k = 0; k < io.nk; ++k) {
+        const long p = (long)k * io.nij + col;
+        const double r = io.rtmp[p];
+        if (!gtp(r, rtmin)) continue;
+        const double rho = sed_load(io.rhodref, p);
+        const double w = split_flux(c, s, r, rho, fm::flog(rho), sed_load(io.pabs, p), sed_load(io.tht, p), cp);
+        if (gtp(w, 1.e-20)) mt = dmin(mt, fm::fdiv(c.SPLIT_MAXCFL * rho * r * sed_load(io.dzz, p), w));
+      }
+      remaint -= mt;
+      // update, top-down with the flux of the level above (:806-830)
+      const double frac = mt * inv_dt;
+      double wa = 0.0;
+      for (int k = io.nk - 1; k >= 0; --k) {
+        const long p = (long)k * io.nij + col;
+        const double r = io.rtmp[p];
+        const double rho = sed_load(io.rhodref, p);
+        const double w = gtp(r, sed_rtmin(c, s))
+                             ? split_flux(c, s, r, rho, fm::flog(rho), sed_load(io.pabs, p), sed_load(io.tht, p), cp)
+                             : 0.0;
+        const double change = mt * fm::fdiv(1.0, rho * sed_load(io.dzz, p)) * (wa - w);
+        io.rtmp[p] = r + change + io.ext[p] * mt;
+        io.src[s][p] += change * inv_dt;
+        if (io.fpr[s]) io.fpr[s][p] += w * frac;
+        if (k == 0) inpr += w / c.RHOLW * frac;
+        wa = w;
+      }
+    }
+    if (io.inpr[s]) io.inpr[s][col] = inpr;
+  }
+  // ICE4_CORRECT_NEGATIVITIES with L/cph of the time-t state (rain_ice.F90:334-345)
+  for (int k = 0; k < io.nk; ++k) {
+    const long p = (long)k * io.nij + col;
+    const double rv = sed_load(io.rvt, p), rc = sed_load(io.rt[0], p), rr = sed_load(io.rt[1], p);
+    const double ri = sed_load(io.rt[2], p), rs = sed_load(io.rt[3], p), rg = sed_load(io.rt[4], p);
+    const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
+    const double t = sed_load(io.tht, p) * sed_load(io.exn, p);
+    const double ls = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
+    const double lv = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
+    double ths = io.ths[p], rvs = io.rvs[p], rcs = io.src[0][p], rrs = io.src[1][p], ris = io.src[2][p];
+    double rss = io.src[3][p], rgs = io.src[4][p];
+    correct_negativities(c, lv, ls, ths, rvs, rcs, rrs, ris, rss, rgs);
+    io.ths[p] = ths; io.rvs[p] = rvs; io.src[0][p] = rcs; io.src[1][p] = rrs; io.src[2][p] = ris;
+    io.src[3][p] = rss; io.src[4][p] = rgs;
+  }
+  return ok;
+}
+
 }  // namespace ice3sed

@@ -56,6 +56,7 @@ extern "C" {
 
 /* Device status word bits (read by ice3gb_status). */
 #define ICE3GB_DEV_PASS_CAP     1u /* a point hit the sub-step pass cap     */
+#define ICE3GB_DEV_SED_CAP      2u /* a column hit the SPLI sub-step cap    */
 
 /*
  * Constants table: every field is a double (switches stored as 0.0/1.0,
@@ -76,7 +77,7 @@ extern "C" {
   X(LEVLIMIT) X(LNULLWETG) X(LWETGPOST) X(SNOW_RIMING) X(LCRFLIMIT)           \
   X(NMAXITER_MICRO) X(MRSTEP) X(TSTEP_TS) X(SUBG_RC_RR_ACCR) X(SUBG_RR_EVAP)  \
   X(SUBG_PR_PDF) X(SUBG_AUCV_RC) X(SUBG_AUCV_RI) X(SUBG_MF_PDF)               \
-  X(LSEDIM_AFTER) X(LSNOW_T)                                                  \
+  X(LSEDIM_AFTER) X(LSNOW_T) X(SPLIT_MAXCFL)                                  \
   /* hydrometeor descriptors (modd_rain_ice_descrn) */                        \
   X(CEXVT) X(V_RTMIN) X(C_RTMIN) X(R_RTMIN) X(I_RTMIN) X(S_RTMIN) X(G_RTMIN)  \
   X(CC) X(DC) X(LBEXC) X(LBC_1) X(LBC_2) X(LBR) X(LBEXR) X(LBI) X(LBEXI)      \
@@ -241,10 +242,15 @@ int ice3gb_status(void *handle, void *stream, uint32_t *bits);
 /* Replaces c_ice_adjust (phyex_bridge.F90:27) / IceAdjustJAX.__call__. */
 int ice3gb_ice_adjust(void *handle, int nij, int nk, double dt,
                       const Ice3gbIceAdjustFields *f, void *stream);
-/* Replaces sedimentation_stat (stencils/sedimentation.py:58). */
+/* Replaces sedimentation_stat (stencils/sedimentation.py:58); the statistical
+ * scheme whatever the table's SEDIM. */
 int ice3gb_sedimentation(void *handle, int nij, int nk, double dt,
                          const Ice3gbSedimentationFields *f, void *stream);
-/* Replaces c_rain_ice (phyex_bridge.F90:242) / RainIceJAX.__call__. */
+/* Replaces c_rain_ice (phyex_bridge.F90:242) / RainIceJAX.__call__.  The
+ * table's SEDIM picks the sedimentation: STAT (1) or SPLI (0, time-split,
+ * micro/mode_ice4_sedimentation_split.F90, followed by
+ * ICE4_CORRECT_NEGATIVITIES, micro/mode_ice4_sedimentation.F90:196-229;
+ * allocates 2 nij*nk doubles of stream-ordered scratch). */
 int ice3gb_rain_ice(void *handle, int nij, int nk, double dt,
                     const Ice3gbRainIceOptions *opt,
                     const Ice3gbRainIceFields *f, void *stream);
@@ -408,7 +414,9 @@ int ice3gb_physics_step_surrogate(void *handle, void *mlp, int nij, int nk, doub
  * rejected with ICE3GB_ERR_RANGE.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress), so make it before any
  * stream capture.  Calls that overlap on the GPU share the array and race:
- * serialise them.  No counterpart exists in the reference. */
+ * serialise them.  A table with SEDIM = SPLI (0) is refused with
+ * ICE3GB_ERR_UNSUPPORTED: the time-split sedimentation needs 2 nij*nk doubles
+ * of stream-ordered scratch.  No counterpart exists in the reference. */
 #define ICE3GB_NOALLOC_MAX_POINTS 4194304
 int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                             const Ice3gbRainIceFields *f, void *stream);

@@ -306,6 +306,137 @@ static void sed_column(const C *c, int nij, int nk, double dt, long col, int for
   for (int s = 0; s < 5; ++s) inpr[s] = fabove[s] / c->RHOLW;   /* :344-348 / F90:213-223 */
 }
 
+/* Time-split sedimentation (SEDIM = SPLI) of one column:
+ * mode_ice4_sedimentation_split.F90 INTERNAL_SEDIM_SPLI (without electric
+ * charges / Beard correction), species in the order c r i s g, then
+ * ICE4_CORRECT_NEGATIVITIES with L/cph of the time-t state
+ * (mode_ice4_sedimentation.F90:196-229, the factors rain_ice.F90:334-345
+ * passes).  rt: mixing ratios at t; returns 0 if a species needed more
+ * than max_iter sub-steps. */
+static int sed_split_column(const C *c, int nij, int nk, double dt, long col, const double *rho,
+                            const double *dzz, const double *pabs, const double *tht, const double *exn,
+                            double sea, double town, int has_sea_town, const double *rt[5], const double *rvt,
+                            double *src[5], double *rvs, double *ths, double *fpr[5], double inpr[5], int max_iter)
+{
+  const double rtmin[5] = {c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN};
+  const double gac_gc = c->GAC / c->GC, gac2_gc2 = c->GAC2 / c->GC2;
+  double lbc, fsedc, conc, ray;                                   /* :120-165, rain_ice.F90:396-420 */
+  if (has_sea_town) {
+    ray = dmax(1.0, 0.5 * ((1.0 - sea) * gac_gc + sea * gac2_gc2));
+    lbc = dmax(dmin(c->LBC_1, c->LBC_2), sea * c->LBC_2 + (1.0 - sea) * c->LBC_1);
+    fsedc = dmax(dmin(c->FSEDC_1, c->FSEDC_2), sea * c->FSEDC_2 + (1.0 - sea) * c->FSEDC_1);
+    conc = (1.0 - town) * (sea * c->CONC_SEA + (1.0 - sea) * c->CONC_LAND) + town * c->CONC_URBAN;
+  } else {
+    ray = dmax(1.0, 0.5 * gac_gc);
+    lbc = c->LBC_1;
+    fsedc = c->FSEDC_1;
+    conc = c->CONC_LAND;
+  }
+  const double fsed[5] = {0.0, c->FSEDR, 0.0, c->FSEDS, c->FSEDG};
+  const double exsed[5] = {0.0, c->EXSEDR, 0.0, c->EXSEDS, c->EXSEDG};
+  const double thr[5] = {c->C_RTMIN, c->R_RTMIN, dmax(c->I_RTMIN, 1.0e-7), c->S_RTMIN, c->G_RTMIN};
+  double *rx = (double *)malloc(sizeof(double) * 3 * (size_t)nk);
+  double *ext = rx + nk, *w = rx + 2 * nk;
+  int ok = 1;
+  for (int s = 0; s < 5; ++s) {
+    if (s == 0 && c->LSEDIC == 0.0) {
+      inpr[0] = 0.0;
+      if (fpr[0]) for (int k = 0; k < nk; ++k) fpr[0][(long)k * nij + col] = 0.0;
+      continue;
+    }
+    for (int k = 0; k < nk; ++k) {                               /* :170-200 */
+      const long p = (long)k * nij + col;
+      rx[k] = rt[s][p];
+      ext[k] = src[s][p] - rt[s][p] / dt;
+      if (fpr[s]) fpr[s][p] = 0.0;
+    }
+    double remaint = dt;
+    inpr[s] = 0.0;
+    int it = 0;
+    while (remaint > 0.0) {
+      if (++it > max_iter) { ok = 0; break; }
+      for (int k = 0; k < nk; ++k) {                             /* fluxes :500-760 */
+        const long p = (long)k * nij + col;
+        w[k] = 0.0;
+        if (rx[k] > thr[s]) {
+          double v;
+          if (s == 0) {
+            const double t = tht[p] * pow(pabs[p] / c->P00, c->RD / c->CPD);
+            const double wlbda = 6.6e-8 * (101325.0 / pabs[p]) * (t / 293.15);
+            v = sed_cloud(c, rx[k], rho[p], wlbda, lbc, conc, ray, fsedc);
+          } else if (s == 2) {
+            v = sed_ice(c, rx[k], rho[p]);
+          } else {
+            v = sed_other(fsed[s], exsed[s], rx[k], rho[p], c->CEXVT);
+          }
+          w[k] = v * rho[p] * rx[k];
+        }
+      }
+      double mt = remaint;                                       /* :770-805 */
+      for (int k = 0; k < nk; ++k) {
+        const long p = (long)k * nij + col;
+        if (rx[k] > rtmin[s] && w[k] > 1.e-20) mt = dmin(mt, c->SPLIT_MAXCFL * rho[p] * rx[k] * dzz[p] / w[k]);
+      }
+      remaint -= mt;
+      inpr[s] += w[0] / c->RHOLW * (mt / dt);
+      for (int k = 0; k < nk; ++k) {                             /* :806-830 */
+        const long p = (long)k * nij + col;
+        const double wa = k + 1 < nk ? w[k + 1] : 0.0;
+        const double change = mt * (1.0 / (rho[p] * dzz[p])) * (wa - w[k]);
+        rx[k] = rx[k] + change + ext[k] * mt;
+        src[s][p] += change / dt;
+        if (fpr[s]) fpr[s][p] += w[k] * (mt / dt);
+      }
+    }
+  }
+  free(rx);
+  for (int k = 0; k < nk; ++k) {                                 /* ICE4_CORRECT_NEGATIVITIES */
+    const long p = (long)k * nij + col;
+    const double zdev = c->CPD + c->CPV * rvt[p] + c->CL * (rt[0][p] + rt[1][p]) +
+                        c->CI * (rt[2][p] + rt[3][p] + rt[4][p]);
+    const double t = tht[p] * exn[p];
+    const double ls = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
+    const double lv = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
+    double rv = rvs[p], rc = src[0][p], rr = src[1][p], ri = src[2][p], rs = src[3][p], rg = src[4][p];
+    double th = ths[p], ww;
+    ww = rc - dmax(rc, 0.); rv += ww; th -= ww * lv; rc -= ww;
+    ww = rr - dmax(rr, 0.); rv += ww; th -= ww * lv; rr -= ww;
+    ww = ri - dmax(ri, 0.); rv += ww; th -= ww * ls; ri -= ww;
+    ww = rs - dmax(rs, 0.); rv += ww; th -= ww * ls; rs -= ww;
+    ww = rg - dmax(rg, 0.); rv += ww; th -= ww * ls; rg -= ww;
+    ww = dmin(1., dmax(c->V_RTMIN - rv, 0.) / dmax(rc + ri, 1.e-20));
+    th -= ww * (rc * lv + ri * ls);
+    rv += ww * (rc + ri);
+    rc = (1. - ww) * rc;
+    ri = (1. - ww) * ri;
+    ww = dmin(dmax(rr, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rr -= ww; th -= ww * lv;
+    ww = dmin(dmax(rs, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rs -= ww; th -= ww * ls;
+    ww = dmin(dmax(rg, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rg -= ww; th -= ww * ls;
+    rvs[p] = rv; src[0][p] = rc; src[1][p] = rr; src[2][p] = ri; src[3][p] = rs; src[4][p] = rg; ths[p] = th;
+  }
+  return ok;
+}
+
+/* SPLI sedimentation + negativity correction alone on a rain_ice field set
+ * (the ICE4_SEDIMENTATION call of rain_ice with SEDIM = SPLI). */
+EXPORT int ice3o_sedimentation_split(const C *c, int nij, int nk, double dt, const Ice3gbRainIceFields *f)
+{
+  const int has = f->sea != NULL && f->town != NULL;
+  int ok = 1;
+#pragma omp parallel for schedule(static) reduction(& : ok)
+  for (long col = 0; col < nij; ++col) {
+    double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
+    double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
+    const double *rt[5] = {f->rct, f->rrt, f->rit, f->rst, f->rgt};
+    double inpr[5];
+    ok &= sed_split_column(c, nij, nk, dt, col, f->rhodref, f->dzz, f->pabs, f->tht, f->exn, has ? f->sea[col] : 0.0,
+                           has ? f->town[col] : 0.0, has, rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000);
+    f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
+    f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+  }
+  return ok;
+}
+
 EXPORT int ice3o_sedimentation(const C *c, int nij, int nk, double dt, const Ice3gbSedimentationFields *f)
 {
   if (!c || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
@@ -1122,10 +1253,39 @@ done:
 EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
                               const double *rg);
 
+/* ICE4_SEDIMENTATION of a rain_ice call (mode_ice4_sedimentation.F90:166-229):
+ * STAT on the sources x dt, or SPLI on the mixing ratios at t followed by
+ * the negativity correction.  Returns 0 if an SPLI column hit its sub-step cap. */
+static int rain_ice_sediment(const C *c, int nij, int nk, double dt, int sed_fortran, int has_st,
+                             const Ice3gbRainIceFields *f)
+{
+  int ok = 1;
+  const int spli = (int)c->SEDIM == 0;
+#pragma omp parallel for schedule(static) reduction(& : ok)
+  for (long col = 0; col < nij; ++col) {
+    double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
+    double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
+    double inpr[5];
+    const double sea = f->sea ? f->sea[col] : 0.0, town = f->town ? f->town[col] : 0.0;
+    if (spli) {
+      const double *rt[5] = {f->rct, f->rrt, f->rit, f->rst, f->rgt};
+      ok &= sed_split_column(c, nij, nk, dt, col, f->rhodref, f->dzz, f->pabs, f->tht, f->exn, sea, town, has_st,
+                             rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000);
+    } else {
+      sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht, sea, town, has_st, src,
+                 fpr, inpr);
+    }
+    f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
+    f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+  }
+  return ok;
+}
+
 static int rain_ice_supported(const C *c)
 {
   if ((int)c->NRR != 6) return 0;
   if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0) return 0;
+  if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1) return 0;                    /* SPLI, STAT */
   if ((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) return 0;  /* NONE, PRFR */
   if ((int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2) return 0;          /* NONE, CLFR, PRFR */
   return 1;
@@ -1154,18 +1314,8 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
   int capped_any = 0;
 
   /* 2. sedimentation before the microphysics (rain_ice.F90:442-462 -> ICE4_SEDIMENTATION) */
-  if (!lsedim_after) {
-#pragma omp parallel for schedule(static)
-    for (long col = 0; col < nij; ++col) {
-      double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
-      double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
-      double inpr[5];
-      sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht,
-                 f->sea ? f->sea[col] : 0.0, f->town ? f->town[col] : 0.0, has_st, src, fpr, inpr);
-      f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
-      f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
-    }
-  }
+  int sed_capped = 0;
+  if (!lsedim_after) sed_capped |= !rain_ice_sediment(c, nij, nk, dt, sed_fortran, has_st, f);
 
   /* 4.2 precipitation fraction (rain_ice.F90:555-605): with a PRFR option,
    * ICE4_COMPUTE_PDF on the time-t state of the LLMICRO points (its
@@ -1293,18 +1443,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     f->ths[p] = th;
   }
   /* 9. sedimentation after (rain_ice.F90:816-841) */
-  if (lsedim_after) {
-#pragma omp parallel for schedule(static)
-    for (long col = 0; col < nij; ++col) {
-      double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
-      double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
-      double inpr[5];
-      sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht,
-                 f->sea ? f->sea[col] : 0.0, f->town ? f->town[col] : 0.0, has_st, src, fpr, inpr);
-      f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
-      f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
-    }
-  }
+  if (lsedim_after) sed_capped |= !rain_ice_sediment(c, nij, nk, dt, sed_fortran, has_st, f);
   /* 10. fog deposition (rain_ice.F90:876-895), level k = 0 */
   for (long col = 0; col < nij; ++col) {
     if (ldeposc) {
@@ -1317,7 +1456,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     }
   }
   free(lsf); free(lvf); free(rvheni); free(key);
-  if (status_bits) *status_bits = capped_any ? ICE3GB_DEV_PASS_CAP : 0u;
+  if (status_bits) *status_bits = (capped_any ? ICE3GB_DEV_PASS_CAP : 0u) | (sed_capped ? ICE3GB_DEV_SED_CAP : 0u);
   return ICE3GB_OK;
 }
 

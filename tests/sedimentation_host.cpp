@@ -59,3 +59,28 @@ extern "C" void sed_vjp_host(const Ice3gbConstants *c, int nij, int nk, double d
     sed_column_vjp(*c, fortran != 0, skip_c, cp, dt, io, flux, g, gx, col);
   }
 }
+
+// Host build of the time-split sedimentation (SEDIM = SPLI) and its
+// negativity correction on a rain_ice field set; scratch: 2 nij nk doubles.
+extern "C" int sed_split_host(const Ice3gbConstants *c, int nij, int nk, double dt, const Ice3gbRainIceFields *f,
+                              double *scratch)
+{
+  const bool has_st = f->sea && f->town;
+  int ok = 1;
+  for (long col = 0; col < nij; ++col) {
+    const CloudPar cp = cloud_params(*c, true, has_st, has_st ? f->sea[col] : 0.0, has_st ? f->town[col] : 0.0);
+    SplitColumnIO io;
+    io.rhodref = f->rhodref; io.dzz = f->dzz; io.pabs = f->pabs; io.tht = f->tht; io.exn = f->exn;
+    io.rt[0] = f->rct; io.rt[1] = f->rrt; io.rt[2] = f->rit; io.rt[3] = f->rst; io.rt[4] = f->rgt;
+    io.rvt = f->rvt; io.rvs = f->rvs; io.ths = f->ths;
+    io.src[0] = f->rcs; io.src[1] = f->rrs; io.src[2] = f->ris; io.src[3] = f->rss; io.src[4] = f->rgs;
+    io.fpr[0] = f->fpr_c; io.fpr[1] = f->fpr_r; io.fpr[2] = f->fpr_i; io.fpr[3] = f->fpr_s; io.fpr[4] = f->fpr_g;
+    io.inpr[0] = f->inprc; io.inpr[1] = f->inprr; io.inpr[2] = f->inpri; io.inpr[3] = f->inprs; io.inpr[4] = f->inprg;
+    io.rtmp = scratch;
+    io.ext = scratch + (long)nij * nk;
+    io.nij = nij;
+    io.nk = nk;
+    ok &= sed_split_column(*c, cp, dt, io, col, 10000) ? 1 : 0;
+  }
+  return ok;
+}

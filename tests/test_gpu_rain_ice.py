@@ -298,3 +298,21 @@ def test_rain_ice_subgrid_warm_options_match_oracle(accr, evap, aucv_rc, aucv_ri
     for k in ("hlc_hcf", "hlc_hrc", "hli_hcf", "hli_hri"):
         assert_parity(out[k], ref[k], spread[k], k)
     assert ri.device_status() == 0
+
+
+@pytest.mark.parametrize("lsedim_after", [False, True])
+def test_rain_ice_split_sedimentation_matches_oracle(lsedim_after):
+    """SEDIM = SPLI: the time-split sedimentation column kernel (with its
+    negativity correction) inside rain_ice, before or after the
+    microphysics, against the oracle's RAIN_ICE."""
+    from ice3gb import RainIce
+    from ice3gb.constants import build_table
+    ri = RainIce()
+    ri.table = build_table(table="phyex", overrides={"SEDIM": 0.0})
+    st = _np_state(32 * 32, seed=23)
+    ref, spread = _oracle_ri(ri.table, st, lsedim_after=int(lsedim_after))
+    out = _run_gpu(ri, st, lsedim_after=lsedim_after)
+    _compare(out, ref, spread)
+    assert ri.device_status() == 0
+    assert np.count_nonzero(out["inprr"]) > 100
+

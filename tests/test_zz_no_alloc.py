@@ -89,3 +89,28 @@ def test_noalloc_refuses_grids_above_its_scratch():
     buf = ctypes.create_string_buffer(256)
     lib.ice3gb_last_error(h.h, buf, 256)
     assert b"static scratch" in buf.value
+
+
+def test_noalloc_refuses_time_split_sedimentation():
+    """SEDIM = SPLI takes stream-ordered scratch for its sub-stepped mixing
+    ratios, which this entry point cannot allocate: ICE3GB_ERR_UNSUPPORTED
+    before any launch, and the in-out fields are left as they were."""
+    from ice3gb import _abi
+    from ice3gb.components import Ice3Handle
+    from ice3gb.constants import build_table
+    from ice3gb.state import make_state
+
+    nij = 16 * 16
+    st = make_state(nij, NK, seed=7, precip=True, device="cuda")
+    h = Ice3Handle(build_table(table="phyex", overrides={"SEDIM": 0.0}))
+    opt = _abi.RainIceOptions(-1, -1, -1, 0, 0)
+    f, out = _fields(st, nij)
+    before = out["rrs"].clone()
+    rc = h.lib.ice3gb_rain_ice_noalloc(h.h, nij, NK, DT, ctypes.byref(opt), ctypes.byref(f),
+                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == -5
+    buf = ctypes.create_string_buffer(256)
+    h.lib.ice3gb_last_error(h.h, buf, 256)
+    assert b"SPLI" in buf.value
+    torch.cuda.synchronize()
+    assert torch.equal(out["rrs"], before)

@@ -41,6 +41,7 @@ struct Handle {
   uint32_t magic;
   Ice3gbConstants c;
   double *d_luts;
+  double *d_tiwmx;   // OCND2 saturation tables: ESTABW then ESTABI
   unsigned int *d_status;
   int device, num_sms;
   bool rain_ice_ok;
@@ -137,7 +138,7 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
     if (!(ptr)) return fail(h, ICE3GB_ERR_NULL, "required field %s is NULL", #ptr); \
   } while (0)
 
-int validate_ice_adjust(Handle *h, const Ice3gbIceAdjustFields *f)
+int validate_ice_adjust(Handle *h, const Ice3gbIceAdjustFields *f, int nk)
 {
   if (!f) return fail(h, ICE3GB_ERR_NULL, "fields pointer is NULL");
   REQUIRE(f->sigqsat); REQUIRE(f->pabs); REQUIRE(f->sigs); REQUIRE(f->th); REQUIRE(f->exn);
@@ -148,7 +149,12 @@ int validate_ice_adjust(Handle *h, const Ice3gbIceAdjustFields *f)
   REQUIRE(f->hlc_hrc); REQUIRE(f->hlc_hcf); REQUIRE(f->hli_hri); REQUIRE(f->hli_hcf);
   REQUIRE(f->cph); REQUIRE(f->lv); REQUIRE(f->ls);
   if (h->c.CONDENS != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "CONDENS=%g (only CB02=0)", h->c.CONDENS);
-  if (h->c.OCND2 != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 is not supported");
+  if (h->c.OCND2 != 0.0) {
+    if (h->c.LSUBG_COND == 0.0)
+      return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 needs LSUBG_COND (subgrid condensation)");
+    if (nk < 2) return fail(h, ICE3GB_ERR_SHAPE, "OCND2 needs nk >= 2 (layer thickness), got %d", nk);
+    REQUIRE(f->zz); REQUIRE(f->ice_cld_wgt);
+  }
   return ICE3GB_OK;
 }
 
@@ -751,6 +757,7 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   h->magic = kMagic;
   h->c = *c;
   h->d_luts = nullptr;
+  h->d_tiwmx = nullptr;
   h->d_status = nullptr;
   h->d_stage = nullptr;
   h->stage_cap = 0;
@@ -762,9 +769,17 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   if (e == cudaSuccess) e = cudaMemcpy(h->d_luts, luts, sizeof(Ice3gbLuts), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&h->d_status, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
+  if (e == cudaSuccess && c->OCND2 != 0.0) {
+    std::vector<double> tab(2 * (size_t)kTiwmxTableN);
+    tiwmx_tables(*c, tab.data(), tab.data() + kTiwmxTableN);
+    e = cudaMalloc(&h->d_tiwmx, sizeof(double) * tab.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(h->d_tiwmx, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     int rc = cuda_fail(nullptr, e, "ice3gb_create");
     if (h->d_luts) cudaFree(h->d_luts);
+    if (h->d_tiwmx) cudaFree(h->d_tiwmx);
     if (h->d_status) cudaFree(h->d_status);
     h->magic = 0;
     delete h;
@@ -841,6 +856,7 @@ int ice3gb_destroy(void *handle)
   drop_events(h);
   pipe_free(h);
   cudaFree(h->d_luts);
+  if (h->d_tiwmx) cudaFree(h->d_tiwmx);
   cudaFree(h->d_status);
   if (h->d_stage) cudaFree(h->d_stage);
   h->magic = 0;
@@ -877,12 +893,13 @@ int ice3gb_ice_adjust(void *handle, int nij, int nk, double dt, const Ice3gbIceA
   Handle *h = as_handle(handle);
   if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_ice_adjust: invalid handle");
   int rc;
-  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f)) || (rc = check_device(h))) return rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f, nk)) || (rc = check_device(h))) return rc;
   const long n = (long)nij * nk;
   IaKernelFields kf;
   kf.f = *f;
   kf.rrs = kf.rss = kf.rgs = nullptr;
   kf.adv_dt = 0.0;
+  kf.tiwmx = h->d_tiwmx;
   cudaError_t e;
   {
     ProfScope ps(h, K_ICE_ADJUST, static_cast<cudaStream_t>(stream));
@@ -1092,15 +1109,17 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
   Handle *h = as_handle(handle);
   if (!h) return fail(nullptr, ICE3GB_ERR_HANDLE, "ice3gb_ice_adjust_host: invalid handle");
   int rc;
-  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f)) || (rc = check_device(h))) return rc;
+  if ((rc = check_shape(h, nij, nk)) || (rc = validate_ice_adjust(h, f, nk)) || (rc = check_device(h))) return rc;
   std::lock_guard<std::mutex> lock(h->mu);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t n = (size_t)nij * nk, b3 = n * sizeof(double);
   const size_t bq = (f->sigqsat_3d ? n : (size_t)nij) * sizeof(double);
   const size_t bq_pad = (bq + 255) & ~(size_t)255, b3_pad = (b3 + 255) & ~(size_t)255;
-  // 15 inputs + 4 in-out + 12 outputs (+ srcs)
+  // 15 inputs + 4 in-out + 12 outputs (+ srcs) (+ OCND2: zz, ice_cld_wgt and 5 outputs)
   const int nsrc = f->srcs ? 1 : 0;
-  if ((rc = ensure_stage(h, bq_pad + (31 + nsrc) * b3_pad))) return rc;
+  const bool ocnd2 = h->c.OCND2 != 0.0;
+  const size_t bw_pad = (((size_t)nij * sizeof(double)) + 255) & ~(size_t)255;
+  if ((rc = ensure_stage(h, bq_pad + (31 + nsrc + (ocnd2 ? 6 : 0)) * b3_pad + (ocnd2 ? bw_pad : 0)))) return rc;
   char *base = reinterpret_cast<char *>(h->d_stage);
   Ice3gbIceAdjustFields d;
   std::memset(&d, 0, sizeof(d));
@@ -1128,12 +1147,31 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
     e = cudaMemcpyAsync(slot, *io_src[i], b3, cudaMemcpyHostToDevice, s);
   }
   for (int i = 0; i < 12; ++i, slot += step) *out_dst[i] = slot;
-  if (nsrc) d.srcs = slot;
+  if (nsrc) {
+    d.srcs = slot;
+    slot += step;
+  }
+  double *const *o2_src[] = {&f->icldfr, &f->wcldfr, &f->ssio, &f->ssiu, &f->ifr};
+  double **o2_dst[] = {&d.icldfr, &d.wcldfr, &d.ssio, &d.ssiu, &d.ifr};
+  if (ocnd2) {
+    if (e == cudaSuccess) {
+      d.zz = slot;
+      e = cudaMemcpyAsync(slot, f->zz, b3, cudaMemcpyHostToDevice, s);
+      slot += step;
+    }
+    for (int i = 0; i < 5; ++i, slot += step)
+      if (*o2_src[i]) *o2_dst[i] = slot;
+    if (e == cudaSuccess) {
+      d.ice_cld_wgt = slot;
+      e = cudaMemcpyAsync(slot, f->ice_cld_wgt, (size_t)nij * sizeof(double), cudaMemcpyHostToDevice, s);
+    }
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
   IaKernelFields kf;
   kf.f = d;
   kf.rrs = kf.rss = kf.rgs = nullptr;
   kf.adv_dt = 0.0;
+  kf.tiwmx = h->d_tiwmx;
   {
     ProfScope ps(h, K_ICE_ADJUST, s);
     e = launch_ice_adjust(h->c, kf, nij, nk, dt, ia_vec2_ok(&d, (long)n), h->num_sms, s);
@@ -1143,6 +1181,8 @@ int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt, const Ice3g
   for (int i = 0; i < 12 && e == cudaSuccess; ++i)
     e = cudaMemcpyAsync(*out_src[i], *out_dst[i], b3, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && nsrc) e = cudaMemcpyAsync(f->srcs, d.srcs, b3, cudaMemcpyDeviceToHost, s);
+  for (int i = 0; i < 5 && ocnd2 && e == cudaSuccess; ++i)
+    if (*o2_src[i]) e = cudaMemcpyAsync(*o2_src[i], *o2_dst[i], b3, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(h, e, "device->host copy");
   return ICE3GB_OK;

@@ -84,6 +84,7 @@ struct IaKernelFields {
   Ice3gbIceAdjustFields f;
   const double *rrs, *rss, *rgs;
   double adv_dt;
+  const double *tiwmx;   // OCND2: ESTABW then ESTABI (2 x 24117 doubles)
 };
 
 // ice_adjust adjoint arguments; sigqsat_out receives the per-point sigqsat
@@ -161,6 +162,11 @@ cudaError_t launch_surrogate_loss(const float *y, const float *tgt, int rows, in
 cudaError_t launch_adam(float *w, const float *g, float *m1, float *m2, __nv_bfloat16 *w16, long n, float lr, float b1,
                         float b2, float eps, int step, cudaStream_t s);
 cudaError_t launch_to_bf16(const float *x, __nv_bfloat16 *y, long n, cudaStream_t s);
+
+// OCND2 saturation tables (micro/mode_ini_tiwmx.F90), filled on the host:
+// ESTABW and ESTABI at T = j/100 K, j = 13200..37316 (ice_adjust.cu).
+constexpr int kTiwmxTableN = 24117;
+void tiwmx_tables(const Ice3gbConstants &c, double *estw, double *esti);
 
 cudaError_t launch_ice_adjust(const Ice3gbConstants &c, const IaKernelFields &kf, int nij, int nk, double dt,
                               bool vec2, int num_sms, cudaStream_t s);

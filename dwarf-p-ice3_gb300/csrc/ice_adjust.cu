@@ -5,6 +5,8 @@
 // moves with one 128-bit load/store (LDG.128/STG.128).  Pure map over the
 // nij*nk points: 19 3-D fields read (+ sigqsat per column), 16 written,
 // 280 algorithmic bytes per point.
+#include <cmath>
+
 #include "ice3gb_device.cuh"
 #include "ice3gb_kernels.h"
 #include "ice_adjust_point.cuh"
@@ -107,7 +109,65 @@ __global__ void __launch_bounds__(256) ice_adjust_v1_kernel(const __grid_constan
   }
 }
 
+// OCND2 (separate liquid and ice clouds): one point per thread; the level
+// above (below at the top) gives the layer thickness of ICECLOUD.
+template <bool SRC>
+__global__ void __launch_bounds__(256) ice_adjust_ocnd2_kernel(const __grid_constant__ Cst c,
+                                                               const __grid_constant__ IaKernelFields kf, long n,
+                                                               int nij, int nk, double dt)
+{
+  const Ice3gbIceAdjustFields &f = kf.f;
+  const double inv_dt = 1.0 / dt;
+  const IaDerived d = ia_derived(c);
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
+    IaIn x;
+    x.sigqsat = f.sigqsat_3d ? ld1(f.sigqsat, p) : ld1(f.sigqsat, p % nij);
+    x.pabs = ld1(f.pabs, p); x.sigs = ld1(f.sigs, p); x.exn = ld1(f.exn, p);
+    x.exn_ref = ld1(f.exn_ref, p); x.rho = ld1(f.rho_dry_ref, p);
+    x.cf_mf = ld1(f.cf_mf, p); x.rc_mf = ld1(f.rc_mf, p); x.ri_mf = ld1(f.ri_mf, p);
+    x.rvs = f.rvs[p]; x.rcs = f.rcs[p]; x.ris = f.ris[p]; x.ths = f.ths[p];
+    x.th = ld1(f.th, p); x.rv = ld1(f.rv, p); x.rc = ld1(f.rc, p); x.ri = ld1(f.ri, p);
+    x.rr = ld1(f.rr, p); x.rs = ld1(f.rs, p); x.rg = ld1(f.rg, p);
+    const long k = p / nij, col = p - k * nij;
+    const long kp = k + 1 < nk ? k + 1 : nk - 1;
+    Ocnd2In oi;
+    oi.estw = kf.tiwmx;
+    oi.esti = kf.tiwmx + kTiwmxN;
+    oi.z = ld1(f.zz, p);
+    oi.dz = ld1(f.zz, kp * nij + col) - ld1(f.zz, (kp - 1) * nij + col);
+    oi.ice_cld_wgt = ld1(f.ice_cld_wgt, col);
+    oi.bottom = k == 0;
+    IaOut o;
+    Ocnd2Out oo;
+    double s0 = 0.0;
+    ia_point<true>(c, d, dt, inv_dt, x, o, SRC ? &s0 : nullptr, &oi, &oo);
+    if (SRC) f.srcs[p] = s0;
+#define ST1(field) if (f.field) f.field[p] = o.field;
+    ST1(t) ST1(rv_out) ST1(rc_out) ST1(ri_out) ST1(cldfr) ST1(hlc_hrc) ST1(hlc_hcf) ST1(hli_hri) ST1(hli_hcf)
+    ST1(cph) ST1(lv) ST1(ls) ST1(rvs) ST1(rcs) ST1(ris) ST1(ths)
+#undef ST1
+    if (f.icldfr) f.icldfr[p] = oo.icldfr;
+    if (f.wcldfr) f.wcldfr[p] = oo.wcldfr;
+    if (f.ssio) f.ssio[p] = oo.ssio;
+    if (f.ssiu) f.ssiu[p] = oo.ssiu;
+    if (f.ifr) f.ifr[p] = 10.0;   // PIFR, condensation.F90:259
+  }
+}
+
 }  // namespace
+
+static_assert(kTiwmxTableN == kTiwmxN, "TIWMX table size");
+
+void tiwmx_tables(const Cst &c, double *estw, double *esti)
+{
+  // mode_tiwmx_fun.F90 ESATW / ESATI; INI_TIWMX keeps the water value above 273.15 K
+  for (int j = kTiwmxStart; j <= kTiwmxStop; ++j) {
+    const double t = (double)j / 100.0;
+    const double w = std::exp(c.ALPW - c.BETAW / t - c.GAMW * std::log(t));
+    estw[j - kTiwmxStart] = w;
+    esti[j - kTiwmxStart] = t > 273.15 ? w : std::exp(c.ALPI - c.BETAI / t - c.GAMI * std::log(t));
+  }
+}
 
 cudaError_t launch_ice_adjust(const Cst &c, const IaKernelFields &kf, int nij, int nk, double dt, bool vec2,
                               int num_sms, cudaStream_t s)
@@ -117,7 +177,12 @@ cudaError_t launch_ice_adjust(const Cst &c, const IaKernelFields &kf, int nij, i
   const long cap = (long)num_sms * 64;
   const bool adv = kf.adv_dt != 0.0;
   const bool src = kf.f.srcs != nullptr;
-  if (vec2) {
+  if (c.OCND2 != 0.0) {   // (the host rejects OCND2 with adv_dt)
+    long blocks = (n + threads - 1) / threads;
+    if (blocks > cap) blocks = cap;
+    if (src) ice_adjust_ocnd2_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, nk, dt);
+    else ice_adjust_ocnd2_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(c, kf, n, nij, nk, dt);
+  } else if (vec2) {
     const long npairs = n / 2;
     long blocks = (npairs + threads - 1) / threads;
     if (blocks > cap) blocks = cap;

@@ -73,6 +73,80 @@ ICE3_HD double sigrc_cb(const Cst &c, double q1)
   return r;
 }
 
+// ---- OCND2 (separate liquid and ice clouds) -----------------------------------
+// TIWMX saturation tables (micro/modd_tiwmx.F90, filled by
+// micro/mode_ini_tiwmx.F90): ESTABW(j) = ESATW(j/100 K), ESTABI(j) = the ice
+// formula at and below 273.15 K, the water one above, j = 13200..37316.
+constexpr int kTiwmxStart = 13200, kTiwmxStop = 37316, kTiwmxN = kTiwmxStop - kTiwmxStart + 1;
+
+// ESATW / ESATI (micro/mode_tiwmx.F90): TAB(NINT(100 T)), NINT rounding half
+// away from zero; the index is clamped to the table.
+ICE3_HD double tiwmx_at(const double *tab, double t)
+{
+  long j = (long)round(100.0 * t);
+  j = j < kTiwmxStart ? kTiwmxStart : (j > kTiwmxStop ? kTiwmxStop : j);
+#if defined(__CUDA_ARCH__)
+  return __ldg(tab + (j - kTiwmxStart));
+#else
+  return tab[j - kTiwmxStart];
+#endif
+}
+
+// Per-point inputs of the OCND2 branch and its extra outputs.
+struct Ocnd2In {
+  const double *estw, *esti;   // TIWMX tables
+  double z, dz;                // height of the level; thickness to the level above (below at the top)
+  double ice_cld_wgt;
+  bool bottom;                 // k = 0 (condensation.F90:619, JK == IKTB)
+};
+struct Ocnd2Out {
+  double icldfr, wcldfr, ssio, ssiu;
+};
+
+// ICECLOUD (micro/mode_icecloud.F90) as CONDENSATION calls it
+// (condensation.F90:381-385: PTSTEP = 1, PPBLH = -1, PWCLD = -1, XW2D = 10;
+// W2D and RSI are not used): ice cloud fraction and ice super-saturations.
+ICE3_HD void icecloud(const Cst &c, double p, double z, double dz, double t, double r, double esw, double esi,
+                      double &sifrc, double &ssio, double &ssiu)
+{
+  const double sigmax = 3.e-4, sigmaz = 1.e-2, xdist = 2500.;
+  const double zr = nmax(0.0, r);
+  sifrc = 0.0;
+  const double za = zr * p / (c.EPSILO + zr);
+  const double rhw = za / esw, rhi = za / esi, i2w = esw / esi;
+  ssiu = nmin(i2w, rhi);
+  ssio = ssiu;
+  if (fgt(t, 273.1) || !fgt(zr, 0.0) || fge(esi, p * 0.5)) {
+    ssiu = ssiu - 1.0;
+    ssio = ssiu;
+    return;
+  }
+  const double rhin = nmax(0.05, nmin(1.0, rhw));
+  const double drhdz = rhin * c.GRAVITY0 / (t * c.RD) * (c.EPSILO * c.LVTT / (c.CPD * t) - 1.0);
+  const double zz = nmin(1.0, nmax(0.0, z * 0.001));
+  double rhdist = sqrt(xdist * sq(sigmax) + xdist * sq(sigmax) + (1.0 - zz) * sq(dz * drhdz) + zz * dz * sq(sigmaz));
+  if (fgt(zz, 0.1)) rhdist = rhdist / (1.0 + rhdist);
+  const double rhlim = nmax(0.5, nmin(0.99, 1.0 - 0.5 * rhdist));
+  double rhdif = 1.0 - sqrt(nmax(0.0, (1.0 - rhw) / (1.0 - rhlim)));
+  const double wcld = nmin(1.0, nmax(rhdif, 0.0));
+  sifrc = wcld;
+  const double rhlimice = 1.0 + i2w * (rhlim - 1.0);
+  if (fge(0.999, rhlim)) {
+    rhdif = (rhi - rhlimice) * (1.0 / (1.0 - rhlimice));
+    if (fge(wcld, 0.0) && fge(0.0, wcld)) sifrc = nmin(1.0, 0.5 * nmax(0.0, rhdif));
+    else sifrc = nmin(1.0, wcld + nmin(1.0, (1.0 - 1.0 / i2w) * 0.5 / (1.0 - rhlim)));
+  }
+  if (fgt(sifrc, 0.01)) {
+    ssiu = sifrc + rhlimice * (1.0 - sifrc);
+    ssio = (rhi - (1.0 - sifrc) * ssiu) / sifrc;
+  } else {
+    sifrc = 0.0;
+    ssiu = nmax(0.0, sifrc + rhlimice * (1.0 - sifrc) + 2.0 * nmin(0.0, rhi - rhlimice));
+  }
+  ssio = nmin(i2w, ssio) - 1.0;
+  ssiu = nmax(0.0, ssiu) - 1.0;
+}
+
 // Constants derived once per thread (divisions of table constants).
 struct IaDerived {
   double rdrv, rvrd, irv;   // RD/RV, RV/RD, 1/RV
@@ -80,8 +154,12 @@ struct IaDerived {
 ICE3_HD IaDerived ia_derived(const Cst &c) { return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV}; }
 
 // srcs (optional): PSRCS of the point (ice_adjust.F90:360, :468).
+// OCND2: the separate liquid / ice cloud option of CONDENSATION
+// (condensation.F90:373-395, :588-637), with its inputs in *oi and extra
+// outputs in *oo (both required then; LSUBG_COND must be set).
+template <bool OCND2 = false>
 ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt, const IaIn &x, IaOut &o,
-                      double *srcs = nullptr)
+                      double *srcs = nullptr, const Ocnd2In *oi = nullptr, Ocnd2Out *oo = nullptr)
 {
   const int nrr = (int)c.NRR;
   double t = x.th * x.exn;
@@ -96,22 +174,36 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
   double cldfr = 0.0, rv_out = 0.0, rc_out = 0.0, ri_out = 0.0;
   double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
   if (c.LSUBG_COND != 0.0) {
-    const double rt = x.rv + x.rc + x.ri;
-    // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
-    const double lt = fm::flog(t), it = fm::frcp(t);
-    const double pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
-    const double piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
-    double frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
-    const int fmode = (int)c.FRAC_ICE_ADJUST;
-    if (fmode == 3) frac = nclip01(frac);
-    else if (fmode == 0) frac = nclip01(fm::fdiv(c.TMAXMIX - t, c.TMAXMIX - c.TMINMIX));
+    // OCND2: ZPRIFACT = 0, the ice is kept out of the total water (condensation.F90:265-273)
+    const double rt = OCND2 ? x.rv + x.rc : x.rv + x.rc + x.ri;
+    const double it = fm::frcp(t);
+    double pv, piv, frac, esw = 0.0;
+    if (!OCND2) {
+      // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
+      const double lt = fm::flog(t);
+      pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
+      piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
+      frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
+      const int fmode = (int)c.FRAC_ICE_ADJUST;
+      if (fmode == 3) frac = nclip01(frac);
+      else if (fmode == 0) frac = nclip01(fm::fdiv(c.TMAXMIX - t, c.TMAXMIX - c.TMINMIX));
+    } else {
+      // condensation.F90:375-395: ICECLOUD, then the tabulated saturation
+      // pressures; no ice fraction (:412, ZFRAC = 0)
+      esw = tiwmx_at(oi->estw, t);
+      const double esi = tiwmx_at(oi->esti, t);
+      icecloud(c, x.pabs, oi->z, oi->dz, t, x.rv, esw, esi, oo->icldfr, oo->ssio, oo->ssiu);
+      pv = nmin(esw, 0.99 * x.pabs);
+      piv = nmin(esi, 0.99 * x.pabs);
+      frac = 0.0;
+    }
     double qsl = fm::fdiv(d.rdrv * pv, x.pabs - pv);
     const double qsi = fm::fdiv(d.rdrv * piv, x.pabs - piv);
     qsl = (1.0 - frac) * qsl + frac * qsi;
     const double lvs = (1.0 - frac) * lv + frac * ls;
     const double ah = lvs * qsl * (it * it * d.irv) * (1.0 + qsl * d.rvrd);
     const double a = fm::frcp(1.0 + lvs * inv_cph * ah);
-    const double sbar = a * (rt - qsl + ah * lvs * (x.rc + x.ri) * inv_cph);
+    const double sbar = a * (rt - qsl + ah * lvs * (OCND2 ? x.rc : x.rc + x.ri) * inv_cph);
     double sigma;
     if (c.LSIGMAS != 0.0 && c.LSTATNW == 0.0)
       sigma = !(fge(x.sigqsat, 0.0) && fge(0.0, x.sigqsat)) ? sqrt(sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a))
@@ -127,10 +219,32 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
     cond *= sigma;
     cldfr = fge(cond, 1e-12) ? nclip01(0.5 + 0.36 * fm::fatan(1.55 * q1)) : 0.0;
     if (fge(cldfr, 0.0) && fge(0.0, cldfr)) cond = 0.0;
-    rc_out = (1.0 - frac) * cond;
-    ri_out = frac * cond;
-    t = t + ((rc_out - x.rc) * lv + (ri_out - x.ri) * ls) * inv_cph;
-    rv_out = rt - rc_out - ri_out;
+    if (!OCND2) {
+      rc_out = (1.0 - frac) * cond;
+      ri_out = frac * cond;
+      t = t + ((rc_out - x.rc) * lv + (ri_out - x.ri) * ls) * inv_cph;
+      rv_out = rt - rc_out - ri_out;
+    } else {
+      // condensation.F90:588-637.  ZRSW = -9999 (:263) keeps the noise
+      // check's sub-saturation branch closed (ZRSDIF = 0): the liquid content
+      // is the condensate, and where the check fires (ZRCOLD = PRC_OUT) the
+      // temperature keeps its value.  The cloud fraction becomes the
+      // radiative one from the water and ice cloud factors.
+      rc_out = cond;
+      double rcold = x.rc;
+      if (fgt(fabs(rc_out - x.rc), 1.0e-12) && fgt(x.pabs * 0.5, esw)) rcold = rc_out;
+      oo->wcldfr = cldfr;
+      const double sdz = sqrt(oi->dz);
+      const double dum1 = nmin(1.0, 20. * rc_out * sdz / qsl);
+      const double dum3 = nmax(0.0, oo->icldfr - cldfr);
+      const double r_ice = oi->bottom ? x.ri : x.ri + x.rs * 0.5 + x.rg * 0.25;
+      const double dum4 = nmax(0.0, nmin(1.0, oi->ice_cld_wgt * r_ice * sdz / qsi));
+      const double dum2 = (0.8 * cldfr + 0.2) * nmin(1.0, dum1 + dum4 * cldfr);
+      cldfr = nmin(1.0, dum2 + (0.5 * dum3 + 0.5) * dum4);
+      ri_out = x.ri;
+      t = t + (rc_out - rcold) * lv * inv_cph;
+      rv_out = rt - rc_out;
+    }
   }
   double rvs = x.rvs, rcs = x.rcs, ris = x.ris, ths = x.ths;
   const double inv_cphex = fm::fdiv(inv_cph, x.exn_ref);

@@ -33,7 +33,11 @@ class IceAdjustFields(ctypes.Structure):
         "rvs", "rcs", "ris", "ths",
         "t", "rv_out", "rc_out", "ri_out", "cldfr",
         "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv", "ls")] + [("sigqsat_3d", ctypes.c_int64),
-                                                                         ("srcs", P)]
+                                                                         ("srcs", P)] + [
+        (n, P) for n in ("zz", "ice_cld_wgt", "icldfr", "wcldfr", "ssio", "ssiu", "ifr")]
+
+# outputs of the OCND2 option of ice_adjust, in the order of IceAdjustFields
+OCND2_OUTPUTS = ("icldfr", "wcldfr", "ssio", "ssiu", "ifr")
 
 
 class SedimentationFields(ctypes.Structure):

@@ -45,7 +45,7 @@ class IceAdjustFunction(torch.autograd.Function):
         x = dict(zip(IA_IN, ctx.saved_tensors))
         ia: IceAdjust = ctx.ia
         shape = tuple(x["pabs"].shape)
-        nij, nk, sig3d = IceAdjust._geometry(shape, tuple(x["sigqsat"].shape))
+        nij, nk, sig3d = IceAdjust._geometry_any(shape, tuple(x["sigqsat"].shape))
         f = _abi.IceAdjustFields()
         for k in IA_IN:
             setattr(f, k, _ptr(x[k]))

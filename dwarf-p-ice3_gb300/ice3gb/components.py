@@ -97,21 +97,37 @@ class IceAdjust:
             self._handle = Ice3Handle(self.table)
         return self._handle
 
+    @property
+    def ocnd2(self) -> bool:
+        return self.table.values["OCND2"] != 0.0
+
     def __call__(self, sigqsat, pabs, sigs, th, exn, exn_ref, rho_dry_ref, rv, rc, ri, rr, rs, rg, cf_mf, rc_mf,
-                 ri_mf, rvs, rcs, ris, ths, timestep: float, return_srcs: bool = False) -> Tuple:
+                 ri_mf, rvs, rcs, ris, ths, timestep: float, return_srcs: bool = False, zz=None,
+                 ice_cld_wgt=None) -> Tuple:
         """The 16-tuple of IceAdjustJAX; with ``return_srcs`` a 17th element,
         PSRCS (s'r_c'/sigma_s^2, the second-order flux term the Fortran
-        ICE_ADJUST returns, ice_adjust.F90:468)."""
+        ICE_ADJUST returns, ice_adjust.F90:468).
+
+        With OCND2 set in the constants table (separate liquid and ice
+        clouds, condensation.F90:373-395, :588-637) the fields are laid out
+        [nk, ...] with k = 0 at the surface, ``zz`` (height of the levels, m,
+        same shape) and ``ice_cld_wgt`` (one value per column) are required,
+        and five more elements follow: icldfr, wcldfr, ssio, ssiu, ifr
+        (ice_adjust.F90:177-183)."""
         args = dict(sigqsat=sigqsat, pabs=pabs, sigs=sigs, th=th, exn=exn, exn_ref=exn_ref,
                     rho_dry_ref=rho_dry_ref, rv=rv, rc=rc, ri=ri, rr=rr, rs=rs, rg=rg, cf_mf=cf_mf, rc_mf=rc_mf,
                     ri_mf=ri_mf, rvs=rvs, rcs=rcs, ris=ris, ths=ths)
+        if self.ocnd2:
+            if zz is None or ice_cld_wgt is None:
+                raise ValueError("OCND2 needs zz and ice_cld_wgt")
+            args.update(zz=zz, ice_cld_wgt=ice_cld_wgt)
         if isinstance(pabs, np.ndarray):
             return self._call_host(args, float(timestep), return_srcs)
         ref = pabs
         shape = tuple(ref.shape)
         dev = {k: _as_device_f64(v, ref) for k, v in args.items()}
         for k, v in dev.items():
-            if k != "sigqsat" and tuple(v.shape) != shape:
+            if k not in ("sigqsat", "ice_cld_wgt") and tuple(v.shape) != shape:
                 raise ValueError(f"{k} has shape {tuple(v.shape)}, expected {shape}")
         nij, nk, sig3d = self._geometry(shape, tuple(dev["sigqsat"].shape))
         outs = {k: torch.empty(shape, dtype=torch.float64, device=ref.device) for k in IA_OUTPUTS}
@@ -124,14 +140,39 @@ class IceAdjust:
         f.sigqsat_3d = sig3d
         srcs = torch.empty(shape, dtype=torch.float64, device=ref.device) if return_srcs else None
         f.srcs = _ptr(srcs)
+        extra = ()
+        if self.ocnd2:
+            self._check_ocnd2(shape, nij, tuple(dev["ice_cld_wgt"].shape))
+            f.zz, f.ice_cld_wgt = _ptr(dev["zz"]), _ptr(dev["ice_cld_wgt"])
+            extra = tuple(torch.empty(shape, dtype=torch.float64, device=ref.device) for _ in _abi.OCND2_OUTPUTS)
+            for k, v in zip(_abi.OCND2_OUTPUTS, extra):
+                setattr(f, k, _ptr(v))
         h = self.handle
         _abi.check(h.lib.ice3gb_ice_adjust(h.h, nij, nk, float(timestep), ctypes.byref(f),
                                            ctypes.c_void_p(_stream_ptr())), h.h, "ice3gb_ice_adjust")
         res = tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
-        return res + (srcs,) if return_srcs else res
+        return (res + (srcs,) if return_srcs else res) + extra
+
+    def _geometry(self, shape, sig_shape):
+        if self.ocnd2:
+            # levels are needed (layer thickness): [nk, ...] whatever sigqsat's shape
+            if len(shape) < 2:
+                raise ValueError("OCND2 needs fields shaped [nk, ...]")
+            nij = int(np.prod(shape[1:]))
+            if tuple(sig_shape) == tuple(shape):
+                return nij, int(shape[0]), 1
+            if int(np.prod(sig_shape)) == nij:
+                return nij, int(shape[0]), 0
+            raise ValueError(f"sigqsat shape {sig_shape} matches neither the fields {shape} nor one level")
+        return self._geometry_any(shape, sig_shape)
 
     @staticmethod
-    def _geometry(shape, sig_shape):
+    def _check_ocnd2(shape, nij, wgt_shape):
+        if int(np.prod(wgt_shape)) != nij:
+            raise ValueError(f"ice_cld_wgt has shape {wgt_shape}, expected one value per column ({nij})")
+
+    @staticmethod
+    def _geometry_any(shape, sig_shape):
         n = int(np.prod(shape))
         if tuple(sig_shape) == tuple(shape):
             return n, 1, 1                       # full 3-D sigqsat: pointwise, any layout
@@ -154,11 +195,19 @@ class IceAdjust:
         srcs = np.empty(shape) if return_srcs else None
         if return_srcs:
             f.srcs = srcs.ctypes.data_as(ctypes.c_void_p)
+        extra = ()
+        if self.ocnd2:
+            self._check_ocnd2(shape, nij, host["ice_cld_wgt"].shape)
+            f.zz = host["zz"].ctypes.data_as(ctypes.c_void_p)
+            f.ice_cld_wgt = host["ice_cld_wgt"].ctypes.data_as(ctypes.c_void_p)
+            extra = tuple(np.empty(shape) for _ in _abi.OCND2_OUTPUTS)
+            for k, v in zip(_abi.OCND2_OUTPUTS, extra):
+                setattr(f, k, v.ctypes.data_as(ctypes.c_void_p))
         h = self.handle
         _abi.check(h.lib.ice3gb_ice_adjust_host(h.h, nij, nk, dt, ctypes.byref(f), ctypes.c_void_p(_stream_ptr())),
                    h.h, "ice3gb_ice_adjust_host")
         res = tuple(outs[k] for k in IA_OUTPUTS) + tuple(io[k] for k in IA_INOUT)
-        return res + (srcs,) if return_srcs else res
+        return (res + (srcs,) if return_srcs else res) + extra
 
 
 # RainIceJAX state keys -> ABI fields (src/ice3/jax/rain_ice.py:209-260,

@@ -68,7 +68,7 @@ extern "C" {
   /* physical constants (modd_cst) */                                         \
   X(TT) X(CPD) X(CPV) X(CL) X(CI) X(RD) X(RV) X(LVTT) X(LSTT) X(LMTT)         \
   X(ESTT) X(ALPW) X(BETAW) X(GAMW) X(ALPI) X(BETAI) X(GAMI) X(EPSILO)         \
-  X(P00) X(RHOLW) X(MNH_TINY)                                                 \
+  X(P00) X(RHOLW) X(MNH_TINY) X(GRAVITY0)                                     \
   /* subgrid condensation (modd_nebn) */                                      \
   X(TMAXMIX) X(TMINMIX) X(LSUBG_COND) X(LSIGMAS) X(LSTATNW)                   \
   X(FRAC_ICE_ADJUST) X(CONDENS) X(OCND2) X(NRR) X(LAMBDA3)                    \
@@ -146,6 +146,15 @@ typedef struct Ice3gbIceAdjustFields {
                                        PSRCS = s'r_c'/sigma_s^2 of
                                        ice_adjust.F90:360,468 and
                                        condensation.F90:566-571, :638-647  */
+  /* OCND2 = 1 only (separate liquid and ice clouds, condensation.F90:373-395,
+   * :588-637, mode_icecloud.F90); ignored otherwise:                       */
+  const double *zz;                 /* [nk][nij] height of the levels (m),
+                                       k = 0 at the surface; nk >= 2        */
+  const double *ice_cld_wgt;        /* [nij] PICE_CLD_WGT                  */
+  double *icldfr, *wcldfr;          /* out: ice / water cloud fraction     */
+  double *ssio, *ssiu;              /* out: ice super-saturation in the
+                                       cloudy / clear part                 */
+  double *ifr;                      /* out: PIFR (10 everywhere)           */
 } Ice3gbIceAdjustFields;
 
 /* ---- statistical sedimentation ---------------------------------------- */

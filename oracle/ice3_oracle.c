@@ -80,6 +80,97 @@ static double sigrc(const C *c, double q1)
   return r;
 }
 
+/* ---- OCND2 (separate liquid and ice clouds) ---------------------------- */
+
+/* TIWMX saturation tables, micro/modd_tiwmx.F90 (XNDEGR = 100, NSTART =
+ * 13200, NSTOP = 37316), filled by micro/mode_ini_tiwmx.F90 from
+ * micro/mode_tiwmx_fun.F90: ESTABW(j) = ESATW(j/100); ESTABI(j) = the ice
+ * formula at and below 273.15 K, the water one above (INI_TIWMX overwrites
+ * ESATI's blend there). */
+#define TIWMX_NSTART 13200
+#define TIWMX_NSTOP 37316
+#define TIWMX_N (TIWMX_NSTOP - TIWMX_NSTART + 1)
+
+EXPORT int ice3o_tiwmx_size(void) { return TIWMX_N; }
+
+EXPORT void ice3o_tiwmx_tables(const C *c, double *estw, double *esti)
+{
+  for (int j = TIWMX_NSTART; j <= TIWMX_NSTOP; ++j) {
+    const double t = (double)j / 100.0;
+    const double w = exp(c->ALPW - c->BETAW / t - c->GAMW * log(t));
+    estw[j - TIWMX_NSTART] = w;
+    esti[j - TIWMX_NSTART] = (t > 273.15) ? w : exp(c->ALPI - c->BETAI / t - c->GAMI * log(t));
+  }
+}
+
+/* ESATW / ESATI of micro/mode_tiwmx.F90: TAB(NINT(XNDEGR*T)); the index is
+ * clamped to the table (the reference reads out of bounds there). */
+static double tiwmx_at(const double *tab, double t)
+{
+  long j = lround(100.0 * t);
+  j = j < TIWMX_NSTART ? TIWMX_NSTART : (j > TIWMX_NSTOP ? TIWMX_NSTOP : j);
+  return tab[j - TIWMX_NSTART];
+}
+
+/* ICECLOUD, micro/mode_icecloud.F90 (as CONDENSATION calls it,
+ * condensation.F90:381-385: PTSTEP = 1, PPBLH = -1, PWCLD = -1, XW2D = PIFR =
+ * 10; W2D and RSI are discarded there).  Returns SIFRC (the ice cloud
+ * fraction) and the super-saturations SSIO / SSIU. */
+static void icecloud(const C *c, double p, double z, double dz, double t, double r, double esw, double esi,
+                     double *sifrc_o, double *ssio_o, double *ssiu_o)
+{
+  const double sigmax = 3.e-4, sigmay = sigmax, sigmaz = 1.e-2, xdist = 2500., ydist = xdist;
+  const double zr = dmax(0., r * 1.0);
+  double sifrc = 0.;
+  double za = zr * p / (c->EPSILO + zr);
+  const double rhw = za / esw;
+  const double rhi = za / esi;
+  const double i2w = esw / esi;
+  double ssiu = dmin(i2w, rhi), ssio = ssiu;
+  if (t > 273.1 || zr <= 0. || esi >= p * 0.5) {
+    ssiu = ssiu - 1.;
+    ssio = ssiu;
+  } else {
+    const double rhin = dmax(0.05, dmin(1., rhw));
+    const double drhdz = rhin * c->GRAVITY0 / (t * c->RD) * (c->EPSILO * c->LVTT / (c->CPD * t) - 1.);
+    const double zz = dmin(1., dmax(0., z * 0.001));
+    double rhdist = sqrt(xdist * sq(sigmax) + ydist * sq(sigmay) + (1. - zz) * sq(dz * drhdz) + zz * dz * sq(sigmaz));
+    if (zz > 0.1) rhdist = rhdist / (1. + rhdist);
+    const double rhlim = dmax(0.5, dmin(0.99, 1. - 0.5 * rhdist));
+    double rhdif = (1. - rhw) / (1.0 - rhlim);
+    rhdif = 1. - sqrt(dmax(0., rhdif));
+    const double wcld = dmin(1., dmax(rhdif, 0.0));
+    sifrc = wcld;
+    const double rhlimice = 1. + i2w * (rhlim - 1.);
+    if (rhlim <= 0.999) {
+      const double rhliminv = 1. / (1. - rhlimice);
+      rhdif = (rhi - rhlimice) * rhliminv;
+      if (wcld == 0.) {
+        sifrc = dmin(1., 0.5 * dmax(0., rhdif));
+      } else {
+        za = 1. - 1. / i2w;
+        sifrc = dmin(1., za * 0.5 / (1. - rhlim));
+        sifrc = dmin(1., wcld + sifrc);
+      }
+    }
+    if (sifrc > 0.01) {
+      ssiu = sifrc + rhlimice * (1. - sifrc);
+      ssio = (rhi - (1. - sifrc) * ssiu) / sifrc;
+    } else {
+      sifrc = 0.;
+      za = dmin(0., rhi - rhlimice);
+      ssiu = dmax(0., sifrc + rhlimice * (1. - sifrc) + 2. * za);
+    }
+    ssio = dmin(i2w, ssio);
+    ssiu = dmax(0., ssiu);
+    ssiu = ssiu - 1.;
+    ssio = ssio - 1.;
+  }
+  *sifrc_o = sifrc;
+  *ssio_o = ssio;
+  *ssiu_o = ssiu;
+}
+
 EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gbIceAdjustFields *f)
 {
   if (!c || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
@@ -89,10 +180,20 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
   const int fmode = (int)c->FRAC_ICE_ADJUST;
   const int sigmas = c->LSIGMAS != 0.0 && c->LSTATNW == 0.0;
   const int mfpdf = (int)c->SUBG_MF_PDF;
-  if (c->CONDENS != 0.0 || c->OCND2 != 0.0) return ICE3GB_ERR_UNSUPPORTED;
+  const int ocnd2 = c->OCND2 != 0.0;
+  if (c->CONDENS != 0.0) return ICE3GB_ERR_UNSUPPORTED;
+  if (ocnd2 && (!subg || nk < 2 || !f->zz || !f->ice_cld_wgt)) return ICE3GB_ERR_UNSUPPORTED;
+  double *estw = NULL, *esti = NULL;
+  if (ocnd2) {
+    estw = (double *)malloc(2 * sizeof(double) * TIWMX_N);
+    if (!estw) return ICE3GB_ERR_SHAPE;
+    esti = estw + TIWMX_N;
+    ice3o_tiwmx_tables(c, estw, esti);
+  }
 #pragma omp parallel for schedule(static)
   for (long p = 0; p < n; ++p) {
     const long col = p % nij;
+    const long k = p / nij;
     const double sigqsat = f->sigqsat_3d ? f->sigqsat[p] : f->sigqsat[col];
     const double pabs = f->pabs[p], sigs = f->sigs[p];
     const double rv = f->rv[p], rc = f->rc[p], ri = f->ri[p];
@@ -107,21 +208,38 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
     else cph = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * (ri + rs + rg);
     double cldfr = 0.0, rv_out = 0.0, rc_out = 0.0, ri_out = 0.0;
     double hlc_hrc = 0.0, hlc_hcf = 0.0, hli_hri = 0.0, hli_hcf = 0.0;
+    double icldfr = 0.0, ssio = 0.0, ssiu = 0.0;
     if (subg) {
-      const double rt = rv + rc + ri;                                  /* :190 */
-      /* es_w/es_i: functions/tiwmx.py:18,60 */
-      const double pv = dmin(exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)), 0.99 * pabs);
-      const double piv = dmin(exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)), 0.99 * pabs);
-      double frac = (rc + ri > 1e-20) ? rc / (rc + ri) : 0.0;          /* :198-202 */
-      if (fmode == 3) frac = clip01(frac);
-      else if (fmode == 0) frac = clip01((c->TMAXMIX - t) / (c->TMAXMIX - c->TMINMIX));
+      /* OCND2: ZPRIFACT = 0, ice kept out of the total water (condensation.F90:265-273) */
+      const double rt = ocnd2 ? rv + rc : rv + rc + ri;                /* :190 */
+      double pv, piv, esw = 0.0, dz = 0.0, frac;
+      if (!ocnd2) {
+        /* es_w/es_i: functions/tiwmx.py:18,60 */
+        pv = dmin(exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)), 0.99 * pabs);
+        piv = dmin(exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)), 0.99 * pabs);
+        frac = (rc + ri > 1e-20) ? rc / (rc + ri) : 0.0;               /* :198-202 */
+        if (fmode == 3) frac = clip01(frac);
+        else if (fmode == 0) frac = clip01((c->TMAXMIX - t) / (c->TMAXMIX - c->TMINMIX));
+      } else {
+        /* condensation.F90:375-395: layer thickness to the level above (below
+         * at the top), ICECLOUD, tabulated saturation pressures; no ice
+         * fraction (:412, ZFRAC = 0) */
+        const long kp = k + 1 < nk ? k + 1 : nk - 1;
+        dz = f->zz[kp * nij + col] - f->zz[(kp - 1) * nij + col];
+        esw = tiwmx_at(estw, t);
+        const double esi = tiwmx_at(esti, t);
+        icecloud(c, pabs, f->zz[p], dz, t, rv, esw, esi, &icldfr, &ssio, &ssiu);
+        pv = dmin(esw, 0.99 * pabs);
+        piv = dmin(esi, 0.99 * pabs);
+        frac = 0.0;
+      }
       double qsl = c->RD / c->RV * pv / (pabs - pv);                   /* :212 */
       const double qsi = c->RD / c->RV * piv / (pabs - piv);
       qsl = (1.0 - frac) * qsl + frac * qsi;
       const double lvs = (1.0 - frac) * lv + frac * ls;
       const double ah = lvs * qsl / (c->RV * sq(t)) * (1.0 + c->RV * qsl / c->RD);
       const double a = 1.0 / (1.0 + lvs / cph * ah);
-      const double sbar = a * (rt - qsl + ah * lvs * (rc + ri) / cph);
+      const double sbar = a * (rt - qsl + ah * lvs * (ocnd2 ? rc : rc + ri) / cph);
       double sigma;
       if (sigmas)                                                      /* :226-233 */
         sigma = (sigqsat != 0.0) ? sqrt(sq(2.0 * sigs) + sq(sigqsat * qsl * a)) : 2.0 * sigs;
@@ -136,10 +254,41 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
       cond *= sigma;
       cldfr = (cond >= 1e-12) ? clip01(0.5 + 0.36 * atan(1.55 * q1)) : 0.0;
       if (cldfr == 0.0) cond = 0.0;
-      rc_out = (1.0 - frac) * cond;                                    /* :263-266 */
-      ri_out = frac * cond;
-      t = t + ((rc_out - rc) * lv + (ri_out - ri) * ls) / cph;
-      rv_out = rt - rc_out - ri_out;
+      if (!ocnd2) {
+        rc_out = (1.0 - frac) * cond;                                  /* :263-266 */
+        ri_out = frac * cond;
+        t = t + ((rc_out - rc) * lv + (ri_out - ri) * ls) / cph;
+        rv_out = rt - rc_out - ri_out;
+      } else {
+        /* condensation.F90:588-637.  ZRSW = -9999 (:263), so the
+         * sub-saturation branch of the noise check is never taken and
+         * ZRSDIF = 0: the liquid content is the condensate, and where the
+         * check fires the temperature keeps its value (ZRCOLD = PRC_OUT). */
+        rc_out = (1.0 - frac) * cond;
+        const double lwinc = rc_out - rc;
+        double rcold = rc;
+        if (fabs(lwinc) > 1.0e-12 && esw < pabs * 0.5) {
+          rcold = rc_out;
+          rc_out = cond - 0.0;
+        }
+        const double wcldfr = cldfr;
+        const double dum1 = dmin(1.0, 20. * rc_out * sqrt(dz) / qsl);
+        const double dum3 = dmax(0., icldfr - wcldfr);
+        double dum4 = (k == 0) ? ri : ri + rs * 0.5 + rg * 0.25;
+        dum4 = dmax(0., dmin(1., f->ice_cld_wgt[col] * dum4 * sqrt(dz) / qsi));
+        const double dum2 = (0.8 * cldfr + 0.2) * dmin(1., dum1 + dum4 * cldfr);
+        cldfr = dmin(1., dum2 + (0.5 * dum3 + 0.5) * dum4);
+        ri_out = ri;
+        t = t + ((rc_out - rcold) * lv + (ri_out - ri) * ls) / cph;
+        rv_out = rt - rc_out - ri_out * 0.0;
+        if (f->wcldfr) f->wcldfr[p] = wcldfr;
+      }
+    }
+    if (ocnd2) {
+      if (f->icldfr) f->icldfr[p] = icldfr;
+      if (f->ssio) f->ssio[p] = ssio;
+      if (f->ssiu) f->ssiu[p] = ssiu;
+      if (f->ifr) f->ifr[p] = 10.;                                     /* condensation.F90:259 */
     }
     double rvs = f->rvs[p], rcs = f->rcs[p], ris = f->ris[p], ths = f->ths[p];
     const double exn_ref = f->exn_ref[p];
@@ -203,6 +352,7 @@ EXPORT int ice3o_ice_adjust(const C *c, int nij, int nk, double dt, const Ice3gb
     f->ris[p] = ris;
     f->ths[p] = ths;
   }
+  free(estw);
   return ICE3GB_OK;
 }
 

@@ -87,10 +87,29 @@ def ice_adjust(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, srcs
     for k, v in {**ins, **io, **out}.items():
         setattr(f, k, _ptr(v))
     f.sigqsat_3d = 1 if ins["sigqsat"].ndim == 2 else 0
+    if table.values["OCND2"] != 0.0:
+        # separate liquid and ice clouds: heights, the per-column ice cloud
+        # weight, and five more outputs (condensation.F90:373-395, :588-637)
+        ins["zz"] = _f64(st["zz"])
+        ins["ice_cld_wgt"] = _f64(st["ice_cld_wgt"])
+        f.zz, f.ice_cld_wgt = _ptr(ins["zz"]), _ptr(ins["ice_cld_wgt"])
+        for k in ("icldfr", "wcldfr", "ssio", "ssiu", "ifr"):
+            out[k] = np.empty((nk, nij))
+            setattr(f, k, _ptr(out[k]))
     rc = lib.ice3o_ice_adjust(ctypes.byref(table.consts), nij, nk, ctypes.c_double(dt), ctypes.byref(f))
     if rc != 0:
         raise RuntimeError(f"oracle ice_adjust returned {rc}")
     return {**out, **io}
+
+
+def tiwmx_tables(table: ConstantsTable):
+    """The oracle's TIWMX saturation tables (ESTABW, ESTABI) at T = j/100 K,
+    j = 13200..37316 (micro/mode_ini_tiwmx.F90)."""
+    lib = load()
+    n = lib.ice3o_tiwmx_size()
+    w, i = np.empty(n), np.empty(n)
+    lib.ice3o_tiwmx_tables(ctypes.byref(table.consts), _ptr(w), _ptr(i))
+    return w, i
 
 
 def src_1d() -> np.ndarray:

@@ -10,6 +10,7 @@ through the numpy stand-in of refshim.py:
 * ``ice4_rainfr_vert``                 (stencils/rain_ice.py:272)
 * ``ice4_warm`` with the CLFR / PRFR evaporation options (stencils/ice4_warm.py:15)
 * the SRC_1D table                     (phyex_common/lookup_table.py:4)
+* ``e_sat_w`` / ``e_sat_i`` on the TIWMX grid (jax/functions/tiwmx.py:18,60)
 
 Inputs are seeded synthetic states (ice3gb.state.make_state) and seeded
 random point sets; both inputs and reference outputs are stored.
@@ -240,6 +241,19 @@ def src_1d_case():
     return {"src_1d": {"SRC_1D": np.asarray(SRC_1D, dtype=np.float64)}}
 
 
+def tiwmx_case(Phyex):
+    """The reference's saturation pressures (src/ice3/jax/functions/tiwmx.py:18,60)
+    on the grid of PHYEX's TIWMX tables, T = j/100 K (micro/modd_tiwmx.F90):
+    a stride through 13200..37316 and every entry around 273.15 K, where
+    ESTABI switches from the ice to the water formula."""
+    from ice3.jax.functions.tiwmx import e_sat_i, e_sat_w
+    ext = Phyex("AROME").to_externals()
+    j = np.unique(np.concatenate([np.arange(13200, 37317, 37), np.arange(27300, 27330), [37316]]))
+    t = _shim(j / 100.0)
+    return {"tiwmx": {"j": j.astype(np.float64), "esw": np.asarray(e_sat_w(t, ext), dtype=np.float64),
+                      "esi": np.asarray(e_sat_i(t, ext), dtype=np.float64)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-src", default="/root/reference/src")
@@ -273,6 +287,7 @@ def main():
     blobs.update(process_cases(mods, Phyex))
     blobs.update(warm_subg_case(mods, Phyex))
     blobs.update(src_1d_case())
+    blobs.update(tiwmx_case(Phyex))
     for name, rec in blobs.items():
         if args.only is not None and name not in args.only:
             continue

@@ -53,3 +53,36 @@ extern "C" void ia_srcs_host(const Ice3gbConstants *c, double dt, long n, const 
     ia_point(*c, d, dt, 1.0 / dt, x, o, srcs + p);
   }
 }
+
+// OCND2 forward on a [nk][nij] grid, as ice_adjust_ocnd2_kernel runs it:
+// in = the 20 IaIn fields (sigqsat per point), zz [nk][nij], ice_cld_wgt
+// [nij], tiwmx = ESTABW then ESTABI; out = the 16 IaOut fields, out2 =
+// icldfr, wcldfr, ssio, ssiu.
+extern "C" void ia_ocnd2_host(const Ice3gbConstants *c, double dt, long nij, long nk, const double *const *in,
+                              const double *zz, const double *wgt, const double *tiwmx, double *const *out,
+                              double *const *out2)
+{
+  const IaDerived d = ia_derived(*c);
+  for (long p = 0; p < nij * nk; ++p) {
+    IaIn x;
+    gather_in(in, p, x);
+    const long k = p / nij, col = p - k * nij;
+    const long kp = k + 1 < nk ? k + 1 : nk - 1;
+    Ocnd2In oi;
+    oi.estw = tiwmx;
+    oi.esti = tiwmx + kTiwmxN;
+    oi.z = zz[p];
+    oi.dz = zz[kp * nij + col] - zz[(kp - 1) * nij + col];
+    oi.ice_cld_wgt = wgt[col];
+    oi.bottom = k == 0;
+    IaOut o;
+    Ocnd2Out oo;
+    ia_point<true>(*c, d, dt, 1.0 / dt, x, o, nullptr, &oi, &oo);
+    const double *v = &o.t;
+    for (int j = 0; j < 16; ++j) out[j][p] = v[j];
+    out2[0][p] = oo.icldfr;
+    out2[1][p] = oo.wcldfr;
+    out2[2][p] = oo.ssio;
+    out2[3][p] = oo.ssiu;
+  }
+}

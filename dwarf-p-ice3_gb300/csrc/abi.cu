@@ -198,6 +198,9 @@ int validate_rain_ice(Handle *h, const Ice3gbRainIceFields *f)
   if ((f->sea == nullptr) != (f->town == nullptr))
     return fail(h, ICE3GB_ERR_NULL, "sea and town must be both given or both NULL");
   if (!h->rain_ice_ok) return fail(h, ICE3GB_ERR_UNSUPPORTED, "%s", h->rain_ice_why.c_str());
+  if ((int)h->c.NRR == 7) {  // hail
+    REQUIRE(f->rht); REQUIRE(f->rhs); REQUIRE(f->inprh);
+  }
   return ICE3GB_OK;
 }
 
@@ -209,6 +212,7 @@ SedArgs sed_args(const Ice3gbSedimentationFields &f, int nij, int nk, double dt,
   a.fpr[0] = f.fpr_c; a.fpr[1] = f.fpr_r; a.fpr[2] = f.fpr_i; a.fpr[3] = f.fpr_s; a.fpr[4] = f.fpr_g;
   a.inpr[0] = f.inprc; a.inpr[1] = f.inprr; a.inpr[2] = f.inpri; a.inpr[3] = f.inprs; a.inpr[4] = f.inprg;
   a.nij = nij; a.nk = nk; a.dt = dt; a.fortran = fortran;
+  a.hsrc = a.hfpr = a.hinpr = nullptr;
   return a;
 }
 
@@ -240,6 +244,7 @@ int check_surrogate(Handle *h, const SurCall &sur, long n)
   if (!sur.norm) return fail(h, ICE3GB_ERR_NULL, "surrogate: normalisation is NULL");
   if ((int)h->c.SUBG_RC_RR_ACCR != 0 || (int)h->c.SUBG_RR_EVAP != 0)
     return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained with SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE only");
+  if ((int)h->c.NRR != 6) return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained for NRR = 6 (no hail)");
   if (n > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "surrogate: at most 2^31 - 1 points per call");
   return ICE3GB_OK;
 }
@@ -319,7 +324,14 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   sf.rcs = f->rcs; sf.rrs = f->rrs; sf.ris = f->ris; sf.rss = f->rss; sf.rgs = f->rgs;
   sf.inprc = f->inprc; sf.inprr = f->inprr; sf.inpri = f->inpri; sf.inprs = f->inprs; sf.inprg = f->inprg;
   sf.fpr_c = f->fpr_c; sf.fpr_r = f->fpr_r; sf.fpr_i = f->fpr_i; sf.fpr_s = f->fpr_s; sf.fpr_g = f->fpr_g;
-  const SedArgs sa = sed_args(sf, nij, nk, dt, sed_fortran);
+  SedArgs sa = sed_args(sf, nij, nk, dt, sed_fortran);
+  const bool hail = (int)h->c.NRR == 7;
+  if (hail) {
+    if (!sed_fortran) return fail(h, ICE3GB_ERR_UNSUPPORTED, "hail (NRR = 7) with the Fortran sedimentation only");
+    sa.hsrc = f->rhs;
+    sa.hfpr = f->fpr_h;
+    sa.hinpr = f->inprh;
+  }
   cudaError_t e;
   // SEDIM: 1 = STAT (statistical), 0 = SPLI (time-split, needs 2 n doubles of scratch)
   const bool spli = (int)c.SEDIM == 0;
@@ -335,6 +347,7 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
     sp.sed = sa;
     sp.rt[0] = f->rct; sp.rt[1] = f->rrt; sp.rt[2] = f->rit; sp.rt[3] = f->rst; sp.rt[4] = f->rgt;
     sp.rvt = f->rvt; sp.exn = f->exn; sp.rvs = f->rvs; sp.ths = f->ths;
+    sp.rht = hail ? f->rht : nullptr;
     sp.status = h->d_status;
     sp.max_iter = 10000;
     double *scr = nullptr;
@@ -429,6 +442,8 @@ int validate_step(Handle *h, const Ice3gbStepFields *f)
   if (h->c.CONDENS != 0.0 || h->c.OCND2 != 0.0)
     return fail(h, ICE3GB_ERR_UNSUPPORTED, "ice_adjust: only CONDENS=CB02 without OCND2");
   if (!h->rain_ice_ok) return fail(h, ICE3GB_ERR_UNSUPPORTED, "%s", h->rain_ice_why.c_str());
+  if ((int)h->c.NRR != 6)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "physics step: NRR = 6 only (the step fields carry no hail)");
   return ICE3GB_OK;
 }
 
@@ -751,7 +766,9 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   *handle = nullptr;
   if ((int)c->NGAMINC != ICE3GB_NGAMINC || (int)c->NACCLBDAS != ICE3GB_NACCLBDAS ||
       (int)c->NACCLBDAR != ICE3GB_NACCLBDAR || (int)c->NDRYLBDAG != ICE3GB_NDRYLBDAG ||
-      (int)c->NDRYLBDAS != ICE3GB_NDRYLBDAS || (int)c->NDRYLBDAR != ICE3GB_NDRYLBDAR)
+      (int)c->NDRYLBDAS != ICE3GB_NDRYLBDAS || (int)c->NDRYLBDAR != ICE3GB_NDRYLBDAR ||
+      (int)c->NWETLBDAH != ICE3GB_NWETLBDAH || (int)c->NWETLBDAS != ICE3GB_NWETLBDAS ||
+      (int)c->NWETLBDAG != ICE3GB_NWETLBDAG || (int)c->NWETLBDAR != ICE3GB_NWETLBDAR)
     return fail(nullptr, ICE3GB_ERR_RANGE, "lookup-table sizes differ from the compiled ones");
   Handle *h = new Handle();
   h->magic = kMagic;
@@ -787,7 +804,8 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   }
   h->rain_ice_ok = true;
   char why[256] = "";
-  if ((int)c->NRR != 6) snprintf(why, sizeof(why), "rain_ice supports NRR=6 only (got %g)", c->NRR);
+  if ((int)c->NRR != 6 && (int)c->NRR != 7)
+    snprintf(why, sizeof(why), "rain_ice supports NRR = 6 or 7 (hail), got %g", c->NRR);
   else if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)
     snprintf(why, sizeof(why), "rain_ice: MRSTEP/TSTEP_TS time-splitting is not supported");
   else if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1)
@@ -1202,9 +1220,11 @@ int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbR
   const bool adju = (int)h->c.SUBG_AUCV_RC == 2 || (int)h->c.SUBG_AUCV_RI == 2;
   const bool st = f->sea != nullptr;
   const bool fpr = f->fpr_c || f->fpr_r || f->fpr_i || f->fpr_s || f->fpr_g;
-  // 14 in + cit + (4 hl/hi) + 7 sources + 2 out 3-D (+5 fpr); 2-D: sea town + 6 out
-  const size_t n3 = 14 + 1 + (adju ? 4 : 0) + 7 + 2 + (fpr ? 5 : 0);
-  if ((rc = ensure_stage(h, n3 * b3p + 8 * b2p))) return rc;
+  const bool hail = (int)h->c.NRR == 7;
+  // 14 in + cit + (4 hl/hi) + 7 sources + 2 out 3-D (+5 fpr) (+ hail: rht, rhs, fpr_h);
+  // 2-D: sea town + 6 out (+ inprh)
+  const size_t n3 = 14 + 1 + (adju ? 4 : 0) + 7 + 2 + (fpr ? 5 : 0) + (hail ? 3 : 0);
+  if ((rc = ensure_stage(h, n3 * b3p + 9 * b2p))) return rc;
   char *base = reinterpret_cast<char *>(h->d_stage);
   size_t off = 0;
   auto take3 = [&]() { double *p = reinterpret_cast<double *>(base + off); off += b3p; return p; };
@@ -1239,6 +1259,12 @@ int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbR
   }
   d.inprc = take2(); d.inprr = take2(); d.inpri = take2(); d.inprs = take2(); d.inprg = take2();
   d.indep = f->indep ? take2() : nullptr;
+  if (hail) {
+    d.rht = up3(f->rht);
+    d.rhs = up3(f->rhs);
+    d.fpr_h = f->fpr_h ? take3() : nullptr;
+    d.inprh = take2();
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
   if ((rc = run_rain_ice(h, nij, nk, dt, opt, &d, s))) return rc;
   struct Pair { double *dst; const double *src; size_t bytes; };
@@ -1248,7 +1274,8 @@ int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbR
       {f->rainfr, d.rainfr, b3}, {f->inprc, d.inprc, b2}, {f->inprr, d.inprr, b2}, {f->inpri, d.inpri, b2},
       {f->inprs, d.inprs, b2}, {f->inprg, d.inprg, b2}, {f->indep, d.indep, b2},
       {f->fpr_c, d.fpr_c, b3}, {f->fpr_r, d.fpr_r, b3}, {f->fpr_i, d.fpr_i, b3}, {f->fpr_s, d.fpr_s, b3},
-      {f->fpr_g, d.fpr_g, b3}};
+      {f->fpr_g, d.fpr_g, b3}, {hail ? f->rhs : nullptr, d.rhs, b3}, {hail ? f->inprh : nullptr, d.inprh, b2},
+      {hail ? f->fpr_h : nullptr, d.fpr_h, b3}};
   for (const Pair &p : back)
     if (p.dst && p.src && e == cudaSuccess) e = cudaMemcpyAsync(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

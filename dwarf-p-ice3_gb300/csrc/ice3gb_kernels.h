@@ -15,12 +15,14 @@ struct SedArgs {
   int nij, nk;
   double dt;
   int fortran;
+  double *hsrc, *hfpr, *hinpr;   // hail (NRR = 7): rhs, its flux, inprh; NULL otherwise
 };
 
 // Time-split sedimentation (SEDIM = SPLI) of a rain_ice call.
 struct SplitArgs {
   SedArgs sed;                     // geometry, sources, outputs, sea/town
   const double *rt[5], *rvt, *exn; // mixing ratios at t, exner
+  const double *rht;               // hail at t (NRR = 7), else NULL
   double *rvs, *ths;               // in-out (negativity correction)
   double *scratch;                 // 2 * nij * nk doubles
   unsigned int *status;            // ICE3GB_DEV_SED_CAP

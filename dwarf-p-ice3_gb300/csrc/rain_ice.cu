@@ -49,7 +49,8 @@ __device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int
 
 // SUBG: the subgrid warm-process options (SUBG_RC_RR_ACCR / SUBG_RR_EVAP
 // other than NONE); the NONE instantiation carries none of their code.
-template <bool SUBG>
+// H: hail (NRR = 7), the hail kernels read from the global copy of the tables.
+template <bool SUBG, bool H = false>
 __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_kernel(const __grid_constant__ Cst c,
                                                                          const __grid_constant__ RainIceArgs a)
 {
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
     if (slot < n) {
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       bool capped;
-      key = rain_ice_point<false, SUBG>(c, dsh, lut, f, p, dt, a.max_passes, capped);
+      key = rain_ice_point<false, SUBG, H>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr, a.luts);
       any_capped |= capped;
       a.scr.keys[p] = key;
     }
@@ -85,10 +86,11 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
 
 // The precipitation fraction of a call with a PRFR option, one thread per
 // column (prfr_column); runs before the point kernel, which starts from it.
+template <bool H>
 __global__ void rain_ice_prfr_kernel(const __grid_constant__ Cst c, const __grid_constant__ RainIceArgs a)
 {
   const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (col < a.nij) prfr_column(c, a.f, a.nij, a.nk, col);
+  if (col < a.nij) prfr_column<H>(c, a.f, a.nij, a.nk, col);
 }
 
 // Processing order: per tile of ORDER_TILE points, a counting sort by regime
@@ -170,22 +172,25 @@ size_t rain_ice_smem_bytes() { return sizeof(double) * LUT_N; }
 cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_sms, cudaStream_t s)
 {
   const bool subg = (int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0;
-  cudaError_t e = cudaFuncSetAttribute(subg ? rain_ice_points_kernel<true> : rain_ice_points_kernel<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rain_ice_smem_bytes());
+  const bool hail = (int)c.NRR == 7;
+  void (*kern)(const Cst, const RainIceArgs) =
+      hail ? (subg ? rain_ice_points_kernel<true, true> : rain_ice_points_kernel<false, true>)
+           : (subg ? rain_ice_points_kernel<true, false> : rain_ice_points_kernel<false, false>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rain_ice_smem_bytes());
   if (e != cudaSuccess) return e;
   const long n = (long)a.nij * a.nk;
   long chunks = (n + RI_THREADS - 1) / RI_THREADS;
   long blocks = (long)num_sms * RI_BLOCKS_PER_SM;
   if (blocks > chunks) blocks = chunks;
   if (blocks < 1) blocks = 1;
-  if (subg) rain_ice_points_kernel<true><<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
-  else rain_ice_points_kernel<false><<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  kern<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rain_ice_prfr(const Cst &c, const RainIceArgs &a, cudaStream_t s)
 {
-  rain_ice_prfr_kernel<<<(unsigned)((a.nij + 127) / 128), 128, 0, s>>>(c, a);
+  if ((int)c.NRR == 7) rain_ice_prfr_kernel<true><<<(unsigned)((a.nij + 127) / 128), 128, 0, s>>>(c, a);
+  else rain_ice_prfr_kernel<false><<<(unsigned)((a.nij + 127) / 128), 128, 0, s>>>(c, a);
   return cudaGetLastError();
 }
 

@@ -24,10 +24,16 @@
 namespace ice3pt {
 
 constexpr int RI_THREADS = 256;
-constexpr int LUT_N = sizeof(Ice3gbLuts) / sizeof(double);
+// The tables of Ice3gbLuts staged in shared memory (all but the hail
+// kernels, which the NRR = 7 instantiation reads from global memory).
+constexpr int LUT_N = 9840;
 constexpr int O_RIM1 = 0, O_RIM2 = 80, O_RIM4 = 160, O_RACCSS = 240, O_RACCS = 1840, O_SACCRG = 3440,
               O_RDRYG = 5040, O_SDRYG = 6640;
-static_assert(LUT_N == 9840, "Ice3gbLuts layout");
+constexpr int O_SWETH = 9840, O_GWETH = 13040, O_RWETH = 14640, LUT_ALL = 16240;
+static_assert(offsetof(Ice3gbLuts, ker_sweth) == sizeof(double) * O_SWETH, "Ice3gbLuts layout");
+static_assert(offsetof(Ice3gbLuts, ker_gweth) == sizeof(double) * O_GWETH, "Ice3gbLuts layout");
+static_assert(offsetof(Ice3gbLuts, ker_rweth) == sizeof(double) * O_RWETH, "Ice3gbLuts layout");
+static_assert(sizeof(Ice3gbLuts) == sizeof(double) * LUT_ALL, "Ice3gbLuts layout");
 
 enum { ITH = 0, IRV, IRC, IRR, IRI, IRS, IRG, NV };
 enum {
@@ -41,6 +47,19 @@ enum {
 };
 enum { RS_RCRIMS, RS_RCRIMSS, RS_RSRIMCG, RS_RRACCS, RS_RRACCSS, RS_RSACCRG, RS_FREEZ1, RS_FREEZ2, NRS };
 enum { RG_RCDRYG, RG_RIDRYG, RG_RIWETG, RG_RSDRYG, RG_RSWETG, RG_RRDRYG, RG_FREEZ1, RG_FREEZ2, NRG };
+// hail (NRR = 7): the eighth state variable, the graupel -> hail conversion
+// and the ICE4_FAST_RH rates (mode_ice4_fast_rh.F90 IRCWETH..IFREEZ2)
+constexpr int IRH = NV, NVH = NV + 1;
+enum {
+  BH_RWETGH, BH_RWETGH_MR, BH_RCWETH, BH_RIWETH, BH_RSWETH, BH_RGWETH, BH_RRWETH, BH_RCDRYH, BH_RIDRYH, BH_RSDRYH,
+  BH_RRDRYH, BH_RGDRYH, BH_RDRYHG, BH_RHMLTR, NBH
+};
+enum { RH_RCWETH, RH_RRWETH, RH_RIDRYH, RH_RIWETH, RH_RSDRYH, RH_RSWETH, RH_RGDRYH, RH_RGWETH, RH_FREEZ1,
+       RH_FREEZ2, NRH };
+struct HailRates {
+  double b[NBH];
+  double t[NRH];
+};
 
 // Constants derived from the table once per block (kept in shared memory).
 struct Derived {
@@ -230,8 +249,8 @@ ICE3_HD double lut2d(const double *lt, int n2, int i1, double f1, int i2, double
 // Slope parameters (mode_ice4_tendencies.F90:389-433): lbda and log(lbda) per
 // precipitating species, zero / -inf where the species is absent.
 struct Slopes {
-  double lbdar, lbdas, lbdag;
-  double llbdar, llbdas, llbdag;
+  double lbdar, lbdas, lbdag, lbdah;
+  double llbdar, llbdas, llbdag, llbdah;
 };
 
 ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const double v[NV], Slopes &s)
@@ -254,6 +273,15 @@ ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const
     s.llbdag = d.lLBG + c.LBEXG * (lrho + fm::flog(dmax(v[IRG], c.G_RTMIN)));
     s.lbdag = fm::fexp(s.llbdag);
   } else { s.lbdag = 0.0; s.llbdag = -INFINITY; }
+}
+
+// hail slope (mode_ice4_tendencies.F90:426-432)
+ICE3_HD void slope_h(const Cst &c, double lrho, double rh, Slopes &s)
+{
+  if (pos(rh)) {
+    s.llbdah = fm::flog(c.LBH) + c.LBEXH * (lrho + fm::flog(dmax(rh, c.H_RTMIN)));
+    s.lbdah = fm::fexp(s.llbdah);
+  } else { s.lbdah = 0.0; s.llbdah = -INFINITY; }
 }
 
 // log of the rain slope parameter within the precipitation fraction
@@ -324,10 +352,13 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
 // ICE4_WARM and the rate parts of ICE4_FAST_RS/RG/RI.  The parts that depend
 // on the current freezing budget (riming/accretion split, wet/dry growth
 // choice) are left to aggregate(), which every pass runs.
-template <bool SUR = false, bool SUBG = false>
+// H (NRR = 7): also the rate parts of ICE4_FAST_RH into *hr, from the hail
+// kernels at hlut (global memory); v then holds NVH values.
+template <bool SUR = false, bool SUBG = false, bool H = false>
 ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
-                        double t, const double v[NV], double cit, const double hl[4], const double hi[4],
-                        double criauti, Rates &R, bool learned_slow = false, double rainfr = 1.0)
+                        double t, const double *v, double cit, const double hl[4], const double hi[4],
+                        double criauti, Rates &R, bool learned_slow = false, double rainfr = 1.0,
+                        HailRates *hr = nullptr, const double *__restrict__ hlut = nullptr)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
@@ -344,8 +375,10 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   const double ssi_rai = fm::fdiv(R.ssi, rho * ai);
   Slopes s;
   slopes(c, d, pf.lrho, t, v, s);
+  if (H) slope_h(c, pf.lrho, v[IRH], s);
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
   const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
+  const bool has_h = H && gtp(v[IRH], c.H_RTMIN);
   const bool warm = gtp(t, c.TT);
   // ventilation factors shared by deposition, freezing and melting
   const double vent_s = has_s ? c.O0DEPS * (d.ex0deps_zero ? 1.0 : fm::fexp(c.EX0DEPS * s.llbdas)) +
@@ -359,13 +392,13 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // lbdar^EXCACCR, shared by RCACCR and (EXICFRR = EXCACCR) RICFRRG
   const double e_caccr = (has_r && (has_c || (has_i && d.icfrr_caccr))) ? fm::fexp(c.EXCACCR * s.llbdar) : 0.0;
   // lbdas^(CXS-BS) (RSACCRG, RSWETG) and lbdag^CXG (RSWETG, RRDRYG)
-  const double e_cxsbs = (has_s && (has_r || has_g)) ? fm::fexp((c.CXS - c.BS) * s.llbdas) : 0.0;
+  const double e_cxsbs = (has_s && (has_r || has_g || has_h)) ? fm::fexp((c.CXS - c.BS) * s.llbdas) : 0.0;
   const double e_cxg = (has_g && (has_s || has_r)) ? fm::fexp(c.CXG * s.llbdag) : 0.0;
   // vapour/heat term of the freezing and melting rates (mode_ice4_fast_rs.F90
   // IFREEZ1/RSMLTG, mode_ice4_fast_rg.F90 IFREEZ1/RGMLTR), e limited by the
   // saturation pressure over ice (freezing) or over water (melting)
   double heat_i = 0.0, heat_w = 0.0;
-  if (has_s || has_g) {
+  if (has_s || has_g || has_h) {
     const double ev = fm::fdiv(v[IRV] * pf.pres, c.EPSILO + v[IRV]);
     const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi) : ev;
     const double ew = c.LEVLIMIT != 0.0 ? dmin(ev, esw) : ev;
@@ -413,7 +446,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 
   // ---- ICE4_FAST_RS rates (mode_ice4_fast_rs.F90) ----
   // collision-freezing denominator, shared with ICE4_FAST_RG
-  const double den = (has_s || has_g) ? fm::frcp(rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
+  const double den = (has_s || has_g || has_h) ? fm::frcp(rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
   const double freez2 = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
   rs[RS_FREEZ1] = has_s ? heat_i * vent_s * den : 0.0;
   rs[RS_FREEZ2] = has_s ? freez2 : 0.0;
@@ -505,6 +538,57 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
                                  rho * c.LMTT));
   } else b[B_RGMLTR] = 0.0;
 
+  // ---- ICE4_FAST_RH rates (mode_ice4_fast_rh.F90, NRR = 7); the dry
+  // collection efficiency of graupel and the wet/dry choice are applied in
+  // aggregate() ----
+  if (H) {
+    double *ht = hr->t;
+    const double base_h = (has_h && (has_c || has_i)) ? fm::fexp((c.CXH - c.DH - 2.0) * s.llbdah) * pf.rho_mcexvt
+                                                      : 0.0;
+    ht[RH_RCWETH] = (has_h && has_c) ? c.FWETH * v[IRC] * base_h : 0.0;
+    if (has_h && has_i) {
+      ht[RH_RIWETH] = c.FWETH * v[IRI] * base_h;
+      ht[RH_RIDRYH] = ht[RH_RIWETH] * (c.COLIH * fm::fexp(c.COLEXIH * (t - c.TT)));
+    } else ht[RH_RIWETH] = ht[RH_RIDRYH] = 0.0;
+    const double e_cxh = (has_h && (has_s || has_g || has_r)) ? fm::fexp(c.CXH * s.llbdah) : 0.0;
+    const double ilh = has_h ? fm::frcp(s.lbdah) : 0.0;
+    if (has_h && has_s) {
+      int i1, i2;
+      const double f1 = lut_index(s.llbdah, c.NWETLBDAH, c.WETINTP1H, c.WETINTP2H, i1);
+      const double f2 = lut_index(s.llbdas, c.NWETLBDAS, c.WETINTP1S, c.WETINTP2S, i2);
+      const double zw = lut2d(hlut + O_SWETH, ICE3GB_NWETLBDAS, i1, f1, i2, f2);
+      ht[RH_RSWETH] = c.FSWETH * zw * e_cxsbs * e_cxh * pf.rho_mcexvt1 *
+                      (c.LBSWETH1 * ilh * ilh + c.LBSWETH2 * ilh * ils + c.LBSWETH3 * ils * ils);
+      ht[RH_RSDRYH] = ht[RH_RSWETH] * (c.COLSH * fm::fexp(c.COLEXSH * (t - c.TT)));
+    } else ht[RH_RSWETH] = ht[RH_RSDRYH] = 0.0;
+    if (has_h && has_g) {
+      int i1, i2;
+      const double f1 = lut_index(s.llbdah, c.NWETLBDAH, c.WETINTP1H, c.WETINTP2H, i1);
+      const double f2 = lut_index(s.llbdag, c.NWETLBDAG, c.WETINTP1G, c.WETINTP2G, i2);
+      const double zw = lut2d(hlut + O_GWETH, ICE3GB_NWETLBDAG, i1, f1, i2, f2);
+      ht[RH_RGWETH] = c.FGWETH * zw * fm::fexp((c.CXG - c.BG) * s.llbdag) * e_cxh * pf.rho_mcexvt1 *
+                      (c.LBGWETH1 * ilh * ilh + c.LBGWETH2 * ilh * ilg + c.LBGWETH3 * ilg * ilg);
+      ht[RH_RGDRYH] = ht[RH_RGWETH];
+    } else ht[RH_RGWETH] = ht[RH_RGDRYH] = 0.0;
+    if (has_h && has_r) {
+      int i1, i2;
+      const double f1 = lut_index(s.llbdah, c.NWETLBDAH, c.WETINTP1H, c.WETINTP2H, i1);
+      const double f2 = lut_index(s.llbdar, c.NWETLBDAR, c.WETINTP1R, c.WETINTP2R, i2);
+      const double zw = lut2d(hlut + O_RWETH, ICE3GB_NWETLBDAR, i1, f1, i2, f2);
+      ht[RH_RRWETH] = c.FRWETH * zw * sq(sq(ilr)) * e_cxh * pf.rho_mcexvt1 *
+                      (c.LBRWETH1 * ilh * ilh + c.LBRWETH2 * ilh * ilr + c.LBRWETH3 * ilr * ilr);
+    } else ht[RH_RRWETH] = 0.0;
+    const double vent_h = has_h ? c.O0DEPH * fm::fexp(c.EX0DEPH * s.llbdah) +
+                                      c.O1DEPH * cj * fm::fexp(c.EX1DEPH * s.llbdah)
+                                : 0.0;
+    ht[RH_FREEZ1] = has_h ? heat_i * vent_h * den : 0.0;
+    ht[RH_FREEZ2] = has_h ? freez2 : 0.0;
+    hr->b[BH_RHMLTR] = (has_h && warm) ? pmax0(fm::fdiv(-heat_w * vent_h - (ht[RH_RCWETH] + ht[RH_RRWETH]) *
+                                                                            (rho * c.CL * (c.TT - t)),
+                                                        rho * c.LMTT))
+                                       : 0.0;
+  }
+
   // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
   if (pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20)) {
     const double l = dmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(fm::fdiv(rho * v[IRI], cit))));
@@ -515,9 +599,9 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 // Rates of a soft pass: the hard-pass values where their condition still
 // holds on the current state, zero elsewhere (the ELSE branches of the
 // process routines under LDSOFT).
-template <bool SUBG = false>
-ICE3_HD void soft_rates(const Cst &c, double t, const double v[NV], double cit, const double hl[4],
-                        const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0)
+template <bool SUBG = false, bool H = false>
+ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, const double hl[4],
+                        const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0, HailRates *hr = nullptr)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
@@ -562,14 +646,30 @@ ICE3_HD void soft_rates(const Cst &c, double t, const double v[NV], double cit, 
   if (!has_g) rg[RG_FREEZ1] = rg[RG_FREEZ2] = 0.0;
   if (!(has_g && warm)) b[B_RGMLTR] = 0.0;
   if (!(pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20))) b[B_RCBERI] = 0.0;
+  if (H) {
+    double *ht = hr->t;
+    const bool has_h = gtp(v[IRH], c.H_RTMIN);
+    if (!(has_h && has_c)) ht[RH_RCWETH] = 0.0;
+    if (!(has_h && has_i)) ht[RH_RIWETH] = ht[RH_RIDRYH] = 0.0;
+    if (!(has_h && has_s)) ht[RH_RSWETH] = ht[RH_RSDRYH] = 0.0;
+    if (!(has_h && has_g)) ht[RH_RGWETH] = ht[RH_RGDRYH] = 0.0;
+    if (!(has_h && has_r)) ht[RH_RRWETH] = 0.0;
+    if (!has_h) ht[RH_FREEZ1] = ht[RH_FREEZ2] = 0.0;
+    if (!(has_h && warm)) hr->b[BH_RHMLTR] = 0.0;
+  }
 }
 
 // Freezing-budget split of riming/accretion and the wet/dry growth choice
 // (mode_ice4_fast_rs.F90:144-176, :188-219; mode_ice4_fast_rg.F90:180-260),
 // evaluated on every pass, then the aggregation into the tendency A (per
 // second), mode_ice4_tendencies.F90:606-717 (KRR = 6).
-ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact, double lsfact, Rates &R,
-                       double A[NV])
+// H (NRR = 7): also the graupel -> hail conversion (mode_ice4_fast_rg.F90:
+// 331-351), the hail growth mode of ICE4_FAST_RH (mode_ice4_fast_rh.F90:
+// 205-213, 250-325; the graupel dry-collection factor on a hard pass) and
+// the hail rows of the aggregation, which also move B (RWETGH_MR).
+template <bool H = false>
+ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, double lsfact, Rates &R,
+                       double *A, bool soft = false, HailRates *hr = nullptr, double *B = nullptr)
 {
   double *b = R.bu;
   const double *rs = R.rs, *rg = R.rg;
@@ -645,6 +745,75 @@ ICE3_HD void aggregate(const Cst &c, double t, const double v[NV], double lvfact
   A[IRG] = b[B_RVDEPG] + b[B_RCRIMSG] + b[B_RSRIMCG] + b[B_RRACCSG] + b[B_RSACCRG] + b[B_RSMLTG] + b[B_RICFRRG] +
            b[B_RRCFRIG] + b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG] + b[B_RCDRYG] + b[B_RIDRYG] +
            b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
+  if (H) {
+    double *hb = hr->b, *ht = hr->t;
+    if (ldwetg) {
+      const double rgsi = b[B_RVDEPG] + b[B_RSMLTG] + b[B_RRACCSG] + b[B_RSACCRG] + b[B_RCRIMSG] + b[B_RSRIMCG];
+      hb[BH_RWETGH] = fm::fdiv((pmax0(rgsi + b[B_RICFRRG] + b[B_RRCFRIG]) + rwetg_init) * rdryg_init,
+                               rwetg_init + rdryg_init);
+      hb[BH_RWETGH_MR] = fm::fdiv(pmax0(b[B_RRHONG_MR]) * rdryg_init, rwetg_init + rdryg_init);
+    } else {
+      hb[BH_RWETGH] = hb[BH_RWETGH_MR] = 0.0;
+    }
+    const bool has_h = gtp(v[IRH], c.H_RTMIN);
+    if (!soft && has_h && has_g && !ldwetg) ht[RH_RGDRYH] = ht[RH_RGDRYH] * (c.COLGH * fm::fexp(c.COLEXGH * (t - c.TT)));
+    const double rdryh_init = ht[RH_RCWETH] + ht[RH_RIDRYH] + ht[RH_RSDRYH] + ht[RH_RRWETH] + ht[RH_RGDRYH];
+    bool llweth = false, lldryh = false;
+    double rweth_init = 0.0;
+    if (has_h) {
+      const double isg = ht[RH_RIWETH] + ht[RH_RSWETH] + ht[RH_RGWETH];
+      rweth_init = dmax(isg, pmax0(ht[RH_FREEZ1] + ht[RH_FREEZ2] * isg));
+      const double wet = pmax0(rweth_init - ht[RH_RIWETH] - ht[RH_RSWETH] - ht[RH_RGWETH]);
+      const double dry = pmax0(rdryh_init - ht[RH_RIDRYH] - ht[RH_RSDRYH] - ht[RH_RGDRYH]);
+      llweth = !gtd(wet, dry);
+      if (c.LNULLWETH != 0.0) llweth = llweth && pos(rdryh_init);
+      else llweth = llweth && pos(rweth_init);
+      if (c.LWETHPOST == 0.0) llweth = llweth && cold;
+      lldryh = cold && gtp(rdryh_init, 1.e-20) &&
+               gtd(pmax0(rweth_init - ht[RH_RIWETH] - ht[RH_RSWETH]), pmax0(rdryh_init - ht[RH_RIDRYH] - ht[RH_RSDRYH]));
+    }
+    if (llweth) {
+      hb[BH_RCWETH] = ht[RH_RCWETH];
+      hb[BH_RIWETH] = ht[RH_RIWETH];
+      hb[BH_RSWETH] = ht[RH_RSWETH];
+      hb[BH_RGWETH] = ht[RH_RGWETH];
+      hb[BH_RRWETH] = rweth_init - ht[RH_RIWETH] - ht[RH_RSWETH] - ht[RH_RGWETH] - ht[RH_RCWETH];
+    } else {
+      hb[BH_RCWETH] = hb[BH_RIWETH] = hb[BH_RSWETH] = hb[BH_RGWETH] = hb[BH_RRWETH] = 0.0;
+    }
+    if (lldryh) {
+      hb[BH_RCDRYH] = ht[RH_RCWETH];
+      hb[BH_RIDRYH] = ht[RH_RIDRYH];
+      hb[BH_RSDRYH] = ht[RH_RSDRYH];
+      hb[BH_RRDRYH] = ht[RH_RRWETH];
+      hb[BH_RGDRYH] = ht[RH_RGDRYH];
+      hb[BH_RDRYHG] = c.LCONVHG != 0.0 ? fm::fdiv(rdryh_init * rweth_init, rdryh_init + rweth_init) : 0.0;
+    } else {
+      hb[BH_RCDRYH] = hb[BH_RIDRYH] = hb[BH_RSDRYH] = hb[BH_RRDRYH] = hb[BH_RGDRYH] = hb[BH_RDRYHG] = 0.0;
+    }
+    // hail rows of mode_ice4_tendencies.F90:619-715
+    A[ITH] += (hb[BH_RRWETH] + hb[BH_RCWETH]) * lsv;
+    A[ITH] += (hb[BH_RCDRYH] + hb[BH_RRDRYH]) * lsv;
+    A[ITH] -= hb[BH_RHMLTR] * lsv;
+    A[IRC] -= hb[BH_RCWETH];
+    A[IRC] -= hb[BH_RCDRYH];
+    A[IRR] -= hb[BH_RRWETH];
+    A[IRR] -= hb[BH_RRDRYH];
+    A[IRR] += hb[BH_RHMLTR];
+    A[IRI] -= hb[BH_RIWETH];
+    A[IRI] -= hb[BH_RIDRYH];
+    A[IRS] -= hb[BH_RSWETH];
+    A[IRS] -= hb[BH_RSDRYH];
+    A[IRG] -= hb[BH_RWETGH];
+    B[IRG] -= hb[BH_RWETGH_MR];
+    A[IRG] -= hb[BH_RGWETH];
+    A[IRG] = A[IRG] - hb[BH_RGDRYH] + hb[BH_RDRYHG];
+    A[IRH] = hb[BH_RWETGH];
+    B[IRH] += hb[BH_RWETGH_MR];
+    A[IRH] = A[IRH] + hb[BH_RCWETH] + hb[BH_RIWETH] + hb[BH_RSWETH] + hb[BH_RGWETH] + hb[BH_RRWETH];
+    A[IRH] = A[IRH] + hb[BH_RCDRYH] + hb[BH_RIDRYH] + hb[BH_RSDRYH] + hb[BH_RRDRYH] + hb[BH_RGDRYH] - hb[BH_RDRYHG];
+    A[IRH] -= hb[BH_RHMLTR];
+  }
 }
 
 // The five ICE4_SLOW rates of a hard pass taken from the learned surrogate
@@ -709,16 +878,18 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
 // nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
 // and all rates are computed; a soft pass keeps the hard-pass rates.
-template <bool SUR = false, bool SUBG = false>
+template <bool SUR = false, bool SUBG = false, bool H = false>
 ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict__ lut, bool soft,
                         const PointFix &pf, double lvfact, double lsfact, double &cit, double t0,
-                        const double vart[NV], Rates &R, double &rainfr, double hl[4], double hi[4], double A[NV],
-                        double B[NV], const double *sur = nullptr)
+                        const double *vart, Rates &R, double &rainfr, double hl[4], double hi[4], double *A,
+                        double *B, const double *sur = nullptr, HailRates *hr = nullptr,
+                        const double *__restrict__ hlut = nullptr)
 {
-  double v[NV];
+  constexpr int NVT = H ? NVH : NV;
+  double v[NVT];
   double t = t0;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) { v[k] = vart[k]; B[k] = 0.0; }
+  for (int k = 0; k < NVT; ++k) { v[k] = vart[k]; B[k] = 0.0; }
   double *b = R.bu;
   if (!soft) {
     hard_adjust(c, d, pf, lvfact, lsfact, cit, t, v, b, B);
@@ -730,25 +901,35 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
   if (llrfr) {
     rainfr = dmax(rainfr, zrainfr);
-    if ((gtp(v[IRR], c.R_RTMIN) || gtp(v[IRS], c.S_RTMIN) || gtp(v[IRG], c.G_RTMIN)) && zerod(rainfr)) rainfr = 1.;
+    bool mask = gtp(v[IRR], c.R_RTMIN) || gtp(v[IRS], c.S_RTMIN) || gtp(v[IRG], c.G_RTMIN);
+    if (H) mask = mask || gtp(v[NVT - 1], c.H_RTMIN);
+    if (mask && zerod(rainfr)) rainfr = 1.;
   } else {
     rainfr = 1.;
   }
-  if (!soft) hard_rates<SUR, SUBG>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr);
-  else soft_rates<SUBG>(c, t, v, cit, hl, hi, R, pf.cf, rainfr);
+  if (!soft) hard_rates<SUR, SUBG, H>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr, hr, hlut);
+  else soft_rates<SUBG, H>(c, t, v, cit, hl, hi, R, pf.cf, rainfr, hr);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
-  aggregate(c, t, v, lvfact, lsfact, R, A);
+  aggregate<H>(c, t, v, lvfact, lsfact, R, A, soft, hr, B);
 }
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
-template <bool SUR = false, bool SUBG = false>
+template <bool SUR = false, bool SUBG = false, bool H = false>
 ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
-                              double dt, int max_passes, double vart[NV], const double ext[NV], double &cit,
+                              double dt, int max_passes, double *vart, const double *ext, double &cit,
                               double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped,
-                              const double *sur = nullptr)
+                              const double *sur = nullptr, const double *__restrict__ hlut = nullptr)
 {
-  const double rsmin[NV] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN};
+  constexpr int NVT = H ? NVH : NV;
+  const double rsmin[NVH] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN, c.H_RTMIN};
+  HailRates HR;
+  if (H) {
+#pragma unroll
+    for (int k = 0; k < NBH; ++k) HR.b[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NRH; ++k) HR.t[k] = 0.0;
+  }
   Rates R;
 #pragma unroll
   for (int k = 0; k < NBU; ++k) R.bu[k] = 0.0;
@@ -773,16 +954,18 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       if (passes >= max_passes) { capped = true; return 0u; }
       ++passes;
       ++inner;
-      const double zsum2 = vart[IRI] + vart[IRS] + vart[IRG];
+      double zsum2 = vart[IRI] + vart[IRS] + vart[IRG];
+      if (H) zsum2 += vart[IRH];
       const double zdev = (c.CPD + c.CPV * vart[IRV] + c.CL * (vart[IRC] + vart[IRR]) + c.CI * zsum2) * pf.exn;
       const double zzt = vart[ITH] * pf.exn;
       const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
-      double A[NV], B[NV];
-      tendencies<SUR, SUBG>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur);
+      double A[NVT], B[NVT];
+      tendencies<SUR, SUBG, H>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
+                               &HR, hlut);
       if (SUR) sur = nullptr;          // learned slow rates: first hard pass only
 #pragma unroll
-      for (int v = 0; v < NV; ++v) A[v] += ext[v];
+      for (int v = 0; v < NVT; ++v) A[v] += ext[v];
       double maxtime = dt - ztime;
       if (c.LFEEDBACKT != 0.0) {
         if (negd((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx))) maxtime = 0.;
@@ -792,7 +975,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
         }
       }
 #pragma unroll
-      for (int v = 1; v < NV; ++v) {
+      for (int v = 1; v < NVT; ++v) {
         if (ltd(A[v], -1.e-20) && gtp(vart[v], rsmin[v])) {
           maxtime = dmin(maxtime, -(B[v] + vart[v]) / A[v]);
           maxtime = dmax(maxtime, c.MNH_TINY);
@@ -807,7 +990,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       // follow the un-contracted evaluation of the Fortran (and of the CPU
       // reference) rather than a fused multiply-add.
 #pragma unroll
-      for (int v = 0; v < NV; ++v) vart[v] = add_rn(add_rn(vart[v], mul_rn(A[v], maxtime)), B[v]);
+      for (int v = 0; v < NVT; ++v) vart[v] = add_rn(add_rn(vart[v], mul_rn(A[v], maxtime)), B[v]);
       if (!pos(vart[IRI])) cit = 0.;
       ztime += maxtime;
       rrevav = R.bu[B_RREVAV];
@@ -832,11 +1015,13 @@ ICE3_HD double ldp(const double *p, long i)
 // sub-stepping, total tendencies and ICE4_CORRECT_NEGATIVITIES on the
 // sources, written back in place.  Returns the pass key (0 for points
 // outside LLMICRO or capped); `capped` reports a point that hit max_passes.
-template <bool SUR = false, bool SUBG = false>
+// H (NRR = 7): with hail (rht / rhs; the hail kernels at hlut).
+template <bool SUR = false, bool SUBG = false, bool H = false>
 ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
                                     const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped,
-                                    const double *sur = nullptr)
+                                    const double *sur = nullptr, const double *__restrict__ hlut = nullptr)
 {
+  constexpr int NVT = H ? NVH : NV;
   const double inv_dt = 1.0 / dt;
   const bool lwarm = c.LWARM != 0.0;
   const bool sigm = (int)c.SUBG_AUCV_RC == 1 && (int)c.SUBG_PR_PDF == 0;
@@ -853,13 +1038,15 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   double ths = f.ths[p], rvs = f.rvs[p], rcs = f.rcs[p], rrs = f.rrs[p], ris = f.ris[p], rss = f.rss[p],
          rgs = f.rgs[p];
   double cit = f.cit[p];
+  const double rh = H ? ldp(f.rht, p) : 0.0;
+  double rhs = H ? f.rhs[p] : 0.0;
   // rain_ice.F90:334-345 (L/cph without exner) and :370-381 (LLMICRO)
-  const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
+  const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (H ? ri + rs + rg + rh : ri + rs + rg);
   const double t = th * pf.exn;
   const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
   const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
   const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
-                     gtp(rg, c.G_RTMIN);
+                     gtp(rg, c.G_RTMIN) || (H && gtp(rh, c.H_RTMIN));
   const double iexnref = fm::frcp(exnref);
   const double lsx = lsf * iexnref, lvx = lvf * iexnref;
   // with a PRFR option the sub-stepping starts from the precipitation
@@ -880,9 +1067,15 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
     pf.rcrautc = c.CRIAUTC * irho;
     pf.cf = ldp(f.cldfr, p);
     pf.sigma_rc = sigm ? 2.0 * ldp(f.sigs, p) : 0.0;
-    double vart[NV] = {th, rv, rc, rr, ri, rs, rg};
-    double ext[NV] = {ths - th * inv_dt, rvs - rv * inv_dt, rcs - rc * inv_dt, rrs - rr * inv_dt,
-                      ris - ri * inv_dt, rss - rs * inv_dt, rgs - rg * inv_dt};
+    double vart[NVT], ext[NVT];
+    vart[ITH] = th; vart[IRV] = rv; vart[IRC] = rc; vart[IRR] = rr; vart[IRI] = ri; vart[IRS] = rs; vart[IRG] = rg;
+    ext[ITH] = ths - th * inv_dt; ext[IRV] = rvs - rv * inv_dt; ext[IRC] = rcs - rc * inv_dt;
+    ext[IRR] = rrs - rr * inv_dt; ext[IRI] = ris - ri * inv_dt; ext[IRS] = rss - rs * inv_dt;
+    ext[IRG] = rgs - rg * inv_dt;
+    if (H) {
+      vart[NVT - 1] = rh;
+      ext[NVT - 1] = rhs - rh * inv_dt;
+    }
     double hl[4] = {0.0, 0.0, 0.0, 0.0}, hi[4] = {0.0, 0.0, 0.0, 0.0};
     if (adju) {
       hl[0] = f.hlc_hcf[p]; hl[2] = f.hlc_hrc[p]; hi[0] = f.hli_hcf[p]; hi[2] = f.hli_hri[p];
@@ -892,15 +1085,18 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
       hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
     }
     double rrevav;
-    key = stepping<SUR, SUBG>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur);
+    key = stepping<SUR, SUBG, H>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur,
+                                 hlut);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) vart[v] -= ext[v] * dt;
+    for (int v = 0; v < NVT; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;
     // total tendencies (rain_ice.F90:758-790)
     const double wv = (vart[IRV] - rv) * inv_dt, wc = (vart[IRC] - rc) * inv_dt;
     const double wr = (vart[IRR] - rr) * inv_dt, wi = (vart[IRI] - ri) * inv_dt;
     const double ws = (vart[IRS] - rs) * inv_dt, wg = (vart[IRG] - rg) * inv_dt;
-    ths += (wc + wr) * lvx + (wi + ws + wg) * lsx + zrvheni * lsx;
+    const double wh = H ? (vart[NVT - 1] - rh) * inv_dt : 0.0;
+    ths += (wc + wr) * lvx + (H ? wi + ws + wg + wh : wi + ws + wg) * lsx + zrvheni * lsx;
+    if (H) rhs += wh;
     rvs += wv - zrvheni;
     rcs += wc;
     rrs += wr;
@@ -919,6 +1115,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
   w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
   w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
+  if (H) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
   w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
   ths -= w * (rcs * lvx + ris * lsx);
   rvs += w * (rcs + ris);
@@ -927,8 +1124,10 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
   w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
   w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
+  if (H) { w = dmin(pmax0(rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; rhs -= w; ths -= w * lsx; }
   f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
   f.rgs[p] = rgs;
+  if (H) f.rhs[p] = rhs;
   f.cit[p] = cit;
   f.evap3d[p] = evap;
   f.rainfr[p] = rainfr;
@@ -943,6 +1142,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
 // from the top level down (mode_ice4_rainfr_vert.F90: 0 at the top, the
 // maximum with the level above where rain, snow or graupel is present, 1 if
 // that is 0, else 0).  Writes f.rainfr of the column.
+template <bool H = false>
 ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, int nk, long col)
 {
   const int aucv_rc = (int)c.SUBG_AUCV_RC, aucv_ri = (int)c.SUBG_AUCV_RI;
@@ -953,8 +1153,9 @@ ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, i
     const long p = (long)k * nij + col;
     const double rc = ldp(f.rct, p), rr = ldp(f.rrt, p), ri = ldp(f.rit, p), rs = ldp(f.rst, p);
     const double rg = ldp(f.rgt, p), cf = ldp(f.cldfr, p);
+    const bool has_h = H && gtp(ldp(f.rht, p), c.H_RTMIN);
     const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
-                       gtp(rg, c.G_RTMIN);
+                       gtp(rg, c.G_RTMIN) || has_h;
     double hl[4] = {f.hlc_hcf[p], 0.0, f.hlc_hrc[p], 0.0}, hi[4] = {f.hli_hcf[p], 0.0, f.hli_hri[p], 0.0};
     if (adju) {                                                    // rain_ice.F90:564-581
       hl[3] = rc - hl[2];
@@ -976,7 +1177,7 @@ ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, i
     }
     f.hlc_hcf[p] = hl[0]; f.hlc_hrc[p] = hl[2]; f.hli_hcf[p] = hi[0]; f.hli_hri[p] = hi[2];
     double pr = 0.0;
-    if (k < nk - 1 && (gtp(rr, c.R_RTMIN) || gtp(rs, c.S_RTMIN) || gtp(rg, c.G_RTMIN))) {
+    if (k < nk - 1 && (gtp(rr, c.R_RTMIN) || gtp(rs, c.S_RTMIN) || gtp(rg, c.G_RTMIN) || has_h)) {
       pr = dmax(rf, above);
       if (zerod(pr)) pr = 1.0;
     }

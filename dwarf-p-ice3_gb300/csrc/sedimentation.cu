@@ -43,6 +43,8 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constan
   io.nij = a.nij;
   io.nk = a.nk;
   sed_column_forward(c, a.fortran, skip_c, cp, a.dt, io, col);
+  // hail (NRR = 7), an independent species: its own sweep of the column
+  if (a.hsrc) sed_hail_column(c, a.dt, a.rhodref, a.dzz, a.hsrc, a.hfpr, a.hinpr, a.nij, a.nk, col);
 }
 
 // Fog deposition on the lowest level (rain_ice.F90:876-895).
@@ -65,6 +67,11 @@ __global__ void __launch_bounds__(128) sedimentation_split_kernel(const __grid_c
     io.fpr[s] = a.sed.fpr[s];
     io.inpr[s] = a.sed.inpr[s];
   }
+  io.nsp = a.rht ? 6 : 5;
+  io.rt[5] = a.rht;
+  io.src[5] = a.sed.hsrc;
+  io.fpr[5] = a.sed.hfpr;
+  io.inpr[5] = a.sed.hinpr;
   io.rtmp = a.scratch;
   io.ext = a.scratch + n;
   io.nij = a.sed.nij;

@@ -60,6 +60,8 @@ ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlb
     }
     case 3:  // snow
       return c.FSEDS * fm::fexp((c.EXSEDS - 1.0) * lr + (c.EXSEDS - c.CEXVT - 1.0) * lrho);
+    case 5:  // hail (NRR = 7): OTHER_SPECIES with XFSEDH / XEXSEDH, F90:186-187
+      return c.FSEDH * fm::fexp((c.EXSEDH - 1.0) * lr + (c.EXSEDH - c.CEXVT - 1.0) * lrho);
     default:  // graupel
       return c.FSEDG * fm::fexp((c.EXSEDG - 1.0) * lr + (c.EXSEDG - c.CEXVT - 1.0) * lrho);
   }
@@ -126,7 +128,8 @@ struct SedColumnIO {
 ICE3_HD double sed_rtmin(const Cst &c, int s)
 {
   return (s == 0) ? c.C_RTMIN : (s == 1) ? c.R_RTMIN : (s == 2) ? dmax(c.I_RTMIN, 1.0e-7) : (s == 3) ? c.S_RTMIN
-                                                                                                : c.G_RTMIN;
+                                                                                     : (s == 4) ? c.G_RTMIN
+                                                                                                : c.H_RTMIN;
 }
 
 ICE3_HD double sed_load(const double *p, long i)
@@ -190,6 +193,34 @@ ICE3_HD void sed_column_forward(const Cst &c, bool fortran, bool skip_c, const C
 #pragma unroll
   for (int s = 0; s < 5; ++s)
     if (!(s == 0 && skip_c) && io.inpr[s]) io.inpr[s][col] = fabove[s] / c.RHOLW;
+}
+
+// Hail in the statistical sweep (NRR = 7; species 7 of
+// mode_ice4_sedimentation_stat.F90:186-222, Fortran semantics) for one
+// column: the hail content is rhs * dt (mode_ice4_sedimentation.F90:179).
+ICE3_HD void sed_hail_column(const Cst &c, double dt, const double *rhodref, const double *dzz, double *rhs,
+                             double *fpr, double *inpr, long nij, int nk, long col)
+{
+  const double inv_dt = 1.0 / dt;
+  const CloudPar cp{};
+  double fabove = 0.0;
+  for (int k = nk - 1; k >= 0; --k) {
+    const long p = (long)k * nij + col;
+    const double rho = sed_load(rhodref, p), dz = sed_load(dzz, p);
+    const double rhodz = rho * dz;
+    const double tsorhodz = fm::fdiv(dt, rhodz);
+    const double src = rhs[p], rt = src * dt, qp = fabove * tsorhodz;
+    const bool c1 = gtp(rt, c.H_RTMIN), c2 = gtp(qp, c.H_RTMIN);
+    const double lrho = (c1 || c2) ? fm::flog(rho) : 0.0;
+    const double w1 = c1 ? fall_speed(c, 5, rt, lrho, 0.0, cp) : 0.0;
+    const double w2 = c2 ? fall_speed(c, 5, qp, lrho, 0.0, cp) : 0.0;
+    double flux = dmin(rhodz * rt * inv_dt, w1 * rho * rt);
+    if (!zerod_(w2)) flux += pmax0(1.0 - fm::fdiv(dz, dt * w2)) * fabove;
+    rhs[p] = src + tsorhodz * (fabove - flux) * inv_dt;
+    if (fpr) fpr[p] = flux;
+    fabove = flux;
+  }
+  inpr[col] = fabove / c.RHOLW;
 }
 
 // Cotangents of the sweep's outputs (NULL = zero) and the wanted gradients
@@ -336,15 +367,16 @@ ICE3_HD void sed_column_vjp(const Cst &c, bool fortran, bool skip_c, const Cloud
 // divergence.
 struct SplitColumnIO {
   const double *rhodref, *dzz, *pabs, *tht, *exn;
-  const double *rt[5];       // mixing ratios at t: rc rr ri rs rg
+  const double *rt[6];       // mixing ratios at t: rc rr ri rs rg (rh)
   const double *rvt;
-  double *src[5];            // in-out sources rcs rrs ris rss rgs
+  double *src[6];            // in-out sources rcs rrs ris rss rgs (rhs)
   double *rvs, *ths;         // in-out (negativity correction)
-  double *fpr[5];            // accumulated fluxes, or NULL
-  double *inpr[5];           // [nij]
+  double *fpr[6];            // accumulated fluxes, or NULL
+  double *inpr[6];           // [nij]
   double *rtmp, *ext;        // [nk][nij] scratch: temporary mixing ratio, external tendency
   long nij;
   int nk;
+  int nsp;                   // 5, or 6 with hail (NRR = 7, species 7 of :340-347)
 };
 
 // Flux rho r v(r) of species s at content r (0 below the species' threshold;
@@ -365,7 +397,7 @@ ICE3_HD double split_flux(const Cst &c, int s, double r, double rho, double lrho
 // ICE4_CORRECT_NEGATIVITIES on the sources (mode_ice4_correct_negativities.F90)
 // with the latent-heat factors lv / ls.
 ICE3_HD void correct_negativities(const Cst &c, double lv, double ls, double &ths, double &rvs, double &rcs,
-                                  double &rrs, double &ris, double &rss, double &rgs)
+                                  double &rrs, double &ris, double &rss, double &rgs, double *rhs = nullptr)
 {
   double w;
   w = rcs - pmax0(rcs); rvs += w; ths -= w * lv; rcs -= w;
@@ -373,6 +405,7 @@ ICE3_HD void correct_negativities(const Cst &c, double lv, double ls, double &th
   w = ris - pmax0(ris); rvs += w; ths -= w * ls; ris -= w;
   w = rss - pmax0(rss); rvs += w; ths -= w * ls; rss -= w;
   w = rgs - pmax0(rgs); rvs += w; ths -= w * ls; rgs -= w;
+  if (rhs) { w = *rhs - pmax0(*rhs); rvs += w; ths -= w * ls; *rhs -= w; }   // :115-120
   w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
   ths -= w * (rcs * lv + ris * ls);
   rvs += w * (rcs + ris);
@@ -381,6 +414,7 @@ ICE3_HD void correct_negativities(const Cst &c, double lv, double ls, double &th
   w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lv;
   w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * ls;
   w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * ls;
+  if (rhs) { w = dmin(pmax0(*rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; *rhs -= w; ths -= w * ls; }   // :165-171
 }
 
 // One column; returns false if a species needed more than max_iter sub-steps
@@ -390,14 +424,15 @@ ICE3_HD bool sed_split_column(const Cst &c, const CloudPar &cp, double dt, const
 {
   const double inv_dt = 1.0 / dt;
   bool ok = true;
-  for (int s = 0; s < 5; ++s) {
+  for (int s = 0; s < io.nsp; ++s) {
     if (s == 0 && c.LSEDIC == 0.0) {          // GSEDIC = .FALSE.: cloud not sedimented
       if (io.inpr[0]) io.inpr[0][col] = 0.0;
       if (io.fpr[0])
         for (int k = 0; k < io.nk; ++k) io.fpr[0][(long)k * io.nij + col] = 0.0;
       continue;
     }
-    const double rtmin = s == 0 ? c.C_RTMIN : s == 1 ? c.R_RTMIN : s == 2 ? c.I_RTMIN : s == 3 ? c.S_RTMIN : c.G_RTMIN;
+    const double rtmin = s == 0 ? c.C_RTMIN : s == 1 ? c.R_RTMIN : s == 2 ? c.I_RTMIN : s == 3 ? c.S_RTMIN
+                                                                                  : s == 4 ? c.G_RTMIN : c.H_RTMIN;
     for (int k = 0; k < io.nk; ++k) {
       const long p = (long)k * io.nij + col;
       const double r = sed_load(io.rt[s], p);
@@ -445,15 +480,19 @@ ICE3_HD bool sed_split_column(const Cst &c, const CloudPar &cp, double dt, const
     const long p = (long)k * io.nij + col;
     const double rv = sed_load(io.rvt, p), rc = sed_load(io.rt[0], p), rr = sed_load(io.rt[1], p);
     const double ri = sed_load(io.rt[2], p), rs = sed_load(io.rt[3], p), rg = sed_load(io.rt[4], p);
-    const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (ri + rs + rg);
+    const bool hail = io.nsp == 6;
+    const double zice = hail ? ri + rs + rg + sed_load(io.rt[5], p) : ri + rs + rg;
+    const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * zice;
     const double t = sed_load(io.tht, p) * sed_load(io.exn, p);
     const double ls = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
     const double lv = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
     double ths = io.ths[p], rvs = io.rvs[p], rcs = io.src[0][p], rrs = io.src[1][p], ris = io.src[2][p];
     double rss = io.src[3][p], rgs = io.src[4][p];
-    correct_negativities(c, lv, ls, ths, rvs, rcs, rrs, ris, rss, rgs);
+    double rhs = hail ? io.src[5][p] : 0.0;
+    correct_negativities(c, lv, ls, ths, rvs, rcs, rrs, ris, rss, rgs, hail ? &rhs : nullptr);
     io.ths[p] = ths; io.rvs[p] = rvs; io.src[0][p] = rcs; io.src[1][p] = rrs; io.src[2][p] = ris;
     io.src[3][p] = rss; io.src[4][p] = rgs;
+    if (hail) io.src[5][p] = rhs;
   }
   return ok;
 }

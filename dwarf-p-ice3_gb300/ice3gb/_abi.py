@@ -55,7 +55,8 @@ class RainIceFields(ctypes.Structure):
         "cit", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf",
         "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs",
         "evap3d", "rainfr", "inprc", "inprr", "inpri", "inprs", "inprg", "indep",
-        "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")]
+        "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g",
+        "rht", "rhs", "inprh", "fpr_h")]          # hail, NRR = 7
 
 
 class StepFields(ctypes.Structure):

@@ -301,6 +301,17 @@ class RainIce:
                 if key.startswith("hl") or key == "ci_t" or key.endswith("s"):
                     v = torch.zeros(shape, dtype=torch.float64, device=ref_t.device)
             fields[abi] = self._to_kij(v).clone()
+        hail = self.table.values["NRR"] == 7.0
+        if hail:
+            # NRR = 7: hail at t and its source (RainIceJAX's state has no hail;
+            # the keys follow its naming, rh_t / rhs)
+            rh = get("rh_t")
+            if rh is None:
+                raise KeyError("state is missing 'rh_t' (NRR = 7)")
+            fields["rht"] = self._to_kij(rh)
+            rhs = get("rhs")
+            fields["rhs"] = (self._to_kij(rhs) if rhs is not None
+                             else torch.zeros((nk, nij), dtype=torch.float64, device=ref_t.device)).clone()
         sea, town = get("sea"), get("town")
         if (sea is None) != (town is None):
             raise ValueError("sea and town must be given together")
@@ -312,6 +323,10 @@ class RainIce:
         if with_fluxes:
             diag.update({k: torch.empty((nk, nij), dtype=torch.float64, device=dev)
                          for k in ("fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")})
+        if hail:
+            diag["inprh"] = torch.empty((nij,), dtype=torch.float64, device=dev)
+            if with_fluxes:
+                diag["fpr_h"] = torch.empty((nk, nij), dtype=torch.float64, device=dev)
         f = _abi.RainIceFields()
         for k, v in fields.items():
             setattr(f, k, _ptr(v))
@@ -355,6 +370,9 @@ class RainIce:
         for key, abi in RI_STATE_INOUT.items():
             v = self._from_kij(fields[abi], shape)
             out_state[key] = v.numpy() if host else v
+        if "rhs" in fields:
+            v = self._from_kij(fields["rhs"], shape)
+            out_state["rhs"] = v.numpy() if host else v
         diagnostics = {}
         for k, v in diag.items():
             v = self._from_kij(v, shape) if v.dim() == 2 else v

@@ -36,6 +36,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _HEADER = os.path.normpath(os.path.join(_HERE, "..", "..", "include", "ice3gb.h"))
 
 NGAMINC, NACCLBDAS, NACCLBDAR, NDRYLBDAG, NDRYLBDAS, NDRYLBDAR = 80, 40, 40, 40, 80, 40
+NWETLBDAH, NWETLBDAS, NWETLBDAG, NWETLBDAR = 40, 80, 40, 40
 
 
 def constant_names(header: str = _HEADER) -> List[str]:
@@ -68,6 +69,9 @@ class Ice3gbLuts(ctypes.Structure):
         ("ker_saccrg", ctypes.c_double * (NACCLBDAR * NACCLBDAS)),
         ("ker_rdryg", ctypes.c_double * (NDRYLBDAG * NDRYLBDAR)),
         ("ker_sdryg", ctypes.c_double * (NDRYLBDAG * NDRYLBDAS)),
+        ("ker_sweth", ctypes.c_double * (NWETLBDAH * NWETLBDAS)),
+        ("ker_gweth", ctypes.c_double * (NWETLBDAH * NWETLBDAG)),
+        ("ker_rweth", ctypes.c_double * (NWETLBDAH * NWETLBDAR)),
     ]
 
 
@@ -127,17 +131,90 @@ class ConstantsTable:
 _DEFAULTS = {"OCND2": 0.0}
 
 
+def _hail_constants(ext: Mapping[str, Any]) -> Dict[str, float]:
+    """The hail constants of INI_RAIN_ICE, which the reference's Python
+    initialisation leaves out (rain_ice_parameters.py:1094): hailstone
+    characteristics (mode_ini_rain_ice.F90:375-392, 436-437), slope and
+    sedimentation (:462-463, :547-549), deposition/melting ventilation
+    (:633-636) and wet growth (:1226-1291), the switches of
+    modd_param_icen.F90 for AROME (LNULLWETH, LWETHPOST, LCONVHG).  The rain,
+    snow and graupel distributions are the table's (ALPHAR, NUR, ...), as for
+    the other collection constants of the table."""
+    from math import exp, gamma, log, sqrt
+
+    def momg(alpha, nu, p):
+        return gamma(nu + p / alpha) / gamma(nu)
+
+    f = lambda k: float(ext[k])  # noqa: E731
+    pi = f("PI")
+    ah, bh, ch, dh, cch, cxh = 470.0, 3.0, 207.0, 0.64, 4.0e4, -1.0
+    f0h, f1h, c1h, alphah, nuh = 0.86, 0.28, 0.5, 1.0, 8.0
+    cexvt = f("CEXVT")
+    # reference density (mode_ini_rain_ice.F90:493-496); LUPDATE_SNOW = XFRMIN(16) > 0 is off
+    ze = 0.5 * exp(f("ALPW") - f("BETAW") / 293.15 - f("GAMW") * log(293.15))
+    zrv = (f("RD") / f("RV")) * ze / (101325.0 - ze)
+    rho00 = 101325.0 * (1.0 + zrv) / (f("RD") + zrv * f("RV")) / 293.15
+    rho00_snow = rho00
+    v = {"H_RTMIN": 1.0e-15, "CXH": cxh, "DH": dh}
+    v["LBEXH"] = 1.0 / (cxh - bh)
+    v["LBH"] = (ah * cch * momg(alphah, nuh, bh)) ** (-v["LBEXH"])
+    v["EXSEDH"] = (bh + dh - cxh) / (bh - cxh)
+    v["FSEDH"] = (ch * ah * cch * momg(alphah, nuh, bh + dh) * (ah * cch * momg(alphah, nuh, bh)) ** (-v["EXSEDH"])
+                  * rho00 ** cexvt)
+    v["O0DEPH"] = (4.0 * pi) * cch * c1h * f0h * momg(alphah, nuh, 1.0)
+    v["O1DEPH"] = (4.0 * pi) * cch * c1h * f1h * sqrt(ch) * momg(alphah, nuh, 0.5 * dh + 1.5)
+    v["EX0DEPH"] = cxh - 1.0
+    v["EX1DEPH"] = cxh - 0.5 * (dh + 3.0)
+    v["COLIH"], v["COLEXIH"] = 0.01, 0.1
+    v["FWETH"] = (pi / 4.0) * cch * ch * (rho00 ** cexvt) * momg(alphah, nuh, dh + 2.0)
+    v["COLSH"], v["COLEXSH"] = 0.01, 0.1
+    v["FSWETH"] = (pi / 4.0) * cch * f("CCS") * f("A_S") * (rho00_snow ** cexvt)     # LNEWCOEFF = .FALSE.
+    al_s, nu_s, bs = f("ALPHAS"), f("NUS"), f("BS")
+    v["LBSWETH1"] = momg(alphah, nuh, 2.0) * momg(al_s, nu_s, bs)
+    v["LBSWETH2"] = 2.0 * momg(alphah, nuh, 1.0) * momg(al_s, nu_s, bs + 1.0)
+    v["LBSWETH3"] = momg(al_s, nu_s, bs + 2.0)
+    v["COLGH"], v["COLEXGH"] = 0.01, 0.1
+    v["FGWETH"] = (pi / 4.0) * cch * f("CCG") * f("AG") * (rho00 ** cexvt)
+    al_g, nu_g, bg = f("ALPHAG"), f("NUG"), f("BG")
+    v["BG"] = bg
+    v["LBGWETH1"] = momg(alphah, nuh, 2.0) * momg(al_g, nu_g, bg)
+    v["LBGWETH2"] = 2.0 * momg(alphah, nuh, 1.0) * momg(al_g, nu_g, bg + 1.0)
+    v["LBGWETH3"] = momg(al_g, nu_g, bg + 2.0)
+    v["FRWETH"] = (pi / 4.0) * cch * f("CCR") * f("AR") * (rho00 ** cexvt)
+    al_r, nu_r, br = f("ALPHAR"), f("NUR"), f("BR")
+    v["LBRWETH1"] = momg(alphah, nuh, 2.0) * momg(al_r, nu_r, br)
+    v["LBRWETH2"] = 2.0 * momg(alphah, nuh, 1.0) * momg(al_r, nu_r, br + 1.0)
+    v["LBRWETH3"] = momg(al_r, nu_r, br + 2.0)
+    # tabulation grids (:1265-1291): one magnitude of lambda over 10 points
+    for x, n, lo, hi in (("S", 80, 2.5e1, 2.5e9), ("G", 40, 1.0e3, 1.0e7), ("R", 40, 1.0e3, 1.0e7),
+                         ("H", 40, 1.0e3, 1.0e7)):
+        zrate = log(hi / lo) / float(n - 1)
+        v[f"NWETLBDA{x}"] = float(n)
+        v[f"WETINTP1{x}"] = 1.0 / zrate
+        v[f"WETINTP2{x}"] = 1.0 - log(lo) / zrate
+    v["LNULLWETH"], v["LWETHPOST"], v["LCONVHG"] = 1.0, 1.0, 1.0
+    return v
+
+
+def _hail_kernels() -> Dict[str, np.ndarray]:
+    d = np.load(os.path.join(_HERE, "data", "hail_kernels.npz"))
+    return {k: d[k] for k in ("ker_sweth", "ker_gweth", "ker_rweth")}
+
+
 def build_table(phyex: Any = None, table: str = "jax", program: str = "AROME",
                 overrides: Optional[Mapping[str, float]] = None) -> ConstantsTable:
     if table not in ("jax", "phyex"):
         raise ValueError("table must be 'jax' or 'phyex'")
     ext = externals_from(phyex, program)
+    hail = _hail_constants(ext)
     values: Dict[str, float] = {}
     for name in CONSTANT_NAMES:
         if name in ext:
             values[name] = float(ext[name])
         elif name in _DEFAULTS:
             values[name] = _DEFAULTS[name]
+        elif name in hail:
+            values[name] = hail[name]
         else:
             raise KeyError(f"constant {name} missing from the externals table")
     rim1 = np.asarray(ext["GAMINC_RIM1"], dtype=np.float64)
@@ -172,6 +249,10 @@ def build_table(phyex: Any = None, table: str = "jax", program: str = "AROME",
     fill(luts.ker_saccrg, ext["ker_saccrg"], (NACCLBDAR, NACCLBDAS))
     fill(luts.ker_rdryg, ext["ker_rdryg"], (NDRYLBDAG, NDRYLBDAR))
     fill(luts.ker_sdryg, ext["ker_sdryg"], (NDRYLBDAG, NDRYLBDAS))
+    hk = _hail_kernels()
+    fill(luts.ker_sweth, hk["ker_sweth"], (NWETLBDAH, NWETLBDAS))
+    fill(luts.ker_gweth, hk["ker_gweth"], (NWETLBDAH, NWETLBDAG))
+    fill(luts.ker_rweth, hk["ker_rweth"], (NWETLBDAH, NWETLBDAR))
     return ConstantsTable(consts=consts, luts=luts, values=values, table=table)
 
 

@@ -100,7 +100,16 @@ extern "C" {
   X(FIDRYG) X(COLSG) X(COLEXSG) X(FSDRYG) X(LBSDRYG1) X(LBSDRYG2)             \
   X(LBSDRYG3) X(FRDRYG) X(LBRDRYG1) X(LBRDRYG2) X(LBRDRYG3) X(DRYINTP1R)      \
   X(DRYINTP2R) X(DRYINTP1S) X(DRYINTP2S) X(DRYINTP1G) X(DRYINTP2G)            \
-  X(NDRYLBDAR) X(NDRYLBDAS) X(NDRYLBDAG)
+  X(NDRYLBDAR) X(NDRYLBDAS) X(NDRYLBDAG)                                      \
+  /* hail, NRR = 7 (mode_ini_rain_ice.F90 2.5, 5, 9; modd_param_icen) */      \
+  X(H_RTMIN) X(LBH) X(LBEXH) X(CXH) X(DH) X(BG) X(FSEDH) X(EXSEDH)            \
+  X(O0DEPH) X(O1DEPH) X(EX0DEPH) X(EX1DEPH) X(FWETH) X(COLIH) X(COLEXIH)      \
+  X(FSWETH) X(LBSWETH1) X(LBSWETH2) X(LBSWETH3) X(COLSH) X(COLEXSH)           \
+  X(FGWETH) X(LBGWETH1) X(LBGWETH2) X(LBGWETH3) X(COLGH) X(COLEXGH)           \
+  X(FRWETH) X(LBRWETH1) X(LBRWETH2) X(LBRWETH3) X(WETINTP1H) X(WETINTP2H)     \
+  X(WETINTP1S) X(WETINTP2S) X(WETINTP1G) X(WETINTP2G) X(WETINTP1R)            \
+  X(WETINTP2R) X(NWETLBDAH) X(NWETLBDAS) X(NWETLBDAG) X(NWETLBDAR)            \
+  X(LNULLWETH) X(LWETHPOST) X(LCONVHG)
 
 typedef struct Ice3gbConstants {
 #define ICE3GB_X_FIELD(name) double name;
@@ -117,6 +126,10 @@ typedef struct Ice3gbConstants {
 #define ICE3GB_NDRYLBDAG 40
 #define ICE3GB_NDRYLBDAS 80
 #define ICE3GB_NDRYLBDAR 40
+#define ICE3GB_NWETLBDAH 40   /* hail tables (NRR = 7 only)               */
+#define ICE3GB_NWETLBDAS 80
+#define ICE3GB_NWETLBDAG 40
+#define ICE3GB_NWETLBDAR 40
 typedef struct Ice3gbLuts {
   double gaminc_rim1[ICE3GB_NGAMINC];
   double gaminc_rim2[ICE3GB_NGAMINC];
@@ -126,6 +139,11 @@ typedef struct Ice3gbLuts {
   double ker_saccrg[ICE3GB_NACCLBDAR * ICE3GB_NACCLBDAS]; /* (lbdar, lbdas) */
   double ker_rdryg[ICE3GB_NDRYLBDAG * ICE3GB_NDRYLBDAR];  /* (lbdag, lbdar) */
   double ker_sdryg[ICE3GB_NDRYLBDAG * ICE3GB_NDRYLBDAS];  /* (lbdag, lbdas) */
+  /* hail collection kernels XKER_SWETH / GWETH / RWETH
+     (micro/mode_read_xker_sweth.F90, _gweth, _rweth)                       */
+  double ker_sweth[ICE3GB_NWETLBDAH * ICE3GB_NWETLBDAS];  /* (lbdah, lbdas) */
+  double ker_gweth[ICE3GB_NWETLBDAH * ICE3GB_NWETLBDAG];  /* (lbdah, lbdag) */
+  double ker_rweth[ICE3GB_NWETLBDAH * ICE3GB_NWETLBDAR];  /* (lbdah, lbdar) */
 } Ice3gbLuts;
 
 /* ---- ice_adjust -------------------------------------------------------- */
@@ -195,6 +213,11 @@ typedef struct Ice3gbRainIceFields {
   double *evap3d, *rainfr;          /* out [nk][nij]                      */
   double *inprc, *inprr, *inpri, *inprs, *inprg, *indep; /* out [nij]     */
   double *fpr_c, *fpr_r, *fpr_i, *fpr_s, *fpr_g;  /* out, optional        */
+  /* hail (NRR = 7 only; ignored otherwise)                                 */
+  const double *rht;                /* hail mixing ratio at t             */
+  double *rhs;                      /* in-out hail source                 */
+  double *inprh;                    /* out [nij] hail precipitation rate  */
+  double *fpr_h;                    /* out, optional                      */
 } Ice3gbRainIceFields;
 
 /* Per-call overrides of RainIceJAX.__call__ keywords
@@ -255,7 +278,8 @@ int ice3gb_ice_adjust(void *handle, int nij, int nk, double dt,
  * scheme whatever the table's SEDIM. */
 int ice3gb_sedimentation(void *handle, int nij, int nk, double dt,
                          const Ice3gbSedimentationFields *f, void *stream);
-/* Replaces c_rain_ice (phyex_bridge.F90:242) / RainIceJAX.__call__.  The
+/* Replaces c_rain_ice (phyex_bridge.F90:242) / RainIceJAX.__call__.  NRR = 7
+ * adds hail (rht, rhs, inprh required; ICE4_FAST_RH and the hail species).  The
  * table's SEDIM picks the sedimentation: STAT (1) or SPLI (0, time-split,
  * micro/mode_ice4_sedimentation_split.F90, followed by
  * ICE4_CORRECT_NEGATIVITIES, micro/mode_ice4_sedimentation.F90:196-229;

@@ -463,12 +463,39 @@ static void sed_column(const C *c, int nij, int nk, double dt, long col, int for
  * (mode_ice4_sedimentation.F90:196-229, the factors rain_ice.F90:334-345
  * passes).  rt: mixing ratios at t; returns 0 if a species needed more
  * than max_iter sub-steps. */
+/* Hail in ICE4_SEDIMENTATION_STAT (species 7, OTHER_SPECIES with XFSEDH /
+ * XEXSEDH, mode_ice4_sedimentation_stat.F90:186-187, 208-222) for one column,
+ * on rh = rhs * dt (mode_ice4_sedimentation.F90:179). */
+static void sed_hail_column(const C *c, int nij, int nk, double dt, long col, const double *rho,
+                            const double *dzz, double *rhs, double *fpr, double *inpr)
+{
+  double fabove = 0.0;
+  for (int k = nk - 1; k >= 0; --k) {
+    const long p = (long)k * nij + col;
+    const double r_rho = rho[p], dz = dzz[p];
+    const double tsorhodz = dt / (r_rho * dz);
+    const double rt = rhs[p] * dt;
+    const double qp = fabove * tsorhodz;
+    double w1 = 0.0, w2 = 0.0;
+    if (rt > c->H_RTMIN) w1 = sed_other(c->FSEDH, c->EXSEDH, rt, r_rho, c->CEXVT);
+    if (qp > c->H_RTMIN) w2 = sed_other(c->FSEDH, c->EXSEDH, qp, r_rho, c->CEXVT);
+    double flux = dmin(r_rho * dz * rt * (1.0 / dt), w1 * r_rho * rt);
+    if (w2 != 0.0) flux += dmax(0.0, 1.0 - dz / (dt * w2)) * fabove;
+    rhs[p] = rhs[p] + tsorhodz * (fabove - flux) * (1.0 / dt);
+    if (fpr) fpr[p] = flux;
+    fabove = flux;
+  }
+  *inpr = fabove / c->RHOLW;
+}
+
 static int sed_split_column(const C *c, int nij, int nk, double dt, long col, const double *rho,
                             const double *dzz, const double *pabs, const double *tht, const double *exn,
-                            double sea, double town, int has_sea_town, const double *rt[5], const double *rvt,
-                            double *src[5], double *rvs, double *ths, double *fpr[5], double inpr[5], int max_iter)
+                            double sea, double town, int has_sea_town, const double *rt[6], const double *rvt,
+                            double *src[6], double *rvs, double *ths, double *fpr[6], double inpr[6], int max_iter,
+                            int nsp)
 {
-  const double rtmin[5] = {c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN};
+  /* nsp = 5, or 6 with hail (KRR = 7, species 7 of :340-347: XFSEDH, XEXSEDH) */
+  const double rtmin[6] = {c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN, c->H_RTMIN};
   const double gac_gc = c->GAC / c->GC, gac2_gc2 = c->GAC2 / c->GC2;
   double lbc, fsedc, conc, ray;                                   /* :120-165, rain_ice.F90:396-420 */
   if (has_sea_town) {
@@ -482,13 +509,13 @@ static int sed_split_column(const C *c, int nij, int nk, double dt, long col, co
     fsedc = c->FSEDC_1;
     conc = c->CONC_LAND;
   }
-  const double fsed[5] = {0.0, c->FSEDR, 0.0, c->FSEDS, c->FSEDG};
-  const double exsed[5] = {0.0, c->EXSEDR, 0.0, c->EXSEDS, c->EXSEDG};
-  const double thr[5] = {c->C_RTMIN, c->R_RTMIN, dmax(c->I_RTMIN, 1.0e-7), c->S_RTMIN, c->G_RTMIN};
+  const double fsed[6] = {0.0, c->FSEDR, 0.0, c->FSEDS, c->FSEDG, c->FSEDH};
+  const double exsed[6] = {0.0, c->EXSEDR, 0.0, c->EXSEDS, c->EXSEDG, c->EXSEDH};
+  const double thr[6] = {c->C_RTMIN, c->R_RTMIN, dmax(c->I_RTMIN, 1.0e-7), c->S_RTMIN, c->G_RTMIN, c->H_RTMIN};
   double *rx = (double *)malloc(sizeof(double) * 3 * (size_t)nk);
   double *ext = rx + nk, *w = rx + 2 * nk;
   int ok = 1;
-  for (int s = 0; s < 5; ++s) {
+  for (int s = 0; s < nsp; ++s) {
     if (s == 0 && c->LSEDIC == 0.0) {
       inpr[0] = 0.0;
       if (fpr[0]) for (int k = 0; k < nk; ++k) fpr[0][(long)k * nij + col] = 0.0;
@@ -542,8 +569,9 @@ static int sed_split_column(const C *c, int nij, int nk, double dt, long col, co
   free(rx);
   for (int k = 0; k < nk; ++k) {                                 /* ICE4_CORRECT_NEGATIVITIES */
     const long p = (long)k * nij + col;
-    const double zdev = c->CPD + c->CPV * rvt[p] + c->CL * (rt[0][p] + rt[1][p]) +
-                        c->CI * (rt[2][p] + rt[3][p] + rt[4][p]);
+    double zice = rt[2][p] + rt[3][p] + rt[4][p];
+    if (nsp == 6) zice += rt[5][p];
+    const double zdev = c->CPD + c->CPV * rvt[p] + c->CL * (rt[0][p] + rt[1][p]) + c->CI * zice;
     const double t = tht[p] * exn[p];
     const double ls = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
     const double lv = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
@@ -554,6 +582,8 @@ static int sed_split_column(const C *c, int nij, int nk, double dt, long col, co
     ww = ri - dmax(ri, 0.); rv += ww; th -= ww * ls; ri -= ww;
     ww = rs - dmax(rs, 0.); rv += ww; th -= ww * ls; rs -= ww;
     ww = rg - dmax(rg, 0.); rv += ww; th -= ww * ls; rg -= ww;
+    double rh = nsp == 6 ? src[5][p] : 0.0;
+    if (nsp == 6) { ww = rh - dmax(rh, 0.); rv += ww; th -= ww * ls; rh -= ww; }
     ww = dmin(1., dmax(c->V_RTMIN - rv, 0.) / dmax(rc + ri, 1.e-20));
     th -= ww * (rc * lv + ri * ls);
     rv += ww * (rc + ri);
@@ -562,7 +592,9 @@ static int sed_split_column(const C *c, int nij, int nk, double dt, long col, co
     ww = dmin(dmax(rr, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rr -= ww; th -= ww * lv;
     ww = dmin(dmax(rs, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rs -= ww; th -= ww * ls;
     ww = dmin(dmax(rg, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rg -= ww; th -= ww * ls;
+    if (nsp == 6) { ww = dmin(dmax(rh, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += ww; rh -= ww; th -= ww * ls; }
     rvs[p] = rv; src[0][p] = rc; src[1][p] = rr; src[2][p] = ri; src[3][p] = rs; src[4][p] = rg; ths[p] = th;
+    if (nsp == 6) src[5][p] = rh;
   }
   return ok;
 }
@@ -575,14 +607,16 @@ EXPORT int ice3o_sedimentation_split(const C *c, int nij, int nk, double dt, con
   int ok = 1;
 #pragma omp parallel for schedule(static) reduction(& : ok)
   for (long col = 0; col < nij; ++col) {
-    double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
-    double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
-    const double *rt[5] = {f->rct, f->rrt, f->rit, f->rst, f->rgt};
-    double inpr[5];
+    const int nsp = (int)c->NRR == 7 ? 6 : 5;
+    double *src[6] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs, f->rhs};
+    double *fpr[6] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g, f->fpr_h};
+    const double *rt[6] = {f->rct, f->rrt, f->rit, f->rst, f->rgt, f->rht};
+    double inpr[6];
     ok &= sed_split_column(c, nij, nk, dt, col, f->rhodref, f->dzz, f->pabs, f->tht, f->exn, has ? f->sea[col] : 0.0,
-                           has ? f->town[col] : 0.0, has, rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000);
+                           has ? f->town[col] : 0.0, has, rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000, nsp);
     f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
     f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+    if (nsp == 6) f->inprh[col] = inpr[5];
   }
   return ok;
 }
@@ -613,7 +647,8 @@ EXPORT int ice3o_sedimentation(const C *c, int nij, int nk, double dt, const Ice
 /* ICE4 processes (one grid point)                                       */
 /* ===================================================================== */
 
-enum { ITH = 0, IRV = 1, IRC = 2, IRR = 3, IRI = 4, IRS = 5, IRG = 6, NV = 7 };
+enum { ITH = 0, IRV = 1, IRC = 2, IRR = 3, IRI = 4, IRS = 5, IRG = 6, NV = 7, IRH = 7, NVH = 8 };
+/* NV: the KRR = 6 state (theta + 6 mixing ratios); NVH: with hail (KRR = 7). */
 
 /* Instantaneous/rate budget slots (Fortran IBU* indices, KRR=6 subset). */
 enum {
@@ -623,19 +658,41 @@ enum {
   B_RCRIMSS, B_RCRIMSG, B_RSRIMCG, B_RRACCSS, B_RRACCSG, B_RSACCRG, B_RSMLTG, B_RCMLTSR,
   B_RICFRRG, B_RRCFRIG, B_RICFRR, B_RCWETG, B_RIWETG, B_RRWETG, B_RSWETG,
   B_RCDRYG, B_RIDRYG, B_RRDRYG, B_RSDRYG, B_RGMLTR, B_RCBERI,
+  /* KRR = 7: graupel -> hail conversion and ICE4_FAST_RH */
+  B_RWETGH, B_RWETGH_MR, B_RCWETH, B_RIWETH, B_RSWETH, B_RGWETH, B_RRWETH,
+  B_RCDRYH, B_RIDRYH, B_RSDRYH, B_RRDRYH, B_RGDRYH, B_RDRYHG, B_RHMLTR,
   NBU
 };
 /* fast_rs persistent tendencies (mode_ice4_fast_rs.F90 IRCRIMS..IFREEZ2) */
 enum { RS_RCRIMS, RS_RCRIMSS, RS_RSRIMCG, RS_RRACCS, RS_RRACCSS, RS_RSACCRG, RS_FREEZ1, RS_FREEZ2, NRS };
 /* fast_rg persistent tendencies (mode_ice4_fast_rg.F90 IRCDRYG..IFREEZ2) */
 enum { RG_RCDRYG, RG_RIDRYG, RG_RIWETG, RG_RSDRYG, RG_RSWETG, RG_RRDRYG, RG_FREEZ1, RG_FREEZ2, NRG };
+/* fast_rh persistent tendencies (mode_ice4_fast_rh.F90 IRCWETH..IFREEZ2) */
+enum { RH_RCWETH, RH_RRWETH, RH_RIDRYH, RH_RIWETH, RH_RSDRYH, RH_RSWETH, RH_RGDRYH, RH_RGWETH, RH_FREEZ1,
+       RH_FREEZ2, NRH };
 
 typedef struct {
   double bu[NBU];
   double rs_tend[NRS];
   double rg_tend[NRG];
+  double rh_tend[NRH];
   double ssi, ka, dv, ai, cj;
+  int tie;    /* a wet/dry growth choice was decided by rounding residuals */
 } PointRates;
+
+/* The wet/dry growth choice compares max(0, .) of differences whose exact
+ * value is often zero (what the wet growth collects equals its initial
+ * estimate); when such a difference cancels two or more non-zero rates, its
+ * computed value is a rounding residual and which side wins depends on the
+ * last bits of the rates.  nz: the number of non-zero rates cancelled. */
+static inline int growth_tie(double a, double b, double scale, int nz)
+{
+  return nz >= 2 && fabs(a - b) <= 1e-13 * scale;
+}
+static inline int nonzero(double a, double b, double c, double d, double e)
+{
+  return (a != 0.) + (b != 0.) + (c != 0.) + (d != 0.) + (e != 0.);
+}
 
 static inline double esatw(const C *c, double t) { return exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)); }
 static inline double esati(const C *c, double t) { return exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)); }
@@ -826,8 +883,9 @@ typedef struct {
   int ldsoft, ldcompute;
   double rhodref, pres, exn, lvfact, lsfact, cf, sigma_rc;
   double t;          /* temperature after the instantaneous processes */
-  double v[NV];      /* state after the instantaneous processes       */
-  double lbdar, lbdar_rf, lbdas, lbdag;
+  double v[NVH];     /* state after the instantaneous processes       */
+  double lbdar, lbdar_rf, lbdas, lbdag, lbdah;
+  int hail;          /* KRR = 7                                       */
   double rainfr;     /* PRAINFR (packed, per point)                   */
   double hl[4], hi[4];
 } Tctx;
@@ -1032,7 +1090,7 @@ static void ice4_fast_rs(const Tctx *x, PointRates *pr)
 }
 
 /* ICE4_FAST_RG, micro/mode_ice4_fast_rg.F90 (KRR = 6, LOCND2 = LNEWCOEFF = .FALSE.). */
-static void ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
+static int ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
 {
   const C *c = x->c;
   const Ice3gbLuts *lut = x->lut;
@@ -1107,12 +1165,29 @@ static void ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
     const double wet = dmax(0., rwetg_init - rg[RG_RIWETG] - rg[RG_RSWETG]);
     const double dry = dmax(0., rdryg_init - rg[RG_RIDRYG] - rg[RG_RSDRYG]);
     ldwetg = wet <= dry;
+    {
+      const int nw = nonzero(rg[RG_RIWETG], rg[RG_RSWETG], 0., 0., 0.);
+      const int nd = nonzero(rg[RG_RCDRYG], rg[RG_RIDRYG], rg[RG_RSDRYG], rg[RG_RRDRYG], 0.);
+      if (growth_tie(wet, dry, fabs(rwetg_init) + fabs(rdryg_init), nw > nd ? nw : nd)) pr->tie = 1;
+    }
     if (c->LNULLWETG != 0.0) ldwetg = ldwetg && rdryg_init > 0.;
     else ldwetg = ldwetg && rwetg_init > 0.;
     if (c->LWETGPOST == 0.0) ldwetg = ldwetg && t < c->TT;
     lldryg = t < c->TT && rdryg_init > 1.e-20 && wet > dry;
   } else {
     rg[RG_FREEZ1] = rg[RG_FREEZ2] = 0.0;
+  }
+  /* :331-351 part of the wet growth converted into hail (KRR = 7); the
+   * graupel sources PRGSI / PRGSI_MR are formed in ICE4_TENDENCIES :510-513 */
+  if (x->hail) {
+    if (ldwetg) {
+      const double rgsi = b[B_RVDEPG] + b[B_RSMLTG] + b[B_RRACCSG] + b[B_RSACCRG] + b[B_RCRIMSG] + b[B_RSRIMCG];
+      const double rgsi_mr = b[B_RRHONG_MR] + b[B_RSRIMCG_MR];
+      b[B_RWETGH] = (dmax(0., rgsi + b[B_RICFRRG] + b[B_RRCFRIG]) + rwetg_init) * rdryg_init / (rwetg_init + rdryg_init);
+      b[B_RWETGH_MR] = dmax(0., rgsi_mr) * rdryg_init / (rwetg_init + rdryg_init);
+    } else {
+      b[B_RWETGH] = b[B_RWETGH_MR] = 0.0;
+    }
   }
   if (ldwetg) {
     b[B_RRWETG] = -(rg[RG_RIWETG] + rg[RG_RSWETG] + rg[RG_RCDRYG] - rwetg_init);
@@ -1140,6 +1215,130 @@ static void ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
       b[B_RGMLTR] = r;
     }
   } else b[B_RGMLTR] = 0.0;
+  return ldwetg;
+}
+
+/* ICE4_FAST_RH, micro/mode_ice4_fast_rh.F90 (LNEWCOEFF = .FALSE.): hail wet
+ * and dry growth by collection of cloud, ice, snow, graupel and rain (the
+ * snow/graupel/rain kernels tabulated, XKER_SWETH/GWETH/RWETH), the wet/dry
+ * choice, the hail -> graupel conversion (LCONVHG) and melting. */
+static void ice4_fast_rh(const Tctx *x, PointRates *pr, int ldwetg)
+{
+  const C *c = x->c;
+  const Ice3gbLuts *lut = x->lut;
+  const double t = x->t, rho = x->rhodref, lbdar = x->lbdar, lbdas = x->lbdas, lbdag = x->lbdag, lbdah = x->lbdah;
+  double *b = pr->bu, *rh = pr->rh_tend;
+  const int hh = x->v[IRH] > c->H_RTMIN && x->ldcompute;
+  /* :109-131 cloud droplets and pristine ice */
+  if (hh && x->v[IRC] > c->C_RTMIN) {
+    if (!x->ldsoft) rh[RH_RCWETH] = c->FWETH * x->v[IRC] * (pow(lbdah, c->CXH - c->DH - 2.0) * pow(rho, -c->CEXVT));
+  } else rh[RH_RCWETH] = 0.0;
+  if (hh && x->v[IRI] > c->I_RTMIN) {
+    if (!x->ldsoft) {
+      rh[RH_RIWETH] = c->FWETH * x->v[IRI] * (pow(lbdah, c->CXH - c->DH - 2.0) * pow(rho, -c->CEXVT));
+      rh[RH_RIDRYH] = rh[RH_RIWETH] * (c->COLIH * exp(c->COLEXIH * (t - c->TT)));
+    }
+  } else rh[RH_RIWETH] = rh[RH_RIDRYH] = 0.0;
+  /* :136-176 snow (XKER_SWETH) */
+  int gwet = hh && x->v[IRS] > c->S_RTMIN;
+  if (!gwet) rh[RH_RSWETH] = rh[RH_RSDRYH] = 0.0;
+  if (!x->ldsoft && gwet) {
+    int i1, i2;
+    const double f1 = lut_index(lbdah, (int)c->NWETLBDAH, c->WETINTP1H, c->WETINTP2H, &i1);
+    const double f2 = lut_index(lbdas, (int)c->NWETLBDAS, c->WETINTP1S, c->WETINTP2S, &i2);
+    const double zzw = lut2d(lut->ker_sweth, ICE3GB_NWETLBDAS, i1, f1, i2, f2);
+    rh[RH_RSWETH] = c->FSWETH * zzw * (pow(lbdas, c->CXS - c->BS)) * (pow(lbdah, c->CXH)) *
+                    (pow(rho, -c->CEXVT - 1.)) *
+                    (c->LBSWETH1 / sq(lbdah) + c->LBSWETH2 / (lbdah * lbdas) + c->LBSWETH3 / sq(lbdas));
+    rh[RH_RSDRYH] = rh[RH_RSWETH] * (c->COLSH * exp(c->COLEXSH * (t - c->TT)));
+  }
+  /* :181-213 graupel (XKER_GWETH); dry collection efficiency only where the
+   * graupel is not itself in wet growth */
+  gwet = hh && x->v[IRG] > c->G_RTMIN;
+  if (!gwet) rh[RH_RGWETH] = rh[RH_RGDRYH] = 0.0;
+  if (!x->ldsoft && gwet) {
+    int i1, i2;
+    const double f1 = lut_index(lbdah, (int)c->NWETLBDAH, c->WETINTP1H, c->WETINTP2H, &i1);
+    const double f2 = lut_index(lbdag, (int)c->NWETLBDAG, c->WETINTP1G, c->WETINTP2G, &i2);
+    const double zzw = lut2d(lut->ker_gweth, ICE3GB_NWETLBDAG, i1, f1, i2, f2);
+    rh[RH_RGWETH] = c->FGWETH * zzw * (pow(lbdag, c->CXG - c->BG)) * (pow(lbdah, c->CXH)) *
+                    (pow(rho, -c->CEXVT - 1.)) *
+                    (c->LBGWETH1 / sq(lbdah) + c->LBGWETH2 / (lbdah * lbdag) + c->LBGWETH3 / sq(lbdag));
+    rh[RH_RGDRYH] = rh[RH_RGWETH];
+    if (!ldwetg) rh[RH_RGDRYH] = rh[RH_RGDRYH] * (c->COLGH * exp(c->COLEXGH * (t - c->TT)));
+  }
+  /* :218-245 rain (XKER_RWETH) */
+  gwet = hh && x->v[IRR] > c->R_RTMIN;
+  if (!gwet) rh[RH_RRWETH] = 0.0;
+  if (!x->ldsoft && gwet) {
+    int i1, i2;
+    const double f1 = lut_index(lbdah, (int)c->NWETLBDAH, c->WETINTP1H, c->WETINTP2H, &i1);
+    const double f2 = lut_index(lbdar, (int)c->NWETLBDAR, c->WETINTP1R, c->WETINTP2R, &i2);
+    const double zzw = lut2d(lut->ker_rweth, ICE3GB_NWETLBDAR, i1, f1, i2, f2);
+    rh[RH_RRWETH] = c->FRWETH * zzw * (pow(lbdar, -4.0)) * (pow(lbdah, c->CXH)) * (pow(rho, -c->CEXVT - 1.)) *
+                    (c->LBRWETH1 / sq(lbdah) + c->LBRWETH2 / (lbdah * lbdar) + c->LBRWETH3 / sq(lbdar));
+  }
+  /* :250-290 freezing rate and growth mode */
+  const double rdryh_init = rh[RH_RCWETH] + rh[RH_RIDRYH] + rh[RH_RSDRYH] + rh[RH_RRWETH] + rh[RH_RGDRYH];
+  double rweth_init = 0.0;
+  int llweth = 0, lldryh = 0;
+  if (hh) {
+    if (!x->ldsoft) {
+      double f1 = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 1);
+      f1 = f1 * (c->O0DEPH * pow(lbdah, c->EX0DEPH) + c->O1DEPH * pr->cj * pow(lbdah, c->EX1DEPH)) /
+           (rho * (c->LMTT - c->CL * (c->TT - t)));
+      rh[RH_FREEZ1] = f1;
+      rh[RH_FREEZ2] = (rho * (c->LMTT + (c->CI - c->CL) * (c->TT - t))) / (rho * (c->LMTT - c->CL * (c->TT - t)));
+    }
+    const double isg = rh[RH_RIWETH] + rh[RH_RSWETH] + rh[RH_RGWETH];
+    rweth_init = dmax(isg, dmax(0., rh[RH_FREEZ1] + rh[RH_FREEZ2] * isg));
+    const double wet = dmax(0., rweth_init - rh[RH_RIWETH] - rh[RH_RSWETH] - rh[RH_RGWETH]);
+    const double dry = dmax(0., rdryh_init - rh[RH_RIDRYH] - rh[RH_RSDRYH] - rh[RH_RGDRYH]);
+    llweth = wet <= dry;
+    const double wet2 = dmax(0., rweth_init - rh[RH_RIWETH] - rh[RH_RSWETH]);
+    const double dry2 = dmax(0., rdryh_init - rh[RH_RIDRYH] - rh[RH_RSDRYH]);
+    const int nw = nonzero(rh[RH_RIWETH], rh[RH_RSWETH], rh[RH_RGWETH], 0., 0.);
+    const int nd = nonzero(rh[RH_RCWETH], rh[RH_RIDRYH], rh[RH_RSDRYH], rh[RH_RRWETH], rh[RH_RGDRYH]);
+    if (growth_tie(wet, dry, fabs(rweth_init) + fabs(rdryh_init), nw > nd ? nw : nd) ||
+        growth_tie(wet2, dry2, fabs(rweth_init) + fabs(rdryh_init), nw > nd ? nw : nd))
+      pr->tie = 1;
+    if (c->LNULLWETH != 0.0) llweth = llweth && rdryh_init > 0.;
+    else llweth = llweth && rweth_init > 0.;
+    if (c->LWETHPOST == 0.0) llweth = llweth && t < c->TT;
+    lldryh = t < c->TT && rdryh_init > 1.e-20 && wet2 > dry2;
+  } else {
+    rh[RH_FREEZ1] = rh[RH_FREEZ2] = 0.0;
+  }
+  const double rdryhg = (c->LCONVHG != 0.0 && lldryh) ? rdryh_init * rweth_init / (rdryh_init + rweth_init) : 0.0;
+  if (llweth) {
+    b[B_RCWETH] = rh[RH_RCWETH];
+    b[B_RIWETH] = rh[RH_RIWETH];
+    b[B_RSWETH] = rh[RH_RSWETH];
+    b[B_RGWETH] = rh[RH_RGWETH];
+    b[B_RRWETH] = (rweth_init - rh[RH_RIWETH] - rh[RH_RSWETH] - rh[RH_RGWETH] - rh[RH_RCWETH]);
+  } else {
+    b[B_RCWETH] = b[B_RIWETH] = b[B_RSWETH] = b[B_RGWETH] = b[B_RRWETH] = 0.0;
+  }
+  if (lldryh) {
+    b[B_RCDRYH] = rh[RH_RCWETH];
+    b[B_RIDRYH] = rh[RH_RIDRYH];
+    b[B_RSDRYH] = rh[RH_RSDRYH];
+    b[B_RRDRYH] = rh[RH_RRWETH];
+    b[B_RGDRYH] = rh[RH_RGDRYH];
+    b[B_RDRYHG] = rdryhg;
+  } else {
+    b[B_RCDRYH] = b[B_RIDRYH] = b[B_RSDRYH] = b[B_RRDRYH] = b[B_RGDRYH] = b[B_RDRYHG] = 0.0;
+  }
+  /* :335-355 melting */
+  if (hh && t > c->TT) {
+    if (!x->ldsoft) {
+      double r = heat_term(c, pr->ka, pr->dv, t, x->v[IRV], x->pres, 0);
+      r = dmax(0., (-r * (c->O0DEPH * pow(lbdah, c->EX0DEPH) + c->O1DEPH * pr->cj * pow(lbdah, c->EX1DEPH)) -
+                    (rh[RH_RCWETH] + rh[RH_RRWETH]) * (rho * c->CL * (c->TT - t))) /
+                       (rho * c->LMTT));
+      b[B_RHMLTR] = r;
+    }
+  } else b[B_RHMLTR] = 0.0;
 }
 
 /* ICE4_FAST_RI, micro/mode_ice4_fast_ri.F90. */
@@ -1178,6 +1377,8 @@ static void ice4_slopes(Tctx *x)
     x->lbdas = (x->v[IRS] > 0.) ? dmin(c->LBDAS_MAX, c->LBS * pow(rho * dmax(x->v[IRS], c->S_RTMIN), c->LBEXS)) : 0.0;
   }
   x->lbdag = (x->v[IRG] > 0.) ? c->LBG * pow(rho * dmax(x->v[IRG], c->G_RTMIN), c->LBEXG) : 0.0;
+  if (x->hail)                                                        /* :426-432 */
+    x->lbdah = (x->v[IRH] > 0.) ? c->LBH * pow(rho * dmax(x->v[IRH], c->H_RTMIN), c->LBEXH) : 0.0;
 }
 
 /* ICE4_TENDENCIES (mode_ice4_tendencies.F90:150-717) for one point.
@@ -1185,15 +1386,17 @@ static void ice4_slopes(Tctx *x)
  * Outputs A (rates) and B (instantaneous increments). */
 static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int ldcompute,
                             double exn, double rhodref, double lvfact, double lsfact, double pres,
-                            double cf, double sigma_rc, double *cit, double t, const double vart[NV],
+                            double cf, double sigma_rc, double *cit, double t, const double vart[NVH],
                             PointRates *pr, double *rainfr, double hl[4], double hi[4],
-                            double A[NV], double B[NV])
+                            double A[NVH], double B[NVH])
 {
   Tctx x;
   x.c = c; x.lut = lut; x.ldsoft = ldsoft; x.ldcompute = ldcompute;
   x.rhodref = rhodref; x.pres = pres; x.exn = exn; x.lvfact = lvfact; x.lsfact = lsfact;
   x.cf = cf; x.sigma_rc = sigma_rc; x.t = t; x.rainfr = *rainfr;
-  for (int v = 0; v < NV; ++v) { x.v[v] = vart[v]; A[v] = 0.0; B[v] = 0.0; }
+  x.hail = (int)c->NRR == 7;
+  x.lbdah = 0.0;
+  for (int v = 0; v < NVH; ++v) { x.v[v] = (v < NV || x.hail) ? vart[v] : 0.0; A[v] = 0.0; B[v] = 0.0; }
   for (int k = 0; k < 4; ++k) { x.hl[k] = hl[k]; x.hi[k] = hi[k]; }
   double *b = pr->bu;
   if (ldsoft) {
@@ -1239,7 +1442,8 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   const int llrfr = (int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2;
   if (llrfr) {                                                        /* :357-380 */
     x.rainfr = dmax(x.rainfr, zrainfr);
-    const int mask = x.v[IRR] > c->R_RTMIN || x.v[IRS] > c->S_RTMIN || x.v[IRG] > c->G_RTMIN;
+    int mask = x.v[IRR] > c->R_RTMIN || x.v[IRS] > c->S_RTMIN || x.v[IRG] > c->G_RTMIN;
+    if (x.hail) mask = mask || x.v[IRH] > c->H_RTMIN;
     if (mask && x.rainfr == 0.) x.rainfr = 1.;
   } else {
     x.rainfr = 1.;
@@ -1248,7 +1452,8 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   ice4_slow(&x, pr);
   ice4_warm(&x, pr);
   ice4_fast_rs(&x, pr);
-  ice4_fast_rg(&x, pr, *cit);
+  const int ldwetg = ice4_fast_rg(&x, pr, *cit);
+  if (x.hail) ice4_fast_rh(&x, pr, ldwetg);                          /* :535-545 */
   ice4_fast_ri(&x, pr, *cit);
   /* :606-717 aggregation (KRR = 6, LOCND2 = .FALSE.) */
   const double lsv = lsfact - lvfact;
@@ -1312,6 +1517,29 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   A[IRG] += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
   A[IRG] += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
   A[IRG] -= b[B_RGMLTR];
+  if (x.hail) {                                                       /* KRR = 7 rows */
+    A[ITH] += (b[B_RRWETH] + b[B_RCWETH]) * lsv;                      /* :620-622 */
+    A[ITH] += (b[B_RCDRYH] + b[B_RRDRYH]) * lsv;
+    A[ITH] -= b[B_RHMLTR] * lsv;
+    A[IRC] -= b[B_RCWETH];                                            /* :641-642 */
+    A[IRC] -= b[B_RCDRYH];
+    A[IRR] -= b[B_RRWETH];                                            /* :657-659 */
+    A[IRR] -= b[B_RRDRYH];
+    A[IRR] += b[B_RHMLTR];
+    A[IRI] -= b[B_RIWETH];                                            /* :669-670 */
+    A[IRI] -= b[B_RIDRYH];
+    A[IRS] -= b[B_RSWETH];                                            /* :688-689 */
+    A[IRS] -= b[B_RSDRYH];
+    A[IRG] -= b[B_RWETGH];                                            /* :699-700 */
+    B[IRG] -= b[B_RWETGH_MR];
+    A[IRG] -= b[B_RGWETH];                                            /* :704-705 */
+    A[IRG] = A[IRG] - b[B_RGDRYH] + b[B_RDRYHG];
+    A[IRH] += b[B_RWETGH];                                            /* :709-715 */
+    B[IRH] += b[B_RWETGH_MR];
+    A[IRH] = A[IRH] + b[B_RCWETH] + b[B_RIWETH] + b[B_RSWETH] + b[B_RGWETH] + b[B_RRWETH];
+    A[IRH] = A[IRH] + b[B_RCDRYH] + b[B_RIDRYH] + b[B_RSDRYH] + b[B_RRDRYH] + b[B_RGDRYH] - b[B_RDRYHG];
+    A[IRH] -= b[B_RHMLTR];
+  }
   *rainfr = x.rainfr;
   for (int k = 0; k < 4; ++k) { hl[k] = x.hl[k]; hi[k] = x.hi[k]; }
 }
@@ -1325,10 +1553,11 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
  * Idle passes move a finished point by at most MNH_TINY seconds of its
  * external tendency; that sub-1e-15 relative drift is not reproduced. */
 typedef struct {
-  double vart[NV];
-  double extpk[NV];
+  double vart[NVH];
+  double extpk[NVH];
   double cit, rainfr, rrevav;
   int outer, inner, capped;
+  int tie;    /* some pass took a growth-mode decision on rounding residuals */
 } StepOut;
 
 static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
@@ -1336,13 +1565,17 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
                                 double hlc_hcf, double hlc_hrc, double hli_hcf, double hli_hri,
                                 StepOut *s)
 {
-  const double rsmin[NV] = {0.0, c->V_RTMIN, c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN};
+  const double rsmin[NVH] = {0.0, c->V_RTMIN, c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN,
+                             c->H_RTMIN};
+  const int hail = (int)c->NRR == 7;
+  const int nv = hail ? NVH : NV;                                     /* 0:KRR */
   const double inv_dt = 1.0 / dt;
   PointRates pr;
   memset(&pr, 0, sizeof(pr));
   double hl[4] = {hlc_hcf, 0.0, hlc_hrc, 0.0}, hi[4] = {hli_hcf, 0.0, hli_hri, 0.0};
+  if (!hail) s->vart[IRH] = s->extpk[IRH] = 0.0;
   /* :151-158 external tendencies */
-  for (int v = 0; v < NV; ++v) s->extpk[v] = s->extpk[v] - s->vart[v] * inv_dt;
+  for (int v = 0; v < nv; ++v) s->extpk[v] = s->extpk[v] - s->vart[v] * inv_dt;
   if ((int)c->SUBG_AUCV_RC == 2 || (int)c->SUBG_AUCV_RI == 2) {     /* :170-189 */
     hl[3] = s->vart[IRC] - hlc_hrc;
     hi[3] = s->vart[IRI] - hli_hri;
@@ -1351,7 +1584,7 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
   }
   double ztime = 0.0;
   int passes = 0;
-  s->outer = 0; s->inner = 0; s->capped = 0; s->rrevav = 0.0;
+  s->outer = 0; s->inner = 0; s->capped = 0; s->rrevav = 0.0; s->tie = 0;
   while (ztime < dt) {                                                /* :204 */
     s->outer++;
     int llcompute = 1, lsoft = 0, inner = 0;
@@ -1359,15 +1592,18 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
       if (passes >= max_passes) { s->capped = 1; goto done; }
       passes++;
       inner++;
-      const double zsum2 = s->vart[IRI] + s->vart[IRS] + s->vart[IRG];
+      double zsum2 = s->vart[IRI] + s->vart[IRS] + s->vart[IRG];       /* :276-281 */
+      if (hail) zsum2 += s->vart[IRH];
       const double zdev = (c->CPD + c->CPV * s->vart[IRV] + c->CL * (s->vart[IRC] + s->vart[IRR]) + c->CI * zsum2) * exn;
       const double zzt = s->vart[ITH] * exn;
       const double lsfact = (c->LSTT + (c->CPV - c->CI) * (zzt - c->TT)) / zdev;
       const double lvfact = (c->LVTT + (c->CPV - c->CL) * (zzt - c->TT)) / zdev;
-      double A[NV], B[NV];
+      double A[NVH], B[NVH];
       ice4_tendencies(c, lut, lsoft, 1, exn, rhodref, lvfact, lsfact, pres, cf, sigma_rc, &s->cit, zzt,
                       s->vart, &pr, &s->rainfr, hl, hi, A, B);
-      for (int v = 0; v < NV; ++v) A[v] += s->extpk[v];             /* :265-272 */
+      s->tie |= pr.tie;
+      pr.tie = 0;
+      for (int v = 0; v < nv; ++v) A[v] += s->extpk[v];             /* :265-272 */
       double maxtime = dt - ztime;                                    /* :275-282 */
       if (c->LFEEDBACKT != 0.0) {                                     /* :284-299 */
         const double zx = c->TT / exn;
@@ -1377,14 +1613,14 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
           if (thr > 0.) maxtime = dmin(maxtime, thr);
         }
       }
-      for (int v = 1; v < NV; ++v) {                                  /* :302-311 */
+      for (int v = 1; v < nv; ++v) {                                  /* :302-311 */
         if (A[v] < -1.e-20 && s->vart[v] > rsmin[v]) {
           maxtime = dmin(maxtime, -(B[v] + s->vart[v]) / A[v]);
           maxtime = dmax(maxtime, c->MNH_TINY);
         }
       }
       if (ztime + maxtime >= dt) llcompute = 0;                       /* :314-319 */
-      for (int v = 0; v < NV; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
+      for (int v = 0; v < nv; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
       if (s->vart[IRI] <= 0.) s->cit = 0.;                            /* :398-401 */
       ztime += maxtime;
       s->rrevav = pr.bu[B_RREVAV];
@@ -1393,7 +1629,7 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
     s->inner = inner;
   }
 done:
-  for (int v = 0; v < NV; ++v) s->vart[v] = s->vart[v] - s->extpk[v] * dt;  /* :503-511 */
+  for (int v = 0; v < nv; ++v) s->vart[v] = s->vart[v] - s->extpk[v] * dt;  /* :503-511 */
 }
 
 /* ===================================================================== */
@@ -1402,6 +1638,8 @@ done:
 
 EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
                               const double *rg);
+static void rainfr_vert_h(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
+                          const double *rg, const double *rh);
 
 /* ICE4_SEDIMENTATION of a rain_ice call (mode_ice4_sedimentation.F90:166-229):
  * STAT on the sources x dt, or SPLI on the mixing ratios at t followed by
@@ -1413,27 +1651,30 @@ static int rain_ice_sediment(const C *c, int nij, int nk, double dt, int sed_for
   const int spli = (int)c->SEDIM == 0;
 #pragma omp parallel for schedule(static) reduction(& : ok)
   for (long col = 0; col < nij; ++col) {
-    double *src[5] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs};
-    double *fpr[5] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g};
-    double inpr[5];
+    const int hail = (int)c->NRR == 7;
+    double *src[6] = {f->rcs, f->rrs, f->ris, f->rss, f->rgs, f->rhs};
+    double *fpr[6] = {f->fpr_c, f->fpr_r, f->fpr_i, f->fpr_s, f->fpr_g, f->fpr_h};
+    double inpr[6];
     const double sea = f->sea ? f->sea[col] : 0.0, town = f->town ? f->town[col] : 0.0;
     if (spli) {
-      const double *rt[5] = {f->rct, f->rrt, f->rit, f->rst, f->rgt};
+      const double *rt[6] = {f->rct, f->rrt, f->rit, f->rst, f->rgt, f->rht};
       ok &= sed_split_column(c, nij, nk, dt, col, f->rhodref, f->dzz, f->pabs, f->tht, f->exn, sea, town, has_st,
-                             rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000);
+                             rt, f->rvt, src, f->rvs, f->ths, fpr, inpr, 10000, hail ? 6 : 5);
     } else {
       sed_column(c, nij, nk, dt, col, sed_fortran, f->rhodref, f->dzz, f->pabs, f->tht, sea, town, has_st, src,
                  fpr, inpr);
+      if (hail) sed_hail_column(c, nij, nk, dt, col, f->rhodref, f->dzz, f->rhs, f->fpr_h, &inpr[5]);
     }
     f->inprc[col] = inpr[0]; f->inprr[col] = inpr[1]; f->inpri[col] = inpr[2];
     f->inprs[col] = inpr[3]; f->inprg[col] = inpr[4];
+    if (hail) f->inprh[col] = inpr[5];
   }
   return ok;
 }
 
 static int rain_ice_supported(const C *c)
 {
-  if ((int)c->NRR != 6) return 0;
+  if ((int)c->NRR != 6 && (int)c->NRR != 7) return 0;
   if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0) return 0;
   if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1) return 0;                    /* SPLI, STAT */
   if ((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) return 0;  /* NONE, PRFR */
@@ -1441,12 +1682,29 @@ static int rain_ice_supported(const C *c)
   return 1;
 }
 
+EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
+                               const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
+                               uint32_t *status_bits, uint8_t *tie);
+
 EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
                           const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
                           uint32_t *status_bits)
 {
+  return ice3o_rain_ice_ties(c, lut, nij, nk, dt, opt, f, status_bits, NULL);
+}
+
+/* ice3o_rain_ice that also marks (tie[p] = 1, when tie is not NULL) the
+ * points whose sub-stepping took a graupel or hail growth-mode decision on
+ * rounding residuals: there the reference's own outcome depends on the last
+ * bits of the collection rates. */
+EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
+                               const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
+                               uint32_t *status_bits, uint8_t *tie)
+{
   if (!c || !lut || !f || nij <= 0 || nk <= 0) return ICE3GB_ERR_SHAPE;
   if (!rain_ice_supported(c)) return ICE3GB_ERR_UNSUPPORTED;
+  const int hail = (int)c->NRR == 7;
+  if (hail && (!f->rht || !f->rhs || !f->inprh || (opt && opt->sed_jax > 0))) return ICE3GB_ERR_UNSUPPORTED;
   const long n = (long)nij * nk;
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (c->LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (c->LDEPOSC != 0.0);
@@ -1479,7 +1737,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     for (long p = 0; p < n; ++p) {
       const double rc = f->rct[p], ri = f->rit[p], cf = f->cldfr[p];
       const int micro = rc > c->C_RTMIN || f->rrt[p] > c->R_RTMIN || ri > c->I_RTMIN || f->rst[p] > c->S_RTMIN ||
-                        f->rgt[p] > c->G_RTMIN;
+                        f->rgt[p] > c->G_RTMIN || (hail && f->rht[p] > c->H_RTMIN);
       double hl[4] = {f->hlc_hcf[p], 0.0, f->hlc_hrc[p], 0.0}, hi[4] = {f->hli_hcf[p], 0.0, f->hli_hri[p], 0.0};
       if (adju) {                                                     /* :564-581 */
         hl[3] = rc - hl[2];
@@ -1492,7 +1750,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       f->hlc_hcf[p] = hl[0]; f->hlc_hrc[p] = hl[2]; f->hli_hcf[p] = hi[0]; f->hli_hri[p] = hi[2];
       f->rainfr[p] = rf;
     }
-    ice3o_rainfr_vert(c, nij, nk, f->rainfr, f->rrt, f->rst, f->rgt);
+    rainfr_vert_h(c, nij, nk, f->rainfr, f->rrt, f->rst, f->rgt, hail ? f->rht : NULL);
   }
 
   /* 1., 3., 4., 5. pointwise part */
@@ -1500,15 +1758,16 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
   for (long p = 0; p < n; ++p) {
     const double exn = f->exn[p], rho = f->rhodref[p], pres = f->pabs[p];
     const double th = f->tht[p], rv = f->rvt[p], rc = f->rct[p], rr = f->rrt[p];
-    const double ri = f->rit[p], rs = f->rst[p], rg = f->rgt[p];
+    const double ri = f->rit[p], rs = f->rst[p], rg = f->rgt[p], rh = hail ? f->rht[p] : 0.0;
     /* :334-345 lsfact/lvfact without exner */
-    const double zrice = ri + rs + rg;
+    const double zrice = hail ? ri + rs + rg + rh : ri + rs + rg;
     const double zdev = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * zrice;
     const double t = th * exn;
     lsf[p] = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
     lvf[p] = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
     /* :370-381 LLMICRO */
-    const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN || rg > c->G_RTMIN;
+    const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN ||
+                      rg > c->G_RTMIN || (hail && rh > c->H_RTMIN);
     f->evap3d[p] = 0.0;
     if (!llrfr) f->rainfr[p] = 1.0;  /* :603-605 */
     double cit = f->cit[p];
@@ -1522,6 +1781,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     zrvheni = dmin(f->rvs[p], zrvheni / dt);
     rvheni[p] = zrvheni;
     key[p] = -1;
+    if (tie) tie[p] = 0;
     if (micro) {
       /* ICE4_PACK + ICE4_STEPPING (mode_ice4_pack.F90:230-330) */
       StepOut s;
@@ -1529,6 +1789,8 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       s.vart[IRI] = ri; s.vart[IRS] = rs; s.vart[IRG] = rg;
       s.extpk[ITH] = f->ths[p]; s.extpk[IRV] = f->rvs[p]; s.extpk[IRC] = f->rcs[p]; s.extpk[IRR] = f->rrs[p];
       s.extpk[IRI] = f->ris[p]; s.extpk[IRS] = f->rss[p]; s.extpk[IRG] = f->rgs[p];
+      s.vart[IRH] = rh;
+      s.extpk[IRH] = hail ? f->rhs[p] : 0.0;
       s.cit = cit;
       s.rainfr = llrfr ? f->rainfr[p] : 1.0;
       const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
@@ -1539,6 +1801,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       if (c->LWARM != 0.0) f->evap3d[p] = s.rrevav;
       f->rainfr[p] = s.rainfr;
       capped_any |= s.capped;
+      if (tie) tie[p] = (uint8_t)s.tie;
       key[p] = ((int64_t)s.outer << 32) | (int64_t)s.inner;
       /* 8.1 total tendencies (rain_ice.F90:758-790, disabled in the vendored copy) */
       const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
@@ -1546,7 +1809,8 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       const double wv = (s.vart[IRV] - rv) * inv, wc = (s.vart[IRC] - rc) * inv;
       const double wr = (s.vart[IRR] - rr) * inv, wi = (s.vart[IRI] - ri) * inv;
       const double ws = (s.vart[IRS] - rs) * inv, wg = (s.vart[IRG] - rg) * inv;
-      const double wth = (wc + wr) * lvx + (wi + ws + wg) * lsx;
+      const double wh = (s.vart[IRH] - rh) * inv;
+      const double wth = (wc + wr) * lvx + (hail ? wi + ws + wg + wh : wi + ws + wg) * lsx;
       f->ths[p] += wth + zrvheni * lsx;
       f->rvs[p] += wv - zrvheni;
       f->rcs[p] += wc;
@@ -1554,6 +1818,7 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
       f->ris[p] += wi + zrvheni;
       f->rss[p] += ws;
       f->rgs[p] += wg;
+      if (hail) f->rhs[p] += wh;
     } else {
       const double lsx = lsf[p] / f->exnref[p];
       f->ths[p] += zrvheni * lsx;
@@ -1575,12 +1840,14 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
   for (long p = 0; p < n; ++p) {
     const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
     double rv = f->rvs[p], rc = f->rcs[p], rr = f->rrs[p], ri = f->ris[p], rs = f->rss[p], rg = f->rgs[p];
+    double rh = hail ? f->rhs[p] : 0.0;
     double th = f->ths[p], w;
     w = rc - dmax(rc, 0.); rv += w; th -= w * lvx; rc -= w;
     w = rr - dmax(rr, 0.); rv += w; th -= w * lvx; rr -= w;
     w = ri - dmax(ri, 0.); rv += w; th -= w * lsx; ri -= w;
     w = rs - dmax(rs, 0.); rv += w; th -= w * lsx; rs -= w;
     w = rg - dmax(rg, 0.); rv += w; th -= w * lsx; rg -= w;
+    if (hail) { w = rh - dmax(rh, 0.); rv += w; th -= w * lsx; rh -= w; }   /* :115-120 */
     w = dmin(1., dmax(c->V_RTMIN - rv, 0.) / dmax(rc + ri, 1.e-20));
     th -= w * (rc * lvx + ri * lsx);
     rv += w * (rc + ri);
@@ -1589,7 +1856,9 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
     w = dmin(dmax(rr, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rr -= w; th -= w * lvx;
     w = dmin(dmax(rs, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rs -= w; th -= w * lsx;
     w = dmin(dmax(rg, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rg -= w; th -= w * lsx;
+    if (hail) { w = dmin(dmax(rh, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rh -= w; th -= w * lsx; }  /* :165-171 */
     f->rvs[p] = rv; f->rcs[p] = rc; f->rrs[p] = rr; f->ris[p] = ri; f->rss[p] = rs; f->rgs[p] = rg;
+    if (hail) f->rhs[p] = rh;
     f->ths[p] = th;
   }
   /* 9. sedimentation after (rain_ice.F90:816-841) */
@@ -1699,6 +1968,26 @@ EXPORT int ice3o_process_rates(const C *c, const Ice3gbLuts *lut, long n, const 
 }
 
 /* ICE4_RAINFR_VERT (micro/mode_ice4_rainfr_vert.F90; stencils/rain_ice.py:272-320). */
+/* ICE4_RAINFR_VERT with the optional hail (rh NULL for KRR = 6). */
+static void rainfr_vert_h(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
+                          const double *rg, const double *rh)
+{
+  for (long col = 0; col < nij; ++col) {
+    prfr[(long)(nk - 1) * nij + col] = 0.0;
+    for (int k = nk - 2; k >= 0; --k) {
+      const long p = (long)k * nij + col;
+      int mask = rr[p] > c->R_RTMIN || rs[p] > c->S_RTMIN || rg[p] > c->G_RTMIN;
+      if (rh) mask = mask || rh[p] > c->H_RTMIN;
+      if (mask) {
+        prfr[p] = dmax(prfr[p], prfr[p + nij]);
+        if (prfr[p] == 0.) prfr[p] = 1.;
+      } else {
+        prfr[p] = 0.;
+      }
+    }
+  }
+}
+
 EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const double *rr, const double *rs,
                               const double *rg)
 {
@@ -1718,6 +2007,34 @@ EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const d
 }
 
 EXPORT int ice3o_budget_count(void) { return NBU; }
+
+/* ICE4_FAST_RH alone on n points (hard pass, LDCOMPUTE): in = [t, rhodref,
+ * pres, rv, rc, rr, ri, rs, rg, rh] per point (n x 10), ldwetg per point;
+ * out = the 10 persistent tendencies PRH_TEND then the 14 hail budget terms
+ * (RWETGH .. RHMLTR, the first two left 0) per point (n x 24).  Derived
+ * fields and slopes as ICE4_TENDENCIES forms them. */
+EXPORT void ice3o_fast_rh(const C *c, const Ice3gbLuts *lut, long n, const double *in, const uint8_t *ldwetg,
+                          double *out)
+{
+  for (long p = 0; p < n; ++p) {
+    const double *x = in + p * 10;
+    Tctx t;
+    memset(&t, 0, sizeof(t));
+    t.c = c; t.lut = lut; t.ldsoft = 0; t.ldcompute = 1; t.hail = 1;
+    t.t = x[0]; t.rhodref = x[1]; t.pres = x[2];
+    t.v[IRV] = x[3]; t.v[IRC] = x[4]; t.v[IRR] = x[5]; t.v[IRI] = x[6]; t.v[IRS] = x[7]; t.v[IRG] = x[8];
+    t.v[IRH] = x[9];
+    t.rainfr = 1.0;
+    PointRates pr;
+    memset(&pr, 0, sizeof(pr));
+    ice4_derived(c, t.t, t.rhodref, t.pres, t.v[IRV], &pr.ssi, &pr.ka, &pr.dv, &pr.ai, &pr.cj);
+    ice4_slopes(&t);
+    ice4_fast_rh(&t, &pr, ldwetg[p]);
+    double *o = out + p * 24;
+    for (int k = 0; k < NRH; ++k) o[k] = pr.rh_tend[k];
+    for (int k = 0; k < 14; ++k) o[NRH + k] = pr.bu[B_RWETGH + k];
+  }
+}
 
 /* ===================================================================== */
 /* Chained step: S1 = ice_adjust(x_t, S0); S2 = rain_ice(x_t, S1);        */
@@ -1785,6 +2102,7 @@ EXPORT int ice3o_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
 {
   StepOut s;
   for (int v = 0; v < NV; ++v) { s.vart[v] = in[3 + v]; s.extpk[v] = in[11 + v]; }
+  s.vart[IRH] = s.extpk[IRH] = 0.0;
   s.cit = in[10];
   s.rainfr = 1.0;
   const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;

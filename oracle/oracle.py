@@ -39,7 +39,10 @@ IA_RESULT = IA_OUT + IA_INOUT
 NBU_NAMES = ("rvheni_mr", "rrhong_mr", "rimltc_mr", "rsrimcg_mr", "rchoni", "rvdeps", "riaggs", "riauts",
              "rvdepg", "rcautr", "rcaccr", "rrevav", "rcrimss", "rcrimsg", "rsrimcg", "rraccss", "rraccsg",
              "rsaccrg", "rsmltg", "rcmltsr", "ricfrrg", "rrcfrig", "ricfrr", "rcwetg", "riwetg", "rrwetg",
-             "rswetg", "rcdryg", "ridryg", "rrdryg", "rsdryg", "rgmltr", "rcberi")
+             "rswetg", "rcdryg", "ridryg", "rrdryg", "rsdryg", "rgmltr", "rcberi",
+             # hail (KRR = 7)
+             "rwetgh", "rwetgh_mr", "rcweth", "riweth", "rsweth", "rgweth", "rrweth", "rcdryh", "ridryh",
+             "rsdryh", "rrdryh", "rgdryh", "rdryhg", "rhmltr")
 RS_NAMES = ("rcrims", "rcrimss", "rsrimcg", "rraccs", "rraccss", "rsaccrg", "freez1", "freez2")
 RG_NAMES = ("rcdryg", "ridryg", "riwetg", "rsdryg", "rswetg", "rrdryg", "freez1", "freez2")
 
@@ -161,8 +164,10 @@ RI_OUT2 = ("inprc", "inprr", "inpri", "inprs", "inprg", "indep")
 
 def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim_after: int = -1,
              ldeposc: int = -1, lfeedbackt: int = -1, max_passes: int = 0, sed_jax: int = 0,
-             with_fpr: bool = False):
-    """Oracle rain_ice on ABI-named fields; returns (outputs dict, status bits)."""
+             with_fpr: bool = False, with_ties: bool = False):
+    """Oracle rain_ice on ABI-named fields; returns (outputs dict, status bits).
+    with_ties: also out["tie"], 1 where the sub-stepping took a graupel or
+    hail growth-mode decision on rounding residuals (ice3o_rain_ice_ties)."""
     lib = load()
     keep = {k: _f64(st[k]) for k in RI_IN}
     nk, nij = keep["exn"].shape
@@ -176,8 +181,17 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
     out = {k: _f64(st[k]).copy() for k in RI_INOUT}
     out.update({k: np.empty((nk, nij)) for k in RI_OUT3})
     out.update({k: np.empty(nij) for k in RI_OUT2})
+    hail = table.values["NRR"] == 7.0
+    if hail:
+        # hail (KRR = 7): mixing ratio at t, in-out source, precipitation
+        keep["rht"] = _f64(st["rht"])
+        f.rht = _ptr(keep["rht"])
+        out["rhs"] = _f64(st["rhs"]).copy()
+        out["inprh"] = np.empty(nij)
     if with_fpr:
         out.update({k: np.empty((nk, nij)) for k in ("fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g")})
+        if hail:
+            out["fpr_h"] = np.empty((nk, nij))
     for k, v in out.items():
         setattr(f, k, _ptr(v))
     opt = RainIceOptions(lsedim_after, ldeposc, lfeedbackt, max_passes, sed_jax)
@@ -185,10 +199,15 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
     lib.ice3o_rain_ice.argtypes = [ctypes.POINTER(Ice3gbConstants), ctypes.POINTER(Ice3gbLuts), ctypes.c_int,
                                    ctypes.c_int, ctypes.c_double, ctypes.POINTER(RainIceOptions),
                                    ctypes.POINTER(RainIceFields), ctypes.POINTER(ctypes.c_uint32)]
-    rc = lib.ice3o_rain_ice(ctypes.byref(table.consts), ctypes.byref(table.luts), nij, nk, dt, ctypes.byref(opt),
-                            ctypes.byref(f), ctypes.byref(bits))
+    tie = np.zeros((nk, nij), dtype=np.uint8) if with_ties else None
+    lib.ice3o_rain_ice_ties.argtypes = lib.ice3o_rain_ice.argtypes + [ctypes.c_void_p]
+    rc = lib.ice3o_rain_ice_ties(ctypes.byref(table.consts), ctypes.byref(table.luts), nij, nk, dt,
+                                 ctypes.byref(opt), ctypes.byref(f), ctypes.byref(bits),
+                                 None if tie is None else tie.ctypes.data_as(ctypes.c_void_p))
     if rc != 0:
         raise RuntimeError(f"oracle rain_ice returned {rc}")
+    if with_ties:
+        out["tie"] = tie
     return out, bits.value
 
 

@@ -41,7 +41,7 @@ struct Handle {
   uint32_t magic;
   Ice3gbConstants c;
   double *d_luts;
-  double *d_tiwmx;   // OCND2 saturation tables: ESTABW then ESTABI
+  double *d_tiwmx;   // OCND2 TIWMX tables (six, see ice3gb_device.cuh)
   unsigned int *d_status;
   int device, num_sms;
   bool rain_ice_ok;
@@ -201,6 +201,11 @@ int validate_rain_ice(Handle *h, const Ice3gbRainIceFields *f)
   if ((int)h->c.NRR == 7) {  // hail
     REQUIRE(f->rht); REQUIRE(f->rhs); REQUIRE(f->inprh);
   }
+  if (h->c.OCND2 != 0.0) {   // the ice_adjust OCND2 outputs of the same state
+    if ((int)h->c.NRR != 6 || (int)h->c.SUBG_RC_RR_ACCR != 0 || (int)h->c.SUBG_RR_EVAP != 0)
+      return fail(h, ICE3GB_ERR_UNSUPPORTED, "rain_ice OCND2: NRR = 6 with SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE");
+    REQUIRE(f->ssio); REQUIRE(f->ssiu); REQUIRE(f->ifr); REQUIRE(f->icldfr);
+  }
   return ICE3GB_OK;
 }
 
@@ -245,6 +250,7 @@ int check_surrogate(Handle *h, const SurCall &sur, long n)
   if ((int)h->c.SUBG_RC_RR_ACCR != 0 || (int)h->c.SUBG_RR_EVAP != 0)
     return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained with SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE only");
   if ((int)h->c.NRR != 6) return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained for NRR = 6 (no hail)");
+  if (h->c.OCND2 != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained without OCND2");
   if (n > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "surrogate: at most 2^31 - 1 points per call");
   return ICE3GB_OK;
 }
@@ -374,6 +380,26 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   a.scr.keys = rs.keys;
   a.order = rs.order;
   a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
+  a.tw = nullptr;
+  a.ocs = nullptr;
+  const bool ocnd2 = c.OCND2 != 0.0;
+  if (ocnd2) {
+    // level heights and droplet concentrations of the OCND2 processes (2 n doubles)
+    if (!rs.may_alloc)
+      return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 needs scratch memory: not available in this entry point");
+    if ((e = cudaMallocAsync(&a.ocs, sizeof(double) * 2 * (size_t)nij * nk, s)) != cudaSuccess)
+      return cuda_fail(h, e, "cudaMallocAsync");
+    a.tw = h->d_tiwmx;
+    if ((e = launch_rain_ice_ocnd2_columns(c, a, s)) != cudaSuccess) {
+      cudaFreeAsync(a.ocs, s);
+      return cuda_fail(h, e, "rain_ice OCND2 columns");
+    }
+  }
+  struct OcsFree {   // the OCND2 scratch goes back to the pool on every return below
+    double *p;
+    cudaStream_t s;
+    ~OcsFree() { if (p) cudaFreeAsync(p, s); }
+  } ocs_free{a.ocs, s};
   if ((int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2) {
     ProfScope ps(h, K_PRFR, s);
     if ((e = launch_rain_ice_prfr(c, a, s)) != cudaSuccess) return cuda_fail(h, e, "rain_ice precipitation fraction");
@@ -787,8 +813,8 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   if (e == cudaSuccess) e = cudaMalloc(&h->d_status, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(unsigned int));
   if (e == cudaSuccess && c->OCND2 != 0.0) {
-    std::vector<double> tab(2 * (size_t)kTiwmxTableN);
-    tiwmx_tables(*c, tab.data(), tab.data() + kTiwmxTableN);
+    std::vector<double> tab((size_t)kTiwmxTables * kTiwmxTableN);
+    tiwmx_tables(*c, tab.data());
     e = cudaMalloc(&h->d_tiwmx, sizeof(double) * tab.size());
     if (e == cudaSuccess)
       e = cudaMemcpy(h->d_tiwmx, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice);
@@ -1220,10 +1246,10 @@ int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbR
   const bool adju = (int)h->c.SUBG_AUCV_RC == 2 || (int)h->c.SUBG_AUCV_RI == 2;
   const bool st = f->sea != nullptr;
   const bool fpr = f->fpr_c || f->fpr_r || f->fpr_i || f->fpr_s || f->fpr_g;
-  const bool hail = (int)h->c.NRR == 7;
-  // 14 in + cit + (4 hl/hi) + 7 sources + 2 out 3-D (+5 fpr) (+ hail: rht, rhs, fpr_h);
-  // 2-D: sea town + 6 out (+ inprh)
-  const size_t n3 = 14 + 1 + (adju ? 4 : 0) + 7 + 2 + (fpr ? 5 : 0) + (hail ? 3 : 0);
+  const bool hail = (int)h->c.NRR == 7, ocnd2 = h->c.OCND2 != 0.0;
+  // 14 in + cit + (4 hl/hi) + 7 sources + 2 out 3-D (+5 fpr) (+ hail: rht, rhs, fpr_h)
+  // (+ OCND2: ssio, ssiu, ifr, icldfr); 2-D: sea town + 6 out (+ inprh)
+  const size_t n3 = 14 + 1 + (adju ? 4 : 0) + 7 + 2 + (fpr ? 5 : 0) + (hail ? 3 : 0) + (ocnd2 ? 4 : 0);
   if ((rc = ensure_stage(h, n3 * b3p + 9 * b2p))) return rc;
   char *base = reinterpret_cast<char *>(h->d_stage);
   size_t off = 0;
@@ -1264,6 +1290,9 @@ int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt, const Ice3gbR
     d.rhs = up3(f->rhs);
     d.fpr_h = f->fpr_h ? take3() : nullptr;
     d.inprh = take2();
+  }
+  if (ocnd2) {
+    d.ssio = up3(f->ssio); d.ssiu = up3(f->ssiu); d.ifr = up3(f->ifr); d.icldfr = up3(f->icldfr);
   }
   if (e != cudaSuccess) return cuda_fail(h, e, "host->device copy");
   if ((rc = run_rain_ice(h, nij, nk, dt, opt, &d, s))) return rc;

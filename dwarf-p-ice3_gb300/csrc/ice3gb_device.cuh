@@ -94,6 +94,27 @@ ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffff
 ICE3_HD double powl_(double logx, double a) { return fm::fexp(a * logx); }
 ICE3_HD double fpow(double x, double a) { return fm::fexp(a * fm::flog(x)); }
 
+// TIWMX saturation tables of OCND2 (micro/modd_tiwmx.F90, filled by
+// micro/mode_ini_tiwmx.F90 from micro/mode_tiwmx_fun.F90) at T = j/100 K,
+// j = 13200..37316, stored one after the other: ESTABW, ESTABI (the ice
+// formula at and below 273.15 K, the water one above), A2TAB (AA2), BB3TAB
+// (BB3), AM3TAB (AM3, 0 above 273.15 K), REDINTAB (REDIN).
+constexpr int kTiwmxStart = 13200, kTiwmxStop = 37316, kTiwmxN = kTiwmxStop - kTiwmxStart + 1;
+enum { TW_ESW = 0, TW_ESI, TW_A2, TW_BB3, TW_AM3, TW_REDIN, TW_N };
+
+// TAB(NINT(100 T)) (micro/mode_tiwmx.F90), NINT rounding half away from
+// zero; the index is clamped to the table.
+ICE3_HD double tiwmx_at(const double *tab, double t)
+{
+  long j = (long)round(100.0 * t);
+  j = j < kTiwmxStart ? kTiwmxStart : (j > kTiwmxStop ? kTiwmxStop : j);
+#if defined(__CUDA_ARCH__)
+  return __ldg(tab + (j - kTiwmxStart));
+#else
+  return tab[j - kTiwmxStart];
+#endif
+}
+
 #if defined(__CUDACC__)
 // 128-bit streaming accessors (LDG.128 / STG.128).
 __device__ __forceinline__ double2 ld2(const double *p, long i) { return __ldg(reinterpret_cast<const double2 *>(p + i)); }

@@ -46,6 +46,8 @@ struct RainIceScratch {
 struct RainIceArgs {
   Ice3gbRainIceFields f;
   const double *luts;  // Ice3gbLuts on the device
+  const double *tw;    // OCND2: the TIWMX tables, else NULL
+  double *ocs;         // OCND2: [2][nk][nij] level heights then droplet concentrations, else NULL
   RainIceScratch scr;
   unsigned int *order; // [n] processing order of the grid points, or NULL (index order)
   int nij, nk;
@@ -86,7 +88,7 @@ struct IaKernelFields {
   Ice3gbIceAdjustFields f;
   const double *rrs, *rss, *rgs;
   double adv_dt;
-  const double *tiwmx;   // OCND2: ESTABW then ESTABI (2 x 24117 doubles)
+  const double *tiwmx;   // OCND2: the six TIWMX tables (6 x 24117 doubles)
 };
 
 // ice_adjust adjoint arguments; sigqsat_out receives the per-point sigqsat
@@ -165,10 +167,11 @@ cudaError_t launch_adam(float *w, const float *g, float *m1, float *m2, __nv_bfl
                         float b2, float eps, int step, cudaStream_t s);
 cudaError_t launch_to_bf16(const float *x, __nv_bfloat16 *y, long n, cudaStream_t s);
 
-// OCND2 saturation tables (micro/mode_ini_tiwmx.F90), filled on the host:
-// ESTABW and ESTABI at T = j/100 K, j = 13200..37316 (ice_adjust.cu).
-constexpr int kTiwmxTableN = 24117;
-void tiwmx_tables(const Ice3gbConstants &c, double *estw, double *esti);
+// OCND2 TIWMX tables (micro/mode_ini_tiwmx.F90), filled on the host: six
+// tables of 24,117 entries at T = j/100 K (ice_adjust.cu; the layout of
+// ice3gb_device.cuh).
+constexpr int kTiwmxTableN = 24117, kTiwmxTables = 6;
+void tiwmx_tables(const Ice3gbConstants &c, double *tab);
 
 cudaError_t launch_ice_adjust(const Ice3gbConstants &c, const IaKernelFields &kf, int nij, int nk, double dt,
                               bool vec2, int num_sms, cudaStream_t s);
@@ -181,6 +184,7 @@ size_t rain_ice_smem_bytes();
 
 cudaError_t launch_sedimentation_split(const Ice3gbConstants &c, const SplitArgs &a, cudaStream_t s);
 // Precipitation fraction of a rain_ice call with a PRFR option (before the point kernel).
+cudaError_t launch_rain_ice_ocnd2_columns(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_prfr(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_surrogate_sample(const Ice3gbConstants &c, const SurSampleArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_rain_ice_surrogate(const Ice3gbConstants &c, const SurRainIceArgs &a, int num_sms, cudaStream_t s);

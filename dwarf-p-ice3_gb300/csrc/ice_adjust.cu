@@ -156,16 +156,25 @@ __global__ void __launch_bounds__(256) ice_adjust_ocnd2_kernel(const __grid_cons
 
 }  // namespace
 
-static_assert(kTiwmxTableN == kTiwmxN, "TIWMX table size");
+static_assert(kTiwmxTableN == kTiwmxN && kTiwmxTables == TW_N, "TIWMX table size");
 
-void tiwmx_tables(const Cst &c, double *estw, double *esti)
+void tiwmx_tables(const Cst &c, double *tab)
 {
-  // mode_tiwmx_fun.F90 ESATW / ESATI; INI_TIWMX keeps the water value above 273.15 K
+  // mode_tiwmx_fun.F90 ESATW / ESATI / AA2 / BB3 / AM3 / REDIN as INI_TIWMX
+  // fills its tables (the water values above 273.15 K for ESTABI, AM3TAB = 0 there)
   for (int j = kTiwmxStart; j <= kTiwmxStop; ++j) {
     const double t = (double)j / 100.0;
+    const long i = j - kTiwmxStart;
     const double w = std::exp(c.ALPW - c.BETAW / t - c.GAMW * std::log(t));
-    estw[j - kTiwmxStart] = w;
-    esti[j - kTiwmxStart] = t > 273.15 ? w : std::exp(c.ALPI - c.BETAI / t - c.GAMI * std::log(t));
+    const double ei = t >= c.TT ? w : std::exp(c.ALPI - c.BETAI / t - c.GAMI * std::log(t));  // ESATI
+    tab[TW_ESW * kTiwmxN + i] = w;
+    tab[TW_ESI * kTiwmxN + i] = t > 273.15 ? w : std::exp(c.ALPI - c.BETAI / t - c.GAMI * std::log(t));
+    const double l = c.LSTT + (c.CPV - c.CI) * (t - c.TT);
+    tab[TW_A2 * kTiwmxN + i] = l * l / (2.38e-2 + 0.0071e-2 * (t - c.TT)) / (t * t * c.RV);
+    tab[TW_BB3 * kTiwmxN + i] = c.RV / (0.211e-4 * std::pow(t / c.TT, 1.94) * c.P00) * t / ei;
+    tab[TW_AM3 * kTiwmxN + i] = t > 273.15 ? 0.0 : 1000. * std::exp(12.96 * (w / ei - 1.) - 0.639);
+    const double z = std::fmax(0., std::fmin(1., (c.TT - t) / 20.));
+    tab[TW_REDIN * kTiwmxN + i] = 1. - (1. - z) / std::pow(z * z * z + (1. - z) * (1. - z) * (1. - z), .333);
   }
 }
 

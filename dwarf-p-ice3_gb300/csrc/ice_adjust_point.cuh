@@ -74,23 +74,8 @@ ICE3_HD double sigrc_cb(const Cst &c, double q1)
 }
 
 // ---- OCND2 (separate liquid and ice clouds) -----------------------------------
-// TIWMX saturation tables (micro/modd_tiwmx.F90, filled by
-// micro/mode_ini_tiwmx.F90): ESTABW(j) = ESATW(j/100 K), ESTABI(j) = the ice
-// formula at and below 273.15 K, the water one above, j = 13200..37316.
-constexpr int kTiwmxStart = 13200, kTiwmxStop = 37316, kTiwmxN = kTiwmxStop - kTiwmxStart + 1;
-
-// ESATW / ESATI (micro/mode_tiwmx.F90): TAB(NINT(100 T)), NINT rounding half
-// away from zero; the index is clamped to the table.
-ICE3_HD double tiwmx_at(const double *tab, double t)
-{
-  long j = (long)round(100.0 * t);
-  j = j < kTiwmxStart ? kTiwmxStart : (j > kTiwmxStop ? kTiwmxStop : j);
-#if defined(__CUDA_ARCH__)
-  return __ldg(tab + (j - kTiwmxStart));
-#else
-  return tab[j - kTiwmxStart];
-#endif
-}
+// The TIWMX tables and tiwmx_at() are in ice3gb_device.cuh (shared with the
+// rain_ice OCND2 processes).
 
 // Per-point inputs of the OCND2 branch and its extra outputs.
 struct Ocnd2In {

@@ -50,7 +50,8 @@ __device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int
 // SUBG: the subgrid warm-process options (SUBG_RC_RR_ACCR / SUBG_RR_EVAP
 // other than NONE); the NONE instantiation carries none of their code.
 // H: hail (NRR = 7), the hail kernels read from the global copy of the tables.
-template <bool SUBG, bool H = false>
+// O: OCND2 (NRR = 6, warm options NONE), with a.tw and the column fields a.ocs.
+template <bool SUBG, bool H = false, bool O = false>
 __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_kernel(const __grid_constant__ Cst c,
                                                                          const __grid_constant__ RainIceArgs a)
 {
@@ -75,7 +76,9 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
     if (slot < n) {
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       bool capped;
-      key = rain_ice_point<false, SUBG, H>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr, a.luts);
+      key = O ? rain_ice_point<false, false, false, true>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr,
+                                                          a.luts, a.tw, a.ocs, a.ocs + n)
+              : rain_ice_point<false, SUBG, H>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr, a.luts);
       any_capped |= capped;
       a.scr.keys[p] = key;
     }
@@ -86,6 +89,13 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
 
 // The precipitation fraction of a call with a PRFR option, one thread per
 // column (prfr_column); runs before the point kernel, which starts from it.
+// OCND2: level heights and droplet concentrations, one thread per column.
+__global__ void rain_ice_ocnd2_column_kernel(const __grid_constant__ Cst c, const __grid_constant__ RainIceArgs a)
+{
+  const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (col < a.nij) ocnd2_column(c, a.f, a.nij, a.nk, col, a.ocs, a.ocs + (long)a.nij * a.nk);
+}
+
 template <bool H>
 __global__ void rain_ice_prfr_kernel(const __grid_constant__ Cst c, const __grid_constant__ RainIceArgs a)
 {
@@ -174,8 +184,9 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
   const bool subg = (int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0;
   const bool hail = (int)c.NRR == 7;
   void (*kern)(const Cst, const RainIceArgs) =
-      hail ? (subg ? rain_ice_points_kernel<true, true> : rain_ice_points_kernel<false, true>)
-           : (subg ? rain_ice_points_kernel<true, false> : rain_ice_points_kernel<false, false>);
+      c.OCND2 != 0.0 ? rain_ice_points_kernel<false, false, true>
+      : hail ? (subg ? rain_ice_points_kernel<true, true> : rain_ice_points_kernel<false, true>)
+             : (subg ? rain_ice_points_kernel<true, false> : rain_ice_points_kernel<false, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rain_ice_smem_bytes());
   if (e != cudaSuccess) return e;
   const long n = (long)a.nij * a.nk;
@@ -184,6 +195,12 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
   if (blocks > chunks) blocks = chunks;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, RI_THREADS, rain_ice_smem_bytes(), s>>>(c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rain_ice_ocnd2_columns(const Cst &c, const RainIceArgs &a, cudaStream_t s)
+{
+  rain_ice_ocnd2_column_kernel<<<(unsigned)((a.nij + 127) / 128), 128, 0, s>>>(c, a);
   return cudaGetLastError();
 }
 

@@ -60,6 +60,18 @@ struct HailRates {
   double b[NBH];
   double t[NRH];
 };
+// OCND2 (separate liquid and ice clouds): the per-point inputs (the TIWMX
+// tables, the ice_adjust OCND2 outputs of the state, the level height and the
+// cloud droplet concentration of rain_ice.F90:386-435) and the hard-pass
+// quantities of ICE4_TENDENCIES it adds (tabulated es_i, collision factors,
+// ICE4_FAST_RI_RS's RVDEPI / RILARS).
+struct OcndPt {
+  const double *tw;
+  double ssio, ssiu, ifr, icldfr, zzz, conc;
+};
+struct OcndRates {
+  double esi, colf, acrf, rvdepi, rilars;
+};
 
 // Constants derived from the table once per block (kept in shared memory).
 struct Derived {
@@ -110,6 +122,53 @@ struct PointFix {
 ICE3_HD double esat_from(double alp, double beta, double gam, double it, double lt)
 {
   return fm::fexp(alp - beta * it - gam * lt);
+}
+
+// The OCND2 branch of ICE4_NUCLEATION (ice4_nucleation.func.h:127-136): the
+// concentration from REDIN, AM3, the height and the ice cloud fraction; no
+// vapour is taken (RVHENI = 0).
+ICE3_HD void nucleation_ocnd2(const Cst &c, const OcndPt &o, double t, double rvt, double &cit, double &rvheni)
+{
+  rvheni = 0.0;
+  if (!(ltp(t, c.TT) && gtp(rvt, c.V_RTMIN))) return;
+  const double redin = tiwmx_at(o.tw + TW_REDIN * kTiwmxN, t);
+  const double am3 = tiwmx_at(o.tw + TW_AM3 * kTiwmxN, dmax(c.FRMIN27, t));
+  const double h = (20000. - dmin(20000., o.zzz)) * (1.0 / 20000.);
+  const double zzw = dmin(redin * dmax(0.1, (h * h) * (h * h)) * am3 * (0.0001 + 0.9999 * o.icldfr), 50.e3);
+  cit = dmax(zzw + cit, cit);
+}
+
+// The level heights and cloud droplet concentrations of one column for OCND2
+// (rain_ice.F90:386-435): the height is the sum of dzz from the last level
+// down to the level minus half its thickness (with k = 0 at the surface the
+// last level is the top), the concentration the land / sea / town blend or
+// the pressure form of XFRMIN(26).
+ICE3_HD void ocnd2_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, int nk, long col, double *zzz,
+                          double *conc)
+{
+  double zsum = 0.0;
+  for (int k = nk - 1; k >= 0; --k) {
+    const long p = (long)k * nij + col;
+    const double dz = f.dzz[p];
+    zsum = zsum + dz;
+    zzz[p] = zsum - dz * 0.5;
+  }
+  const bool st = f.sea && f.town;
+  const double sea = st ? f.sea[col] : 0.0, town = st ? f.town[col] : 0.0;
+  const double top = zzz[(long)(nk - 1) * nij + col];
+  for (int k = 0; k < nk; ++k) {
+    const long p = (long)k * nij + col;
+    double cc = c.CONC_LAND;
+    if (st && c.FRMIN26 < 0.001) cc = (1. - town) * (sea * c.CONC_SEA + (1. - sea) * c.CONC_LAND) + town * c.CONC_URBAN;
+    if (c.FRMIN26 > 0.001) {
+      cc = c.FRMIN26 * f.pabs[p] / c.P00;
+      if (c.FRMIN22 > 0.001 && st) {
+        const double tmp = dmax(0., dmin(1., (zzz[p] - top) / dmax(0.01, c.FRMIN29 - top)));
+        cc = cc * (c.FRMIN22 * (sea * c.FRMIN30 + (1. - sea)) * (1. - tmp) + tmp);
+      }
+    }
+    conc[p] = cc;
+  }
 }
 
 // x < 0 (not -0), on the bit pattern.
@@ -354,23 +413,52 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
 // choice) are left to aggregate(), which every pass runs.
 // H (NRR = 7): also the rate parts of ICE4_FAST_RH into *hr, from the hail
 // kernels at hlut (global memory); v then holds NVH values.
-template <bool SUR = false, bool SUBG = false, bool H = false>
+// O (OCND2): the tabulated derived fields, collision factors, tuning factors
+// and ICE4_FAST_RI_RS of the LOCND2 branches, with the point inputs *op; the
+// hard-pass OCND2 quantities go to *orr.
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
 ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                         double t, const double *v, double cit, const double hl[4], const double hi[4],
                         double criauti, Rates &R, bool learned_slow = false, double rainfr = 1.0,
-                        HailRates *hr = nullptr, const double *__restrict__ hlut = nullptr)
+                        HailRates *hr = nullptr, const double *__restrict__ hlut = nullptr,
+                        const OcndPt *op = nullptr, OcndRates *orr = nullptr)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
-  // derived fields (mode_ice4_tendencies.F90:303-320)
+  // derived fields (mode_ice4_tendencies.F90:303-320; OCND2: es_i and ai
+  // from the TIWMX tables, :304-309)
   const double lt = fm::flog(t), it = fm::frcp(t);
-  const double esi = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+  // es_i of the freezing heat terms stays the formula; OCND2 takes the table
+  // for ssi, ai and ICE4_FAST_RI_RS only
+  const double esi_f = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+  const double esi = O ? tiwmx_at(op->tw + TW_ESI * kTiwmxN, t) : esi_f;
   const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   R.ssi = fm::fdiv(v[IRV] * (pf.pres - esi), c.EPSILO * esi) - 1.0;
   const double ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
   const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
   const double ika = fm::frcp(ka), idv = fm::frcp(dv);
-  const double ai = sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esi);
+  const double ai = O ? tiwmx_at(op->tw + TW_A2 * kTiwmxN, t) + tiwmx_at(op->tw + TW_BB3 * kTiwmxN, t) * pf.pres
+                      : sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * (ika * d.irv * it * it) +
+                            (c.RV * t) * fm::fdiv(idv, esi);
+  double colf = 1.0, acrf = 1.0;
+  if (O) {
+    // collision factors from the mean droplet radius (:322-346, LLCOL)
+    orr->esi = esi;
+    colf = acrf = 0.00001;
+    if (gtp(v[IRC], 1.0e-10)) {
+      const double rcw = 0.1 * fm::fexp(0.333 * fm::flog(fm::fdiv(0.75 * v[IRC] * rho, c.PI * (op->conc * 0.000001))));
+      double vt = ltp(rcw, 0.0065) ? 1.19e6 * sq(rcw) : 8000. * rcw;
+      vt = dmin(10., vt);
+      const double st = dmax(0.01, fm::fdiv(2. * (100. - vt) * vt, c.GRAVITY0 * 10.));
+      if (gtp(st, 0.1)) colf = dmax(0.01, dmin(1., 0.939 * fm::fexp(2.657 * fm::flog(st))));
+      if (gtp(v[IRR], 1.0e-10) && gtp(rcw, 1.0e-5)) {
+        const double r20 = fm::fexp(rcw * 2000.);
+        acrf = fm::fdiv(r20 - 1., r20 + 1.);
+      }
+    }
+    orr->colf = colf;
+    orr->acrf = acrf;
+  }
   const double cj = fm::fdiv(c.SCFAC * fm::fexp(0.3 * pf.lrho), sqrt(1.718e-5 + 4.9e-8 * (t - c.TT)));
   const double ssi_rai = fm::fdiv(R.ssi, rho * ai);
   Slopes s;
@@ -400,7 +488,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   double heat_i = 0.0, heat_w = 0.0;
   if (has_s || has_g || has_h) {
     const double ev = fm::fdiv(v[IRV] * pf.pres, c.EPSILO + v[IRV]);
-    const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi) : ev;
+    const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi_f) : ev;
     const double ew = c.LEVLIMIT != 0.0 ? dmin(ev, esw) : ev;
     const double kt = ka * (c.TT - t);
     const double dl = dv * (c.LVTT + (c.CPV - c.CL) * (t - c.TT));
@@ -415,14 +503,14 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c)
                       ? dmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3))
                       : 0.0;
-    b[B_RVDEPS] = (has_v && has_s) ? ssi_rai * vent_s : 0.0;
+    b[B_RVDEPS] = (has_v && has_s) ? (O ? ssi_rai * vent_s * c.FRMIN40 : ssi_rai * vent_s) : 0.0;
     b[B_RIAGGS] = (has_i && has_s)
                       ? c.FIAGGS * fm::fexp(c.COLEXIS * (t - c.TT) + c.EXIAGGS * s.llbdas) * v[IRI] * pf.rho_mcexvt
                       : 0.0;
     b[B_RIAUTS] = gtp(hi[2], c.I_RTMIN)
                       ? c.TIMAUTI * fm::fexp(c.TEXAUTI * (t - c.TT)) * pmax0(hi[2] - criauti * hi[0])
                       : 0.0;
-    b[B_RVDEPG] = (has_v && has_g) ? ssi_rai * vent_g : 0.0;
+    b[B_RVDEPG] = (has_v && has_g) ? (O ? ssi_rai * vent_g * c.FRMIN39 : ssi_rai * vent_g) : 0.0;
   }
 
   // ---- ICE4_WARM (mode_ice4_warm.F90) ----
@@ -432,7 +520,9 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   } else if (c.LWARM != 0.0) {
     // SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
-    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt : 0.0;
+    b[B_RCACCR] = (has_c && has_r) ? (O ? c.FCACCR * v[IRC] * acrf * e_caccr * pf.rho_mcexvt
+                                        : c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt)
+                                   : 0.0;
     if (has_r && !has_c) {
       const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
       const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esw);
@@ -457,8 +547,10 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double zw2 = lut1d(lut + O_RIM2, i, fr);
     const double zw3 = lut1d(lut + O_RIM4, i, fr);
     const double e_crimss = fm::fexp(c.EXCRIMSS * s.llbdas);
-    rs[RS_RCRIMSS] = c.CRIMSS * zw1 * v[IRC] * e_crimss * pf.rho_mcexvt;
-    rs[RS_RCRIMS] = c.CRIMSG * v[IRC] * (d.crims_same ? e_crimss : fm::fexp(c.EXCRIMSG * s.llbdas)) * pf.rho_mcexvt;
+    const double rcc = O ? v[IRC] * colf : v[IRC];                 // PCOLF
+    rs[RS_RCRIMSS] = O ? c.CRIMSS * zw1 * v[IRC] * colf * e_crimss * pf.rho_mcexvt
+                       : c.CRIMSS * zw1 * v[IRC] * e_crimss * pf.rho_mcexvt;
+    rs[RS_RCRIMS] = c.CRIMSG * rcc * (d.crims_same ? e_crimss : fm::fexp(c.EXCRIMSG * s.llbdas)) * pf.rho_mcexvt;
     if ((int)c.SNOW_RIMING == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
       const double e_srimcg = fm::fexp(c.EXSRIMCG * s.llbdas);
@@ -478,10 +570,12 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double zw3 = lut2d(lut + O_SACCRG, ICE3GB_NACCLBDAS, i2, f2, i1, f1);
     const double zzw = c.FRACCSS * (d.cxs_one ? s.lbdas : fm::fexp(c.CXS * s.llbdas)) * pf.rho_mcexvt1 *
                        (c.LBRACCS1 * ils * ils + c.LBRACCS2 * ils * ilr + c.LBRACCS3 * ilr * ilr) * sq(sq(ilr));
-    rs[RS_RRACCSS] = zw1 * zzw;
+    rs[RS_RRACCSS] = O ? zw1 * zzw * c.FRMIN7 : zw1 * zzw;        // OCND2: XFRMIN(7), fast_rs :327
     rs[RS_RRACCS] = zw2 * zzw;
-    rs[RS_RSACCRG] = c.FSACCRG * zw3 * e_cxsbs * pf.rho_mcexvt1 *
-                     (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr;
+    rs[RS_RSACCRG] = (!O || gtp(v[IRS], c.FRMIN1))                 // OCND2: rs > XFRMIN(1), :347
+                         ? c.FSACCRG * zw3 * e_cxsbs * pf.rho_mcexvt1 *
+                               (c.LBSACCR1 * ilr * ilr + c.LBSACCR2 * ilr * ils + c.LBSACCR3 * ils * ils) * ilr
+                         : 0.0;
   } else {
     rs[RS_RRACCS] = rs[RS_RRACCSS] = rs[RS_RSACCRG] = 0.0;
   }
@@ -514,7 +608,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     rg[RG_RIDRYG] = c.FIDRYG * e * v[IRI] * base_g;
     rg[RG_RIWETG] = fm::fdiv(rg[RG_RIDRYG], c.COLIG * e);
   } else rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
-  if (has_s && has_g) {
+  if (has_s && has_g && !O) {             // OCND2: no snow-graupel collection (fast_rg :183-189, :207)
     int i1, i2;
     const double f1 = lut_index(s.llbdag, c.NDRYLBDAG, c.DRYINTP1G, c.DRYINTP2G, i1);
     const double f2 = lut_index(s.llbdas, c.NDRYLBDAS, c.DRYINTP1S, c.DRYINTP2S, i2);
@@ -589,6 +683,37 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
                                        : 0.0;
   }
 
+  // ---- OCND2: ICE4_FAST_RI_RS (mode_ice4_fast_ri_rs.F90, LMODICEDEP = .FALSE.)
+  // in place of ICE4_FAST_RI (mode_ice4_tendencies.F90:568-596) ----
+  if (O) {
+    b[B_RCBERI] = 0.0;
+    const double ri = v[IRI], dicrit = c.FRMIN15, timesc = c.FRMIN14;
+    double rilars = (pos(ri) && gtp(R.ssi, 0.001)) ? dmin(ri, fm::fdiv(ri, fm::fdiv(87.5 * (dicrit * dicrit) * ai, R.ssi)))
+                                                  : 0.0;
+    double rvdepi = 0.0;
+    if (pos(pf.pres * 0.5 - esi) && pos(cit)) {
+      const double w2d = fm::frcp(op->ifr * op->icldfr + 1. - op->icldfr);
+      const double xw2d13 = fm::fexp(0.333 * fm::flog(op->ifr));
+      const double wcitred23 = fm::fexp(0.667 * fm::flog(0.1));
+      const double tc = dmax(-18., dmin(-1., t - c.TT));
+      const double hu = dmin(0.15, pmax0(R.ssi));
+      const double cryssha = 1.1 + 3. * hu * (1. + sin(0.64 * tc - 1.3));
+      const double qimax = fm::fdiv(366.5 * (dicrit * dicrit * dicrit) * cit * 0.1, rho);
+      double ci2s = 0.;
+      if (gtp(ri, 1.0e-12) && pos(timesc))
+        ci2s = fm::fdiv(ri * (1. - dmin(1., fm::fdiv(0.5 * qimax, ri))) * (1. - op->icldfr) * w2d, timesc * 0.5);
+      const double zzwc = fm::fdiv(cryssha * 0.878, ai) * fm::fexp(0.667 * fm::flog(fm::fdiv(cit, rho))) *
+                          fm::fexp(0.333 * fm::flog(dmax(c.I_RTMIN, ri) * w2d));
+      if (pos(op->ssio) && gtp(op->icldfr, 0.02)) rvdepi = rvdepi + zzwc * xw2d13 * op->ssio * op->icldfr;
+      if (negd(op->ssiu) && ltp(op->icldfr, 0.98)) {
+        rilars = rilars + ci2s;
+        rvdepi = rvdepi + zzwc * wcitred23 * op->ssiu * (1. - op->icldfr);
+      }
+    }
+    orr->rilars = rilars;
+    orr->rvdepi = rvdepi;
+    return;
+  }
   // ---- ICE4_FAST_RI (mode_ice4_fast_ri.F90) ----
   if (pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20)) {
     const double l = dmin(1.e8, c.LBI * fm::fexp(c.LBEXI * fm::flog(fm::fdiv(rho * v[IRI], cit))));
@@ -599,10 +724,12 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 // Rates of a soft pass: the hard-pass values where their condition still
 // holds on the current state, zero elsewhere (the ELSE branches of the
 // process routines under LDSOFT).
-template <bool SUBG = false, bool H = false>
+template <bool SUBG = false, bool H = false, bool O = false>
 ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, const double hl[4],
-                        const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0, HailRates *hr = nullptr)
+                        const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0, HailRates *hr = nullptr,
+                        OcndRates *orr = nullptr)
 {
+  if (O) orr->rvdepi = orr->rilars = 0.0;   // ICE4_FAST_RI_RS resets both and computes them on hard passes only
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
   const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
@@ -667,9 +794,12 @@ ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, con
 // 331-351), the hail growth mode of ICE4_FAST_RH (mode_ice4_fast_rh.F90:
 // 205-213, 250-325; the graupel dry-collection factor on a hard pass) and
 // the hail rows of the aggregation, which also move B (RWETGH_MR).
-template <bool H = false>
+// O (OCND2): the part of the graupel deposition given to snow
+// (mode_ice4_tendencies.F90:445-458) and the RVDEPI / RILARS rows.
+template <bool H = false, bool O = false>
 ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, double lsfact, Rates &R,
-                       double *A, bool soft = false, HailRates *hr = nullptr, double *B = nullptr)
+                       double *A, bool soft = false, HailRates *hr = nullptr, double *B = nullptr,
+                       const OcndRates *orr = nullptr)
 {
   double *b = R.bu;
   const double *rs = R.rs, *rg = R.rg;
@@ -742,9 +872,23 @@ ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, d
            b[B_RCBERI];
   A[IRS] = b[B_RVDEPS] + b[B_RIAGGS] + b[B_RIAUTS] + b[B_RCRIMSS] - b[B_RSRIMCG] + b[B_RRACCSS] - b[B_RSACCRG] -
            b[B_RSMLTG] - b[B_RSWETG] - b[B_RSDRYG];
-  A[IRG] = b[B_RVDEPG] + b[B_RCRIMSG] + b[B_RSRIMCG] + b[B_RRACCSG] + b[B_RSACCRG] + b[B_RSMLTG] + b[B_RICFRRG] +
-           b[B_RRCFRIG] + b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG] + b[B_RCDRYG] + b[B_RIDRYG] +
-           b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
+  double depg_s = 0.0, nodepg_s = 1.0;
+  if (O && gtd(c.FRMIN5, 1.0e-12) && gtd(c.FRMIN6, 0.01)) {
+    depg_s = dmax(0., dmin(1., (c.FRMIN5 - fm::fdiv(v[IRG], c.FRMIN5)))) * dmax(0., dmin(1., fm::fdiv(R.ssi, c.FRMIN6)));
+    nodepg_s = 1. - depg_s;
+  }
+  A[IRG] = (O ? b[B_RVDEPG] * nodepg_s : b[B_RVDEPG]) + b[B_RCRIMSG] + b[B_RSRIMCG] + b[B_RRACCSG] + b[B_RSACCRG] +
+           b[B_RSMLTG] + b[B_RICFRRG] + b[B_RRCFRIG] + b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG] +
+           b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
+  if (O) {
+    // OCND2 rows (mode_ice4_tendencies.F90:625, 630, 673-677, 691)
+    A[ITH] += orr->rvdepi * lsfact;
+    A[IRV] -= orr->rvdepi;
+    A[IRI] += orr->rvdepi;
+    A[IRI] -= orr->rilars;
+    A[IRS] += b[B_RVDEPG] * depg_s;
+    A[IRS] += orr->rilars;
+  }
   if (H) {
     double *hb = hr->b, *ht = hr->t;
     if (ldwetg) {
@@ -836,10 +980,12 @@ ICE3_HD void slow_rates_from(const Cst &c, double t, const double v[NV], const d
 // The state adjustments of a hard pass (mode_ice4_tendencies.F90:166-300):
 // nucleation (HENI), RRHONG and RIMLTC with their T-feedback limits; v and
 // t are updated in place, the increments go to b and B.
+template <bool O = false>
 ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, double lvfact, double lsfact,
-                         double &cit, double &t, double v[NV], double *b, double B[NV])
+                         double &cit, double &t, double v[NV], double *b, double B[NV], const OcndPt *op = nullptr)
 {
-  nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
+  if (O) nucleation_ocnd2(c, *op, t, v[IRV], cit, b[B_RVHENI_MR]);
+  else nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
   v[ITH] += b[B_RVHENI_MR] * lsfact;
   t = v[ITH] * pf.exn;
   v[IRV] -= b[B_RVHENI_MR];
@@ -878,12 +1024,13 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
 // nucleation, RRHONG and RIMLTC adjust the state (their increments go to B)
 // and all rates are computed; a soft pass keeps the hard-pass rates.
-template <bool SUR = false, bool SUBG = false, bool H = false>
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
 ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict__ lut, bool soft,
                         const PointFix &pf, double lvfact, double lsfact, double &cit, double t0,
                         const double *vart, Rates &R, double &rainfr, double hl[4], double hi[4], double *A,
                         double *B, const double *sur = nullptr, HailRates *hr = nullptr,
-                        const double *__restrict__ hlut = nullptr)
+                        const double *__restrict__ hlut = nullptr, const OcndPt *op = nullptr,
+                        OcndRates *orr = nullptr)
 {
   constexpr int NVT = H ? NVH : NV;
   double v[NVT];
@@ -892,7 +1039,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   for (int k = 0; k < NVT; ++k) { v[k] = vart[k]; B[k] = 0.0; }
   double *b = R.bu;
   if (!soft) {
-    hard_adjust(c, d, pf, lvfact, lsfact, cit, t, v, b, B);
+    hard_adjust<O>(c, d, pf, lvfact, lsfact, cit, t, v, b, B, op);
   } else {
     b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = 0.0;
   }
@@ -907,20 +1054,24 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   } else {
     rainfr = 1.;
   }
-  if (!soft) hard_rates<SUR, SUBG, H>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr, hr, hlut);
-  else soft_rates<SUBG, H>(c, t, v, cit, hl, hi, R, pf.cf, rainfr, hr);
+  if (!soft)
+    hard_rates<SUR, SUBG, H, O>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr, hr, hlut, op,
+                                orr);
+  else soft_rates<SUBG, H, O>(c, t, v, cit, hl, hi, R, pf.cf, rainfr, hr, orr);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
-  aggregate<H>(c, t, v, lvfact, lsfact, R, A, soft, hr, B);
+  aggregate<H, O>(c, t, v, lvfact, lsfact, R, A, soft, hr, B, orr);
 }
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
-template <bool SUR = false, bool SUBG = false, bool H = false>
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
 ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                               double dt, int max_passes, double *vart, const double *ext, double &cit,
                               double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped,
-                              const double *sur = nullptr, const double *__restrict__ hlut = nullptr)
+                              const double *sur = nullptr, const double *__restrict__ hlut = nullptr,
+                              const OcndPt *op = nullptr)
 {
+  OcndRates OR{0.0, 1.0, 1.0, 0.0, 0.0};
   constexpr int NVT = H ? NVH : NV;
   const double rsmin[NVH] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN, c.H_RTMIN};
   HailRates HR;
@@ -961,8 +1112,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
       double A[NVT], B[NVT];
-      tendencies<SUR, SUBG, H>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
-                               &HR, hlut);
+      tendencies<SUR, SUBG, H, O>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
+                                  &HR, hlut, op, &OR);
       if (SUR) sur = nullptr;          // learned slow rates: first hard pass only
 #pragma unroll
       for (int v = 0; v < NVT; ++v) A[v] += ext[v];
@@ -1016,10 +1167,14 @@ ICE3_HD double ldp(const double *p, long i)
 // sources, written back in place.  Returns the pass key (0 for points
 // outside LLMICRO or capped); `capped` reports a point that hit max_passes.
 // H (NRR = 7): with hail (rht / rhs; the hail kernels at hlut).
-template <bool SUR = false, bool SUBG = false, bool H = false>
+// O (OCND2): the LOCND2 branches, with the TIWMX tables tw and the level
+// heights / droplet concentrations of ocnd2_column() at ozz / oconc.
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
 ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
                                     const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped,
-                                    const double *sur = nullptr, const double *__restrict__ hlut = nullptr)
+                                    const double *sur = nullptr, const double *__restrict__ hlut = nullptr,
+                                    const double *tw = nullptr, const double *ozz = nullptr,
+                                    const double *oconc = nullptr)
 {
   constexpr int NVT = H ? NVH : NV;
   const double inv_dt = 1.0 / dt;
@@ -1045,8 +1200,18 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   const double t = th * pf.exn;
   const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
   const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
-  const bool micro = gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
-                     gtp(rg, c.G_RTMIN) || (H && gtp(rh, c.H_RTMIN));
+  OcndPt op;
+  if (O) {
+    op.tw = tw;
+    op.ssio = ldp(f.ssio, p); op.ssiu = ldp(f.ssiu, p); op.ifr = ldp(f.ifr, p); op.icldfr = ldp(f.icldfr, p);
+    op.zzz = ozz[p];
+    op.conc = oconc[p];
+  }
+  // LLMICRO (OCND2: rain_ice.F90:347-363, the XFRMIN(12) / XFRMIN(13) thresholds)
+  const bool micro = O ? (gtp(op.ssio, c.FRMIN12) || gtp(rc, c.FRMIN13) || gtp(rr, c.FRMIN13) || gtp(ri, c.FRMIN13) ||
+                          gtp(rs, c.FRMIN13) || gtp(rg, c.FRMIN13))
+                       : (gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
+                          gtp(rg, c.G_RTMIN) || (H && gtp(rh, c.H_RTMIN)));
   const double iexnref = fm::frcp(exnref);
   const double lsx = lsf * iexnref, lvx = lvf * iexnref;
   // with a PRFR option the sub-stepping starts from the precipitation
@@ -1056,7 +1221,8 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   double zrvheni = 0.0;
   if (!micro) {
     cit = 0.0;
-    nucleation(c, d, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
+    if (O) nucleation_ocnd2(c, op, t, rv, cit, zrvheni);
+    else nucleation(c, d, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
   }
   zrvheni = dmin(rvs, zrvheni * inv_dt);
   if (micro) {
@@ -1085,8 +1251,8 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
       hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
     }
     double rrevav;
-    key = stepping<SUR, SUBG, H>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped, sur,
-                                 hlut);
+    key = stepping<SUR, SUBG, H, O>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped,
+                                    sur, hlut, &op);
 #pragma unroll
     for (int v = 0; v < NVT; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;

@@ -56,7 +56,8 @@ class RainIceFields(ctypes.Structure):
         "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs",
         "evap3d", "rainfr", "inprc", "inprr", "inpri", "inprs", "inprg", "indep",
         "fpr_c", "fpr_r", "fpr_i", "fpr_s", "fpr_g",
-        "rht", "rhs", "inprh", "fpr_h")]          # hail, NRR = 7
+        "rht", "rhs", "inprh", "fpr_h",           # hail, NRR = 7
+        "ssio", "ssiu", "ifr", "icldfr")]         # OCND2
 
 
 class StepFields(ctypes.Structure):

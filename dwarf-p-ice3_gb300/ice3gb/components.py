@@ -312,6 +312,14 @@ class RainIce:
             rhs = get("rhs")
             fields["rhs"] = (self._to_kij(rhs) if rhs is not None
                              else torch.zeros((nk, nij), dtype=torch.float64, device=ref_t.device)).clone()
+        if self.table.values["OCND2"] != 0.0:
+            # OCND2: the ice_adjust OCND2 outputs of the same state (IceAdjust's
+            # five extra outputs), same names
+            for k in ("ssio", "ssiu", "ifr", "icldfr"):
+                v = get(k)
+                if v is None:
+                    raise KeyError(f"state is missing {k!r} (OCND2)")
+                fields[k] = self._to_kij(v)
         sea, town = get("sea"), get("town")
         if (sea is None) != (town is None):
             raise ValueError("sea and town must be given together")

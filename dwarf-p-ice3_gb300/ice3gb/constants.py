@@ -196,6 +196,17 @@ def _hail_constants(ext: Mapping[str, Any]) -> Dict[str, float]:
     return v
 
 
+# XFRMIN_NAM(1:40) of modd_param_icen.F90:366-395 (the Fortran defaults; the
+# reference's Python table holds uninitialised values at 9, 22, 30 and 38)
+_FRMIN = {1: 0., 2: 0., 3: 0., 4: 0., 5: 0., 6: 0., 7: 1., 8: 1., 9: 1., 10: 10., 11: 1., 12: 0., 13: 1.0e-15,
+          14: 120., 15: 1.0e-4, 16: 0., 17: 0., 18: 0., 19: 0., 20: 0., 21: 1., 22: 1., 23: 0.5, 24: 1.5,
+          25: 30., 26: 0., 27: 0., 28: 0., 29: 0., 30: 1., 39: 0.25, 40: 0.15}
+
+
+def _frmin_constants() -> Dict[str, float]:
+    return {f"FRMIN{i}": float(_FRMIN.get(i, 0.0)) for i in range(1, 41)}
+
+
 def _hail_kernels() -> Dict[str, np.ndarray]:
     d = np.load(os.path.join(_HERE, "data", "hail_kernels.npz"))
     return {k: d[k] for k in ("ker_sweth", "ker_gweth", "ker_rweth")}
@@ -206,7 +217,7 @@ def build_table(phyex: Any = None, table: str = "jax", program: str = "AROME",
     if table not in ("jax", "phyex"):
         raise ValueError("table must be 'jax' or 'phyex'")
     ext = externals_from(phyex, program)
-    hail = _hail_constants(ext)
+    hail = {**_hail_constants(ext), **_frmin_constants()}
     values: Dict[str, float] = {}
     for name in CONSTANT_NAMES:
         if name in ext:

@@ -68,7 +68,7 @@ extern "C" {
   /* physical constants (modd_cst) */                                         \
   X(TT) X(CPD) X(CPV) X(CL) X(CI) X(RD) X(RV) X(LVTT) X(LSTT) X(LMTT)         \
   X(ESTT) X(ALPW) X(BETAW) X(GAMW) X(ALPI) X(BETAI) X(GAMI) X(EPSILO)         \
-  X(P00) X(RHOLW) X(MNH_TINY) X(GRAVITY0)                                     \
+  X(P00) X(RHOLW) X(MNH_TINY) X(GRAVITY0) X(PI)                               \
   /* subgrid condensation (modd_nebn) */                                      \
   X(TMAXMIX) X(TMINMIX) X(LSUBG_COND) X(LSIGMAS) X(LSTATNW)                   \
   X(FRAC_ICE_ADJUST) X(CONDENS) X(OCND2) X(NRR) X(LAMBDA3)                    \
@@ -109,7 +109,15 @@ extern "C" {
   X(FRWETH) X(LBRWETH1) X(LBRWETH2) X(LBRWETH3) X(WETINTP1H) X(WETINTP2H)     \
   X(WETINTP1S) X(WETINTP2S) X(WETINTP1G) X(WETINTP2G) X(WETINTP1R)            \
   X(WETINTP2R) X(NWETLBDAH) X(NWETLBDAS) X(NWETLBDAG) X(NWETLBDAR)            \
-  X(LNULLWETH) X(LWETHPOST) X(LCONVHG)
+  X(LNULLWETH) X(LWETHPOST) X(LCONVHG)                                        \
+  /* XFRMIN(1:40), the OCND2 tuning vector (modd_param_icen.F90:366-395) */     \
+  X(FRMIN1) X(FRMIN2) X(FRMIN3) X(FRMIN4) X(FRMIN5) X(FRMIN6) X(FRMIN7)       \
+  X(FRMIN8) X(FRMIN9) X(FRMIN10) X(FRMIN11) X(FRMIN12) X(FRMIN13)             \
+  X(FRMIN14) X(FRMIN15) X(FRMIN16) X(FRMIN17) X(FRMIN18) X(FRMIN19)           \
+  X(FRMIN20) X(FRMIN21) X(FRMIN22) X(FRMIN23) X(FRMIN24) X(FRMIN25)           \
+  X(FRMIN26) X(FRMIN27) X(FRMIN28) X(FRMIN29) X(FRMIN30) X(FRMIN31)           \
+  X(FRMIN32) X(FRMIN33) X(FRMIN34) X(FRMIN35) X(FRMIN36) X(FRMIN37)           \
+  X(FRMIN38) X(FRMIN39) X(FRMIN40)
 
 typedef struct Ice3gbConstants {
 #define ICE3GB_X_FIELD(name) double name;
@@ -218,6 +226,9 @@ typedef struct Ice3gbRainIceFields {
   double *rhs;                      /* in-out hail source                 */
   double *inprh;                    /* out [nij] hail precipitation rate  */
   double *fpr_h;                    /* out, optional                      */
+  /* OCND2 only (ignored otherwise): the ice_adjust OCND2 outputs of the
+   * same state (Ice3gbIceAdjustFields ssio, ssiu, ifr, icldfr)           */
+  const double *ssio, *ssiu, *ifr, *icldfr;
 } Ice3gbRainIceFields;
 
 /* Per-call overrides of RainIceJAX.__call__ keywords

@@ -103,6 +103,34 @@ EXPORT void ice3o_tiwmx_tables(const C *c, double *estw, double *esti)
   }
 }
 
+/* The six TIWMX tables OCND2 reads (micro/mode_ini_tiwmx.F90, functions of
+ * micro/mode_tiwmx_fun.F90): ESTABW, ESTABI, A2TAB (AA2), BB3TAB (BB3),
+ * AM3TAB (AM3, 0 above 273.15 K), REDINTAB (REDIN), each TIWMX_N long. */
+enum { TW_ESW, TW_ESI, TW_A2, TW_BB3, TW_AM3, TW_REDIN, TW_N };
+
+static double esatw_fun(const C *c, double t) { return exp(c->ALPW - c->BETAW / t - c->GAMW * log(t)); }
+/* ESATI of mode_tiwmx_fun.F90: the water formula at and above TT, the ice one below */
+static double esati_fun(const C *c, double t)
+{
+  return t >= c->TT ? esatw_fun(c, t) : exp(c->ALPI - c->BETAI / t - c->GAMI * log(t));
+}
+
+EXPORT void ice3o_tiwmx_all(const C *c, double *tab)
+{
+  ice3o_tiwmx_tables(c, tab + TW_ESW * TIWMX_N, tab + TW_ESI * TIWMX_N);
+  for (int j = TIWMX_NSTART; j <= TIWMX_NSTOP; ++j) {
+    const double t = (double)j / 100.0;
+    const long i = j - TIWMX_NSTART;
+    tab[TW_A2 * TIWMX_N + i] = sq(c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / (2.38e-2 + 0.0071e-2 * (t - c->TT)) /
+                               (sq(t) * c->RV);
+    tab[TW_BB3 * TIWMX_N + i] = c->RV / (0.211e-4 * pow(t / c->TT, 1.94) * c->P00) * t / esati_fun(c, t);
+    tab[TW_AM3 * TIWMX_N + i] =
+        t > 273.15 ? 0. : 1000. * exp(12.96 * (esatw_fun(c, t) / esati_fun(c, t) - 1.) - 0.639);
+    const double zzt = dmax(0., dmin(1., (c->TT - t) / 20.));
+    tab[TW_REDIN * TIWMX_N + i] = 1. - (1. - zzt) / pow(zzt * zzt * zzt + (1. - zzt) * (1. - zzt) * (1. - zzt), .333);
+  }
+}
+
 /* ESATW / ESATI of micro/mode_tiwmx.F90: TAB(NINT(XNDEGR*T)); the index is
  * clamped to the table (the reference reads out of bounds there). */
 static double tiwmx_at(const double *tab, double t)
@@ -661,6 +689,8 @@ enum {
   /* KRR = 7: graupel -> hail conversion and ICE4_FAST_RH */
   B_RWETGH, B_RWETGH_MR, B_RCWETH, B_RIWETH, B_RSWETH, B_RGWETH, B_RRWETH,
   B_RCDRYH, B_RIDRYH, B_RSDRYH, B_RRDRYH, B_RGDRYH, B_RDRYHG, B_RHMLTR,
+  /* OCND2: ICE4_FAST_RI_RS */
+  B_RVDEPI, B_RILARS,
   NBU
 };
 /* fast_rs persistent tendencies (mode_ice4_fast_rs.F90 IRCRIMS..IFREEZ2) */
@@ -678,6 +708,7 @@ typedef struct {
   double rh_tend[NRH];
   double ssi, ka, dv, ai, cj;
   int tie;    /* a wet/dry growth choice was decided by rounding residuals */
+  double esi, colf, acrf;   /* OCND2, hard pass: tabulated es_i, collision factors */
 } PointRates;
 
 /* The wet/dry growth choice compares max(0, .) of differences whose exact
@@ -698,13 +729,29 @@ static inline double esatw(const C *c, double t) { return exp(c->ALPW - c->BETAW
 static inline double esati(const C *c, double t) { return exp(c->ALPI - c->BETAI / t - c->GAMI * log(t)); }
 
 /* ICE4_NUCLEATION, micro/ice4_nucleation.func.h:69-144 (LOCND2 = .FALSE.). */
+static double tiwmx_at(const double *tab, double t);
+
+/* tw != NULL: the OCND2 branch (:127-136): concentration from REDIN, AM3,
+ * the height zzz and the ice cloud fraction, no vapour taken (HENI = 0). */
 static void ice4_nucleation(const C *c, int ldcompute, double tht, double pabst, double rhodref,
                             double exn, double lsfact, double t, double rvt, double *cit,
-                            double *rvheni_mr, double *ssi_out)
+                            double *rvheni_mr, double *ssi_out, const double *tw, double zzz, double icldfr)
 {
   const int gnegt = ldcompute && t < c->TT && rvt > c->V_RTMIN;
   double zusw = 0.0, zzw = 0.0, zssi = 0.0;
   *rvheni_mr = 0.0;
+  if (tw) {
+    if (gnegt) {
+      const double redin = tiwmx_at(tw + TW_REDIN * TIWMX_N, t);
+      const double am3 = tiwmx_at(tw + TW_AM3 * TIWMX_N, dmax(c->FRMIN27, t));
+      const double h = (20000. - dmin(20000., zzz)) / 20000.;
+      zzw = redin * dmax(0.1, h * h * h * h) * am3 * (0.0001 + 0.9999 * icldfr);
+      zzw = dmin(zzw, 50.e3);
+      *cit = dmax(zzw + *cit, *cit);
+    }
+    if (ssi_out) *ssi_out = 0.0;
+    return;
+  }
   if (gnegt) {
     zzw = log(t);
     zusw = exp(c->ALPW - c->BETAW / t - c->GAMW * zzw);
@@ -876,6 +923,15 @@ static inline double lut2d(const double *lt, int n2, int i1, double f1, int i2, 
 #undef L
 }
 
+/* OCND2 inputs of one point: the TIWMX tables, the ice_adjust OCND2 outputs
+ * (super-saturations over ice in the cloudy / clear parts, PIFR, the ice
+ * cloud fraction), the level height (rain_ice.F90:386-394) and the cloud
+ * droplet concentration (:396-435). */
+typedef struct {
+  const double *tw;
+  double ssio, ssiu, ifr, icldfr, zzz, conc;
+} Ocnd2Pt;
+
 /* Per-point context passed to the process routines. */
 typedef struct {
   const C *c;
@@ -886,6 +942,9 @@ typedef struct {
   double v[NVH];     /* state after the instantaneous processes       */
   double lbdar, lbdar_rf, lbdas, lbdag, lbdah;
   int hail;          /* KRR = 7                                       */
+  /* OCND2 (tw != NULL): TIWMX tables and the per-point inputs */
+  const double *tw;
+  double ssio, ssiu, ifr, icldfr, zzz, conc;
   double rainfr;     /* PRAINFR (packed, per point)                   */
   double hl[4], hi[4];
 } Tctx;
@@ -900,9 +959,11 @@ static void ice4_slow(const Tctx *x, PointRates *pr)
     if (!x->ldsoft) b[B_RCHONI] = dmin(1000., c->HON * rho * x->v[IRC] * exp(c->ALPHA3 * (t - c->TT) - c->BETA3));
   } else b[B_RCHONI] = 0.0;
   if (x->v[IRV] > c->V_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute) {
-    if (!x->ldsoft)
+    if (!x->ldsoft) {
       b[B_RVDEPS] = (pr->ssi / (rho * pr->ai)) *
                     (c->O0DEPS * pow(x->lbdas, c->EX0DEPS) + c->O1DEPS * pr->cj * pow(x->lbdas, c->EX1DEPS));
+      if (x->tw) b[B_RVDEPS] = b[B_RVDEPS] * c->FRMIN40;        /* ZREDSN, :92-99, 142 */
+    }
   } else b[B_RVDEPS] = 0.0;
   if (x->v[IRI] > c->I_RTMIN && x->v[IRS] > c->S_RTMIN && x->ldcompute) {
     if (!x->ldsoft)
@@ -916,9 +977,11 @@ static void ice4_slow(const Tctx *x, PointRates *pr)
     }
   } else b[B_RIAUTS] = 0.0;
   if (x->v[IRV] > c->V_RTMIN && x->v[IRG] > c->G_RTMIN && x->ldcompute) {
-    if (!x->ldsoft)
+    if (!x->ldsoft) {
       b[B_RVDEPG] = (pr->ssi / (rho * pr->ai)) *
                     (c->O0DEPG * pow(x->lbdag, c->EX0DEPG) + c->O1DEPG * pr->cj * pow(x->lbdag, c->EX1DEPG));
+      if (x->tw) b[B_RVDEPG] = b[B_RVDEPG] * c->FRMIN39;        /* ZREDGR, :212 */
+    }
   } else b[B_RVDEPG] = 0.0;
 }
 
@@ -935,7 +998,8 @@ static void ice4_warm(const Tctx *x, PointRates *pr)
   if ((int)c->SUBG_RC_RR_ACCR == 0) {
     if (x->v[IRC] > c->C_RTMIN && x->v[IRR] > c->R_RTMIN && x->ldcompute) {
       if (!x->ldsoft)
-        b[B_RCACCR] = c->FCACCR * x->v[IRC] * 1.0 /* PACRF */ * pow(x->lbdar, c->EXCACCR) * pow(rho, -c->CEXVT);
+        b[B_RCACCR] = c->FCACCR * x->v[IRC] * (x->tw ? pr->acrf : 1.0) /* PACRF */ * pow(x->lbdar, c->EXCACCR) *
+                      pow(rho, -c->CEXVT);
     } else b[B_RCACCR] = 0.0;
   } else {
     const int m = x->v[IRC] > c->C_RTMIN && x->v[IRR] > c->R_RTMIN && x->ldcompute;
@@ -1020,8 +1084,9 @@ static void ice4_fast_rs(const Tctx *x, PointRates *pr)
     const double zw1 = lut1d(lut->gaminc_rim1, i, fr);
     const double zw2 = lut1d(lut->gaminc_rim2, i, fr);
     const double zw3 = lut1d(lut->gaminc_rim4, i, fr);
-    rs[RS_RCRIMSS] = c->CRIMSS * zw1 * x->v[IRC] * 1.0 /* PCOLF */ * pow(lbdas, c->EXCRIMSS) * pow(rho, -c->CEXVT);
-    rs[RS_RCRIMS] = c->CRIMSG * x->v[IRC] * 1.0 * pow(lbdas, c->EXCRIMSG) * pow(rho, -c->CEXVT);
+    const double colf = x->tw ? pr->colf : 1.0;                      /* PCOLF */
+    rs[RS_RCRIMSS] = c->CRIMSS * zw1 * x->v[IRC] * colf * pow(lbdas, c->EXCRIMSS) * pow(rho, -c->CEXVT);
+    rs[RS_RCRIMS] = c->CRIMSG * x->v[IRC] * colf * pow(lbdas, c->EXCRIMSG) * pow(rho, -c->CEXVT);
     if ((int)c->SNOW_RIMING == 0) { /* M90 */
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
       double r = c->SRIMCG * pow(lbdas, c->EXSRIMCG) * (1.0 - zw2);
@@ -1057,9 +1122,11 @@ static void ice4_fast_rs(const Tctx *x, PointRates *pr)
                          (c->LBRACCS1 / sq(lbdas) + c->LBRACCS2 / (lbdas * lbdar) + c->LBRACCS3 / sq(lbdar)) /
                          sq(sq(lbdar));
       rs[RS_RRACCSS] = zw1 * zzw;
+      if (x->tw) rs[RS_RRACCSS] = rs[RS_RRACCSS] * c->FRMIN7;         /* :327 */
       rs[RS_RRACCS] = zw2 * zzw;
-      rs[RS_RSACCRG] = c->FSACCRG * zw3 * pow(lbdas, c->CXS - c->BS) * pow(rho, -c->CEXVT - 1.) *
-                       (c->LBSACCR1 / sq(lbdar) + c->LBSACCR2 / (lbdar * lbdas) + c->LBSACCR3 / sq(lbdas)) / lbdar;
+      if (!x->tw || x->v[IRS] > c->FRMIN1)                             /* :347 */
+        rs[RS_RSACCRG] = c->FSACCRG * zw3 * pow(lbdas, c->CXS - c->BS) * pow(rho, -c->CEXVT - 1.) *
+                         (c->LBSACCR1 / sq(lbdar) + c->LBSACCR2 / (lbdar * lbdas) + c->LBSACCR3 / sq(lbdas)) / lbdar;
     }
   }
   if (gacc && t < c->TT) {
@@ -1126,8 +1193,8 @@ static int ice4_fast_rg(const Tctx *x, PointRates *pr, double cit)
   } else rg[RG_RIDRYG] = rg[RG_RIWETG] = 0.0;
   /* snow collection (SDRYG LUT): :203-235 */
   const int gdry_s = x->v[IRS] > c->S_RTMIN && x->v[IRG] > c->G_RTMIN && x->ldcompute;
-  if (!gdry_s) rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;
-  if (!x->ldsoft && gdry_s) {
+  if (!gdry_s || x->tw) rg[RG_RSDRYG] = rg[RG_RSWETG] = 0.0;      /* OCND2: no snow-graupel collection */
+  if (!x->ldsoft && gdry_s && !x->tw) {
     int i1, i2;
     const double f1 = lut_index(lbdag, (int)c->NDRYLBDAG, c->DRYINTP1G, c->DRYINTP2G, &i1);
     const double f2 = lut_index(lbdas, (int)c->NDRYLBDAS, c->DRYINTP1S, c->DRYINTP2S, &i2);
@@ -1346,6 +1413,7 @@ static void ice4_fast_ri(const Tctx *x, PointRates *pr, double cit)
 {
   const C *c = x->c;
   double *b = pr->bu;
+  if (x->tw) { b[B_RCBERI] = 0.0; return; }                        /* mode_ice4_tendencies.F90:568-579 */
   if (pr->ssi > 0. && x->v[IRC] > c->C_RTMIN && x->v[IRI] > c->I_RTMIN && cit > 1.e-20 && x->ldcompute) {
     if (!x->ldsoft) {
       double l = dmin(1.e8, c->LBI * pow(x->rhodref * x->v[IRI] / cit, c->LBEXI));
@@ -1353,6 +1421,68 @@ static void ice4_fast_ri(const Tctx *x, PointRates *pr, double cit)
                     (c->O0DEPI / l + c->O2DEPI * pr->cj * pr->cj / pow(l, c->DI + 2.0));
     }
   } else b[B_RCBERI] = 0.0;
+}
+
+/* ICE4_FAST_RI_RS, micro/mode_ice4_fast_ri_rs.F90 (OCND2, LMODICEDEP =
+ * .FALSE.): conversion of large ice crystals to snow (RILARS) and the
+ * deposition on ice in the cloudy and clear parts (RVDEPI); zero on soft
+ * passes (both are reset on entry and computed only when LDSOFT is false). */
+static void ice4_fast_ri_rs(const Tctx *x, PointRates *pr, double cit)
+{
+  const C *c = x->c;
+  double *b = pr->bu;
+  const double ztimesc = c->FRMIN14, zdicrit = c->FRMIN15;
+  const double rit = x->v[IRI], rho = x->rhodref, t = x->t;
+  const double zwcitred = 0.1;
+  b[B_RILARS] = 0.;
+  b[B_RVDEPI] = 0.;
+  if (x->ldsoft) return;
+  if (rit > 0.0 && pr->ssi > 0.001)
+    b[B_RILARS] = dmin(rit, rit / (87.5 * (zdicrit * zdicrit) * pr->ai / pr->ssi));
+  const double zw2d = 1. / (x->ifr * x->icldfr + 1. - x->icldfr);
+  if ((x->pres * 0.5 - pr->esi) > 0. && cit > 0. && x->ldcompute) {
+    const double xw2d13 = pow(x->ifr, 0.333);
+    const double wcitred23 = pow(zwcitred, 0.667);
+    const double tc = dmax(-18., dmin(-1., t - c->TT));
+    const double hu = dmin(0.15, dmax(0., pr->ssi));
+    const double cryssha = 1.1 + 3. * hu * (1. + sin(0.64 * tc - 1.3));
+    const double qimax = 366.5 * (zdicrit * zdicrit * zdicrit) * cit * zwcitred / rho;
+    double ci2s = 0.;
+    if (rit > 1.0e-12 && ztimesc > 0.)
+      ci2s = rit * (1. - dmin(1., 0.5 * qimax / rit)) * (1. - x->icldfr) * zw2d / (ztimesc * 0.5);
+    const double zzwc = cryssha * 0.878 / pr->ai * pow(cit / rho, 0.667) * pow(dmax(c->I_RTMIN, rit) * zw2d, 0.333);
+    if (x->ssio > 0. && x->icldfr > 0.02) b[B_RVDEPI] = b[B_RVDEPI] + zzwc * xw2d13 * x->ssio * x->icldfr;
+    if (x->ssiu < 0. && x->icldfr < 0.98) {
+      b[B_RILARS] = b[B_RILARS] + ci2s;
+      b[B_RVDEPI] = b[B_RVDEPI] + zzwc * wcitred23 * x->ssiu * (1. - x->icldfr);
+    }
+  }
+}
+
+/* The OCND2 parts of the derived fields (mode_ice4_tendencies.F90:303-346,
+ * after ice4_derived): tabulated es_i, ssi and ai = AA2 + BB3 p (LLTAB), and
+ * the collision factors of cloud water with rain (ACRF) and with snow /
+ * graupel (COLF) from the mean droplet radius (LLCOL). */
+static void ocnd2_derived(const Tctx *x, PointRates *pr)
+{
+  const C *c = x->c;
+  pr->esi = tiwmx_at(x->tw + TW_ESI * TIWMX_N, x->t);
+  pr->ssi = x->v[IRV] * (x->pres - pr->esi) / (c->EPSILO * pr->esi) - 1.0;
+  pr->ai = tiwmx_at(x->tw + TW_A2 * TIWMX_N, x->t) + tiwmx_at(x->tw + TW_BB3 * TIWMX_N, x->t) * x->pres;
+  const double conc = x->conc * 0.000001;
+  pr->colf = 0.00001;
+  pr->acrf = 0.00001;
+  if (x->v[IRC] > 1.0e-10) {
+    const double rcw = 0.1 * pow(0.75 * x->v[IRC] * x->rhodref / (c->PI * conc), 0.333);
+    double vt = rcw < 0.0065 ? 1.19e6 * sq(rcw) : 8000. * rcw;
+    vt = dmin(10., vt);
+    const double st = dmax(0.01, 2. * (100. - vt) * vt / (c->GRAVITY0 * 10.));
+    if (st > 0.1) pr->colf = dmax(0.01, dmin(1., 0.939 * pow(st, 2.657)));
+    if (x->v[IRR] > 1.0e-10 && rcw > 1.0e-5) {
+      const double r20 = exp(rcw * 2000.);
+      pr->acrf = (r20 - 1.) / (r20 + 1.);
+    }
+  }
 }
 
 /* Slope parameters, mode_ice4_tendencies.F90:389-433 (LSNOW_T optional). */
@@ -1388,7 +1518,7 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
                             double exn, double rhodref, double lvfact, double lsfact, double pres,
                             double cf, double sigma_rc, double *cit, double t, const double vart[NVH],
                             PointRates *pr, double *rainfr, double hl[4], double hi[4],
-                            double A[NVH], double B[NVH])
+                            double A[NVH], double B[NVH], const Ocnd2Pt *oc)
 {
   Tctx x;
   x.c = c; x.lut = lut; x.ldsoft = ldsoft; x.ldcompute = ldcompute;
@@ -1396,6 +1526,11 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   x.cf = cf; x.sigma_rc = sigma_rc; x.t = t; x.rainfr = *rainfr;
   x.hail = (int)c->NRR == 7;
   x.lbdah = 0.0;
+  x.tw = oc ? oc->tw : NULL;
+  if (oc) {
+    x.ssio = oc->ssio; x.ssiu = oc->ssiu; x.ifr = oc->ifr; x.icldfr = oc->icldfr; x.zzz = oc->zzz;
+    x.conc = oc->conc;
+  }
   for (int v = 0; v < NVH; ++v) { x.v[v] = (v < NV || x.hail) ? vart[v] : 0.0; A[v] = 0.0; B[v] = 0.0; }
   for (int k = 0; k < 4; ++k) { x.hl[k] = hl[k]; x.hi[k] = hi[k]; }
   double *b = pr->bu;
@@ -1403,7 +1538,8 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
     b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = b[B_RSRIMCG_MR] = 0.0;
   } else {
     /* :171-183 nucleation */
-    ice4_nucleation(c, ldcompute, x.v[ITH], pres, rhodref, exn, lsfact, x.t, x.v[IRV], cit, &b[B_RVHENI_MR], NULL);
+    ice4_nucleation(c, ldcompute, x.v[ITH], pres, rhodref, exn, lsfact, x.t, x.v[IRV], cit, &b[B_RVHENI_MR], NULL,
+                    oc ? oc->tw : NULL, oc ? oc->zzz : 0.0, oc ? oc->icldfr : 0.0);
     x.v[ITH] += b[B_RVHENI_MR] * lsfact;
     x.t = x.v[ITH] * exn;
     x.v[IRV] -= b[B_RVHENI_MR];
@@ -1435,6 +1571,7 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
     B[IRG] += b[B_RSRIMCG_MR];
     /* :303-320 derived fields */
     ice4_derived(c, x.t, rhodref, pres, x.v[IRV], &pr->ssi, &pr->ka, &pr->dv, &pr->ai, &pr->cj);
+    if (oc) ocnd2_derived(&x, pr);
   }
   /* :352 compute_pdf */
   x.rainfr = *rainfr;
@@ -1455,6 +1592,15 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   const int ldwetg = ice4_fast_rg(&x, pr, *cit);
   if (x.hail) ice4_fast_rh(&x, pr, ldwetg);                          /* :535-545 */
   ice4_fast_ri(&x, pr, *cit);
+  /* :445-458 part of the graupel deposition given to snow; :585-596 RVDEPI, RILARS */
+  double depg_s = 0.0, nodepg_s = 1.0;
+  if (x.tw) {
+    if (c->FRMIN5 > 1.0e-12 && c->FRMIN6 > 0.01) {
+      depg_s = dmax(0., dmin(1., (c->FRMIN5 - x.v[IRG] / c->FRMIN5))) * dmax(0., dmin(1., (pr->ssi / c->FRMIN6)));
+      nodepg_s = 1. - depg_s;
+    }
+    ice4_fast_ri_rs(&x, pr, *cit);
+  }
   /* :606-717 aggregation (KRR = 6, LOCND2 = .FALSE.) */
   const double lsv = lsfact - lvfact;
   A[ITH] += b[B_RVDEPG] * lsfact;
@@ -1509,7 +1655,7 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   A[IRS] -= b[B_RSMLTG];
   A[IRS] -= b[B_RSWETG];
   A[IRS] -= b[B_RSDRYG];
-  A[IRG] += b[B_RVDEPG];                 /* * ZNODEPG_S = 1 */
+  A[IRG] += x.tw ? b[B_RVDEPG] * nodepg_s : b[B_RVDEPG];         /* :693 */
   A[IRG] += b[B_RCRIMSG] + b[B_RSRIMCG];
   A[IRG] += b[B_RRACCSG] + b[B_RSACCRG];
   A[IRG] += b[B_RSMLTG];
@@ -1517,6 +1663,14 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
   A[IRG] += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
   A[IRG] += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
   A[IRG] -= b[B_RGMLTR];
+  if (x.tw) {                                                         /* OCND2 rows */
+    A[ITH] += b[B_RVDEPI] * lsfact;                                   /* :625 */
+    A[IRV] -= b[B_RVDEPI];                                            /* :630 */
+    A[IRI] += b[B_RVDEPI];                                            /* :673-674 */
+    A[IRI] -= b[B_RILARS];
+    A[IRS] += b[B_RVDEPG] * depg_s;                                   /* :677 */
+    A[IRS] += b[B_RILARS];                                            /* :691 */
+  }
   if (x.hail) {                                                       /* KRR = 7 rows */
     A[ITH] += (b[B_RRWETH] + b[B_RCWETH]) * lsv;                      /* :620-622 */
     A[ITH] += (b[B_RCDRYH] + b[B_RRDRYH]) * lsv;
@@ -1557,13 +1711,14 @@ typedef struct {
   double extpk[NVH];
   double cit, rainfr, rrevav;
   int outer, inner, capped;
-  int tie;    /* some pass took a growth-mode decision on rounding residuals */
+  int tie;    /* bit 0: some pass took a growth-mode decision on rounding
+               residuals; bit 1: the CIT reset followed an ice residual */
 } StepOut;
 
 static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
                                 double exn, double rhodref, double pres, double cf, double sigma_rc,
                                 double hlc_hcf, double hlc_hrc, double hli_hcf, double hli_hri,
-                                StepOut *s)
+                                StepOut *s, const Ocnd2Pt *oc)
 {
   const double rsmin[NVH] = {0.0, c->V_RTMIN, c->C_RTMIN, c->R_RTMIN, c->I_RTMIN, c->S_RTMIN, c->G_RTMIN,
                              c->H_RTMIN};
@@ -1600,7 +1755,7 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
       const double lvfact = (c->LVTT + (c->CPV - c->CL) * (zzt - c->TT)) / zdev;
       double A[NVH], B[NVH];
       ice4_tendencies(c, lut, lsoft, 1, exn, rhodref, lvfact, lsfact, pres, cf, sigma_rc, &s->cit, zzt,
-                      s->vart, &pr, &s->rainfr, hl, hi, A, B);
+                      s->vart, &pr, &s->rainfr, hl, hi, A, B, oc);
       s->tie |= pr.tie;
       pr.tie = 0;
       for (int v = 0; v < nv; ++v) A[v] += s->extpk[v];             /* :265-272 */
@@ -1620,7 +1775,13 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
         }
       }
       if (ztime + maxtime >= dt) llcompute = 0;                       /* :314-319 */
+      const double ri0 = s->vart[IRI];
       for (int v = 0; v < nv; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
+      /* the ice depleted to a rounding residual: whether CIT is reset below
+       * follows the last bits of the pass (a tie, as the growth choice) */
+      if (s->cit > 0. && (ri0 != 0. || B[IRI] != 0.) &&
+          fabs(s->vart[IRI]) <= 1e-12 * (fabs(ri0) + fabs(B[IRI]) + fabs(A[IRI] * maxtime)))
+        s->tie |= 2;
       if (s->vart[IRI] <= 0.) s->cit = 0.;                            /* :398-401 */
       ztime += maxtime;
       s->rrevav = pr.bu[B_RREVAV];
@@ -1693,10 +1854,11 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
   return ice3o_rain_ice_ties(c, lut, nij, nk, dt, opt, f, status_bits, NULL);
 }
 
-/* ice3o_rain_ice that also marks (tie[p] = 1, when tie is not NULL) the
- * points whose sub-stepping took a graupel or hail growth-mode decision on
- * rounding residuals: there the reference's own outcome depends on the last
- * bits of the collection rates. */
+/* ice3o_rain_ice that also marks (tie[p] != 0, when tie is not NULL) the
+ * points whose sub-stepping took a decision on rounding residuals (bit 0: a
+ * graupel or hail growth-mode choice; bit 1: the reset of CIT after a pass
+ * that depleted the ice to a residual); there the reference's own outcome
+ * depends on the last bits of the rates. */
 EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
                                const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
                                uint32_t *status_bits, uint8_t *tie)
@@ -1705,7 +1867,49 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
   if (!rain_ice_supported(c)) return ICE3GB_ERR_UNSUPPORTED;
   const int hail = (int)c->NRR == 7;
   if (hail && (!f->rht || !f->rhs || !f->inprh || (opt && opt->sed_jax > 0))) return ICE3GB_ERR_UNSUPPORTED;
+  const int ocnd2 = c->OCND2 != 0.0;
+  if (ocnd2 && (hail || (int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0 || !f->ssio || !f->ssiu ||
+                !f->ifr || !f->icldfr))
+    return ICE3GB_ERR_UNSUPPORTED;
   const long n = (long)nij * nk;
+  /* OCND2: TIWMX tables, level heights (rain_ice.F90:386-394: the sum of
+   * dzz from the last level IKTE down to the level, minus half its own
+   * thickness; with k = 0 at the surface (NKL = 1) IKTE is the top level) and
+   * the cloud droplet concentration (:396-435) */
+  double *tw = NULL, *zzz = NULL, *conc = NULL;
+  if (ocnd2) {
+    tw = (double *)malloc(sizeof(double) * TW_N * TIWMX_N);
+    zzz = (double *)malloc(sizeof(double) * 2 * n);
+    if (!tw || !zzz) { free(tw); free(zzz); return ICE3GB_ERR_RANGE; }
+    conc = zzz + n;
+    ice3o_tiwmx_all(c, tw);
+    const int st = f->sea != NULL && f->town != NULL;
+    for (long col = 0; col < nij; ++col) {
+      double zsum = 0.;
+      for (int k = nk - 1; k >= 0; --k) {
+        const long p = (long)k * nij + col;
+        zsum = zsum + f->dzz[p];
+        zzz[p] = zsum - f->dzz[p] * 0.5;
+      }
+      const double top = zzz[(long)(nk - 1) * nij + col];
+      for (int k = 0; k < nk; ++k) {
+        const long p = (long)k * nij + col;
+        double cc = c->CONC_LAND;
+        if (st && c->FRMIN26 < 0.001) {
+          const double tmp = f->sea[col] * c->CONC_SEA + (1. - f->sea[col]) * c->CONC_LAND;
+          cc = (1. - f->town[col]) * tmp + f->town[col] * c->CONC_URBAN;
+        }
+        if (c->FRMIN26 > 0.001) {
+          cc = c->FRMIN26 * f->pabs[p] / c->P00;
+          if (c->FRMIN22 > 0.001 && st) {
+            const double tmp = dmax(0., dmin(1., (zzz[p] - top) / (dmax(0.01, c->FRMIN29 - top))));
+            cc = cc * (c->FRMIN22 * (f->sea[col] * c->FRMIN30 + (1. - f->sea[col])) * (1. - tmp) + tmp);
+          }
+        }
+        conc[p] = cc;
+      }
+    }
+  }
   const int lsedim_after = (opt && opt->lsedim_after >= 0) ? opt->lsedim_after : (c->LSEDIM_AFTER != 0.0);
   const int ldeposc = (opt && opt->ldeposc >= 0) ? opt->ldeposc : (c->LDEPOSC != 0.0);
   const int max_passes = (opt && opt->max_passes > 0) ? opt->max_passes : 256;
@@ -1718,7 +1922,10 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
   double *lvf = (double *)malloc(sizeof(double) * n);
   double *rvheni = (double *)malloc(sizeof(double) * n);
   int64_t *key = (int64_t *)malloc(sizeof(int64_t) * n);
-  if (!lsf || !lvf || !rvheni || !key) { free(lsf); free(lvf); free(rvheni); free(key); return ICE3GB_ERR_RANGE; }
+  if (!lsf || !lvf || !rvheni || !key) {
+    free(lsf); free(lvf); free(rvheni); free(key); free(tw); free(zzz);
+    return ICE3GB_ERR_RANGE;
+  }
   int capped_any = 0;
 
   /* 2. sedimentation before the microphysics (rain_ice.F90:442-462 -> ICE4_SEDIMENTATION) */
@@ -1766,8 +1973,15 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
     lsf[p] = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
     lvf[p] = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
     /* :370-381 LLMICRO */
-    const int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN ||
-                      rg > c->G_RTMIN || (hail && rh > c->H_RTMIN);
+    int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN ||
+                rg > c->G_RTMIN || (hail && rh > c->H_RTMIN);
+    Ocnd2Pt oc;
+    if (ocnd2) {                                                      /* :347-363 */
+      const double m = c->FRMIN13;
+      micro = f->ssio[p] > c->FRMIN12 || rc > m || rr > m || ri > m || rs > m || rg > m;
+      oc.tw = tw; oc.ssio = f->ssio[p]; oc.ssiu = f->ssiu[p]; oc.ifr = f->ifr[p]; oc.icldfr = f->icldfr[p];
+      oc.zzz = zzz[p]; oc.conc = conc[p];
+    }
     f->evap3d[p] = 0.0;
     if (!llrfr) f->rainfr[p] = 1.0;  /* :603-605 */
     double cit = f->cit[p];
@@ -1775,7 +1989,8 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
     if (!micro) {
       /* :506-529 nucleation outside LLMICRO points */
       cit = 0.0;
-      ice4_nucleation(c, 1, th, pres, rho, exn, lsf[p] / exn, t, rv, &cit, &zrvheni, NULL);
+      ice4_nucleation(c, 1, th, pres, rho, exn, lsf[p] / exn, t, rv, &cit, &zrvheni, NULL, ocnd2 ? tw : NULL,
+                      ocnd2 ? oc.zzz : 0.0, ocnd2 ? oc.icldfr : 0.0);
     }
     /* :535-539 */
     zrvheni = dmin(f->rvs[p], zrvheni / dt);
@@ -1796,7 +2011,7 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
       const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
       const double sigma_rc = sigm ? 2.0 * f->sigs[p] : 0.0;  /* pack :266 + stepping :160-166 */
       ice4_stepping_point(c, lut, dt, max_passes, exn, rho, pres, f->cldfr[p], sigma_rc,
-                          f->hlc_hcf[p], f->hlc_hrc[p], f->hli_hcf[p], f->hli_hri[p], &s);
+                          f->hlc_hcf[p], f->hlc_hrc[p], f->hli_hcf[p], f->hli_hri[p], &s, ocnd2 ? &oc : NULL);
       cit = s.cit;
       if (c->LWARM != 0.0) f->evap3d[p] = s.rrevav;
       f->rainfr[p] = s.rainfr;
@@ -1874,7 +2089,7 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
       f->indep[col] = 0.0;
     }
   }
-  free(lsf); free(lvf); free(rvheni); free(key);
+  free(lsf); free(lvf); free(rvheni); free(key); free(tw); free(zzz);
   if (status_bits) *status_bits = (capped_any ? ICE3GB_DEV_PASS_CAP : 0u) | (sed_capped ? ICE3GB_DEV_SED_CAP : 0u);
   return ICE3GB_OK;
 }
@@ -1889,7 +2104,7 @@ EXPORT void ice3o_nucleation(const C *c, long n, const double *tht, const double
 {
   for (long p = 0; p < n; ++p)
     ice4_nucleation(c, ldcompute[p], tht[p], pabst[p], rhodref[p], exn[p], lsfact[p], t[p], rvt[p], &cit[p],
-                    &rvheni_mr[p], NULL);
+                    &rvheni_mr[p], NULL, NULL, 0.0, 0.0);
 }
 
 EXPORT void ice3o_rrhong_rimltc(const C *c, long n, const double *t, const double *exn, const double *lvfact,
@@ -2008,6 +2223,40 @@ EXPORT void ice3o_rainfr_vert(const C *c, int nij, int nk, double *prfr, const d
 
 EXPORT int ice3o_budget_count(void) { return NBU; }
 
+/* The OCND2 pieces of ICE4_TENDENCIES on n points, hard pass, LDCOMPUTE:
+ * in = [t, rhodref, pres, rv, rc, rr, ri, rs, rg, cit, ssio, ssiu, ifr,
+ * icldfr, zzz, conc] per point (n x 16); out = [cit after the nucleation,
+ * es_i, ssi, ai, colf, acrf, rilars, rvdepi] per point (n x 8), with ssi and
+ * ai those after the tabulated derived fields (in = state after the
+ * instantaneous processes, exn = 1). */
+EXPORT void ice3o_ocnd2_rates(const C *c, long n, const double *in, double *out)
+{
+  double *tw = (double *)malloc(sizeof(double) * TW_N * TIWMX_N);
+  if (!tw) return;
+  ice3o_tiwmx_all(c, tw);
+  for (long p = 0; p < n; ++p) {
+    const double *x = in + p * 16;
+    Ocnd2Pt oc = {tw, x[10], x[11], x[12], x[13], x[14], x[15]};
+    double cit = x[9], rvheni;
+    ice4_nucleation(c, 1, x[0], x[2], x[1], 1.0, 1.0, x[0], x[3], &cit, &rvheni, NULL, tw, oc.zzz, oc.icldfr);
+    Tctx t;
+    memset(&t, 0, sizeof(t));
+    t.c = c; t.ldsoft = 0; t.ldcompute = 1; t.t = x[0]; t.rhodref = x[1]; t.pres = x[2];
+    t.v[IRV] = x[3]; t.v[IRC] = x[4]; t.v[IRR] = x[5]; t.v[IRI] = x[6]; t.v[IRS] = x[7]; t.v[IRG] = x[8];
+    t.tw = tw; t.ssio = oc.ssio; t.ssiu = oc.ssiu; t.ifr = oc.ifr; t.icldfr = oc.icldfr; t.zzz = oc.zzz;
+    t.conc = oc.conc;
+    PointRates pr;
+    memset(&pr, 0, sizeof(pr));
+    ice4_derived(c, t.t, t.rhodref, t.pres, t.v[IRV], &pr.ssi, &pr.ka, &pr.dv, &pr.ai, &pr.cj);
+    ocnd2_derived(&t, &pr);
+    ice4_fast_ri_rs(&t, &pr, cit);
+    double *o = out + p * 8;
+    o[0] = cit; o[1] = pr.esi; o[2] = pr.ssi; o[3] = pr.ai; o[4] = pr.colf; o[5] = pr.acrf;
+    o[6] = pr.bu[B_RILARS]; o[7] = pr.bu[B_RVDEPI];
+  }
+  free(tw);
+}
+
 /* ICE4_FAST_RH alone on n points (hard pass, LDCOMPUTE): in = [t, rhodref,
  * pres, rv, rc, rr, ri, rs, rg, rh] per point (n x 10), ldwetg per point;
  * out = the 10 persistent tendencies PRH_TEND then the 14 hail budget terms
@@ -2107,7 +2356,7 @@ EXPORT int ice3o_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
   s.rainfr = 1.0;
   const int sigm = (int)c->SUBG_AUCV_RC == 1 && (int)c->SUBG_PR_PDF == 0;
   ice4_stepping_point(c, lut, dt, max_passes, in[0], in[1], in[2], in[18], sigm ? 2.0 * in[19] : 0.0,
-                      0.0, 0.0, 0.0, 0.0, &s);
+                      0.0, 0.0, 0.0, 0.0, &s, NULL);
   for (int v = 0; v < NV; ++v) out[v] = s.vart[v];
   out[7] = s.cit; out[8] = s.rrevav; out[9] = s.capped;
   *outer = s.outer; *inner = s.inner;

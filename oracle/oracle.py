@@ -42,7 +42,9 @@ NBU_NAMES = ("rvheni_mr", "rrhong_mr", "rimltc_mr", "rsrimcg_mr", "rchoni", "rvd
              "rswetg", "rcdryg", "ridryg", "rrdryg", "rsdryg", "rgmltr", "rcberi",
              # hail (KRR = 7)
              "rwetgh", "rwetgh_mr", "rcweth", "riweth", "rsweth", "rgweth", "rrweth", "rcdryh", "ridryh",
-             "rsdryh", "rrdryh", "rgdryh", "rdryhg", "rhmltr")
+             "rsdryh", "rrdryh", "rgdryh", "rdryhg", "rhmltr",
+             # OCND2 (ICE4_FAST_RI_RS)
+             "rvdepi", "rilars")
 RS_NAMES = ("rcrims", "rcrimss", "rsrimcg", "rraccs", "rraccss", "rsaccrg", "freez1", "freez2")
 RG_NAMES = ("rcdryg", "ridryg", "riwetg", "rsdryg", "rswetg", "rrdryg", "freez1", "freez2")
 
@@ -181,6 +183,11 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
     out = {k: _f64(st[k]).copy() for k in RI_INOUT}
     out.update({k: np.empty((nk, nij)) for k in RI_OUT3})
     out.update({k: np.empty(nij) for k in RI_OUT2})
+    if table.values["OCND2"] != 0.0:
+        # OCND2: the ice_adjust OCND2 outputs of the same state
+        for k in ("ssio", "ssiu", "ifr", "icldfr"):
+            keep[k] = _f64(st[k])
+            setattr(f, k, _ptr(keep[k]))
     hail = table.values["NRR"] == 7.0
     if hail:
         # hail (KRR = 7): mixing ratio at t, in-out source, precipitation

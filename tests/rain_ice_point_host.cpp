@@ -1,5 +1,7 @@
 // Host build of the rain_ice kernel's per-point code (the same
 // rain_ice_point() the device runs), exported for tests/test_rain_ice_host.py.
+#include <vector>
+
 #include "../dwarf-p-ice3_gb300/csrc/rain_ice_point.cuh"
 
 extern "C" int rain_ice_points_host(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk, double dt,
@@ -54,6 +56,29 @@ extern "C" int rain_ice_points_host_hail(const Ice3gbConstants *c, const Ice3gbL
     bool capped;
     keys[p] = subg ? ice3pt::rain_ice_point<false, true, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt)
                    : ice3pt::rain_ice_point<false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt);
+    capped_any |= capped;
+  }
+  return capped_any;
+}
+
+// With OCND2 (the kernel's O instantiation): the column heights and droplet
+// concentrations first (ocnd2_column), then the points; tw = the six TIWMX
+// tables (ice3o_tiwmx_all layout).
+extern "C" int rain_ice_points_host_ocnd2(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk,
+                                          double dt, int max_passes, const Ice3gbRainIceFields *f, const double *tw,
+                                          unsigned int *keys)
+{
+  ice3pt::Derived d;
+  ice3pt::make_derived(*c, d);
+  const double *lt = reinterpret_cast<const double *>(luts);
+  const long n = (long)nij * nk;
+  std::vector<double> ocs(2 * (size_t)n);
+  for (long col = 0; col < nij; ++col) ice3pt::ocnd2_column(*c, *f, nij, nk, col, ocs.data(), ocs.data() + n);
+  int capped_any = 0;
+  for (long p = 0; p < n; ++p) {
+    bool capped;
+    keys[p] = ice3pt::rain_ice_point<false, false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt,
+                                                                tw, ocs.data(), ocs.data() + n);
     capped_any |= capped;
   }
   return capped_any;

@@ -10,11 +10,12 @@ REF_SRC = "/root/reference/src"
 
 
 def test_snapshot_has_every_constant():
-    from ice3gb.constants import _hail_constants
+    from ice3gb.constants import _frmin_constants, _hail_constants
     ext = load_snapshot()
     # OCND2 has a default; the hail constants come from INI_RAIN_ICE's
-    # formulas, which the reference's Python initialisation leaves out
-    hail = _hail_constants(ext)
+    # formulas, which the reference's Python initialisation leaves out, and
+    # XFRMIN from the Fortran namelist defaults
+    hail = {**_hail_constants(ext), **_frmin_constants()}
     missing = [n for n in CONSTANT_NAMES if n not in ext and n != "OCND2" and n not in hail]
     assert not missing
     assert all(np.isfinite(v) for v in hail.values())

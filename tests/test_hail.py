@@ -232,24 +232,32 @@ def _fields(x, nk, nij):
 
 
 def _untie(spread, tie, max_share=0.02):
-    """Points where the oracle took a graupel or hail growth-mode decision on
-    rounding residuals (ice3o_rain_ice_ties: the wet-growth estimate minus
-    what it collects, a difference of several non-zero rates that is zero
-    up to rounding, against the dry-growth one), and the levels below them,
-    where the sedimentation carries their outcome, get an unbounded
-    allowance; the surface fields of their columns too.  They must stay a
-    small share of the grid."""
+    """Points where the oracle took a decision on rounding residuals
+    (ice3o_rain_ice_ties) get an unbounded allowance.  Bit 0, a graupel or
+    hail growth-mode choice (the wet-growth estimate minus what it collects,
+    a difference of several non-zero rates that is zero up to rounding,
+    against the dry-growth one): the point and the levels below it, where the
+    sedimentation carries its outcome, for every field, and the surface
+    fields of its column.  Bit 1, the reset of the ice concentration after a
+    pass that left the ice at a rounding residual: cit at the point.  They
+    must stay a small share of the grid."""
     nk = tie.shape[0]
-    below = np.flip(np.maximum.accumulate(np.flip(tie != 0, axis=0), axis=0), axis=0)   # tie at or above k
+    growth = (tie & 1) != 0
+    below = np.flip(np.maximum.accumulate(np.flip(growth, axis=0), axis=0), axis=0)   # tie at or above k
     cols = below[0]
+    cit_tie = (tie & 2) != 0
     assert below.mean() <= max_share, f"{below.mean():.2%} of the points lie at or below a growth-mode tie"
+    # ice sublimating to zero within a pass is common (OCND2 states: up to a
+    # fifth of the points); only cit is exempted there
+    assert cit_tie.mean() <= 0.3, f"{cit_tie.mean():.2%} of the points reset cit on an ice residual"
     out, share = {}, {}
     for k, v in spread.items():
         v = np.array(v, dtype=np.float64)
         share[k] = 0.0
         if v.ndim == 2 and v.shape[0] == nk:
-            v[below] = np.inf
-            share[k] = float(below.mean())
+            m = below | cit_tie if k == "cit" else below
+            v[m] = np.inf
+            share[k] = float(m.mean())
         elif v.ndim == 1 and v.shape[0] == cols.shape[0]:
             v[cols] = np.inf
             share[k] = float(cols.mean())

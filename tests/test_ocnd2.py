@@ -12,6 +12,7 @@ points.  Then the device code's host build (CPU) and the device kernel
 against the oracle."""
 import ctypes
 import math
+import os
 
 import numpy as np
 import pytest
@@ -290,3 +291,239 @@ def test_device_rejects_ocnd2_without_levels():
         ia(**{k: dev[k] for k in H.IN}, timestep=DT, zz=dev["zz"], ice_cld_wgt=dev["ice_cld_wgt"])
     with pytest.raises(ValueError, match="zz"):
         ia(**{k: dev[k] for k in H.IN}, timestep=DT)
+
+
+# ---------------------------------------------------------------------------- OCND2 in rain_ice: pins
+
+def _tiwmx_fun(v, tt):
+    """The TIWMX table entry at NINT(100 T) (mode_tiwmx.F90) of the functions of
+    mode_tiwmx_fun.F90 as INI_TIWMX fills them."""
+    j = min(max(int(math.floor(abs(100.0 * tt) + 0.5)), 13200), 37316)
+    T = j / 100.0
+    TT = v["TT"]
+    esw = math.exp(v["ALPW"] - v["BETAW"] / T - v["GAMW"] * math.log(T))
+    esi_f = esw if T >= TT else math.exp(v["ALPI"] - v["BETAI"] / T - v["GAMI"] * math.log(T))   # ESATI, SIGN(0.5, 0) = 0.5
+    estabi = esw if T > 273.15 else esi_f
+    a2 = (v["LSTT"] + (v["CPV"] - v["CI"]) * (T - TT)) ** 2 / (2.38E-2 + 0.0071E-2 * (T - TT)) / (T ** 2 * v["RV"])
+    bb3 = v["RV"] / (0.211E-4 * (T / TT) ** 1.94 * v["P00"]) * T / esi_f
+    am3 = 0.0 if T > 273.15 else 1000. * math.exp(12.96 * (esw / esi_f - 1.) - 0.639)
+    zzt = max(0., min(1., (TT - T) / 20.))
+    redin = 1. - (1. - zzt) / (zzt ** 3 + (1. - zzt) ** 3) ** .333
+    return dict(esi=estabi, a2=a2, bb3=bb3, am3=am3, redin=redin)
+
+
+def ocnd2_rates_py(v, x):
+    """ICE4_NUCLEATION's OCND2 branch (ice4_nucleation.func.h:127-136), the
+    tabulated derived fields and collision factors (mode_ice4_tendencies.F90:
+    303-346, LLTAB, LLCOL) and ICE4_FAST_RI_RS (mode_ice4_fast_ri_rs.F90,
+    LMODICEDEP = .FALSE.) for one point, written from the Fortran text."""
+    t, rho, p, rv, rc, rr, ri, rs, rg, cit, ssio, ssiu, ifr, icldfr, zzz, conc = x
+    TT = v["TT"]
+    if t < TT and rv > v["V_RTMIN"]:
+        zzw = _tiwmx_fun(v, t)["redin"] * max(0.1, ((20000. - min(20000., zzz)) / 20000.) ** 4) \
+            * _tiwmx_fun(v, max(v["FRMIN27"], t))["am3"] * (0.0001 + 0.9999 * icldfr)
+        zzw = min(zzw, 50.E3)
+        cit = max(zzw + cit, cit)
+    tab = _tiwmx_fun(v, t)
+    esi = tab["esi"]
+    ssi = rv * (p - esi) / (v["EPSILO"] * esi) - 1.0
+    ai = tab["a2"] + tab["bb3"] * p
+    zconc = conc * 0.000001
+    colf = acrf = 0.00001
+    if rc > 1.0E-10:
+        rcw = 0.1 * (0.75 * rc * rho / (v["PI"] * zconc)) ** 0.333
+        vt = 1.19E6 * rcw ** 2 if rcw < 0.0065 else 8000. * rcw
+        vt = min(10., vt)
+        st = max(0.01, 2. * (100. - vt) * vt / (v["GRAVITY0"] * 10.))
+        if st > 0.1:
+            colf = max(0.01, min(1., 0.939 * st ** 2.657))
+        if rr > 1.0E-10 and rcw > 1.0E-5:
+            r20 = math.exp(rcw * 2000.)
+            acrf = (r20 - 1.) / (r20 + 1.)
+    timesc, dicrit = v["FRMIN14"], v["FRMIN15"]
+    rilars = 0.
+    if ri > 0.0 and ssi > 0.001:
+        rilars = min(ri, ri / (87.5 * dicrit ** 2 * ai / ssi))
+    rvdepi = 0.
+    w2d = 1. / (ifr * icldfr + 1. - icldfr)
+    if (p * 0.5 - esi) > 0. and cit > 0.:
+        xw2d13 = ifr ** 0.333
+        wcitred23 = 0.1 ** 0.667
+        tc = max(-18., min(-1., t - TT))
+        hu = min(0.15, max(0., ssi))
+        cryssha = 1.1 + 3. * hu * (1. + math.sin(0.64 * tc - 1.3))
+        qimax = 366.5 * dicrit ** 3 * cit * 0.1 / rho
+        ci2s = 0.
+        if ri > 1.0e-12 and timesc > 0.:
+            ci2s = ri * (1. - min(1., 0.5 * qimax / ri)) * (1. - icldfr) * w2d / (timesc * 0.5)
+        zzwc = cryssha * 0.878 / ai * (cit / rho) ** 0.667 * (max(v["I_RTMIN"], ri) * w2d) ** 0.333
+        if ssio > 0. and icldfr > 0.02:
+            rvdepi += zzwc * xw2d13 * ssio * icldfr
+        if ssiu < 0. and icldfr < 0.98:
+            rilars += ci2s
+            rvdepi += zzwc * wcitred23 * ssiu * (1. - icldfr)
+    return [cit, esi, ssi, ai, colf, acrf, rilars, rvdepi]
+
+
+def test_oracle_ocnd2_rain_ice_pieces_match_python_restatement():
+    import oracle
+    from ice3gb.constants import build_table
+    t = build_table(table="phyex", overrides={"OCND2": 1.0})
+    v = {k: float(x) for k, x in t.values.items()}
+    rng = np.random.default_rng(9)
+    n = 500
+    T = rng.uniform(225.0, 285.0, n)
+    rho = rng.uniform(0.3, 1.2, n)
+    p = rho * 287.0 * T
+    mix = lambda pz: np.exp(rng.uniform(np.log(1e-9), np.log(3e-3), n)) * (rng.uniform(size=n) > pz)  # noqa: E731
+    rv = rng.uniform(0.5, 1.2, n) * 0.622 * 611.0 * np.exp(17.5 * (T - 273.15) / (T - 36.0)) / p
+    x = np.stack([T, rho, p, rv, mix(0.3), mix(0.3), mix(0.3), mix(0.3), mix(0.3),
+                  rng.uniform(0, 2e4, n) * (rng.uniform(size=n) > 0.3),        # cit
+                  rng.uniform(-0.3, 0.2, n), rng.uniform(-0.5, 0.0, n), np.full(n, 10.0),   # ssio, ssiu, ifr
+                  rng.uniform(0, 1, n) * (rng.uniform(size=n) > 0.2),          # icldfr
+                  rng.uniform(0, 25000.0, n), rng.choice([1e8, 3e8, 5e8], n)], axis=1)   # zzz, conc
+    out = np.empty((n, 8))
+    lib = oracle.load()
+    lib.ice3o_ocnd2_rates(ctypes.byref(t.consts), ctypes.c_long(n), np.ascontiguousarray(x).ctypes.data_as(
+        ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p))
+    active = np.zeros(8, dtype=int)
+    for i in range(n):
+        ref = np.array(ocnd2_rates_py(v, tuple(x[i])))
+        np.testing.assert_allclose(out[i], ref, rtol=1e-12, atol=1e-300, err_msg=f"point {i}")
+        active += (ref != 0.0) & (ref != x[i, 9])
+    assert np.all(active[[0, 4, 5, 6, 7]] > 10), active
+
+
+# ---------------------------------------------------------------------------- OCND2 in rain_ice: host build, device
+
+def ocnd2_rain_ice_state(nij, seed):
+    """A rain_ice state (ABI names) with the OCND2 ice_adjust outputs of the
+    same atmosphere (ssio, ssiu, ifr, icldfr)."""
+    import oracle
+    from ice3gb.constants import build_table
+    from ice3gb.state import make_state
+    from test_gpu_rain_ice import _abi_rain_ice_state
+    st = {k: v.numpy() for k, v in make_state(nij, 90, seed=seed, precip=True).items()}
+    x = _abi_rain_ice_state(st)
+    ia = _state(nij, seed)
+    oa = oracle.ice_adjust(build_table(table="jax", overrides={"OCND2": 1.0}), ia, DT)
+    for k in ("ssio", "ssiu", "ifr", "icldfr"):
+        x[k] = oa[k]
+    return x
+
+
+def _ri_table(**kw):
+    from ice3gb.constants import build_table
+    return build_table(table="phyex", overrides={"OCND2": 1.0, **kw})
+
+
+RI_OUT = ("ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "cit", "inprc", "inprr", "inpri", "inprs", "inprg")
+
+
+def _ri_scale(x, ref, fl, k):
+    rhodz = x["rhodref"] * x["dzz"]
+    s = np.abs(x[k]) + np.abs(ref[k])
+    key = {"rcs": "c", "rrs": "r", "ris": "i", "rss": "s", "rgs": "g"}.get(k)
+    if key:
+        f_ = fl["fpr_" + key]
+        fa = np.concatenate([f_[1:], np.zeros_like(f_[:1])], axis=0)
+        s = s + (np.abs(f_) + np.abs(fa)) / rhodz
+    return s
+
+
+def test_ocnd2_rain_ice_host_build_matches_oracle():
+    import oracle
+    import subprocess
+    from ice3gb import _abi
+    from test_hail import _untie
+    d = os.path.dirname(os.path.abspath(__file__))
+    libs = {}
+    for name in ("rain_ice_point_host", "sedimentation_host"):
+        out = f"/tmp/ocnd2_{name}_{os.getpid()}.so"
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I",
+                        os.path.join(d, "..", "include"), os.path.join(d, f"{name}.cpp"), "-o", out], check=True)
+        libs[name] = ctypes.CDLL(out)
+    t = _ri_table(LSEDIM_AFTER=1.0, LDEPOSC=0.0)
+    nij, nk = 24 * 24, 90
+    x = ocnd2_rain_ice_state(nij, seed=3)
+    keep, f = {}, _abi.RainIceFields()
+    for k in ("exn", "dzz", "rhodref", "exnref", "pabs", "cldfr", "sigs", "tht", "rvt", "rct", "rrt", "rit", "rst",
+              "rgt", "sea", "town", "ssio", "ssiu", "ifr", "icldfr"):
+        keep[k] = np.ascontiguousarray(x[k], dtype=np.float64)
+        setattr(f, k, keep[k].ctypes.data)
+    for k in ("cit", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs"):
+        keep[k] = np.array(x[k], dtype=np.float64)
+        setattr(f, k, keep[k].ctypes.data)
+    for k in ("evap3d", "rainfr"):
+        keep[k] = np.zeros((nk, nij))
+        setattr(f, k, keep[k].ctypes.data)
+    for k in ("inprc", "inprr", "inpri", "inprs", "inprg"):
+        keep[k] = np.zeros(nij)
+        setattr(f, k, keep[k].ctypes.data)
+    lib = oracle.load()
+    tw = np.empty(6 * 24117)
+    lib.ice3o_tiwmx_all(ctypes.byref(t.consts), tw.ctypes.data_as(ctypes.c_void_p))
+    keys = np.zeros(nij * nk, dtype=np.uint32)
+    capped = libs["rain_ice_point_host"].rain_ice_points_host_ocnd2(
+        ctypes.byref(t.consts), ctypes.byref(t.luts), nij, nk, ctypes.c_double(DT), 256, ctypes.byref(f),
+        tw.ctypes.data_as(ctypes.c_void_p), keys.ctypes.data_as(ctypes.c_void_p))
+    assert capped == 0
+    libs["sedimentation_host"].sed_stat_rain_ice_host(ctypes.byref(t.consts), nij, nk, ctypes.c_double(DT),
+                                                      ctypes.byref(f))
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
+    spread, share = _untie(spread, fl["tie"])
+    for k in RI_OUT:
+        sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
+        assert_parity(keep[k], ref[k], spread[k], f"ocnd2 host/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+
+
+@pytest.mark.parametrize("sedim", [1.0, 0.0])
+def test_ocnd2_rain_ice_water_budget(sedim):
+    import oracle
+    t = _ri_table(SEDIM=sedim)
+    nij, nk = 16 * 16, 90
+    x = ocnd2_rain_ice_state(nij, seed=4)
+    out, bits = oracle.rain_ice(t, x, DT)
+    assert bits == 0
+    rhodz = x["rhodref"] * x["dzz"]
+    src = ("rvs", "rcs", "rrs", "ris", "rss", "rgs")
+    d = sum(out[k] - x[k] for k in src)
+    col = (rhodz * d).sum(axis=0) * DT
+    precip = sum(out[k] for k in ("inprc", "inprr", "inpri", "inprs", "inprg")) * t.values["RHOLW"] * DT
+    scale = (rhodz * sum(np.abs(x[k]) for k in src)).sum(axis=0) * DT
+    assert np.abs(col + precip).max() <= 1e-12 * scale.max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("after", [False, True])
+def test_ocnd2_rain_ice_device_matches_oracle(after):
+    import oracle
+    import torch
+    from ice3gb import RainIce
+    from test_hail import _untie
+    t = _ri_table()
+    nij = 32 * 32
+    x = ocnd2_rain_ice_state(nij, seed=5)
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT, lsedim_after=int(after))[0], x, rel=1e-12,
+                              trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, lsedim_after=int(after), with_fpr=True, with_ties=True)
+    spread, share = _untie(spread, fl["tie"])
+    ri = RainIce()
+    ri.table = t
+    m = {"exn": "exn", "dzz": "dzz", "rhodref": "rhodref", "exnref": "exnref", "pres": "pabs", "cldfr": "cldfr",
+         "sigs": "sigs", "th_t": "tht", "rv_t": "rvt", "rc_t": "rct", "rr_t": "rrt", "ri_t": "rit", "rs_t": "rst",
+         "rg_t": "rgt", "ci_t": "cit", "hlc_hrc": "hlc_hrc", "hlc_hcf": "hlc_hcf", "hli_hri": "hli_hri",
+         "hli_hcf": "hli_hcf", "ths": "ths", "rvs": "rvs", "rcs": "rcs", "rrs": "rrs", "ris": "ris", "rss": "rss",
+         "rgs": "rgs", "sea": "sea", "town": "town", "ssio": "ssio", "ssiu": "ssiu", "ifr": "ifr", "icldfr": "icldfr"}
+    state = {k: torch.as_tensor(np.ascontiguousarray(x[v])).cuda() for k, v in m.items()}
+    new, diag = ri(state, DT, lsedim_after=after)
+    got = {"cit": new["ci_t"].cpu().numpy()}
+    for k in ("ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs"):
+        got[k] = new[k].cpu().numpy()
+    for k in ("inprc", "inprr", "inpri", "inprs", "inprg"):
+        got[k] = diag[k].cpu().numpy()
+    for k in RI_OUT:
+        sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
+        assert_parity(got[k], ref[k], spread[k], f"ocnd2 device/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+    assert ri.device_status() == 0

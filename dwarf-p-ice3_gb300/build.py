@@ -22,8 +22,8 @@ LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(LIB_DIR, "libice3gb.so")
 INCLUDE = os.path.normpath(os.path.join(HERE, "..", "include"))
-SOURCES = ["ice_adjust.cu", "ice_adjust_vjp.cu", "sedimentation.cu", "sedimentation_vjp.cu", "rain_ice.cu", "mlp.cu",
-           "surrogate.cu", "surrogate_rain_ice.cu", "abi.cu", "rain_ice_noalloc.cu"]
+SOURCES = ["ice_adjust.cu", "ice_adjust_vjp.cu", "sedimentation.cu", "sedimentation_vjp.cu", "rain_ice.cu",
+           "rain_ice_ts.cu", "mlp.cu", "surrogate.cu", "surrogate_rain_ice.cu", "abi.cu", "rain_ice_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

@@ -251,6 +251,8 @@ int check_surrogate(Handle *h, const SurCall &sur, long n)
     return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained with SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE only");
   if ((int)h->c.NRR != 6) return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained for NRR = 6 (no hail)");
   if (h->c.OCND2 != 0.0) return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: trained without OCND2");
+  if (h->c.MRSTEP != 0.0 || h->c.TSTEP_TS != 0.0)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "surrogate: no MRSTEP / TSTEP_TS time splitting");
   if (n > 2147483647L) return fail(h, ICE3GB_ERR_RANGE, "surrogate: at most 2^31 - 1 points per call");
   return ICE3GB_OK;
 }
@@ -832,8 +834,8 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   char why[256] = "";
   if ((int)c->NRR != 6 && (int)c->NRR != 7)
     snprintf(why, sizeof(why), "rain_ice supports NRR = 6 or 7 (hail), got %g", c->NRR);
-  else if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)
-    snprintf(why, sizeof(why), "rain_ice: MRSTEP/TSTEP_TS time-splitting is not supported");
+  else if (c->OCND2 != 0.0 && (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0))
+    snprintf(why, sizeof(why), "rain_ice: OCND2 with the MRSTEP / TSTEP_TS time splitting is not supported");
   else if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1)
     snprintf(why, sizeof(why), "rain_ice: SEDIM must be SPLI (0) or STAT (1), got %g", c->SEDIM);
   else if (((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) ||

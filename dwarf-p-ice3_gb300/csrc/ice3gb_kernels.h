@@ -184,6 +184,7 @@ size_t rain_ice_smem_bytes();
 
 cudaError_t launch_sedimentation_split(const Ice3gbConstants &c, const SplitArgs &a, cudaStream_t s);
 // Precipitation fraction of a rain_ice call with a PRFR option (before the point kernel).
+cudaError_t launch_rain_ice_points_ts(const Ice3gbConstants &c, const RainIceArgs &a, int num_sms, cudaStream_t s);
 cudaError_t launch_rain_ice_ocnd2_columns(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_rain_ice_prfr(const Ice3gbConstants &c, const RainIceArgs &a, cudaStream_t s);
 cudaError_t launch_surrogate_sample(const Ice3gbConstants &c, const SurSampleArgs &a, int num_sms, cudaStream_t s);

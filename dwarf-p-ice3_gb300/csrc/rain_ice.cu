@@ -30,65 +30,12 @@
 //    a second small kernel.
 #include "ice3gb_device.cuh"
 #include "ice3gb_kernels.h"
-#include "rain_ice_point.cuh"
-
-// Resident blocks of rain_ice_points_kernel per SM (2 x 256 threads: 128
-// registers per thread, two copies of the 78.7 KB lookup tables per SM).
-#ifndef RI_BLOCKS_PER_SM
-#define RI_BLOCKS_PER_SM 2
-#endif
+#include "rain_ice_kernel.cuh"
 
 namespace {
 using namespace ice3pt;
+using namespace ice3ri;
 
-__device__ __forceinline__ void warp_key_max(unsigned int *key_max, unsigned int key)
-{
-  const unsigned int m = __reduce_max_sync(0xffffffffu, key);
-  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(key_max, m);
-}
-
-// SUBG: the subgrid warm-process options (SUBG_RC_RR_ACCR / SUBG_RR_EVAP
-// other than NONE); the NONE instantiation carries none of their code.
-// H: hail (NRR = 7), the hail kernels read from the global copy of the tables.
-// O: OCND2 (NRR = 6, warm options NONE), with a.tw and the column fields a.ocs.
-template <bool SUBG, bool H = false, bool O = false>
-__global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_kernel(const __grid_constant__ Cst c,
-                                                                         const __grid_constant__ RainIceArgs a)
-{
-  extern __shared__ double lut[];
-  __shared__ Derived dsh;
-  for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
-  if (threadIdx.x == 0) make_derived(c, dsh);
-  __shared__ unsigned int chunk;
-  __syncthreads();
-  const Ice3gbRainIceFields &f = a.f;
-  const long n = (long)a.nij * a.nk;
-  const double dt = a.dt;
-  bool any_capped = false;
-  for (;;) {
-    if (threadIdx.x == 0) chunk = atomicAdd(a.scr.chunk_counter, 1u);
-    __syncthreads();
-    const long base = (long)chunk * blockDim.x;
-    __syncthreads();
-    if (base >= n) break;
-    const long slot = base + threadIdx.x;
-    unsigned int key = 0u;
-    if (slot < n) {
-      const long p = a.order ? (long)__ldg(a.order + slot) : slot;
-      bool capped;
-      key = O ? rain_ice_point<false, false, false, true>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr,
-                                                          a.luts, a.tw, a.ocs, a.ocs + n)
-              : rain_ice_point<false, SUBG, H>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr, a.luts);
-      any_capped |= capped;
-      a.scr.keys[p] = key;
-    }
-    warp_key_max(a.scr.key_max, key);
-  }
-  if (any_capped) atomicOr(a.scr.status, ICE3GB_DEV_PASS_CAP);
-}
-
-// The precipitation fraction of a call with a PRFR option, one thread per
-// column (prfr_column); runs before the point kernel, which starts from it.
 // OCND2: level heights and droplet concentrations, one thread per column.
 __global__ void rain_ice_ocnd2_column_kernel(const __grid_constant__ Cst c, const __grid_constant__ RainIceArgs a)
 {
@@ -183,6 +130,7 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
 {
   const bool subg = (int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0;
   const bool hail = (int)c.NRR == 7;
+  if (c.MRSTEP != 0.0 || c.TSTEP_TS != 0.0) return launch_rain_ice_points_ts(c, a, num_sms, s);
   void (*kern)(const Cst, const RainIceArgs) =
       c.OCND2 != 0.0 ? rain_ice_points_kernel<false, false, true>
       : hail ? (subg ? rain_ice_points_kernel<true, true> : rain_ice_points_kernel<false, true>)

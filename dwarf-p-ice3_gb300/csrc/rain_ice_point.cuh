@@ -1064,7 +1064,11 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
 // Returns the pass key (outer << 16 | inner-of-last-outer), 0 if capped.
-template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
+// TS: the MRSTEP / TSTEP_TS time splitting (mode_ice4_stepping.F90:191-197,
+// :387-453): per outer iteration (IITER) the state and time at its start; a
+// pass ends early when the TSTEP_TS sub-step is used up or a mixing ratio has
+// moved by MRSTEP since the start, for the first INB_ITER_MAX iterations.
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false, bool TS = false>
 ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__restrict__ lut, const PointFix &pf,
                               double dt, int max_passes, double *vart, const double *ext, double &cit,
                               double &rainfr, double &rrevav, double hl[4], double hi[4], bool &capped,
@@ -1072,6 +1076,18 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
                               const OcndPt *op = nullptr)
 {
   OcndRates OR{0.0, 1.0, 1.0, 0.0, 0.0};
+  int nb_iter_max = 0;
+  double ztstep = 0.0, tlast = 0.0;
+  double z0rt[H ? NVH : NV];
+  if (TS) {
+    nb_iter_max = (int)c.NMAXITER_MICRO;
+    if (c.TSTEP_TS != 0.0) {
+      int nb = (int)(dt / c.TSTEP_TS);
+      nb = nb > 1 ? nb : 1;
+      ztstep = dt / nb;
+      nb_iter_max = nb_iter_max > nb ? nb_iter_max : nb;
+    }
+  }
   constexpr int NVT = H ? NVH : NV;
   const double rsmin[NVH] = {0.0, c.V_RTMIN, c.C_RTMIN, c.R_RTMIN, c.I_RTMIN, c.S_RTMIN, c.G_RTMIN, c.H_RTMIN};
   HailRates HR;
@@ -1101,6 +1117,11 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
     ++outer;
     inner = 0;
     bool llcompute = true, soft = false;
+    if (TS) {
+      tlast = ztime;
+#pragma unroll
+      for (int v = 0; v < (H ? NVH : NV); ++v) z0rt[v] = vart[v];
+    }
     while (llcompute) {
       if (passes >= max_passes) { capped = true; return 0u; }
       ++passes;
@@ -1133,6 +1154,29 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
         }
       }
       if (!ltd(ztime + maxtime, dt)) llcompute = false;
+      if (TS && outer < nb_iter_max) {
+        if (c.TSTEP_TS != 0.0 && gtd(ztime + maxtime, tlast + ztstep)) {
+          maxtime = tlast - ztime + ztstep;
+          llcompute = false;
+        }
+        if (c.MRSTEP != 0.0) {
+          double maxb = 0.0;
+#pragma unroll
+          for (int v = 1; v < (H ? NVH : NV); ++v) {
+            const double thr = abs_gtp(A[v], 1.e-20) ? (copysign(1., A[v]) * c.MRSTEP + z0rt[v] - vart[v] - B[v]) / A[v]
+                                                    : -1.;
+            if (!negd(thr) && ltd(thr, maxtime) && (gtp(vart[v], rsmin[v]) || gtd(A[v], 0.0))) {
+              maxtime = dmin(maxtime, thr);
+              llcompute = false;
+            }
+            maxb = v == 1 ? fabs(B[v]) : dmax(maxb, fabs(B[v]));
+          }
+          if (gtd(maxb, c.MRSTEP)) {
+            maxtime = 0.;
+            llcompute = false;
+          }
+        }
+      }
       // State update with separately rounded product and sums (no FMA
       // contraction): after a species is depleted, v + A*t + B leaves a
       // rounding residual, and whether it exceeds XRTMIN decides whether the
@@ -1169,7 +1213,8 @@ ICE3_HD double ldp(const double *p, long i)
 // H (NRR = 7): with hail (rht / rhs; the hail kernels at hlut).
 // O (OCND2): the LOCND2 branches, with the TIWMX tables tw and the level
 // heights / droplet concentrations of ocnd2_column() at ozz / oconc.
-template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false>
+// TS: the MRSTEP / TSTEP_TS time splitting.
+template <bool SUR = false, bool SUBG = false, bool H = false, bool O = false, bool TS = false>
 ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double *__restrict__ lut,
                                     const Ice3gbRainIceFields &f, long p, double dt, int max_passes, bool &capped,
                                     const double *sur = nullptr, const double *__restrict__ hlut = nullptr,
@@ -1251,8 +1296,8 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
       hi[1] = pos(ri) ? pf.cf - hi[0] : 0.;
     }
     double rrevav;
-    key = stepping<SUR, SUBG, H, O>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi, capped,
-                                    sur, hlut, &op);
+    key = stepping<SUR, SUBG, H, O, TS>(c, d, lut, pf, dt, max_passes, vart, ext, cit, rainfr, rrevav, hl, hi,
+                                        capped, sur, hlut, &op);
 #pragma unroll
     for (int v = 0; v < NVT; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;

@@ -1712,7 +1712,8 @@ typedef struct {
   double cit, rainfr, rrevav;
   int outer, inner, capped;
   int tie;    /* bit 0: some pass took a growth-mode decision on rounding
-               residuals; bit 1: the CIT reset followed an ice residual */
+               residuals; bit 1: the CIT reset followed an ice residual;
+               bit 2: an MRSTEP threshold fell on the chosen sub-step */
 } StepOut;
 
 static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
@@ -1740,9 +1741,22 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
   double ztime = 0.0;
   int passes = 0;
   s->outer = 0; s->inner = 0; s->capped = 0; s->rrevav = 0.0; s->tie = 0;
+  /* :191-197 time splitting: the maximum number of outer iterations with
+   * their own limits, and the sub-step length of TSTEP_TS */
+  int nb_iter_max = (int)c->NMAXITER_MICRO;
+  double ztstep = 0.0;
+  if (c->TSTEP_TS != 0.0) {
+    int nb = (int)(dt / c->TSTEP_TS);
+    nb = nb > 1 ? nb : 1;
+    ztstep = dt / nb;
+    nb_iter_max = nb_iter_max > nb ? nb_iter_max : nb;
+  }
+  double z0rt[NVH], tlast = 0.0;
   while (ztime < dt) {                                                /* :204 */
-    s->outer++;
+    s->outer++;                                                       /* IITER, :258-266 */
     int llcompute = 1, lsoft = 0, inner = 0;
+    tlast = ztime;                                                    /* ZTIME_LASTCALL */
+    for (int v = 0; v < nv; ++v) z0rt[v] = s->vart[v];               /* Z0RT, :409-411 */
     while (llcompute) {                                               /* :227 */
       if (passes >= max_passes) { s->capped = 1; goto done; }
       passes++;
@@ -1775,6 +1789,36 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
         }
       }
       if (ztime + maxtime >= dt) llcompute = 0;                       /* :314-319 */
+      if (c->TSTEP_TS != 0.0 && s->outer < nb_iter_max && ztime + maxtime > tlast + ztstep) {  /* :387-397 */
+        maxtime = tlast - ztime + ztstep;
+        llcompute = 0;
+      }
+      if (c->MRSTEP != 0.0 && s->outer < nb_iter_max) {              /* :402-453 */
+        double maxb = 0.0;
+        for (int v = 1; v < nv; ++v) {
+          const double thr = fabs(A[v]) > 1.e-20
+                                 ? (copysign(1., A[v]) * c->MRSTEP + z0rt[v] - s->vart[v] - B[v]) / A[v] : -1.;
+          /* the threshold on a sub-step that does not end the outer
+           * iteration yet, up to rounding: a species that grew from zero to
+           * MRSTEP in the last outer iteration and now depletes reaches
+           * -MRSTEP + Z0RT = 0 together with its depletion time; whether
+           * the pass ends the outer iteration (a hard recompute) or
+           * continues soft is decided by the last bits of both (a tie,
+           * reported with bit 2) */
+          if (llcompute && thr >= 0. && fabs(thr - maxtime) <= 1e-12 * maxtime &&
+              (s->vart[v] > rsmin[v] || A[v] > 0.))
+            s->tie |= 4;
+          if (thr >= 0. && thr < maxtime && (s->vart[v] > rsmin[v] || A[v] > 0.)) {
+            maxtime = dmin(maxtime, thr);
+            llcompute = 0;
+          }
+          maxb = v == 1 ? fabs(B[v]) : dmax(maxb, fabs(B[v]));
+        }
+        if (maxb > c->MRSTEP) {
+          maxtime = 0.;
+          llcompute = 0;
+        }
+      }
       const double ri0 = s->vart[IRI];
       for (int v = 0; v < nv; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
       /* the ice depleted to a rounding residual: whether CIT is reset below
@@ -1836,7 +1880,7 @@ static int rain_ice_sediment(const C *c, int nij, int nk, double dt, int sed_for
 static int rain_ice_supported(const C *c)
 {
   if ((int)c->NRR != 6 && (int)c->NRR != 7) return 0;
-  if (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0) return 0;
+  if (c->OCND2 != 0.0 && (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)) return 0;
   if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1) return 0;                    /* SPLI, STAT */
   if ((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) return 0;  /* NONE, PRFR */
   if ((int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2) return 0;          /* NONE, CLFR, PRFR */
@@ -1857,7 +1901,9 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
 /* ice3o_rain_ice that also marks (tie[p] != 0, when tie is not NULL) the
  * points whose sub-stepping took a decision on rounding residuals (bit 0: a
  * graupel or hail growth-mode choice; bit 1: the reset of CIT after a pass
- * that depleted the ice to a residual); there the reference's own outcome
+ * that depleted the ice to a residual; bit 2: an MRSTEP threshold equal to
+ * the sub-step, which decides between a soft pass and a new outer
+ * iteration); there the reference's own outcome
  * depends on the last bits of the rates. */
 EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
                                const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,

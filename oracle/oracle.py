@@ -168,8 +168,10 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
              ldeposc: int = -1, lfeedbackt: int = -1, max_passes: int = 0, sed_jax: int = 0,
              with_fpr: bool = False, with_ties: bool = False):
     """Oracle rain_ice on ABI-named fields; returns (outputs dict, status bits).
-    with_ties: also out["tie"], 1 where the sub-stepping took a graupel or
-    hail growth-mode decision on rounding residuals (ice3o_rain_ice_ties)."""
+    with_ties: also out["tie"], the bits of the sub-stepping's decisions on
+    rounding residuals (ice3o_rain_ice_ties): 1 a graupel or hail growth
+    mode, 2 the CIT reset after an ice residual, 4 an MRSTEP threshold on
+    the chosen sub-step."""
     lib = load()
     keep = {k: _f64(st[k]) for k in RI_IN}
     nk, nij = keep["exn"].shape

@@ -84,6 +84,37 @@ extern "C" int rain_ice_points_host_ocnd2(const Ice3gbConstants *c, const Ice3gb
   return capped_any;
 }
 
+// With the MRSTEP / TSTEP_TS time splitting (the kernel's TS instantiation),
+// any warm option, with or without hail.
+extern "C" int rain_ice_points_host_ts(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk, double dt,
+                                       int max_passes, const Ice3gbRainIceFields *f, unsigned int *keys)
+{
+  ice3pt::Derived d;
+  ice3pt::make_derived(*c, d);
+  const double *lt = reinterpret_cast<const double *>(luts);
+  const bool subg = (int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0;
+  const bool hail = (int)c->NRR == 7;
+  if ((int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2)
+    for (long col = 0; col < nij; ++col) {
+      if (hail) ice3pt::prfr_column<true>(*c, *f, nij, nk, col);
+      else ice3pt::prfr_column<false>(*c, *f, nij, nk, col);
+    }
+  int capped_any = 0;
+  for (long p = 0; p < (long)nij * nk; ++p) {
+    bool capped;
+    unsigned int k;
+    if (hail)
+      k = subg ? ice3pt::rain_ice_point<false, true, true, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt)
+               : ice3pt::rain_ice_point<false, false, true, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt);
+    else
+      k = subg ? ice3pt::rain_ice_point<false, true, false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped)
+               : ice3pt::rain_ice_point<false, false, false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped);
+    keys[p] = k;
+    capped_any |= capped;
+  }
+  return capped_any;
+}
+
 // Host build of the surrogate's feature / target sampling (surrogate_point.cuh):
 // per grid point the 16 features and the five plain slow rates of a micro
 // point at its first hard pass; micro[p] = 0 elsewhere.

@@ -231,20 +231,26 @@ def _fields(x, nk, nij):
     return keep, f
 
 
-def _untie(spread, tie, max_share=0.02):
+def _untie(spread, tie, max_share=0.02, sed_after=True):
     """Points where the oracle took a decision on rounding residuals
     (ice3o_rain_ice_ties) get an unbounded allowance.  Bit 0, a graupel or
     hail growth-mode choice (the wet-growth estimate minus what it collects,
     a difference of several non-zero rates that is zero up to rounding,
-    against the dry-growth one): the point and the levels below it, where the
-    sedimentation carries its outcome, for every field, and the surface
-    fields of its column.  Bit 1, the reset of the ice concentration after a
-    pass that left the ice at a rounding residual: cit at the point.  They
-    must stay a small share of the grid."""
+    against the dry-growth one): the point, for every field, and when the
+    sedimentation follows the sub-stepping (sed_after) also the levels below
+    it, where the sedimentation carries the outcome, and the surface fields
+    of its column.  Bit 2, an MRSTEP threshold on the sub-step already
+    chosen (a soft pass or a new outer iteration), the same.  Bit 1, the
+    reset of the ice concentration after a pass that left the ice at a
+    rounding residual: cit at the point.  They must stay a small share of
+    the grid."""
     nk = tie.shape[0]
-    growth = (tie & 1) != 0
-    below = np.flip(np.maximum.accumulate(np.flip(growth, axis=0), axis=0), axis=0)   # tie at or above k
-    cols = below[0]
+    growth = (tie & 5) != 0
+    if sed_after:
+        below = np.flip(np.maximum.accumulate(np.flip(growth, axis=0), axis=0), axis=0)   # tie at or above k
+        cols = below[0]
+    else:
+        below, cols = growth, np.zeros(tie.shape[1], dtype=bool)
     cit_tie = (tie & 2) != 0
     assert below.mean() <= max_share, f"{below.mean():.2%} of the points lie at or below a growth-mode tie"
     # ice sublimating to zero within a pass is common (OCND2 states: up to a
@@ -341,10 +347,13 @@ def _run_device(t, x, host=False, **kw):
     res = {}
     back = {"ci_t": "cit", "ths": "ths", "rvs": "rvs", "rcs": "rcs", "rrs": "rrs", "ris": "ris", "rss": "rss",
             "rgs": "rgs", "rhs": "rhs"}
+    # without hail (NRR = 6) there is no rhs / inprh
     for k, v in back.items():
-        res[v] = np.asarray(new[k] if host else new[k].cpu().numpy())
+        if k in new:
+            res[v] = np.asarray(new[k] if host else new[k].cpu().numpy())
     for k in INPR7:
-        res[k] = np.asarray(diag[k] if host else diag[k].cpu().numpy())
+        if k in diag:
+            res[k] = np.asarray(diag[k] if host else diag[k].cpu().numpy())
     return res, ri
 
 

@@ -1,0 +1,176 @@
+"""MRSTEP / TSTEP_TS time splitting of the ICE4 sub-stepping
+(micro/mode_ice4_stepping.F90:191-197 the outer-iteration budget
+INB_ITER_MAX and the sub-step ZTSTEP, :255-259 ZTIME_LASTCALL, :387-397 the
+TSTEP_TS limit, :402-453 the MRSTEP limits against Z0RT and ZMAXB).
+
+The reference's Python port has no time splitting (MRSTEP and TSTEP_TS are
+only parameters there: ice_parameters.py:430-479) and its Fortran cannot be
+compiled here, so the oracle's restatement is pinned by its invariants:
+limits that cannot bind leave the step bit for bit unchanged, a TSTEP_TS
+sub-step forces at least PTSTEP / TSTEP_TS outer iterations on every active
+point, and the water budget closes.  Then the device code's host build (CPU)
+and the device kernels (GPU) against the oracle."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from parity import assert_parity, sensitivity
+from test_hail import INPR7, SRC7, _fields, _run_device, _scale, _untie, hail_state, host_libs  # noqa: F401
+
+DT = 50.0
+SRC6, INPR6 = SRC7[:-1], INPR7[:-1]
+
+
+def _table(**kw):
+    from ice3gb.constants import build_table
+    return build_table(table="phyex", overrides=kw)
+
+
+def _keys(nrr):
+    return (SRC7, INPR7) if nrr == 7 else (SRC6, INPR6)
+
+
+def _scale_ts(x, ref, fl, k, src):
+    """The terms of a source: those of the hail tests, and for a condensed
+    species the condensate of the point, which the sub-steps may carry
+    through the species and deplete to a rounding residual of it within the
+    step (snow converted to graupel in one TSTEP_TS sub-step and melted in
+    the next: graupel is zero before and after)."""
+    s = _scale(x, ref, fl, k)
+    if k in src[1:]:
+        s = s + sum(np.abs(x[j]) for j in src[1:])
+    return s
+
+
+# ---------------------------------------------------------------------------- oracle invariants (CPU)
+
+@pytest.mark.parametrize("nrr", [6.0, 7.0])
+def test_unbinding_limits_leave_the_step_unchanged(nrr):
+    """MRSTEP = 1 kg/kg is never reached within a step and TSTEP_TS = PTSTEP
+    gives one sub-step: the splitting must not change a bit."""
+    import oracle
+    x = hail_state(16 * 16, seed=11)
+    base, _ = oracle.rain_ice(_table(NRR=nrr), x, DT)
+    for kw in ({"MRSTEP": 1.0}, {"TSTEP_TS": DT}, {"MRSTEP": 1.0, "TSTEP_TS": DT}):
+        out, bits = oracle.rain_ice(_table(NRR=nrr, **kw), x, DT)
+        assert bits == 0
+        for k in base:
+            np.testing.assert_array_equal(out[k], base[k], err_msg=f"{kw} {k}")
+
+
+def _stepping_point_counts(t, x, idx):
+    """Outer iterations of ICE4_STEPPING at the given points (oracle hook)."""
+    import oracle
+    lib = oracle.load()
+    names = ("exn", "rhodref", "pabs", "tht", "rvt", "rct", "rrt", "rit", "rst", "rgt", "cit", "ths", "rvs", "rcs",
+             "rrs", "ris", "rss", "rgs", "cldfr", "sigs")
+    outer = np.zeros(len(idx), dtype=np.int64)
+    for j, (k, i) in enumerate(idx):
+        inp = np.array([x[n][k, i] for n in names], dtype=np.float64)
+        out = np.zeros(10)
+        o, inn = ctypes.c_int(), ctypes.c_int()
+        lib.ice3o_stepping_point(ctypes.byref(t.consts), ctypes.byref(t.luts), ctypes.c_double(DT), 4096,
+                                 inp.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p),
+                                 ctypes.byref(o), ctypes.byref(inn))
+        assert out[9] == 0.0
+        outer[j] = o.value
+    return outer
+
+
+def test_tstep_ts_forces_sub_steps():
+    """With TSTEP_TS = 10 s on a 50 s step every point that steps at all
+    makes at least five outer iterations (ZTSTEP = 10 s), without it most
+    make one; MRSTEP = 5e-6 kg/kg makes more of them than the default."""
+    x = hail_state(8 * 8, seed=12)
+    rng = np.random.default_rng(0)
+    idx = [(int(k), int(i)) for k, i in zip(rng.integers(0, 90, 200), rng.integers(0, 64, 200))]
+    base = _stepping_point_counts(_table(), x, idx)
+    ts = _stepping_point_counts(_table(TSTEP_TS=10.0), x, idx)
+    mr = _stepping_point_counts(_table(MRSTEP=5e-6), x, idx)
+    active = base > 0
+    assert active.sum() > 100
+    assert np.all(ts[active] >= 5) and np.median(base[active]) <= 2
+    assert np.all(mr >= base) and np.mean(mr > base) > 0.05
+
+
+@pytest.mark.parametrize("kw", [{"MRSTEP": 5e-5}, {"TSTEP_TS": 10.0}, {"MRSTEP": 1e-5, "TSTEP_TS": 20.0}])
+def test_time_split_water_budget_closes(kw):
+    import oracle
+    t = _table(NRR=7.0, **kw)
+    x = hail_state(16 * 16, seed=13)
+    out, bits = oracle.rain_ice(t, x, DT)
+    assert bits == 0
+    rhodz = x["rhodref"] * x["dzz"]
+    col = (rhodz * sum(out[k] - x[k] for k in SRC7)).sum(axis=0) * DT
+    precip = sum(out[k] for k in INPR7) * t.values["RHOLW"] * DT
+    scale = (rhodz * sum(np.abs(x[k]) for k in SRC7)).sum(axis=0) * DT
+    assert np.abs(col + precip).max() <= 1e-12 * scale.max()
+    base, _ = oracle.rain_ice(_table(NRR=7.0), x, DT)
+    assert np.abs(out["rrs"] - base["rrs"]).max() > 0.0
+
+
+# ---------------------------------------------------------------------------- host build (CPU)
+
+@pytest.mark.parametrize("nrr,kw", [(6.0, {"MRSTEP": 5e-5}), (6.0, {"TSTEP_TS": 10.0}),
+                                    (7.0, {"MRSTEP": 1e-5, "TSTEP_TS": 20.0}),
+                                    (6.0, {"MRSTEP": 5e-5, "SUBG_RC_RR_ACCR": 1.0, "SUBG_RR_EVAP": 1.0})])
+def test_time_split_host_build_matches_oracle(host_libs, nrr, kw):
+    """rain_ice_point's time-splitting instantiation built for the host, then
+    the statistical sedimentation after it, against the oracle."""
+    import oracle
+    t = _table(NRR=nrr, LSEDIM_AFTER=1.0, **kw)
+    nij, nk = 16 * 16, 90
+    x = hail_state(nij, seed=14)
+    src, inpr = _keys(nrr)
+    keep, f = _fields(x, nk, nij)
+    keys = np.zeros(nij * nk, dtype=np.uint32)
+    capped = host_libs["rain_ice_point_host"].rain_ice_points_host_ts(
+        ctypes.byref(t.consts), ctypes.byref(t.luts), nij, nk, ctypes.c_double(DT), 4096, ctypes.byref(f),
+        keys.ctypes.data_as(ctypes.c_void_p))
+    assert capped == 0
+    host_libs["sedimentation_host"].sed_stat_rain_ice_host(ctypes.byref(t.consts), nij, nk, ctypes.c_double(DT),
+                                                           ctypes.byref(f))
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT, max_passes=4096)[0], x, rel=1e-12, trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, max_passes=4096, with_fpr=True, with_ties=True)
+    # MRSTEP thresholds on the sub-step are frequent (a species grown from
+    # zero to MRSTEP that then depletes), and the sedimentation after the
+    # sub-stepping carries them down the column
+    spread, share = _untie(spread, fl["tie"], max_share=0.15)
+    for k in ("ths",) + src + ("cit",) + inpr:
+        sc = _scale_ts(x, ref, fl, k, src) if k in ("ths",) + src else None
+        assert_parity(keep[k], ref[k], spread[k], f"time split host {kw}/{k}", scale=sc,
+                      max_frac_conditioned=0.01 + share[k])
+
+
+# ---------------------------------------------------------------------------- GPU
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nrr,kw", [(6.0, {"MRSTEP": 5e-5}), (6.0, {"TSTEP_TS": 10.0}),
+                                    (7.0, {"MRSTEP": 1e-5, "TSTEP_TS": 20.0}),
+                                    (6.0, {"MRSTEP": 5e-5, "SUBG_RC_RR_ACCR": 1.0, "SUBG_RR_EVAP": 1.0})])
+def test_time_split_device_matches_oracle(nrr, kw):
+    import oracle
+    t = _table(NRR=nrr, **kw)
+    x = hail_state(32 * 32, seed=15)
+    src, inpr = _keys(nrr)
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
+    spread, share = _untie(spread, fl["tie"], sed_after=False)
+    got, ri = _run_device(t, x)
+    for k in ("ths",) + src + ("cit",) + inpr:
+        sc = _scale_ts(x, ref, fl, k, src) if k in ("ths",) + src else None
+        assert_parity(got[k], ref[k], spread[k], f"time split device {kw}/{k}", scale=sc,
+                      max_frac_conditioned=0.01 + share[k])
+    assert ri.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_unbinding_limits_on_the_device():
+    """The time-splitting kernels with limits that cannot bind give the
+    default kernels' results bit for bit."""
+    x = hail_state(16 * 16, seed=16)
+    base, _ = _run_device(_table(), x)
+    got, _ = _run_device(_table(MRSTEP=1.0, TSTEP_TS=DT), x)
+    for k in base:
+        np.testing.assert_array_equal(got[k], base[k], err_msg=k)

@@ -174,3 +174,21 @@ def test_unbinding_limits_on_the_device():
     got, _ = _run_device(_table(MRSTEP=1.0, TSTEP_TS=DT), x)
     for k in base:
         np.testing.assert_array_equal(got[k], base[k], err_msg=k)
+
+
+@pytest.mark.gpu
+def test_physics_step_takes_the_time_splitting():
+    """The chained step (ice_adjust -> rain_ice -> ice_adjust) dispatches to
+    the time-splitting kernels: limits that cannot bind give the default
+    step bit for bit, MRSTEP = 5e-5 another step."""
+    from ice3gb.components import Ice3Handle
+    from test_gpu_rain_ice import _gpu_step, _np_state, _step_state
+    st = _step_state(_np_state(16 * 16, seed=22))
+    base = _gpu_step(Ice3Handle(_table()), st)
+    same = _gpu_step(Ice3Handle(_table(MRSTEP=1.0, TSTEP_TS=DT)), st)
+    for k in base:
+        np.testing.assert_array_equal(same[k], base[k], err_msg=k)
+    h = Ice3Handle(_table(MRSTEP=5e-5))
+    split = _gpu_step(h, st)
+    assert h.status() == 0
+    assert max(np.abs(split[k] - base[k]).max() for k in ("ths", "rrs", "rss")) > 0.0

@@ -192,3 +192,31 @@ def test_physics_step_takes_the_time_splitting():
     split = _gpu_step(h, st)
     assert h.status() == 0
     assert max(np.abs(split[k] - base[k]).max() for k in ("ths", "rrs", "rss")) > 0.0
+
+
+def test_oracle_refuses_time_splitting_with_ocnd2():
+    """OCND2 with MRSTEP / TSTEP_TS is not built: the oracle refuses it."""
+    import oracle
+    from test_ocnd2 import ocnd2_rain_ice_state
+    x = ocnd2_rain_ice_state(4 * 4, seed=1)
+    for kw in ({"MRSTEP": 5e-5}, {"TSTEP_TS": 10.0}):
+        with pytest.raises(RuntimeError):
+            oracle.rain_ice(_table(OCND2=1.0, **kw), x, DT)
+
+
+@pytest.mark.gpu
+def test_device_refuses_time_splitting_with_ocnd2():
+    import torch
+    from ice3gb import RainIce, _abi
+    from test_ocnd2 import ocnd2_rain_ice_state
+    x = ocnd2_rain_ice_state(4 * 4, seed=1)
+    ri = RainIce()
+    ri.table = _table(OCND2=1.0, MRSTEP=5e-5)
+    m = {"exn": "exn", "dzz": "dzz", "rhodref": "rhodref", "exnref": "exnref", "pres": "pabs", "cldfr": "cldfr",
+         "sigs": "sigs", "th_t": "tht", "rv_t": "rvt", "rc_t": "rct", "rr_t": "rrt", "ri_t": "rit", "rs_t": "rst",
+         "rg_t": "rgt", "ci_t": "cit", "hlc_hrc": "hlc_hrc", "hlc_hcf": "hlc_hcf", "hli_hri": "hli_hri",
+         "hli_hcf": "hli_hcf", "ths": "ths", "rvs": "rvs", "rcs": "rcs", "rrs": "rrs", "ris": "ris", "rss": "rss",
+         "rgs": "rgs", "sea": "sea", "town": "town", "ssio": "ssio", "ssiu": "ssiu", "ifr": "ifr", "icldfr": "icldfr"}
+    state = {k: torch.as_tensor(np.ascontiguousarray(x[v])).cuda() for k, v in m.items()}
+    with pytest.raises(_abi.Ice3gbError, match="MRSTEP"):
+        ri(state, DT)

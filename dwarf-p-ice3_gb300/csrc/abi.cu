@@ -834,8 +834,6 @@ int ice3gb_create(const Ice3gbConstants *c, const Ice3gbLuts *luts, void **handl
   char why[256] = "";
   if ((int)c->NRR != 6 && (int)c->NRR != 7)
     snprintf(why, sizeof(why), "rain_ice supports NRR = 6 or 7 (hail), got %g", c->NRR);
-  else if (c->OCND2 != 0.0 && (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0))
-    snprintf(why, sizeof(why), "rain_ice: OCND2 with the MRSTEP / TSTEP_TS time splitting is not supported");
   else if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1)
     snprintf(why, sizeof(why), "rain_ice: SEDIM must be SPLI (0) or STAT (1), got %g", c->SEDIM);
   else if (((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) ||

@@ -1713,7 +1713,8 @@ typedef struct {
   int outer, inner, capped;
   int tie;    /* bit 0: some pass took a growth-mode decision on rounding
                residuals; bit 1: the CIT reset followed an ice residual;
-               bit 2: an MRSTEP threshold fell on the chosen sub-step */
+               bit 2: an MRSTEP threshold fell on the chosen sub-step;
+               bit 3: a hard pass followed a bit-1 reset */
 } StepOut;
 
 static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
@@ -1754,6 +1755,9 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
   double z0rt[NVH], tlast = 0.0;
   while (ztime < dt) {                                                /* :204 */
     s->outer++;                                                       /* IITER, :258-266 */
+    /* a hard pass after a rounding-decided CIT reset (MRSTEP / TSTEP_TS
+     * outer iterations): the reset now reaches every rate of the point */
+    if (s->tie & 2) s->tie |= 8;
     int llcompute = 1, lsoft = 0, inner = 0;
     tlast = ztime;                                                    /* ZTIME_LASTCALL */
     for (int v = 0; v < nv; ++v) z0rt[v] = s->vart[v];               /* Z0RT, :409-411 */
@@ -1880,7 +1884,6 @@ static int rain_ice_sediment(const C *c, int nij, int nk, double dt, int sed_for
 static int rain_ice_supported(const C *c)
 {
   if ((int)c->NRR != 6 && (int)c->NRR != 7) return 0;
-  if (c->OCND2 != 0.0 && (c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0)) return 0;
   if ((int)c->SEDIM != 0 && (int)c->SEDIM != 1) return 0;                    /* SPLI, STAT */
   if ((int)c->SUBG_RC_RR_ACCR != 0 && (int)c->SUBG_RC_RR_ACCR != 1) return 0;  /* NONE, PRFR */
   if ((int)c->SUBG_RR_EVAP < 0 || (int)c->SUBG_RR_EVAP > 2) return 0;          /* NONE, CLFR, PRFR */
@@ -1903,7 +1906,8 @@ EXPORT int ice3o_rain_ice(const C *c, const Ice3gbLuts *lut, int nij, int nk, do
  * graupel or hail growth-mode choice; bit 1: the reset of CIT after a pass
  * that depleted the ice to a residual; bit 2: an MRSTEP threshold equal to
  * the sub-step, which decides between a soft pass and a new outer
- * iteration); there the reference's own outcome
+ * iteration; bit 3: a new outer iteration's hard pass after a bit-1 reset,
+ * which carries the reset into every rate); there the reference's own outcome
  * depends on the last bits of the rates. */
 EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int nk, double dt,
                                const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,

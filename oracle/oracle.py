@@ -171,7 +171,7 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
     with_ties: also out["tie"], the bits of the sub-stepping's decisions on
     rounding residuals (ice3o_rain_ice_ties): 1 a graupel or hail growth
     mode, 2 the CIT reset after an ice residual, 4 an MRSTEP threshold on
-    the chosen sub-step."""
+    the chosen sub-step, 8 a hard pass after such a CIT reset."""
     lib = load()
     keep = {k: _f64(st[k]) for k in RI_IN}
     nk, nij = keep["exn"].shape

@@ -240,12 +240,13 @@ def _untie(spread, tie, max_share=0.02, sed_after=True):
     sedimentation follows the sub-stepping (sed_after) also the levels below
     it, where the sedimentation carries the outcome, and the surface fields
     of its column.  Bit 2, an MRSTEP threshold on the sub-step already
-    chosen (a soft pass or a new outer iteration), the same.  Bit 1, the
+    chosen (a soft pass or a new outer iteration), and bit 3, a hard pass
+    of a later outer iteration after a bit-1 reset, the same.  Bit 1, the
     reset of the ice concentration after a pass that left the ice at a
     rounding residual: cit at the point.  They must stay a small share of
     the grid."""
     nk = tie.shape[0]
-    growth = (tie & 5) != 0
+    growth = (tie & 13) != 0
     if sed_after:
         below = np.flip(np.maximum.accumulate(np.flip(growth, axis=0), axis=0), axis=0)   # tie at or above k
         cols = below[0]

@@ -358,7 +358,7 @@ ICE3_HD double llbdar_rf(const Cst &c, const Derived &d, double lrho, double rr,
 // pass (mode_ice4_warm.F90).
 ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, double t, const double v[NV],
                           const double hl[4], double ka, double dv, double cj, const Slopes &s, double rainfr,
-                          double e_caccr, Rates &R)
+                          double e_caccr, Rates &R, const double *acrf = nullptr)
 {
   double *b = R.bu;
   const bool has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
@@ -366,7 +366,10 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
   const bool llrfr = accr == 1 || evap == 2;
   const double llrf = llrfr ? llbdar_rf(c, d, pf.lrho, v[IRR], rainfr) : s.llbdar;
   if (accr == 0) {
-    b[B_RCACCR] = (has_c && has_r) ? c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt : 0.0;
+    // OCND2: the collision factor PACRF (mode_ice4_warm.F90:128)
+    b[B_RCACCR] = (has_c && has_r) ? (acrf ? c.FCACCR * v[IRC] * *acrf * e_caccr * pf.rho_mcexvt
+                                           : c.FCACCR * v[IRC] * e_caccr * pf.rho_mcexvt)
+                                   : 0.0;
   } else {
     const bool m = has_c && has_r;
     const bool m1 = m && gtp(hl[2], c.C_RTMIN) && pos(hl[0]);
@@ -516,7 +519,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // ---- ICE4_WARM (mode_ice4_warm.F90) ----
   if (SUBG && c.LWARM != 0.0 && ((int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0)) {
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
-    warm_subgrid(c, d, pf, t, v, hl, ka, dv, cj, s, rainfr, e_caccr, R);
+    warm_subgrid(c, d, pf, t, v, hl, ka, dv, cj, s, rainfr, e_caccr, R, O ? &acrf : nullptr);
   } else if (c.LWARM != 0.0) {
     // SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;

@@ -1918,8 +1918,7 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
   const int hail = (int)c->NRR == 7;
   if (hail && (!f->rht || !f->rhs || !f->inprh || (opt && opt->sed_jax > 0))) return ICE3GB_ERR_UNSUPPORTED;
   const int ocnd2 = c->OCND2 != 0.0;
-  if (ocnd2 && (hail || (int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0 || !f->ssio || !f->ssiu ||
-                !f->ifr || !f->icldfr))
+  if (ocnd2 && (hail || !f->ssio || !f->ssiu || !f->ifr || !f->icldfr))
     return ICE3GB_ERR_UNSUPPORTED;
   const long n = (long)nij * nk;
   /* OCND2: TIWMX tables, level heights (rain_ice.F90:386-394: the sum of

@@ -61,9 +61,10 @@ extern "C" int rain_ice_points_host_hail(const Ice3gbConstants *c, const Ice3gbL
   return capped_any;
 }
 
-// With OCND2 (the kernel's O instantiation): the column heights and droplet
-// concentrations first (ocnd2_column), then the points; tw = the six TIWMX
-// tables (ice3o_tiwmx_all layout).
+// With OCND2 (the kernel's O instantiation, with any warm option and the
+// time splitting): the precipitation fraction of a PRFR option and the column
+// heights and droplet concentrations first (prfr_column, ocnd2_column), then
+// the points; tw = the six TIWMX tables (ice3o_tiwmx_all layout).
 extern "C" int rain_ice_points_host_ocnd2(const Ice3gbConstants *c, const Ice3gbLuts *luts, int nij, int nk,
                                           double dt, int max_passes, const Ice3gbRainIceFields *f, const double *tw,
                                           unsigned int *keys)
@@ -73,12 +74,26 @@ extern "C" int rain_ice_points_host_ocnd2(const Ice3gbConstants *c, const Ice3gb
   const double *lt = reinterpret_cast<const double *>(luts);
   const long n = (long)nij * nk;
   std::vector<double> ocs(2 * (size_t)n);
+  const bool subg = (int)c->SUBG_RC_RR_ACCR != 0 || (int)c->SUBG_RR_EVAP != 0;
+  const bool ts = c->MRSTEP != 0.0 || c->TSTEP_TS != 0.0;
+  if ((int)c->SUBG_RC_RR_ACCR == 1 || (int)c->SUBG_RR_EVAP == 2)
+    for (long col = 0; col < nij; ++col) ice3pt::prfr_column(*c, *f, nij, nk, col);
   for (long col = 0; col < nij; ++col) ice3pt::ocnd2_column(*c, *f, nij, nk, col, ocs.data(), ocs.data() + n);
   int capped_any = 0;
+  double *zz = ocs.data(), *conc = ocs.data() + n;
   for (long p = 0; p < n; ++p) {
     bool capped;
-    keys[p] = ice3pt::rain_ice_point<false, false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt,
-                                                                tw, ocs.data(), ocs.data() + n);
+    using namespace ice3pt;
+    if (subg)
+      keys[p] = ts ? rain_ice_point<false, true, false, true, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr,
+                                                                    lt, tw, zz, conc)
+                   : rain_ice_point<false, true, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt,
+                                                              tw, zz, conc);
+    else
+      keys[p] = ts ? rain_ice_point<false, false, false, true, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr,
+                                                                     lt, tw, zz, conc)
+                   : rain_ice_point<false, false, false, true>(*c, d, lt, *f, p, dt, max_passes, capped, nullptr, lt,
+                                                               tw, zz, conc);
     capped_any |= capped;
   }
   return capped_any;

@@ -431,7 +431,9 @@ def _ri_scale(x, ref, fl, k):
     return s
 
 
-def test_ocnd2_rain_ice_host_build_matches_oracle():
+@pytest.mark.parametrize("kw", [{}, {"SUBG_RC_RR_ACCR": 1.0, "SUBG_RR_EVAP": 2.0}, {"SUBG_RR_EVAP": 1.0},
+                                {"SUBG_RR_EVAP": 1.0, "MRSTEP": 5e-5}])
+def test_ocnd2_rain_ice_host_build_matches_oracle(kw):
     import oracle
     import subprocess
     from ice3gb import _abi
@@ -443,7 +445,7 @@ def test_ocnd2_rain_ice_host_build_matches_oracle():
         subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I",
                         os.path.join(d, "..", "include"), os.path.join(d, f"{name}.cpp"), "-o", out], check=True)
         libs[name] = ctypes.CDLL(out)
-    t = _ri_table(LSEDIM_AFTER=1.0, LDEPOSC=0.0)
+    t = _ri_table(LSEDIM_AFTER=1.0, LDEPOSC=0.0, **kw)
     nij, nk = 24 * 24, 90
     x = ocnd2_rain_ice_state(nij, seed=3)
     keep, f = {}, _abi.RainIceFields()
@@ -526,4 +528,24 @@ def test_ocnd2_rain_ice_device_matches_oracle(after):
     for k in RI_OUT:
         sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
         assert_parity(got[k], ref[k], spread[k], f"ocnd2 device/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+    assert ri.device_status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kw", [{"SUBG_RC_RR_ACCR": 1.0, "SUBG_RR_EVAP": 2.0}, {"SUBG_RR_EVAP": 1.0}])
+def test_ocnd2_rain_ice_warm_options_device_matches_oracle(kw):
+    """OCND2 with the subgrid warm-process options (the OCND2 branches leave
+    ICE4_WARM and ICE4_COMPUTE_PDF as they are)."""
+    import oracle
+    from test_hail import _untie
+    from test_time_splitting import _ocnd2_device
+    t = _ri_table(**kw)
+    x = ocnd2_rain_ice_state(32 * 32, seed=6)
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
+    spread, share = _untie(spread, fl["tie"], sed_after=False)
+    got, ri = _ocnd2_device(t, x)
+    for k in RI_OUT:
+        sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
+        assert_parity(got[k], ref[k], spread[k], f"ocnd2 warm {kw}/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
     assert ri.device_status() == 0

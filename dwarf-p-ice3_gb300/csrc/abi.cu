@@ -202,7 +202,6 @@ int validate_rain_ice(Handle *h, const Ice3gbRainIceFields *f)
     REQUIRE(f->rht); REQUIRE(f->rhs); REQUIRE(f->inprh);
   }
   if (h->c.OCND2 != 0.0) {   // the ice_adjust OCND2 outputs of the same state
-    if ((int)h->c.NRR != 6) return fail(h, ICE3GB_ERR_UNSUPPORTED, "rain_ice OCND2: NRR = 6 only (no hail)");
     REQUIRE(f->ssio); REQUIRE(f->ssiu); REQUIRE(f->ifr); REQUIRE(f->icldfr);
   }
   return ICE3GB_OK;

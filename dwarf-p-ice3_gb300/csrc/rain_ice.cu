@@ -132,7 +132,9 @@ cudaError_t launch_rain_ice_points(const Cst &c, const RainIceArgs &a, int num_s
   const bool hail = (int)c.NRR == 7;
   if (c.MRSTEP != 0.0 || c.TSTEP_TS != 0.0) return launch_rain_ice_points_ts(c, a, num_sms, s);
   void (*kern)(const Cst, const RainIceArgs) =
-      c.OCND2 != 0.0 ? (subg ? rain_ice_points_kernel<true, false, true> : rain_ice_points_kernel<false, false, true>)
+      c.OCND2 != 0.0
+          ? (hail ? (subg ? rain_ice_points_kernel<true, true, true> : rain_ice_points_kernel<false, true, true>)
+                  : (subg ? rain_ice_points_kernel<true, false, true> : rain_ice_points_kernel<false, false, true>))
       : hail ? (subg ? rain_ice_points_kernel<true, true> : rain_ice_points_kernel<false, true>)
              : (subg ? rain_ice_points_kernel<true, false> : rain_ice_points_kernel<false, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rain_ice_smem_bytes());

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM) rain_ice_points_
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       bool capped;
       if (O)
-        key = rain_ice_point<false, SUBG, false, true, TS>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr,
+        key = rain_ice_point<false, SUBG, H, true, TS>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr,
                                                            a.luts, a.tw, a.ocs, a.ocs + n);
       else
         key = rain_ice_point<false, SUBG, H, false, TS>(c, dsh, lut, f, p, dt, a.max_passes, capped, nullptr, a.luts);

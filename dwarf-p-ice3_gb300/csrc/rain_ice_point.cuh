@@ -1257,7 +1257,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   }
   // LLMICRO (OCND2: rain_ice.F90:347-363, the XFRMIN(12) / XFRMIN(13) thresholds)
   const bool micro = O ? (gtp(op.ssio, c.FRMIN12) || gtp(rc, c.FRMIN13) || gtp(rr, c.FRMIN13) || gtp(ri, c.FRMIN13) ||
-                          gtp(rs, c.FRMIN13) || gtp(rg, c.FRMIN13))
+                          gtp(rs, c.FRMIN13) || gtp(rg, c.FRMIN13) || (H && gtp(rh, c.FRMIN13)))
                        : (gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
                           gtp(rg, c.G_RTMIN) || (H && gtp(rh, c.H_RTMIN)));
   const double iexnref = fm::frcp(exnref);

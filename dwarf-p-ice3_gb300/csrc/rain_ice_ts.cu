@@ -13,8 +13,9 @@ cudaError_t launch_rain_ice_points_ts(const Cst &c, const RainIceArgs &a, int nu
   const bool subg = (int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0;
   const bool hail = (int)c.NRR == 7;
   void (*kern)(const Cst, const RainIceArgs) =
-      c.OCND2 != 0.0 ? (subg ? rain_ice_points_kernel<true, false, true, true>
-                            : rain_ice_points_kernel<false, false, true, true>)
+      c.OCND2 != 0.0
+          ? (hail ? (subg ? rain_ice_points_kernel<true, true, true, true> : rain_ice_points_kernel<false, true, true, true>)
+                  : (subg ? rain_ice_points_kernel<true, false, true, true> : rain_ice_points_kernel<false, false, true, true>))
       : hail ? (subg ? rain_ice_points_kernel<true, true, false, true> : rain_ice_points_kernel<false, true, false, true>)
              : (subg ? rain_ice_points_kernel<true, false, false, true> : rain_ice_points_kernel<false, false, false, true>);
   const size_t smem = sizeof(double) * LUT_N;

@@ -1918,7 +1918,7 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
   const int hail = (int)c->NRR == 7;
   if (hail && (!f->rht || !f->rhs || !f->inprh || (opt && opt->sed_jax > 0))) return ICE3GB_ERR_UNSUPPORTED;
   const int ocnd2 = c->OCND2 != 0.0;
-  if (ocnd2 && (hail || !f->ssio || !f->ssiu || !f->ifr || !f->icldfr))
+  if (ocnd2 && (!f->ssio || !f->ssiu || !f->ifr || !f->icldfr))
     return ICE3GB_ERR_UNSUPPORTED;
   const long n = (long)nij * nk;
   /* OCND2: TIWMX tables, level heights (rain_ice.F90:386-394: the sum of
@@ -2027,7 +2027,7 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
     Ocnd2Pt oc;
     if (ocnd2) {                                                      /* :347-363 */
       const double m = c->FRMIN13;
-      micro = f->ssio[p] > c->FRMIN12 || rc > m || rr > m || ri > m || rs > m || rg > m;
+      micro = f->ssio[p] > c->FRMIN12 || rc > m || rr > m || ri > m || rs > m || rg > m || (hail && rh > m);
       oc.tw = tw; oc.ssio = f->ssio[p]; oc.ssiu = f->ssiu[p]; oc.ifr = f->ifr[p]; oc.icldfr = f->icldfr[p];
       oc.zzz = zzz[p]; oc.conc = conc[p];
     }

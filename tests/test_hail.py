@@ -387,3 +387,68 @@ def test_hail_host_entry_point_equals_device():
     for k in dev:
         np.testing.assert_array_equal(host[k], dev[k], err_msg=k)
     assert TOL > 0
+
+
+# ---------------------------------------------------------------------------- hail with OCND2
+
+def ocnd2_hail_state(nij, seed):
+    """An OCND2 rain_ice state (the ice_adjust OCND2 outputs included) with
+    hail on 40 % of the points."""
+    from test_ocnd2 import ocnd2_rain_ice_state
+    x = ocnd2_rain_ice_state(nij, seed)
+    nk = x["exn"].shape[0]
+    rng = np.random.default_rng(seed + 2000)
+    rh = np.exp(rng.normal(np.log(1e-4), 1.5, (nk, nij))) * (rng.uniform(size=(nk, nij)) < 0.4)
+    x["rht"] = rh
+    x["rhs"] = rh / DT * rng.uniform(0.5, 1.5, (nk, nij))
+    return x
+
+
+def test_ocnd2_hail_water_budget_closes():
+    """OCND2 with hail (the LOCND2 rows and LLMICRO with PRHT,
+    rain_ice.F90:349-356): the water budget of the step closes."""
+    import oracle
+    t = _table(OCND2=1.0)
+    x = ocnd2_hail_state(16 * 16, seed=7)
+    out, bits = oracle.rain_ice(t, x, DT)
+    assert bits == 0
+    rhodz = x["rhodref"] * x["dzz"]
+    col = (rhodz * sum(out[k] - x[k] for k in SRC7)).sum(axis=0) * DT
+    precip = sum(out[k] for k in INPR7) * t.values["RHOLW"] * DT
+    scale = (rhodz * sum(np.abs(x[k]) for k in SRC7)).sum(axis=0) * DT
+    assert np.abs(col + precip).max() <= 1e-12 * scale.max()
+    assert np.count_nonzero(out["inprh"]) > 20
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kw", [{}, {"MRSTEP": 5e-5}])
+def test_ocnd2_hail_device_matches_oracle(kw):
+    import oracle
+    import torch
+    from ice3gb import RainIce
+    t = _table(OCND2=1.0, **kw)
+    x = ocnd2_hail_state(32 * 32, seed=8)
+    ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
+    fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
+    spread, share = _untie(spread, fl["tie"], max_share=0.1, sed_after=False)
+    ri = RainIce()
+    ri.table = t
+    m = {"exn": "exn", "dzz": "dzz", "rhodref": "rhodref", "exnref": "exnref", "pres": "pabs", "cldfr": "cldfr",
+         "sigs": "sigs", "th_t": "tht", "rv_t": "rvt", "rc_t": "rct", "rr_t": "rrt", "ri_t": "rit", "rs_t": "rst",
+         "rg_t": "rgt", "rh_t": "rht", "ci_t": "cit", "hlc_hrc": "hlc_hrc", "hlc_hcf": "hlc_hcf",
+         "hli_hri": "hli_hri", "hli_hcf": "hli_hcf", "ths": "ths", "rvs": "rvs", "rcs": "rcs", "rrs": "rrs",
+         "ris": "ris", "rss": "rss", "rgs": "rgs", "rhs": "rhs", "sea": "sea", "town": "town", "ssio": "ssio",
+         "ssiu": "ssiu", "ifr": "ifr", "icldfr": "icldfr"}
+    state = {k: torch.as_tensor(np.ascontiguousarray(x[v])).cuda() for k, v in m.items()}
+    new, diag = ri(state, DT)
+    got = {"cit": new["ci_t"].cpu().numpy()}
+    for k in ("ths",) + SRC7:
+        got[k] = new[k].cpu().numpy()
+    for k in INPR7:
+        got[k] = diag[k].cpu().numpy()
+    for k in ("ths",) + SRC7 + ("cit",) + INPR7:
+        sc = _scale(x, ref, fl, k) if k in ("ths",) + SRC7 else None
+        assert_parity(got[k], ref[k], spread[k], f"ocnd2 hail device {kw}/{k}", scale=sc,
+                      max_frac_conditioned=0.01 + share[k])
+    assert ri.device_status() == 0
+    assert np.count_nonzero(got["inprh"]) > 50

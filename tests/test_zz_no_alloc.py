@@ -46,7 +46,10 @@ OUTPUTS = ("cit", "ths", "rvs", "rcs", "rrs", "ris", "rss", "rgs", "evap3d", "ra
            "inprs", "inprg", "indep")
 
 
-def test_noalloc_matches_allocating_entry_point_twice():
+@pytest.mark.parametrize("overrides", [{}, {"MRSTEP": 5e-5, "TSTEP_TS": 10.0}])
+def test_noalloc_matches_allocating_entry_point_twice(overrides):
+    """Also with the MRSTEP / TSTEP_TS time splitting, whose kernels need no
+    more scratch than the default ones."""
     from ice3gb import _abi
     from ice3gb.components import Ice3Handle
     from ice3gb.constants import build_table
@@ -55,7 +58,7 @@ def test_noalloc_matches_allocating_entry_point_twice():
     nij = 64 * 64
     assert nij * NK <= _abi.NOALLOC_MAX_POINTS
     st = make_state(nij, NK, seed=5, precip=True, device="cuda")
-    h = Ice3Handle(build_table(table="phyex"))
+    h = Ice3Handle(build_table(table="phyex", overrides=overrides))
     lib = h.lib
     opt = _abi.RainIceOptions(-1, -1, -1, 0, 0)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

@@ -341,8 +341,12 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   cudaError_t e;
   // SEDIM: 1 = STAT (statistical), 0 = SPLI (time-split, needs 2 n doubles of scratch)
   const bool spli = (int)c.SEDIM == 0;
+  const bool ocnd2 = c.OCND2 != 0.0;
+  // both refusals come before the first launch: a refused call leaves every field untouched
   if (spli && !rs.may_alloc)
     return fail(h, ICE3GB_ERR_UNSUPPORTED, "SEDIM=SPLI needs scratch memory: not available in this entry point");
+  if (ocnd2 && !rs.may_alloc)
+    return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 needs scratch memory: not available in this entry point");
   auto sediment = [&]() -> int {
     ProfScope ps(h, K_SEDIM, s);
     if (!spli) {
@@ -382,11 +386,8 @@ int run_rain_ice_core(Handle *h, int nij, int nk, double dt, const Ice3gbRainIce
   a.nij = nij; a.nk = nk; a.dt = dt; a.max_passes = max_passes; a.lfeedbackt = (int)c.LFEEDBACKT;
   a.tw = nullptr;
   a.ocs = nullptr;
-  const bool ocnd2 = c.OCND2 != 0.0;
   if (ocnd2) {
     // level heights and droplet concentrations of the OCND2 processes (2 n doubles)
-    if (!rs.may_alloc)
-      return fail(h, ICE3GB_ERR_UNSUPPORTED, "OCND2 needs scratch memory: not available in this entry point");
     if ((e = cudaMallocAsync(&a.ocs, sizeof(double) * 2 * (size_t)nij * nk, s)) != cudaSuccess)
       return cuda_fail(h, e, "cudaMallocAsync");
     a.tw = h->d_tiwmx;
@@ -744,7 +745,9 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
 }  // namespace
 
 // Validation + launch sequence with caller-provided scratch (used by the
-// entry point of rain_ice_noalloc.cu, which owns its static scratch).
+// entry point of rain_ice_noalloc.cu, which owns its static scratch: four
+// control words, then scratch_points pass keys, then scratch_points order
+// words).
 int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double dt,
                                           const Ice3gbRainIceOptions *opt, const Ice3gbRainIceFields *f,
                                           unsigned int *scratch, long scratch_points, void *stream)
@@ -758,7 +761,8 @@ int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double 
                 (long)nij * nk, scratch_points);
   if ((rc = validate_rain_ice(h, f)) || (rc = check_device(h))) return rc;
   if (!scratch) return fail(h, ICE3GB_ERR_CUDA, "static scratch address unavailable");
-  const RiScratch rs = {scratch, scratch + 1, scratch + 4, nullptr, true, true, false};
+  // control words [0, 4), pass keys [4, 4 + nij*nk), processing order from 4 + scratch_points
+  const RiScratch rs = {scratch, scratch + 1, scratch + 4, scratch + 4 + scratch_points, true, true, false};
   return run_rain_ice_core(h, nij, nk, dt, opt, f, rs, static_cast<cudaStream_t>(stream));
 }
 

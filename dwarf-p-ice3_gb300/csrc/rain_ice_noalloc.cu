@@ -8,19 +8,22 @@
 // allocation can then fail at any step, long after initialisation), or a
 // deployment that caps device memory outside the library.  This
 // entry point serves them with a scratch array that is part of the loaded
-// library itself: a file-scope __device__ array of ICE3GB_NOALLOC_MAX_POINTS
-// pass keys plus four control words (16 MiB + 16 B), which every GPU that
-// loads the library holds until the process exits.
+// library itself: a file-scope __device__ array of four control words, then
+// ICE3GB_NOALLOC_MAX_POINTS pass keys and as many processing-order words (the
+// regime sort of the points, as in ice3gb_rain_ice): 32 MiB + 16 B, which
+// every GPU that loads the library holds until the process exits.
 //
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in), so the device address is looked up with
 // cudaGetSymbolAddress once per device, with that device current, on the
 // first call made on it; that first call should therefore come before any
 // stream capture.  All calls share the one array: the control words are
-// cleared on the stream at the start of every call (the pass keys are all
-// rewritten by the kernel), and calls whose work overlaps on the GPU — on
-// different streams, or from different host threads — race on it and must be
-// serialised by the caller.
+// cleared on the stream at the start of every call (the pass keys and the
+// order words of the call's points are all rewritten by its kernels), and
+// calls whose work overlaps on the GPU — on different streams, or from
+// different host threads — race on it and must be serialised by the caller.
+// The cached address belongs to the CUDA context it was looked up in: a
+// cudaDeviceReset between calls is not supported.
 #include <mutex>
 
 #include "ice3gb_device.cuh"
@@ -31,9 +34,9 @@ int ice3gb_internal_rain_ice_with_scratch(void *handle, int nij, int nk, double 
                                           unsigned int *scratch, long scratch_points, void *stream);
 int ice3gb_internal_cuda_fail(void *handle, cudaError_t e, const char *where);
 
-// Four control words (work counter, maximum pass key, two spare) followed by
-// one pass key per grid point.
-static __device__ __align__(256) unsigned int g_rain_ice_scratch[4 + ICE3GB_NOALLOC_MAX_POINTS];
+// Four control words (work counter, maximum pass key, two spare), one pass
+// key per grid point, one processing-order word per grid point.
+static __device__ __align__(256) unsigned int g_rain_ice_scratch[4 + 2 * (size_t)ICE3GB_NOALLOC_MAX_POINTS];
 
 namespace {
 

@@ -453,14 +453,19 @@ int ice3gb_physics_step_surrogate(void *handle, void *mlp, int nij, int nk, doub
  * not allocate device memory during the call (a model that gives the GPU's
  * memory to its own pool at start-up, or runs under a device-memory cap set
  * outside the library).  Its scratch is a static device array
- * inside the library, sized for ICE3GB_NOALLOC_MAX_POINTS grid points (16 MiB
- * held on every GPU that loads the library, until exit); nij*nk above that is
- * rejected with ICE3GB_ERR_RANGE.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  Calls that overlap on the GPU share the array and race:
- * serialise them.  A table with SEDIM = SPLI (0) is refused with
- * ICE3GB_ERR_UNSUPPORTED: the time-split sedimentation needs 2 nij*nk doubles
- * of stream-ordered scratch.  No counterpart exists in the reference. */
+ * inside the library, sized for ICE3GB_NOALLOC_MAX_POINTS grid points (32 MiB:
+ * a pass key and a processing-order word per point, held on every GPU that
+ * loads the library, until exit); nij*nk above that is rejected with
+ * ICE3GB_ERR_RANGE.  The points run in the same regime order as in
+ * ice3gb_rain_ice.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture; a
+ * cudaDeviceReset between calls is not supported.  Calls that overlap on the
+ * GPU share the array and race: serialise them.  Refused with
+ * ICE3GB_ERR_UNSUPPORTED before any launch (the fields are left untouched):
+ * a table with SEDIM = SPLI (0), whose time-split sedimentation needs
+ * 2 nij*nk doubles of stream-ordered scratch, and a table with OCND2, whose
+ * level heights and droplet concentrations need as much.  No counterpart
+ * exists in the reference. */
 #define ICE3GB_NOALLOC_MAX_POINTS 4194304
 int ice3gb_rain_ice_noalloc(void *handle, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                             const Ice3gbRainIceFields *f, void *stream);

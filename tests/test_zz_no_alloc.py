@@ -117,3 +117,35 @@ def test_noalloc_refuses_time_split_sedimentation():
     assert b"SPLI" in buf.value
     torch.cuda.synchronize()
     assert torch.equal(out["rrs"], before)
+
+
+def test_noalloc_refuses_ocnd2_before_any_launch():
+    """OCND2 takes stream-ordered scratch for its level heights and droplet
+    concentrations: ICE3GB_ERR_UNSUPPORTED, and no kernel has run (the
+    sedimentation, which comes first by default, has not touched the sources
+    nor the surface precipitation)."""
+    from ice3gb import _abi
+    from ice3gb.components import Ice3Handle
+    from ice3gb.constants import build_table
+    from ice3gb.state import make_state
+
+    nij = 16 * 16
+    st = make_state(nij, NK, seed=7, precip=True, device="cuda")
+    h = Ice3Handle(build_table(table="phyex", overrides={"OCND2": 1.0}))
+    opt = _abi.RainIceOptions(-1, -1, -1, 0, 0)
+    f, out = _fields(st, nij)
+    for k in ("ssio", "ssiu", "ifr", "icldfr"):       # never read: the call is refused first
+        out[k] = torch.zeros((NK, nij), dtype=torch.float64, device="cuda")
+        setattr(f, k, ctypes.c_void_p(out[k].data_ptr()))
+    for k in ("inprc", "inprr", "inpri", "inprs", "inprg"):
+        out[k].fill_(-1.0)
+    before = {k: out[k].clone() for k in ("rcs", "rrs", "ris", "rss", "rgs", "ths", "rvs", "cit", "inprr", "inprs")}
+    rc = h.lib.ice3gb_rain_ice_noalloc(h.h, nij, NK, DT, ctypes.byref(opt), ctypes.byref(f),
+                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == -5
+    buf = ctypes.create_string_buffer(256)
+    h.lib.ice3gb_last_error(h.h, buf, 256)
+    assert b"OCND2" in buf.value
+    torch.cuda.synchronize()
+    for k, v in before.items():
+        assert torch.equal(out[k], v), k

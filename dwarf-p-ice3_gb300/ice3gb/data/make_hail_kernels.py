@@ -39,7 +39,7 @@ def parse(path: str, name: str, shape):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--micro", default="/root/reference/PHYEX-IAL_CY50T1/micro")
+    ap.add_argument("--micro", required=True, help="the reference's PHYEX-IAL_CY50T1/micro directory")
     ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "hail_kernels.npz"))
     args = ap.parse_args()
     out = {}

@@ -21,7 +21,9 @@ import numpy as np
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    ap.add_argument("--reference-src", default=os.environ.get("ICE3GB_REFERENCE_SRC"),
+                    required="ICE3GB_REFERENCE_SRC" not in os.environ,
+                    help="the reference's src/ directory (or set ICE3GB_REFERENCE_SRC)")
     ap.add_argument("--program", default="AROME")
     ap.add_argument("--out", default=None)
     args = ap.parse_args()

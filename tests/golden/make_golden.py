@@ -256,7 +256,9 @@ def tiwmx_case(Phyex):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    ap.add_argument("--reference-src", default=os.environ.get("ICE3GB_REFERENCE_SRC"),
+                    required="ICE3GB_REFERENCE_SRC" not in os.environ,
+                    help="the reference's src/ directory (or set ICE3GB_REFERENCE_SRC)")
     ap.add_argument("--only", nargs="*", default=None, help="write only these golden files (names without .npz)")
     args = ap.parse_args()
     import refshim

@@ -6,7 +6,8 @@ import pytest
 
 from ice3gb.constants import CONSTANT_NAMES, build_table, load_snapshot, luts_arrays
 
-REF_SRC = "/root/reference/src"
+# the reference's src/ directory, when a checkout is at hand
+REF_SRC = os.environ.get("ICE3GB_REFERENCE_SRC", "")
 
 
 def test_snapshot_has_every_constant():
@@ -26,7 +27,7 @@ def test_snapshot_has_every_constant():
     assert L["ker_raccss"][0, 0] == pytest.approx(7.78513)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference checkout not mounted")
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="ICE3GB_REFERENCE_SRC names no reference checkout")
 def test_snapshot_equals_reference_phyex():
     import sys
     sys.path.insert(0, REF_SRC)

@@ -1514,6 +1514,109 @@ static void ice4_slopes(Tctx *x)
 /* ICE4_TENDENCIES (mode_ice4_tendencies.F90:150-717) for one point.
  * `vart` is the state at the start of the pass (PVART), `t` = th*exn.
  * Outputs A (rates) and B (instantaneous increments). */
+/* The aggregation of ICE4_TENDENCIES (mode_ice4_tendencies.F90:606-717):
+ * the rates b[] of one pass into the tendencies A[] (per second) and the
+ * instantaneous changes B[], with the OCND2 rows (RVDEPI, RILARS, the
+ * graupel deposition split depg_s / nodepg_s) and the KRR = 7 rows.  The
+ * NRR = 6 rows are those of ice4_total_tendencies_update
+ * (src/ice3/jax/stencils/ice4_tendencies.py:330-441). */
+static void ice4_aggregate(const double *b, double lsfact, double lvfact, int ocnd2, double depg_s,
+                           double nodepg_s, int hail, double A[NVH], double B[NVH])
+{
+  const double lsv = lsfact - lvfact;
+  A[ITH] += b[B_RVDEPG] * lsfact;
+  A[ITH] += b[B_RCHONI] * lsv;
+  A[ITH] += b[B_RVDEPS] * lsfact;
+  A[ITH] -= b[B_RREVAV] * lvfact;
+  A[ITH] += b[B_RCRIMSS] * lsv;
+  A[ITH] += b[B_RCRIMSG] * lsv;
+  A[ITH] += b[B_RRACCSS] * lsv;
+  A[ITH] += b[B_RRACCSG] * lsv;
+  A[ITH] += (b[B_RRCFRIG] - b[B_RICFRR]) * lsv;
+  A[ITH] += (b[B_RCWETG] + b[B_RRWETG]) * lsv;
+  A[ITH] += (b[B_RCDRYG] + b[B_RRDRYG]) * lsv;
+  A[ITH] -= b[B_RGMLTR] * lsv;
+  A[ITH] += b[B_RCBERI] * lsv;
+  A[IRV] -= b[B_RVDEPG];
+  A[IRV] -= b[B_RVDEPS];
+  A[IRV] += b[B_RREVAV];
+  A[IRC] -= b[B_RCHONI];
+  A[IRC] -= b[B_RCAUTR];
+  A[IRC] -= b[B_RCACCR];
+  A[IRC] -= b[B_RCRIMSS];
+  A[IRC] -= b[B_RCRIMSG];
+  A[IRC] -= b[B_RCMLTSR];
+  A[IRC] -= b[B_RCWETG];
+  A[IRC] -= b[B_RCDRYG];
+  A[IRC] -= b[B_RCBERI];
+  A[IRR] += b[B_RCAUTR];
+  A[IRR] += b[B_RCACCR];
+  A[IRR] -= b[B_RREVAV];
+  A[IRR] -= b[B_RRACCSS];
+  A[IRR] -= b[B_RRACCSG];
+  A[IRR] += b[B_RCMLTSR];
+  A[IRR] = A[IRR] - b[B_RRCFRIG] + b[B_RICFRR];
+  A[IRR] -= b[B_RRWETG];
+  A[IRR] -= b[B_RRDRYG];
+  A[IRR] += b[B_RGMLTR];
+  A[IRI] += b[B_RCHONI];
+  A[IRI] -= b[B_RIAGGS];
+  A[IRI] -= b[B_RIAUTS];
+  A[IRI] = A[IRI] - b[B_RICFRRG] - b[B_RICFRR];
+  A[IRI] -= b[B_RIWETG];
+  A[IRI] -= b[B_RIDRYG];
+  A[IRI] += b[B_RCBERI];
+  A[IRS] += b[B_RVDEPS];
+  A[IRS] += b[B_RIAGGS];
+  A[IRS] += b[B_RIAUTS];
+  A[IRS] += b[B_RCRIMSS];
+  A[IRS] -= b[B_RSRIMCG];
+  A[IRS] += b[B_RRACCSS];
+  A[IRS] -= b[B_RSACCRG];
+  A[IRS] -= b[B_RSMLTG];
+  A[IRS] -= b[B_RSWETG];
+  A[IRS] -= b[B_RSDRYG];
+  A[IRG] += ocnd2 ? b[B_RVDEPG] * nodepg_s : b[B_RVDEPG];         /* :693 */
+  A[IRG] += b[B_RCRIMSG] + b[B_RSRIMCG];
+  A[IRG] += b[B_RRACCSG] + b[B_RSACCRG];
+  A[IRG] += b[B_RSMLTG];
+  A[IRG] += b[B_RICFRRG] + b[B_RRCFRIG];
+  A[IRG] += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
+  A[IRG] += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
+  A[IRG] -= b[B_RGMLTR];
+  if (ocnd2) {                                                        /* OCND2 rows */
+    A[ITH] += b[B_RVDEPI] * lsfact;                                   /* :625 */
+    A[IRV] -= b[B_RVDEPI];                                            /* :630 */
+    A[IRI] += b[B_RVDEPI];                                            /* :673-674 */
+    A[IRI] -= b[B_RILARS];
+    A[IRS] += b[B_RVDEPG] * depg_s;                                   /* :677 */
+    A[IRS] += b[B_RILARS];                                            /* :691 */
+  }
+  if (hail) {                                                         /* KRR = 7 rows */
+    A[ITH] += (b[B_RRWETH] + b[B_RCWETH]) * lsv;                      /* :620-622 */
+    A[ITH] += (b[B_RCDRYH] + b[B_RRDRYH]) * lsv;
+    A[ITH] -= b[B_RHMLTR] * lsv;
+    A[IRC] -= b[B_RCWETH];                                            /* :641-642 */
+    A[IRC] -= b[B_RCDRYH];
+    A[IRR] -= b[B_RRWETH];                                            /* :657-659 */
+    A[IRR] -= b[B_RRDRYH];
+    A[IRR] += b[B_RHMLTR];
+    A[IRI] -= b[B_RIWETH];                                            /* :669-670 */
+    A[IRI] -= b[B_RIDRYH];
+    A[IRS] -= b[B_RSWETH];                                            /* :688-689 */
+    A[IRS] -= b[B_RSDRYH];
+    A[IRG] -= b[B_RWETGH];                                            /* :699-700 */
+    B[IRG] -= b[B_RWETGH_MR];
+    A[IRG] -= b[B_RGWETH];                                            /* :704-705 */
+    A[IRG] = A[IRG] - b[B_RGDRYH] + b[B_RDRYHG];
+    A[IRH] += b[B_RWETGH];                                            /* :709-715 */
+    B[IRH] += b[B_RWETGH_MR];
+    A[IRH] = A[IRH] + b[B_RCWETH] + b[B_RIWETH] + b[B_RSWETH] + b[B_RGWETH] + b[B_RRWETH];
+    A[IRH] = A[IRH] + b[B_RCDRYH] + b[B_RIDRYH] + b[B_RSDRYH] + b[B_RRDRYH] + b[B_RGDRYH] - b[B_RDRYHG];
+    A[IRH] -= b[B_RHMLTR];
+  }
+}
+
 static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int ldcompute,
                             double exn, double rhodref, double lvfact, double lsfact, double pres,
                             double cf, double sigma_rc, double *cit, double t, const double vart[NVH],
@@ -1601,101 +1704,43 @@ static void ice4_tendencies(const C *c, const Ice3gbLuts *lut, int ldsoft, int l
     }
     ice4_fast_ri_rs(&x, pr, *cit);
   }
-  /* :606-717 aggregation (KRR = 6, LOCND2 = .FALSE.) */
-  const double lsv = lsfact - lvfact;
-  A[ITH] += b[B_RVDEPG] * lsfact;
-  A[ITH] += b[B_RCHONI] * lsv;
-  A[ITH] += b[B_RVDEPS] * lsfact;
-  A[ITH] -= b[B_RREVAV] * lvfact;
-  A[ITH] += b[B_RCRIMSS] * lsv;
-  A[ITH] += b[B_RCRIMSG] * lsv;
-  A[ITH] += b[B_RRACCSS] * lsv;
-  A[ITH] += b[B_RRACCSG] * lsv;
-  A[ITH] += (b[B_RRCFRIG] - b[B_RICFRR]) * lsv;
-  A[ITH] += (b[B_RCWETG] + b[B_RRWETG]) * lsv;
-  A[ITH] += (b[B_RCDRYG] + b[B_RRDRYG]) * lsv;
-  A[ITH] -= b[B_RGMLTR] * lsv;
-  A[ITH] += b[B_RCBERI] * lsv;
-  A[IRV] -= b[B_RVDEPG];
-  A[IRV] -= b[B_RVDEPS];
-  A[IRV] += b[B_RREVAV];
-  A[IRC] -= b[B_RCHONI];
-  A[IRC] -= b[B_RCAUTR];
-  A[IRC] -= b[B_RCACCR];
-  A[IRC] -= b[B_RCRIMSS];
-  A[IRC] -= b[B_RCRIMSG];
-  A[IRC] -= b[B_RCMLTSR];
-  A[IRC] -= b[B_RCWETG];
-  A[IRC] -= b[B_RCDRYG];
-  A[IRC] -= b[B_RCBERI];
-  A[IRR] += b[B_RCAUTR];
-  A[IRR] += b[B_RCACCR];
-  A[IRR] -= b[B_RREVAV];
-  A[IRR] -= b[B_RRACCSS];
-  A[IRR] -= b[B_RRACCSG];
-  A[IRR] += b[B_RCMLTSR];
-  A[IRR] = A[IRR] - b[B_RRCFRIG] + b[B_RICFRR];
-  A[IRR] -= b[B_RRWETG];
-  A[IRR] -= b[B_RRDRYG];
-  A[IRR] += b[B_RGMLTR];
-  A[IRI] += b[B_RCHONI];
-  A[IRI] -= b[B_RIAGGS];
-  A[IRI] -= b[B_RIAUTS];
-  A[IRI] = A[IRI] - b[B_RICFRRG] - b[B_RICFRR];
-  A[IRI] -= b[B_RIWETG];
-  A[IRI] -= b[B_RIDRYG];
-  A[IRI] += b[B_RCBERI];
-  A[IRS] += b[B_RVDEPS];
-  A[IRS] += b[B_RIAGGS];
-  A[IRS] += b[B_RIAUTS];
-  A[IRS] += b[B_RCRIMSS];
-  A[IRS] -= b[B_RSRIMCG];
-  A[IRS] += b[B_RRACCSS];
-  A[IRS] -= b[B_RSACCRG];
-  A[IRS] -= b[B_RSMLTG];
-  A[IRS] -= b[B_RSWETG];
-  A[IRS] -= b[B_RSDRYG];
-  A[IRG] += x.tw ? b[B_RVDEPG] * nodepg_s : b[B_RVDEPG];         /* :693 */
-  A[IRG] += b[B_RCRIMSG] + b[B_RSRIMCG];
-  A[IRG] += b[B_RRACCSG] + b[B_RSACCRG];
-  A[IRG] += b[B_RSMLTG];
-  A[IRG] += b[B_RICFRRG] + b[B_RRCFRIG];
-  A[IRG] += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
-  A[IRG] += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
-  A[IRG] -= b[B_RGMLTR];
-  if (x.tw) {                                                         /* OCND2 rows */
-    A[ITH] += b[B_RVDEPI] * lsfact;                                   /* :625 */
-    A[IRV] -= b[B_RVDEPI];                                            /* :630 */
-    A[IRI] += b[B_RVDEPI];                                            /* :673-674 */
-    A[IRI] -= b[B_RILARS];
-    A[IRS] += b[B_RVDEPG] * depg_s;                                   /* :677 */
-    A[IRS] += b[B_RILARS];                                            /* :691 */
-  }
-  if (x.hail) {                                                       /* KRR = 7 rows */
-    A[ITH] += (b[B_RRWETH] + b[B_RCWETH]) * lsv;                      /* :620-622 */
-    A[ITH] += (b[B_RCDRYH] + b[B_RRDRYH]) * lsv;
-    A[ITH] -= b[B_RHMLTR] * lsv;
-    A[IRC] -= b[B_RCWETH];                                            /* :641-642 */
-    A[IRC] -= b[B_RCDRYH];
-    A[IRR] -= b[B_RRWETH];                                            /* :657-659 */
-    A[IRR] -= b[B_RRDRYH];
-    A[IRR] += b[B_RHMLTR];
-    A[IRI] -= b[B_RIWETH];                                            /* :669-670 */
-    A[IRI] -= b[B_RIDRYH];
-    A[IRS] -= b[B_RSWETH];                                            /* :688-689 */
-    A[IRS] -= b[B_RSDRYH];
-    A[IRG] -= b[B_RWETGH];                                            /* :699-700 */
-    B[IRG] -= b[B_RWETGH_MR];
-    A[IRG] -= b[B_RGWETH];                                            /* :704-705 */
-    A[IRG] = A[IRG] - b[B_RGDRYH] + b[B_RDRYHG];
-    A[IRH] += b[B_RWETGH];                                            /* :709-715 */
-    B[IRH] += b[B_RWETGH_MR];
-    A[IRH] = A[IRH] + b[B_RCWETH] + b[B_RIWETH] + b[B_RSWETH] + b[B_RGWETH] + b[B_RRWETH];
-    A[IRH] = A[IRH] + b[B_RCDRYH] + b[B_RIDRYH] + b[B_RSDRYH] + b[B_RRDRYH] + b[B_RGDRYH] - b[B_RDRYHG];
-    A[IRH] -= b[B_RHMLTR];
-  }
+  /* :606-717 aggregation */
+  ice4_aggregate(b, lsfact, lvfact, x.tw != NULL, depg_s, nodepg_s, x.hail, A, B);
   *rainfr = x.rainfr;
   for (int k = 0; k < 4; ++k) { hl[k] = x.hl[k]; hi[k] = x.hi[k]; }
+}
+
+/* The sub-step limits of ICE4_STEPPING.  limit_feedback: with LFEEDBACKT,
+ * no sub-step across theta = TT/exn (zx), mode_ice4_stepping.F90:284-299,
+ * the temperature part of ice4_step_limiter (src/ice3/jax/stencils/
+ * ice4_stepping.py:109-194).  limit_depletion: a species that is present
+ * (r > rsmin) and depleting (A < -1e-20) ends the sub-step where it reaches
+ * zero, at least MNH_TINY seconds on (:302-311). */
+static inline double limit_feedback(double zx, double th, double a, double b, double maxtime)
+{
+  if ((th - zx) * (th + b - zx) < 0.) maxtime = 0.;
+  if (fabs(a) > 1.e-20) {
+    const double thr = (zx - b - th) / a;
+    if (thr > 0.) maxtime = dmin(maxtime, thr);
+  }
+  return maxtime;
+}
+
+static inline double limit_depletion(double a, double b, double r, double rsmin, double tiny, double maxtime)
+{
+  if (a < -1.e-20 && r > rsmin) {
+    maxtime = dmin(maxtime, -(b + r) / a);
+    maxtime = dmax(maxtime, tiny);
+  }
+  return maxtime;
+}
+
+/* The state after a sub-step: x + A dt + B, in that order
+ * (mode_ice4_stepping.F90:388-395; state_update of
+ * src/ice3/jax/stencils/ice4_stepping.py:232-291). */
+static inline void state_update(int nv, double *vart, const double *A, const double *B, double maxtime)
+{
+  for (int v = 0; v < nv; ++v) vart[v] = vart[v] + A[v] * maxtime + B[v];
 }
 
 /* ICE4_STEPPING (mode_ice4_stepping.F90:139-518) restated for one packed
@@ -1778,20 +1823,10 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
       pr.tie = 0;
       for (int v = 0; v < nv; ++v) A[v] += s->extpk[v];             /* :265-272 */
       double maxtime = dt - ztime;                                    /* :275-282 */
-      if (c->LFEEDBACKT != 0.0) {                                     /* :284-299 */
-        const double zx = c->TT / exn;
-        if ((s->vart[ITH] - zx) * (s->vart[ITH] + B[ITH] - zx) < 0.) maxtime = 0.;
-        if (fabs(A[ITH]) > 1.e-20) {
-          const double thr = (zx - B[ITH] - s->vart[ITH]) / A[ITH];
-          if (thr > 0.) maxtime = dmin(maxtime, thr);
-        }
-      }
-      for (int v = 1; v < nv; ++v) {                                  /* :302-311 */
-        if (A[v] < -1.e-20 && s->vart[v] > rsmin[v]) {
-          maxtime = dmin(maxtime, -(B[v] + s->vart[v]) / A[v]);
-          maxtime = dmax(maxtime, c->MNH_TINY);
-        }
-      }
+      if (c->LFEEDBACKT != 0.0)                                       /* :284-299 */
+        maxtime = limit_feedback(c->TT / exn, s->vart[ITH], A[ITH], B[ITH], maxtime);
+      for (int v = 1; v < nv; ++v)                                    /* :302-311 */
+        maxtime = limit_depletion(A[v], B[v], s->vart[v], rsmin[v], c->MNH_TINY, maxtime);
       if (ztime + maxtime >= dt) llcompute = 0;                       /* :314-319 */
       if (c->TSTEP_TS != 0.0 && s->outer < nb_iter_max && ztime + maxtime > tlast + ztstep) {  /* :387-397 */
         maxtime = tlast - ztime + ztstep;
@@ -1824,7 +1859,7 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
         }
       }
       const double ri0 = s->vart[IRI];
-      for (int v = 0; v < nv; ++v) s->vart[v] = s->vart[v] + A[v] * maxtime + B[v];  /* :388-395 */
+      state_update(nv, s->vart, A, B, maxtime);                       /* :388-395 */
       /* the ice depleted to a rounding residual: whether CIT is reset below
        * follows the last bits of the pass (a tie, as the growth choice) */
       if (s->cit > 0. && (ri0 != 0. || B[IRI] != 0.) &&
@@ -1879,6 +1914,96 @@ static int rain_ice_sediment(const C *c, int nij, int nk, double dt, int sed_for
     if (hail) f->inprh[col] = inpr[5];
   }
   return ok;
+}
+
+/* lsfact / lvfact of RAIN_ICE at time t, without the Exner function
+ * (rain_ice.F90:334-345; rain_ice_thermo, src/ice3/jax/stencils/rain_ice.py:95). */
+static inline void rain_ice_thermo(const C *c, int hail, double t, double rv, double rc, double rr, double ri,
+                                   double rs, double rg, double rh, double *lsf, double *lvf)
+{
+  const double zrice = hail ? ri + rs + rg + rh : ri + rs + rg;
+  const double zdev = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * zrice;
+  *lsf = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
+  *lvf = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
+}
+
+/* LLMICRO without OCND2 (rain_ice.F90:370-381; rain_ice_mask,
+ * src/ice3/jax/stencils/rain_ice.py:141). */
+static inline int rain_ice_micro(const C *c, int hail, double rc, double rr, double ri, double rs, double rg,
+                                 double rh)
+{
+  return rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN || rg > c->G_RTMIN ||
+         (hail && rh > c->H_RTMIN);
+}
+
+/* Total tendencies of a micro point (rain_ice.F90:758-790, disabled in the
+ * vendored copy; rain_ice_total_tendencies, src/ice3/jax/stencils/
+ * rain_ice.py:19-92): (r_end - r_t)/dt per species, theta from L/cph (lvx,
+ * lsx: already divided by the reference Exner function), plus the RVHENI
+ * taken outside the sub-stepping.  r0: theta and the mixing ratios at t;
+ * src: the sources (src[IRH] NULL without hail). */
+static void total_tendencies(int hail, double inv, double lvx, double lsx, const double vart[NVH],
+                             const double r0[NVH], double zrvheni, double *src[NVH])
+{
+  const double wv = (vart[IRV] - r0[IRV]) * inv, wc = (vart[IRC] - r0[IRC]) * inv;
+  const double wr = (vart[IRR] - r0[IRR]) * inv, wi = (vart[IRI] - r0[IRI]) * inv;
+  const double ws = (vart[IRS] - r0[IRS]) * inv, wg = (vart[IRG] - r0[IRG]) * inv;
+  const double wh = (vart[IRH] - r0[IRH]) * inv;
+  const double wth = (wc + wr) * lvx + (hail ? wi + ws + wg + wh : wi + ws + wg) * lsx;
+  *src[ITH] += wth + zrvheni * lsx;
+  *src[IRV] += wv - zrvheni;
+  *src[IRC] += wc;
+  *src[IRR] += wr;
+  *src[IRI] += wi + zrvheni;
+  *src[IRS] += ws;
+  *src[IRG] += wg;
+  if (hail) *src[IRH] += wh;
+}
+
+/* ICE4_CORRECT_NEGATIVITIES on the sources (mode_ice4_correct_negativities.F90:
+ * 9-178): negative hydrometeors go back to vapour with theta compensated
+ * (:96-120), then vapour below XRTMIN(1) is refilled from cloud and ice in
+ * proportion (:123-136), from rain, snow, graupel and hail (:140-171).
+ * x[] = theta, rv, rc, rr, ri, rs, rg, rh sources.  The reference's JAX
+ * stencil (src/ice3/jax/stencils/ice4_correct_negativities.py:14) has the
+ * first part and only the snow and graupel lines of the second, with the
+ * snow / graupel minima as the vapour threshold: `fortran` = 0 runs that
+ * form (s_min, g_min its thresholds), 1 the Fortran (s_min = g_min =
+ * XRTMIN(1)). */
+static void correct_negativities(double s_min, double g_min, int hail, int fortran, double lvx, double lsx,
+                                 double x[NVH])
+{
+  double th = x[ITH], rv = x[IRV], rc = x[IRC], rr = x[IRR], ri = x[IRI], rs = x[IRS], rg = x[IRG];
+  double rh = hail ? x[IRH] : 0.0, w;
+  w = rc - dmax(rc, 0.); rv += w; th -= w * lvx; rc -= w;
+  w = rr - dmax(rr, 0.); rv += w; th -= w * lvx; rr -= w;
+  w = ri - dmax(ri, 0.); rv += w; th -= w * lsx; ri -= w;
+  w = rs - dmax(rs, 0.); rv += w; th -= w * lsx; rs -= w;
+  w = rg - dmax(rg, 0.); rv += w; th -= w * lsx; rg -= w;
+  if (hail) { w = rh - dmax(rh, 0.); rv += w; th -= w * lsx; rh -= w; }   /* :115-120 */
+  if (fortran) {
+    w = dmin(1., dmax(s_min - rv, 0.) / dmax(rc + ri, 1.e-20));
+    th -= w * (rc * lvx + ri * lsx);
+    rv += w * (rc + ri);
+    rc = (1. - w) * rc;
+    ri = (1. - w) * ri;
+    w = dmin(dmax(rr, 0.), dmax(s_min - rv, 0.)); rv += w; rr -= w; th -= w * lvx;
+  }
+  w = dmin(dmax(rs, 0.), dmax(s_min - rv, 0.)); rv += w; rs -= w; th -= w * lsx;
+  w = dmin(dmax(rg, 0.), dmax(g_min - rv, 0.)); rv += w; rg -= w; th -= w * lsx;
+  if (hail) { w = dmin(dmax(rh, 0.), dmax(g_min - rv, 0.)); rv += w; rh -= w; th -= w * lsx; }  /* :165-171 */
+  x[ITH] = th; x[IRV] = rv; x[IRC] = rc; x[IRR] = rr; x[IRI] = ri; x[IRS] = rs; x[IRG] = rg;
+  if (hail) x[IRH] = rh;
+}
+
+/* Fog deposition at the lowest level (rain_ice.F90:876-895; fog_deposition,
+ * src/ice3/jax/stencils/rain_ice.py:323): returns the deposit INDEP. */
+static inline double fog_deposition(const C *c, double rct, double rhodref, double dzz, double *rcs, double *inprc)
+{
+  const double indep = c->VDEPOSC * rct * rhodref / c->RHOLW;
+  *rcs -= c->VDEPOSC * rct / dzz;
+  *inprc += indep;
+  return indep;
 }
 
 static int rain_ice_supported(const C *c)
@@ -2016,14 +2141,10 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
     const double th = f->tht[p], rv = f->rvt[p], rc = f->rct[p], rr = f->rrt[p];
     const double ri = f->rit[p], rs = f->rst[p], rg = f->rgt[p], rh = hail ? f->rht[p] : 0.0;
     /* :334-345 lsfact/lvfact without exner */
-    const double zrice = hail ? ri + rs + rg + rh : ri + rs + rg;
-    const double zdev = c->CPD + c->CPV * rv + c->CL * (rc + rr) + c->CI * zrice;
     const double t = th * exn;
-    lsf[p] = (c->LSTT + (c->CPV - c->CI) * (t - c->TT)) / zdev;
-    lvf[p] = (c->LVTT + (c->CPV - c->CL) * (t - c->TT)) / zdev;
+    rain_ice_thermo(c, hail, t, rv, rc, rr, ri, rs, rg, rh, &lsf[p], &lvf[p]);
     /* :370-381 LLMICRO */
-    int micro = rc > c->C_RTMIN || rr > c->R_RTMIN || ri > c->I_RTMIN || rs > c->S_RTMIN ||
-                rg > c->G_RTMIN || (hail && rh > c->H_RTMIN);
+    int micro = rain_ice_micro(c, hail, rc, rr, ri, rs, rg, rh);
     Ocnd2Pt oc;
     if (ocnd2) {                                                      /* :347-363 */
       const double m = c->FRMIN13;
@@ -2068,21 +2189,10 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
       if (tie) tie[p] = (uint8_t)s.tie;
       key[p] = ((int64_t)s.outer << 32) | (int64_t)s.inner;
       /* 8.1 total tendencies (rain_ice.F90:758-790, disabled in the vendored copy) */
-      const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
-      const double inv = 1.0 / dt;
-      const double wv = (s.vart[IRV] - rv) * inv, wc = (s.vart[IRC] - rc) * inv;
-      const double wr = (s.vart[IRR] - rr) * inv, wi = (s.vart[IRI] - ri) * inv;
-      const double ws = (s.vart[IRS] - rs) * inv, wg = (s.vart[IRG] - rg) * inv;
-      const double wh = (s.vart[IRH] - rh) * inv;
-      const double wth = (wc + wr) * lvx + (hail ? wi + ws + wg + wh : wi + ws + wg) * lsx;
-      f->ths[p] += wth + zrvheni * lsx;
-      f->rvs[p] += wv - zrvheni;
-      f->rcs[p] += wc;
-      f->rrs[p] += wr;
-      f->ris[p] += wi + zrvheni;
-      f->rss[p] += ws;
-      f->rgs[p] += wg;
-      if (hail) f->rhs[p] += wh;
+      const double r0[NVH] = {th, rv, rc, rr, ri, rs, rg, rh};
+      double *src[NVH] = {&f->ths[p], &f->rvs[p], &f->rcs[p], &f->rrs[p], &f->ris[p], &f->rss[p], &f->rgs[p],
+                          hail ? &f->rhs[p] : NULL};
+      total_tendencies(hail, 1.0 / dt, lvf[p] / f->exnref[p], lsf[p] / f->exnref[p], s.vart, r0, zrvheni, src);
     } else {
       const double lsx = lsf[p] / f->exnref[p];
       f->ths[p] += zrvheni * lsx;
@@ -2102,37 +2212,19 @@ EXPORT int ice3o_rain_ice_ties(const C *c, const Ice3gbLuts *lut, int nij, int n
   /* 8.2 negativity correction on the sources (ICE4_CORRECT_NEGATIVITIES) */
 #pragma omp parallel for schedule(static)
   for (long p = 0; p < n; ++p) {
-    const double lsx = lsf[p] / f->exnref[p], lvx = lvf[p] / f->exnref[p];
-    double rv = f->rvs[p], rc = f->rcs[p], rr = f->rrs[p], ri = f->ris[p], rs = f->rss[p], rg = f->rgs[p];
-    double rh = hail ? f->rhs[p] : 0.0;
-    double th = f->ths[p], w;
-    w = rc - dmax(rc, 0.); rv += w; th -= w * lvx; rc -= w;
-    w = rr - dmax(rr, 0.); rv += w; th -= w * lvx; rr -= w;
-    w = ri - dmax(ri, 0.); rv += w; th -= w * lsx; ri -= w;
-    w = rs - dmax(rs, 0.); rv += w; th -= w * lsx; rs -= w;
-    w = rg - dmax(rg, 0.); rv += w; th -= w * lsx; rg -= w;
-    if (hail) { w = rh - dmax(rh, 0.); rv += w; th -= w * lsx; rh -= w; }   /* :115-120 */
-    w = dmin(1., dmax(c->V_RTMIN - rv, 0.) / dmax(rc + ri, 1.e-20));
-    th -= w * (rc * lvx + ri * lsx);
-    rv += w * (rc + ri);
-    rc = (1. - w) * rc;
-    ri = (1. - w) * ri;
-    w = dmin(dmax(rr, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rr -= w; th -= w * lvx;
-    w = dmin(dmax(rs, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rs -= w; th -= w * lsx;
-    w = dmin(dmax(rg, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rg -= w; th -= w * lsx;
-    if (hail) { w = dmin(dmax(rh, 0.), dmax(c->V_RTMIN - rv, 0.)); rv += w; rh -= w; th -= w * lsx; }  /* :165-171 */
-    f->rvs[p] = rv; f->rcs[p] = rc; f->rrs[p] = rr; f->ris[p] = ri; f->rss[p] = rs; f->rgs[p] = rg;
-    if (hail) f->rhs[p] = rh;
-    f->ths[p] = th;
+    double x[NVH] = {f->ths[p], f->rvs[p], f->rcs[p], f->rrs[p], f->ris[p], f->rss[p], f->rgs[p],
+                     hail ? f->rhs[p] : 0.0};
+    correct_negativities(c->V_RTMIN, c->V_RTMIN, hail, 1, lvf[p] / f->exnref[p], lsf[p] / f->exnref[p], x);
+    f->ths[p] = x[ITH]; f->rvs[p] = x[IRV]; f->rcs[p] = x[IRC]; f->rrs[p] = x[IRR]; f->ris[p] = x[IRI];
+    f->rss[p] = x[IRS]; f->rgs[p] = x[IRG];
+    if (hail) f->rhs[p] = x[IRH];
   }
   /* 9. sedimentation after (rain_ice.F90:816-841) */
   if (lsedim_after) sed_capped |= !rain_ice_sediment(c, nij, nk, dt, sed_fortran, has_st, f);
   /* 10. fog deposition (rain_ice.F90:876-895), level k = 0 */
   for (long col = 0; col < nij; ++col) {
     if (ldeposc) {
-      const double indep = c->VDEPOSC * f->rct[col] * f->rhodref[col] / c->RHOLW;
-      f->rcs[col] -= c->VDEPOSC * f->rct[col] / f->dzz[col];
-      f->inprc[col] += indep;
+      const double indep = fog_deposition(c, f->rct[col], f->rhodref[col], f->dzz[col], &f->rcs[col], &f->inprc[col]);
       if (f->indep) f->indep[col] = indep;
     } else if (f->indep) {
       f->indep[col] = 0.0;

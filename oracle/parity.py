@@ -35,7 +35,9 @@ def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_c
     (`scale`, optional, is the magnitude of the terms the value is a sum of),
     where `spread` is the oracle's own response to ~1e-14 input perturbations
     (points whose value comes from cancellation); at most `max_frac_conditioned`
-    of the points may need the spread term, and NaN/inf must match exactly."""
+    of the points may need the spread term, and NaN/inf must match exactly.
+
+    Returns how the points met the bound (see `allowance_stats`)."""
     got = np.asarray(got, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)
     fg, fr = np.isfinite(got), np.isfinite(ref)
@@ -51,3 +53,23 @@ def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_c
         f"{float(np.max(d / np.maximum(np.abs(r), floor_frac * rms + 1e-300))):.3e}")
     frac = 1.0 - float(np.mean(strict_ok)) if r.size else 0.0
     assert frac <= max_frac_conditioned, f"{name}: {frac:.2%} of points need the conditioning allowance"
+    return allowance_stats(d, r, base, tol, floor_frac * rms)
+
+
+def allowance_stats(d, r, base, tol, floor):
+    """How the points of one field met the parity bound:
+    n: finite points compared;
+    n_scale: points within tol of the operand scale but not of their own
+        magnitude (values that are sums of larger terms);
+    n_spread: points that needed the oracle's own conditioning spread;
+    worst_rel: max |got-ref| / max(|ref|, floor) over all points;
+    worst_excess: max |got-ref| / (tol max(|ref|, scale, floor)) over the
+        points that needed the spread (0 when none did)."""
+    own = tol * np.maximum(np.abs(r), floor)
+    n_scale = int(np.sum((d > own) & (d <= base)))
+    over = d > base
+    n_spread = int(np.sum(over))
+    worst_rel = float(np.max(d / np.maximum(np.abs(r), floor + 1e-300))) if d.size else 0.0
+    worst_excess = float(np.max(d[over] / np.maximum(base[over], 1e-300))) if n_spread else 0.0
+    return {"n": int(d.size), "n_scale": n_scale, "n_spread": n_spread, "worst_rel": worst_rel,
+            "worst_excess": worst_excess}

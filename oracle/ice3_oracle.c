@@ -1759,8 +1759,25 @@ typedef struct {
   int tie;    /* bit 0: some pass took a growth-mode decision on rounding
                residuals; bit 1: the CIT reset followed an ice residual;
                bit 2: an MRSTEP threshold fell on the chosen sub-step;
-               bit 3: a hard pass followed a bit-1 reset */
+               bit 3: a hard pass followed a bit-1 reset;
+               bit 4: a depleted species ended a pass at a rounding residual
+               whose comparison with XRTMIN decides a MNH_TINY pass */
 } StepOut;
+
+/* Depletion ties (StepOut.tie bit 4): a species whose depletion limit was
+ * evaluated in a pass (present, A < -1e-20) ends the pass at r + A t + B = 0
+ * in exact arithmetic when that limit bound the sub-step; the computed value
+ * is a rounding residual, and whether it is above XRTMIN decides whether the
+ * next pass is one more MNH_TINY step (mode_ice4_stepping.F90:302-311).  At
+ * the 1000/s cap of RCHONI that step moves 2.2e-13 kg/kg, so an evaluation
+ * whose rates differ in the last bits (FMA contraction) can land on the other
+ * side.  g_depl_flip is a bit mask: with bit k-1 set the oracle takes the
+ * other outcome at the k-th such decision of every point (a residual above
+ * XRTMIN becomes 0, one at or below it becomes 2 XRTMIN), so that the
+ * branches can be enumerated. */
+static int g_depl_flip = 0;
+
+EXPORT void ice3o_set_depletion_flip(int k) { g_depl_flip = k; }
 
 static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, int max_passes,
                                 double exn, double rhodref, double pres, double cf, double sigma_rc,
@@ -1798,6 +1815,7 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
     nb_iter_max = nb_iter_max > nb ? nb_iter_max : nb;
   }
   double z0rt[NVH], tlast = 0.0;
+  int depl_events = 0;
   while (ztime < dt) {                                                /* :204 */
     s->outer++;                                                       /* IITER, :258-266 */
     /* a hard pass after a rounding-decided CIT reset (MRSTEP / TSTEP_TS
@@ -1859,7 +1877,19 @@ static void ice4_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
         }
       }
       const double ri0 = s->vart[IRI];
+      double rstart[NVH];
+      for (int v = 0; v < nv; ++v) rstart[v] = s->vart[v];
       state_update(nv, s->vart, A, B, maxtime);                       /* :388-395 */
+      for (int v = 1; v < nv; ++v) {                                  /* depletion ties (bit 4) */
+        if (!(A[v] < -1.e-20 && rstart[v] > rsmin[v])) continue;
+        const double noise = 4.0 * 2.220446049250313e-16 * (fabs(rstart[v]) + fabs(B[v]) + fabs(A[v] * maxtime));
+        if (noise > rsmin[v] && fabs(s->vart[v]) <= noise) {
+          s->tie |= 16;
+          if (depl_events < 31 && ((g_depl_flip >> depl_events) & 1))
+            s->vart[v] = s->vart[v] > rsmin[v] ? 0.0 : 2.0 * rsmin[v];
+          ++depl_events;
+        }
+      }
       /* the ice depleted to a rounding residual: whether CIT is reset below
        * follows the last bits of the pass (a tie, as the growth choice) */
       if (s->cit > 0. && (ri0 != 0. || B[IRI] != 0.) &&
@@ -2502,4 +2532,103 @@ EXPORT int ice3o_stepping_point(const C *c, const Ice3gbLuts *lut, double dt, in
   out[7] = s.cit; out[8] = s.rrevav; out[9] = s.capped;
   *outer = s.outer; *inner = s.inner;
   return 0;
+}
+
+/* ===================================================================== */
+/* RAIN_ICE / ICE4_STEPPING pieces for the golden-vector tests            */
+/* (each entry point runs the routine the oracle's rain_ice runs)         */
+/* ===================================================================== */
+
+/* rain_ice_thermo + rain_ice_mask (NRR = 6): lsfact / lvfact without the
+ * Exner function and LLMICRO, from T and the mixing ratios. */
+EXPORT void ice3o_rain_ice_thermo(const C *c, long n, const double *t, const double *rv, const double *rc,
+                                  const double *rr, const double *ri, const double *rs, const double *rg,
+                                  double *lsf, double *lvf, uint8_t *micro)
+{
+  for (long p = 0; p < n; ++p) {
+    rain_ice_thermo(c, 0, t[p], rv[p], rc[p], rr[p], ri[p], rs[p], rg[p], 0.0, &lsf[p], &lvf[p]);
+    micro[p] = (uint8_t)rain_ice_micro(c, 0, rc[p], rr[p], ri[p], rs[p], rg[p], 0.0);
+  }
+}
+
+/* Total tendencies of micro points (NRR = 6).  vend / r0: [7][n] theta and
+ * mixing ratios at the end of the sub-stepping / at t; src: [7][n] sources,
+ * updated in place. */
+EXPORT void ice3o_total_tendencies(long n, double dt, const double *vend, const double *r0, const double *lvx,
+                                   const double *lsx, const double *rvheni, double *src)
+{
+  for (long p = 0; p < n; ++p) {
+    double ve[NVH], r[NVH];
+    double *s[NVH];
+    for (int v = 0; v < NV; ++v) { ve[v] = vend[v * n + p]; r[v] = r0[v * n + p]; s[v] = &src[v * n + p]; }
+    ve[IRH] = r[IRH] = 0.0;
+    s[IRH] = NULL;
+    total_tendencies(0, 1.0 / dt, lvx[p], lsx[p], ve, r, rvheni[p], s);
+  }
+}
+
+/* The aggregation of one pass (NRR = 6, no OCND2): bu [NBU][n] rates, A
+ * [7][n] tendencies out (from zero). */
+EXPORT void ice3o_aggregate(long n, const double *bu, const double *lsfact, const double *lvfact, double *A_out)
+{
+  for (long p = 0; p < n; ++p) {
+    double b[NBU], A[NVH] = {0}, B[NVH] = {0};
+    for (int k = 0; k < NBU; ++k) b[k] = bu[k * n + p];
+    ice4_aggregate(b, lsfact[p], lvfact[p], 0, 0.0, 1.0, 0, A, B);
+    for (int v = 0; v < NV; ++v) A_out[v * n + p] = A[v];
+  }
+}
+
+/* The sub-step length of one pass (NRR = 6): the time left (dt - t_micro,
+ * 0 where ldcompute is off), the LFEEDBACKT limit, the depletion limits
+ * with the thresholds rsmin[7]; llcompute_out: the pass does not reach dt.
+ * vart, A, B: [7][n]. */
+EXPORT void ice3o_step_limiter(const C *c, long n, double dt, const double *rsmin, const double *exn,
+                               const double *vart, const double *A, const double *B, const double *t_micro,
+                               const uint8_t *ldcompute, double *maxtime, uint8_t *llcompute_out)
+{
+  for (long p = 0; p < n; ++p) {
+    double m = ldcompute[p] ? dt - t_micro[p] : 0.0;
+    if (c->LFEEDBACKT != 0.0) m = limit_feedback(c->TT / exn[p], vart[p], A[p], B[p], m);
+    for (int v = 1; v < NV; ++v) m = limit_depletion(A[v * n + p], B[v * n + p], vart[v * n + p], rsmin[v], c->MNH_TINY, m);
+    maxtime[p] = m;
+    llcompute_out[p] = (uint8_t)(ldcompute[p] && !(t_micro[p] + m >= dt));
+  }
+}
+
+/* The state update of one sub-step and the reset of the ice concentration
+ * where the ice is gone (mode_ice4_stepping.F90:388-401); vart [7][n] and
+ * cit updated in place. */
+EXPORT void ice3o_state_update(long n, const double *A, const double *B, const double *dt_micro,
+                               const uint8_t *ldmicro, double *vart, double *cit)
+{
+  for (long p = 0; p < n; ++p) {
+    double v[NVH], a[NVH], b[NVH];
+    for (int k = 0; k < NV; ++k) { v[k] = vart[k * n + p]; a[k] = A[k * n + p]; b[k] = B[k * n + p]; }
+    state_update(NV, v, a, b, dt_micro[p]);
+    for (int k = 0; k < NV; ++k) vart[k * n + p] = v[k];
+    if (ldmicro[p] && v[IRI] <= 0.) cit[p] = 0.;
+  }
+}
+
+/* ICE4_CORRECT_NEGATIVITIES (NRR = 6) on x [7][n] in place; fortran = 1:
+ * the Fortran form with the vapour threshold XRTMIN(1) (s_min = g_min =
+ * V_RTMIN), 0: the reference JAX stencil's form with its thresholds. */
+EXPORT void ice3o_correct_negativities(long n, int fortran, double s_min, double g_min, const double *lvx,
+                                       const double *lsx, double *x)
+{
+  for (long p = 0; p < n; ++p) {
+    double v[NVH];
+    for (int k = 0; k < NV; ++k) v[k] = x[k * n + p];
+    v[IRH] = 0.0;
+    correct_negativities(s_min, g_min, 0, fortran, lvx[p], lsx[p], v);
+    for (int k = 0; k < NV; ++k) x[k * n + p] = v[k];
+  }
+}
+
+/* Fog deposition on n columns (their lowest level). */
+EXPORT void ice3o_fog_deposition(const C *c, long n, const double *rct, const double *rhodref, const double *dzz,
+                                 double *rcs, double *inprc)
+{
+  for (long p = 0; p < n; ++p) (void)fog_deposition(c, rct[p], rhodref[p], dzz[p], &rcs[p], &inprc[p]);
 }

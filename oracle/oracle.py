@@ -220,6 +220,38 @@ def rain_ice(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float, lsedim
     return out, bits.value
 
 
+def rain_ice_depletion_alternatives(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float,
+                                    masks=(1, 2, 3), **kw):
+    """Oracle rain_ice with other outcomes of its depletion ties: for each bit
+    mask, the k-th rounding-decided MNH_TINY-pass decision of every point
+    (bit k-1 set) takes the other branch (ice3o_set_depletion_flip).  Returns
+    the list of output dicts, one per mask."""
+    lib = load()
+    outs = []
+    try:
+        for m in masks:
+            lib.ice3o_set_depletion_flip(int(m))
+            outs.append(rain_ice(table, st, dt, **kw)[0])
+    finally:
+        lib.ice3o_set_depletion_flip(0)
+    return outs
+
+
+def physics_step_depletion_alternatives(table: ConstantsTable, st: Dict[str, np.ndarray], dt: float,
+                                        masks=(1, 2, 3), **kw):
+    """physics_step with the depletion-tie outcomes of
+    rain_ice_depletion_alternatives."""
+    lib = load()
+    outs = []
+    try:
+        for m in masks:
+            lib.ice3o_set_depletion_flip(int(m))
+            outs.append(physics_step(table, st, dt, **kw)[0])
+    finally:
+        lib.ice3o_set_depletion_flip(0)
+    return outs
+
+
 # ---- per-process entry points (hard pass) --------------------------------
 
 def nucleation(table, tht, pabst, rhodref, exn, lsfact, t, rvt, cit, ldcompute):

@@ -28,7 +28,8 @@ def sensitivity(fn, inputs, rel=1e-13, trials=3, seed=0):
     return base, spread
 
 
-def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_conditioned=0.01, scale=None):
+def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_conditioned=0.01, scale=None,
+                  alts=()):
     """Parity of a device field against the oracle.
 
     Every point must satisfy |got-ref| <= tol*max(|ref|, scale, floor) + 4*spread,
@@ -36,6 +37,9 @@ def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_c
     where `spread` is the oracle's own response to ~1e-14 input perturbations
     (points whose value comes from cancellation); at most `max_frac_conditioned`
     of the points may need the spread term, and NaN/inf must match exactly.
+    `alts`: the oracle's outputs with other outcomes of its rounding-decided
+    branches (the depletion ties of the sub-stepping); a point that meets
+    tol*max(|alt|, scale, floor) for one of them needs no spread.
 
     Returns how the points met the bound (see `allowance_stats`)."""
     got = np.asarray(got, dtype=np.float64)
@@ -44,32 +48,45 @@ def assert_parity(got, ref, spread, name, tol=1e-10, floor_frac=1e-5, max_frac_c
     assert np.array_equal(fg, fr), f"{name}: non-finite values differ"
     g, r, s = got[fr], ref[fr], np.asarray(spread, dtype=np.float64)[fr]
     rms = float(np.sqrt(np.mean(r * r))) if r.size else 0.0
-    mag = np.abs(r) if scale is None else np.maximum(np.abs(r), np.asarray(scale, dtype=np.float64)[fr])
+    sc = None if scale is None else np.asarray(scale, dtype=np.float64)[fr]
+    mag = np.abs(r) if sc is None else np.maximum(np.abs(r), sc)
     base = tol * np.maximum(mag, floor_frac * rms)
     d = np.abs(g - r)
-    strict_ok = d <= base
-    assert np.all(d <= base + 4.0 * s), (
-        f"{name}: {int(np.sum(d > base + 4 * s))} points beyond tolerance, worst rel "
-        f"{float(np.max(d / np.maximum(np.abs(r), floor_frac * rms + 1e-300))):.3e}")
-    frac = 1.0 - float(np.mean(strict_ok)) if r.size else 0.0
+    alt_ok = np.zeros(d.shape, dtype=bool)
+    for a in alts:
+        a = np.asarray(a, dtype=np.float64)[fr]
+        amag = np.abs(a) if sc is None else np.maximum(np.abs(a), sc)
+        alt_ok |= np.abs(g - a) <= tol * np.maximum(amag, floor_frac * rms)
+    ok = (d <= base) | alt_ok
+    assert np.all(ok | (d <= base + 4.0 * s)), (
+        f"{name}: {int(np.sum(~ok & (d > base + 4 * s)))} points beyond tolerance, worst rel "
+        f"{float(np.max(np.where(ok, 0.0, d) / np.maximum(np.abs(r), floor_frac * rms + 1e-300))):.3e}")
+    frac = 1.0 - float(np.mean(ok)) if r.size else 0.0
     assert frac <= max_frac_conditioned, f"{name}: {frac:.2%} of points need the conditioning allowance"
-    return allowance_stats(d, r, base, tol, floor_frac * rms)
+    return allowance_stats(d, r, base, tol, floor_frac * rms, alt_ok)
 
 
-def allowance_stats(d, r, base, tol, floor):
+def allowance_stats(d, r, base, tol, floor, alt_ok=None):
     """How the points of one field met the parity bound:
     n: finite points compared;
     n_scale: points within tol of the operand scale but not of their own
         magnitude (values that are sums of larger terms);
+    n_alt: points within tol of another outcome of the oracle's
+        rounding-decided branches (and not of the first);
     n_spread: points that needed the oracle's own conditioning spread;
-    worst_rel: max |got-ref| / max(|ref|, floor) over all points;
+    worst_rel: max |got-ref| / max(|ref|, floor) over the points matched
+        without an alternative outcome;
     worst_excess: max |got-ref| / (tol max(|ref|, scale, floor)) over the
         points that needed the spread (0 when none did)."""
+    if alt_ok is None:
+        alt_ok = np.zeros(d.shape, dtype=bool)
     own = tol * np.maximum(np.abs(r), floor)
     n_scale = int(np.sum((d > own) & (d <= base)))
-    over = d > base
+    n_alt = int(np.sum((d > base) & alt_ok))
+    over = (d > base) & ~alt_ok
     n_spread = int(np.sum(over))
-    worst_rel = float(np.max(d / np.maximum(np.abs(r), floor + 1e-300))) if d.size else 0.0
+    rel = np.where(alt_ok & (d > base), 0.0, d) / np.maximum(np.abs(r), floor + 1e-300)
+    worst_rel = float(np.max(rel)) if d.size else 0.0
     worst_excess = float(np.max(d[over] / np.maximum(base[over], 1e-300))) if n_spread else 0.0
-    return {"n": int(d.size), "n_scale": n_scale, "n_spread": n_spread, "worst_rel": worst_rel,
+    return {"n": int(d.size), "n_scale": n_scale, "n_alt": n_alt, "n_spread": n_spread, "worst_rel": worst_rel,
             "worst_excess": worst_excess}

@@ -124,6 +124,9 @@ def _oracle_ri(table, st, **kw):
         ref["_scale"][s_] = np.abs(abi[s_]) + np.abs(ref[s_]) + (np.abs(f) + np.abs(fa)) / rhodz
     for s_ in ("ths", "rvs"):
         ref["_scale"][s_] = np.abs(abi[s_]) + np.abs(ref[s_])
+    # the other outcomes of the depletion ties (a rounding residual against
+    # XRTMIN deciding one more MNH_TINY pass)
+    ref["_alts"] = oracle.rain_ice_depletion_alternatives(table, abi, DT, **kw)
     return ref, spread
 
 
@@ -134,7 +137,8 @@ def _compare(out, ref, spread, skip=()):
     for mine, theirs in pairs.items():
         if mine in skip:
             continue
-        assert_parity(out[mine], ref[theirs], spread[theirs], mine, scale=ref["_scale"].get(theirs))
+        assert_parity(out[mine], ref[theirs], spread[theirs], mine, scale=ref["_scale"].get(theirs),
+                      alts=[a[theirs] for a in ref["_alts"]])
 
 
 @pytest.mark.parametrize("seed,nij", [(0, 32 * 32), (3, 64 * 64)])

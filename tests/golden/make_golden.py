@@ -3,7 +3,8 @@
 Runs maurinl26/dwarf-p-ice3's own JAX implementation, unmodified, in float64
 through the numpy stand-in of refshim.py:
 
-* ``IceAdjustJAX.__call__``            (src/ice3/jax/ice_adjust.py:139)
+* ``IceAdjustJAX.__call__``            (src/ice3/jax/ice_adjust.py:139), also on the
+  states of the reference's own tests (tests/components/test_ice_adjust_jax.py)
 * ``sedimentation_stat``               (src/ice3/jax/stencils/sedimentation.py:58)
 * the ICE4 process stencils            (src/ice3/jax/stencils/ice4_*.py), hard pass
 * ``ice4_derived_fields`` / ``ice4_slope_parameters`` (stencils/ice4_tendencies.py:191,248)
@@ -11,6 +12,11 @@ through the numpy stand-in of refshim.py:
 * ``ice4_warm`` with the CLFR / PRFR evaporation options (stencils/ice4_warm.py:15)
 * the SRC_1D table                     (phyex_common/lookup_table.py:4)
 * ``e_sat_w`` / ``e_sat_i`` on the TIWMX grid (jax/functions/tiwmx.py:18,60)
+* the RAIN_ICE / ICE4_STEPPING stencils: ``rain_ice_thermo``, ``rain_ice_mask``,
+  ``rain_ice_total_tendencies``, ``fog_deposition`` (stencils/rain_ice.py),
+  ``ice4_total_tendencies_update`` (stencils/ice4_tendencies.py:330),
+  ``ice4_step_limiter``, ``state_update`` (stencils/ice4_stepping.py:109,232),
+  ``ice4_correct_negativities`` (stencils/ice4_correct_negativities.py:14)
 
 Inputs are seeded synthetic states (ice3gb.state.make_state) and seeded
 random point sets; both inputs and reference outputs are stored.
@@ -235,6 +241,189 @@ def warm_subg_case(mods, Phyex):
     return {"warm_subg": rec}
 
 
+def rain_ice_pieces_case(Phyex):
+    """The RAIN_ICE / ICE4_STEPPING stencils of the reference JAX on seeded
+    random points (src/ice3/jax/stencils/rain_ice.py:19, :95, :141, :323;
+    stencils/ice4_tendencies.py:330; stencils/ice4_stepping.py:59, :109,
+    :232; stencils/ice4_correct_negativities.py:14).
+
+    Where the JAX stencil and the Fortran ICE4_STEPPING differ (the JAX
+    depletion limit is the time to reach XRTMIN from (r_min - r - b) / a for
+    growing or present species; the Fortran one the time to reach zero of a
+    present, depleting species), the inputs are drawn inside the set where
+    both give the same answer: every r > 0, instantaneous changes b >= 0,
+    vapour never depleting, thresholds r_min = 0 passed to the JAX.  The JAX
+    negativity correction refills vapour from snow and graupel only, up to
+    their own minima: case A has vapour far above every threshold (the
+    Fortran refill lines do nothing), case B pins the JAX form itself."""
+    import ice3.jax.stencils.ice4_correct_negativities as neg
+    import ice3.jax.stencils.ice4_stepping as stp
+    import ice3.jax.stencils.ice4_tendencies as tend
+    import ice3.jax.stencils.rain_ice as rit
+
+    ext = dict(Phyex("AROME", TSTEP=DT).to_externals())
+    rng = np.random.default_rng(55)
+    n = 1024
+    rec = {}
+
+    def mix(lo=-8, hi=-2, pzero=0.3, size=n):
+        v = 10 ** rng.uniform(lo, hi, size)
+        return np.where(rng.random(size) < pzero, 0.0, v)
+
+    # thermo + mask
+    t = rng.uniform(215.0, 305.0, n)
+    exn = rng.uniform(0.6, 1.02, n)
+    th = t / exn
+    r = {k: mix() for k in ("rv", "rc", "rr", "ri", "rs", "rg")}
+    r["rv"] = 10 ** rng.uniform(-6, -1.8, n)
+    for k in ("rc", "rr", "ri", "rs", "rg"):        # a few values right at and below the thresholds
+        r[k] = np.where(rng.random(n) < 0.05, ext[k[1].upper() + "_RTMIN"] * rng.choice([0.5, 1.0, 2.0], n), r[k])
+    ls, lv = rit.rain_ice_thermo(_shim(exn), _shim(th), *(_shim(r[k]) for k in ("rv", "rc", "rr", "ri", "rs", "rg")),
+                                 ext)
+    mask = rit.rain_ice_mask(*(_shim(r[k]) for k in ("rc", "rr", "ri", "rs", "rg")), ext)
+    rec.update(th_exn=exn, th_th=th, **{f"th_{k}": v for k, v in r.items()}, th_out_ls=ls, th_out_lv=lv,
+               th_out_mask=np.asarray(mask, dtype=np.float64))
+
+    # total tendencies: end-of-step values near the start values
+    names = ("th", "v", "c", "r", "i", "s", "g")
+    r0 = {"th": th, "v": r["rv"], "c": r["rc"], "r": r["rr"], "i": r["ri"], "s": r["rs"], "g": r["rg"]}
+    wr = {k: v * (1.0 + rng.uniform(-0.5, 0.5, n)) for k, v in r0.items()}
+    src = {k: rng.uniform(-1e-6, 1e-6, n) for k in names}
+    src["th"] = rng.uniform(-1e-2, 1e-2, n)
+    rvheni = mix(-12, -7, 0.5)
+    lsx, lvx = np.asarray(ls) / exn, np.asarray(lv) / exn
+    ext_t = dict(ext, INV_TSTEP=1.0 / DT)
+    res = rit.rain_ice_total_tendencies(*(_shim(wr[k]) for k in names), _shim(lsx), _shim(lvx), _shim(exn),
+                                        *(_shim(src[k]) for k in names), _shim(rvheni),
+                                        *(_shim(r0[k]) for k in names[1:]), ext_t)
+    rec.update({f"tt_wr_{k}": wr[k] for k in names})
+    rec.update({f"tt_src_{k}": src[k] for k in names})
+    rec.update(tt_rvheni=rvheni, tt_lsx=lsx, tt_lvx=lvx)
+    for k, v in zip(("th", "v", "c", "r", "i", "s", "g"), res[7:]):
+        rec[f"tt_out_{k}"] = np.asarray(v, dtype=np.float64)
+
+    # fog deposition on the lowest level of (1, n, 2) columns
+    rcs3 = rng.uniform(-1e-7, 1e-6, (1, n, 2))
+    rct3 = np.stack([mix(-8, -3, 0.3), mix(-8, -3, 0.3)], axis=-1)[None]
+    rho3 = rng.uniform(0.3, 1.3, (1, n, 2))
+    dz3 = rng.uniform(10.0, 300.0, (1, n, 2))
+    inprc = rng.uniform(0.0, 1e-6, (1, n))
+    fr, fi = rit.fog_deposition(_shim(rcs3), _shim(rct3), _shim(rho3), _shim(dz3), _shim(inprc), ext)
+    rec.update(fog_rcs=rcs3[0, :, 0], fog_rct=rct3[0, :, 0], fog_rho=rho3[0, :, 0], fog_dzz=dz3[0, :, 0],
+               fog_inprc=inprc[0], fog_out_rcs=np.asarray(fr)[0, :, 0], fog_out_inprc=np.asarray(fi)[0])
+
+    # aggregation of one pass
+    rate_names = ("rchoni", "rvdeps", "riaggs", "riauts", "rvdepg", "rcautr", "rcaccr", "rrevav", "rcberi",
+                  "rsmltg", "rcmltsr", "rraccss", "rraccsg", "rsaccrg", "rcrimss", "rcrimsg", "rsrimcg",
+                  "ricfrrg", "rrcfrig", "ricfrr", "rcwetg", "riwetg", "rrwetg", "rswetg", "rcdryg", "ridryg",
+                  "rrdryg", "rsdryg", "rgmltr")
+    rates = {k: mix(-12, -5, 0.4) for k in rate_names}
+    rates["rvdeps"] = np.where(rng.random(n) < 0.3, -rates["rvdeps"], rates["rvdeps"])   # sublimation
+    rates["rvdepg"] = np.where(rng.random(n) < 0.3, -rates["rvdepg"], rates["rvdepg"])
+    z = np.zeros(n)
+    res = tend.ice4_total_tendencies_update(_shim(lsx), _shim(lvx), *([_shim(z)] * 7),
+                                            *(_shim(rates[k]) for k in rate_names))
+    rec.update({f"ag_{k}": v for k, v in rates.items()})
+    rec.update(ag_ls=lsx, ag_lv=lvx)
+    for k, v in zip(names, res):
+        rec[f"ag_out_{k}"] = np.asarray(v, dtype=np.float64)
+
+    # step limiter and state update
+    sp = ("c", "r", "i", "s", "g")
+    rt = {k: 10 ** rng.uniform(-9, -3, n) for k in sp}
+    a = {k: np.where(rng.random(n) < 0.2, 0.0, rng.choice([-1.0, 1.0], n) * 10 ** rng.uniform(-9, -5, n))
+         for k in sp}
+    b = {k: np.where(rng.random(n) < 0.5, 0.0, 10 ** rng.uniform(-10, -4, n)) for k in sp}
+    a_th = np.where(rng.random(n) < 0.2, 0.0, rng.uniform(-2e-3, 2e-3, n))
+    b_th = np.where(rng.random(n) < 0.5, 0.0, rng.uniform(-0.5, 0.5, n))
+    th_s = ext["TT"] / exn + rng.uniform(-1.0, 1.0, n)          # around the 0 C crossing
+    t_micro = np.where(rng.random(n) < 0.5, 0.0, rng.uniform(0.0, DT, n))
+    ld = rng.random(n) < 0.9
+    ext0 = dict(ext, C_RTMIN=0.0, R_RTMIN=0.0, I_RTMIN=0.0, S_RTMIN=0.0, G_RTMIN=0.0)
+    dtm, ld_new = stp.ice4_step_limiter(_shim(exn), _shim(th_s), _shim(a_th), _shim(b_th),
+                                        *(_shim(rt[k]) for k in sp), *(_shim(a[k]) for k in sp),
+                                        *(_shim(b[k]) for k in sp), _shim(t_micro), ld, DT, ext0)
+    rec.update(sl_exn=exn, sl_th=th_s, sl_a_th=a_th, sl_b_th=b_th, sl_t_micro=t_micro,
+               sl_ld=ld.astype(np.float64), sl_out_dt=np.asarray(dtm, dtype=np.float64),
+               sl_out_ld=np.asarray(ld_new, dtype=np.float64))
+    rec.update({f"sl_r{k}": rt[k] for k in sp})
+    rec.update({f"sl_a{k}": a[k] for k in sp})
+    rec.update({f"sl_b{k}": b[k] for k in sp})
+    ci = np.where(rng.random(n) < 0.3, 0.0, 10 ** rng.uniform(2, 6, n))
+    rt_u = {k: np.where(rng.random(n) < 0.2, -rt[k] * 0.5, rt[k]) for k in sp}    # some depletions below zero
+    res = stp.state_update(_shim(th_s), _shim(a_th), _shim(b_th), *(_shim(rt_u[k]) for k in sp),
+                           *(_shim(a[k]) for k in sp), *(_shim(-np.abs(b[k])) for k in sp), _shim(ci),
+                           _shim(np.asarray(dtm)), ld)
+    rec.update({f"su_r{k}": rt_u[k] for k in sp})
+    rec.update(su_ci=ci)
+    for k, v in zip(("th", "c", "r", "i", "s", "g", "ci"), res):
+        rec[f"su_out_{k}"] = np.asarray(v, dtype=np.float64)
+
+    # negativity correction, case A (vapour far above every threshold) and B (vapour near zero)
+    for case, rv_neg in (("A", 10 ** rng.uniform(-5, -2, n)), ("B", rng.uniform(-1e-9, 1e-14, n))):
+        # case A: the negative parts (at most 5e-6 in all) stay below the vapour (at least 1e-5)
+        hi = -6.0 if case == "A" else -4.0
+        x = {k: rng.choice([-1.0, 1.0], n) * mix(-10, hi, 0.2) for k in ("rc", "rr", "ri", "rs", "rg")}
+        if case == "B":
+            for k in ("rs", "rg"):
+                x[k] = np.abs(x[k])
+        th_n = rng.uniform(250.0, 320.0, n)
+        res = neg.ice4_correct_negativities(_shim(th_n), _shim(rv_neg), *(_shim(x[k]) for k in ("rc", "rr", "ri",
+                                            "rs", "rg")), _shim(lvx), _shim(lsx), ext)
+        rec.update({f"cn{case}_{k}": v for k, v in x.items()})
+        rec.update({f"cn{case}_th": th_n, f"cn{case}_rv": rv_neg})
+        for k, v in zip(("th", "rv", "rc", "rr", "ri", "rs", "rg"), res):
+            rec[f"cn{case}_out_{k}"] = np.asarray(v, dtype=np.float64)
+    rec["cn_lsx"], rec["cn_lvx"] = lsx, lvx
+    return {"ri_pieces": rec}
+
+
+def reference_fixture_states():
+    """The ice_adjust states of the reference's own component tests
+    (tests/components/test_ice_adjust_jax.py): `simple_test_data` (:30-69),
+    `realistic_test_data` (:72-151) and the supersaturated state of
+    `test_cloud_formation` (:285-318), restated with numpy; timestep 60 s,
+    Phyex("AROME", TSTEP=60)."""
+    zero = ("rc", "ri", "rr", "rs", "rg", "cf_mf", "rc_mf", "ri_mf", "rvs", "rcs", "ris", "ths")
+
+    def uniform(shape, th, rv):
+        st = dict(sigqsat=np.full(shape, 0.01), pabs=np.full(shape, 85000.0), sigs=np.full(shape, 0.1),
+                  th=np.full(shape, th), exn=np.full(shape, 0.95), exn_ref=np.full(shape, 0.95),
+                  rho_dry_ref=np.ones(shape), rv=np.full(shape, rv))
+        st.update({k: np.zeros(shape) for k in zero})
+        return st
+
+    nx, ny, nz = 10, 10, 20
+    z = np.linspace(0.0, 10000.0, nz)
+    p0, t0, gamma = 101325.0, 288.15, 0.0065
+    pabs = np.tile(p0 * (1 - gamma * z / t0) ** 5.26, (nx, ny, 1))
+    temp = np.tile(t0 - gamma * z, (nx, ny, 1))
+    exn = (pabs / 100000.0) ** (287.0 / 1004.0)
+    real = dict(sigqsat=np.full((nx, ny, nz), 0.01), pabs=pabs, sigs=np.full((nx, ny, nz), 0.1), th=temp / exn,
+                exn=exn, exn_ref=exn, rho_dry_ref=pabs / (287.0 * temp),
+                rv=np.tile(0.015 * np.exp(-z / 2000.0), (nx, ny, 1)),
+                rc=np.where(np.tile((z > 2000.0) & (z < 6000.0), (nx, ny, 1)), 0.001, 0.0),
+                ri=np.where(np.tile(z > 5000.0, (nx, ny, 1)), 0.0005, 0.0))
+    real.update({k: np.zeros((nx, ny, nz)) for k in zero if k not in ("rc", "ri")})
+    return {"simple": uniform((5, 5, 10), 285.0, 0.010), "realistic": real,
+            "cloud_formation": uniform((5, 5, 10), 280.0, 0.020)}
+
+
+def ia_fixtures_case(IceAdjustJAX, Phyex):
+    """IceAdjustJAX (jit off) on the reference test states, timestep 60 s."""
+    ia = IceAdjustJAX(Phyex("AROME", TSTEP=60.0), jit=False)
+    names = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv",
+             "ls", "rvs", "rcs", "ris", "ths")
+    rec = {}
+    for cname, st in reference_fixture_states().items():
+        res = ia(**{k: _shim(v) for k, v in st.items()}, timestep=60.0)
+        for k, v in st.items():
+            rec[f"{cname}_in_{k}"] = v
+        for n, r in zip(names, res):
+            rec[f"{cname}_out_{n}"] = np.asarray(r, dtype=np.float64)
+    return {"ia_fixtures": rec}
+
+
 def src_1d_case():
     """The SRC_1D table of the reference (src/ice3/phyex_common/lookup_table.py:4)."""
     from ice3.phyex_common.lookup_table import SRC_1D
@@ -290,6 +479,8 @@ def main():
     blobs.update(warm_subg_case(mods, Phyex))
     blobs.update(src_1d_case())
     blobs.update(tiwmx_case(Phyex))
+    blobs.update(rain_ice_pieces_case(Phyex))
+    blobs.update(ia_fixtures_case(IceAdjustJAX, Phyex))
     for name, rec in blobs.items():
         if args.only is not None and name not in args.only:
             continue

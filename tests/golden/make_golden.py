@@ -12,6 +12,8 @@ through the numpy stand-in of refshim.py:
 * ``ice4_warm`` with the CLFR / PRFR evaporation options (stencils/ice4_warm.py:15)
 * the SRC_1D table                     (phyex_common/lookup_table.py:4)
 * ``e_sat_w`` / ``e_sat_i`` on the TIWMX grid (jax/functions/tiwmx.py:18,60)
+* centred differences of ``IceAdjustJAX`` and ``sedimentation_stat`` for the
+  adjoint checks
 * the RAIN_ICE / ICE4_STEPPING stencils: ``rain_ice_thermo``, ``rain_ice_mask``,
   ``rain_ice_total_tendencies``, ``fog_deposition`` (stencils/rain_ice.py),
   ``ice4_total_tendencies_update`` (stencils/ice4_tendencies.py:330),
@@ -424,6 +426,71 @@ def ia_fixtures_case(IceAdjustJAX, Phyex):
     return {"ia_fixtures": rec}
 
 
+def adjoint_fd_case(IceAdjustJAX, sedimentation_stat, Phyex):
+    """Reference directional derivatives for the adjoint checks: centred
+    differences (h = 1e-7, relative directions N(0,1)|x|) of the reference's
+    own IceAdjustJAX and sedimentation_stat run in FP64.  ice_adjust: 32
+    columns x 90 levels, N(0,1) cotangents on T, rv, rc, ri and cloud
+    fraction (sigqsat held fixed), the sources scaled by U[0.5, 1.5] off the
+    kink of the source limiter; J = <g, y> per point at x + h dx, x, x - h dx.
+    Sedimentation (JAX semantics): 24 columns, cotangents on the five sources
+    and the surface precipitation, J per column."""
+    from ice3gb.state import make_state
+    h = 1e-7
+    rec = {}
+    ia = IceAdjustJAX(Phyex("AROME", TSTEP=DT), jit=False)
+    st = _np(make_state(32, 90, seed=31, precip=True))
+    rng = np.random.default_rng(66)
+    ins = ("sigqsat", "pabs", "sigs", "th", "exn", "exn_ref", "rho_dry_ref", "rv", "rc", "ri", "rr", "rs", "rg",
+           "cf_mf", "rc_mf", "ri_mf", "rvs", "rcs", "ris", "ths")
+    outs = ("t", "rv_out", "rc_out", "ri_out", "cldfr", "hlc_hrc", "hlc_hcf", "hli_hri", "hli_hcf", "cph", "lv",
+            "ls", "rvs", "rcs", "ris", "ths")
+    shape = st["th"].shape
+    x = {k: st[k] for k in ins if k != "sigqsat"}
+    x["sigqsat"] = np.broadcast_to(st["sigqsat"][None, :], shape).copy()
+    for k in ("rvs", "rcs", "ris", "ths"):
+        x[k] = x[k] * rng.uniform(0.5, 1.5, shape)
+    dx = {k: rng.standard_normal(shape) * np.abs(v) for k, v in x.items()}
+    dx["sigqsat"][:] = 0.0
+    g = {k: rng.standard_normal(shape) for k in ("t", "rv_out", "rc_out", "ri_out", "cldfr")}
+
+    def j_ia(xx):
+        y = dict(zip(outs, ia(**{k: _shim(v) for k, v in xx.items()}, timestep=DT)))
+        return sum(g[k] * np.asarray(y[k], dtype=np.float64) for k in g)
+    for tag, sgn in (("p", 1.0), ("0", 0.0), ("m", -1.0)):
+        rec[f"ia_j{tag}"] = j_ia({k: v + sgn * h * dx[k] for k, v in x.items()})
+    rec.update({f"ia_x_{k}": v for k, v in x.items()})
+    rec.update({f"ia_dx_{k}": v for k, v in dx.items()})
+    rec.update({f"ia_g_{k}": v for k, v in g.items()})
+
+    ext = dict(Phyex("AROME", TSTEP=DT).to_externals())
+    ext.update(LBC_LAND=ext["LBC_1"], LBC_SEA=ext["LBC_2"], FSEDC_LAND=ext["FSEDC_1"], FSEDC_SEA=ext["FSEDC_2"])
+    st = _np(make_state(24, 90, seed=32, precip=True))
+    nk, nij = st["pabs"].shape
+    sx = {"rhodref": st["rho_dry_ref"], "dzz": st["dzz"], "pabs": st["pabs"], "tht": st["th"]}
+    for k, r in (("rcs", "rc"), ("rrs", "rr"), ("ris", "ri"), ("rss", "rs"), ("rgs", "rg")):
+        sx[k] = st[r] / DT * rng.uniform(0.5, 1.5, (nk, nij))
+    sdx = {k: rng.standard_normal((nk, nij)) * np.abs(v) for k, v in sx.items()}
+    src = ("rcs", "rrs", "ris", "rss", "rgs")
+    gs = {k: rng.standard_normal((nk, nij)) for k in src}
+    gp = {k: rng.standard_normal(nij) for k in ("inprc", "inprr", "inpri", "inprs", "inprg")}
+    z = np.zeros(nij)
+    T = lambda a: _shim(np.ascontiguousarray(a.T[None, :, :]))
+
+    def j_sed(xx):
+        res = sedimentation_stat(*(T(xx[k]) for k in ("rhodref", "dzz", "pabs", "tht") + src), _shim(z[None, :, None]),
+                                 _shim(z[None, :, None]), ext)
+        y = [np.asarray(r, dtype=np.float64)[0] for r in res]
+        j = sum((gs[k] * y[i].T).sum(axis=0) for i, k in enumerate(src))
+        return j + sum(gp[k] * y[10 + i] for i, k in enumerate(gp))
+    for tag, sgn in (("p", 1.0), ("0", 0.0), ("m", -1.0)):
+        rec[f"sed_j{tag}"] = j_sed({k: v + sgn * h * sdx[k] for k, v in sx.items()})
+    rec.update({f"sed_x_{k}": v for k, v in sx.items()})
+    rec.update({f"sed_dx_{k}": v for k, v in sdx.items()})
+    rec.update({f"sed_g_{k}": v for k, v in {**gs, **gp}.items()})
+    return {"adjoint_fd": rec}
+
+
 def src_1d_case():
     """The SRC_1D table of the reference (src/ice3/phyex_common/lookup_table.py:4)."""
     from ice3.phyex_common.lookup_table import SRC_1D
@@ -481,6 +548,7 @@ def main():
     blobs.update(tiwmx_case(Phyex))
     blobs.update(rain_ice_pieces_case(Phyex))
     blobs.update(ia_fixtures_case(IceAdjustJAX, Phyex))
+    blobs.update(adjoint_fd_case(IceAdjustJAX, sedimentation_stat, Phyex))
     for name, rec in blobs.items():
         if args.only is not None and name not in args.only:
             continue

@@ -212,3 +212,59 @@ def test_sedimentation_adjoint_matches_finite_differences(sedlib, fortran):
         fd = sum(float(np.sum(g[k] * (yp[k] - ym[k]))) for k in g) / (2 * h)
         scale = sum(float(np.sum(np.abs(gx[k] * dx[k]))) for k in subset)
         assert abs(ad - fd) <= 1e-6 * max(scale, 1e-300), (subset, ad, fd)
+
+
+# ---- against the reference's own derivatives (tests/golden/adjoint_fd.npz) ----
+
+def _reference_fd(g, prefix, h=1e-7):
+    jp, j0, jm = (np.asarray(g[f"{prefix}_j{t}"]).ravel() for t in "p0m")
+    noise = 4e-16 * (np.abs(j0) + np.abs(jp) + np.abs(jm)) / h
+    return (jp - jm) / (2 * h), smooth_points(jp, j0, jm, h), noise
+
+
+def reference_ice_adjust_check(ad, g):
+    """Adjoint directional derivatives against the centred differences of the
+    reference IceAdjustJAX: every smooth point within 1e-6."""
+    fd, smooth, noise = _reference_fd(g, "ia")
+    assert_mostly_smooth(ad, smooth, "ice_adjust vs reference")
+    rel = np.abs(ad - fd) / (np.abs(ad) + noise)
+    assert rel[smooth].max() <= 1e-6, rel[smooth].max()
+    return rel[smooth]
+
+
+def reference_sedimentation_check(ad, g):
+    fd, smooth, noise = _reference_fd(g, "sed")
+    assert_mostly_smooth(ad, smooth, "sedimentation vs reference")
+    rel = np.abs(ad - fd) / (np.abs(ad) + noise)
+    assert rel[smooth].max() <= 1e-6, rel[smooth].max()
+    return rel[smooth]
+
+
+def test_ice_adjust_adjoint_matches_reference_differences(lib):
+    """The adjoint (host build) against centred differences of the
+    reference's own IceAdjustJAX in FP64 (h = 1e-7, relative directions,
+    N(0,1) cotangents on T, rv, rc, ri, cloud fraction; 32 x 90 points)."""
+    from conftest import load_golden
+    from ice3gb.constants import build_table
+    g = load_golden("adjoint_fd")
+    table = build_table(table="jax")
+    x = {k: g[f"ia_x_{k}"] for k in IN}
+    dx = {k: g[f"ia_dx_{k}"] for k in IN}
+    gx = vjp(lib, table, x, {k: g[f"ia_g_{k}"] for k in ("t", "rv_out", "rc_out", "ri_out", "cldfr")})
+    ad = sum(gx[k].reshape(x[k].shape) * dx[k] for k in IN).ravel()
+    reference_ice_adjust_check(ad, g)
+
+
+def test_sedimentation_adjoint_matches_reference_differences(sedlib):
+    """The reverse sweep (host build, the reference JAX semantics) against
+    centred differences of the reference's own sedimentation_stat in FP64,
+    per column (24 columns x 90 levels)."""
+    from conftest import load_golden
+    from ice3gb.constants import build_table
+    g = load_golden("adjoint_fd")
+    table = build_table(table="jax")
+    sin = ("rhodref", "dzz", "pabs", "tht") + SRC
+    x = {k: g[f"sed_x_{k}"] for k in sin}
+    gx = sed_vjp(sedlib, table, x, {k: g[f"sed_g_{k}"] for k in SRC + INPR}, False)
+    ad = sum((gx[k] * g[f"sed_dx_{k}"]).sum(axis=0) for k in sin)
+    reference_sedimentation_check(ad, g)

@@ -107,3 +107,26 @@ def test_sedimentation_autograd_matches_finite_differences():
             ym = sedimentation(sed, DT, **{k: v - h * dx[k] for k, v in x.items()})
         fd = sum(float((g[k] * (yp[k] - ym[k])).sum()) for k in outs) / (2 * h)
         assert abs(ad - fd) <= 1e-6 * scale, (semantics, ad, fd, scale)
+
+
+def test_adjoints_match_reference_differences():
+    """The device adjoints through torch.autograd against centred differences
+    of the reference's own IceAdjustJAX and sedimentation_stat (FP64, h = 1e-7;
+    tests/golden/adjoint_fd.npz): every smooth point within 1e-6."""
+    from conftest import load_golden
+    from ice3gb import IceAdjust, Sedimentation
+    from ice3gb.autodiff import ice_adjust, sedimentation
+    g = load_golden("adjoint_fd")
+    x = {k: torch.as_tensor(g[f"ia_x_{k}"]).cuda().requires_grad_(True) for k in H.IN}
+    y = ice_adjust(IceAdjust(), DT, **x)
+    sum((y[k] * torch.as_tensor(g[f"ia_g_{k}"]).cuda()).sum() for k in TARGETS).backward()
+    ad = sum(x[k].grad.cpu().numpy() * g[f"ia_dx_{k}"] for k in H.IN).ravel()
+    H.reference_ice_adjust_check(ad, g)
+
+    sin = ("rhodref", "dzz", "pabs", "tht") + H.SRC
+    sx = {k: torch.as_tensor(g[f"sed_x_{k}"]).cuda().requires_grad_(True) for k in sin}
+    ys = sedimentation(Sedimentation(semantics="jax"), DT, **sx)
+    loss = sum((ys[k] * torch.as_tensor(g[f"sed_g_{k}"]).cuda()).sum() for k in H.SRC + H.INPR)
+    loss.backward()
+    ad = sum((sx[k].grad.cpu().numpy() * g[f"sed_dx_{k}"]).sum(axis=0) for k in sin)
+    H.reference_sedimentation_check(ad, g)

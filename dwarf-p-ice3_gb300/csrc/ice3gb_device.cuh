@@ -85,6 +85,19 @@ ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
 ICE3_HD bool zerod_(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) == 0; }
 // |a| > b for b >= +0.
 ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > fm::bits_(b); }
+// a != 0 (nor -0), on the bit pattern.
+ICE3_HD bool nz(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) != 0; }
+// True on every lane when the predicate holds on some active lane of the warp:
+// a block of arithmetic that is exact when skipped on lanes whose inputs are
+// zero runs for the warp or for none of it (the host build: the lane alone).
+ICE3_HD bool warp_any(bool p)
+{
+#if defined(__CUDA_ARCH__)
+  return __any_sync(__activemask(), p);
+#else
+  return p;
+#endif
+}
 
 // x**a evaluated as exp(a*log(x)) with the FP64-lean exp/log of
 // fastmath.cuh.  For the exponents of the scheme (|a*log x| < 60) this stays

@@ -272,7 +272,11 @@ ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit,
     }
   }
   hl[0] = hcf; hl[1] = lcf; hl[2] = hrc; hl[3] = lrc;
-  criauti = dmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+  // the ice threshold matters where the ice is present, or with the CLFR ice
+  // partition (criauti * cf); with NONE and no ice it is never read
+  criauti = c.CRIAUTI;
+  if (warp_any(aucv_ri != 0 || gtp(rit, c.I_RTMIN)))
+    criauti = dmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
   double ihcf = 0, ilcf = 0, ihri = 0, ilri = 0;
   if (aucv_ri == 0) {
     if (gtd(rit, criauti)) { ihcf = 1.0; ihri = rit; }
@@ -862,34 +866,106 @@ ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, d
     b[B_RCDRYG] = b[B_RRDRYG] = b[B_RIDRYG] = b[B_RSDRYG] = 0.0;
   }
   const double lsv = lsfact - lvfact;
-  A[ITH] = b[B_RVDEPG] * lsfact + b[B_RCHONI] * lsv + b[B_RVDEPS] * lsfact - b[B_RREVAV] * lvfact +
-           b[B_RCRIMSS] * lsv + b[B_RCRIMSG] * lsv + b[B_RRACCSS] * lsv + b[B_RRACCSG] * lsv +
-           (b[B_RRCFRIG] - b[B_RICFRR]) * lsv + (b[B_RCWETG] + b[B_RRWETG]) * lsv +
-           (b[B_RCDRYG] + b[B_RRDRYG]) * lsv - b[B_RGMLTR] * lsv + b[B_RCBERI] * lsv;
-  A[IRV] = -b[B_RVDEPG] - b[B_RVDEPS] + b[B_RREVAV];
-  A[IRC] = -b[B_RCHONI] - b[B_RCAUTR] - b[B_RCACCR] - b[B_RCRIMSS] - b[B_RCRIMSG] - b[B_RCMLTSR] - b[B_RCWETG] -
-           b[B_RCDRYG] - b[B_RCBERI];
-  A[IRR] = b[B_RCAUTR] + b[B_RCACCR] - b[B_RREVAV] - b[B_RRACCSS] - b[B_RRACCSG] + b[B_RCMLTSR] - b[B_RRCFRIG] +
-           b[B_RICFRR] - b[B_RRWETG] - b[B_RRDRYG] + b[B_RGMLTR];
-  A[IRI] = b[B_RCHONI] - b[B_RIAGGS] - b[B_RIAUTS] - b[B_RICFRRG] - b[B_RICFRR] - b[B_RIWETG] - b[B_RIDRYG] +
-           b[B_RCBERI];
-  A[IRS] = b[B_RVDEPS] + b[B_RIAGGS] + b[B_RIAUTS] + b[B_RCRIMSS] - b[B_RSRIMCG] + b[B_RRACCSS] - b[B_RSACCRG] -
-           b[B_RSMLTG] - b[B_RSWETG] - b[B_RSDRYG];
+  // The aggregation (mode_ice4_tendencies.F90:606-717) written as transfers:
+  // every rate moves water from one species to another (and theta by L/cph),
+  // one block per group of processes; a block runs when a lane of the warp
+  // has a nonzero rate in it (on a pass about 3 of the 29 rates are nonzero,
+  // and the points of a warp share their regime).
   double depg_s = 0.0, nodepg_s = 1.0;
   if (O && gtd(c.FRMIN5, 1.0e-12) && gtd(c.FRMIN6, 0.01)) {
     depg_s = dmax(0., dmin(1., (c.FRMIN5 - fm::fdiv(v[IRG], c.FRMIN5)))) * dmax(0., dmin(1., fm::fdiv(R.ssi, c.FRMIN6)));
     nodepg_s = 1. - depg_s;
   }
-  A[IRG] = (O ? b[B_RVDEPG] * nodepg_s : b[B_RVDEPG]) + b[B_RCRIMSG] + b[B_RSRIMCG] + b[B_RRACCSG] + b[B_RSACCRG] +
-           b[B_RSMLTG] + b[B_RICFRRG] + b[B_RRCFRIG] + b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG] +
-           b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG] - b[B_RGMLTR];
+  double ath = 0.0, av = 0.0, ac = 0.0, ar = 0.0, ai = 0.0, as = 0.0, ag = 0.0;
+  if (warp_any(nz(b[B_RVDEPG]))) {                                  // vapour -> graupel (and snow, OCND2)
+    const double x = b[B_RVDEPG];
+    ath += x * lsfact;
+    av -= x;
+    if (O) { ag += x * nodepg_s; as += x * depg_s; }
+    else ag += x;
+  }
+  if (warp_any(nz(b[B_RVDEPS]))) {                                  // vapour -> snow
+    const double x = b[B_RVDEPS];
+    ath += x * lsfact;
+    av -= x;
+    as += x;
+  }
+  if (warp_any(nz(b[B_RREVAV]))) {                                  // rain -> vapour
+    const double x = b[B_RREVAV];
+    ath -= x * lvfact;
+    av += x;
+    ar -= x;
+  }
+  if (warp_any(nz(b[B_RCHONI]) || nz(b[B_RCBERI]))) {               // cloud -> ice
+    const double x = b[B_RCHONI] + b[B_RCBERI];
+    ath += x * lsv;
+    ac -= x;
+    ai += x;
+  }
+  if (warp_any(nz(b[B_RCAUTR]) || nz(b[B_RCACCR]) || nz(b[B_RCMLTSR]))) {   // cloud -> rain
+    const double x = b[B_RCAUTR] + b[B_RCACCR] + b[B_RCMLTSR];
+    ac -= x;
+    ar += x;
+  }
+  if (warp_any(nz(b[B_RIAGGS]) || nz(b[B_RIAUTS]))) {               // ice -> snow
+    const double x = b[B_RIAGGS] + b[B_RIAUTS];
+    ai -= x;
+    as += x;
+  }
+  if (warp_any(nz(b[B_RCRIMSS]) || nz(b[B_RCRIMSG]) || nz(b[B_RSRIMCG]))) {  // riming
+    const double x = b[B_RCRIMSS] + b[B_RCRIMSG];
+    ath += x * lsv;
+    ac -= x;
+    as += b[B_RCRIMSS] - b[B_RSRIMCG];
+    ag += b[B_RCRIMSG] + b[B_RSRIMCG];
+  }
+  if (warp_any(nz(b[B_RRACCSS]) || nz(b[B_RRACCSG]) || nz(b[B_RSACCRG]))) {  // rain accretion on snow
+    const double x = b[B_RRACCSS] + b[B_RRACCSG];
+    ath += x * lsv;
+    ar -= x;
+    as += b[B_RRACCSS] - b[B_RSACCRG];
+    ag += b[B_RRACCSG] + b[B_RSACCRG];
+  }
+  if (warp_any(nz(b[B_RICFRRG]) || nz(b[B_RRCFRIG]) || nz(b[B_RICFRR]))) {   // rain contact freezing
+    ath += (b[B_RRCFRIG] - b[B_RICFRR]) * lsv;
+    ar += b[B_RICFRR] - b[B_RRCFRIG];
+    ai -= b[B_RICFRRG] + b[B_RICFRR];
+    ag += b[B_RICFRRG] + b[B_RRCFRIG];
+  }
+  if (warp_any(nz(b[B_RCWETG]) || nz(b[B_RRWETG]) || nz(b[B_RIWETG]) || nz(b[B_RSWETG]))) {  // graupel wet growth
+    ath += (b[B_RCWETG] + b[B_RRWETG]) * lsv;
+    ac -= b[B_RCWETG];
+    ar -= b[B_RRWETG];
+    ai -= b[B_RIWETG];
+    as -= b[B_RSWETG];
+    ag += b[B_RCWETG] + b[B_RIWETG] + b[B_RSWETG] + b[B_RRWETG];
+  }
+  if (warp_any(nz(b[B_RCDRYG]) || nz(b[B_RRDRYG]) || nz(b[B_RIDRYG]) || nz(b[B_RSDRYG]))) {  // graupel dry growth
+    ath += (b[B_RCDRYG] + b[B_RRDRYG]) * lsv;
+    ac -= b[B_RCDRYG];
+    ar -= b[B_RRDRYG];
+    ai -= b[B_RIDRYG];
+    as -= b[B_RSDRYG];
+    ag += b[B_RCDRYG] + b[B_RIDRYG] + b[B_RSDRYG] + b[B_RRDRYG];
+  }
+  if (warp_any(nz(b[B_RSMLTG]))) {                                  // snow -> graupel (melting conversion)
+    as -= b[B_RSMLTG];
+    ag += b[B_RSMLTG];
+  }
+  if (warp_any(nz(b[B_RGMLTR]))) {                                  // graupel -> rain
+    const double x = b[B_RGMLTR];
+    ath -= x * lsv;
+    ar += x;
+    ag -= x;
+  }
+  A[ITH] = ath; A[IRV] = av; A[IRC] = ac; A[IRR] = ar; A[IRI] = ai; A[IRS] = as; A[IRG] = ag;
   if (O) {
-    // OCND2 rows (mode_ice4_tendencies.F90:625, 630, 673-677, 691)
+    // OCND2 rows (mode_ice4_tendencies.F90:625, 630, 673-674, 691; the
+    // graupel deposition given to snow, :677, is in the block above)
     A[ITH] += orr->rvdepi * lsfact;
     A[IRV] -= orr->rvdepi;
     A[IRI] += orr->rvdepi;
     A[IRI] -= orr->rilars;
-    A[IRS] += b[B_RVDEPG] * depg_s;
     A[IRS] += orr->rilars;
   }
   if (H) {
@@ -1142,8 +1218,10 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
 #pragma unroll
       for (int v = 0; v < NVT; ++v) A[v] += ext[v];
       double maxtime = dt - ztime;
+      // B (the instantaneous changes) is zero on soft passes: no theta jump
+      // across TT/exn, no B in the depletion limits and the state update
       if (c.LFEEDBACKT != 0.0) {
-        if (negd((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx))) maxtime = 0.;
+        if (!soft && negd((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx))) maxtime = 0.;
         if (abs_gtp(A[ITH], 1.e-20)) {
           const double thr = (zx - B[ITH] - vart[ITH]) / A[ITH];
           if (pos(thr)) maxtime = dmin(maxtime, thr);
@@ -1187,8 +1265,13 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       // cap of RCHONI that quantum moves 2.2e-13 kg/kg, so the rounding must
       // follow the un-contracted evaluation of the Fortran (and of the CPU
       // reference) rather than a fused multiply-add.
+      if (soft) {
 #pragma unroll
-      for (int v = 0; v < NVT; ++v) vart[v] = add_rn(add_rn(vart[v], mul_rn(A[v], maxtime)), B[v]);
+        for (int v = 0; v < NVT; ++v) vart[v] = add_rn(vart[v], mul_rn(A[v], maxtime));
+      } else {
+#pragma unroll
+        for (int v = 0; v < NVT; ++v) vart[v] = add_rn(add_rn(vart[v], mul_rn(A[v], maxtime)), B[v]);
+      }
       if (!pos(vart[IRI])) cit = 0.;
       ztime += maxtime;
       rrevav = R.bu[B_RREVAV];
@@ -1322,23 +1405,29 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
     rvs -= zrvheni;
     ris += zrvheni;
   }
-  // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the sources
-  double w;
-  w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
-  w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
-  w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
-  w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
-  w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
-  if (H) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
-  w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
-  ths -= w * (rcs * lvx + ris * lsx);
-  rvs += w * (rcs + ris);
-  rcs = (1. - w) * rcs;
-  ris = (1. - w) * ris;
-  w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
-  w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
-  w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
-  if (H) { w = dmin(pmax0(rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; rhs -= w; ths -= w * lsx; }
+  // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the
+  // sources; with no negative source and the vapour source at or above
+  // XRTMIN(1) every line below moves nothing, and the warp skips it
+  const bool neg = negd(rcs) || negd(rrs) || negd(ris) || negd(rss) || negd(rgs) || (H && negd(rhs)) ||
+                   ltd(rvs, c.V_RTMIN);
+  if (warp_any(neg)) {
+    double w;
+    w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
+    w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
+    w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
+    w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
+    w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
+    if (H) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
+    w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
+    ths -= w * (rcs * lvx + ris * lsx);
+    rvs += w * (rcs + ris);
+    rcs = (1. - w) * rcs;
+    ris = (1. - w) * ris;
+    w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
+    w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
+    w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
+    if (H) { w = dmin(pmax0(rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; rhs -= w; ths -= w * lsx; }
+  }
   f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
   f.rgs[p] = rgs;
   if (H) f.rhs[p] = rhs;

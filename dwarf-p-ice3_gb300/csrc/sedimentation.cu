@@ -7,7 +7,9 @@
 // (selected by `fortran`).  A thread owns one column and walks k from the top
 // level to the surface with the five species side by side, keeping each
 // species' incoming flux F_{k+1} in a register; consecutive threads own
-// consecutive columns, so every level access is coalesced.  What the species
+// consecutive columns, so every level access is coalesced.  The fall speeds a
+// warp needs at a level are evaluated together, with every lane busy
+// (warp_fall_speeds).  What the species
 // share at a level (rho, dz, rho dz, dt/(rho dz) and log rho, computed only
 // when a species sediments there) is computed once; threshold tests and
 // clamps run on the integer pipe (GB300's FP64 pipe is the bound).
@@ -18,19 +20,118 @@
 namespace {
 using namespace ice3sed;
 
+// The fall speeds of species s at one level for the whole warp.  A lane
+// needs w1 (content r1 above its threshold, c1) and / or w2 (the flux from
+// above, r2, c2); about half of these requests are live, and evaluating them
+// in place would run each fall-speed formula for all 32 lanes whenever one
+// lane needs it.  The requests are dealt out to consecutive lanes instead
+// (the inputs fetched with shuffles), evaluated 32 at a time with every lane
+// busy, and the speeds shuffled back to the lanes that asked.  Same function
+// on the same arguments: the values are those of the per-lane evaluation.
+__device__ __forceinline__ void warp_fall_speeds(const Cst &c, int s, bool c1, double r1, bool c2, double r2,
+                                                 double lrho, double wlbda, const CloudPar &cp, double &w1,
+                                                 double &w2)
+{
+  const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+  const unsigned m1 = __ballot_sync(full, c1), m2 = __ballot_sync(full, c2);
+  const int n1 = __popc(m1), ntot = n1 + __popc(m2);
+  const int i1 = __popc(m1 & lt), i2 = n1 + __popc(m2 & lt);   // this lane's request numbers
+  w1 = w2 = 0.0;
+  for (int base = 0; base < ntot; base += 32) {                  // uniform over the warp
+    const int j = base + (int)lane;                              // the request this lane evaluates
+    const bool first = j < n1;
+    int owner = 0;
+    if (j < ntot) owner = (int)(first ? __fns(m1, 0u, j + 1) : __fns(m2, 0u, j - n1 + 1));
+    const double ra = __shfl_sync(full, r1, owner), rb = __shfl_sync(full, r2, owner);
+    const double lr = __shfl_sync(full, lrho, owner);
+    double wl = 0.0;
+    CloudPar cq = cp;
+    if (s == 0) {                                                // the cloud speed: per-column parameters
+      wl = __shfl_sync(full, wlbda, owner);
+      cq.log_lbc_conc = __shfl_sync(full, cp.log_lbc_conc, owner);
+      cq.ray_inv = __shfl_sync(full, cp.ray_inv, owner);
+      cq.fsedc = __shfl_sync(full, cp.fsedc, owner);
+    }
+    double v = 0.0;
+    if (j < ntot) v = fall_speed(c, s, first ? ra : rb, lr, wl, cq);
+    const double v1 = __shfl_sync(full, v, (unsigned)(i1 - base) & 31u);
+    const double v2 = __shfl_sync(full, v, (unsigned)(i2 - base) & 31u);
+    if (c1 && i1 >= base && i1 < base + 32) w1 = v1;
+    if (c2 && i2 >= base && i2 < base + 32) w2 = v2;
+  }
+}
+
+// sed_column_forward with the warp's fall speeds evaluated together
+// (warp_fall_speeds); every lane of the warp runs the level loop, lanes
+// past the last column (valid = false) without loads, stores or requests.
+__device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c, const CloudPar &cp, double dt,
+                                        const SedColumnIO &io, long col, bool valid)
+{
+  const double inv_dt = 1.0 / dt;
+  double rtmin[5];
+#pragma unroll
+  for (int s = 0; s < 5; ++s) rtmin[s] = sed_rtmin(c, s);
+  double fabove[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int k = io.nk - 1; k >= 0; --k) {
+    const long p = (long)k * io.nij + col;
+    const double rho = valid ? sed_load(io.rhodref, p) : 1.0, dz = valid ? sed_load(io.dzz, p) : 1.0;
+    const double rhodz = rho * dz;
+    const double tsorhodz = fm::fdiv(dt, rhodz);
+    double src[5], rt[5], qp[5];
+    bool c1[5], c2[5];
+    bool any = false;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      if (s == 0 && skip_c) { c1[s] = c2[s] = false; src[s] = rt[s] = qp[s] = 0.0; continue; }
+      src[s] = valid ? io.src_in[s][p] : 0.0;
+      rt[s] = src[s] * dt;
+      qp[s] = fabove[s] * tsorhodz;
+      c1[s] = valid && gtp(rt[s], rtmin[s]);
+      c2[s] = valid && gtp(qp[s], rtmin[s]);
+      any = any || c1[s] || c2[s];
+    }
+    const double lrho = any ? fm::flog(rho) : 0.0;
+    const double wlbda =
+        (c1[0] || c2[0]) ? 6.6e-8 * fm::fdiv(101325.0, sed_load(io.pabs, p)) * (sed_load(io.tht, p) * (1.0 / 293.15))
+                         : 0.0;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      if (s == 0 && skip_c) continue;
+      double w1, w2;
+      warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, w1, w2);
+      double flux = dmin(rhodz * rt[s] * inv_dt, w1 * rho * rt[s]);
+      if (!zerod_(w2)) flux += pmax0(1.0 - fm::fdiv(dz, dt * w2)) * fabove[s];
+      if (valid) {
+        if (io.src_out[s]) {
+          if (fortran) io.src_out[s][p] = src[s] + tsorhodz * (fabove[s] - flux) * inv_dt;
+          else io.src_out[s][p] = src[s] + fm::fdiv(fabove[s] - flux, rhodz * dt);
+        }
+        if (io.fpr[s]) io.fpr[s][p] = flux;
+      }
+      fabove[s] = flux;
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < 5; ++s)
+    if (valid && !(s == 0 && skip_c) && io.inpr[s]) io.inpr[s][col] = fabove[s] / c.RHOLW;
+}
+
 __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
 {
   const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (col >= a.nij) return;
+  // whole warps run the sweep (they share the fall-speed evaluations); a
+  // warp entirely past the last column leaves
+  const bool valid = col < a.nij;
+  if (__all_sync(0xffffffffu, !valid)) return;
   // PHYEX skips the cloud species when LSEDIC is off
   const bool skip_c = a.fortran && c.LSEDIC == 0.0;
-  if (skip_c) {
+  if (skip_c && valid) {
     if (a.fpr[0])
       for (int k = 0; k < a.nk; ++k) a.fpr[0][(long)k * a.nij + col] = 0.0;
     a.inpr[0][col] = 0.0;
   }
   const bool has_st = a.sea != nullptr && a.town != nullptr;
-  const double sea = a.sea ? a.sea[col] : 0.0, town = a.town ? a.town[col] : 0.0;
+  const double sea = (a.sea && valid) ? a.sea[col] : 0.0, town = (a.town && valid) ? a.town[col] : 0.0;
   const CloudPar cp = cloud_params(c, a.fortran, has_st, sea, town);
   SedColumnIO io;
   io.rhodref = a.rhodref; io.dzz = a.dzz; io.pabs = a.pabs; io.tht = a.tht;
@@ -42,9 +143,9 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constan
   }
   io.nij = a.nij;
   io.nk = a.nk;
-  sed_column_forward(c, a.fortran, skip_c, cp, a.dt, io, col);
+  sed_column_forward_warp(c, a.fortran, skip_c, cp, a.dt, io, col, valid);
   // hail (NRR = 7), an independent species: its own sweep of the column
-  if (a.hsrc) sed_hail_column(c, a.dt, a.rhodref, a.dzz, a.hsrc, a.hfpr, a.hinpr, a.nij, a.nk, col);
+  if (a.hsrc && valid) sed_hail_column(c, a.dt, a.rhodref, a.dzz, a.hsrc, a.hfpr, a.hinpr, a.nij, a.nk, col);
 }
 
 // Fog deposition on the lowest level (rain_ice.F90:876-895).

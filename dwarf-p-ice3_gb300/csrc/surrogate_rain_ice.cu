@@ -48,7 +48,9 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const 
   __syncthreads();
   const long n = (long)a.nij * a.nk;
   const unsigned lane = threadIdx.x & 31u;
-  // uniform trip count: whole warps reach the ballots
+  __shared__ unsigned wrows[SAMPLE_THREADS / 32];
+  __shared__ unsigned long long block_base;
+  // uniform trip count: whole warps reach the ballots, whole blocks the barriers
   const long stride = (long)gridDim.x * blockDim.x;
   for (long p0 = (long)blockIdx.x * blockDim.x; p0 < n; p0 += stride) {
     const long p = p0 + threadIdx.x;
@@ -69,11 +71,24 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) surrogate_sample_kernel(const 
         xf[j] = v;
       }
     }
+    // rows handed out per block (one atomic per block: a per-warp atomic on
+    // the one counter serialised the kernel at the L2)
     const unsigned m = __ballot_sync(0xffffffffu, ok);
-    unsigned long long base = 0;
-    if (lane == 0 && m) base = atomicAdd(a.count, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    const long row = ok ? (long)(base + __popc(m & ((1u << lane) - 1u))) : -1;
+    const unsigned warp = threadIdx.x >> 5;
+    if (lane == 0) wrows[warp] = (unsigned)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned tot = 0;
+      for (int w = 0; w < SAMPLE_THREADS / 32; ++w) {
+        const unsigned cw = wrows[w];
+        wrows[w] = tot;
+        tot += cw;
+      }
+      block_base = tot ? atomicAdd(a.count, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const long row = ok ? (long)(block_base + wrows[warp] + __popc(m & ((1u << lane) - 1u))) : -1;
+    __syncthreads();                  // wrows and block_base are rewritten by the next iteration
     const bool kept = ok && row < a.cap;
     if (kept) {
       float4 *fr = reinterpret_cast<float4 *>(a.feat + row * ROW);

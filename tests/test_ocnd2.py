@@ -437,7 +437,7 @@ def test_ocnd2_rain_ice_host_build_matches_oracle(kw):
     import oracle
     import subprocess
     from ice3gb import _abi
-    from test_hail import _untie
+    from test_hail import _report_ties, _untie
     d = os.path.dirname(os.path.abspath(__file__))
     libs = {}
     for name in ("rain_ice_point_host", "sedimentation_host"):
@@ -474,10 +474,11 @@ def test_ocnd2_rain_ice_host_build_matches_oracle(kw):
                                                       ctypes.byref(f))
     ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
     fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
-    spread, share = _untie(spread, fl["tie"])
+    spread, share, exempt = _untie(spread, fl["tie"])
     for k in RI_OUT:
         sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
-        assert_parity(keep[k], ref[k], spread[k], f"ocnd2 host/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(keep[k], ref[k], spread[k], f"ocnd2 host/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"ocnd2 host/{k}", keep[k], ref[k], sc, exempt[k], stats)
 
 
 @pytest.mark.parametrize("sedim", [1.0, 0.0])
@@ -503,14 +504,14 @@ def test_ocnd2_rain_ice_device_matches_oracle(after):
     import oracle
     import torch
     from ice3gb import RainIce
-    from test_hail import _untie
+    from test_hail import _report_ties, _untie
     t = _ri_table()
     nij = 32 * 32
     x = ocnd2_rain_ice_state(nij, seed=5)
     ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT, lsedim_after=int(after))[0], x, rel=1e-12,
                               trials=4)
     fl, _ = oracle.rain_ice(t, x, DT, lsedim_after=int(after), with_fpr=True, with_ties=True)
-    spread, share = _untie(spread, fl["tie"])
+    spread, share, exempt = _untie(spread, fl["tie"])
     ri = RainIce()
     ri.table = t
     m = {"exn": "exn", "dzz": "dzz", "rhodref": "rhodref", "exnref": "exnref", "pres": "pabs", "cldfr": "cldfr",
@@ -527,7 +528,8 @@ def test_ocnd2_rain_ice_device_matches_oracle(after):
         got[k] = diag[k].cpu().numpy()
     for k in RI_OUT:
         sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
-        assert_parity(got[k], ref[k], spread[k], f"ocnd2 device/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(got[k], ref[k], spread[k], f"ocnd2 device/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"ocnd2 device/{k}", got[k], ref[k], sc, exempt[k], stats)
     assert ri.device_status() == 0
 
 
@@ -537,15 +539,16 @@ def test_ocnd2_rain_ice_warm_options_device_matches_oracle(kw):
     """OCND2 with the subgrid warm-process options (the OCND2 branches leave
     ICE4_WARM and ICE4_COMPUTE_PDF as they are)."""
     import oracle
-    from test_hail import _untie
+    from test_hail import _report_ties, _untie
     from test_time_splitting import _ocnd2_device
     t = _ri_table(**kw)
     x = ocnd2_rain_ice_state(32 * 32, seed=6)
     ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
     fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
-    spread, share = _untie(spread, fl["tie"], sed_after=False)
+    spread, share, exempt = _untie(spread, fl["tie"], sed_after=False)
     got, ri = _ocnd2_device(t, x)
     for k in RI_OUT:
         sc = _ri_scale(x, ref, fl, k) if k not in ("cit",) and not k.startswith("inpr") else None
-        assert_parity(got[k], ref[k], spread[k], f"ocnd2 warm {kw}/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(got[k], ref[k], spread[k], f"ocnd2 warm {kw}/{k}", scale=sc, max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"ocnd2 warm {kw}/{k}", got[k], ref[k], sc, exempt[k], stats)
     assert ri.device_status() == 0

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from parity import assert_parity, sensitivity
-from test_hail import INPR7, SRC7, _fields, _run_device, _scale, _untie, hail_state, host_libs  # noqa: F401
+from test_hail import INPR7, SRC7, _fields, _report_ties, _run_device, _scale, _untie, hail_state, host_libs  # noqa: F401
 
 DT = 50.0
 SRC6, INPR6 = SRC7[:-1], INPR7[:-1]
@@ -136,11 +136,12 @@ def test_time_split_host_build_matches_oracle(host_libs, nrr, kw):
     # MRSTEP thresholds on the sub-step are frequent (a species grown from
     # zero to MRSTEP that then depletes), and the sedimentation after the
     # sub-stepping carries them down the column
-    spread, share = _untie(spread, fl["tie"], max_share=0.15)
+    spread, share, exempt = _untie(spread, fl["tie"], max_share=0.15)
     for k in ("ths",) + src + ("cit",) + inpr:
         sc = _scale_ts(x, ref, fl, k, src) if k in ("ths",) + src else None
-        assert_parity(keep[k], ref[k], spread[k], f"time split host {kw}/{k}", scale=sc,
-                      max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(keep[k], ref[k], spread[k], f"time split host {kw}/{k}", scale=sc,
+                              max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"time split host {kw}/{k}", keep[k], ref[k], sc, exempt[k], stats)
 
 
 # ---------------------------------------------------------------------------- GPU
@@ -156,12 +157,13 @@ def test_time_split_device_matches_oracle(nrr, kw):
     src, inpr = _keys(nrr)
     ref, spread = sensitivity(lambda y: oracle.rain_ice(t, y, DT)[0], x, rel=1e-12, trials=4)
     fl, _ = oracle.rain_ice(t, x, DT, with_fpr=True, with_ties=True)
-    spread, share = _untie(spread, fl["tie"], sed_after=False)
+    spread, share, exempt = _untie(spread, fl["tie"], sed_after=False)
     got, ri = _run_device(t, x)
     for k in ("ths",) + src + ("cit",) + inpr:
         sc = _scale_ts(x, ref, fl, k, src) if k in ("ths",) + src else None
-        assert_parity(got[k], ref[k], spread[k], f"time split device {kw}/{k}", scale=sc,
-                      max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(got[k], ref[k], spread[k], f"time split device {kw}/{k}", scale=sc,
+                              max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"time split device {kw}/{k}", got[k], ref[k], sc, exempt[k], stats)
     assert ri.device_status() == 0
 
 
@@ -251,12 +253,13 @@ def test_ocnd2_time_split_device_matches_oracle(kw):
     # OCND2 sublimates the ice to a rounding residual at about a fifth of the
     # points; with TSTEP_TS every such reset of cit is followed by hard
     # passes (tie bit 3), 6 % of the points of this state
-    spread, share = _untie(spread, fl["tie"], max_share=0.1, sed_after=False)
+    spread, share, exempt = _untie(spread, fl["tie"], max_share=0.1, sed_after=False)
     got, ri = _ocnd2_device(t, x)
     for k in ("ths",) + SRC6 + ("cit",) + INPR6:
         sc = _scale_ts(x, ref, fl, k, SRC6) if k in ("ths",) + SRC6 else None
-        assert_parity(got[k], ref[k], spread[k], f"ocnd2 time split device {kw}/{k}", scale=sc,
-                      max_frac_conditioned=0.01 + share[k])
+        stats = assert_parity(got[k], ref[k], spread[k], f"ocnd2 time split device {kw}/{k}", scale=sc,
+                              max_frac_conditioned=0.01 + share[k])
+        _report_ties(f"ocnd2 time split device {kw}/{k}", got[k], ref[k], sc, exempt[k], stats)
     assert ri.device_status() == 0
     # limits that cannot bind: the OCND2 kernel's results bit for bit
     base, _ = _ocnd2_device(_table(OCND2=1.0), x)

@@ -19,7 +19,10 @@ Metric: grid-points/s (points of the step / step time).
   roofline: dominant kernel's algorithmic bytes per launch / its average
           launch time (CUDA events around each launch on the launching stream),
           against the measured HBM copy bandwidth.
-  cpu_baseline: the CPU oracle (C, OpenMP, all host cores) on a column sample.
+  cpu_baseline: the CPU oracle (C, OpenMP, all host cores) on the same whole
+          state, one warm-up then at least 2 steps (about 10 s).
+  --impl reference: the same oracle (the reference's own code cannot run on
+          the box) on the same workload, W warm-up and K timed steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -136,65 +139,75 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- CPU side
 
-def cpu_chain_baseline(st_np, budget_s=10.0, min_steps=2):
-    """Oracle chained step on the host cores (OpenMP, all threads)."""
+def workload_config(nij, seed):
+    """The workload named in both arms' JSON lines (the same for each)."""
+    n = nij * NK
+    return {"workload": f"chained ice_adjust->rain_ice->ice_adjust, {nij} columns x {NK} levels "
+                        f"({n} grid points) per GPU, FP64, dt={DT}s, AROME table (PHYEX values)",
+            "columns_per_gpu": nij, "levels": NK, "dt": DT, "seed": seed,
+            "l2": "inputs larger than L2 (no flush)"}
+
+
+def cpu_chain_steps(st_np, steps, warmup=1, budget_s=None):
+    """The oracle's chained step on the host cores (C, OpenMP, all threads) on
+    the whole state `st_np`: `warmup` untimed steps, then `steps` timed ones
+    (or, with `budget_s`, at least `steps` and until the budget is spent).
+    Outputs are allocated once; each step starts from the same in-out fields;
+    the time is the step call alone.  Returns the per-step times."""
     import oracle
     from ice3gb.constants import build_table
 
     table = build_table(table="phyex")
-    nk, nij = st_np["pabs"].shape
-    oracle.physics_step(table, st_np, DT)          # warm-up (page-in, thread pool)
+    out = None
+    for _ in range(max(warmup, 1)):
+        out, _ = oracle.physics_step(table, st_np, DT, out=out)
     times = []
     t_start = time.perf_counter()
-    while len(times) < min_steps or (time.perf_counter() - t_start) < budget_s:
-        t0 = time.perf_counter()
-        oracle.physics_step(table, st_np, DT)
-        times.append(time.perf_counter() - t0)
-        if len(times) >= 50:
-            break
-    pts = nij * nk
-    return pts / statistics.median(times), times
+    while len(times) < steps or (budget_s is not None and time.perf_counter() - t_start < budget_s
+                                 and len(times) < 50):
+        oracle.physics_step(table, st_np, DT, out=out, elapsed=times)
+    return times
 
 
-def run_reference(args):
-    """--impl reference: the reference path's CPU restatement (oracle port; the
-    reference's own Fortran and JAX code cannot run on the box) on a bounded
-    sample of the same workload, every host core."""
-    import numpy as np
+def host_state(nij, seed):
+    """The benchmark's state in host memory: generated on the GPU like the GPU
+    arm's (the same numbers) when one is visible, else on the host (the same
+    distributions, other draws)."""
     import torch
 
     from ice3gb.state import make_state
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    st = step_state(make_state(nij, NK, seed=seed, precip=True, device=dev))
+    out = {k: v.cpu().numpy() for k, v in st.items()}
+    del st
+    if dev == "cuda":
+        torch.cuda.empty_cache()
+    return out, dev
 
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU restatement (the oracle port;
+    the reference's own Fortran and JAX code cannot run on the box) on the
+    whole workload, every host core, `warmup` untimed then `steps` timed
+    steps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    cols = args.cpu_cols
-    st = {k: v.numpy() for k, v in make_state(cols, NK, seed=args.seed, precip=True).items()}
-    st = step_state(st)
-    import oracle
-    from ice3gb.constants import build_table
-
-    table = build_table(table="phyex")
-    for _ in range(args.warmup):
-        oracle.physics_step(table, st, DT)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        oracle.physics_step(table, st, DT)
-        times.append(time.perf_counter() - t0)
-    pts = cols * NK
+    st, dev = host_state(args.nij, args.seed)
+    times = cpu_chain_steps(st, args.steps, warmup=args.warmup)
+    pts = args.nij * NK
     total = sum(times)
     value = pts * len(times) / total
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "grid-points/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"chained ice_adjust->rain_ice->ice_adjust, CPU sample {cols} columns x {NK} "
-                               f"levels of the 1024x1024x90 workload", "dt": DT, "seed": args.seed},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded AROME-like states)", "config": workload_config(args.nij, args.seed),
         "cpu_baseline": {"value": value, "unit": "grid-points/s", "cores": cores, "kind": "port",
-                         "sample": f"{cols} columns x {NK} levels ({pts} points) per step, OpenMP over "
-                                   f"{cores} threads; PHYEX Fortran/JAX reference not runnable on the box"},
+                         "sample": f"the whole workload, {pts} points per step (state generated on the {dev}), "
+                                   f"C/OpenMP over {cores} threads; the reference's PHYEX Fortran and JAX code "
+                                   f"cannot run on the box"},
         "e2e": {"value": value, "unit": "grid-points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -321,25 +334,22 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "grid-points/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded AROME-like states)",
-        "config": {"workload": f"chained ice_adjust->rain_ice->ice_adjust, {nij} columns x {NK} levels "
-                               f"({n} grid points) per GPU, FP64, dt={DT}s, AROME table (PHYEX values)",
-                   "columns_per_gpu": nij, "levels": NK, "dt": DT, "seed": args.seed,
-                   "l2": "inputs larger than L2 (no flush)",
-                   "timed_step": "restore 8 in-out fields (device copies) + ice3gb_physics_step"},
+        "config": workload_config(nij, args.seed),
+        "timed_step": "restore 8 in-out fields (device copies) + ice3gb_physics_step",
         "gpu_launches": launches_total, "device_status_bits": bits,
         "roofline": roofline, "clocks": clocks.summary(), "e2e": e2e, "surrogate": surrogate,
     }
     if not args.no_cpu and rank == 0:
-        cols = args.cpu_cols
-        st_cpu = {k: v[:, :cols].cpu().numpy().copy() if v.dim() == 2 else v[:cols].cpu().numpy().copy()
-                  for k, v in st.items()}
+        # the oracle's chained step on the same (whole) state, host cores
+        st_cpu = {k: v.cpu().numpy() for k, v in st.items()}
         for k in STEP_INOUT:
-            v = pristine[k]
-            st_cpu[k] = v[:, :cols].cpu().numpy().copy()
-        cval, ctimes = cpu_chain_baseline(st_cpu, budget_s=args.cpu_seconds)
+            st_cpu[k] = pristine[k].cpu().numpy()
+        ctimes = cpu_chain_steps(st_cpu, 2, warmup=1, budget_s=args.cpu_seconds)
+        del st_cpu
+        cval = n / statistics.median(ctimes)
         line["cpu_baseline"] = {"value": cval, "unit": "grid-points/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{cols} columns x {NK} levels of the same state, {len(ctimes)} steps, "
-                                          f"median step {statistics.median(ctimes):.3f}s"}
+                                "sample": f"the whole workload ({n} points), {len(ctimes)} steps after one "
+                                          f"warm-up, median step {statistics.median(ctimes):.3f}s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -511,13 +521,18 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--nij", type=int, default=1024 * 1024)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cpu-cols", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)   # timing rule: at least 3 warm-up steps
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world:
+        # one process per GPU: N > 1 comes from torchrun (WORLD_SIZE = N)
+        print(f"bench.py: --gpus {args.gpus} needs {args.gpus} ranks (torchrun --nproc-per-node {args.gpus}); "
+              f"WORLD_SIZE is {world}", file=sys.stderr)
+        return 2
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

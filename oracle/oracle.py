@@ -12,6 +12,7 @@ import ctypes
 import os
 import subprocess
 import sys
+import time
 from typing import Dict, Optional
 
 import numpy as np
@@ -328,8 +329,13 @@ def rainfr_vert(table, prfr, rr, rs, rg):
     return prfr
 
 
-def physics_step(table, st: Dict[str, np.ndarray], dt: float, max_passes: int = 0, sed_jax: int = 0):
-    """Oracle chained step (ice3o_physics_step); `st` uses the StepFields names."""
+def physics_step(table, st: Dict[str, np.ndarray], dt: float, max_passes: int = 0, sed_jax: int = 0,
+                 out: Optional[Dict[str, np.ndarray]] = None, elapsed: Optional[list] = None):
+    """Oracle chained step (ice3o_physics_step); `st` uses the StepFields names.
+    `out`: the arrays of a previous call's result, reused (the in-out fields
+    are copied in again from `st`), so that repeated steps allocate nothing.
+    `elapsed`: a list the wall time of the step itself (the C call) is
+    appended to."""
     lib = load()
     keep = {k: _f64(st[k]) for k in STEP_IN}
     nk, nij = keep["pabs"].shape
@@ -340,9 +346,13 @@ def physics_step(table, st: Dict[str, np.ndarray], dt: float, max_passes: int = 
         if st.get(k) is not None:
             keep[k] = _f64(st[k])
             setattr(f, k, _ptr(keep[k]))
-    out = {k: _f64(st[k]).copy() for k in STEP_INOUT}
-    out.update({k: np.empty((nk, nij)) for k in STEP_OUT3})
-    out.update({k: np.empty(nij) for k in STEP_OUT2})
+    if out is None:
+        out = {k: _f64(st[k]).copy() for k in STEP_INOUT}
+        out.update({k: np.empty((nk, nij)) for k in STEP_OUT3})
+        out.update({k: np.empty(nij) for k in STEP_OUT2})
+    else:
+        for k in STEP_INOUT:
+            np.copyto(out[k], st[k])
     for k, v in out.items():
         setattr(f, k, _ptr(v))
     opt = RainIceOptions(-1, -1, -1, max_passes, sed_jax)
@@ -350,8 +360,11 @@ def physics_step(table, st: Dict[str, np.ndarray], dt: float, max_passes: int = 
     lib.ice3o_physics_step.argtypes = [ctypes.POINTER(Ice3gbConstants), ctypes.POINTER(Ice3gbLuts), ctypes.c_int,
                                        ctypes.c_int, ctypes.c_double, ctypes.POINTER(RainIceOptions),
                                        ctypes.POINTER(StepFields), ctypes.POINTER(ctypes.c_uint32)]
+    t0 = time.perf_counter()
     rc = lib.ice3o_physics_step(ctypes.byref(table.consts), ctypes.byref(table.luts), nij, nk, dt, ctypes.byref(opt),
                                 ctypes.byref(f), ctypes.byref(bits))
+    if elapsed is not None:
+        elapsed.append(time.perf_counter() - t0)
     if rc != 0:
         raise RuntimeError(f"oracle physics_step returned {rc}")
     return out, bits.value

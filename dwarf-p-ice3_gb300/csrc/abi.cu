@@ -596,6 +596,32 @@ void pipe_free(Handle *h)
   P = HostPipe();
 }
 
+// Column boundaries of the slabs: slabs of w_max columns, the first and the
+// last ones graded (w_max / 4, w_max / 4, w_max / 2 at each end, multiples of
+// 64 columns) when the grid holds at least 6 of them, because the first
+// slab's copy-in and the last slab's copy-out overlap no kernel.
+std::vector<long> slab_cuts(long nij, long w_max)
+{
+  std::vector<long> widths;
+  const long q = (w_max / 4 + 63) / 64 * 64, hlf = (w_max / 2 + 63) / 64 * 64;
+  long left = nij;
+  const bool graded = nij >= 6 * w_max && q >= 64;
+  if (graded) {
+    for (long w : {q, q, hlf}) { widths.push_back(w); left -= w; }
+    left -= 2 * q + hlf;                             // the trailing ones
+  }
+  while (left > 0) {
+    const long w = left < w_max ? left : w_max;
+    widths.push_back(w);
+    left -= w;
+  }
+  if (graded)
+    for (long w : {hlf, q, q}) widths.push_back(w);
+  std::vector<long> cuts(1, 0);
+  for (long w : widths) cuts.push_back(cuts.back() + w);
+  return cuts;
+}
+
 int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                                const Ice3gbStepFields *f, cudaStream_t s)
 {
@@ -641,12 +667,13 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
       (e = cudaMemsetAsync(P.keys_all, 0, 4 * sizeof(unsigned int), P.s_cmp)) != cudaSuccess)
     return cuda_fail(h, e, "slab pipeline start");
   const size_t hp = (size_t)nij * sizeof(double);   // host row pitch of 3-D fields
-  const long nslab = ((long)nij + w_max - 1) / w_max;
+  const std::vector<long> cuts = slab_cuts(nij, w_max);
+  const long nslab = (long)cuts.size() - 1;
   long pt_off = 0;                                   // offset of the slab in evap_all / keys
   for (long i = 0; i < nslab && rc == ICE3GB_OK; ++i) {
     const int b = (int)(i % HostPipe::NB);
-    const long col0 = i * w_max;
-    const long w = ((long)nij - col0) < w_max ? ((long)nij - col0) : w_max;
+    const long col0 = cuts[i];
+    const long w = cuts[i + 1] - cuts[i];
     const size_t wb = (size_t)w * sizeof(double);
     char *base = P.buf[b];
     size_t off = 0;
@@ -724,8 +751,8 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
     if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_out, P.fix_done, 0);
     long off_pts = 0;
     for (long i = 0; i < nslab && e == cudaSuccess; ++i) {
-      const long col0 = i * w_max;
-      const long w = ((long)nij - col0) < w_max ? ((long)nij - col0) : w_max;
+      const long col0 = cuts[i];
+      const long w = cuts[i + 1] - cuts[i];
       const size_t wb = (size_t)w * sizeof(double);
       e = cudaMemcpy2DAsync(f->evap3d + col0, hp, P.evap_all + off_pts, wb, wb, (size_t)nk, cudaMemcpyDeviceToHost,
                             P.s_out);

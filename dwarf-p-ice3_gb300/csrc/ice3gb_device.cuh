@@ -81,12 +81,25 @@ ICE3_HD bool pos(double a) { return fm::bits_(a) > 0; }                   // a >
 ICE3_HD double pmax0(double a) { return pos(a) ? a : 0.0; }               // fmax(0, a)
 ICE3_HD double dmax(double a, double b) { return gtd(a, b) ? a : b; }
 ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
+// The bit pattern of x through an inline-assembly move, which the compiler
+// cannot see through: a test that equals an FP64 comparison (x == 0, x != 0)
+// would otherwise be turned back into one, on the FP64 pipe.
+ICE3_HD uint64_t opaque_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+#else
+  return (uint64_t)fm::bits_(x);
+#endif
+}
 // a == +-0.
-ICE3_HD bool zerod_(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) == 0; }
+ICE3_HD bool zerod_(double a) { return (opaque_bits(a) << 1) == 0; }
 // |a| > b for b >= +0.
 ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > fm::bits_(b); }
 // a != 0 (nor -0), on the bit pattern.
-ICE3_HD bool nz(double a) { return (fm::bits_(a) & 0x7fffffffffffffffLL) != 0; }
+ICE3_HD bool nz(double a) { return (opaque_bits(a) << 1) != 0; }
 // True on every lane when the predicate holds on some active lane of the warp:
 // a block of arithmetic that is exact when skipped on lanes whose inputs are
 // zero runs for the warp or for none of it (the host build: the lane alone).

@@ -174,7 +174,7 @@ ICE3_HD void ocnd2_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, 
 // x < 0 (not -0), on the bit pattern.
 ICE3_HD bool negd(double x) { return fm::bits_(x) < 0 && fm::bits_(x) != INT64_MIN; }
 // x == 0 or -0, on the bit pattern.
-ICE3_HD bool zerod(double x) { return (fm::bits_(x) & 0x7fffffffffffffffLL) == 0; }
+ICE3_HD bool zerod(double x) { return (opaque_bits(x) << 1) == 0; }
 
 // ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.).
 ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst, double rhodref, double exn,

@@ -267,12 +267,13 @@ def test_physics_step_matches_oracle_and_host_path():
 
 
 
-@pytest.mark.parametrize("nij", [128 * 128, 3 * 4096 + 100])
+@pytest.mark.parametrize("nij", [128 * 128, 3 * 4096 + 100, 6 * 4096 + 64])
 def test_physics_step_host_slab_pipeline_matches_device(nij):
     """The host entry point runs the step in column slabs (4096 columns and
-    more) on three streams; its outputs, evap3d's fix-up on the maximum pass
-    key of the whole call included, equal the device entry point's bit for
-    bit, also with a ragged last slab."""
+    more, the first and last three graded down to a quarter when the grid
+    holds six) on three streams; its outputs, evap3d's fix-up on the maximum
+    pass key of the whole call included, equal the device entry point's bit
+    for bit, also with a ragged slab."""
     from ice3gb.components import Ice3Handle
     from ice3gb.constants import build_table
     h = Ice3Handle(build_table(table="phyex"))

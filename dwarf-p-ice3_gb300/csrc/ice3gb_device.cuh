@@ -46,6 +46,19 @@ ICE3_HD double add_rn(double a, double b)
   return p;
 #endif
 }
+// The bit pattern of x through an inline-assembly move, which the compiler
+// cannot see through: a test that equals an FP64 comparison (x == 0, x != 0)
+// would otherwise be turned back into one, on the FP64 pipe.
+ICE3_HD uint64_t opaque_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+#else
+  return (uint64_t)fm::bits_(x);
+#endif
+}
 // Comparisons and clamps on the IEEE bit patterns.  On GB300 an FP64 compare
 // (and so fmin/fmax) issues on the FP64 pipe at the FP64 FMA rate, while the
 // same test on the 64-bit pattern runs on the integer pipe at ~30x the rate.
@@ -81,19 +94,6 @@ ICE3_HD bool pos(double a) { return fm::bits_(a) > 0; }                   // a >
 ICE3_HD double pmax0(double a) { return pos(a) ? a : 0.0; }               // fmax(0, a)
 ICE3_HD double dmax(double a, double b) { return gtd(a, b) ? a : b; }
 ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
-// The bit pattern of x through an inline-assembly move, which the compiler
-// cannot see through: a test that equals an FP64 comparison (x == 0, x != 0)
-// would otherwise be turned back into one, on the FP64 pipe.
-ICE3_HD uint64_t opaque_bits(double x)
-{
-#if defined(__CUDA_ARCH__)
-  unsigned long long b;
-  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
-  return b;
-#else
-  return (uint64_t)fm::bits_(x);
-#endif
-}
 // a == +-0.
 ICE3_HD bool zerod_(double a) { return (opaque_bits(a) << 1) == 0; }
 // |a| > b for b >= +0.

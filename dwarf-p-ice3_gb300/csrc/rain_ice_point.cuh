@@ -806,7 +806,7 @@ ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, con
 template <bool H = false, bool O = false>
 ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, double lsfact, Rates &R,
                        double *A, bool soft = false, HailRates *hr = nullptr, double *B = nullptr,
-                       const OcndRates *orr = nullptr)
+                       const OcndRates *orr = nullptr, const double *ext = nullptr)
 {
   double *b = R.bu;
   const double *rs = R.rs, *rg = R.rg;
@@ -876,7 +876,12 @@ ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, d
     depg_s = dmax(0., dmin(1., (c.FRMIN5 - fm::fdiv(v[IRG], c.FRMIN5)))) * dmax(0., dmin(1., fm::fdiv(R.ssi, c.FRMIN6)));
     nodepg_s = 1. - depg_s;
   }
+  // the sums start from the external tendencies (ICE4_STEPPING adds them to
+  // the microphysical ones, mode_ice4_stepping.F90:265-272)
   double ath = 0.0, av = 0.0, ac = 0.0, ar = 0.0, ai = 0.0, as = 0.0, ag = 0.0;
+  if (ext) {
+    ath = ext[ITH]; av = ext[IRV]; ac = ext[IRC]; ar = ext[IRR]; ai = ext[IRI]; as = ext[IRS]; ag = ext[IRG];
+  }
   if (warp_any(nz(b[B_RVDEPG]))) {                                  // vapour -> graupel (and snow, OCND2)
     const double x = b[B_RVDEPG];
     ath += x * lsfact;
@@ -1031,7 +1036,7 @@ ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, d
     B[IRG] -= hb[BH_RWETGH_MR];
     A[IRG] -= hb[BH_RGWETH];
     A[IRG] = A[IRG] - hb[BH_RGDRYH] + hb[BH_RDRYHG];
-    A[IRH] = hb[BH_RWETGH];
+    A[IRH] = ext ? ext[IRH] + hb[BH_RWETGH] : hb[BH_RWETGH];
     B[IRH] += hb[BH_RWETGH_MR];
     A[IRH] = A[IRH] + hb[BH_RCWETH] + hb[BH_RIWETH] + hb[BH_RSWETH] + hb[BH_RGWETH] + hb[BH_RRWETH];
     A[IRH] = A[IRH] + hb[BH_RCDRYH] + hb[BH_RIDRYH] + hb[BH_RSDRYH] + hb[BH_RRDRYH] + hb[BH_RGDRYH] - hb[BH_RDRYHG];
@@ -1109,7 +1114,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
                         const double *vart, Rates &R, double &rainfr, double hl[4], double hi[4], double *A,
                         double *B, const double *sur = nullptr, HailRates *hr = nullptr,
                         const double *__restrict__ hlut = nullptr, const OcndPt *op = nullptr,
-                        OcndRates *orr = nullptr)
+                        OcndRates *orr = nullptr, const double *ext = nullptr)
 {
   constexpr int NVT = H ? NVH : NV;
   double v[NVT];
@@ -1138,7 +1143,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
                                 orr);
   else soft_rates<SUBG, H, O>(c, t, v, cit, hl, hi, R, pf.cf, rainfr, hr, orr);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
-  aggregate<H, O>(c, t, v, lvfact, lsfact, R, A, soft, hr, B, orr);
+  aggregate<H, O>(c, t, v, lvfact, lsfact, R, A, soft, hr, B, orr, ext);
 }
 
 // ICE4_STEPPING for one micro point (mode_ice4_stepping.F90:139-518).
@@ -1213,10 +1218,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
       double A[NVT], B[NVT];
       tendencies<SUR, SUBG, H, O>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
-                                  &HR, hlut, op, &OR);
+                                  &HR, hlut, op, &OR, ext);    // A includes the external tendencies
       if (SUR) sur = nullptr;          // learned slow rates: first hard pass only
-#pragma unroll
-      for (int v = 0; v < NVT; ++v) A[v] += ext[v];
       double maxtime = dt - ztime;
       // B (the instantaneous changes) is zero on soft passes: no theta jump
       // across TT/exn, no B in the depletion limits and the state update

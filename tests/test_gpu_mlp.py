@@ -84,10 +84,11 @@ def test_mlp_gradients_match_oracle(n):
     g = g.cpu().numpy().astype(np.float64)
     lr, gr = mlp_ref.loss_grad(net.get_params(), net.layout(), x, t)
     assert abs(loss - lr) <= 1e-4 * abs(lr), (loss, lr)
-    for (wo, bo, o, i) in net.layout():
-        for lo, hi in ((wo, wo + o * i), (bo, bo + o)):
+    for li, (wo, bo, o, i) in enumerate(net.layout()):
+        for what, lo, hi in (("W", wo, wo + o * i), ("b", bo, bo + o)):
             a, r = g[lo:hi], gr[lo:hi]
             rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
+            print(f"n={n} layer {li} {what}: rel {rel:.2e}")
             assert rel <= 2e-2, (lo, hi, rel)
 
 

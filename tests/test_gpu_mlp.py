@@ -77,19 +77,26 @@ def test_fused_inference_equals_layered(n):
 @pytest.mark.parametrize("n", [1000, 4096, 20000])
 def test_mlp_gradients_match_oracle(n):
     """Hand-written backward pass (tcgen05 GEMMs with transposed staging,
-    split-K over the batch) against the FP64 restatement, per layer."""
+    split-K over the batch) against the FP64 restatement, per layer and per
+    weight / bias block, within 5e-3 in relative norm (the restatement models
+    the BF16 roundings, so what remains is FP32 summation order)."""
     net, x, t = _mlp_case(2 + n, n)
     loss, g = net.loss_grad(torch.as_tensor(x).cuda(), torch.as_tensor(t).cuda())
     net.check()
     g = g.cpu().numpy().astype(np.float64)
     lr, gr = mlp_ref.loss_grad(net.get_params(), net.layout(), x, t)
     assert abs(loss - lr) <= 1e-4 * abs(lr), (loss, lr)
+    # measured on GB300: at most 1.1e-3 (layer 0 W, n = 1000), 4e-5 .. 3e-4 for
+    # the biases; a transposed square weight gradient is off by O(1)
     for li, (wo, bo, o, i) in enumerate(net.layout()):
         for what, lo, hi in (("W", wo, wo + o * i), ("b", bo, bo + o)):
             a, r = g[lo:hi], gr[lo:hi]
             rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-30)
             print(f"n={n} layer {li} {what}: rel {rel:.2e}")
-            assert rel <= 2e-2, (lo, hi, rel)
+            assert rel <= 5e-3, (lo, hi, rel)
+            if what == "W" and o == i:
+                at = a.reshape(o, i).T.ravel()
+                assert np.linalg.norm(at - r) / max(np.linalg.norm(r), 1e-30) > 0.1
 
 
 def test_mlp_training_lowers_loss():

@@ -112,6 +112,21 @@ ICE3_HD bool warp_any(bool p)
 #endif
 }
 
+// num / den to within 2^-22 relative, from the FP32 reciprocal of den
+// (truncated to FP32) and one FP64 multiply; exact in sign.  0 where den is
+// outside FP32's normal range.  Used to skip an IEEE division whose result
+// cannot change a min / max.
+ICE3_HD double quot_est(double num, double den)
+{
+  const int e = (int)((fm::bits_(den) >> 52) & 0x7ff);
+  if (e <= 898 || e >= 1149) return 0.0;
+  return num * fm::to_f64(fm::rcpf_(fm::to_f32(den)));
+}
+// True only if the quotient that est estimates (quot_est) is above bound
+// for certain.
+ICE3_HD bool est_above(double est, double bound) { return gtd(est, bound + fabs(bound) * 0x1p-18); }
+ICE3_HD bool quot_above(double num, double den, double bound) { return est_above(quot_est(num, den), bound); }
+
 // x**a evaluated as exp(a*log(x)) with the FP64-lean exp/log of
 // fastmath.cuh.  For the exponents of the scheme (|a*log x| < 60) this stays
 // within ~1e-14 relative of pow(), well inside the 1e-10 parity bar, at a

@@ -24,11 +24,12 @@ static_assert(sizeof(IaIn) == 20 * sizeof(double), "IaIn layout");
 static_assert(sizeof(IaOut) == 16 * sizeof(double), "IaOut layout");
 
 // Triangle-PDF subgrid autoconversion (stencils/ice_adjust.py:316-341).
+// 1 / max(1e-20, w_dt)^2 is formed only in the branches that read it (with
+// no mass flux, w_dt = 0, it would be an IEEE division of 1e-40).
 ICE3_HD void triangle_pdf(double w_dt, double crit, double cf_mf, double &hcf, double &hr)
 {
-  const double wmax = nmax(1e-20, w_dt);
-  const double inv_w2 = fm::frcp(sq(wmax));
   if (fgt(w_dt, crit)) {
+    const double inv_w2 = fm::frcp(sq(nmax(1e-20, w_dt)));
     const double cc = crit * cf_mf;
     hcf = 1.0 - 0.5 * sq(cc) * inv_w2;
     hr = w_dt - cc * cc * cc * (inv_w2 * (1.0 / 3.0));
@@ -36,6 +37,7 @@ ICE3_HD void triangle_pdf(double w_dt, double crit, double cf_mf, double &hcf, d
     hcf = 0.0;
     hr = 0.0;
   } else {
+    const double inv_w2 = fm::frcp(sq(nmax(1e-20, w_dt)));
     hcf = 0.5 * sq(2.0 * w_dt - crit) * inv_w2;
     hr = (4.0 * w_dt * w_dt * w_dt - 3.0 * w_dt * sq(crit) + crit * crit * crit) * (inv_w2 * (1.0 / 3.0));
   }
@@ -258,8 +260,14 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
     ths = ths + (w1m * lv + w2m * ls) * inv_cphex;
     const int mfpdf = (int)c.SUBG_MF_PDF;
     if (mfpdf == 0 || mfpdf == 1) {
-      const double criaut = fm::fdiv(c.CRIAUTC, x.rho);
-      const double criaut_i = nmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+      // the thresholds enter only as cf_mf * threshold: where cf_mf is +-0
+      // that is +-0 whatever their (finite, positive) value, so they are
+      // not formed there
+      double criaut = 0.0, criaut_i = 0.0;
+      if (nz(x.cf_mf)) {
+        criaut = fm::fdiv(c.CRIAUTC, x.rho);
+        criaut_i = nmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+      }
       if (mfpdf == 0) {
         if (fgt(w1m * dt, x.cf_mf * criaut)) { hlc_hrc = w1m * dt; hlc_hcf = nmin(1.0, x.cf_mf); }
         if (fgt(w2m * dt, x.cf_mf * criaut_i)) { hli_hri = w2m * dt; hli_hcf = nmin(1.0, x.cf_mf); }

@@ -12,7 +12,10 @@
 //    SACCRG, KER_RDRYG, KER_SDRYG; 78,720 B FP64) are staged once per block
 //    in shared memory; blocks are persistent (2 per SM) and pull 1-point-per-
 //    thread chunks from a global counter, which balances the data-dependent
-//    number of sub-steps across SMs;
+//    number of sub-steps across SMs.  The chunk barrier keeps the warps of a
+//    block in step through the (large) point code: warps that pull their own
+//    32-point chunks drift apart and the step takes 305 instead of 177 ms at
+//    1024x1024x90;
 //  * every per-point quantity that is fixed over the sub-steps (log rho and
 //    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;

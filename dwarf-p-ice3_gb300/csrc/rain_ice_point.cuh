@@ -23,7 +23,11 @@
 
 namespace ice3pt {
 
-constexpr int RI_THREADS = 256;
+// Threads per block of the rain_ice point kernels.
+#ifndef ICE3GB_RI_THREADS
+#define ICE3GB_RI_THREADS 256
+#endif
+constexpr int RI_THREADS = ICE3GB_RI_THREADS;
 // The tables of Ice3gbLuts staged in shared memory (all but the hail
 // kernels, which the NRR = 7 instantiation reads from global memory).
 constexpr int LUT_N = 9840;
@@ -82,6 +86,10 @@ struct Derived {
   // computed is reused (AROME: EX0DEPS = 0, EXCRIMSG = EXCRIMSS,
   // EXSRIMCG2 = 2 EXSRIMCG, CXS = 1, EXICFRR = EXCACCR, EX0EVAR = -2)
   int ex0deps_zero, ex0depg_zero, crims_same, srimcg2_twice, cxs_one, icfrr_caccr, ex0evar_m2;
+  // the option switches of the table as integers, so that no lane converts
+  // or compares the FP64 table entries
+  int aucv_rc, aucv_ri, prpdf, accr, evap, snow_riming;
+  int lwarm, lfeedbackt, lsnow_t, lcrflimit, llrfr;
 };
 
 ICE3_HD void make_derived(const Cst &c, Derived &d)
@@ -100,6 +108,17 @@ ICE3_HD void make_derived(const Cst &c, Derived &d)
   d.cxs_one = c.CXS == 1.0;
   d.icfrr_caccr = c.EXICFRR == c.EXCACCR;
   d.ex0evar_m2 = c.EX0EVAR == -2.0;
+  d.aucv_rc = (int)c.SUBG_AUCV_RC;
+  d.aucv_ri = (int)c.SUBG_AUCV_RI;
+  d.prpdf = (int)c.SUBG_PR_PDF;
+  d.accr = (int)c.SUBG_RC_RR_ACCR;
+  d.evap = (int)c.SUBG_RR_EVAP;
+  d.snow_riming = (int)c.SNOW_RIMING;
+  d.lwarm = c.LWARM != 0.0;
+  d.lfeedbackt = c.LFEEDBACKT != 0.0;
+  d.lsnow_t = c.LSNOW_T != 0.0;
+  d.lcrflimit = c.LCRFLIMIT != 0.0;
+  d.llrfr = d.accr == 1 || d.evap == 2;
 }
 
 // Rates that persist between the hard pass and the following soft passes
@@ -117,6 +136,7 @@ struct PointFix {
   double rho_mcexvt;    // rho**(-CEXVT)
   double rho_mcexvt1;   // rho**(-CEXVT-1)
   double rcrautc;       // CRIAUTC / rho
+  double zx;            // TT / exn (IEEE division: where th stops at the T = TT limit)
 };
 
 ICE3_HD double esat_from(double alp, double beta, double gam, double it, double lt)
@@ -176,15 +196,25 @@ ICE3_HD bool negd(double x) { return fm::bits_(x) < 0 && fm::bits_(x) != INT64_M
 // x == 0 or -0, on the bit pattern.
 ICE3_HD bool zerod(double x) { return (opaque_bits(x) << 1) == 0; }
 
-// ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.).
-ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst, double rhodref, double exn,
-                        double lsfact, double t, double rvt, double &cit, double &rvheni)
+// The T-dependent terms of a hard pass that nucleation computes and the
+// rates of the same pass reuse while T keeps its bit pattern (no HENI,
+// RRHONG or RIMLTC change in between): log T, 1/T, es_w and es_i.
+struct TTerms {
+  double t, lt, it, esw, esi;
+  bool set;
+};
+
+// ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.);
+// zx = TT/exn (IEEE division).
+ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst, double rhodref, double zx,
+                        double lsfact, double t, double rvt, double &cit, double &rvheni, TTerms *tt = nullptr)
 {
   rvheni = 0.0;
   if (!(ltp(t, c.TT) && gtp(rvt, c.V_RTMIN))) return;
   const double lt = fm::flog(t), it = fm::frcp(t);
   double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   double zzw = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+  if (tt) { tt->t = t; tt->lt = lt; tt->it = it; tt->esw = zusw; tt->esi = zzw; tt->set = true; }
   zzw = dmin(pabst * 0.5, zzw);
   double zssi = fm::fdiv(rvt * (pabst - zzw), c.EPSILO * zzw) - 1.0;
   zusw = dmin(pabst * 0.5, zusw);
@@ -198,10 +228,17 @@ ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst
   }
   zzw = dmin(zzw - cit, 50.e3);
   rvheni = dmin(rvt, fm::fdiv(pmax0(zzw) * c.MNU0, rhodref));
-  if (c.LFEEDBACKT != 0.0) {
-    // IEEE divisions: the limiter puts th exactly on TT/exn, and the next
-    // T < TT test must see the same rounding as the Fortran
-    const double w = dmin(rvheni, pmax0((c.TT / exn - tht) / lsfact)) / dmax(rvheni, 1.e-20);
+  if (d.lfeedbackt) {
+    // w = MIN(rvheni, MAX(0, (TT/exn - th) / lsfact)) / MAX(rvheni, 1e-20)
+    // with IEEE divisions, as the Fortran: the limit puts th exactly on
+    // TT/exn, and the next T < TT test must see the same rounding.  Where
+    // the limit cannot bind the quotient is not formed: w = 0 for rvheni = +0
+    // (0 / 1e-20), w = 1 for rvheni > 1e-20 (rvheni / rvheni).
+    const double num = zx - tht;
+    double w;
+    if (opaque_bits(rvheni) == 0) w = 0.0;
+    else if (gtp(rvheni, 1.e-20) && quot_above(num, lsfact, rvheni)) w = 1.0;
+    else w = dmin(rvheni, pmax0(num / lsfact)) / dmax(rvheni, 1.e-20);
     rvheni *= w;
     zzw *= w;
   }
@@ -211,10 +248,10 @@ ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst
 // ICE4_COMPUTE_PDF (micro/mode_ice4_compute_pdf.F90), one point; returns RF.
 // `criauti` receives MIN(CRIAUTI, 10**(ACRIAUTI (T-TT) + BCRIAUTI)), which
 // the ice autoconversion of the same pass uses too.
-ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit, double cf, double t,
-                           double sigma_rc, double hl[4], double hi[4], double &criauti)
+ICE3_HD double compute_pdf(const Cst &c, const Derived &d, double rcrautc, double rct, double rit, double cf,
+                           double t, double sigma_rc, double hl[4], double hi[4], double &criauti, bool soft = false)
 {
-  const int aucv_rc = (int)c.SUBG_AUCV_RC, aucv_ri = (int)c.SUBG_AUCV_RI, prpdf = (int)c.SUBG_PR_PDF;
+  const int aucv_rc = d.aucv_rc, aucv_ri = d.aucv_ri, prpdf = d.prpdf;
   double hcf = 0, lcf = 0, hrc = 0, lrc = 0;
   if (aucv_rc == 0) {
     if (gtd(rct, rcrautc)) { hcf = 1.0; hrc = rct; }
@@ -275,11 +312,27 @@ ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit,
   // the ice threshold matters where the ice is present, or with the CLFR ice
   // partition (criauti * cf); with NONE and no ice it is never read
   criauti = c.CRIAUTI;
-  if (warp_any(aucv_ri != 0 || gtp(rit, c.I_RTMIN)))
+  bool ice_high = false;
+  if (soft && aucv_ri == 0) {
+    // a soft pass reads only rit > MIN(CRIAUTI, 10**x) = rit > CRIAUTI or
+    // rit > 10**x, decided from an FP32 estimate of 10**x (within 1e-5)
+    // unless rit is within 2^-14 of it
+    ice_high = gtd(rit, c.CRIAUTI);
+    const bool open = !ice_high && gtp(rit, c.I_RTMIN);
+    double x = 0.0, ea = 0.0;
+    if (warp_any(open)) {
+      x = c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI;
+      ea = fm::to_f64(exp2f(fm::to_f32(x) * 3.32192809488736235f));
+    }
+    const bool near = open && !gtd(rit, ea + ea * 0x1p-14) && !ltd(rit, ea - ea * 0x1p-14);
+    if (open && gtd(rit, ea + ea * 0x1p-14)) ice_high = true;
+    if (warp_any(near) && near) ice_high = gtd(rit, fm::fexp10(x));
+  } else if (warp_any(aucv_ri != 0 || gtp(rit, c.I_RTMIN))) {
     criauti = dmin(c.CRIAUTI, fm::fexp10(c.ACRIAUTI * (t - c.TT) + c.BCRIAUTI));
+  }
   double ihcf = 0, ilcf = 0, ihri = 0, ilri = 0;
   if (aucv_ri == 0) {
-    if (gtd(rit, criauti)) { ihcf = 1.0; ihri = rit; }
+    if (soft ? ice_high : gtd(rit, criauti)) { ihcf = 1.0; ihri = rit; }
     else if (gtp(rit, c.I_RTMIN)) { ilcf = 1.0; ilri = rit; }
   } else if (aucv_ri == 1) {
     if (pos(cf) && gtd(rit, criauti * cf)) { ihcf = cf; ihri = rit; }
@@ -294,11 +347,20 @@ ICE3_HD double compute_pdf(const Cst &c, double rcrautc, double rct, double rit,
 }
 
 // INTERP_MICRO (micro/interp_micro.func.h, packed path): index from log(x).
+// floor(z) is taken from z truncated to FP32 (never above z; one below
+// floor(z) only within 2^-23 z above an integer, fixed by the f >= 1 test),
+// so that no FP64 <-> integer conversion is issued; same i and f as
+// (int)z, z - (double)(int)z.
 ICE3_HD double lut_index(double logx, double knum, double p1, double p2, int &i)
 {
   const double z = dmax(1.00001, dmin(knum - 0.00001, p1 * logx + p2));
-  i = (int)z;
-  return z - (double)i;
+  i = (int)fm::to_f32(z);
+  double f = z - fm::i2d(i);
+  if (!ltp(f, 1.0)) {
+    ++i;
+    f = z - fm::i2d(i);
+  }
+  return f;
 }
 ICE3_HD double lut1d(const double *lt, int i, double f) { return lt[i] * f - lt[i - 1] * (f - 1.0); }
 // PLT(i1+1, i2+1) of the 1-based Fortran table is row i1, column i2 of the
@@ -322,7 +384,7 @@ ICE3_HD void slopes(const Cst &c, const Derived &d, double lrho, double t, const
     s.llbdar = d.lLBR + c.LBEXR * (lrho + fm::flog(dmax(v[IRR], c.R_RTMIN)));
     s.lbdar = fm::fexp(s.llbdar);
   } else { s.lbdar = 0.0; s.llbdar = -INFINITY; }
-  if (c.LSNOW_T != 0.0) {
+  if (d.lsnow_t) {
     if (pos(v[IRS])) {
       const double e = gtp(t, 263.15) ? fm::fexp10(14.554 - 0.0423 * t) : fm::fexp10(6.226 - 0.0106 * t);
       s.lbdas = dmax(dmin(c.LBDAS_MAX, e), c.LBDAS_MIN) * c.TRANS_MP_GAMMAS;
@@ -366,7 +428,7 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
 {
   double *b = R.bu;
   const bool has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
-  const int accr = (int)c.SUBG_RC_RR_ACCR, evap = (int)c.SUBG_RR_EVAP;
+  const int accr = d.accr, evap = d.evap;
   const bool llrfr = accr == 1 || evap == 2;
   const double llrf = llrfr ? llbdar_rf(c, d, pf.lrho, v[IRR], rainfr) : s.llbdar;
   if (accr == 0) {
@@ -428,18 +490,23 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
                         double t, const double *v, double cit, const double hl[4], const double hi[4],
                         double criauti, Rates &R, bool learned_slow = false, double rainfr = 1.0,
                         HailRates *hr = nullptr, const double *__restrict__ hlut = nullptr,
-                        const OcndPt *op = nullptr, OcndRates *orr = nullptr)
+                        const OcndPt *op = nullptr, OcndRates *orr = nullptr, const TTerms *tt = nullptr)
 {
   double *b = R.bu, *rs = R.rs, *rg = R.rg;
   const double rho = pf.rho;
   // derived fields (mode_ice4_tendencies.F90:303-320; OCND2: es_i and ai
-  // from the TIWMX tables, :304-309)
-  const double lt = fm::flog(t), it = fm::frcp(t);
-  // es_i of the freezing heat terms stays the formula; OCND2 takes the table
-  // for ssi, ai and ICE4_FAST_RI_RS only
-  const double esi_f = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+  // from the TIWMX tables, :304-309); es_i of the freezing heat terms stays
+  // the formula, OCND2 takes the table for ssi, ai and ICE4_FAST_RI_RS only.
+  // The nucleation of the same pass has formed them already if T is unchanged.
+  double lt, it, esi_f, esw;
+  if (tt && tt->set && fm::bits_(tt->t) == fm::bits_(t)) {
+    lt = tt->lt; it = tt->it; esi_f = tt->esi; esw = tt->esw;
+  } else {
+    lt = fm::flog(t); it = fm::frcp(t);
+    esi_f = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
+    esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
+  }
   const double esi = O ? tiwmx_at(op->tw + TW_ESI * kTiwmxN, t) : esi_f;
-  const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   R.ssi = fm::fdiv(v[IRV] * (pf.pres - esi), c.EPSILO * esi) - 1.0;
   const double ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
   const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
@@ -521,10 +588,10 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   }
 
   // ---- ICE4_WARM (mode_ice4_warm.F90) ----
-  if (SUBG && c.LWARM != 0.0 && ((int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0)) {
+  if (SUBG && d.lwarm && (d.accr != 0 || d.evap != 0)) {
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
     warm_subgrid(c, d, pf, t, v, hl, ka, dv, cj, s, rainfr, e_caccr, R, O ? &acrf : nullptr);
-  } else if (c.LWARM != 0.0) {
+  } else if (d.lwarm) {
     // SUBG_RC_RR_ACCR = SUBG_RR_EVAP = NONE
     b[B_RCAUTR] = (gtp(hl[2], c.C_RTMIN) && pos(hl[0])) ? c.TIMAUTC * pmax0(hl[2] - hl[0] * pf.rcrautc) : 0.0;
     b[B_RCACCR] = (has_c && has_r) ? (O ? c.FCACCR * v[IRC] * acrf * e_caccr * pf.rho_mcexvt
@@ -558,7 +625,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     rs[RS_RCRIMSS] = O ? c.CRIMSS * zw1 * v[IRC] * colf * e_crimss * pf.rho_mcexvt
                        : c.CRIMSS * zw1 * v[IRC] * e_crimss * pf.rho_mcexvt;
     rs[RS_RCRIMS] = c.CRIMSG * rcc * (d.crims_same ? e_crimss : fm::fexp(c.EXCRIMSG * s.llbdas)) * pf.rho_mcexvt;
-    if ((int)c.SNOW_RIMING == 0) {
+    if (d.snow_riming == 0) {
       const double zzw = rs[RS_RCRIMS] - rs[RS_RCRIMSS];
       const double e_srimcg = fm::fexp(c.EXSRIMCG * s.llbdas);
       const double e_srimcg2 = d.srimcg2_twice ? e_srimcg * e_srimcg : fm::fexp(c.EXSRIMCG2 * s.llbdas);
@@ -598,7 +665,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   if (has_i && has_r) {
     b[B_RICFRRG] = c.ICFRR * v[IRI] * (d.icfrr_caccr ? e_caccr : fm::fexp(c.EXICFRR * s.llbdar)) * pf.rho_mcexvt;
     b[B_RRCFRIG] = c.RCFRI * cit * fm::fexp(c.EXRCFRI * s.llbdar) * pf.rho_mcexvt1;
-    if (c.LCRFLIMIT != 0.0) {
+    if (d.lcrflimit) {
       const double zw = pmax0(dmin(1., fm::fdiv((b[B_RICFRRG] * c.CI + b[B_RRCFRIG] * c.CL) * (c.TT - t),
                                                   dmax(1.e-20, c.LVTT * b[B_RRCFRIG]))));
       b[B_RRCFRIG] = zw * b[B_RRCFRIG];
@@ -732,7 +799,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
 // holds on the current state, zero elsewhere (the ELSE branches of the
 // process routines under LDSOFT).
 template <bool SUBG = false, bool H = false, bool O = false>
-ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, const double hl[4],
+ICE3_HD void soft_rates(const Cst &c, const Derived &d, double t, const double *v, double cit, const double hl[4],
                         const double hi[4], Rates &R, double cf = 0.0, double rainfr = 1.0, HailRates *hr = nullptr,
                         OcndRates *orr = nullptr)
 {
@@ -746,22 +813,22 @@ ICE3_HD void soft_rates(const Cst &c, double t, const double *v, double cit, con
   if (!(has_i && has_s)) b[B_RIAGGS] = 0.0;
   if (!gtp(hi[2], c.I_RTMIN)) b[B_RIAUTS] = 0.0;
   if (!(has_v && has_g)) b[B_RVDEPG] = 0.0;
-  if (SUBG && c.LWARM != 0.0 && ((int)c.SUBG_RC_RR_ACCR != 0 || (int)c.SUBG_RR_EVAP != 0)) {
+  if (SUBG && d.lwarm && (d.accr != 0 || d.evap != 0)) {
     if (!(gtp(hl[2], c.C_RTMIN) && pos(hl[0]))) b[B_RCAUTR] = 0.0;
-    if ((int)c.SUBG_RC_RR_ACCR == 0) {
+    if (d.accr == 0) {
       if (!(has_c && has_r)) b[B_RCACCR] = 0.0;
     } else {
       const bool m = has_c && has_r;
       if (!((m && gtp(hl[2], c.C_RTMIN) && pos(hl[0])) || (m && gtp(hl[3], c.C_RTMIN) && gtp(hl[1], 1.e-20))))
         b[B_RCACCR] = 0.0;
     }
-    const int evap = (int)c.SUBG_RR_EVAP;
+    const int evap = d.evap;
     if (evap == 0) {
       if (!(has_r && !has_c)) b[B_RREVAV] = 0.0;
     } else if (!(has_r && gtd(evap == 1 ? 1.0 : rainfr, cf))) {
       b[B_RREVAV] = 0.0;
     }
-  } else if (c.LWARM != 0.0) {
+  } else if (d.lwarm) {
     if (!(gtp(hl[2], c.C_RTMIN) && pos(hl[0]))) b[B_RCAUTR] = 0.0;
     if (!(has_c && has_r)) b[B_RCACCR] = 0.0;
     if (!(has_r && !has_c)) b[B_RREVAV] = 0.0;
@@ -1066,10 +1133,11 @@ ICE3_HD void slow_rates_from(const Cst &c, double t, const double v[NV], const d
 // t are updated in place, the increments go to b and B.
 template <bool O = false>
 ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, double lvfact, double lsfact,
-                         double &cit, double &t, double v[NV], double *b, double B[NV], const OcndPt *op = nullptr)
+                         double &cit, double &t, double v[NV], double *b, double B[NV], const OcndPt *op = nullptr,
+                         TTerms *tt = nullptr)
 {
   if (O) nucleation_ocnd2(c, *op, t, v[IRV], cit, b[B_RVHENI_MR]);
-  else nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.exn, lsfact, t, v[IRV], cit, b[B_RVHENI_MR]);
+  else nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.zx, lsfact, t, v[IRV], cit, b[B_RVHENI_MR], tt);
   v[ITH] += b[B_RVHENI_MR] * lsfact;
   t = v[ITH] * pf.exn;
   v[IRV] -= b[B_RVHENI_MR];
@@ -1078,7 +1146,7 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
   double r = 0.0;
   if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
     r = v[IRR];
-    if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
+    if (d.lfeedbackt) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
   }
   b[B_RRHONG_MR] = r;
   v[ITH] += r * (lsfact - lvfact);
@@ -1089,7 +1157,11 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
   r = 0.0;
   if (pos(v[IRI]) && gtp(t, c.TT)) {
     r = v[IRI];
-    if (c.LFEEDBACKT != 0.0) r = dmin(r, pmax0((v[ITH] - c.TT / pf.exn) / (lsfact - lvfact)));
+    if (d.lfeedbackt) {
+      // the IEEE quotient only where it can be below r
+      const double num = v[ITH] - pf.zx, den = lsfact - lvfact;
+      if (!quot_above(num, den, r)) r = dmin(r, pmax0(num / den));
+    }
   }
   b[B_RIMLTC_MR] = r;
   v[ITH] -= r * (lsfact - lvfact);
@@ -1122,14 +1194,16 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
 #pragma unroll
   for (int k = 0; k < NVT; ++k) { v[k] = vart[k]; B[k] = 0.0; }
   double *b = R.bu;
+  TTerms tt;
+  tt.set = false;
   if (!soft) {
-    hard_adjust<O>(c, d, pf, lvfact, lsfact, cit, t, v, b, B, op);
+    hard_adjust<O>(c, d, pf, lvfact, lsfact, cit, t, v, b, B, op, &tt);
   } else {
     b[B_RVHENI_MR] = b[B_RRHONG_MR] = b[B_RIMLTC_MR] = 0.0;
   }
   double criauti;
-  const double zrainfr = compute_pdf(c, pf.rcrautc, v[IRC], v[IRI], pf.cf, t, pf.sigma_rc, hl, hi, criauti);
-  const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
+  const double zrainfr = compute_pdf(c, d, pf.rcrautc, v[IRC], v[IRI], pf.cf, t, pf.sigma_rc, hl, hi, criauti, soft);
+  const bool llrfr = d.llrfr;
   if (llrfr) {
     rainfr = dmax(rainfr, zrainfr);
     bool mask = gtp(v[IRR], c.R_RTMIN) || gtp(v[IRS], c.S_RTMIN) || gtp(v[IRG], c.G_RTMIN);
@@ -1140,8 +1214,8 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   }
   if (!soft)
     hard_rates<SUR, SUBG, H, O>(c, d, lut, pf, t, v, cit, hl, hi, criauti, R, sur != nullptr, rainfr, hr, hlut, op,
-                                orr);
-  else soft_rates<SUBG, H, O>(c, t, v, cit, hl, hi, R, pf.cf, rainfr, hr, orr);
+                                orr, &tt);
+  else soft_rates<SUBG, H, O>(c, d, t, v, cit, hl, hi, R, pf.cf, rainfr, hr, orr);
   if (SUR && !soft && sur) slow_rates_from(c, t, v, hi, sur, R);
   aggregate<H, O>(c, t, v, lvfact, lsfact, R, A, soft, hr, B, orr, ext);
 }
@@ -1196,7 +1270,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
   // TT/exn, lsfact and lvfact with IEEE divisions, as the Fortran: the
   // LFEEDBACKT sub-step ends with th on TT/exn, and which side of TT the next
   // pass sees is decided by their rounding
-  const double zx = c.TT / pf.exn;
+  const double zx = pf.zx;
   while (ltd(ztime, dt)) {
     ++outer;
     inner = 0;
@@ -1223,20 +1297,31 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       double maxtime = dt - ztime;
       // B (the instantaneous changes) is zero on soft passes: no theta jump
       // across TT/exn, no B in the depletion limits and the state update
-      if (c.LFEEDBACKT != 0.0) {
+      if (d.lfeedbackt) {
         if (!soft && negd((vart[ITH] - zx) * (vart[ITH] + B[ITH] - zx))) maxtime = 0.;
         if (abs_gtp(A[ITH], 1.e-20)) {
-          const double thr = (zx - B[ITH] - vart[ITH]) / A[ITH];
-          if (pos(thr)) maxtime = dmin(maxtime, thr);
+          // the IEEE quotient only where it can be positive and below maxtime
+          const double num = zx - B[ITH] - vart[ITH];
+          const double e = quot_est(num, A[ITH]);
+          if (!negd(e) && !est_above(e, maxtime)) {
+            const double thr = num / A[ITH];
+            if (pos(thr)) maxtime = dmin(maxtime, thr);
+          }
         }
       }
+      // MAX(MIN(maxtime, time to deplete), MNH_TINY) per limited species is
+      // MAX(MIN over all of them, MNH_TINY); a species' IEEE quotient is only
+      // formed where it can be below the running minimum
+      bool limited = false;
 #pragma unroll
       for (int v = 1; v < NVT; ++v) {
         if (ltd(A[v], -1.e-20) && gtp(vart[v], rsmin[v])) {
-          maxtime = dmin(maxtime, -(B[v] + vart[v]) / A[v]);
-          maxtime = dmax(maxtime, c.MNH_TINY);
+          limited = true;
+          const double num = -(B[v] + vart[v]);
+          if (!quot_above(num, A[v], maxtime)) maxtime = dmin(maxtime, num / A[v]);
         }
       }
+      if (limited) maxtime = dmax(maxtime, c.MNH_TINY);
       if (!ltd(ztime + maxtime, dt)) llcompute = false;
       if (TS && outer < nb_iter_max) {
         if (c.TSTEP_TS != 0.0 && gtd(ztime + maxtime, tlast + ztstep)) {
@@ -1312,15 +1397,16 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
 {
   constexpr int NVT = H ? NVH : NV;
   const double inv_dt = 1.0 / dt;
-  const bool lwarm = c.LWARM != 0.0;
-  const bool sigm = (int)c.SUBG_AUCV_RC == 1 && (int)c.SUBG_PR_PDF == 0;
-  const bool adju = (int)c.SUBG_AUCV_RC == 2 || (int)c.SUBG_AUCV_RI == 2;
+  const bool lwarm = d.lwarm;
+  const bool sigm = d.aucv_rc == 1 && d.prpdf == 0;
+  const bool adju = d.aucv_rc == 2 || d.aucv_ri == 2;
   unsigned int key = 0u;
   capped = false;
   PointFix pf;
   pf.exn = ldp(f.exn, p);
   pf.rho = ldp(f.rhodref, p);
   pf.pres = ldp(f.pabs, p);
+  pf.zx = c.TT / pf.exn;
   const double th = ldp(f.tht, p), rv = ldp(f.rvt, p), rc = ldp(f.rct, p), rr = ldp(f.rrt, p);
   const double ri = ldp(f.rit, p), rs = ldp(f.rst, p), rg = ldp(f.rgt, p);
   const double exnref = ldp(f.exnref, p);
@@ -1350,13 +1436,13 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   const double lsx = lsf * iexnref, lvx = lvf * iexnref;
   // with a PRFR option the sub-stepping starts from the precipitation
   // fraction of prfr_column (rain_ice.F90:555-602, ICE4_PACK :326)
-  const bool llrfr = (int)c.SUBG_RC_RR_ACCR == 1 || (int)c.SUBG_RR_EVAP == 2;
+  const bool llrfr = d.llrfr;
   double evap = 0.0, rainfr = (SUBG && llrfr) ? f.rainfr[p] : 1.0;
   double zrvheni = 0.0;
   if (!micro) {
     cit = 0.0;
     if (O) nucleation_ocnd2(c, op, t, rv, cit, zrvheni);
-    else nucleation(c, d, th, pf.pres, pf.rho, pf.exn, lsf / pf.exn, t, rv, cit, zrvheni);
+    else nucleation(c, d, th, pf.pres, pf.rho, pf.zx, lsf / pf.exn, t, rv, cit, zrvheni);
   }
   zrvheni = dmin(rvs, zrvheni * inv_dt);
   if (micro) {
@@ -1409,11 +1495,10 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
     ris += zrvheni;
   }
   // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the
-  // sources; with no negative source and the vapour source at or above
-  // XRTMIN(1) every line below moves nothing, and the warp skips it
-  const bool neg = negd(rcs) || negd(rrs) || negd(ris) || negd(rss) || negd(rgs) || (H && negd(rhs)) ||
-                   ltd(rvs, c.V_RTMIN);
-  if (warp_any(neg)) {
+  // sources, in three blocks a warp skips when every lane would move
+  // nothing: the negative sources back to vapour; cloud and ice to vapour
+  // while the vapour source is below XRTMIN(1); then rain, snow, graupel
+  if (warp_any(negd(rcs) || negd(rrs) || negd(ris) || negd(rss) || negd(rgs) || (H && negd(rhs)))) {
     double w;
     w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
     w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
@@ -1421,15 +1506,19 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
     w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
     w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
     if (H) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
-    w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
+  }
+  if (warp_any(ltd(rvs, c.V_RTMIN))) {
+    double w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
     ths -= w * (rcs * lvx + ris * lsx);
     rvs += w * (rcs + ris);
     rcs = (1. - w) * rcs;
     ris = (1. - w) * ris;
-    w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
-    w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
-    w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
-    if (H) { w = dmin(pmax0(rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; rhs -= w; ths -= w * lsx; }
+    if (warp_any(ltd(rvs, c.V_RTMIN))) {
+      w = dmin(pmax0(rrs), pmax0(c.V_RTMIN - rvs)); rvs += w; rrs -= w; ths -= w * lvx;
+      w = dmin(pmax0(rss), pmax0(c.V_RTMIN - rvs)); rvs += w; rss -= w; ths -= w * lsx;
+      w = dmin(pmax0(rgs), pmax0(c.V_RTMIN - rvs)); rvs += w; rgs -= w; ths -= w * lsx;
+      if (H) { w = dmin(pmax0(rhs), pmax0(c.V_RTMIN - rvs)); rvs += w; rhs -= w; ths -= w * lsx; }
+    }
   }
   f.ths[p] = ths; f.rvs[p] = rvs; f.rcs[p] = rcs; f.rrs[p] = rrs; f.ris[p] = ris; f.rss[p] = rss;
   f.rgs[p] = rgs;
@@ -1451,7 +1540,9 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
 template <bool H = false>
 ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, int nk, long col)
 {
-  const int aucv_rc = (int)c.SUBG_AUCV_RC, aucv_ri = (int)c.SUBG_AUCV_RI;
+  Derived d;
+  make_derived(c, d);
+  const int aucv_rc = d.aucv_rc, aucv_ri = d.aucv_ri;
   const bool sigm = aucv_rc == 1 && (int)c.SUBG_PR_PDF == 0;
   const bool adju = aucv_rc == 2 || aucv_ri == 2;
   double above = 0.0;
@@ -1474,7 +1565,7 @@ ICE3_HD void prfr_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, i
       const double sig = sigm ? ldp(f.sigs, p) : 0.0;
       const double rho = ldp(f.rhodref, p);
       double criauti;
-      rf = compute_pdf(c, c.CRIAUTC / rho, rc, ri, cf, ldp(f.tht, p) * ldp(f.exn, p), sig * sig, hl, hi, criauti);
+      rf = compute_pdf(c, d, c.CRIAUTC / rho, rc, ri, cf, ldp(f.tht, p) * ldp(f.exn, p), sig * sig, hl, hi, criauti);
     } else {
       if (aucv_rc != 2) hl[0] = 0.0;
       hl[2] = 0.0;

@@ -58,8 +58,14 @@
 
 #if defined(__CUDACC__)
 #define FM_HD __host__ __device__ __forceinline__
+// exp, exp10 and log are called from dozens of sites of the large point
+// kernels: one out-of-line copy per kernel keeps those kernels' code in the
+// instruction cache (rain_ice 172.5 -> 171.5 ms, sedimentation 46.1 -> 44.7
+// ms per launch at 1024x1024x90 against inlined copies)
+#define FM_NI static __host__ __device__ __noinline__
 #else
 #define FM_HD inline
+#define FM_NI static inline
 #endif
 
 namespace fm {
@@ -197,7 +203,7 @@ FM_HD double exp_core(int32_t k, double r, float corr)
 }
 
 // e^x.
-FM_HD double fexp(double x)
+FM_NI double fexp(double x)
 {
   const int64_t ax = bits_(x) & 0x7fffffffffffffffLL;
   if (ax > 0x40861f0000000000LL) {                               // |x| > 707.875, inf, NaN
@@ -212,7 +218,7 @@ FM_HD double fexp(double x)
 }
 
 // 10^x.
-FM_HD double fexp10(double x)
+FM_NI double fexp10(double x)
 {
   const int64_t ax = bits_(x) & 0x7fffffffffffffffLL;
   if (ax > 0x4073300000000000LL) {                               // |x| > 307, inf, NaN
@@ -227,7 +233,7 @@ FM_HD double fexp10(double x)
 }
 
 // Natural logarithm.
-FM_HD double flog(double x)
+FM_NI double flog(double x)
 {
   int64_t b = bits_(x);
   int ebias = 0;

@@ -10,12 +10,10 @@
 // GB300 mapping:
 //  * the ICE4 collection-kernel tables (GAMINC_RIM1/2/4, KER_RACCSS/RACCS/
 //    SACCRG, KER_RDRYG, KER_SDRYG; 78,720 B FP64) are staged once per block
-//    in shared memory; blocks are persistent (2 per SM) and pull 1-point-per-
-//    thread chunks from a global counter, which balances the data-dependent
-//    number of sub-steps across SMs.  The chunk barrier keeps the warps of a
-//    block in step through the (large) point code: warps that pull their own
-//    32-point chunks drift apart and the step takes 305 instead of 177 ms at
-//    1024x1024x90;
+//    in shared memory; blocks are persistent (one of 512 threads per SM) and
+//    pull 1-point-per-thread chunks from a global counter, which balances the
+//    data-dependent number of sub-steps across SMs; the chunk barrier keeps
+//    the warps of a block in step through the (large) point code;
 //  * every per-point quantity that is fixed over the sub-steps (log rho and
 //    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;

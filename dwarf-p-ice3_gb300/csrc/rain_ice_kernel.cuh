@@ -8,10 +8,15 @@
 #include "ice3gb_kernels.h"
 #include "rain_ice_point.cuh"
 
-// Resident blocks of rain_ice_points_kernel per SM (2 x 256 threads: 128
-// registers per thread, two copies of the 78.7 KB lookup tables per SM).
+// Resident blocks of rain_ice_points_kernel per SM: one block of RI_THREADS
+// = 512 threads (128 registers per thread, one copy of the 78.7 KB lookup
+// tables per SM, the rest of the shared memory left to L1 for the register
+// spills).  The chunk barrier keeps the 16 warps in step through the (large)
+// point code; warps that pull their own chunks drift apart and run it from
+// the instruction cache's misses (305 instead of 177 ms at 1024x1024x90).
+// 512 x 1 measured 172.5 ms against 176.7 ms for 256 x 2.
 #ifndef RI_BLOCKS_PER_SM
-#define RI_BLOCKS_PER_SM 2
+#define RI_BLOCKS_PER_SM 1
 #endif
 
 namespace ice3ri {

@@ -23,9 +23,11 @@
 
 namespace ice3pt {
 
-// Threads per block of the rain_ice point kernels.
+// Threads per block of the rain_ice point kernels (one block per SM: the 16
+// warps share one copy of the lookup tables and keep in step, see
+// rain_ice_kernel.cuh).
 #ifndef ICE3GB_RI_THREADS
-#define ICE3GB_RI_THREADS 256
+#define ICE3GB_RI_THREADS 512
 #endif
 constexpr int RI_THREADS = ICE3GB_RI_THREADS;
 // The tables of Ice3gbLuts staged in shared memory (all but the hail

@@ -18,8 +18,9 @@
 #include "ice3gb_kernels.h"
 #include "surrogate_point.cuh"
 
+// One block of RI_THREADS per SM, as the plain rain_ice kernel.
 #ifndef RI_BLOCKS_PER_SM
-#define RI_BLOCKS_PER_SM 2
+#define RI_BLOCKS_PER_SM 1
 #endif
 
 namespace {

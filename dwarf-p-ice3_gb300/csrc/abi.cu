@@ -21,15 +21,17 @@ constexpr uint32_t kMagic = 0x1CE3B300u;
 constexpr long kMaxPoints = 1L << 40;
 
 // Resources of the slab pipeline of ice3gb_physics_step_host (created on
-// first use, grow-only): copy-in, compute and copy-out streams, NB rotating
-// sets of slab buffers, and the full-size evap3d / pass-key arrays whose
-// fix-up needs the maximum pass key over all slabs.
+// first use, grow-only): a copy-in stream, two compute streams (slabs
+// alternate between them, so that one slab's kernels fill the SMs the tail
+// of the other's leaves idle), a copy-out stream, NB rotating sets of slab
+// buffers, and the full-size evap3d / pass-key arrays whose fix-up needs the
+// maximum pass key over all slabs.
 struct HostPipe {
-  static constexpr int NB = 3;
+  static constexpr int NB = 4, NC = 2;
   bool ready = false;
-  cudaStream_t s_in = nullptr, s_cmp = nullptr, s_out = nullptr;
+  cudaStream_t s_in = nullptr, s_cmp[NC] = {}, s_out = nullptr;
   cudaEvent_t in_done[NB] = {}, cmp_done[NB] = {}, out_done[NB] = {};
-  cudaEvent_t start = nullptr, fix_done = nullptr;
+  cudaEvent_t start = nullptr, fix_done = nullptr, cleared = nullptr, cmp_end[NC] = {};
   char *buf[NB] = {};
   size_t buf_cap = 0;              // bytes per slab set
   double *evap_all = nullptr;      // [n] evap3d, slab after slab
@@ -548,18 +550,22 @@ int ensure_stage(Handle *h, size_t bytes)
 // ---- slab pipeline of the chained step on host buffers -----------------------
 // Columns are independent, so ice3gb_physics_step_host runs the step on
 // column slabs: pitched copies of slab i+1 in (host [nk][nij] -> compact
-// device [nk][w]) and of slab i-1 out overlap the kernels of slab i, on three
-// streams ordered by events.  evap3d keeps PRREVAV only at points active in
-// the last pass of the whole call, so the slabs share one maximum-pass-key
-// word and write evap3d and the pass keys to full-size arrays; one fix-up
-// after the last slab and a final copy-out of evap3d give the same result as
-// ice3gb_physics_step on the whole grid.
+// device [nk][w]) and of slab i-1 out overlap the kernels of slab i; the
+// slabs alternate between two compute streams, so that the kernels of two
+// slabs overlap as well (streams ordered by events).  evap3d keeps PRREVAV
+// only at points active in the last pass of the whole call, so the slabs
+// share one maximum-pass-key word and write evap3d and the pass keys to
+// full-size arrays; one fix-up after the last slab and a final copy-out of
+// evap3d give the same result as ice3gb_physics_step on the whole grid.
 int pipe_init(Handle *h)
 {
   HostPipe &P = h->pipe;
   if (P.ready) return ICE3GB_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&P.s_in, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.s_cmp, cudaStreamNonBlocking);
+  for (int k = 0; k < HostPipe::NC && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&P.s_cmp[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.cmp_end[k], cudaEventDisableTiming);
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.s_out, cudaStreamNonBlocking);
   for (int b = 0; b < HostPipe::NB && e == cudaSuccess; ++b) {
     e = cudaEventCreateWithFlags(&P.in_done[b], cudaEventDisableTiming);
@@ -568,6 +574,7 @@ int pipe_init(Handle *h)
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.start, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.fix_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P.cleared, cudaEventDisableTiming);
   if (e != cudaSuccess) return cuda_fail(h, e, "slab pipeline streams/events");
   P.ready = true;
   return ICE3GB_OK;
@@ -578,7 +585,7 @@ void pipe_free(Handle *h)
   HostPipe &P = h->pipe;
   if (!P.ready) return;
   cudaStreamSynchronize(P.s_in);
-  cudaStreamSynchronize(P.s_cmp);
+  for (int k = 0; k < HostPipe::NC; ++k) cudaStreamSynchronize(P.s_cmp[k]);
   cudaStreamSynchronize(P.s_out);
   for (int b = 0; b < HostPipe::NB; ++b) {
     cudaEventDestroy(P.in_done[b]);
@@ -588,8 +595,12 @@ void pipe_free(Handle *h)
   }
   cudaEventDestroy(P.start);
   cudaEventDestroy(P.fix_done);
+  cudaEventDestroy(P.cleared);
+  for (int k = 0; k < HostPipe::NC; ++k) {
+    cudaEventDestroy(P.cmp_end[k]);
+    cudaStreamDestroy(P.s_cmp[k]);
+  }
   cudaStreamDestroy(P.s_in);
-  cudaStreamDestroy(P.s_cmp);
   cudaStreamDestroy(P.s_out);
   if (P.evap_all) cudaFree(P.evap_all);
   if (P.keys_all) cudaFree(P.keys_all);
@@ -661,10 +672,14 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(evap3d/keys)");
     P.all_cap = (size_t)n_all;
   }
-  // order after the caller's earlier work on its stream; clear the shared key_max
+  // order after the caller's earlier work on its stream; clear the control
+  // words (work counters of the two compute streams at 0 and 2, the shared
+  // key_max at 1) before either compute stream starts
   if ((e = cudaEventRecord(P.start, s)) != cudaSuccess || (e = cudaStreamWaitEvent(P.s_in, P.start, 0)) != cudaSuccess ||
-      (e = cudaStreamWaitEvent(P.s_cmp, P.start, 0)) != cudaSuccess ||
-      (e = cudaMemsetAsync(P.keys_all, 0, 4 * sizeof(unsigned int), P.s_cmp)) != cudaSuccess)
+      (e = cudaStreamWaitEvent(P.s_cmp[0], P.start, 0)) != cudaSuccess ||
+      (e = cudaMemsetAsync(P.keys_all, 0, 4 * sizeof(unsigned int), P.s_cmp[0])) != cudaSuccess ||
+      (e = cudaEventRecord(P.cleared, P.s_cmp[0])) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(P.s_cmp[1], P.cleared, 0)) != cudaSuccess)
     return cuda_fail(h, e, "slab pipeline start");
   const size_t hp = (size_t)nij * sizeof(double);   // host row pitch of 3-D fields
   const std::vector<long> cuts = slab_cuts(nij, w_max);
@@ -709,11 +724,14 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
     d.evap3d = P.evap_all + pt_off;
     if (e == cudaSuccess) e = cudaEventRecord(P.in_done[b], P.s_in);
     if (e != cudaSuccess) break;
-    // ---- compute (the fix-up of evap3d waits for the last slab)
-    if ((e = cudaStreamWaitEvent(P.s_cmp, P.in_done[b], 0)) != cudaSuccess) break;
-    const RiScratch rs = {P.keys_all + 0, P.keys_all + 1, P.keys_all + 4 + pt_off, order, false, false};
-    if ((rc = run_physics_step(h, (int)w, nk, dt, opt, &d, P.s_cmp, &rs))) break;
-    if ((e = cudaEventRecord(P.cmp_done[b], P.s_cmp)) != cudaSuccess) break;
+    // ---- compute on the slab's compute stream, with that stream's work
+    // counter (the fix-up of evap3d waits for both streams)
+    const int k = (int)(i % HostPipe::NC);
+    cudaStream_t sc = P.s_cmp[k];
+    if ((e = cudaStreamWaitEvent(sc, P.in_done[b], 0)) != cudaSuccess) break;
+    const RiScratch rs = {P.keys_all + 2 * k, P.keys_all + 1, P.keys_all + 4 + pt_off, order, false, false};
+    if ((rc = run_physics_step(h, (int)w, nk, dt, opt, &d, sc, &rs))) break;
+    if ((e = cudaEventRecord(P.cmp_done[b], sc)) != cudaSuccess) break;
     // ---- copy out (everything but evap3d)
     if ((e = cudaStreamWaitEvent(P.s_out, P.cmp_done[b], 0)) != cudaSuccess) break;
     struct Out { double *dst; const double *src; bool three_d; };
@@ -743,11 +761,13 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
     a.scr.key_max = P.keys_all + 1;
     a.nij = nij;
     a.nk = nk;
-    {
-      ProfScope ps(h, K_EVAP_FIXUP, P.s_cmp);
-      e = launch_rain_ice_evap_fixup(a, P.s_cmp);
+    if ((e = cudaEventRecord(P.cmp_end[1], P.s_cmp[1])) == cudaSuccess)
+      e = cudaStreamWaitEvent(P.s_cmp[0], P.cmp_end[1], 0);
+    if (e == cudaSuccess) {
+      ProfScope ps(h, K_EVAP_FIXUP, P.s_cmp[0]);
+      e = launch_rain_ice_evap_fixup(a, P.s_cmp[0]);
     }
-    if (e == cudaSuccess) e = cudaEventRecord(P.fix_done, P.s_cmp);
+    if (e == cudaSuccess) e = cudaEventRecord(P.fix_done, P.s_cmp[0]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(P.s_out, P.fix_done, 0);
     long off_pts = 0;
     for (long i = 0; i < nslab && e == cudaSuccess; ++i) {
@@ -759,9 +779,11 @@ int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3
       off_pts += w * nk;
     }
   }
-  // drain all three streams before returning (the call is synchronous)
+  // drain all streams before returning (the call is synchronous)
   const cudaError_t e1 = cudaStreamSynchronize(P.s_in);
-  const cudaError_t e2 = cudaStreamSynchronize(P.s_cmp);
+  cudaError_t e2 = cudaStreamSynchronize(P.s_cmp[0]);
+  const cudaError_t e2b = cudaStreamSynchronize(P.s_cmp[1]);
+  if (e2 == cudaSuccess) e2 = e2b;
   const cudaError_t e3 = cudaStreamSynchronize(P.s_out);
   if (rc != ICE3GB_OK) return rc;
   if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;

@@ -271,7 +271,8 @@ def test_physics_step_matches_oracle_and_host_path():
 def test_physics_step_host_slab_pipeline_matches_device(nij):
     """The host entry point runs the step in column slabs (4096 columns and
     more, the first and last three graded down to a quarter when the grid
-    holds six) on three streams; its outputs, evap3d's fix-up on the maximum
+    holds six) on a copy-in, two compute and a copy-out stream; its outputs,
+    evap3d's fix-up on the maximum
     pass key of the whole call included, equal the device entry point's bit
     for bit, also with a ragged slab."""
     from ice3gb.components import Ice3Handle

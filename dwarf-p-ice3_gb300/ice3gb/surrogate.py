@@ -299,9 +299,33 @@ def physics_step_surrogate(handle, surrogate: SlowSurrogate, fields: "_abi.StepF
     return dict(zip(_abi.SUR_STATS, (int(v) for v in stats)))
 
 
+def time_inference(sur: SlowSurrogate, rows: int, reps: int = 5) -> Dict[str, float]:
+    """Device time of the network on `rows` standardised feature rows (CUDA
+    events on the current stream, after one warm-up call): ms per call and
+    the tensor throughput it implies (2 * multiply-adds of the layers)."""
+    n_in, n_hid, nh, n_out = sur.mlp.shape
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(0)
+    x = torch.randn((rows, n_in), generator=gen, device="cuda", dtype=torch.float32)
+    sur.mlp(x)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        sur.mlp(x)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flop = 2.0 * rows * (n_in * n_hid + (nh - 1) * n_hid * n_hid + n_hid * n_out)
+    return {"rows": rows, "ms": ms, "tflops": flop / (ms * 1e-3) / 1e12,
+            "path": "fused" if (n_in, n_hid, nh) == (16, 256, 3) else "one GEMM launch per layer"}
+
+
 def main(argv=None) -> int:
     """Train the surrogate on the GPU and save it:
-    python -m ice3gb.surrogate --points 16777216 --epochs 12 --out PATH"""
+    python -m ice3gb.surrogate --points 16777216 --epochs 12 --out PATH
+    (--hidden / --layers for another width or depth, --time-rows N to time
+    the network on N rows)"""
     import argparse
     import json
     import time
@@ -312,21 +336,27 @@ def main(argv=None) -> int:
     ap.add_argument("--batch", type=int, default=16384)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--hidden", type=int, default=256)
+    ap.add_argument("--layers", type=int, default=3)
+    ap.add_argument("--time-rows", type=int, default=0)
     ap.add_argument("--out", default=DEFAULT_PATH)
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
     t0 = time.time()
     raw, tgt = training_set(a.points, seed=1000)
     t1 = time.time()
-    sur = SlowSurrogate(seed=a.seed)
+    sur = SlowSurrogate(seed=a.seed, n_hidden=a.hidden, n_hidden_layers=a.layers)
     sur.train(raw, tgt, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed)
     torch.cuda.synchronize()
     t2 = time.time()
     ev_raw, ev_tgt = training_set(a.eval_points, seed=900000)
-    rep = {"train_points": a.points, "epochs": a.epochs, "batch": a.batch, "lr": a.lr,
+    rep = {"hidden": a.hidden, "layers": a.layers, "train_points": a.points, "epochs": a.epochs, "batch": a.batch,
+           "lr": a.lr,
            "sample_s": t1 - t0, "train_s": t2 - t1, "history": sur.history,
            "held_out": sur.rate_errors(ev_raw, ev_tgt),
            "held_out_inside_envelope": float(sur.inside(sur.standardize(ev_raw)).double().mean())}
+    if a.time_rows:
+        rep["inference"] = time_inference(sur, a.time_rows)
     sur.save(a.out)
     print(json.dumps(rep, indent=1))
     if a.report:

@@ -96,6 +96,8 @@ ICE3_HD double dmax(double a, double b) { return gtd(a, b) ? a : b; }
 ICE3_HD double dmin(double a, double b) { return gtd(a, b) ? b : a; }
 // a == +-0.
 ICE3_HD bool zerod_(double a) { return (opaque_bits(a) << 1) == 0; }
+// x < 0 (not -0), on the bit pattern.
+ICE3_HD bool negd(double x) { return fm::bits_(x) < 0 && fm::bits_(x) != INT64_MIN; }
 // |a| > b for b >= +0.
 ICE3_HD bool abs_gtp(double a, double b) { return (fm::bits_(a) & 0x7fffffffffffffffLL) > fm::bits_(b); }
 // a != 0 (nor -0), on the bit pattern.

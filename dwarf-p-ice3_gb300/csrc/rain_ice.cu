@@ -18,11 +18,13 @@
 //    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;
 //  * points are processed in regime order: a first kernel sorts each tile of
-//    32,768 points by which hydrometeors are present and whether T < TT (the
+//    131,072 points by which hydrometeors are present and whether T < TT (the
 //    masks that decide which process branches and how many sub-steps a point
 //    takes), so a warp's lanes take the same branches instead of the union
 //    of all regimes; the tile keeps the gathered accesses within a window of
-//    256 KB per field.  Results do not depend on the order;
+//    1 MB per field (tiles of 32,768 / 65,536 / 131,072 points: rain_ice
+//    171.6 / 170.6 / 170.2 ms at 1024x1024x90, fewer part-filled warps at
+//    the regime boundaries).  Results do not depend on the order;
 //  * with a PRFR option a column kernel first forms the precipitation
 //    fraction the sub-stepping starts from (prfr_column);
 //  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
@@ -54,13 +56,17 @@ __global__ void rain_ice_prfr_kernel(const __grid_constant__ Cst c, const __grid
 // Processing order: per tile of ORDER_TILE points, a counting sort by regime
 // (bit 0..4: cloud, rain, ice, snow, graupel above XRTMIN; bit 5: T < TT).
 // Warp-aggregated shared-memory atomics give each point its slot in the tile;
-// the order inside a regime follows the atomics and does not matter.
-constexpr int ORDER_TILE = 32768, ORDER_THREADS = 1024, ORDER_BINS = 64;
+// the order inside a regime follows the atomics and does not matter.  The
+// tile's keys (one byte per point) sit in dynamic shared memory.
+#ifndef ICE3GB_ORDER_TILE
+#define ICE3GB_ORDER_TILE 131072
+#endif
+constexpr int ORDER_TILE = ICE3GB_ORDER_TILE, ORDER_THREADS = 1024, ORDER_BINS = 64;
 
 __global__ void __launch_bounds__(ORDER_THREADS) rain_ice_order_kernel(const __grid_constant__ Cst c,
                                                                        const __grid_constant__ RainIceArgs a)
 {
-  __shared__ unsigned char key[ORDER_TILE];
+  extern __shared__ unsigned char key[];   // [ORDER_TILE]
   __shared__ unsigned int cnt[ORDER_BINS];
   const Ice3gbRainIceFields &f = a.f;
   const long n = (long)a.nij * a.nk;
@@ -166,7 +172,9 @@ cudaError_t launch_rain_ice_order(const Cst &c, const RainIceArgs &a, cudaStream
 {
   const long n = (long)a.nij * a.nk;
   const long tiles = (n + ORDER_TILE - 1) / ORDER_TILE;
-  rain_ice_order_kernel<<<(unsigned)tiles, ORDER_THREADS, 0, s>>>(c, a);
+  cudaError_t e = cudaFuncSetAttribute(rain_ice_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ORDER_TILE);
+  if (e != cudaSuccess) return e;
+  rain_ice_order_kernel<<<(unsigned)tiles, ORDER_THREADS, ORDER_TILE, s>>>(c, a);
   return cudaGetLastError();
 }
 

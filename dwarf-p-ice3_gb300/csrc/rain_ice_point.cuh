@@ -193,8 +193,6 @@ ICE3_HD void ocnd2_column(const Cst &c, const Ice3gbRainIceFields &f, long nij, 
   }
 }
 
-// x < 0 (not -0), on the bit pattern.
-ICE3_HD bool negd(double x) { return fm::bits_(x) < 0 && fm::bits_(x) != INT64_MIN; }
 // x == 0 or -0, on the bit pattern.
 ICE3_HD bool zerod(double x) { return (opaque_bits(x) << 1) == 0; }
 

@@ -97,6 +97,17 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
 #pragma unroll
     for (int s = 0; s < 5; ++s) {
       if (s == 0 && skip_c) continue;
+      // a species that no lane of the warp moves at this level (content at
+      // or below its threshold and not negative, nothing falling in) has a
+      // zero flux and keeps its source; the warp skips its arithmetic
+      if (__all_sync(0xffffffffu, !c1[s] && !c2[s] && !negd(rt[s]) && zerod_(fabove[s]))) {
+        if (valid) {
+          if (io.src_out[s] && io.src_out[s] != io.src_in[s]) io.src_out[s][p] = src[s];
+          if (io.fpr[s]) io.fpr[s][p] = 0.0;
+        }
+        fabove[s] = 0.0;
+        continue;
+      }
       double w1, w2;
       warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, w1, w2);
       double flux = dmin(rhodz * rt[s] * inv_dt, w1 * rho * rt[s]);

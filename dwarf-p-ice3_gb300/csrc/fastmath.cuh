@@ -33,6 +33,12 @@
 //          3 FP64 ops (an IEEE FP64 divide costs ~9 on GB300).  fdiv(a, b) =
 //          a * frcp(b), within 2 ulp.  Outside 2^-125 < |d| < 2^125 (and for
 //          zero, inf, NaN) it falls back to the IEEE division.
+//   frsqrt 1/sqrt(d): y0 = the FP32 reciprocal of the FP32 square root of d
+//          (truncated to FP32; |eps| = |1 - d y0^2| < 2^-21), then
+//          y0 (1 + eps/2 + 3 eps^2/8), the series of (1 - eps)^(-1/2) to its
+//          quadratic term (remainder 5 eps^3/16 < 2^-63).  5 FP64 ops, within
+//          1 ulp; outside 2^-120 < d < 2^120 (and for zero, negative, inf,
+//          NaN) 1 / sqrt(d).
 //   fatan  reduction to [0, 1] by atan(x) = pi/2 - atan(1/x), then
 //          atan(y) = atan(c) + atan(r), c = j/64 the nearest table point,
 //          r = (y - c)/(1 + y c) (|r| <= 1/128), atan(r) by its Taylor series
@@ -86,6 +92,7 @@ __device__ __forceinline__ void atan_entry(bool comp, int j, double &hi, float &
   lo = __int_as_float((int)(uint32_t)__double_as_longlong(v.y));
 }
 __device__ __forceinline__ float rcpf_(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ float sqrtf_(float x) { return __fsqrt_rn(x); }
 __device__ __forceinline__ void exp_entry(int j, double &hi, float &lo)
 {
   const double2 v = __ldg(reinterpret_cast<const double2 *>(kExpTable) + j);
@@ -121,6 +128,7 @@ inline void atan_entry(bool comp, int j, double &hi, float &lo)
   hi = e.hi; lo = e.lo;
 }
 inline float rcpf_(float x) { volatile float r = 1.0f / x; return r; }
+inline float sqrtf_(float x) { volatile float r = std::sqrt(x); return r; }
 inline void exp_entry(int j, double &hi, float &lo) { hi = kExpTable[j].hi; lo = kExpTable[j].lo; }
 inline void log_entry(int i, double &invc, double &nlog_hi, float &nlog_lo, int &fold)
 {
@@ -278,6 +286,20 @@ FM_HD double frcp(double d)
   return fma_(r0, fma_(eps, eps, eps), r0);
 }
 FM_HD double fdiv(double a, double b) { return mul_(a, frcp(b)); }
+
+// 1/sqrt(d) (see the header) for 2^-120 < d < 2^120; frsqrt_ok tells.
+FM_HD bool frsqrt_ok(double d)
+{
+  const int64_t e = bits_(d) >> 52;                               // the sign bit makes e >= 2048
+  return e >= 1023 - 120 && e <= 1023 + 120;
+}
+FM_HD double frsqrt(double d)
+{
+  if (!frsqrt_ok(d)) return 1.0 / sqrt(d);                        // zero, tiny, huge, negative, inf, NaN
+  const double y0 = to_f64(rcpf_(sqrtf_(to_f32(d))));
+  const double eps = fma_(-d, mul_(y0, y0), 1.0);                  // y0^2 exact (24-bit y0)
+  return fma_(mul_(y0, eps), fma_(eps, 0.375, 0.5), y0);
+}
 
 // Arc tangent (see the header).
 FM_HD double fatan(double x)

@@ -191,14 +191,23 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
     const double ah = lvs * qsl * (it * it * d.irv) * (1.0 + qsl * d.rvrd);
     const double a = fm::frcp(1.0 + lvs * inv_cph * ah);
     const double sbar = a * (rt - qsl + ah * lvs * (OCND2 ? x.rc : x.rc + x.ri) * inv_cph);
-    double sigma;
-    if (c.LSIGMAS != 0.0 && c.LSTATNW == 0.0)
-      sigma = !(fge(x.sigqsat, 0.0) && fge(0.0, x.sigqsat)) ? sqrt(sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a))
-                                                             : 2.0 * x.sigs;
-    else
+    // sigma = sqrt(S) as S * S^(-1/2), the reciprocal reused for q1 when the
+    // 1e-10 floor leaves sigma alone
+    double sigma, isig = 0.0;
+    if (c.LSIGMAS != 0.0 && c.LSTATNW == 0.0 && !(fge(x.sigqsat, 0.0) && fge(0.0, x.sigqsat))) {
+      const double s2 = sq(2.0 * x.sigs) + sq(x.sigqsat * qsl * a);
+      if (fm::frsqrt_ok(s2)) {
+        isig = fm::frsqrt(s2);
+        sigma = s2 * isig;
+      } else {
+        sigma = sqrt(s2);
+      }
+    } else {
       sigma = 2.0 * x.sigs;
-    sigma = nmax(1e-10, sigma);
-    const double q1 = fm::fdiv(sbar, sigma);
+    }
+    const double sig = nmax(1e-10, sigma);
+    const double q1 = (nz(isig) && fm::bits_(sig) == fm::bits_(sigma)) ? sbar * isig : fm::fdiv(sbar, sig);
+    sigma = sig;
     if (srcs) *srcs = sigrc_cb(c, q1);
     double cond;
     if (fgt(q1, 0.0)) cond = fge(2.0, q1) ? nmin(0.36787944117144233 + 0.66 * q1 + 0.086 * q1 * q1, 2.0) : q1;

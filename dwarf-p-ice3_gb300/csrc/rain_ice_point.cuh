@@ -533,7 +533,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     orr->colf = colf;
     orr->acrf = acrf;
   }
-  const double cj = fm::fdiv(c.SCFAC * fm::fexp(0.3 * pf.lrho), sqrt(1.718e-5 + 4.9e-8 * (t - c.TT)));
+  const double cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) * fm::frsqrt(1.718e-5 + 4.9e-8 * (t - c.TT));
   const double ssi_rai = fm::fdiv(R.ssi, rho * ai);
   Slopes s;
   slopes(c, d, pf.lrho, t, v, s);
@@ -902,7 +902,9 @@ ICE3_HD void aggregate(const Cst &c, double t, const double *v, double lvfact, d
   } else {
     b[B_RRACCSS] = b[B_RRACCSG] = b[B_RSACCRG] = 0.0;
   }
-  const double rdryg_init = rg[RG_RCDRYG] + rg[RG_RIDRYG] + rg[RG_RSDRYG] + rg[RG_RRDRYG];
+  // the dry-growth sum is read only where graupel is present (and by the hail rows)
+  double rdryg_init = 0.0;
+  if (H || warp_any(has_g)) rdryg_init = rg[RG_RCDRYG] + rg[RG_RIDRYG] + rg[RG_RSDRYG] + rg[RG_RRDRYG];
   bool ldwetg = false, lldryg = false;
   double rwetg_init = 0.0;
   if (has_g) {
@@ -1138,43 +1140,54 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
 {
   if (O) nucleation_ocnd2(c, *op, t, v[IRV], cit, b[B_RVHENI_MR]);
   else nucleation(c, d, v[ITH], pf.pres, pf.rho, pf.zx, lsfact, t, v[IRV], cit, b[B_RVHENI_MR], tt);
-  v[ITH] += b[B_RVHENI_MR] * lsfact;
-  t = v[ITH] * pf.exn;
-  v[IRV] -= b[B_RVHENI_MR];
-  v[IRI] += b[B_RVHENI_MR];
+  // each adjustment below moves the state only where its amount is nonzero
+  // (x + 0 = x), and a warp skips the updates when none of its lanes has one
+  const double lsv = lsfact - lvfact;
+  if (warp_any(nz(b[B_RVHENI_MR]))) {
+    v[ITH] += b[B_RVHENI_MR] * lsfact;
+    t = v[ITH] * pf.exn;
+    v[IRV] -= b[B_RVHENI_MR];
+    v[IRI] += b[B_RVHENI_MR];
+  }
   // RRHONG (mode_ice4_rrhong.F90)
   double r = 0.0;
   if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
     r = v[IRR];
-    if (d.lfeedbackt) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / (lsfact - lvfact)));
+    if (d.lfeedbackt) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / lsv));
   }
   b[B_RRHONG_MR] = r;
-  v[ITH] += r * (lsfact - lvfact);
-  t = v[ITH] * pf.exn;
-  v[IRR] -= r;
-  v[IRG] += r;
+  if (warp_any(nz(r))) {
+    v[ITH] += r * lsv;
+    t = v[ITH] * pf.exn;
+    v[IRR] -= r;
+    v[IRG] += r;
+  }
   // RIMLTC (mode_ice4_rimltc.F90)
   r = 0.0;
   if (pos(v[IRI]) && gtp(t, c.TT)) {
     r = v[IRI];
     if (d.lfeedbackt) {
       // the IEEE quotient only where it can be below r
-      const double num = v[ITH] - pf.zx, den = lsfact - lvfact;
-      if (!quot_above(num, den, r)) r = dmin(r, pmax0(num / den));
+      const double num = v[ITH] - pf.zx;
+      if (!quot_above(num, lsv, r)) r = dmin(r, pmax0(num / lsv));
     }
   }
   b[B_RIMLTC_MR] = r;
-  v[ITH] -= r * (lsfact - lvfact);
-  t = v[ITH] * pf.exn;
-  v[IRC] += r;
-  v[IRI] -= r;
-  const double lsv = lsfact - lvfact;
-  B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
-  B[IRV] = -b[B_RVHENI_MR];
-  B[IRC] = b[B_RIMLTC_MR];
-  B[IRR] = -b[B_RRHONG_MR];
-  B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
-  B[IRG] = b[B_RRHONG_MR];
+  if (warp_any(nz(r))) {
+    v[ITH] -= r * lsv;
+    t = v[ITH] * pf.exn;
+    v[IRC] += r;
+    v[IRI] -= r;
+  }
+  // B stays zero (as tendencies() set it) where all three amounts are zero
+  if (warp_any(nz(b[B_RVHENI_MR]) || nz(b[B_RRHONG_MR]) || nz(b[B_RIMLTC_MR]))) {
+    B[ITH] = b[B_RVHENI_MR] * lsfact + b[B_RRHONG_MR] * lsv - b[B_RIMLTC_MR] * lsv;
+    B[IRV] = -b[B_RVHENI_MR];
+    B[IRC] = b[B_RIMLTC_MR];
+    B[IRR] = -b[B_RRHONG_MR];
+    B[IRI] = b[B_RVHENI_MR] - b[B_RIMLTC_MR];
+    B[IRG] = b[B_RRHONG_MR];
+  }
 }
 
 // ICE4_TENDENCIES for one point (mode_ice4_tendencies.F90): on a hard pass
@@ -1313,12 +1326,16 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       // MAX(MIN over all of them, MNH_TINY); a species' IEEE quotient is only
       // formed where it can be below the running minimum
       bool limited = false;
+      double mt_hi = maxtime + fabs(maxtime) * 0x1p-18;   // est_above's bound, updated with maxtime
 #pragma unroll
       for (int v = 1; v < NVT; ++v) {
         if (ltd(A[v], -1.e-20) && gtp(vart[v], rsmin[v])) {
           limited = true;
           const double num = -(B[v] + vart[v]);
-          if (!quot_above(num, A[v], maxtime)) maxtime = dmin(maxtime, num / A[v]);
+          if (!gtd(quot_est(num, A[v]), mt_hi)) {
+            maxtime = dmin(maxtime, num / A[v]);
+            mt_hi = maxtime + fabs(maxtime) * 0x1p-18;
+          }
         }
       }
       if (limited) maxtime = dmax(maxtime, c.MNH_TINY);
@@ -1418,8 +1435,10 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   // rain_ice.F90:334-345 (L/cph without exner) and :370-381 (LLMICRO)
   const double zdev = c.CPD + c.CPV * rv + c.CL * (rc + rr) + c.CI * (H ? ri + rs + rg + rh : ri + rs + rg);
   const double t = th * pf.exn;
-  const double lsf = (c.LSTT + (c.CPV - c.CI) * (t - c.TT)) / zdev;
-  const double lvf = (c.LVTT + (c.CPV - c.CL) * (t - c.TT)) / zdev;
+  // L_s / cph and L_v / cph for the total tendencies (one reciprocal for
+  // both); the IEEE lsfact that nucleation's T-feedback limit needs outside
+  // micro points is formed there
+  const double ls_num = c.LSTT + (c.CPV - c.CI) * (t - c.TT), lv_num = c.LVTT + (c.CPV - c.CL) * (t - c.TT);
   OcndPt op;
   if (O) {
     op.tw = tw;
@@ -1432,8 +1451,8 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
                           gtp(rs, c.FRMIN13) || gtp(rg, c.FRMIN13) || (H && gtp(rh, c.FRMIN13)))
                        : (gtp(rc, c.C_RTMIN) || gtp(rr, c.R_RTMIN) || gtp(ri, c.I_RTMIN) || gtp(rs, c.S_RTMIN) ||
                           gtp(rg, c.G_RTMIN) || (H && gtp(rh, c.H_RTMIN)));
-  const double iexnref = fm::frcp(exnref);
-  const double lsx = lsf * iexnref, lvx = lvf * iexnref;
+  const double izx = fm::frcp(zdev) * fm::frcp(exnref);
+  const double lsx = ls_num * izx, lvx = lv_num * izx;
   // with a PRFR option the sub-stepping starts from the precipitation
   // fraction of prfr_column (rain_ice.F90:555-602, ICE4_PACK :326)
   const bool llrfr = d.llrfr;
@@ -1442,7 +1461,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   if (!micro) {
     cit = 0.0;
     if (O) nucleation_ocnd2(c, op, t, rv, cit, zrvheni);
-    else nucleation(c, d, th, pf.pres, pf.rho, pf.zx, lsf / pf.exn, t, rv, cit, zrvheni);
+    else nucleation(c, d, th, pf.pres, pf.rho, pf.zx, ls_num / zdev / pf.exn, t, rv, cit, zrvheni);
   }
   zrvheni = dmin(rvs, zrvheni * inv_dt);
   if (micro) {

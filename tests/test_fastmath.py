@@ -106,3 +106,13 @@ def test_fatan_within_2ulp(fm):
     edge = fm(4, np.array([np.inf, -np.inf, np.nan, -0.0, 1e300]))
     assert edge[0] == np.pi / 2 and edge[1] == -np.pi / 2 and np.isnan(edge[2]) and edge[3] == 0.0
     assert edge[4] == np.pi / 2
+
+
+def test_frsqrt_within_1ulp(fm):
+    rng = np.random.default_rng(7)
+    xs = np.concatenate([10.0 ** rng.uniform(-36, 36, 4000), rng.uniform(1.0, 4.0, 3000),
+                         rng.uniform(1e-12, 1e-7, 2000), [1.0, 2.0, 4.0, 0.25, 3.0, 1.718e-5, 2.0 ** 119]])
+    assert ulp_err(fm(5, xs), lambda v: 1 / mp.sqrt(v), xs) <= 1.0
+    edge = fm(5, np.array([0.0, np.inf, -1.0, np.nan, 1e-300, 1e300]))
+    assert edge[0] == np.inf and edge[1] == 0.0 and np.isnan(edge[2]) and np.isnan(edge[3])
+    assert edge[4] == 1.0 / np.sqrt(1e-300) and edge[5] == 1.0 / np.sqrt(1e300)

@@ -92,6 +92,9 @@ struct Derived {
   // or compares the FP64 table entries
   int aucv_rc, aucv_ri, prpdf, accr, evap, snow_riming;
   int lwarm, lfeedbackt, lsnow_t, lcrflimit, llrfr;
+  // differences of table constants, formed once per block (the same IEEE
+  // values as formed in place)
+  double cpv_cl, cpv_ci, ci_cl, tt_m35, tt_m5, tt_m2;
 };
 
 ICE3_HD void make_derived(const Cst &c, Derived &d)
@@ -121,6 +124,12 @@ ICE3_HD void make_derived(const Cst &c, Derived &d)
   d.lsnow_t = c.LSNOW_T != 0.0;
   d.lcrflimit = c.LCRFLIMIT != 0.0;
   d.llrfr = d.accr == 1 || d.evap == 2;
+  d.cpv_cl = c.CPV - c.CL;
+  d.cpv_ci = c.CPV - c.CI;
+  d.ci_cl = c.CI - c.CL;
+  d.tt_m35 = c.TT - 35.0;
+  d.tt_m5 = c.TT - 5.0;
+  d.tt_m2 = c.TT - 2.0;
 }
 
 // Rates that persist between the hard pass and the following soft passes
@@ -221,9 +230,9 @@ ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst
   zusw = fm::fdiv(zusw * (pabst - zzw), zzw * (pabst - zusw)) - 1.0;
   zssi = dmin(zssi, zusw);
   zzw = 0.0;
-  if (ltp(t, c.TT - 5.0) && pos(zssi)) {
+  if (ltp(t, d.tt_m5) && pos(zssi)) {
     zzw = c.NU20 * fm::fexp(c.ALPHA2 * zssi - c.BETA2);
-  } else if (!gtp(t, c.TT - 2.0) && !ltp(t, c.TT - 5.0) && pos(zssi)) {
+  } else if (!gtp(t, d.tt_m2) && !ltp(t, d.tt_m5) && pos(zssi)) {
     zzw = dmax(d.nu20_eb2, c.NU10 * fm::fexp(-c.BETA1 * (t - c.TT) + c.ALPHA1 * fm::flog(fm::fdiv(zssi, zusw))));
   }
   zzw = dmin(zzw - cit, 50.e3);
@@ -452,7 +461,7 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
     if (has_r && !has_c) {
       const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, fm::frcp(t), fm::flog(t));
       const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
-      const double av = fm::fdiv(sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)), ka * c.RV * t * t) +
+      const double av = fm::fdiv(sq(c.LVTT + d.cpv_cl * (t - c.TT)), ka * c.RV * t * t) +
                         fm::fdiv(c.RV * t, dv * esw);
       b[B_RREVAV] = fm::fdiv(pmax0(usw), pf.rho * av) *
                     (c.O0EVAR * fm::fexp(c.EX0EVAR * s.llbdar) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
@@ -466,7 +475,7 @@ ICE3_HD void warm_subgrid(const Cst &c, const Derived &d, const PointFix &pf, do
       const double zw2 = fm::fdiv(thlt * t, tht);
       const double esw = esat_from(c.ALPW, c.BETAW, c.GAMW, fm::frcp(zw2), fm::flog(zw2));
       const double usw = 1.0 - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
-      const double av = fm::fdiv(sq(c.LVTT + (c.CPV - c.CL) * (zw2 - c.TT)), ka * c.RV * zw2 * zw2) +
+      const double av = fm::fdiv(sq(c.LVTT + d.cpv_cl * (zw2 - c.TT)), ka * c.RV * zw2 * zw2) +
                         fm::fdiv(c.RV * zw2, dv * esw);
       b[B_RREVAV] = fm::fdiv(pmax0(usw), pf.rho * av) *
                     (c.O0EVAR * fm::fexp(c.EX0EVAR * lz3) + c.O1EVAR * cj * fm::fexp(c.EX1EVAR * lz3)) *
@@ -512,7 +521,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
   const double ika = fm::frcp(ka), idv = fm::frcp(dv);
   const double ai = O ? tiwmx_at(op->tw + TW_A2 * kTiwmxN, t) + tiwmx_at(op->tw + TW_BB3 * kTiwmxN, t) * pf.pres
-                      : sq(c.LSTT + (c.CPV - c.CI) * (t - c.TT)) * (ika * d.irv * it * it) +
+                      : sq(c.LSTT + d.cpv_ci * (t - c.TT)) * (ika * d.irv * it * it) +
                             (c.RV * t) * fm::fdiv(idv, esi);
   double colf = 1.0, acrf = 1.0;
   if (O) {
@@ -565,7 +574,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     const double ei = c.LEVLIMIT != 0.0 ? dmin(ev, esi_f) : ev;
     const double ew = c.LEVLIMIT != 0.0 ? dmin(ev, esw) : ev;
     const double kt = ka * (c.TT - t);
-    const double dl = dv * (c.LVTT + (c.CPV - c.CL) * (t - c.TT));
+    const double dl = dv * (c.LVTT + d.cpv_cl * (t - c.TT));
     const double irt = it * d.irv;
     heat_i = kt + (dl * (c.ESTT - ei) * irt);
     heat_w = kt + (dl * (c.ESTT - ew) * irt);
@@ -574,7 +583,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // ---- ICE4_SLOW (mode_ice4_slow.F90); taken from the surrogate instead
   // where it supplies them (slow_rates_from) ----
   if (!(SUR && learned_slow)) {
-    b[B_RCHONI] = (ltp(t, c.TT - 35.0) && has_c)
+    b[B_RCHONI] = (ltp(t, d.tt_m35) && has_c)
                       ? dmin(1000., c.HON * rho * v[IRC] * fm::fexp(c.ALPHA3 * (t - c.TT) - c.BETA3))
                       : 0.0;
     b[B_RVDEPS] = (has_v && has_s) ? (O ? ssi_rai * vent_s * c.FRMIN40 : ssi_rai * vent_s) : 0.0;
@@ -599,7 +608,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
                                    : 0.0;
     if (has_r && !has_c) {
       const double usw = 1. - fm::fdiv(v[IRV] * (pf.pres - esw), c.EPSILO * esw);
-      const double av = sq(c.LVTT + (c.CPV - c.CL) * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esw);
+      const double av = sq(c.LVTT + d.cpv_cl * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esw);
       b[B_RREVAV] = fm::fdiv(pmax0(usw), rho * av) *
                     (c.O0EVAR * (d.ex0evar_m2 ? ilr * ilr : fm::fexp(c.EX0EVAR * s.llbdar)) +
                      c.O1EVAR * cj * fm::fexp(c.EX1EVAR * s.llbdar));
@@ -611,7 +620,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // ---- ICE4_FAST_RS rates (mode_ice4_fast_rs.F90) ----
   // collision-freezing denominator, shared with ICE4_FAST_RG
   const double den = (has_s || has_g || has_h) ? fm::frcp(rho * (c.LMTT - c.CL * (c.TT - t))) : 0.0;
-  const double freez2 = (rho * (c.LMTT + (c.CI - c.CL) * (c.TT - t))) * den;
+  const double freez2 = (rho * (c.LMTT + d.ci_cl * (c.TT - t))) * den;
   rs[RS_FREEZ1] = has_s ? heat_i * vent_s * den : 0.0;
   rs[RS_FREEZ2] = has_s ? freez2 : 0.0;
   if (has_c && has_s) {
@@ -808,7 +817,7 @@ ICE3_HD void soft_rates(const Cst &c, const Derived &d, double t, const double *
   const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
   const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
   const bool warm = gtp(t, c.TT);
-  if (!(ltp(t, c.TT - 35.0) && has_c)) b[B_RCHONI] = 0.0;
+  if (!(ltp(t, d.tt_m35) && has_c)) b[B_RCHONI] = 0.0;
   if (!(has_v && has_s)) b[B_RVDEPS] = 0.0;
   if (!(has_i && has_s)) b[B_RIAGGS] = 0.0;
   if (!gtp(hi[2], c.I_RTMIN)) b[B_RIAUTS] = 0.0;
@@ -1151,9 +1160,16 @@ ICE3_HD void hard_adjust(const Cst &c, const Derived &d, const PointFix &pf, dou
   }
   // RRHONG (mode_ice4_rrhong.F90)
   double r = 0.0;
-  if (ltp(t, c.TT - 35.0) && gtp(v[IRR], c.R_RTMIN)) {
+  if (ltp(t, d.tt_m35) && gtp(v[IRR], c.R_RTMIN)) {
     r = v[IRR];
-    if (d.lfeedbackt) r = dmin(r, pmax0(((c.TT - 35.0) / pf.exn - v[ITH]) / lsv));
+    if (d.lfeedbackt) {
+      // the IEEE quotients only where the limit can bind: (TT - 35)/exn
+      // estimated within 2^-22 and taken 2^-20 low, so that the estimated
+      // quotient is below the true one
+      const double zq = quot_est(d.tt_m35, pf.exn);
+      if (!quot_above(zq - fabs(zq) * 0x1p-20 - v[ITH], lsv, r))
+        r = dmin(r, pmax0((d.tt_m35 / pf.exn - v[ITH]) / lsv));
+    }
   }
   b[B_RRHONG_MR] = r;
   if (warp_any(nz(r))) {
@@ -1301,8 +1317,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       if (H) zsum2 += vart[IRH];
       const double zdev = (c.CPD + c.CPV * vart[IRV] + c.CL * (vart[IRC] + vart[IRR]) + c.CI * zsum2) * pf.exn;
       const double zzt = vart[ITH] * pf.exn;
-      const double lsfact = (c.LSTT + (c.CPV - c.CI) * (zzt - c.TT)) / zdev;
-      const double lvfact = (c.LVTT + (c.CPV - c.CL) * (zzt - c.TT)) / zdev;
+      const double lsfact = (c.LSTT + d.cpv_ci * (zzt - c.TT)) / zdev;
+      const double lvfact = (c.LVTT + d.cpv_cl * (zzt - c.TT)) / zdev;
       double A[NVT], B[NVT];
       tendencies<SUR, SUBG, H, O>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
                                   &HR, hlut, op, &OR, ext);    // A includes the external tendencies
@@ -1438,7 +1454,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   // L_s / cph and L_v / cph for the total tendencies (one reciprocal for
   // both); the IEEE lsfact that nucleation's T-feedback limit needs outside
   // micro points is formed there
-  const double ls_num = c.LSTT + (c.CPV - c.CI) * (t - c.TT), lv_num = c.LVTT + (c.CPV - c.CL) * (t - c.TT);
+  const double ls_num = c.LSTT + d.cpv_ci * (t - c.TT), lv_num = c.LVTT + d.cpv_cl * (t - c.TT);
   OcndPt op;
   if (O) {
     op.tw = tw;

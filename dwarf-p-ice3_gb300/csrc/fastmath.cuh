@@ -275,17 +275,66 @@ FM_NI double flog(double x)
   return add_(hi, add_(r, tail));
 }
 
+// The IEEE 1/d and 1/sqrt(d), out of line: the rare fallbacks of frcp and
+// frsqrt, which are inlined at many sites.
+FM_NI double rcp_ieee_(double d) { return 1.0 / d; }
+FM_NI double rsqrt_ieee_(double d) { return 1.0 / sqrt(d); }
+
 // 1/d (see the header): FP32 seed + one Newton-Raphson step with its
 // quadratic term.
 FM_HD double frcp(double d)
 {
   const int64_t e = (bits_(d) >> 52) & 0x7ff;
-  if (e < 1023 - 125 || e > 1023 + 125) return 1.0 / d;          // zero, tiny, huge, inf, NaN
+  if (e < 1023 - 125 || e > 1023 + 125) return rcp_ieee_(d);     // zero, tiny, huge, inf, NaN
   const double r0 = to_f64(rcpf_(to_f32(d)));
   const double eps = fma_(-d, r0, 1.0);
   return fma_(r0, fma_(eps, eps, eps), r0);
 }
 FM_HD double fdiv(double a, double b) { return mul_(a, frcp(b)); }
+
+// a / b rounded to nearest (the IEEE quotient) for 2^-400 <= |a|, |b| <=
+// 2^400, from y = frcp(b): q0 = a y, then q1 = q0 + (a - b q0) y, checked
+// with the exact remainder r = a - b q1 (one fma): q1 is the rounded quotient
+// iff |r| < |b| ulp(q1) / 2 (a / b is never halfway between two doubles; q1
+// a power of two, whose lower neighbour is closer, is not accepted).  Where
+// the check fails or the operands are out of range, the IEEE division.  4
+// FP64 operations per quotient besides the reciprocal; the check is integer
+// work.  fdiv_rn2 shares the reciprocal between two numerators.
+// the IEEE division, out of line (the rare fallback of the paths below)
+FM_NI double div_ieee_(double a, double b) { return a / b; }
+FM_HD bool div_rn_range_(double x)
+{
+  const int64_t e = (bits_(x) >> 52) & 0x7ff;
+  return e >= 1023 - 400 && e <= 1023 + 400;
+}
+FM_HD double div_rn_with_(double a, double b, double y)
+{
+  const double q0 = mul_(a, y);
+  const double q1 = fma_(fma_(-q0, b, a), y, q0);
+  const double r = fma_(-q1, b, a);
+  const int64_t bq = bits_(q1) & 0x7fffffffffffffffLL, bb = bits_(b) & 0x7fffffffffffffffLL;
+  // |b| ulp(q1) / 2 = |b| 2^(E(q1) - 1023 - 53): add to b's exponent
+  const int64_t eh = (bb >> 52) + (bq >> 52) - (1023 + 53);
+  if (eh >= 1 && (bq & 0x000fffffffffffffLL) != 0 && (bits_(r) & 0x7fffffffffffffffLL) < bb + ((eh - (bb >> 52)) << 52))
+    return q1;
+  return div_ieee_(a, b);
+}
+FM_HD double fdiv_rn(double a, double b)
+{
+  if (!(div_rn_range_(a) && div_rn_range_(b))) return div_ieee_(a, b);
+  return div_rn_with_(a, b, frcp(b));
+}
+FM_HD void fdiv_rn2(double a1, double a2, double b, double &q1, double &q2)
+{
+  if (!(div_rn_range_(a1) && div_rn_range_(a2) && div_rn_range_(b))) {
+    q1 = div_ieee_(a1, b);
+    q2 = div_ieee_(a2, b);
+    return;
+  }
+  const double y = frcp(b);
+  q1 = div_rn_with_(a1, b, y);
+  q2 = div_rn_with_(a2, b, y);
+}
 
 // 1/sqrt(d) (see the header) for 2^-120 < d < 2^120; frsqrt_ok tells.
 FM_HD bool frsqrt_ok(double d)
@@ -295,7 +344,7 @@ FM_HD bool frsqrt_ok(double d)
 }
 FM_HD double frsqrt(double d)
 {
-  if (!frsqrt_ok(d)) return 1.0 / sqrt(d);                        // zero, tiny, huge, negative, inf, NaN
+  if (!frsqrt_ok(d)) return rsqrt_ieee_(d);                       // zero, tiny, huge, negative, inf, NaN
   const double y0 = to_f64(rcpf_(sqrtf_(to_f32(d))));
   const double eps = fma_(-d, mul_(y0, y0), 1.0);                  // y0^2 exact (24-bit y0)
   return fma_(mul_(y0, eps), fma_(eps, 0.375, 0.5), y0);

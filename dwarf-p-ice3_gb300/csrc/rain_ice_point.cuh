@@ -1296,9 +1296,9 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
   int passes = 0, outer = 0, inner = 0;
   rrevav = 0.0;
   capped = false;
-  // TT/exn, lsfact and lvfact with IEEE divisions, as the Fortran: the
+  // TT/exn, lsfact and lvfact are the IEEE quotients, as the Fortran's (the
   // LFEEDBACKT sub-step ends with th on TT/exn, and which side of TT the next
-  // pass sees is decided by their rounding
+  // pass sees is decided by their rounding), formed by fm::fdiv_rn(2)
   const double zx = pf.zx;
   while (ltd(ztime, dt)) {
     ++outer;
@@ -1317,8 +1317,8 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
       if (H) zsum2 += vart[IRH];
       const double zdev = (c.CPD + c.CPV * vart[IRV] + c.CL * (vart[IRC] + vart[IRR]) + c.CI * zsum2) * pf.exn;
       const double zzt = vart[ITH] * pf.exn;
-      const double lsfact = (c.LSTT + d.cpv_ci * (zzt - c.TT)) / zdev;
-      const double lvfact = (c.LVTT + d.cpv_cl * (zzt - c.TT)) / zdev;
+      double lsfact, lvfact;     // the IEEE quotients (fdiv_rn2: one reciprocal, checked)
+      fm::fdiv_rn2(c.LSTT + d.cpv_ci * (zzt - c.TT), c.LVTT + d.cpv_cl * (zzt - c.TT), zdev, lsfact, lvfact);
       double A[NVT], B[NVT];
       tendencies<SUR, SUBG, H, O>(c, d, lut, soft, pf, lvfact, lsfact, cit, zzt, vart, R, rainfr, hl, hi, A, B, sur,
                                   &HR, hlut, op, &OR, ext);    // A includes the external tendencies
@@ -1333,7 +1333,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
           const double num = zx - B[ITH] - vart[ITH];
           const double e = quot_est(num, A[ITH]);
           if (!negd(e) && !est_above(e, maxtime)) {
-            const double thr = num / A[ITH];
+            const double thr = fm::fdiv_rn(num, A[ITH]);
             if (pos(thr)) maxtime = dmin(maxtime, thr);
           }
         }
@@ -1349,7 +1349,7 @@ ICE3_HD unsigned int stepping(const Cst &c, const Derived &d, const double *__re
           limited = true;
           const double num = -(B[v] + vart[v]);
           if (!gtd(quot_est(num, A[v]), mt_hi)) {
-            maxtime = dmin(maxtime, num / A[v]);
+            maxtime = dmin(maxtime, fm::fdiv_rn(num, A[v]));
             mt_hi = maxtime + fabs(maxtime) * 0x1p-18;
           }
         }
@@ -1439,7 +1439,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   pf.exn = ldp(f.exn, p);
   pf.rho = ldp(f.rhodref, p);
   pf.pres = ldp(f.pabs, p);
-  pf.zx = c.TT / pf.exn;
+  pf.zx = fm::fdiv_rn(c.TT, pf.exn);
   const double th = ldp(f.tht, p), rv = ldp(f.rvt, p), rc = ldp(f.rct, p), rr = ldp(f.rrt, p);
   const double ri = ldp(f.rit, p), rs = ldp(f.rst, p), rg = ldp(f.rgt, p);
   const double exnref = ldp(f.exnref, p);
@@ -1477,7 +1477,7 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
   if (!micro) {
     cit = 0.0;
     if (O) nucleation_ocnd2(c, op, t, rv, cit, zrvheni);
-    else nucleation(c, d, th, pf.pres, pf.rho, pf.zx, ls_num / zdev / pf.exn, t, rv, cit, zrvheni);
+    else nucleation(c, d, th, pf.pres, pf.rho, pf.zx, fm::fdiv_rn(fm::fdiv_rn(ls_num, zdev), pf.exn), t, rv, cit, zrvheni);
   }
   zrvheni = dmin(rvs, zrvheni * inv_dt);
   if (micro) {

@@ -34,7 +34,7 @@ ICE3_HD void point_fix(const Cst &c, const Ice3gbRainIceFields &f, long p, Point
   pf.exn = ldp(f.exn, p);
   pf.rho = ldp(f.rhodref, p);
   pf.pres = ldp(f.pabs, p);
-  pf.zx = c.TT / pf.exn;
+  pf.zx = fm::fdiv_rn(c.TT, pf.exn);
   pf.lrho = fm::flog(pf.rho);
   pf.rho_mcexvt = fm::fexp(-c.CEXVT * pf.lrho);
   const double irho = fm::frcp(pf.rho);

@@ -23,12 +23,15 @@ def fm(tmp_path_factory):
                    check=True)
     lib = ctypes.CDLL(str(out))
     lib.fm_eval.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long]
+    lib.fm_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.c_long]
 
     def ev(fn, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty_like(x)
         lib.fm_eval(fn, x.ctypes.data, y.ctypes.data, x.size)
         return y
+    ev.lib = lib
     return ev
 
 
@@ -116,3 +119,29 @@ def test_frsqrt_within_1ulp(fm):
     edge = fm(5, np.array([0.0, np.inf, -1.0, np.nan, 1e-300, 1e300]))
     assert edge[0] == np.inf and edge[1] == 0.0 and np.isnan(edge[2]) and np.isnan(edge[3])
     assert edge[4] == 1.0 / np.sqrt(1e-300) and edge[5] == 1.0 / np.sqrt(1e300)
+
+
+def test_fdiv_rn_is_the_ieee_quotient(fm):
+    """fdiv_rn / fdiv_rn2 return the IEEE quotient bit for bit: random
+    operands over the whole accepted range and magnitudes of the scheme,
+    significands near 1 and 2 (where ulp changes), powers of two, and values
+    outside the range (the fallback)."""
+    rng = np.random.default_rng(8)
+    n = 400000
+    a = np.concatenate([10.0 ** rng.uniform(-100, 100, n), rng.uniform(1e6, 3e6, n), -(10.0 ** rng.uniform(-20, 20, n)),
+                        np.ldexp(1.0 + rng.integers(0, 64, n) * 2.0 ** -52, rng.integers(-50, 50, n)),
+                        np.ldexp(2.0 - rng.integers(1, 64, n) * 2.0 ** -52, rng.integers(-50, 50, n))])
+    b = np.concatenate([10.0 ** rng.uniform(-100, 100, n), rng.uniform(900.0, 4000.0, n), 10.0 ** rng.uniform(-20, 20, n),
+                        np.ldexp(2.0 - rng.integers(1, 64, n) * 2.0 ** -52, rng.integers(-50, 50, n)),
+                        np.ldexp(1.0 + rng.integers(0, 64, n) * 2.0 ** -52, rng.integers(-50, 50, n))])
+    a = np.concatenate([a, [1.0, 3.0, 1e300, 1e-300, 0.0, -0.0, np.inf, np.nan, 7.0]])
+    b = np.concatenate([b, [4.0, 1.5, 3.0, 7.0, 2.0, 3.0, 5.0, 2.0, 0.0]])
+    q, q2 = np.empty_like(a), np.empty_like(a)
+    fm.lib.fm_div(0, a.ctypes.data, b.ctypes.data, q.ctypes.data, q2.ctypes.data, a.size)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ref = a / b
+        ref2 = (2.5 * a) / b
+    np.testing.assert_array_equal(q.view(np.uint64), ref.view(np.uint64))
+    fm.lib.fm_div(1, a.ctypes.data, b.ctypes.data, q.ctypes.data, q2.ctypes.data, a.size)
+    np.testing.assert_array_equal(q.view(np.uint64), ref.view(np.uint64))
+    np.testing.assert_array_equal(q2.view(np.uint64), ref2.view(np.uint64))

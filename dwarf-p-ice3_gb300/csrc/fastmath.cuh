@@ -64,10 +64,12 @@
 
 #if defined(__CUDACC__)
 #define FM_HD __host__ __device__ __forceinline__
-// exp, exp10 and log are called from dozens of sites of the large point
-// kernels: one out-of-line copy per kernel keeps those kernels' code in the
-// instruction cache (rain_ice 172.5 -> 171.5 ms, sedimentation 46.1 -> 44.7
-// ms per launch at 1024x1024x90 against inlined copies)
+// exp, exp10, log, the reciprocal and the rounded division are called from
+// dozens of sites of the large point kernels: one out-of-line copy per
+// kernel keeps those kernels' code in the instruction cache (rain_ice 172.5
+// -> 171.5 ms and sedimentation 46.1 -> 44.7 ms per launch at 1024x1024x90
+// for exp / log; rain_ice 162.4 -> 159.2 ms for the reciprocal, 160.7 ms
+// for the division)
 #define FM_NI static __host__ __device__ __noinline__
 #else
 #define FM_HD inline
@@ -282,7 +284,7 @@ FM_NI double rsqrt_ieee_(double d) { return 1.0 / sqrt(d); }
 
 // 1/d (see the header): FP32 seed + one Newton-Raphson step with its
 // quadratic term.
-FM_HD double frcp(double d)
+FM_NI double frcp(double d)
 {
   const int64_t e = (bits_(d) >> 52) & 0x7ff;
   if (e < 1023 - 125 || e > 1023 + 125) return rcp_ieee_(d);     // zero, tiny, huge, inf, NaN
@@ -319,12 +321,12 @@ FM_HD double div_rn_with_(double a, double b, double y)
     return q1;
   return div_ieee_(a, b);
 }
-FM_HD double fdiv_rn(double a, double b)
+FM_NI double fdiv_rn(double a, double b)
 {
   if (!(div_rn_range_(a) && div_rn_range_(b))) return div_ieee_(a, b);
   return div_rn_with_(a, b, frcp(b));
 }
-FM_HD void fdiv_rn2(double a1, double a2, double b, double &q1, double &q2)
+FM_NI void fdiv_rn2(double a1, double a2, double b, double &q1, double &q2)
 {
   if (!(div_rn_range_(a1) && div_rn_range_(a2) && div_rn_range_(b))) {
     q1 = div_ieee_(a1, b);

@@ -211,28 +211,37 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 
 // Bias + GELU of the 128 x 256 accumulator into the activation tile.  Warp
 // w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the 64 columns
-// 64 (w / 4) .. + 63, two 32-column loads in flight per wait.
+// 64 (w / 4) .. + 63 as two 32-column loads: the second is in flight while
+// the first half's GELU runs (the MUFU tanh is the epilogue's bound); the
+// biases are read four at a time (the same address for the whole warp).
+__device__ __forceinline__ void fz_gelu_half(const uint32_t r[32], const float *bias, int cb0, int row,
+                                             __nv_bfloat16 *sH)
+{
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int cb = cb0 + 8 * g;
+    const float4 b0 = *reinterpret_cast<const float4 *>(bias + cb);
+    const float4 b1 = *reinterpret_cast<const float4 *>(bias + cb + 4);
+    const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      w[j] = pack_bf16x2(gelu(__uint_as_float(r[8 * g + 2 * j]) + bb[2 * j]),
+                         gelu(__uint_as_float(r[8 * g + 2 * j + 1]) + bb[2 * j + 1]));
+    *reinterpret_cast<uint4 *>(sH + tc::core_off(row, cb, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
 __device__ __forceinline__ void fz_epilogue_gelu(uint32_t tmem, int warp, const float *bias, __nv_bfloat16 *sH)
 {
   const int q = warp & 3, c0 = (warp >> 2) * 64;
   const int row = 32 * q + (threadIdx.x & 31);
-  uint32_t r[2][32];
-  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, r[0]);
-  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 32), r[1]);
+  uint32_t r0[32], r1[32];
+  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, r0);
   tc::tmem_wait_ld();
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-      const int cb = c0 + 32 * h + 8 * g;
-      uint32_t w[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        w[j] = pack_bf16x2(gelu(__uint_as_float(r[h][8 * g + 2 * j]) + bias[cb + 2 * j]),
-                           gelu(__uint_as_float(r[h][8 * g + 2 * j + 1]) + bias[cb + 2 * j + 1]));
-      *reinterpret_cast<uint4 *>(sH + tc::core_off(row, cb, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-  }
+  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 32), r1);
+  fz_gelu_half(r0, bias, c0, row, sH);
+  tc::tmem_wait_ld();
+  fz_gelu_half(r1, bias, c0 + 32, row, sH);
 }
 
 __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFusedArgs a)

@@ -489,7 +489,11 @@ const char *ice3gb_kernel_name(int kernel_id);
 /* ---- host-buffer entry points (synchronous) ---------------------------- */
 /* Same as above with HOST pointers, as c_ice_adjust / c_rain_ice take them:
  * host->device copies, the kernels and device->host copies all run on
- * `stream`; the call returns when the outputs are in host memory. */
+ * `stream`; the call returns when the outputs are in host memory.
+ * ice3gb_physics_step_host runs the step in column slabs on the handle's
+ * own streams (copy-in, two compute, copy-out; ordered after the caller's
+ * earlier work on `stream`), so that the copies of one slab overlap the
+ * kernels of others; its outputs equal ice3gb_physics_step's bit for bit. */
 int ice3gb_ice_adjust_host(void *handle, int nij, int nk, double dt,
                            const Ice3gbIceAdjustFields *f, void *stream);
 int ice3gb_rain_ice_host(void *handle, int nij, int nk, double dt,

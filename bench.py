@@ -508,9 +508,36 @@ def run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist):
         total += ms
     ms_step = total / args.steps
     del host, pristine, outs
+    bw = copy_bandwidth(dev)
     return {"value": world * n / (ms_step / 1e3), "unit": "grid-points/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": ms_step,
-            "path": "ice3gb_physics_step_host, pinned host buffers"}
+            "path": "ice3gb_physics_step_host, pinned host buffers",
+            # the box's pinned-copy bandwidth, measured right after: the copies alone, one
+            # direction after the other, would take h2d / h2d_gbs + d2h / d2h_gbs
+            "copy_gbs": bw, "copies_alone_ms": 1e3 * (h2d / (bw["h2d"] * 1e9) + d2h / (bw["d2h"] * 1e9))}
+
+
+def copy_bandwidth(dev, nbytes=1 << 30, reps=3):
+    """Best-of-reps GB/s of one pinned host <-> device copy of nbytes each way."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / (best * 1e-3) / 1e9
+    del h, d
+    return out
 
 
 def main():

@@ -77,6 +77,9 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
     const double rho = valid ? sed_load(io.rhodref, p) : 1.0, dz = valid ? sed_load(io.dzz, p) : 1.0;
     const double rhodz = rho * dz;
     const double tsorhodz = fm::fdiv(dt, rhodz);
+    // per-level factors of the species' fluxes and sources (formed once
+    // instead of per species)
+    const double rhodz_idt = rhodz * inv_dt, tso_idt = tsorhodz * inv_dt, dz_idt = dz * inv_dt;
     double src[5], rt[5], qp[5];
     bool c1[5], c2[5];
     bool any = false;
@@ -110,11 +113,11 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
       }
       double w1, w2;
       warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, w1, w2);
-      double flux = dmin(rhodz * rt[s] * inv_dt, w1 * rho * rt[s]);
-      if (!zerod_(w2)) flux += pmax0(1.0 - fm::fdiv(dz, dt * w2)) * fabove[s];
+      double flux = dmin(rhodz_idt * rt[s], w1 * rho * rt[s]);
+      if (!zerod_(w2)) flux += pmax0(1.0 - dz_idt * fm::frcp(w2)) * fabove[s];
       if (valid) {
         if (io.src_out[s]) {
-          if (fortran) io.src_out[s][p] = src[s] + tsorhodz * (fabove[s] - flux) * inv_dt;
+          if (fortran) io.src_out[s][p] = src[s] + tso_idt * (fabove[s] - flux);
           else io.src_out[s][p] = src[s] + fm::fdiv(fabove[s] - flux, rhodz * dt);
         }
         if (io.fpr[s]) io.fpr[s][p] = flux;

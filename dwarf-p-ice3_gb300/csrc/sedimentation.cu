@@ -29,8 +29,8 @@ using namespace ice3sed;
 // busy, and the speeds shuffled back to the lanes that asked.  Same function
 // on the same arguments: the values are those of the per-lane evaluation.
 __device__ __forceinline__ void warp_fall_speeds(const Cst &c, int s, bool c1, double r1, bool c2, double r2,
-                                                 double lrho, double wlbda, const CloudPar &cp, double &w1,
-                                                 double &w2)
+                                                 double lrho, double wlbda, const CloudPar &cp, const double *fx,
+                                                 double &w1, double &w2)
 {
   const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
   const unsigned m1 = __ballot_sync(full, c1), m2 = __ballot_sync(full, c2);
@@ -53,7 +53,7 @@ __device__ __forceinline__ void warp_fall_speeds(const Cst &c, int s, bool c1, d
       cq.fsedc = __shfl_sync(full, cp.fsedc, owner);
     }
     double v = 0.0;
-    if (j < ntot) v = fall_speed(c, s, first ? ra : rb, lr, wl, cq);
+    if (j < ntot) v = fall_speed(c, s, first ? ra : rb, lr, wl, cq, fx);
     const double v1 = __shfl_sync(full, v, (unsigned)(i1 - base) & 31u);
     const double v2 = __shfl_sync(full, v, (unsigned)(i2 - base) & 31u);
     if (c1 && i1 >= base && i1 < base + 32) w1 = v1;
@@ -65,7 +65,7 @@ __device__ __forceinline__ void warp_fall_speeds(const Cst &c, int s, bool c1, d
 // (warp_fall_speeds); every lane of the warp runs the level loop, lanes
 // past the last column (valid = false) without loads, stores or requests.
 __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c, const CloudPar &cp, double dt,
-                                        const SedColumnIO &io, long col, bool valid)
+                                        const SedColumnIO &io, long col, bool valid, const double *fx)
 {
   const double inv_dt = 1.0 / dt;
   double rtmin[5];
@@ -112,7 +112,7 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
         continue;
       }
       double w1, w2;
-      warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, w1, w2);
+      warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, fx, w1, w2);
       double flux = dmin(rhodz_idt * rt[s], w1 * rho * rt[s]);
       if (!zerod_(w2)) flux += pmax0(1.0 - dz_idt * fm::frcp(w2)) * fabove[s];
       if (valid) {
@@ -136,6 +136,9 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
 __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
 {
   const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  __shared__ double fx[12];
+  if (threadIdx.x == 0) fall_exponents(c, fx);
+  __syncthreads();
   // whole warps run the sweep (they share the fall-speed evaluations); a
   // warp entirely past the last column leaves
   const bool valid = col < a.nij;
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constan
   }
   io.nij = a.nij;
   io.nk = a.nk;
-  sed_column_forward_warp(c, a.fortran, skip_c, cp, a.dt, io, col, valid);
+  sed_column_forward_warp(c, a.fortran, skip_c, cp, a.dt, io, col, valid, fx);
   // hail (NRR = 7), an independent species: its own sweep of the column
   if (a.hsrc && valid) sed_hail_column(c, a.dt, a.rhodref, a.dzz, a.hsrc, a.hfpr, a.hinpr, a.nij, a.nk, col);
 }

@@ -42,8 +42,22 @@ ICE3_HD CloudPar cloud_params(const Cst &c, bool fortran, bool has_st, double se
   return p;
 }
 
+// The exponents (EXSED - 1, EXSED - CEXVT - 1) of rain, snow, graupel and
+// hail at [2 s], [2 s + 1] (the others unused), formed once per block by
+// the device sweep instead of per fall speed; the same values as in place.
+ICE3_HD void fall_exponents(const Cst &c, double fx[12])
+{
+  const double ex[6] = {0.0, c.EXSEDR, 0.0, c.EXSEDS, c.EXSEDG, c.EXSEDH};
+  for (int s = 0; s < 6; ++s) {
+    fx[2 * s] = ex[s] - 1.0;
+    fx[2 * s + 1] = ex[s] - c.CEXVT - 1.0;
+  }
+}
+
 // Fall speed for content r (> threshold checked by the caller); lrho = log(rho).
-ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlbda, const CloudPar &cp)
+// fx: the exponents of fall_exponents, or null to form them here.
+ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlbda, const CloudPar &cp,
+                          const double *fx = nullptr)
 {
   const double lr = fm::flog(r);
   switch (s) {
@@ -53,17 +67,17 @@ ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlb
       return fm::fexp(-c.CEXVT * lrho - c.DC * lwlbdc) * cc * cp.fsedc;
     }
     case 1:  // rain
-      return c.FSEDR * fm::fexp((c.EXSEDR - 1.0) * lr + (c.EXSEDR - c.CEXVT - 1.0) * lrho);
+      return c.FSEDR * fm::fexp((fx ? fx[2] : c.EXSEDR - 1.0) * lr + (fx ? fx[3] : c.EXSEDR - c.CEXVT - 1.0) * lrho);
     case 2: {  // pristine ice: sedimentation.py:46-55, F90:307-311
       const double dmax_ = dmax(0.05e6, -0.15319e6 - 0.021454e6 * (lrho + lr));
       return c.FSEDI * fm::fexp(-c.CEXVT * lrho + c.EXCSEDI * fm::flog(dmax_));
     }
     case 3:  // snow
-      return c.FSEDS * fm::fexp((c.EXSEDS - 1.0) * lr + (c.EXSEDS - c.CEXVT - 1.0) * lrho);
+      return c.FSEDS * fm::fexp((fx ? fx[6] : c.EXSEDS - 1.0) * lr + (fx ? fx[7] : c.EXSEDS - c.CEXVT - 1.0) * lrho);
     case 5:  // hail (NRR = 7): OTHER_SPECIES with XFSEDH / XEXSEDH, F90:186-187
-      return c.FSEDH * fm::fexp((c.EXSEDH - 1.0) * lr + (c.EXSEDH - c.CEXVT - 1.0) * lrho);
+      return c.FSEDH * fm::fexp((fx ? fx[10] : c.EXSEDH - 1.0) * lr + (fx ? fx[11] : c.EXSEDH - c.CEXVT - 1.0) * lrho);
     default:  // graupel
-      return c.FSEDG * fm::fexp((c.EXSEDG - 1.0) * lr + (c.EXSEDG - c.CEXVT - 1.0) * lrho);
+      return c.FSEDG * fm::fexp((fx ? fx[8] : c.EXSEDG - 1.0) * lr + (fx ? fx[9] : c.EXSEDG - c.CEXVT - 1.0) * lrho);
   }
 }
 

@@ -95,6 +95,7 @@ struct Derived {
   // differences of table constants, formed once per block (the same IEEE
   // values as formed in place)
   double cpv_cl, cpv_ci, ci_cl, tt_m35, tt_m5, tt_m2;
+  double cxs_bs, cxg_dg2, cxh_dh2, cxg_bg, srimcg32;
 };
 
 ICE3_HD void make_derived(const Cst &c, Derived &d)
@@ -130,6 +131,11 @@ ICE3_HD void make_derived(const Cst &c, Derived &d)
   d.tt_m35 = c.TT - 35.0;
   d.tt_m5 = c.TT - 5.0;
   d.tt_m2 = c.TT - 2.0;
+  d.cxs_bs = c.CXS - c.BS;
+  d.cxg_dg2 = c.CXG - c.DG - 2.;
+  d.cxh_dh2 = c.CXH - c.DH - 2.0;
+  d.cxg_bg = c.CXG - c.BG;
+  d.srimcg32 = c.SRIMCG3 * c.SRIMCG2;
 }
 
 // Rates that persist between the hard pass and the following soft passes
@@ -563,7 +569,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // lbdar^EXCACCR, shared by RCACCR and (EXICFRR = EXCACCR) RICFRRG
   const double e_caccr = (has_r && (has_c || (has_i && d.icfrr_caccr))) ? fm::fexp(c.EXCACCR * s.llbdar) : 0.0;
   // lbdas^(CXS-BS) (RSACCRG, RSWETG) and lbdag^CXG (RSWETG, RRDRYG)
-  const double e_cxsbs = (has_s && (has_r || has_g || has_h)) ? fm::fexp((c.CXS - c.BS) * s.llbdas) : 0.0;
+  const double e_cxsbs = (has_s && (has_r || has_g || has_h)) ? fm::fexp(d.cxs_bs * s.llbdas) : 0.0;
   const double e_cxg = (has_g && (has_s || has_r)) ? fm::fexp(c.CXG * s.llbdag) : 0.0;
   // vapour/heat term of the freezing and melting rates (mode_ice4_fast_rs.F90
   // IFREEZ1/RSMLTG, mode_ice4_fast_rg.F90 IFREEZ1/RGMLTR), e limited by the
@@ -639,7 +645,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
       const double e_srimcg = fm::fexp(c.EXSRIMCG * s.llbdas);
       const double e_srimcg2 = d.srimcg2_twice ? e_srimcg * e_srimcg : fm::fexp(c.EXSRIMCG2 * s.llbdas);
       const double r = c.SRIMCG * e_srimcg * (1.0 - zw2);
-      rs[RS_RSRIMCG] = fm::fdiv(zzw * r, dmax(1.e-20, c.SRIMCG3 * c.SRIMCG2 * e_srimcg2 * (1. - zw3) - c.SRIMCG3 * r));
+      rs[RS_RSRIMCG] = fm::fdiv(zzw * r, dmax(1.e-20, d.srimcg32 * e_srimcg2 * (1. - zw3) - c.SRIMCG3 * r));
     } else rs[RS_RSRIMCG] = 0.0;
   } else {
     rs[RS_RCRIMS] = rs[RS_RCRIMSS] = rs[RS_RSRIMCG] = 0.0;
@@ -684,7 +690,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   } else {
     b[B_RICFRRG] = b[B_RRCFRIG] = b[B_RICFRR] = 0.0;
   }
-  const double base_g = (has_g && (has_c || has_i)) ? fm::fexp((c.CXG - c.DG - 2.) * s.llbdag) * pf.rho_mcexvt : 0.0;
+  const double base_g = (has_g && (has_c || has_i)) ? fm::fexp(d.cxg_dg2 * s.llbdag) * pf.rho_mcexvt : 0.0;
   rg[RG_RCDRYG] = (has_g && has_c) ? c.FCDRYG * v[IRC] * base_g : 0.0;
   if (has_g && has_i) {
     const double e = fm::fexp(c.COLEXIG * (t - c.TT));
@@ -720,7 +726,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // aggregate() ----
   if (H) {
     double *ht = hr->t;
-    const double base_h = (has_h && (has_c || has_i)) ? fm::fexp((c.CXH - c.DH - 2.0) * s.llbdah) * pf.rho_mcexvt
+    const double base_h = (has_h && (has_c || has_i)) ? fm::fexp(d.cxh_dh2 * s.llbdah) * pf.rho_mcexvt
                                                       : 0.0;
     ht[RH_RCWETH] = (has_h && has_c) ? c.FWETH * v[IRC] * base_h : 0.0;
     if (has_h && has_i) {
@@ -743,7 +749,7 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
       const double f1 = lut_index(s.llbdah, c.NWETLBDAH, c.WETINTP1H, c.WETINTP2H, i1);
       const double f2 = lut_index(s.llbdag, c.NWETLBDAG, c.WETINTP1G, c.WETINTP2G, i2);
       const double zw = lut2d(hlut + O_GWETH, ICE3GB_NWETLBDAG, i1, f1, i2, f2);
-      ht[RH_RGWETH] = c.FGWETH * zw * fm::fexp((c.CXG - c.BG) * s.llbdag) * e_cxh * pf.rho_mcexvt1 *
+      ht[RH_RGWETH] = c.FGWETH * zw * fm::fexp(d.cxg_bg * s.llbdag) * e_cxh * pf.rho_mcexvt1 *
                       (c.LBGWETH1 * ilh * ilh + c.LBGWETH2 * ilh * ilg + c.LBGWETH3 * ilg * ilg);
       ht[RH_RGDRYH] = ht[RH_RGWETH];
     } else ht[RH_RGWETH] = ht[RH_RGDRYH] = 0.0;

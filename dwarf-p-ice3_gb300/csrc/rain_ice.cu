@@ -18,13 +18,14 @@
 //    the rho powers) is computed once; real powers are fm::fexp(a*log x) with the
 //    logarithms of the slope parameters shared by all processes;
 //  * points are processed in regime order: a first kernel sorts each tile of
-//    131,072 points by which hydrometeors are present and whether T < TT (the
-//    masks that decide which process branches and how many sub-steps a point
-//    takes), so a warp's lanes take the same branches instead of the union
-//    of all regimes; the tile keeps the gathered accesses within a window of
-//    1 MB per field (tiles of 32,768 / 65,536 / 131,072 points: rain_ice
-//    171.6 / 170.6 / 170.2 ms at 1024x1024x90, fewer part-filled warps at
-//    the regime boundaries).  Results do not depend on the order;
+//    131,072 points by which hydrometeors are present, whether T < TT and
+//    whether the air is supersaturated over ice (the masks that decide which
+//    process branches and how many sub-steps a point takes), so a warp's
+//    lanes take the same branches instead of the union of all regimes; the
+//    tile keeps the gathered accesses within a window of 1 MB per field
+//    (tiles of 32,768 / 65,536 / 131,072 points: rain_ice 171.6 / 170.6 /
+//    170.2 ms at 1024x1024x90, fewer part-filled warps at the regime
+//    boundaries).  Results do not depend on the order;
 //  * with a PRFR option a column kernel first forms the precipitation
 //    fraction the sub-stepping starts from (prfr_column);
 //  * the only cross-point coupling of the Fortran stepping (PRREVAV taken
@@ -54,14 +55,29 @@ __global__ void rain_ice_prfr_kernel(const __grid_constant__ Cst c, const __grid
 }
 
 // Processing order: per tile of ORDER_TILE points, a counting sort by regime
-// (bit 0..4: cloud, rain, ice, snow, graupel above XRTMIN; bit 5: T < TT).
-// Warp-aggregated shared-memory atomics give each point its slot in the tile;
-// the order inside a regime follows the atomics and does not matter.  The
-// tile's keys (one byte per point) sit in dynamic shared memory.
+// (bit 0..4: cloud, rain, ice, snow, graupel above XRTMIN; bit 5: T < TT;
+// bit 6: supersaturation over ice, from an FP32 estimate of e_si(T)).  The
+// last bit decides the costly branches that few points of a regime take: the
+// nucleation (ice4_nucleation.func.h:40-89) and the Bergeron process
+// (mode_ice4_fast_ri.F90:60-75), exp / log / divisions that a warp otherwise
+// runs for one or two of its lanes.  Warp-aggregated shared-memory atomics
+// give each point its slot in the tile; the order inside a regime follows the
+// atomics and does not matter.  The tile's keys (one byte per point) sit in
+// dynamic shared memory.
 #ifndef ICE3GB_ORDER_TILE
 #define ICE3GB_ORDER_TILE 131072
 #endif
-constexpr int ORDER_TILE = ICE3GB_ORDER_TILE, ORDER_THREADS = 1024, ORDER_BINS = 64;
+constexpr int ORDER_TILE = ICE3GB_ORDER_TILE, ORDER_THREADS = 1024, ORDER_BINS = 128;
+static_assert(ORDER_BINS % 32 == 0 && ORDER_BINS <= 256, "bins per lane in the scan; one-byte keys");
+
+// rv > e_si (EPSILO + rv) / p, i.e. ice supersaturation, in FP32 (a sort key
+// only: the rounding of the estimate does not reach the results)
+__device__ __forceinline__ bool ice_supersat_est(const Cst &c, double t, double p, double rv)
+{
+  const float tf = (float)t, pf = (float)p, rvf = (float)rv;
+  const float esi = expf((float)c.ALPI - (float)c.BETAI / tf - (float)c.GAMI * logf(tf));
+  return rvf * pf > esi * ((float)c.EPSILO + rvf);
+}
 
 __global__ void __launch_bounds__(ORDER_THREADS) rain_ice_order_kernel(const __grid_constant__ Cst c,
                                                                        const __grid_constant__ RainIceArgs a)
@@ -80,26 +96,31 @@ __global__ void __launch_bounds__(ORDER_THREADS) rain_ice_order_kernel(const __g
     unsigned k = 0xffu;
     if (i < m) {
       const long p = base + i;
+      const double t = ld1(f.tht, p) * ld1(f.exn, p);
       k = (gtp(ld1(f.rct, p), c.C_RTMIN) ? 1u : 0u) | (gtp(ld1(f.rrt, p), c.R_RTMIN) ? 2u : 0u) |
           (gtp(ld1(f.rit, p), c.I_RTMIN) ? 4u : 0u) | (gtp(ld1(f.rst, p), c.S_RTMIN) ? 8u : 0u) |
-          (gtp(ld1(f.rgt, p), c.G_RTMIN) ? 16u : 0u) | (ltp(ld1(f.tht, p) * ld1(f.exn, p), c.TT) ? 32u : 0u);
+          (gtp(ld1(f.rgt, p), c.G_RTMIN) ? 16u : 0u) | (ltp(t, c.TT) ? 32u : 0u) |
+          (ice_supersat_est(c, t, ld1(f.pabs, p), ld1(f.rvt, p)) ? 64u : 0u);
       key[i] = (unsigned char)k;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, k);
     if (k != 0xffu && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&cnt[k], (unsigned)__popc(peers));
   }
   __syncthreads();
-  if (threadIdx.x < 32) {                               // exclusive scan of the 64 counts, two per lane
-    const unsigned c0 = cnt[2 * lane], c1 = cnt[2 * lane + 1];
-    unsigned s = c0 + c1;
+  if (threadIdx.x < 32) {                               // exclusive scan of the counts, BPL per lane
+    constexpr int BPL = ORDER_BINS / 32;
+    unsigned own[BPL], s = 0u;
+#pragma unroll
+    for (int j = 0; j < BPL; ++j) { own[j] = cnt[BPL * lane + j]; s += own[j]; }
+    const unsigned tot = s;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const unsigned t = __shfl_up_sync(0xffffffffu, s, d);
       if (lane >= (unsigned)d) s += t;
     }
-    const unsigned excl = s - (c0 + c1);
-    cnt[2 * lane] = excl;
-    cnt[2 * lane + 1] = excl + c0;
+    unsigned excl = s - tot;
+#pragma unroll
+    for (int j = 0; j < BPL; ++j) { cnt[BPL * lane + j] = excl; excl += own[j]; }
   }
   __syncthreads();
   for (int i0 = 0; i0 < m; i0 += ORDER_THREADS) {

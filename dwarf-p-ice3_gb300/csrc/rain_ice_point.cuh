@@ -1536,20 +1536,19 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
     ris += zrvheni;
   }
   // ICE4_CORRECT_NEGATIVITIES (mode_ice4_correct_negativities.F90) on the
-  // sources, in three blocks a warp skips when every lane would move
-  // nothing: the negative sources back to vapour; cloud and ice to vapour
+  // sources, in blocks a warp skips when every lane would move nothing: the
+  // negative sources back to vapour, one species at a time (a warp holds
+  // negative sources of about 1.6 of the 5 species); cloud and ice to vapour
   // while the vapour source is below XRTMIN(1); then rain, snow, graupel
-  if (warp_any(negd(rcs) || negd(rrs) || negd(ris) || negd(rss) || negd(rgs) || (H && negd(rhs)))) {
-    double w;
-    w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w;
-    w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w;
-    w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w;
-    w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w;
-    w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w;
-    if (H) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
-  }
+  double w;
+  if (warp_any(negd(rcs))) { w = rcs - pmax0(rcs); rvs += w; ths -= w * lvx; rcs -= w; }
+  if (warp_any(negd(rrs))) { w = rrs - pmax0(rrs); rvs += w; ths -= w * lvx; rrs -= w; }
+  if (warp_any(negd(ris))) { w = ris - pmax0(ris); rvs += w; ths -= w * lsx; ris -= w; }
+  if (warp_any(negd(rss))) { w = rss - pmax0(rss); rvs += w; ths -= w * lsx; rss -= w; }
+  if (warp_any(negd(rgs))) { w = rgs - pmax0(rgs); rvs += w; ths -= w * lsx; rgs -= w; }
+  if (H && warp_any(negd(rhs))) { w = rhs - pmax0(rhs); rvs += w; ths -= w * lsx; rhs -= w; }
   if (warp_any(ltd(rvs, c.V_RTMIN))) {
-    double w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
+    w = dmin(1., fm::fdiv(pmax0(c.V_RTMIN - rvs), dmax(rcs + ris, 1.e-20)));
     ths -= w * (rcs * lvx + ris * lsx);
     rvs += w * (rcs + ris);
     rcs = (1. - w) * rcs;

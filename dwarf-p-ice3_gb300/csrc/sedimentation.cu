@@ -61,6 +61,70 @@ __device__ __forceinline__ void warp_fall_speeds(const Cst &c, int s, bool c1, d
   }
 }
 
+// The power-law fall speeds of rain, snow and graupel (species 1, 3, 4) at
+// one level for the whole warp, with the requests of the three species
+// numbered together (in six slots: species x content / incoming flux) and
+// evaluated 32 at a time, so that a round of the exp / log is shared across
+// species instead of each species rounding its own requests up to a full
+// warp.  Same function (power_speed) on the same arguments as fall_speed.
+// live[s]: species s has a request in some lane (its warp is not skipped).
+__device__ __forceinline__ void warp_power_speeds(const Cst &c, const bool live[5], const bool c1[5],
+                                                  const double r1[5], const bool c2[5], const double r2[5],
+                                                  double lrho, const double *fx, double w1[5], double w2[5])
+{
+  constexpr int SP[3] = {1, 3, 4};
+  const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+  unsigned m[6];
+  int off[7];
+  off[0] = 0;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int s = SP[q >> 1];
+    m[q] = live[s] ? __ballot_sync(full, (q & 1) ? c2[s] : c1[s]) : 0u;
+    off[q + 1] = off[q] + __popc(m[q]);
+  }
+  const int ntot = off[6];
+  int mine[6];                                                   // this lane's request numbers
+#pragma unroll
+  for (int q = 0; q < 6; ++q) mine[q] = off[q] + __popc(m[q] & lt);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w1[SP[k]] = w2[SP[k]] = 0.0;
+  for (int base = 0; base < ntot; base += 32) {                  // uniform over the warp
+    const int j = base + (int)lane;                              // the request this lane evaluates
+    int q = 0;
+    unsigned mq = m[0];
+    int oq = 0;
+#pragma unroll
+    for (int t = 1; t < 6; ++t)
+      if (j >= off[t]) { q = t; mq = m[t]; oq = off[t]; }     // selects, not an indexed local array
+    const int owner = j < ntot ? (int)__fns(mq, 0u, j - oq + 1) : 0;
+    double arg = 0.0;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const int s = SP[t >> 1];
+      const double x = __shfl_sync(full, (t & 1) ? r2[s] : r1[s], owner);
+      if (q == t) arg = x;
+    }
+    const double lr = __shfl_sync(full, lrho, owner);
+    double v = 0.0;
+    if (j < ntot) {
+      const int k = q >> 1, s = k == 0 ? 1 : k + 2;
+      const double f = k == 0 ? c.FSEDR : (k == 1 ? c.FSEDS : c.FSEDG);
+      v = power_speed(f, fx[2 * s], fx[2 * s + 1], fm::flog(arg), lr);
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const int s = SP[t >> 1];
+      const double x = __shfl_sync(full, v, (unsigned)(mine[t] - base) & 31u);
+      const bool asked = (t & 1) ? c2[s] : c1[s];
+      if (live[s] && asked && mine[t] >= base && mine[t] < base + 32) {
+        if (t & 1) w2[s] = x;
+        else w1[s] = x;
+      }
+    }
+  }
+}
+
 // sed_column_forward with the warp's fall speeds evaluated together
 // (warp_fall_speeds); every lane of the warp runs the level loop, lanes
 // past the last column (valid = false) without loads, stores or requests.
@@ -97,13 +161,21 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
     const double wlbda =
         (c1[0] || c2[0]) ? 6.6e-8 * fm::fdiv(101325.0, sed_load(io.pabs, p)) * (sed_load(io.tht, p) * (1.0 / 293.15))
                          : 0.0;
+    // a species that no lane of the warp moves at this level (content at or
+    // below its threshold and not negative, nothing falling in) has a zero
+    // flux and keeps its source; the warp skips its arithmetic
+    bool live[5];
+#pragma unroll
+    for (int s = 0; s < 5; ++s)
+      live[s] = !(s == 0 && skip_c) && !__all_sync(0xffffffffu, !c1[s] && !c2[s] && !negd(rt[s]) && zerod_(fabove[s]));
+    double w1[5], w2[5];
+    warp_power_speeds(c, live, c1, rt, c2, qp, lrho, fx, w1, w2);
+    if (live[0]) warp_fall_speeds(c, 0, c1[0], rt[0], c2[0], qp[0], lrho, wlbda, cp, fx, w1[0], w2[0]);
+    if (live[2]) warp_fall_speeds(c, 2, c1[2], rt[2], c2[2], qp[2], lrho, wlbda, cp, fx, w1[2], w2[2]);
 #pragma unroll
     for (int s = 0; s < 5; ++s) {
       if (s == 0 && skip_c) continue;
-      // a species that no lane of the warp moves at this level (content at
-      // or below its threshold and not negative, nothing falling in) has a
-      // zero flux and keeps its source; the warp skips its arithmetic
-      if (__all_sync(0xffffffffu, !c1[s] && !c2[s] && !negd(rt[s]) && zerod_(fabove[s]))) {
+      if (!live[s]) {
         if (valid) {
           if (io.src_out[s] && io.src_out[s] != io.src_in[s]) io.src_out[s][p] = src[s];
           if (io.fpr[s]) io.fpr[s][p] = 0.0;
@@ -111,10 +183,8 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
         fabove[s] = 0.0;
         continue;
       }
-      double w1, w2;
-      warp_fall_speeds(c, s, c1[s], rt[s], c2[s], qp[s], lrho, wlbda, cp, fx, w1, w2);
-      double flux = dmin(rhodz_idt * rt[s], w1 * rho * rt[s]);
-      if (!zerod_(w2)) flux += pmax0(1.0 - dz_idt * fm::frcp(w2)) * fabove[s];
+      double flux = dmin(rhodz_idt * rt[s], w1[s] * rho * rt[s]);
+      if (!zerod_(w2[s])) flux += pmax0(1.0 - dz_idt * fm::frcp(w2[s])) * fabove[s];
       if (valid) {
         if (io.src_out[s]) {
           if (fortran) io.src_out[s][p] = src[s] + tso_idt * (fabove[s] - flux);

@@ -54,6 +54,14 @@ ICE3_HD void fall_exponents(const Cst &c, double fx[12])
   }
 }
 
+// The power-law fall speed F r^a rho^b = F exp(a log r + b log rho) of rain,
+// snow, graupel and hail (a = EXSED - 1, b = EXSED - CEXVT - 1), the sum of
+// products fused as fma(a, log r, b log rho) wherever it is formed.
+ICE3_HD double power_speed(double f, double a, double b, double lr, double lrho)
+{
+  return f * fm::fexp(fm::fma_(a, lr, b * lrho));
+}
+
 // Fall speed for content r (> threshold checked by the caller); lrho = log(rho).
 // fx: the exponents of fall_exponents, or null to form them here.
 ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlbda, const CloudPar &cp,
@@ -67,17 +75,17 @@ ICE3_HD double fall_speed(const Cst &c, int s, double r, double lrho, double wlb
       return fm::fexp(-c.CEXVT * lrho - c.DC * lwlbdc) * cc * cp.fsedc;
     }
     case 1:  // rain
-      return c.FSEDR * fm::fexp((fx ? fx[2] : c.EXSEDR - 1.0) * lr + (fx ? fx[3] : c.EXSEDR - c.CEXVT - 1.0) * lrho);
+      return power_speed(c.FSEDR, fx ? fx[2] : c.EXSEDR - 1.0, fx ? fx[3] : c.EXSEDR - c.CEXVT - 1.0, lr, lrho);
     case 2: {  // pristine ice: sedimentation.py:46-55, F90:307-311
       const double dmax_ = dmax(0.05e6, -0.15319e6 - 0.021454e6 * (lrho + lr));
       return c.FSEDI * fm::fexp(-c.CEXVT * lrho + c.EXCSEDI * fm::flog(dmax_));
     }
     case 3:  // snow
-      return c.FSEDS * fm::fexp((fx ? fx[6] : c.EXSEDS - 1.0) * lr + (fx ? fx[7] : c.EXSEDS - c.CEXVT - 1.0) * lrho);
+      return power_speed(c.FSEDS, fx ? fx[6] : c.EXSEDS - 1.0, fx ? fx[7] : c.EXSEDS - c.CEXVT - 1.0, lr, lrho);
     case 5:  // hail (NRR = 7): OTHER_SPECIES with XFSEDH / XEXSEDH, F90:186-187
-      return c.FSEDH * fm::fexp((fx ? fx[10] : c.EXSEDH - 1.0) * lr + (fx ? fx[11] : c.EXSEDH - c.CEXVT - 1.0) * lrho);
+      return power_speed(c.FSEDH, fx ? fx[10] : c.EXSEDH - 1.0, fx ? fx[11] : c.EXSEDH - c.CEXVT - 1.0, lr, lrho);
     default:  // graupel
-      return c.FSEDG * fm::fexp((fx ? fx[8] : c.EXSEDG - 1.0) * lr + (fx ? fx[9] : c.EXSEDG - c.CEXVT - 1.0) * lrho);
+      return power_speed(c.FSEDG, fx ? fx[8] : c.EXSEDG - 1.0, fx ? fx[9] : c.EXSEDG - c.CEXVT - 1.0, lr, lrho);
   }
 }
 
@@ -120,7 +128,7 @@ ICE3_HD double fall_speed_d(const Cst &c, int s, double r, double lrho, double w
       if (s == 1) { fsed = c.FSEDR; ex = c.EXSEDR; }
       else if (s == 3) { fsed = c.FSEDS; ex = c.EXSEDS; }
       else { fsed = c.FSEDG; ex = c.EXSEDG; }
-      const double v = fsed * fm::fexp((ex - 1.0) * lr + (ex - c.CEXVT - 1.0) * lrho);
+      const double v = power_speed(fsed, ex - 1.0, ex - c.CEXVT - 1.0, lr, lrho);
       d_lr = (ex - 1.0) * v;
       d_lrho = (ex - c.CEXVT - 1.0) * v;
       return v;

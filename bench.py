@@ -489,6 +489,7 @@ def run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist):
             host[k].copy_(pristine[k])
         call()
     total = 0.0
+    per_step = []
     for _ in range(args.steps):
         for k in STEP_INOUT:
             host[k].copy_(pristine[k])                    # restore in-out host fields (untimed)
@@ -506,11 +507,13 @@ def run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
         total += ms
+        per_step.append(ms)
     ms_step = total / args.steps
     del host, pristine, outs
     bw = copy_bandwidth(dev)
     return {"value": world * n / (ms_step / 1e3), "unit": "grid-points/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": ms_step,
+            "step_ms_min_max": [min(per_step), max(per_step)],
             "path": "ice3gb_physics_step_host, pinned host buffers",
             # the box's pinned-copy bandwidth, measured right after: the copies alone, one
             # direction after the other, would take h2d / h2d_gbs + d2h / d2h_gbs

@@ -20,8 +20,14 @@ using namespace ice3ia;
 // microphysics in the chained physics step) instead of th/rv/.../rg, which
 // are then not read; rrs/rss/rgs are read instead.  Output pointers may be
 // NULL in the internal chained use (store skipped).
+// Blocks of 256 per SM the registers are capped for: the default leaves
+// 126 registers (two blocks, 16 warps per SM); three blocks (80 registers,
+// spilling) measured 39.95 against 39.43 ms per launch at 1024x1024x90.
+#ifndef IA_MIN_BLOCKS
+#define IA_MIN_BLOCKS 1
+#endif
 template <bool ADV, bool SRC>
-__global__ void __launch_bounds__(256) ice_adjust_v2_kernel(const __grid_constant__ Cst c,
+__global__ void __launch_bounds__(256, IA_MIN_BLOCKS) ice_adjust_v2_kernel(const __grid_constant__ Cst c,
                                                             const __grid_constant__ IaKernelFields kf,
                                                             long npairs, int nij, double dt)
 {

@@ -1517,11 +1517,18 @@ ICE3_HD unsigned int rain_ice_point(const Cst &c, const Derived &d, const double
 #pragma unroll
     for (int v = 0; v < NVT; ++v) vart[v] -= ext[v] * dt;
     evap = lwarm ? rrevav : 0.0;
-    // total tendencies (rain_ice.F90:758-790)
-    const double wv = (vart[IRV] - rv) * inv_dt, wc = (vart[IRC] - rc) * inv_dt;
-    const double wr = (vart[IRR] - rr) * inv_dt, wi = (vart[IRI] - ri) * inv_dt;
-    const double ws = (vart[IRS] - rs) * inv_dt, wg = (vart[IRG] - rg) * inv_dt;
-    const double wh = H ? (vart[NVT - 1] - rh) * inv_dt : 0.0;
+    // total tendencies (rain_ice.F90:758-790).  The state at t and the
+    // sources are read again here instead of being kept live across the
+    // sub-stepping (the point's inputs are unchanged until its results are
+    // written below): 13 values the register allocator would otherwise spill.
+    const double rv0 = ldp(f.rvt, p), rc0 = ldp(f.rct, p), rr0 = ldp(f.rrt, p);
+    const double ri0 = ldp(f.rit, p), rs0 = ldp(f.rst, p), rg0 = ldp(f.rgt, p);
+    ths = f.ths[p]; rvs = f.rvs[p]; rcs = f.rcs[p]; rrs = f.rrs[p]; ris = f.ris[p]; rss = f.rss[p]; rgs = f.rgs[p];
+    if (H) rhs = f.rhs[p];
+    const double wv = (vart[IRV] - rv0) * inv_dt, wc = (vart[IRC] - rc0) * inv_dt;
+    const double wr = (vart[IRR] - rr0) * inv_dt, wi = (vart[IRI] - ri0) * inv_dt;
+    const double ws = (vart[IRS] - rs0) * inv_dt, wg = (vart[IRG] - rg0) * inv_dt;
+    const double wh = H ? (vart[NVT - 1] - ldp(f.rht, p)) * inv_dt : 0.0;
     ths += (wc + wr) * lvx + (H ? wi + ws + wg + wh : wi + ws + wg) * lsx + zrvheni * lsx;
     if (H) rhs += wh;
     rvs += wv - zrvheni;

@@ -124,6 +124,11 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM)
 {
   extern __shared__ double lut[];
   __shared__ Derived dsh;
+  // the in-out fields a point starts from, for the fall-back to the plain
+  // path: kept in shared memory rather than in registers across the point
+  // code (fewer spills of the large point kernel)
+  __shared__ double s_in[8][RI_THREADS];
+  __shared__ double s_sur[RI_THREADS][NRATE];          // the decoded learned rates of a thread's point
   const RainIceArgs &a = sa.ri;
   for (int i = threadIdx.x; i < LUT_N; i += blockDim.x) lut[i] = a.luts[i];
   if (threadIdx.x == 0) make_derived(c, dsh);
@@ -145,13 +150,15 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM)
     if (slot < n) {
       const long p = a.order ? (long)__ldg(a.order + slot) : slot;
       const int row = __ldg(sa.row_of_point + p);
-      double sur[NRATE];
       const double *use = nullptr;
       if (row >= 0) {
-        decode_rates(sa.y + (long)row * sa.ldy, sur);
-        use = sur;
+        decode_rates(sa.y + (long)row * sa.ldy, s_sur[threadIdx.x]);
+        use = s_sur[threadIdx.x];
       }
-      const double in[8] = {f.ths[p], f.rvs[p], f.rcs[p], f.rrs[p], f.ris[p], f.rss[p], f.rgs[p], f.cit[p]};
+      double *in0 = &s_in[0][threadIdx.x];                        // element k at in0[k * RI_THREADS]
+      in0[0 * RI_THREADS] = f.ths[p]; in0[1 * RI_THREADS] = f.rvs[p]; in0[2 * RI_THREADS] = f.rcs[p];
+      in0[3 * RI_THREADS] = f.rrs[p]; in0[4 * RI_THREADS] = f.ris[p]; in0[5 * RI_THREADS] = f.rss[p];
+      in0[6 * RI_THREADS] = f.rgs[p]; in0[7 * RI_THREADS] = f.cit[p];
       for (int attempt = 0; attempt < 2; ++attempt) {
         bool capped;
         key = rain_ice_point<true>(c, dsh, lut, f, p, dt, a.max_passes, capped, use);
@@ -159,6 +166,9 @@ __global__ void __launch_bounds__(RI_THREADS, RI_BLOCKS_PER_SM)
         // fix-up check of the surrogate-assisted point
         const double o_th = f.ths[p], o_v = f.rvs[p], o_c = f.rcs[p], o_r = f.rrs[p], o_i = f.ris[p];
         const double o_s = f.rss[p], o_g = f.rgs[p];
+        double in[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) in[k] = in0[k * RI_THREADS];
         const double w_in = in[1] + in[2] + in[3] + in[4] + in[5] + in[6];
         const double w_out = o_v + o_c + o_r + o_i + o_s + o_g;
         const double w_abs = fabs(in[1]) + fabs(in[2]) + fabs(in[3]) + fabs(in[4]) + fabs(in[5]) + fabs(in[6]);

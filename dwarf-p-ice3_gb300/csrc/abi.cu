@@ -633,14 +633,18 @@ std::vector<long> slab_cuts(long nij, long w_max)
   return cuts;
 }
 
+#ifndef ICE3GB_HOST_SLABS
+#define ICE3GB_HOST_SLABS 8
+#endif
+
 int run_physics_step_pipelined(Handle *h, int nij, int nk, double dt, const Ice3gbRainIceOptions *opt,
                                const Ice3gbStepFields *f, cudaStream_t s)
 {
   int rc;
   if ((rc = pipe_init(h))) return rc;
   HostPipe &P = h->pipe;
-  // slab width: about 8 slabs, at least 4096 columns, a multiple of 64
-  long w_max = ((long)nij / 8 + 63) / 64 * 64;
+  // slab width: about ICE3GB_HOST_SLABS slabs, at least 4096 columns, a multiple of 64
+  long w_max = ((long)nij / ICE3GB_HOST_SLABS + 63) / 64 * 64;
   if (w_max < 4096) w_max = 4096;
   if (w_max > nij) w_max = nij;
   const long n_all = (long)nij * nk;

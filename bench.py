@@ -514,6 +514,7 @@ def run_e2e(args, lib, handle, st, opt, nij, n, dev, world, dist):
     return {"value": world * n / (ms_step / 1e3), "unit": "grid-points/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": ms_step,
             "step_ms_min_max": [min(per_step), max(per_step)],
+            "step_ms": [round(x, 1) for x in per_step],
             "path": "ice3gb_physics_step_host, pinned host buffers",
             # the box's pinned-copy bandwidth, measured right after: the copies alone, one
             # direction after the other, would take h2d / h2d_gbs + d2h / d2h_gbs

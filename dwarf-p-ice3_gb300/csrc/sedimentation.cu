@@ -8,11 +8,12 @@
 // level to the surface with the five species side by side, keeping each
 // species' incoming flux F_{k+1} in a register; consecutive threads own
 // consecutive columns, so every level access is coalesced.  The fall speeds a
-// warp needs at a level are evaluated together, with every lane busy
-// (warp_fall_speeds).  What the species
-// share at a level (rho, dz, rho dz, dt/(rho dz) and log rho, computed only
-// when a species sediments there) is computed once; threshold tests and
-// clamps run on the integer pipe (GB300's FP64 pipe is the bound).
+// warp needs at a level are evaluated together, with every lane busy: those
+// of rain, snow and graupel pooled across the three species
+// (warp_power_speeds), cloud and ice per species (warp_fall_speeds).  What
+// the species share at a level (rho, dz, rho dz, dt/(rho dz) and log rho,
+// computed only when a species sediments there) is computed once; threshold
+// tests and clamps run on the integer pipe (GB300's FP64 pipe is the bound).
 #include "ice3gb_device.cuh"
 #include "ice3gb_kernels.h"
 #include "sedimentation_point.cuh"

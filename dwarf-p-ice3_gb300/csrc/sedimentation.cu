@@ -202,9 +202,12 @@ __device__ void sed_column_forward_warp(const Cst &c, bool fortran, bool skip_c,
 }
 
 // 128 threads, ~148 registers: 3 blocks per SM; capping the registers for
-// 4 or 5 blocks (128 / 96 registers) measured 45.4 / 45.8 against 42.7 ms
-// at 1024x1024 columns.
-__global__ void __launch_bounds__(128) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
+// 4 or 5 blocks (SED_MIN_BLOCKS: 128 / 96 registers) measured 39.7 / 44.0
+// against 38.0 ms at 1024x1024 columns.
+#ifndef SED_MIN_BLOCKS
+#define SED_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(128, SED_MIN_BLOCKS) sedimentation_kernel(const __grid_constant__ Cst c, SedArgs a)
 {
   const long col = blockIdx.x * (long)blockDim.x + threadIdx.x;
   __shared__ double fx[12];

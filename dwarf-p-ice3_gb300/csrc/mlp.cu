@@ -189,13 +189,16 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const TcGemmArgs a)
 // ---------------------------------------------------------------------------
 // Fused inference of the surrogate's MLP shape (16 -> 256 -> 256 -> 256 ->
 // n_out <= 16, GELU): one persistent CTA per SM walks 128-row tiles.  Per
-// tile the 128 x 256 FP32 accumulator lives in TMEM (256 columns), the BF16
-// activations in shared memory (64 KB, K-major core matrices), W1 and the
-// output layer stay resident in shared memory, and W2 / W3 stream from L2 as
-// eight 32 KB K-chunks (pre-packed in the core-matrix layout) through a
-// four-stage ring filled by bulk asynchronous copies.  Thread 0 issues the
-// copies and the tcgen05.mma; all four warps run the epilogues (tcgen05.ld,
-// bias, GELU, BF16 pack into the activation tile).
+// tile the 128 x 256 FP32 accumulators of consecutive layers alternate
+// between the two halves of TMEM (columns 0-255 and 256-511), the BF16
+// activations sit in shared memory (64 KB, K-major core matrices), W1 and
+// the output layer stay resident in shared memory, and W2 / W3 stream from
+// L2 as eight 32 KB K-chunks (pre-packed in the core-matrix layout) through
+// a four-stage ring filled by bulk asynchronous copies.  Thread 0 issues the
+// copies and the tcgen05.mma; all 16 warps run the epilogues (tcgen05.ld,
+// bias, GELU, BF16 pack into the activation tile) in two halves of 128
+// columns: the MMAs of the next layer's first two K-chunks (the first
+// half's activations) run while the warps form the second half.
 constexpr int FZ_NST = 4;                               // weight ring stages (3: 5.14, 4: 4.98 ms on 8.4 M rows)
 constexpr int FZ_THREADS = 512;                         // 16 warps: 4 row groups x 4 column quarters
 constexpr uint32_t FZ_CHUNK_BYTES = 256 * 64 * 2;       // one K-chunk of W2 / W3
@@ -209,11 +212,12 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// Bias + GELU of the 128 x 256 accumulator into the activation tile.  Warp
-// w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the 64 columns
-// 64 (w / 4) .. + 63 as two 32-column loads: the second is in flight while
-// the first half's GELU runs (the MUFU tanh is the epilogue's bound); the
-// biases are read four at a time (the same address for the whole warp).
+// Bias + GELU of 32 accumulator columns (from cb0) of one row into the
+// activation tile.  In an epilogue half h, warp w holds TMEM lanes
+// 32 (w % 4) .. + 31 (its rows) and the columns 128 h + 32 (w / 4) .. + 31;
+// the load of the second half is in flight while the first half's GELU runs
+// (the MUFU tanh is the epilogue's bound); the biases are read four at a
+// time (the same address for the whole warp).
 __device__ __forceinline__ void fz_gelu_half(const uint32_t r[32], const float *bias, int cb0, int row,
                                              __nv_bfloat16 *sH)
 {
@@ -230,18 +234,6 @@ __device__ __forceinline__ void fz_gelu_half(const uint32_t r[32], const float *
                          gelu(__uint_as_float(r[8 * g + 2 * j + 1]) + bb[2 * j + 1]));
     *reinterpret_cast<uint4 *>(sH + tc::core_off(row, cb, 256)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
-}
-__device__ __forceinline__ void fz_epilogue_gelu(uint32_t tmem, int warp, const float *bias, __nv_bfloat16 *sH)
-{
-  const int q = warp & 3, c0 = (warp >> 2) * 64;
-  const int row = 32 * q + (threadIdx.x & 31);
-  uint32_t r0[32], r1[32];
-  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, r0);
-  tc::tmem_wait_ld();
-  tc::tmem_ld32_nowait(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c0 + 32), r1);
-  fz_gelu_half(r0, bias, c0, row, sH);
-  tc::tmem_wait_ld();
-  fz_gelu_half(r1, bias, c0 + 32, row, sH);
 }
 
 __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFusedArgs a)
@@ -277,7 +269,7 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFused
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_base, 256);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   tc::fence_async_smem();
   tc::fence_before();
   __syncthreads();
@@ -301,15 +293,67 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFused
   };
   if (tid == 0)
     for (long g = 0; g < FZ_NST - 1 && g < total_chunks && ok; ++g) ok = issue(g);
+  // Accumulators: the layers alternate between TMEM columns 0-255 (A) and
+  // 256-511 (B), so that the MMAs of a layer's first K half (activation
+  // columns 0-127, written by the first half of the previous epilogue) run
+  // while the warps form the second half of that epilogue.
+  const uint32_t tA = tmem, tB = tmem + 256u;
+  const int lane = tid & 31, q4 = warp & 3, row = 32 * q4 + lane;
+  auto ld_half = [&](uint32_t tacc, int h, uint32_t r[32]) {
+    tc::tmem_ld32_nowait(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)(128 * h + 32 * (warp >> 2)), r);
+  };
+  auto gelu_half = [&](const uint32_t r[32], const float *bias, int h) {
+    fz_gelu_half(r, bias, 128 * h + 32 * (warp >> 2), row, sH);
+  };
+  auto sync_async = [&]() {     // activation writes visible to the tensor core; TMEM accesses ordered
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  };
+  long n_commit = 0;            // commits to bar_mma (thread 0)
+  bool uncommitted = false;     // MMAs issued after the last commit to bar_mma (thread 0)
+  // thread 0: the MMAs of K-chunks c0, c0 + 1 of a hidden layer into tacc
+  auto mma_chunks = [&](uint32_t tacc, int c0) -> bool {
+    for (int c = c0; c < c0 + 2; ++c) {
+      const long g = consumed;
+      const int s = (int)(g % FZ_NST);
+      if (!tc::mbar_wait(&bar_full[s], (uint32_t)((g / FZ_NST) & 1), WAIT_ITERS)) return false;
+      tc::fence_after();
+      const uint32_t aS = tc::smem_u32(smem + FZ_OFF_STAGE + s * 32768);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        tc::mma_bf16(tacc, tc::desc(aH + (uint32_t)(c * 8 + 2 * j) * 128u, 128u, 4096u),
+                     tc::desc(aS + (uint32_t)(2 * j) * 128u, 128u, 1024u), id256, c > 0 || j > 0);
+      uncommitted = true;
+      tc::commit(&bar_free[s]);
+      ++consumed;
+      const long gn = g + FZ_NST - 1;
+      if (gn < total_chunks && gn >= issued && !issue(gn)) return false;
+    }
+    return true;
+  };
+  auto commit_mma = [&]() {
+    tc::commit(&bar_mma);
+    ++n_commit;
+    uncommitted = false;
+  };
+  // all threads: wait for the last commit to bar_mma
+  auto wait_mma = [&]() -> bool {
+    ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
+    mma_phase ^= 1u;
+    tc::fence_after();
+    return ok;
+  };
   long tile = blockIdx.x;
   for (long it = 0; it < my_tiles; ++it, tile += gridDim.x) {
     const long r0 = tile * 128;
     // ---- input rows -> BF16 tile (threads 0..127, one row each)
     if (tid < 128) {
-      const long row = r0 + tid;
+      const long rw = r0 + tid;
       float x[16];
-      if (row < a.n) {
-        const float4 *xp = reinterpret_cast<const float4 *>(a.x + row * 16);
+      if (rw < a.n) {
+        const float4 *xp = reinterpret_cast<const float4 *>(a.x + rw * 16);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float4 v = __ldg(xp + q);
@@ -325,76 +369,63 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFused
           make_uint4(pack_bf16x2(x[8], x[9]), pack_bf16x2(x[10], x[11]), pack_bf16x2(x[12], x[13]),
                      pack_bf16x2(x[14], x[15]));
     }
-    tc::fence_async_smem();
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-    // ---- layer 1: K = 16, one MMA
+    sync_async();
+    // ---- layer 1: K = 16, one MMA into A
     if (tid == 0) {
-      tc::mma_bf16(tmem, tc::desc(aX, 128u, 256u), tc::desc(aW1, 128u, 256u), id256, false);
-      tc::commit(&bar_mma);
+      tc::mma_bf16(tA, tc::desc(aX, 128u, 256u), tc::desc(aW1, 128u, 256u), id256, false);
+      commit_mma();
     }
-    ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
-    mma_phase ^= 1u;
-    tc::fence_after();
-    if (!ok) break;
-    fz_epilogue_gelu(tmem, warp, sB, sH);
-    // ---- layers 2 and 3: K = 256 in four chunks each
+    if (!wait_mma()) break;
+    // ---- layers 2 (into B) and 3 (into A): K = 256 in four chunks; the
+    // first two chunks start after the first half of the previous epilogue
     for (int layer = 0; layer < 2 && ok; ++layer) {
-      tc::fence_async_smem();
-      tc::fence_before();
-      __syncthreads();
-      tc::fence_after();
+      const uint32_t tprev = layer == 0 ? tA : tB, tcur = layer == 0 ? tB : tA;
+      const float *bprev = sB + 256 * layer;
+      uint32_t rh0[32], rh1[32];
+      ld_half(tprev, 0, rh0);
+      tc::tmem_wait_ld();
+      ld_half(tprev, 1, rh1);                   // in flight during the first half
+      gelu_half(rh0, bprev, 0);
+      sync_async();
+      if (tid == 0) ok = mma_chunks(tcur, 0);
+      tc::tmem_wait_ld();
+      gelu_half(rh1, bprev, 1);
+      sync_async();
       if (tid == 0) {
-        for (int c = 0; c < 4 && ok; ++c) {
-          const long g = consumed;
-          const int s = (int)(g % FZ_NST);
-          ok = tc::mbar_wait(&bar_full[s], (uint32_t)((g / FZ_NST) & 1), WAIT_ITERS);
-          if (!ok) break;
-          tc::fence_after();
-          const uint32_t aS = tc::smem_u32(smem + FZ_OFF_STAGE + s * 32768);
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            tc::mma_bf16(tmem, tc::desc(aH + (uint32_t)(c * 8 + 2 * j) * 128u, 128u, 4096u),
-                         tc::desc(aS + (uint32_t)(2 * j) * 128u, 128u, 1024u), id256, c > 0 || j > 0);
-          tc::commit(&bar_free[s]);
-          ++consumed;
-          const long gn = g + FZ_NST - 1;
-          if (gn < total_chunks && gn >= issued) ok = issue(gn);
-        }
-        tc::commit(&bar_mma);
+        if (ok) ok = mma_chunks(tcur, 2);
+        commit_mma();
       }
-      ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
-      mma_phase ^= 1u;
-      tc::fence_after();
-      if (!ok) break;
-      fz_epilogue_gelu(tmem, warp, sB + 256 * (layer + 1), sH);
+      if (!wait_mma()) break;
     }
     if (!ok) break;
-    // ---- output layer: N = 16, K = 256
-    tc::fence_async_smem();
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
+    // ---- epilogue of layer 3 (A), both halves, then the output layer
+    // (N = 16, K = 256) into B
+    {
+      uint32_t rh0[32], rh1[32];
+      ld_half(tA, 0, rh0);
+      tc::tmem_wait_ld();
+      ld_half(tA, 1, rh1);
+      gelu_half(rh0, sB + 512, 0);
+      tc::tmem_wait_ld();
+      gelu_half(rh1, sB + 512, 1);
+    }
+    sync_async();
     if (tid == 0) {
 #pragma unroll
       for (int j = 0; j < 16; ++j)
-        tc::mma_bf16(tmem, tc::desc(aH + (uint32_t)(2 * j) * 128u, 128u, 4096u),
+        tc::mma_bf16(tB, tc::desc(aH + (uint32_t)(2 * j) * 128u, 128u, 4096u),
                      tc::desc(aW4 + (uint32_t)(2 * j) * 128u, 128u, 4096u), id16, j > 0);
-      tc::commit(&bar_mma);
+      commit_mma();
     }
-    ok = __syncthreads_and(ok && tc::mbar_wait(&bar_mma, mma_phase, WAIT_ITERS)) != 0;
-    mma_phase ^= 1u;
-    tc::fence_after();
-    if (!ok) break;
+    if (!wait_mma()) break;
     if (warp < 4) {                  // output columns 0..15: the first column quarter's warps
       float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
-      const long row = r0 + tid;
-      if (row < a.n) {
+      tc::tmem_ld16(tB + ((uint32_t)(warp * 32) << 16), v);
+      const long rw = r0 + tid;
+      if (rw < a.n) {
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          if (j < a.n_out) a.y[row * a.n_out + j] = v[j] + sB[768 + j];
+          if (j < a.n_out) a.y[rw * a.n_out + j] = v[j] + sB[768 + j];
       }
     }
     tc::fence_before();
@@ -404,17 +435,18 @@ __global__ void __launch_bounds__(FZ_THREADS, 1) mlp_fused_kernel(const MlpFused
   if (!ok) {
     if (tid == 0) atomicExch(a.err, 1);
     // let the tensor core and the copies in flight finish before the
-    // shared memory and TMEM are released (the last committed MMA phase is
-    // mma_phase ^ 1)
+    // shared memory and TMEM are released: one more commit covers every MMA
+    // issued so far; its phase is the parity of the commit count
     if (tid == 0) {
-      tc::mbar_wait(&bar_mma, mma_phase ^ 1u, WAIT_ITERS);
+      if (uncommitted) commit_mma();
+      if (n_commit > 0) tc::mbar_wait(&bar_mma, (uint32_t)((n_commit - 1) & 1), WAIT_ITERS);
       for (long g = consumed; g < issued; ++g)
         tc::mbar_wait(&bar_full[g % FZ_NST], (uint32_t)((g / FZ_NST) & 1), WAIT_ITERS);
     }
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // FP32 master weights -> the fused kernel's BF16 layouts: W1 [256][16] and

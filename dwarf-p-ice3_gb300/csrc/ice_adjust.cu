@@ -21,8 +21,10 @@ using namespace ice3ia;
 // are then not read; rrs/rss/rgs are read instead.  Output pointers may be
 // NULL in the internal chained use (store skipped).
 // Blocks of 256 per SM the registers are capped for: the default leaves
-// 126 registers (two blocks, 16 warps per SM); three blocks (80 registers,
-// spilling) measured 39.95 against 39.43 ms per launch at 1024x1024x90.
+// 158-162 registers (one block, 8 warps per SM); two blocks (128 registers)
+// measured 35.67 against 35.58 ms per launch at 1024x1024x90, three (80
+// registers, spilling) 39.95 against 39.43 ms before the saturation terms
+// were skipped by their weight.
 #ifndef IA_MIN_BLOCKS
 #define IA_MIN_BLOCKS 1
 #endif

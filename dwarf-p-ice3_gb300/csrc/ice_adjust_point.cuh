@@ -137,8 +137,12 @@ ICE3_HD void icecloud(const Cst &c, double p, double z, double dz, double t, dou
 // Constants derived once per thread (divisions of table constants).
 struct IaDerived {
   double rdrv, rvrd, irv;   // RD/RV, RV/RD, 1/RV
+  double imix;              // the reciprocal of TMAXMIX - TMINMIX that fm::fdiv would form per point
 };
-ICE3_HD IaDerived ia_derived(const Cst &c) { return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV}; }
+ICE3_HD IaDerived ia_derived(const Cst &c)
+{
+  return {c.RD / c.RV, c.RV / c.RD, 1.0 / c.RV, fm::frcp(c.TMAXMIX - c.TMINMIX)};
+}
 
 // srcs (optional): PSRCS of the point (ice_adjust.F90:360, :468).
 // OCND2: the separate liquid / ice cloud option of CONDENSATION
@@ -168,12 +172,23 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
     if (!OCND2) {
       // es_w and es_i share fm::flog(T) and 1/T (functions/tiwmx.py:18,60)
       const double lt = fm::flog(t);
-      pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
-      piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
-      frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
+      // the ice fraction: of the temperature (FRAC_ICE_ADJUST 0, the AROME
+      // setting; fm::fdiv's product with the reciprocal formed once), else
+      // of the condensate
       const int fmode = (int)c.FRAC_ICE_ADJUST;
-      if (fmode == 3) frac = nclip01(frac);
-      else if (fmode == 0) frac = nclip01(fm::fdiv(c.TMAXMIX - t, c.TMAXMIX - c.TMINMIX));
+      if (fmode == 0) {
+        frac = nclip01(fm::mul_(c.TMAXMIX - t, d.imix));
+      } else {
+        frac = fgt(x.rc + x.ri, 1e-20) ? fm::fdiv(x.rc, x.rc + x.ri) : 0.0;
+        if (fmode == 3) frac = nclip01(frac);
+      }
+      // saturation over water and over ice, each only where the fraction
+      // gives it a weight: qsl = (1 - frac) qsl_w + frac qsl_i is qsl_w
+      // exactly where frac is 0 and qsl_i where it is 1 (the other term is
+      // 0 times a finite value); a NaN fraction keeps both
+      pv = piv = 0.0;
+      if (fm::bits_(frac) != fm::bits_(1.0)) pv = nmin(fm::fexp(c.ALPW - c.BETAW * it - c.GAMW * lt), 0.99 * x.pabs);
+      if (!zerod_(frac)) piv = nmin(fm::fexp(c.ALPI - c.BETAI * it - c.GAMI * lt), 0.99 * x.pabs);
     } else {
       // condensation.F90:375-395: ICECLOUD, then the tabulated saturation
       // pressures; no ice fraction (:412, ZFRAC = 0)
@@ -184,8 +199,9 @@ ICE3_HD void ia_point(const Cst &c, const IaDerived &d, double dt, double inv_dt
       piv = nmin(esi, 0.99 * x.pabs);
       frac = 0.0;
     }
-    double qsl = fm::fdiv(d.rdrv * pv, x.pabs - pv);
-    const double qsi = fm::fdiv(d.rdrv * piv, x.pabs - piv);
+    // (OCND2: frac = 0 and qsi feeds the ice cloud factor below)
+    double qsl = (OCND2 || fm::bits_(frac) != fm::bits_(1.0)) ? fm::fdiv(d.rdrv * pv, x.pabs - pv) : 0.0;
+    const double qsi = (OCND2 || !zerod_(frac)) ? fm::fdiv(d.rdrv * piv, x.pabs - piv) : 0.0;
     qsl = (1.0 - frac) * qsl + frac * qsi;
     const double lvs = (1.0 - frac) * lv + frac * ls;
     const double ah = lvs * qsl * (it * it * d.irv) * (1.0 + qsl * d.rvrd);

@@ -216,7 +216,7 @@ ICE3_HD bool zerod(double x) { return (opaque_bits(x) << 1) == 0; }
 // RRHONG or RIMLTC change in between): log T, 1/T, es_w and es_i.
 struct TTerms {
   double t, lt, it, esw, esi;
-  bool set;
+  bool set, esw_set;   // esw only where the nucleation needed it
 };
 
 // ICE4_NUCLEATION (micro/ice4_nucleation.func.h:69-144, LOCND2 = .FALSE.);
@@ -227,11 +227,17 @@ ICE3_HD void nucleation(const Cst &c, const Derived &d, double tht, double pabst
   rvheni = 0.0;
   if (!(ltp(t, c.TT) && gtp(rvt, c.V_RTMIN))) return;
   const double lt = fm::flog(t), it = fm::frcp(t);
-  double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   double zzw = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
-  if (tt) { tt->t = t; tt->lt = lt; tt->it = it; tt->esw = zusw; tt->esi = zzw; tt->set = true; }
+  if (tt) { tt->t = t; tt->lt = lt; tt->it = it; tt->esi = zzw; tt->set = true; tt->esw_set = false; }
   zzw = dmin(pabst * 0.5, zzw);
   double zssi = fm::fdiv(rvt * (pabst - zzw), c.EPSILO * zzw) - 1.0;
+  // Not supersaturated over ice: the MIN with the water term below is not
+  // positive either, no crystal nucleates, and with cit >= 0 the rest leaves
+  // rvheni = 0 and cit as they are (zzw = MIN(-cit, 5e4) <= 0): es_w is not
+  // needed.  (A negative cit goes the full way: it is reset to 0 there.)
+  if (!pos(zssi) && !negd(cit)) return;
+  double zusw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
+  if (tt) { tt->esw = zusw; tt->esw_set = true; }
   zusw = dmin(pabst * 0.5, zusw);
   zusw = fm::fdiv(zusw * (pabst - zzw), zzw * (pabst - zusw)) - 1.0;
   zssi = dmin(zssi, zusw);
@@ -513,13 +519,18 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   // from the TIWMX tables, :304-309); es_i of the freezing heat terms stays
   // the formula, OCND2 takes the table for ssi, ai and ICE4_FAST_RI_RS only.
   // The nucleation of the same pass has formed them already if T is unchanged.
-  double lt, it, esi_f, esw;
+  // es_w serves the melting heat term (T > TT) and the evaporation of rain
+  // without cloud only; it is not formed for the other points
+  const bool need_esw = gtp(t, c.TT) || (gtp(v[IRR], c.R_RTMIN) && !gtp(v[IRC], c.C_RTMIN));
+  double lt, it, esi_f, esw = 0.0;
   if (tt && tt->set && fm::bits_(tt->t) == fm::bits_(t)) {
-    lt = tt->lt; it = tt->it; esi_f = tt->esi; esw = tt->esw;
+    lt = tt->lt; it = tt->it; esi_f = tt->esi;
+    if (tt->esw_set) esw = tt->esw;
+    else if (need_esw) esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   } else {
     lt = fm::flog(t); it = fm::frcp(t);
     esi_f = esat_from(c.ALPI, c.BETAI, c.GAMI, it, lt);
-    esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
+    if (need_esw) esw = esat_from(c.ALPW, c.BETAW, c.GAMW, it, lt);
   }
   const double esi = O ? tiwmx_at(op->tw + TW_ESI * kTiwmxN, t) : esi_f;
   R.ssi = fm::fdiv(v[IRV] * (pf.pres - esi), c.EPSILO * esi) - 1.0;
@@ -1230,7 +1241,7 @@ ICE3_HD void tendencies(const Cst &c, const Derived &d, const double *__restrict
   for (int k = 0; k < NVT; ++k) { v[k] = vart[k]; B[k] = 0.0; }
   double *b = R.bu;
   TTerms tt;
-  tt.set = false;
+  tt.set = tt.esw_set = false;
   if (!soft) {
     hard_adjust<O>(c, d, pf, lvfact, lsfact, cit, t, v, b, B, op, &tt);
   } else {

@@ -534,12 +534,26 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
   }
   const double esi = O ? tiwmx_at(op->tw + TW_ESI * kTiwmxN, t) : esi_f;
   R.ssi = fm::fdiv(v[IRV] * (pf.pres - esi), c.EPSILO * esi) - 1.0;
-  const double ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
-  const double dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
-  const double ika = fm::frcp(ka), idv = fm::frcp(dv);
-  const double ai = O ? tiwmx_at(op->tw + TW_A2 * kTiwmxN, t) + tiwmx_at(op->tw + TW_BB3 * kTiwmxN, t) * pf.pres
-                      : sq(c.LSTT + d.cpv_ci * (t - c.TT)) * (ika * d.irv * it * it) +
-                            (c.RV * t) * fm::fdiv(idv, esi);
+  const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
+  const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
+  const bool has_h = H && gtp(v[IRH], c.H_RTMIN);
+  const bool warm = gtp(t, c.TT);
+  // The diffusion / conduction terms (ka, dv, ai), the ventilation
+  // coefficient cj and ssi / (rho ai) serve the processes of snow, graupel
+  // and hail (deposition, heat terms), the evaporation of rain, the
+  // Bergeron process and the OCND2 ice processes only; points with none of
+  // them (cloud and / or ice alone) do not form them.
+  const bool need_dep = O || SUBG || has_s || has_g || has_h || (d.lwarm && has_r && !has_c) ||
+                        (pos(R.ssi) && has_c && has_i && gtp(cit, 1.e-20));
+  double ka = 0.0, dv = 0.0, ika = 0.0, idv = 0.0, ai = 0.0;
+  if (need_dep) {
+    ka = 2.38e-2 + 7.1e-5 * (t - c.TT);
+    dv = 2.11e-5 * fm::fexp(1.94 * (lt - d.lTT)) * fm::fdiv(c.P00, pf.pres);
+    ika = fm::frcp(ka);
+    idv = fm::frcp(dv);
+    ai = O ? tiwmx_at(op->tw + TW_A2 * kTiwmxN, t) + tiwmx_at(op->tw + TW_BB3 * kTiwmxN, t) * pf.pres
+           : sq(c.LSTT + d.cpv_ci * (t - c.TT)) * (ika * d.irv * it * it) + (c.RV * t) * fm::fdiv(idv, esi);
+  }
   double colf = 1.0, acrf = 1.0;
   if (O) {
     // collision factors from the mean droplet radius (:322-346, LLCOL)
@@ -559,15 +573,14 @@ ICE3_HD void hard_rates(const Cst &c, const Derived &d, const double *__restrict
     orr->colf = colf;
     orr->acrf = acrf;
   }
-  const double cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) * fm::frsqrt(1.718e-5 + 4.9e-8 * (t - c.TT));
-  const double ssi_rai = fm::fdiv(R.ssi, rho * ai);
+  double cj = 0.0, ssi_rai = 0.0;
+  if (need_dep) {
+    cj = c.SCFAC * fm::fexp(0.3 * pf.lrho) * fm::frsqrt(1.718e-5 + 4.9e-8 * (t - c.TT));
+    ssi_rai = fm::fdiv(R.ssi, rho * ai);
+  }
   Slopes s;
   slopes(c, d, pf.lrho, t, v, s);
   if (H) slope_h(c, pf.lrho, v[IRH], s);
-  const bool has_v = gtp(v[IRV], c.V_RTMIN), has_c = gtp(v[IRC], c.C_RTMIN), has_r = gtp(v[IRR], c.R_RTMIN);
-  const bool has_i = gtp(v[IRI], c.I_RTMIN), has_s = gtp(v[IRS], c.S_RTMIN), has_g = gtp(v[IRG], c.G_RTMIN);
-  const bool has_h = H && gtp(v[IRH], c.H_RTMIN);
-  const bool warm = gtp(t, c.TT);
   // ventilation factors shared by deposition, freezing and melting
   const double vent_s = has_s ? c.O0DEPS * (d.ex0deps_zero ? 1.0 : fm::fexp(c.EX0DEPS * s.llbdas)) +
                                     c.O1DEPS * cj * fm::fexp(c.EX1DEPS * s.llbdas)
